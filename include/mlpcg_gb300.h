@@ -1,0 +1,249 @@
+/*
+ * mlpcg_gb300.h -- C ABI of the GB300 (sm_103a) neural-preconditioned CG library.
+ *
+ * Every entry point takes plain device pointers, sizes and a CUDA stream
+ * (passed as void*, i.e. a cudaStream_t; NULL = legacy default stream), launches
+ * asynchronously on that stream and returns an int status (0 = ok, negative =
+ * argument error, see MLPCG_ERR_*).  A failing call leaves a message readable
+ * through mlpcg_last_error() (thread-local).  No entry point allocates device
+ * memory: where scratch space is needed the caller passes a workspace whose
+ * size is given by the matching *_workspace() query.  Nothing is retained
+ * between calls except the opaque solver objects created by
+ * mlpcg_solver_create(), which hold host-side state only.
+ *
+ * Grid layout: a field on an N1 x N2 x N3 grid is stored contiguously with
+ * N3 fastest (index (i*N2 + j)*N3 + k), batches of B fields back to back.
+ * That is the layout of the reference's (B, 1, N1, N2, N3) tensors.
+ * "padded" inputs are (N1+2) x (N2+2) x (N3+2) arrays whose outer layer is
+ * read as the halo, exactly like the F.pad'ed tensors the reference's
+ * extension modules receive (sm_model_3d.py:24-26).
+ *
+ * Reference file citations are paths inside kai-lan/MLPCG.
+ */
+#ifndef MLPCG_GB300_H
+#define MLPCG_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes --------------------------------------------------------- */
+#define MLPCG_OK               0
+#define MLPCG_ERR_ARG         -1  /* null pointer, bad enum, negative size   */
+#define MLPCG_ERR_SHAPE       -2  /* sizes the operation does not support    */
+#define MLPCG_ERR_ALIGN       -3  /* pointer / stride alignment violated     */
+#define MLPCG_ERR_WORKSPACE   -4  /* workspace too small                     */
+#define MLPCG_ERR_CUDA        -5  /* a CUDA runtime call failed              */
+#define MLPCG_ERR_UNSUPPORTED -6  /* dtype / mode combination not provided   */
+
+/* ---- element types -------------------------------------------------------- */
+#define MLPCG_F32  0
+#define MLPCG_BF16 1
+#define MLPCG_F64  2
+
+/* ---- cell flags (lib/read_data.py:13-16) ---------------------------------- */
+#define MLPCG_BOUNDARY 0
+#define MLPCG_SOLID    1
+#define MLPCG_FLUID    2
+#define MLPCG_AIR      3
+
+/* Message of the last failing call on this host thread ("" if none). */
+const char *mlpcg_last_error(void);
+/* ABI version of the loaded library. */
+int mlpcg_abi_version(void);
+
+/* =========================================================================
+ * Stencil-coefficient generation and application (the two halves of the
+ * reference's sm_block_3d / sm_block_trans_3d kernels).
+ * ========================================================================= */
+
+/*
+ * K_p(q) = bias[p] + sum_{s<3, m,n,o<3} weight[p][s][m][n][o] * img(s, q+(m-1,n-1,o-1))
+ * for the 27 taps p of every cell q (img zero outside the grid, or read from
+ * the halo when image_padded).  Writes 27 planes K[p*plane_stride + cell].
+ * Replaces the per-thread coefficient loop of sm_block_3d_cuda_inference_kernel
+ * (torch_extension/sm_block_3d_kernel.cu:45-65), which the reference re-runs
+ * on every call; here it runs once per (image, weights).
+ * k_dtype: MLPCG_F32 or MLPCG_BF16.  plane_stride >= N1*N2*N3, multiple of 8.
+ */
+int mlpcg_stencil_gen(const float *image, int image_padded, int N1, int N2, int N3,
+                      const float *weight, const float *bias,
+                      void *K, int k_dtype, int64_t plane_stride, void *stream);
+
+/*
+ * transpose = 0:  y(q) = sum_p K_p(q) * x(q + off_p)           (sm_block_3d_kernel.cu:66-70)
+ * transpose = 1:  y(q) = sum_p K_p(q - off_p) * x(q - off_p)   (sm_block_trans_3d_kernel.cu:45-73)
+ * with off_p = (p/9-1, (p/3)%3-1, p%3-1) and x zero outside the grid (or read
+ * from the halo when x_padded).  x, y hold B fields.
+ * K: F32|BF16; x: F32|BF16; y: F32|BF16.
+ */
+int mlpcg_stencil_apply(const void *K, int k_dtype, int64_t plane_stride,
+                        const void *x, int x_dtype, int x_padded,
+                        void *y, int y_dtype,
+                        int B, int N1, int N2, int N3, int transpose, void *stream);
+
+/*
+ * Gradient of a stencil application with respect to its coefficients, summed
+ * over the batch:
+ *   transpose = 0:  dK_p(q)  = sum_b g_b(q) * x_b(q + off_p)
+ *   transpose = 1:  dK_p(q)  = sum_b g_b(q + off_p) * x_b(q)
+ * (the cell-level factors of sm_block_3d_cuda_dwdb_fast_kernel,
+ *  sm_block_3d_kernel.cu:122-229, and its transpose, sm_block_trans_3d_kernel.cu:173-289).
+ * dK is F32 with 27 planes of plane_stride.
+ */
+int mlpcg_stencil_coeff_grad(const float *g, const float *x, int x_padded, float *dK,
+                             int64_t plane_stride, int B, int N1, int N2, int N3,
+                             int transpose, void *stream);
+
+/*
+ * grad_weight[p][s][m][n][o] = sum_q dK_p(q) * img(s, q+(m-1,n-1,o-1)),
+ * grad_bias[p] = sum_q dK_p(q).  Deterministic two-pass reduction (no atomics).
+ * Overwrites grad_weight (27*81 floats) and grad_bias (27 floats).
+ * Workspace: mlpcg_stencil_wgrad_workspace(N1,N2,N3) bytes.
+ */
+size_t mlpcg_stencil_wgrad_workspace(int N1, int N2, int N3);
+int mlpcg_stencil_wgrad(const float *dK, int64_t plane_stride,
+                        const float *image, int image_padded, int N1, int N2, int N3,
+                        float *grad_weight, float *grad_bias,
+                        void *workspace, size_t workspace_bytes, void *stream);
+
+/*
+ * Gradient with respect to the image channels:
+ *   grad_image(s, c) = sum_{p, m,n,o} weight[p][s][m][n][o] * dK_p(c - (m-1,n-1,o-1)).
+ * (The reference returns no image gradient; this is the adjoint of
+ * mlpcg_stencil_gen restricted to its image argument.)  Overwrites grad_image
+ * (3 x N1 x N2 x N3, F32, unpadded).
+ */
+int mlpcg_stencil_image_grad(const float *dK, int64_t plane_stride,
+                             const float *weight, float *grad_image,
+                             int N1, int N2, int N3, void *stream);
+
+/* =========================================================================
+ * Reference extension ops (smblock3d / smblocktrans3d / smlinear3d)
+ * ========================================================================= */
+
+/* Workspace of mlpcg_sm_block_3d_forward/backward: one K buffer (+ reduction space). */
+size_t mlpcg_sm_block_3d_workspace(int N1, int N2, int N3);
+
+/*
+ * smblock3d.inference/forward (transpose = 0) and smblocktrans3d.inference/forward
+ * (transpose = 1): torch_extension/sm_block_3d.cpp:31-55,
+ * sm_block_3d_kernel.cu:329-418, sm_block_trans_3d_kernel.cu:381-470.
+ * image: 3 x N1 x N2 x N3 (or padded), x: B x N1 x N2 x N3 (or padded),
+ * weight: 27 x 3 x 3 x 3 x 3, bias: 27, y: B x N1 x N2 x N3.  All F32.
+ * Unlike the reference, any B and any N >= 1 are accepted (the reference's
+ * forward asserts N3 % 2 == 0, sm_block_3d_kernel.cu:399).
+ */
+int mlpcg_sm_block_3d_forward(const float *image, int image_padded,
+                              const float *x, int x_padded,
+                              const float *weight, const float *bias, float *y,
+                              int B, int N1, int N2, int N3, int transpose,
+                              void *workspace, size_t workspace_bytes, void *stream);
+
+/*
+ * smblock3d.backward / smblocktrans3d.backward: sm_block_3d.cpp:57-69,
+ * sm_block_3d_kernel.cu:420-484, sm_block_trans_3d_kernel.cu:472-535.
+ * Returns grad_x (B x N), grad_weight (27 x 81), grad_bias (27), F32, for any B
+ * (the reference's dx kernels are only correct for B = 128,
+ * sm_block_3d_kernel.cu:18-20).  grad_image may be NULL; when given it
+ * receives d/d image (3 x N, unpadded), which the reference does not provide.
+ */
+int mlpcg_sm_block_3d_backward(const float *grad_out,
+                               const float *image, int image_padded,
+                               const float *x, int x_padded,
+                               const float *weight, const float *bias,
+                               float *grad_x, float *grad_weight, float *grad_bias,
+                               float *grad_image,
+                               int B, int N1, int N2, int N3, int transpose,
+                               void *workspace, size_t workspace_bytes, void *stream);
+
+/*
+ * smlinear3d.inference/forward: sm_linear_3d.cpp:25-47, sm_linear_3d_kernel.cu:152-227.
+ *   y[s][k][l][o] = (1/(N1 N2 N3)) sum_q img(s, q + (k-1,l-1,o-1))   (81 values, img zero outside)
+ *   z[j]          = sum_i weight[j][i] * y[i] + bias[j]             for j < nlin
+ * image: 3 x N1 x N2 x N3 unpadded, weight: nlin x 81, bias: nlin, z: nlin, y: 81, F32.
+ * nlin > 1 evaluates several linear blocks on one image in one pass (the
+ * reference's c0/c1 blocks of one level share the image).
+ * Workspace: mlpcg_sm_linear_3d_workspace(N1,N2,N3) bytes.
+ */
+size_t mlpcg_sm_linear_3d_workspace(int N1, int N2, int N3);
+int mlpcg_sm_linear_3d_forward(const float *image, int N1, int N2, int N3,
+                               const float *weight, const float *bias, int nlin,
+                               float *z, float *y,
+                               void *workspace, size_t workspace_bytes, void *stream);
+
+/*
+ * smlinear3d.backward: sm_linear_3d_kernel.cu:229-238.
+ *   grad_weight[i] = y[i] * grad_out[0]   (81 values), grad_bias[0] = grad_out[0].
+ */
+int mlpcg_sm_linear_3d_backward(const float *grad_out, const float *y,
+                                float *grad_weight, float *grad_bias, void *stream);
+
+/*
+ * Gradient of z = w.y(img) + b with respect to the image:
+ *   grad_image(s, c) = grad_out * (1/N) * sum_{k,l,o : c-(k-1,l-1,o-1) in grid} w[s][k][l][o].
+ * (Not provided by the reference.)  Overwrites grad_image (3 x N, F32).
+ */
+int mlpcg_sm_linear_3d_image_grad(const float *grad_out, const float *weight,
+                                  float *grad_image, int N1, int N2, int N3, void *stream);
+
+/* =========================================================================
+ * Grid transfer between levels (ATen ops the reference calls,
+ * sm_model_3d.py:206-230, 269-278)
+ * ========================================================================= */
+
+/* F.avg_pool3d(x, 2): N1,N2,N3 are the fine sizes (even); y is B x N/2. */
+int mlpcg_avg_pool2(const void *x, void *y, int dtype, int B, int N1, int N2, int N3,
+                    void *stream);
+/* Adjoint of avg_pool2: x(fine) = y(coarse cell containing it) / 8. */
+int mlpcg_avg_pool2_adjoint(const void *y, void *x, int dtype, int B, int N1, int N2, int N3,
+                            void *stream);
+/* F.interpolate(x, scale_factor=2, mode='trilinear', align_corners=False):
+ * n1,n2,n3 are the coarse sizes; y is B x 2n. */
+int mlpcg_upsample2(const void *x, void *y, int dtype, int B, int n1, int n2, int n3,
+                    void *stream);
+/* Adjoint of mlpcg_upsample2 (gradient of the interpolation w.r.t. its input). */
+int mlpcg_upsample2_adjoint(const void *y, void *x, int dtype, int B, int n1, int n2, int n3,
+                            void *stream);
+/* out = c0[0]*x + c1[0]*y with c0, c1 device scalars (sm_model_3d.py:258,286). */
+int mlpcg_axpby(const float *c0, const void *x, const float *c1, const void *y, void *out,
+                int dtype, int64_t n, void *stream);
+
+/* =========================================================================
+ * Matrix-free 7-point Poisson operator with mixed boundaries.
+ * The reference assembles it as an FP64 CSR (lib/discrete_laplacian.py:122-160,
+ * lib/read_data.py:110-165) and multiplies with torch.sparse (cg_tests.py:53,80,83).
+ *   (A x)(c) = d(c) x(c) - sum_{fluid face neighbours n} x(n)  for FLUID c, else 0,
+ *   d(c)     = number of non-solid (FLUID or AIR) face neighbours.
+ * Cells outside the grid count as solid.
+ * ========================================================================= */
+int mlpcg_laplacian_apply(const uint8_t *flags, const void *x, void *y, int dtype,
+                          int N1, int N2, int N3, void *stream);
+
+/* =========================================================================
+ * Reductions
+ * ========================================================================= */
+
+/* out[0] (FP64, device) = sum_i x[i] * y[i], deterministic (fixed-order
+ * FP64 block partials).  dtype F32|BF16|F64.  Replaces the torch dot / norm
+ * calls of cg_tests.py:32,55-56,228,245.  Workspace: mlpcg_dot_workspace(n). */
+size_t mlpcg_dot_workspace(int64_t n);
+int mlpcg_dot(const void *x, const void *y, int dtype, int64_t n, double *out,
+              void *workspace, size_t workspace_bytes, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+
+#endif /* MLPCG_GB300_H */

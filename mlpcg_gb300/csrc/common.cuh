@@ -1,0 +1,97 @@
+// Shared helpers of the sm_103a kernels: element loads/stores, tap offsets,
+// error reporting, launch checks.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string>
+
+#include "../../include/mlpcg_gb300.h"
+
+namespace mlpcg {
+
+// ---------------------------------------------------------------------------
+// error reporting (thread-local last-error string, see mlpcg_last_error)
+// ---------------------------------------------------------------------------
+void set_error(const char *fmt, ...);
+void clear_error();
+
+#define MLPCG_REQUIRE(cond, code, ...)        \
+  do {                                        \
+    if (!(cond)) {                            \
+      ::mlpcg::set_error(__VA_ARGS__);        \
+      return (code);                          \
+    }                                         \
+  } while (0)
+
+#define MLPCG_CUDA_CHECK(expr)                                                  \
+  do {                                                                          \
+    cudaError_t _e = (expr);                                                    \
+    if (_e != cudaSuccess) {                                                    \
+      ::mlpcg::set_error("%s failed: %s (%s:%d)", #expr, cudaGetErrorString(_e), \
+                         __FILE__, __LINE__);                                   \
+      return MLPCG_ERR_CUDA;                                                    \
+    }                                                                           \
+  } while (0)
+
+// Checks the launch that was just issued (configuration errors only; the
+// kernel itself runs asynchronously).
+#define MLPCG_LAUNCH_CHECK() MLPCG_CUDA_CHECK(cudaGetLastError())
+
+inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+inline bool valid_dtype(int dt) { return dt == MLPCG_F32 || dt == MLPCG_BF16 || dt == MLPCG_F64; }
+inline size_t dtype_size(int dt) { return dt == MLPCG_F64 ? 8 : (dt == MLPCG_BF16 ? 2 : 4); }
+
+__host__ __device__ inline int64_t cells(int n1, int n2, int n3) { return (int64_t)n1 * n2 * n3; }
+inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
+
+// ---------------------------------------------------------------------------
+// element access in float (fp32 compute for fp32 / bf16 storage)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float ldf(const float *p) { return __ldg(p); }
+__device__ __forceinline__ float ldf(const __nv_bfloat16 *p) { return __bfloat162float(*p); }
+__device__ __forceinline__ float ldf(const double *p) { return (float)__ldg(p); }
+__device__ __forceinline__ void stf(float *p, float v) { *p = v; }
+__device__ __forceinline__ void stf(__nv_bfloat16 *p, float v) { *p = __float2bfloat16_rn(v); }
+__device__ __forceinline__ void stf(double *p, float v) { *p = (double)v; }
+
+// Tap p = 9k + 3l + o  <->  offset (k-1, l-1, o-1): the index order of the
+// reference's 27 coefficient channels (sm_block_3d_kernel.cu:45-52).
+__host__ __device__ __forceinline__ int tap_dx(int p) { return p / 9 - 1; }
+__host__ __device__ __forceinline__ int tap_dy(int p) { return (p / 3) % 3 - 1; }
+__host__ __device__ __forceinline__ int tap_dz(int p) { return p % 3 - 1; }
+
+// Geometry of a field, either unpadded (halo reads outside [0,N) give 0) or
+// padded (halo is the outer layer of an (N+2)^3 array).
+struct FieldGeom {
+  int n1, n2, n3;     // interior sizes
+  int padded;         // 0 or 1
+  int64_t sy, sx;     // strides of j and i in elements
+  int64_t origin;     // element offset of interior cell (0,0,0)
+  int64_t bstride;    // elements between batch items
+  __host__ __device__ static FieldGeom make(int n1, int n2, int n3, int padded) {
+    FieldGeom g;
+    g.n1 = n1; g.n2 = n2; g.n3 = n3; g.padded = padded;
+    int p3 = n3 + 2 * padded, p2 = n2 + 2 * padded, p1 = n1 + 2 * padded;
+    g.sy = p3;
+    g.sx = (int64_t)p2 * p3;
+    g.origin = padded ? (g.sx + g.sy + 1) : 0;
+    g.bstride = (int64_t)p1 * p2 * p3;
+    return g;
+  }
+  // value at interior coordinates (i,j,k), each in [-1, n]; 0 outside the
+  // interior of an unpadded field.
+  template <typename T>
+  __device__ __forceinline__ float at(const T *base, int i, int j, int k) const {
+    if (!padded) {
+      if ((unsigned)i >= (unsigned)n1 || (unsigned)j >= (unsigned)n2 || (unsigned)k >= (unsigned)n3)
+        return 0.f;
+    }
+    return ldf(base + origin + i * sx + j * sy + k);
+  }
+};
+
+}  // namespace mlpcg

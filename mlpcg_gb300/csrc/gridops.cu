@@ -1,0 +1,408 @@
+// Level transfer (restriction / prolongation / combine), the per-level linear
+// coefficients (sm_linear_3d) and the matrix-free mixed-boundary Laplacian.
+#include "common.cuh"
+
+namespace mlpcg {
+
+// ---------------------------------------------------------------------------
+// avg_pool3d(x, 2) and its adjoint.  Sum in (a, b, c) loop order, then / 8.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_avg_pool2(const T *__restrict__ x, T *__restrict__ y, int n1, int n2, int n3) {
+  const int c1 = n1 / 2, c2 = n2 / 2, c3 = n3 / 2;
+  const int64_t nc = cells(c1, c2, c3);
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nc) return;
+  const int b = blockIdx.y;
+  const int k = (int)(q % c3);
+  const int64_t t = q / c3;
+  const int j = (int)(t % c2);
+  const int i = (int)(t / c2);
+  const T *xb = x + (int64_t)b * cells(n1, n2, n3);
+  float s = 0.f;
+#pragma unroll
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int bb = 0; bb < 2; ++bb)
+#pragma unroll
+      for (int c = 0; c < 2; ++c)
+        s += ldf(xb + ((int64_t)(2 * i + a) * n2 + (2 * j + bb)) * n3 + (2 * k + c));
+  stf(y + (int64_t)b * nc + q, s / 8.f);
+}
+
+template <typename T>
+__global__ void k_avg_pool2_adjoint(const T *__restrict__ y, T *__restrict__ x, int n1, int n2, int n3) {
+  const int64_t n = cells(n1, n2, n3);
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int b = blockIdx.y;
+  const int k = (int)(q % n3);
+  const int64_t t = q / n3;
+  const int j = (int)(t % n2);
+  const int i = (int)(t / n2);
+  const int c2 = n2 / 2, c3 = n3 / 2;
+  const int64_t nc = cells(n1 / 2, c2, c3);
+  const float v = ldf(y + (int64_t)b * nc + ((int64_t)(i / 2) * c2 + j / 2) * c3 + k / 2);
+  stf(x + (int64_t)b * n + q, v / 8.f);
+}
+
+// ---------------------------------------------------------------------------
+// Trilinear x2 interpolation, align_corners=False (the semantics of
+// F.interpolate(scale_factor=2, mode='trilinear')): per axis the source
+// coordinate is max(0, 0.5*(f+0.5)-0.5), i0 = floor, i1 = min(i0+1, n-1),
+// weights (1-l, l).
+// ---------------------------------------------------------------------------
+struct Lin1 {
+  int i0, i1;
+  float l0, l1;
+};
+__device__ __forceinline__ Lin1 lin1(int f, int n) {
+  float src = 0.5f * ((float)f + 0.5f) - 0.5f;
+  if (src < 0.f) src = 0.f;
+  Lin1 r;
+  r.i0 = (int)src;
+  r.i1 = r.i0 + (r.i0 < n - 1 ? 1 : 0);
+  r.l1 = src - (float)r.i0;
+  r.l0 = 1.f - r.l1;
+  return r;
+}
+
+template <typename T>
+__global__ void k_upsample2(const T *__restrict__ x, T *__restrict__ y, int n1, int n2, int n3) {
+  const int f1 = 2 * n1, f2 = 2 * n2, f3 = 2 * n3;
+  const int64_t nf = cells(f1, f2, f3);
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nf) return;
+  const int b = blockIdx.y;
+  const int k = (int)(q % f3);
+  const int64_t t = q / f3;
+  const int j = (int)(t % f2);
+  const int i = (int)(t / f2);
+  const Lin1 a = lin1(i, n1), bb = lin1(j, n2), c = lin1(k, n3);
+  const T *xb = x + (int64_t)b * cells(n1, n2, n3);
+  auto X = [&](int ii, int jj, int kk) { return ldf(xb + ((int64_t)ii * n2 + jj) * n3 + kk); };
+  const float v =
+      a.l0 * (bb.l0 * (c.l0 * X(a.i0, bb.i0, c.i0) + c.l1 * X(a.i0, bb.i0, c.i1)) +
+              bb.l1 * (c.l0 * X(a.i0, bb.i1, c.i0) + c.l1 * X(a.i0, bb.i1, c.i1))) +
+      a.l1 * (bb.l0 * (c.l0 * X(a.i1, bb.i0, c.i0) + c.l1 * X(a.i1, bb.i0, c.i1)) +
+              bb.l1 * (c.l0 * X(a.i1, bb.i1, c.i0) + c.l1 * X(a.i1, bb.i1, c.i1)));
+  stf(y + (int64_t)b * nf + q, v);
+}
+
+// Adjoint: each coarse cell gathers the weighted fine values that read it.
+// Along one axis, coarse index c is read by fine f in {2c-1, 2c, 2c+1, 2c+2}
+// (clamped at the ends); gathering keeps the kernel deterministic.
+template <typename T>
+__global__ void k_upsample2_adjoint(const T *__restrict__ y, T *__restrict__ x, int n1, int n2, int n3) {
+  const int f1 = 2 * n1, f2 = 2 * n2, f3 = 2 * n3;
+  const int64_t nc = cells(n1, n2, n3);
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nc) return;
+  const int b = blockIdx.y;
+  const int k = (int)(q % n3);
+  const int64_t t = q / n3;
+  const int j = (int)(t % n2);
+  const int i = (int)(t / n2);
+  const T *yb = y + (int64_t)b * cells(f1, f2, f3);
+  // weights of coarse index c in fine index f along an axis of coarse size n
+  auto wt = [](int f, int c, int n) -> float {
+    const Lin1 l = lin1(f, n);
+    float w = 0.f;
+    if (l.i0 == c) w += l.l0;
+    if (l.i1 == c) w += l.l1;
+    return w;
+  };
+  float acc = 0.f;
+  for (int fi = 2 * i - 1; fi <= 2 * i + 2; ++fi) {
+    if (fi < 0 || fi >= f1) continue;
+    const float wi = wt(fi, i, n1);
+    if (wi == 0.f) continue;
+    for (int fj = 2 * j - 1; fj <= 2 * j + 2; ++fj) {
+      if (fj < 0 || fj >= f2) continue;
+      const float wj = wt(fj, j, n2);
+      if (wj == 0.f) continue;
+      for (int fk = 2 * k - 1; fk <= 2 * k + 2; ++fk) {
+        if (fk < 0 || fk >= f3) continue;
+        const float wk = wt(fk, k, n3);
+        if (wk == 0.f) continue;
+        acc += wi * wj * wk * ldf(yb + ((int64_t)fi * f2 + fj) * f3 + fk);
+      }
+    }
+  }
+  stf(x + (int64_t)b * nc + q, acc);
+}
+
+// out = c0*x + c1*y, the two products rounded separately like torch's
+// c0 * x + c1 * y.
+template <typename T>
+__global__ void k_axpby(const float *__restrict__ c0, const T *__restrict__ x,
+                        const float *__restrict__ c1, const T *__restrict__ y, T *__restrict__ out,
+                        int64_t n) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const float a = __fmul_rn(c0[0], ldf(x + q));
+  const float b = __fmul_rn(c1[0], ldf(y + q));
+  stf(out + q, __fadd_rn(a, b));
+}
+
+// ---------------------------------------------------------------------------
+// sm_linear_3d: the 81 shifted means of the 3 image channels.
+// Every cell belongs to one of 27 boundary classes (per axis: first plane,
+// interior, last plane).  Each shifted sum is a sum of class sums, so one
+// pass computes 27 x 3 class sums and the 81 shifted sums follow by
+// inclusion (deterministic: per-block FP64 partials summed in fixed order).
+// ---------------------------------------------------------------------------
+constexpr int kLinBlocks = 128;
+constexpr int kLinThreads = 256;
+
+struct Range1 { int lo, hi; };  // [lo, hi)
+__device__ __forceinline__ Range1 class_range(int cls, int n) {
+  Range1 r;
+  if (n == 1) { r.lo = (cls == 0) ? 0 : 1; r.hi = (cls == 0) ? 1 : 1; return r; }
+  if (cls == 0) { r.lo = 0; r.hi = 1; }
+  else if (cls == 1) { r.lo = 1; r.hi = n - 1; }
+  else { r.lo = n - 1; r.hi = n; }
+  return r;
+}
+
+__global__ void __launch_bounds__(kLinThreads)
+k_class_sums(const float *__restrict__ img, int n1, int n2, int n3, double *__restrict__ partial) {
+  // blockIdx.y = class (cx*9 + cy*3 + cz)
+  const int cls = blockIdx.y;
+  const Range1 rx = class_range(cls / 9, n1), ry = class_range((cls / 3) % 3, n2),
+               rz = class_range(cls % 3, n3);
+  const int64_t ex = rx.hi > rx.lo ? rx.hi - rx.lo : 0;
+  const int64_t ey = ry.hi > ry.lo ? ry.hi - ry.lo : 0;
+  const int64_t ez = rz.hi > rz.lo ? rz.hi - rz.lo : 0;
+  const int64_t cnt = ex * ey * ez;
+  const int64_t n = cells(n1, n2, n3);
+  float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < cnt;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int k = rz.lo + (int)(e % ez);
+    const int64_t t = e / ez;
+    const int j = ry.lo + (int)(t % ey);
+    const int i = rx.lo + (int)(t / ey);
+    const int64_t q = ((int64_t)i * n2 + j) * n3 + k;
+    s0 += img[q];
+    s1 += img[n + q];
+    s2 += img[2 * n + q];
+  }
+  __shared__ double red[3][kLinThreads / 32];
+  double d0 = s0, d1 = s1, d2 = s2;
+  for (int o = 16; o > 0; o >>= 1) {
+    d0 += __shfl_xor_sync(0xffffffffu, d0, o);
+    d1 += __shfl_xor_sync(0xffffffffu, d1, o);
+    d2 += __shfl_xor_sync(0xffffffffu, d2, o);
+  }
+  const int w = threadIdx.x / 32, l = threadIdx.x % 32;
+  if (l == 0) { red[0][w] = d0; red[1][w] = d1; red[2][w] = d2; }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    double s = 0.0;
+    for (int ww = 0; ww < kLinThreads / 32; ++ww) s += red[threadIdx.x][ww];
+    partial[((int64_t)cls * 3 + threadIdx.x) * gridDim.x + blockIdx.x] = s;
+  }
+}
+
+// One block of 128 threads: class sums -> 81 shifted means y -> nlin outputs z.
+__global__ void k_linear_finalize(const double *__restrict__ partial, int nblk, int n1, int n2, int n3,
+                                  const float *__restrict__ W, const float *__restrict__ bias,
+                                  int nlin, float *__restrict__ z, float *__restrict__ yout) {
+  __shared__ double cs[27 * 3];
+  __shared__ double ym[81];
+  const int t = threadIdx.x;
+  if (t < 81) {
+    double s = 0.0;
+    for (int b = 0; b < nblk; ++b) s += partial[(int64_t)t * nblk + b];
+    cs[t] = s;  // index cls*3 + channel
+  }
+  __syncthreads();
+  // shift index k in {0,1,2} (offset k-1) keeps classes: k=0 -> {0,1}, k=1 -> all, k=2 -> {1,2};
+  // for an axis of size 1 the single plane is class 0 and only k=1 keeps it.
+  auto keep = [](int k, int cls, int n) -> bool {
+    if (n == 1) return k == 1 && cls == 0;
+    if (k == 0) return cls != 2;
+    if (k == 2) return cls != 0;
+    return true;
+  };
+  const double inv_n = 1.0 / (double)cells(n1, n2, n3);
+  if (t < 81) {
+    const int s = t / 27, kk = (t / 9) % 3, ll = (t / 3) % 3, oo = t % 3;
+    double acc = 0.0;
+    for (int cx = 0; cx < 3; ++cx) {
+      if (!keep(kk, cx, n1)) continue;
+      for (int cy = 0; cy < 3; ++cy) {
+        if (!keep(ll, cy, n2)) continue;
+        for (int cz = 0; cz < 3; ++cz) {
+          if (!keep(oo, cz, n3)) continue;
+          acc += cs[(cx * 9 + cy * 3 + cz) * 3 + s];
+        }
+      }
+    }
+    ym[t] = acc * inv_n;
+    if (yout) yout[t] = (float)(acc * inv_n);
+  }
+  __syncthreads();
+  // z_j = w_j . y + b_j   (w . y in float like the reference's dot, then + bias)
+  if (t < nlin) {
+    double acc = 0.0;
+    for (int e = 0; e < 81; ++e) acc += (double)W[t * 81 + e] * ym[e];
+    z[t] = (float)(acc + (double)bias[t]);
+  }
+}
+
+__global__ void k_linear_backward(const float *__restrict__ g, const float *__restrict__ y,
+                                  float *__restrict__ gw, float *__restrict__ gb) {
+  const int t = threadIdx.x;
+  if (t < 81) gw[t] = y[t] * g[0];
+  if (t == 0) gb[0] = g[0];
+}
+
+// d z / d img(s, c) = g/N * sum over shifts d with c - d in grid of w[s][d]
+__global__ void k_linear_image_grad(const float *__restrict__ g, const float *__restrict__ W, int n1,
+                                    int n2, int n3, float *__restrict__ gimg) {
+  const int64_t n = cells(n1, n2, n3);
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int k = (int)(q % n3);
+  const int64_t t = q / n3;
+  const int j = (int)(t % n2);
+  const int i = (int)(t / n2);
+  const float scale = g[0] / (float)n;
+  for (int s = 0; s < 3; ++s) {
+    float acc = 0.f;
+    for (int o = 0; o < 27; ++o) {
+      // y[s][o] sums img(q + d_o) over q in grid: img cell c is counted iff c - d_o in grid
+      const int ii = i - (o / 9 - 1), jj = j - ((o / 3) % 3 - 1), kk = k - (o % 3 - 1);
+      if ((unsigned)ii < (unsigned)n1 && (unsigned)jj < (unsigned)n2 && (unsigned)kk < (unsigned)n3)
+        acc += W[s * 27 + o];
+    }
+    gimg[s * n + q] = acc * scale;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Matrix-free mixed-boundary 7-point operator.  Neighbours are visited in
+// the column order of the assembled CSR row (i-1, j-1, k-1, centre, k+1,
+// j+1, i+1).
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_laplacian(const uint8_t *__restrict__ flags, const T *__restrict__ x,
+                            T *__restrict__ y, int n1, int n2, int n3) {
+  const int64_t n = cells(n1, n2, n3);
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  if (flags[q] != MLPCG_FLUID) { y[q] = T(0); return; }
+  const int k = (int)(q % n3);
+  const int64_t t = q / n3;
+  const int j = (int)(t % n2);
+  const int i = (int)(t / n2);
+  const int64_t sx = (int64_t)n2 * n3, sy = n3;
+  T off = T(0);
+  int d = 0;
+  auto visit = [&](bool inside, int64_t nb) {
+    if (!inside) return;
+    const uint8_t f = flags[nb];
+    if (f == MLPCG_FLUID) { off += x[nb]; ++d; }
+    else if (f == MLPCG_AIR) { ++d; }
+  };
+  visit(i > 0, q - sx);
+  visit(j > 0, q - sy);
+  visit(k > 0, q - 1);
+  visit(k < n3 - 1, q + 1);
+  visit(j < n2 - 1, q + sy);
+  visit(i < n1 - 1, q + sx);
+  y[q] = T(d) * x[q] - off;
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+#define MLPCG_DISPATCH_DT(dt, T, ...)                                   \
+  do {                                                                  \
+    if ((dt) == MLPCG_F32) { using T = float; __VA_ARGS__; }            \
+    else if ((dt) == MLPCG_BF16) { using T = __nv_bfloat16; __VA_ARGS__; } \
+    else { using T = double; __VA_ARGS__; }                             \
+  } while (0)
+
+int launch_avg_pool2(const void *x, void *y, int dt, int B, int n1, int n2, int n3, cudaStream_t st) {
+  dim3 grid(blocks_for(cells(n1 / 2, n2 / 2, n3 / 2), 256), B);
+  MLPCG_DISPATCH_DT(dt, T, k_avg_pool2<T><<<grid, 256, 0, st>>>((const T *)x, (T *)y, n1, n2, n3));
+  MLPCG_LAUNCH_CHECK();
+  return MLPCG_OK;
+}
+
+int launch_avg_pool2_adjoint(const void *y, void *x, int dt, int B, int n1, int n2, int n3,
+                             cudaStream_t st) {
+  dim3 grid(blocks_for(cells(n1, n2, n3), 256), B);
+  MLPCG_DISPATCH_DT(dt, T, k_avg_pool2_adjoint<T><<<grid, 256, 0, st>>>((const T *)y, (T *)x, n1, n2, n3));
+  MLPCG_LAUNCH_CHECK();
+  return MLPCG_OK;
+}
+
+int launch_upsample2(const void *x, void *y, int dt, int B, int n1, int n2, int n3, cudaStream_t st) {
+  dim3 grid(blocks_for(cells(2 * n1, 2 * n2, 2 * n3), 256), B);
+  MLPCG_DISPATCH_DT(dt, T, k_upsample2<T><<<grid, 256, 0, st>>>((const T *)x, (T *)y, n1, n2, n3));
+  MLPCG_LAUNCH_CHECK();
+  return MLPCG_OK;
+}
+
+int launch_upsample2_adjoint(const void *y, void *x, int dt, int B, int n1, int n2, int n3,
+                             cudaStream_t st) {
+  dim3 grid(blocks_for(cells(n1, n2, n3), 256), B);
+  MLPCG_DISPATCH_DT(dt, T, k_upsample2_adjoint<T><<<grid, 256, 0, st>>>((const T *)y, (T *)x, n1, n2, n3));
+  MLPCG_LAUNCH_CHECK();
+  return MLPCG_OK;
+}
+
+int launch_axpby(const float *c0, const void *x, const float *c1, const void *y, void *out, int dt,
+                 int64_t n, cudaStream_t st) {
+  MLPCG_DISPATCH_DT(dt, T, k_axpby<T><<<blocks_for(n, 256), 256, 0, st>>>(c0, (const T *)x, c1,
+                                                                            (const T *)y, (T *)out, n));
+  MLPCG_LAUNCH_CHECK();
+  return MLPCG_OK;
+}
+
+size_t linear_workspace() { return (size_t)27 * 3 * kLinBlocks * sizeof(double); }
+
+int launch_linear_forward(const float *img, int n1, int n2, int n3, const float *W, const float *bias,
+                          int nlin, float *z, float *y, void *ws, size_t ws_bytes, cudaStream_t st) {
+  MLPCG_REQUIRE(ws_bytes >= linear_workspace(), MLPCG_ERR_WORKSPACE,
+                "sm_linear_3d workspace too small: %zu < %zu", ws_bytes, linear_workspace());
+  k_class_sums<<<dim3(kLinBlocks, 27), kLinThreads, 0, st>>>(img, n1, n2, n3, (double *)ws);
+  MLPCG_LAUNCH_CHECK();
+  k_linear_finalize<<<1, 128, 0, st>>>((const double *)ws, kLinBlocks, n1, n2, n3, W, bias, nlin, z, y);
+  MLPCG_LAUNCH_CHECK();
+  return MLPCG_OK;
+}
+
+int launch_linear_backward(const float *g, const float *y, float *gw, float *gb, cudaStream_t st) {
+  k_linear_backward<<<1, 96, 0, st>>>(g, y, gw, gb);
+  MLPCG_LAUNCH_CHECK();
+  return MLPCG_OK;
+}
+
+int launch_linear_image_grad(const float *g, const float *W, float *gimg, int n1, int n2, int n3,
+                             cudaStream_t st) {
+  k_linear_image_grad<<<blocks_for(cells(n1, n2, n3), 256), 256, 0, st>>>(g, W, n1, n2, n3, gimg);
+  MLPCG_LAUNCH_CHECK();
+  return MLPCG_OK;
+}
+
+int launch_laplacian(const uint8_t *flags, const void *x, void *y, int dt, int n1, int n2, int n3,
+                     cudaStream_t st) {
+  const int64_t n = cells(n1, n2, n3);
+  if (dt == MLPCG_F32)
+    k_laplacian<float><<<blocks_for(n, 256), 256, 0, st>>>(flags, (const float *)x, (float *)y, n1, n2, n3);
+  else if (dt == MLPCG_F64)
+    k_laplacian<double><<<blocks_for(n, 256), 256, 0, st>>>(flags, (const double *)x, (double *)y, n1, n2, n3);
+  else {
+    set_error("laplacian: dtype must be F32 or F64");
+    return MLPCG_ERR_UNSUPPORTED;
+  }
+  MLPCG_LAUNCH_CHECK();
+  return MLPCG_OK;
+}
+
+}  // namespace mlpcg

@@ -1,0 +1,351 @@
+"""Drop-in for the reference's sm_model_3d.py: autograd Functions, blocks and SmallSMModelDn3D.
+
+Class names, constructor signatures, forward / eval_forward signatures and
+parameter names (state-dict keys) are those of the reference
+(sm_model_3d.py:21-287), so reference checkpoints load unchanged
+(``model.load_state_dict(torch.load(f)['model_state_dict'])``).  Every
+numerical step runs in the sm_103a kernels of ``libmlpcg_gb300.so``:
+
+* blocks evaluate their coefficients from the image and apply them
+  (reference semantics: recomputed per call, FP32);
+* avg-pool restriction, trilinear prolongation and the c0/c1 combine are
+  library kernels, each with a hand-written adjoint for training;
+* the image needs no F.pad copy: out-of-grid neighbours read as zero.
+
+For the fast solve path (coefficients precomputed once per image, BF16
+storage, fused level transfers) see ``precond.PrecondPlan``.
+"""
+from __future__ import annotations
+
+import torch
+import torch.nn as nn
+
+from . import ops
+from .model import BaseModel
+
+# The reference's JIT extension modules (sm_model_3d.py:11-16).
+smblock3d = ops.smblock3d
+smblocktrans3d = ops.smblocktrans3d
+smlinear3d = ops.smlinear3d
+
+
+def _tstart(timer, name):
+    if timer:
+        timer.start(name)
+
+
+def _tstop(timer, name):
+    if timer:
+        torch.cuda.synchronize()
+        timer.stop(name)
+
+
+######################
+# SM block
+######################
+class SMBlockFunction3D(torch.autograd.Function):
+    """y(q) = sum_p K_p(q) x(q + off_p), K = bias + Conv3d(3->27)(image) (sm_model_3d.py:21-48)."""
+
+    @staticmethod
+    def inference(image, x, weights, bias, timer=None):
+        _tstart(timer, "Forward")
+        y = ops.block_forward(image, x, weights, bias, transpose=False)
+        _tstop(timer, "Forward")
+        return y
+
+    @staticmethod
+    def forward(ctx, image, x, weights, bias):
+        y = ops.block_forward(image, x, weights, bias, transpose=False)
+        ctx.save_for_backward(image, x, weights, bias)
+        return y
+
+    @staticmethod
+    def backward(ctx, grad_output):
+        image, x, weights, bias = ctx.saved_tensors
+        gx, gw, gb, gi = ops.block_backward(grad_output, image, x, weights, bias, transpose=False,
+                                            image_grad=ctx.needs_input_grad[0])
+        return gi, gx, gw, gb
+
+
+class SMBlockTransFunction3D(torch.autograd.Function):
+    """Transpose of SMBlockFunction3D (sm_model_3d.py:50-76)."""
+
+    @staticmethod
+    def inference(image, x, weights, bias, timer=None):
+        _tstart(timer, "Forward")
+        y = ops.block_forward(image, x, weights, bias, transpose=True)
+        _tstop(timer, "Forward")
+        return y
+
+    @staticmethod
+    def forward(ctx, image, x, weights, bias):
+        y = ops.block_forward(image, x, weights, bias, transpose=True)
+        ctx.save_for_backward(image, x, weights, bias)
+        return y
+
+    @staticmethod
+    def backward(ctx, grad_output):
+        image, x, weights, bias = ctx.saved_tensors
+        gx, gw, gb, gi = ops.block_backward(grad_output, image, x, weights, bias, transpose=True,
+                                            image_grad=ctx.needs_input_grad[0])
+        return gi, gx, gw, gb
+
+
+class SmallSMBlock3D(BaseModel):
+    def __init__(self, num_imgs=3, mask=False):
+        super().__init__()
+        if num_imgs != 3:
+            raise ValueError("the sm_103a kernels take 3 image channels (air, fluid, non-solid)")
+        self.mask = mask
+        self.weight = nn.Parameter(torch.ones(27, num_imgs, 3, 3, 3))
+        self.bias = nn.Parameter(torch.ones(27))
+        self.reset_parameters(self.weight, self.bias)
+
+    def forward(self, image, x):
+        y = SMBlockFunction3D.apply(image, x, self.weight, self.bias)
+        if self.mask:
+            y = torch.where(image[1] == 0, 0.0, y)
+        return y
+
+    def eval_forward(self, image, x, timer=None):
+        y = SMBlockFunction3D.inference(image, x, self.weight, self.bias, timer)
+        if self.mask:
+            y = torch.where(image[1] == 0, 0.0, y)
+        return y
+
+
+class SmallSMBlockTrans3D(BaseModel):
+    def __init__(self, num_imgs=3, weight=None, bias=None):
+        super().__init__()
+        if num_imgs != 3:
+            raise ValueError("the sm_103a kernels take 3 image channels (air, fluid, non-solid)")
+        self.weight = nn.Parameter(torch.ones(27, num_imgs, 3, 3, 3)) if weight is None else weight
+        self.bias = nn.Parameter(torch.ones(27)) if bias is None else bias
+        if weight is None and bias is None:
+            self.reset_parameters(self.weight, self.bias)
+
+    def forward(self, image, x):
+        return SMBlockTransFunction3D.apply(image, x, self.weight, self.bias)
+
+    def eval_forward(self, image, x, timer=None):
+        return SMBlockTransFunction3D.inference(image, x, self.weight, self.bias, timer)
+
+
+######################
+# SM linear
+######################
+class SMLinearFunction3D(torch.autograd.Function):
+    """z = w . mean_q(shifted image patches) + b (sm_model_3d.py:118-144)."""
+
+    @staticmethod
+    def inference(image, weights, bias, timer=None):
+        _tstart(timer, "Forward")
+        z, _ = ops.linear_forward(image, weights, bias)
+        _tstop(timer, "Forward")
+        return z
+
+    @staticmethod
+    def forward(ctx, image, weights, bias, timer=None):
+        z, y = ops.linear_forward(image, weights, bias)
+        ctx.save_for_backward(y, weights)
+        ctx.dims = tuple(image.shape[1:])
+        return z
+
+    @staticmethod
+    def backward(ctx, grad_output):
+        y, weights = ctx.saved_tensors
+        gw, gb = ops.linear_backward(grad_output, y)
+        gi = ops.linear_image_grad(grad_output, weights, ctx.dims) if ctx.needs_input_grad[0] else None
+        return gi, gw, gb, None
+
+
+class SmallLinearBlock3DNew(BaseModel):
+    def __init__(self, num_imgs=3):
+        super().__init__()
+        if num_imgs != 3:
+            raise ValueError("the sm_103a kernels take 3 image channels (air, fluid, non-solid)")
+        self.weight = torch.ones(27, num_imgs, 3, 3, 3)
+        self.bias = torch.ones(27)
+        self.reset_parameters(self.weight, self.bias)
+        self.weight = nn.Parameter(self.weight.mean(dim=0, keepdim=True))
+        self.bias = nn.Parameter(self.bias.mean(dim=0, keepdim=True))
+
+    def forward(self, image):
+        return SMLinearFunction3D.apply(image, self.weight, self.bias)
+
+    def eval_forward(self, image, timer=None):
+        return SMLinearFunction3D.inference(image, self.weight, self.bias, timer)
+
+
+######################
+# level transfer with hand-written adjoints
+######################
+class AvgPool2Function(torch.autograd.Function):
+    """F.avg_pool3d(x, (2, 2, 2))."""
+
+    @staticmethod
+    def forward(ctx, x):
+        return ops.avg_pool2(x.contiguous())
+
+    @staticmethod
+    def backward(ctx, g):
+        return ops.avg_pool2_adjoint(g.contiguous())
+
+
+class Upsample2Function(torch.autograd.Function):
+    """F.interpolate(x, scale_factor=2, mode='trilinear')."""
+
+    @staticmethod
+    def forward(ctx, x):
+        return ops.upsample2(x.contiguous())
+
+    @staticmethod
+    def backward(ctx, g):
+        return ops.upsample2_adjoint(g.contiguous())
+
+
+class CombineFunction(torch.autograd.Function):
+    """c0 * x + c1 * y with scalar (1,) tensors c0, c1 (sm_model_3d.py:258,286)."""
+
+    @staticmethod
+    def forward(ctx, c0, x, c1, y):
+        x, y = x.contiguous(), y.contiguous()
+        ctx.save_for_backward(c0, x, c1, y)
+        return ops.axpby(c0, x, c1, y)
+
+    @staticmethod
+    def backward(ctx, g):
+        c0, x, c1, y = ctx.saved_tensors
+        g = g.contiguous()
+        zero = torch.zeros(1, dtype=torch.float32, device=g.device)
+        gx = ops.axpby(c0, g, zero, g) if ctx.needs_input_grad[1] else None
+        gy = ops.axpby(c1, g, zero, g) if ctx.needs_input_grad[3] else None
+        gc0 = ops.dot(g, x).to(c0.dtype).reshape(c0.shape) if ctx.needs_input_grad[0] else None
+        gc1 = ops.dot(g, y).to(c1.dtype).reshape(c1.shape) if ctx.needs_input_grad[2] else None
+        return gc0, gx, gc1, gy
+
+
+def _check_mode(mode):
+    if mode != "trilinear":
+        raise ValueError(f"interpolation_mode {mode!r}: only 'trilinear' is provided by the sm_103a kernels")
+
+
+######################
+# Full SM Model
+######################
+class SmallSMModelDn3D(BaseModel):
+    """Multilevel preconditioner network (sm_model_3d.py:164-287).
+
+    Parameters are created in the reference's order (pre[1..n-1], pre[0],
+    post[1..n-1], post[0], l, c0[*], c1[*]) so that a given torch seed gives
+    the reference's initial weights.
+    """
+
+    def __init__(self, n, num_imgs=3, interpolation_mode="trilinear", mask=False, swap_sm_order=False):
+        super().__init__()
+        _check_mode(interpolation_mode)
+        self.n = n
+        self.mode = interpolation_mode
+        self.swap_ord = swap_sm_order
+        self.pre = nn.ModuleList([SmallSMBlock3D(num_imgs) for _ in range(n - 1)])
+        self.pre.insert(0, SmallSMBlock3D(num_imgs, mask))
+        self.post = nn.ModuleList([SmallSMBlock3D(num_imgs) for _ in range(n - 1)])
+        self.post.insert(0, SmallSMBlock3D(num_imgs, mask))
+        self.l = SmallSMBlock3D(num_imgs)
+        self.c0 = nn.ModuleList([SmallLinearBlock3DNew(num_imgs) for _ in range(n)])
+        self.c1 = nn.ModuleList([SmallLinearBlock3DNew(num_imgs) for _ in range(n)])
+
+    def check_grid(self, shape):
+        n1, n2, n3 = shape[-3:]
+        f = 2 ** self.n
+        if n1 % f or n2 % f or n3 % f:
+            raise ValueError(f"grid {tuple(shape[-3:])} must be divisible by 2**n = {f} "
+                             "(each level halves it and the upsampled level must match)")
+
+    def eval_forward(self, image, b, timer=None, imgs=None, c0=None, c1=None):
+        """Inference pass (sm_model_3d.py:180-262).  ``imgs``, ``c0``, ``c1`` are
+        caller-owned cache lists, filled on the first call and reused after; when
+        omitted a fresh cache is used (the reference shares mutable default
+        lists across calls, which reuses a stale pyramid if the image changes)."""
+        self.check_grid(image.shape)
+        imgs = [] if imgs is None else imgs
+        c0 = [] if c0 is None else c0
+        c1 = [] if c1 is None else c1
+        imgs_cached, c0_cached, c1_cached = bool(imgs), bool(c0), bool(c1)
+        if not imgs_cached:
+            imgs.extend([None] * self.n)
+        if not c0_cached:
+            c0.extend([None] * self.n)
+        if not c1_cached:
+            c1.extend([None] * self.n)
+
+        _tstart(timer, "SM block")
+        x = [self.pre[0].eval_forward(image, b, timer)]
+        if not imgs_cached:
+            imgs[0] = image
+        _tstop(timer, "SM block")
+
+        for i in range(1, self.n):
+            _tstart(timer, "Downsampling")
+            x.append(ops.avg_pool2(x[-1]))
+            if not imgs_cached:
+                imgs[i] = ops.avg_pool2(imgs[i - 1])
+            _tstop(timer, "Downsampling")
+            _tstart(timer, "SM block")
+            x[-1] = self.pre[i].eval_forward(imgs[i], x[-1], timer)
+            _tstop(timer, "SM block")
+
+        _tstart(timer, "Downsampling")
+        x.append(ops.avg_pool2(x[-1]))
+        fine_img = ops.avg_pool2(imgs[-1])
+        _tstop(timer, "Downsampling")
+        _tstart(timer, "SM block")
+        x[-1] = self.l.eval_forward(fine_img, x[-1], timer)
+        _tstop(timer, "SM block")
+
+        for i in range(self.n, 0, -1):
+            _tstart(timer, "Upsamping")
+            x[i] = ops.upsample2(x[i])
+            _tstop(timer, "Upsamping")
+            _tstart(timer, "SM linear")
+            if not c0_cached:
+                c0[i - 1] = self.c0[i - 1].eval_forward(imgs[i - 1], timer)
+            if not c1_cached:
+                c1[i - 1] = self.c1[i - 1].eval_forward(imgs[i - 1], timer)
+            _tstop(timer, "SM linear")
+            if self.swap_ord:
+                x[i - 1] = ops.axpby(c0[i - 1], x[i - 1], c1[i - 1], x[i])
+                x[i - 1] = self.post[i - 1].eval_forward(imgs[i - 1], x[i - 1], timer)
+            else:
+                x[i] = self.post[i - 1].eval_forward(imgs[i - 1], x[i], timer)
+                x[i - 1] = ops.axpby(c0[i - 1], x[i - 1], c1[i - 1], x[i])
+        return x[0]
+
+    def forward(self, image, b):
+        """Training pass with autograd (sm_model_3d.py:264-287)."""
+        self.check_grid(image.shape)
+        x = [self.pre[0](image, b)]
+        imgs = [image]
+        for i in range(1, self.n):
+            x.append(AvgPool2Function.apply(x[-1]))
+            imgs.append(AvgPool2Function.apply(imgs[-1]))
+            x[-1] = self.pre[i](imgs[-1], x[-1])
+        x.append(AvgPool2Function.apply(x[-1]))
+        imgs.append(AvgPool2Function.apply(imgs[-1]))
+        x[-1] = self.l(imgs[-1], x[-1])
+        for i in range(self.n, 0, -1):
+            x[i] = Upsample2Function.apply(x[i])
+            c0 = self.c0[i - 1](imgs[i - 1])
+            c1 = self.c1[i - 1](imgs[i - 1])
+            if self.swap_ord:
+                x[i - 1] = CombineFunction.apply(c0, x[i - 1], c1, x[i])
+                x[i - 1] = self.post[i - 1](imgs[i - 1], x[i - 1])
+            else:
+                x[i] = self.post[i - 1](imgs[i - 1], x[i])
+                x[i - 1] = CombineFunction.apply(c0, x[i - 1], c1, x[i])
+        return x[0]
+
+    def precond_plan(self, image, storage=torch.bfloat16, fluid_mask=None):
+        """Coefficients of every block precomputed on ``image``: see precond.PrecondPlan."""
+        from .precond import PrecondPlan
+        return PrecondPlan(self, image, storage=storage, fluid_mask=fluid_mask)

@@ -1,0 +1,280 @@
+"""Generates the golden fixtures of tests/golden/ from the reference itself.
+
+Run in a container that has the reference checkout (its Python CPU path needs
+only torch, numpy and scipy):
+
+    python tests/golden/make_golden.py /path/to/MLPCG
+
+What it imports from the reference, unmodified:
+
+* sm_model_3d_py.py -- SmallSMBlock3DPY (Conv3d + unfold) and SmallLinearBlock3DPY,
+  the reference's own CPU statement of the block and linear ops;
+* sm_model_3d.py    -- SmallSMModelDn3D and its autograd Functions; its JIT
+  extension modules (CUDA, cannot run here) are replaced by thin adapters that
+  evaluate the ops with the SmallSMBlock3DPY / SmallLinearBlock3DPY math, so
+  the reference's own module tree, initialisation order and orchestration
+  (forward / eval_forward) run on the CPU;
+* model.py          -- BaseModel.reset_parameters;
+* lib/discrete_laplacian.py, lib/read_data.py -- lap_with_bc, compressedMat,
+  convert_to_binary_images;
+* cg_tests.py       -- npcg, npcg_flex, npsd (cupy / AMGCL imports stubbed,
+  torch.cuda.synchronize made a no-op).
+
+Outputs (FP64 unless noted): ops_*.npz, model_*.npz, laplacian_*.npz, cg_*.npz.
+The scenes come from mlpcg_gb300.scenes (seeded), stored in the fixtures.
+"""
+from __future__ import annotations
+
+import sys
+import types
+from pathlib import Path
+
+import numpy as np
+import torch
+import torch.nn.functional as F
+
+HERE = Path(__file__).resolve().parent
+REPO = HERE.parent.parent
+sys.path.insert(0, str(REPO))
+
+from mlpcg_gb300.scenes import make_scene  # noqa: E402
+
+
+def _import_reference(ref: Path):
+    sys.path.insert(0, str(ref))
+    sys.path.insert(0, str(ref / "lib"))
+    # sm_model_3d.py JIT-builds CUDA extensions at import; the adapters below replace them.
+    import torch.utils.cpp_extension as ce
+    real_load = ce.load
+    ce.load = lambda *a, **k: types.SimpleNamespace()
+    try:
+        import sm_model_3d as ref_model
+    finally:
+        ce.load = real_load
+    import sm_model_3d_py as ref_py
+    import discrete_laplacian as ref_lap
+    import read_data as ref_read
+    # cg_tests.py imports cupy and the AMGCL/IC builds at module level
+    for name in ("cupy", "cupyx", "cupyx.scipy", "cupyx.scipy.sparse", "cupyx.scipy.sparse.linalg",
+                 "cxx_src", "cxx_src.build"):
+        sys.modules.setdefault(name, types.ModuleType(name))
+    b = sys.modules["cxx_src.build"]
+    for n in ("pyamgcl", "pyamgcl_cuda", "pyamgcl_vexcl", "pyic", "pyic_cuda", "pyic_vexcl"):
+        setattr(b, n, None)
+    torch.cuda.synchronize = lambda *a, **k: None
+    import cg_tests as ref_cg
+    return ref_model, ref_py, ref_lap, ref_read, ref_cg
+
+
+class _BlockAdapter:
+    """smblock3d / smblocktrans3d interface evaluated with SmallSMBlock3DPY."""
+
+    def __init__(self, ref_py, transpose):
+        self.ref_py = ref_py
+        self.t = transpose
+
+    def _blk(self, W, b):
+        blk = self.ref_py.SmallSMBlock3DPY(3).to(W.dtype)
+        with torch.no_grad():
+            blk.KL.weight.copy_(W)
+            blk.KL.bias.copy_(b)
+        return blk
+
+    def _fwd(self, image_p, x_p, W, b):
+        image = image_p[:, 1:-1, 1:-1, 1:-1]
+        x = x_p[..., 1:-1, 1:-1, 1:-1]
+        blk = self._blk(W, b)
+        if not self.t:
+            with torch.no_grad():
+                return blk(image, x)
+        xx = torch.zeros_like(x, requires_grad=True)
+        with torch.enable_grad():
+            out = blk(image, xx)
+            (gx,) = torch.autograd.grad(out, xx, grad_outputs=x)
+        return gx.detach()
+
+    def inference(self, image_p, x_p, W, b):
+        return [self._fwd(image_p, x_p, W, b)]
+
+    forward = inference
+
+
+class _LinearAdapter:
+    """smlinear3d interface evaluated with SmallLinearBlock3DPY."""
+
+    def __init__(self, ref_py):
+        self.ref_py = ref_py
+
+    def inference(self, image, W, b):
+        blk = self.ref_py.SmallLinearBlock3DPY(3).to(W.dtype)
+        with torch.no_grad():
+            blk.KL.weight.copy_(W.reshape(1, 3, 3, 3, 3).expand(27, 3, 3, 3, 3))
+            blk.KL.bias.copy_(b.reshape(1).expand(27))
+            z = blk(image).reshape(1)
+            eye = torch.eye(81, dtype=image.dtype).reshape(81, 3, 3, 3, 3)
+            y = F.conv3d(image[None], eye, padding=1).mean(dim=(2, 3, 4)).reshape(1, 3, 3, 3, 3)
+        return [z, y]
+
+    forward = inference
+
+
+def _py_block(ref_py, W, b, dtype):
+    blk = ref_py.SmallSMBlock3DPY(3).to(dtype)
+    with torch.no_grad():
+        blk.KL.weight.copy_(W)
+        blk.KL.bias.copy_(b)
+    return blk
+
+
+def make_ops(ref_py, shape, seed, B=2):
+    torch.manual_seed(seed)
+    dt = torch.float64
+    image = torch.rand(3, *shape, dtype=dt)
+    x = torch.rand(B, 1, *shape, dtype=dt)
+    g = torch.rand(B, 1, *shape, dtype=dt)
+    blk0 = ref_py.SmallSMBlock3DPY(3)
+    W = blk0.KL.weight.detach().to(dt).clone()
+    b = blk0.KL.bias.detach().to(dt).clone()
+    out = dict(image=image.numpy(), x=x.numpy(), g=g.numpy(), W=W.numpy(), b=b.numpy())
+    # forward block, its gradients (autograd through the reference's Conv3d + unfold)
+    blk = _py_block(ref_py, W, b, dt)
+    xx = x.clone().requires_grad_(True)
+    img = image.clone().requires_grad_(True)
+    y = blk(img, xx)
+    y.backward(g)
+    out.update(y=y.detach().numpy(), dx=xx.grad.numpy(), dW=blk.KL.weight.grad.numpy(),
+               db=blk.KL.bias.grad.numpy(), dimg=img.grad.numpy())
+    # transposed block: y_t = B^T x as a vector-Jacobian product of the forward block
+    blk = _py_block(ref_py, W, b, dt)
+    img = image.clone().requires_grad_(True)
+    v = torch.zeros_like(x, requires_grad=True)
+    with torch.enable_grad():
+        yv = blk(img, v)
+        (yt,) = torch.autograd.grad(yv, v, grad_outputs=x, create_graph=True)
+    out["yt"] = yt.detach().numpy()
+    blk.zero_grad()
+    yt.backward(g)
+    out.update(dxt=None if v.grad is None else v.grad.numpy())
+    out["dWt"] = blk.KL.weight.grad.numpy()
+    out["dbt"] = blk.KL.bias.grad.numpy()
+    out["dimgt"] = img.grad.numpy()
+    # B applied to g equals the gradient of <g, B^T x> w.r.t. x
+    with torch.no_grad():
+        out["dxt"] = blk(image, g).numpy()
+    # linear block (mean-weight form of SmallLinearBlock3DNew)
+    lin = ref_py.SmallLinearBlock3DPY(3).to(dt)
+    Wl = lin.KL.weight.detach().mean(0, keepdim=True)
+    bl = lin.KL.bias.detach().mean(0, keepdim=True)
+    img = image.clone().requires_grad_(True)
+    z = lin(img)
+    z.backward()
+    eye = torch.eye(81, dtype=dt).reshape(81, 3, 3, 3, 3)
+    ymean = F.conv3d(image[None], eye, padding=1).mean(dim=(2, 3, 4)).reshape(1, 3, 3, 3, 3)
+    out.update(Wl=Wl.numpy(), bl=bl.numpy(), z=np.array([z.item()]), ylin=ymean.numpy(),
+               dimg_lin=img.grad.numpy())
+    # pooling / interpolation (torch CPU = ATen reference semantics)
+    if all(s % 2 == 0 for s in shape):
+        out["pool"] = F.avg_pool3d(x, (2, 2, 2)).numpy()
+    out["up"] = F.interpolate(x, scale_factor=2, mode="trilinear").numpy()
+    return out
+
+
+def make_model(ref_model, ref_py, shape, n, seed_scene, seed_init=0):
+    ref_model.smblock3d = _BlockAdapter(ref_py, False)
+    ref_model.smblocktrans3d = _BlockAdapter(ref_py, True)
+    ref_model.smlinear3d = _LinearAdapter(ref_py)
+    torch.manual_seed(seed_init)
+    model = ref_model.SmallSMModelDn3D(n, 3, "trilinear")
+    sd = {k: v.detach().numpy().copy() for k, v in model.state_dict().items()}
+    scene = make_scene(shape, seed_scene)
+    image = torch.from_numpy(scene.image())
+    torch.manual_seed(1234)
+    b = torch.rand(2, 1, *shape)
+    with torch.no_grad():
+        y = model(image, b)
+        from global_clock import GlobalClock
+        ye = model.eval_forward(image, b[:1], GlobalClock(), [], [], [])
+    out = {"flags": scene.flags, "image": scene.image(), "b": b.numpy(), "y": y.numpy(), "y_eval": ye.numpy(),
+           "n": np.array(n)}
+    out.update({"param:" + k: v for k, v in sd.items()})
+    return out, model, scene
+
+
+def make_laplacian(ref_lap, ref_read, shape, seed):
+    scene = make_scene(shape, seed)
+    f = scene.flags
+    n = f.shape[0]
+    idx = lambda code: [tuple(int(c) for c in t) for t in np.argwhere(f == code)]
+    A_full = ref_lap.lap_with_bc(n, 3, solid=idx(1), air=idx(3), bd=idx(0), bd_padding=True, dtype=np.float64)
+    # the flat cell index of every row compressedMat keeps (rows with stored entries)
+    kept = np.flatnonzero(A_full.tocsr().getnnz(1) > 0)
+    A = ref_read.compressedMat(A_full, f)
+    A = A.tocsr()
+    A.sort_indices()
+    img = ref_read.convert_to_binary_images(f, 3)
+    return {"flags": f, "indptr": A.indptr, "indices": A.indices, "data": A.data, "kept_cells": kept,
+            "image": img.astype(np.float32), "rhs": scene.rhs}
+
+
+def make_cg(ref_cg, model, scene, max_it=30):
+    import scipy.sparse as sp
+    from mlpcg_gb300.laplacian import csr_from_flags  # noqa: F401 (not used: reference matrix below)
+    lap = sys.modules["discrete_laplacian"]
+    rd = sys.modules["read_data"]
+    f = scene.flags
+    n = f.shape[0]
+    idx = lambda code: [tuple(int(c) for c in t) for t in np.argwhere(f == code)]
+    A = lap.lap_with_bc(n, 3, solid=idx(1), air=idx(3), bd=idx(0), bd_padding=True, dtype=np.float64)
+    A = rd.compressedMat(A, f).tocsr()
+    A.sort_indices()
+    assert A.shape[0] == int((f == 2).sum()), "scene must have no sphere touching the wall layer"
+    At = torch.sparse_csr_tensor(A.indptr, A.indices, A.data, A.shape, dtype=torch.float64)
+    fluid = torch.from_numpy(np.flatnonzero(f.ravel() == 2))
+    rhs = torch.from_numpy(scene.rhs.ravel()[fluid.numpy()]).double()
+    image = torch.from_numpy(scene.image())
+    shape = tuple(f.shape)
+
+    def predict(r, timer, imgs=[], c0=[], c1=[]):  # test.py:42-51 restated (test.py cannot be imported)
+        with torch.no_grad():
+            r = F.normalize(r.to(torch.float32), dim=0)
+            bb = torch.zeros(int(np.prod(shape)), dtype=torch.float32)
+            bb[fluid] = r
+            x = model.eval_forward(image, bb.view((1, 1) + shape), timer, imgs, c0, c1).flatten().double()
+        return x[fluid]
+
+    out = {"flags": f, "rhs": scene.rhs}
+    for name in ("npsd", "npcg", "npcg_flex"):
+        hist = []
+        solver = getattr(ref_cg, name)
+        pred = predict if name == "npsd" else (lambda r, timer, _p=predict, _c=([], [], []): _p(r, timer, *_c))
+        x, iters, _, res = solver(rhs, At, torch.zeros_like(rhs), pred, max_it, tol=1e-6, atol=1e-20,
+                                  callback=lambda nrm, t: hist.append(nrm))
+        out[f"{name}_hist"] = np.array(hist)
+        out[f"{name}_iters"] = np.array(iters)
+        out[f"{name}_x"] = x.numpy()
+    return out
+
+
+def main(ref_root: str):
+    ref = Path(ref_root)
+    ref_model, ref_py, ref_lap, ref_read, ref_cg = _import_reference(ref)
+    torch.set_default_dtype(torch.float32)
+    for shape, seed in (((8, 8, 8), 0), ((6, 4, 10), 1), ((16, 16, 16), 2)):
+        out = make_ops(ref_py, shape, seed)
+        out = {k: v for k, v in out.items() if v is not None}
+        np.savez_compressed(HERE / f"ops_{'x'.join(map(str, shape))}.npz", **out)
+    out, model, scene = make_model(ref_model, ref_py, (16, 16, 16), 3, seed_scene=3)
+    np.savez_compressed(HERE / "model_16_l3.npz", **out)
+    # initial weights of the 4-level and 5-level networks under torch.manual_seed(0)
+    for n in (4, 5):
+        torch.manual_seed(0)
+        m = ref_model.SmallSMModelDn3D(n, 3, "trilinear")
+        np.savez_compressed(HERE / f"init_l{n}_seed0.npz",
+                            **{k: v.detach().numpy() for k, v in m.state_dict().items()})
+    np.savez_compressed(HERE / "laplacian_12.npz", **make_laplacian(ref_lap, ref_read, (12, 12, 12), 5))
+    np.savez_compressed(HERE / "cg_16_l3.npz", **make_cg(ref_cg, model, scene))
+    print("fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

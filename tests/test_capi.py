@@ -1,0 +1,75 @@
+"""The C-ABI library builds, loads without a GPU, exports every declared symbol and
+rejects bad arguments before touching the device (CPU only)."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def _declared():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        names |= set(re.findall(r"\b(mlpcg_[a-z0-9_]+)\s*\(", text))
+    return names
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from mlpcg_gb300 import _lib
+    return _lib.load()
+
+
+def test_exports_every_declared_symbol(lib):
+    import subprocess
+    from mlpcg_gb300 import _build
+    declared = _declared()
+    assert len(declared) >= 20
+    out = subprocess.run(["nm", "-D", "--defined-only", str(_build.LIB_PATH)], capture_output=True,
+                         text=True, check=True).stdout
+    exported = set(re.findall(r"\bT (mlpcg_[a-z0-9_]+)", out))
+    assert declared <= exported, sorted(declared - exported)
+    # nothing but the ABI is exported
+    assert exported == declared, sorted(exported - declared)
+    for name in declared:
+        getattr(lib, name)
+
+
+def test_ctypes_prototypes_cover_header(lib):
+    from mlpcg_gb300 import _lib
+    assert set(_lib.exported_symbols()) == _declared()
+
+
+def test_abi_version(lib):
+    assert lib.mlpcg_abi_version() >= 1
+
+
+def test_null_pointer_rejected_without_device(lib):
+    from mlpcg_gb300._lib import MLPCGError, call
+    with pytest.raises(MLPCGError, match="image must not be NULL"):
+        call("mlpcg_stencil_gen", None, 0, 8, 8, 8, None, None, None, 0, 512, None)
+    assert b"NULL" in lib.mlpcg_last_error()
+
+
+def test_bad_shapes_rejected(lib):
+    from mlpcg_gb300._lib import MLPCGError, call
+    dummy = C.c_void_p(16)  # never dereferenced: validation fails first
+    with pytest.raises(MLPCGError, match="grid sizes"):
+        call("mlpcg_stencil_gen", dummy, 0, 0, 8, 8, dummy, dummy, dummy, 0, 512, None)
+    with pytest.raises(MLPCGError, match="plane_stride"):
+        call("mlpcg_stencil_gen", dummy, 0, 8, 8, 8, dummy, dummy, dummy, 0, 100, None)
+    with pytest.raises(MLPCGError, match="even"):
+        call("mlpcg_avg_pool2", dummy, dummy, 0, 1, 7, 8, 8, None)
+    with pytest.raises(MLPCGError, match="workspace too small"):
+        call("mlpcg_sm_block_3d_forward", dummy, 0, dummy, 0, dummy, dummy, dummy, 1, 8, 8, 8, 0,
+             dummy, 16, None)
+
+
+def test_workspace_queries(lib):
+    from mlpcg_gb300._lib import query
+    assert query("mlpcg_sm_block_3d_workspace", 8, 8, 8) >= 27 * 512 * 4
+    assert query("mlpcg_sm_linear_3d_workspace", 8, 8, 8) > 0
+    assert query("mlpcg_dot_workspace", 1 << 20) >= 8
