@@ -228,6 +228,98 @@ int mlpcg_laplacian_apply(const uint8_t *flags, const void *x, void *y, int dtyp
                           int N1, int N2, int N3, void *stream);
 
 /* =========================================================================
+ * Preconditioner plan: SmallSMModelDn3D.eval_forward (sm_model_3d.py:180-262)
+ * with every block's coefficients precomputed once per (image, weights).
+ * The reference re-evaluates them inside every sm_block_3d call
+ * (sm_block_3d_kernel.cu:45-65) and only caches the image pyramid and c0/c1
+ * (sm_model_3d.py:180-239).  Application = 2*levels+1 fused kernels:
+ * restriction fused into the pre-blocks, trilinear prolongation and the
+ * c0/c1 combine fused into the post-blocks.
+ * ========================================================================= */
+typedef struct mlpcg_precond mlpcg_precond;
+
+/* Host-side plan for an N1 x N2 x N3 grid (each divisible by 2^levels).
+ * k_dtype / act_dtype: storage of coefficients / level activations, F32 or
+ * BF16 (arithmetic is FP32).  swap_sm_order and mask have the meaning of the
+ * SmallSMModelDn3D constructor arguments. */
+int mlpcg_precond_create(int N1, int N2, int N3, int levels, int k_dtype, int act_dtype,
+                         int swap_sm_order, int mask, mlpcg_precond **out);
+/* Device bytes the plan needs (caller allocates, 256-byte aligned). */
+size_t mlpcg_precond_workspace(const mlpcg_precond *plan);
+void mlpcg_precond_destroy(mlpcg_precond *plan);
+/*
+ * Builds the image pyramid, the coefficient planes of all 2*levels+1 blocks
+ * and the per-level c0/c1 scalars.  image: 3 x N (F32, the [air, fluid,
+ * non-solid] channels, lib/read_data.py:28-39).  params: device F32 array
+ * packing, in order, pre[0..n-1], post[0..n-1], l as (weight 2187, bias 27)
+ * and then c0[0..n-1], c1[0..n-1] as (weight 81, bias 1).
+ */
+int mlpcg_precond_setup(mlpcg_precond *plan, void *workspace, size_t workspace_bytes,
+                        const float *image, const float *params, void *stream);
+/*
+ * z = M(r * r_scale[0]) on the fine grid (r_scale may be NULL = 1; the
+ * reference feeds the network r/||r||, test.py:46).  z is F32 and zero on
+ * non-fluid cells (image channel 1 == 0), which is what the reference's
+ * gather of fluid cells keeps (test.py:49-50).  r 16-byte, z 32-byte aligned.
+ */
+int mlpcg_precond_apply(const mlpcg_precond *plan, const float *r, const float *r_scale, float *z,
+                        void *stream);
+/* Runs stages [first, last] of one application (stage s < n: pre-block of
+ * level s; s = n: coarsest block; s > n: post-block of level 2n - s), using
+ * the plan's own level buffers.  Stage 0 reads r, stage 2n writes z.  Used
+ * to time the kernels of an application one by one. */
+int mlpcg_precond_apply_stages(const mlpcg_precond *plan, int first, int last, const float *r,
+                               const float *r_scale, float *z, void *stream);
+/* Sizes of level `level` (0 = finest) and whether it runs the tiled kernels
+ * (z size a multiple of 8) or the general ones. */
+int mlpcg_precond_level_info(const mlpcg_precond *plan, int level, int *n1, int *n2, int *n3,
+                             int *fast);
+/* Copies the 2*levels per-level scalars (c0[0..n-1], c1[0..n-1]) to c_out (device). */
+int mlpcg_precond_coefficients(const mlpcg_precond *plan, float *c_out, void *stream);
+
+/* =========================================================================
+ * Fused solver: the iteration of npsd (cg_tests.py:189-284, the solver of
+ * test.py:327-328) or npcg (cg_tests.py:26-101) run entirely on the GPU,
+ * captured once as a CUDA graph whose conditional WHILE node loops until
+ * convergence.  Vectors on the full grid (zero off-fluid): r, z, p, Ap FP32;
+ * x and b FP64; dot products reduced in FP64; the residual recomputed as
+ * r = b - A x in FP64 every true_every iterations and before convergence is
+ * declared, so the reported relative residual is the FP64 true residual.
+ * ========================================================================= */
+typedef struct mlpcg_solver mlpcg_solver;
+
+#define MLPCG_METHOD_NPSD 0
+#define MLPCG_METHOD_NPCG 1
+
+#define MLPCG_STATUS_RUNNING    0
+#define MLPCG_STATUS_CONVERGED  1
+#define MLPCG_STATUS_MAXIT      2
+#define MLPCG_STATUS_BREAKDOWN  3  /* p.Ap <= 0 */
+#define MLPCG_STATUS_NONFINITE  4  /* NaN / Inf met */
+
+/* The solver keeps `plan` (not owned) as its preconditioner. */
+int mlpcg_solver_create(int N1, int N2, int N3, const mlpcg_precond *plan, int method,
+                        int max_it, double tol, int true_every, mlpcg_solver **out);
+size_t mlpcg_solver_workspace(const mlpcg_solver *solver);
+void mlpcg_solver_destroy(mlpcg_solver *solver);
+/* flags: N uint8 cell codes; b: N FP64 rhs (read on FLUID cells only);
+ * x: N FP64, the initial guess on entry to solve and the solution after. */
+int mlpcg_solver_bind(mlpcg_solver *solver, void *workspace, size_t workspace_bytes,
+                      const uint8_t *flags, const double *b, double *x);
+/* Enqueues the solve on `stream`.  use_graph = 1: one graph launch (the graph
+ * is captured on the first call and reused until the next bind); 0: plain
+ * launches with a host status check per iteration. */
+int mlpcg_solver_solve(mlpcg_solver *solver, int use_graph, void *stream);
+/* Synchronises `stream`, then returns iterations, status, the final relative
+ * residual and (if history != NULL) max_it+1 relative residuals (host). */
+int mlpcg_solver_result(const mlpcg_solver *solver, int *iterations, int *status, double *rel_res,
+                        double *history, void *stream);
+
+/* Image channels [air, fluid, non-solid] (F32, 3 x N) from cell flags
+ * (convert_to_binary_images, lib/read_data.py:28-39). */
+int mlpcg_flags_to_image(const uint8_t *flags, float *image, int64_t n, void *stream);
+
+/* =========================================================================
  * Reductions
  * ========================================================================= */
 

@@ -42,6 +42,21 @@ _PROTOS = {
     "mlpcg_upsample2_adjoint": (_i, [_vp, _vp, _i, _i, _i, _i, _i, _vp]),
     "mlpcg_axpby": (_i, [_fp, _vp, _fp, _vp, _vp, _i, _i64, _vp]),
     "mlpcg_laplacian_apply": (_i, [_u8p, _vp, _vp, _i, _i, _i, _i, _vp]),
+    "mlpcg_precond_create": (_i, [_i, _i, _i, _i, _i, _i, _i, _i, _vp]),
+    "mlpcg_precond_workspace": (_sz, [_vp]),
+    "mlpcg_precond_destroy": (None, [_vp]),
+    "mlpcg_precond_setup": (_i, [_vp, _vp, _sz, _fp, _fp, _vp]),
+    "mlpcg_precond_apply": (_i, [_vp, _fp, _fp, _fp, _vp]),
+    "mlpcg_precond_coefficients": (_i, [_vp, _fp, _vp]),
+    "mlpcg_precond_apply_stages": (_i, [_vp, _i, _i, _fp, _fp, _fp, _vp]),
+    "mlpcg_precond_level_info": (_i, [_vp, _i, _vp, _vp, _vp, _vp]),
+    "mlpcg_solver_create": (_i, [_i, _i, _i, _vp, _i, _i, C.c_double, _i, _vp]),
+    "mlpcg_solver_workspace": (_sz, [_vp]),
+    "mlpcg_solver_destroy": (None, [_vp]),
+    "mlpcg_solver_bind": (_i, [_vp, _vp, _sz, _u8p, _vp, _vp]),
+    "mlpcg_solver_solve": (_i, [_vp, _i, _vp]),
+    "mlpcg_solver_result": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "mlpcg_flags_to_image": (_i, [_u8p, _fp, _i64, _vp]),
     "mlpcg_dot_workspace": (_sz, [_i64]),
     "mlpcg_dot": (_i, [_vp, _vp, _i, _i64, _vp, _vp, _sz, _vp]),
 }

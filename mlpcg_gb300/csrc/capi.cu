@@ -39,6 +39,7 @@ int launch_linear_forward(const float *, int, int, int, const float *, const flo
 int launch_linear_backward(const float *, const float *, float *, float *, cudaStream_t);
 int launch_linear_image_grad(const float *, const float *, float *, int, int, int, cudaStream_t);
 int launch_laplacian(const uint8_t *, const void *, void *, int, int, int, int, cudaStream_t);
+int launch_flags_to_image(const uint8_t *, float *, int64_t, cudaStream_t);
 // launchers (blas.cu)
 size_t dot_workspace(int64_t);
 int launch_dot(const void *, const void *, int, int64_t, double *, void *, size_t, cudaStream_t);
@@ -289,6 +290,13 @@ int mlpcg_laplacian_apply(const uint8_t *flags, const void *x, void *y, int dtyp
   CHECK_PTR(flags); CHECK_PTR(x); CHECK_PTR(y);
   RETURN_IF(check_dims(N1, N2, N3));
   return launch_laplacian(flags, x, y, dtype, N1, N2, N3, as_stream(stream));
+}
+
+int mlpcg_flags_to_image(const uint8_t *flags, float *image, int64_t n, void *stream) {
+  clear_error();
+  CHECK_PTR(flags); CHECK_PTR(image);
+  MLPCG_REQUIRE(n >= 1, MLPCG_ERR_ARG, "flags_to_image: n must be >= 1");
+  return launch_flags_to_image(flags, image, n, as_stream(stream));
 }
 
 size_t mlpcg_dot_workspace(int64_t n) { return dot_workspace(n < 1 ? 1 : n); }

@@ -316,9 +316,25 @@ __global__ void k_laplacian(const uint8_t *__restrict__ flags, const T *__restri
   y[q] = T(d) * x[q] - off;
 }
 
+// [air, fluid, non-solid] channels from flag codes
+__global__ void k_flags_to_image(const uint8_t *__restrict__ flags, float *__restrict__ img, int64_t n) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const uint8_t f = flags[q];
+  img[q] = f == MLPCG_AIR ? 1.f : 0.f;
+  img[n + q] = f == MLPCG_FLUID ? 1.f : 0.f;
+  img[2 * n + q] = f > MLPCG_SOLID ? 1.f : 0.f;
+}
+
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
+int launch_flags_to_image(const uint8_t *flags, float *img, int64_t n, cudaStream_t st) {
+  k_flags_to_image<<<blocks_for(n, 256), 256, 0, st>>>(flags, img, n);
+  MLPCG_LAUNCH_CHECK();
+  return MLPCG_OK;
+}
+
 #define MLPCG_DISPATCH_DT(dt, T, ...)                                   \
   do {                                                                  \
     if ((dt) == MLPCG_F32) { using T = float; __VA_ARGS__; }            \

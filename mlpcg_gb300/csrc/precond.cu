@@ -1,0 +1,604 @@
+// Preconditioner plan: every block's coefficients precomputed once per
+// (image, weights), applied by fused, tiled, bandwidth-bound kernels.
+//
+// SmallSMModelDn3D.eval_forward (sm_model_3d.py:180-262) on one rhs becomes
+// 2n+1 launches:
+//   pre_l   y_l = B_pre_l(x_l)          fused with x_{l+1} = avg_pool(y_l)
+//   l       x_n = B_l(x_n)
+//   post_l  x_l = c0_l y_l + c1_l B_post_l(up(x_{l+1}))   (prolongation + combine fused)
+// (or, with swap_sm_order, x_l = B_post_l(c0_l y_l + c1_l up(x_{l+1}))).
+// Levels whose z size is not a multiple of 8 use the general kernels of
+// stencil.cu / gridops.cu instead.
+//
+// Tile: 2 (x) x 16 (y) x 64 (z) outputs per 128-thread CTA; each thread owns
+// a run of 8 consecutive z cells in 2 x-planes.  The input with its one-cell
+// halo is staged in shared memory (4 x 18 x 66 floats); coefficients stream
+// from HBM as 16-byte vectors (8 BF16 or 4 FP32 values) with the
+// cache-streaming hint, since each is read exactly once per application.
+#include <vector>
+#include "common.cuh"
+
+namespace mlpcg {
+
+constexpr int TZ = 64, TY = 16, TX = 2;
+constexpr int ZT = 8;                 // threads along z, 8 cells each
+constexpr int PT = ZT * TY;           // 128 threads
+constexpr int HZ = TZ + 2, HY = TY + 2, HX = TX + 2;
+constexpr int CZ = TZ / 2 + 2, CY = TY / 2 + 2, CX = TX / 2 + 2;
+
+// ---- 8-wide vector access --------------------------------------------------
+__device__ __forceinline__ void ld8cs(const float *p, float v[8]) {
+  const float4 a = __ldcs(reinterpret_cast<const float4 *>(p));
+  const float4 b = __ldcs(reinterpret_cast<const float4 *>(p) + 1);
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+__device__ __forceinline__ void unpack_bf16x2(uint32_t u, float &lo, float &hi) {
+  lo = __uint_as_float(u << 16);
+  hi = __uint_as_float(u & 0xffff0000u);
+}
+__device__ __forceinline__ void ld8cs(const __nv_bfloat16 *p, float v[8]) {
+  const uint4 u = __ldcs(reinterpret_cast<const uint4 *>(p));
+  unpack_bf16x2(u.x, v[0], v[1]); unpack_bf16x2(u.y, v[2], v[3]);
+  unpack_bf16x2(u.z, v[4], v[5]); unpack_bf16x2(u.w, v[6], v[7]);
+}
+__device__ __forceinline__ void ld8(const float *p, float v[8]) {
+  const float4 a = __ldg(reinterpret_cast<const float4 *>(p));
+  const float4 b = __ldg(reinterpret_cast<const float4 *>(p) + 1);
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+__device__ __forceinline__ void ld8(const __nv_bfloat16 *p, float v[8]) {
+  const uint4 u = __ldg(reinterpret_cast<const uint4 *>(p));
+  unpack_bf16x2(u.x, v[0], v[1]); unpack_bf16x2(u.y, v[2], v[3]);
+  unpack_bf16x2(u.z, v[4], v[5]); unpack_bf16x2(u.w, v[6], v[7]);
+}
+__device__ __forceinline__ void st8(float *p, const float v[8]) {
+  reinterpret_cast<float4 *>(p)[0] = make_float4(v[0], v[1], v[2], v[3]);
+  reinterpret_cast<float4 *>(p)[1] = make_float4(v[4], v[5], v[6], v[7]);
+}
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t *>(&h);
+}
+__device__ __forceinline__ void st8(__nv_bfloat16 *p, const float v[8]) {
+  uint4 u;
+  u.x = pack_bf16x2(v[0], v[1]); u.y = pack_bf16x2(v[2], v[3]);
+  u.z = pack_bf16x2(v[4], v[5]); u.w = pack_bf16x2(v[6], v[7]);
+  *reinterpret_cast<uint4 *>(p) = u;
+}
+__device__ __forceinline__ void st4(float *p, const float v[4]) {
+  *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ __forceinline__ void st4(__nv_bfloat16 *p, const float v[4]) {
+  uint2 u;
+  u.x = pack_bf16x2(v[0], v[1]);
+  u.y = pack_bf16x2(v[2], v[3]);
+  *reinterpret_cast<uint2 *>(p) = u;
+}
+
+// 27-tap application of one 8-cell run from the staged tile.
+// S is the (HX, HY, HZ) tile, (tx, ty, tz8) the run's position in the tile.
+template <typename KT>
+__device__ __forceinline__ void apply_run(const float (*S)[HY][HZ], int tx, int ty, int tz8,
+                                          const KT *__restrict__ K, int64_t ps, int64_t q,
+                                          float acc[8]) {
+#pragma unroll
+  for (int c = 0; c < 8; ++c) acc[c] = 0.f;
+#pragma unroll
+  for (int dx = 0; dx < 3; ++dx)
+#pragma unroll
+    for (int dy = 0; dy < 3; ++dy) {
+      float xr[10];
+      const float *row = &S[tx + dx][ty + dy][tz8];
+#pragma unroll
+      for (int c = 0; c < 10; ++c) xr[c] = row[c];
+#pragma unroll
+      for (int dz = 0; dz < 3; ++dz) {
+        const int p = dx * 9 + dy * 3 + dz;  // the reference's tap order
+        float kv[8];
+        ld8cs(K + p * ps + q, kv);
+#pragma unroll
+        for (int c = 0; c < 8; ++c) acc[c] = fmaf(kv[c], xr[c + dz], acc[c]);
+      }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// pre-block (and the coarsest l-block): y = B(x), optional fused avg-pool
+// ---------------------------------------------------------------------------
+template <typename KT, typename XT, typename YT, bool POOL>
+__global__ void __launch_bounds__(PT)
+k_pre_fused(const KT *__restrict__ K, int64_t ps, const XT *__restrict__ x,
+            const float *__restrict__ xscale, YT *__restrict__ y, YT *__restrict__ ypool,
+            const uint8_t *__restrict__ mask, int n1, int n2, int n3) {
+  __shared__ float S[HX][HY][HZ];
+  const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY, x0 = blockIdx.z * TX;
+  const float sc = xscale ? __ldg(xscale) : 1.f;
+  for (int e = threadIdx.x; e < HX * HY * HZ; e += PT) {
+    const int hz = e % HZ, t = e / HZ, hy = t % HY, hx = t / HY;
+    const int i = x0 + hx - 1, j = y0 + hy - 1, k = z0 + hz - 1;
+    float v = 0.f;
+    if ((unsigned)i < (unsigned)n1 && (unsigned)j < (unsigned)n2 && (unsigned)k < (unsigned)n3)
+      v = ldf(x + ((int64_t)i * n2 + j) * n3 + k) * sc;
+    S[hx][hy][hz] = v;
+  }
+  __syncthreads();
+  const int tz = threadIdx.x % ZT, ty = threadIdx.x / ZT;
+  const int k0 = z0 + tz * 8, j = y0 + ty;
+  const bool active = k0 < n3 && j < n2;  // n3 % 8 == 0: a run is all in or all out
+  float pool[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+  for (int tx = 0; tx < TX; ++tx) {
+    const int i = x0 + tx;
+    if (!active || i >= n1) continue;
+    const int64_t q = ((int64_t)i * n2 + j) * n3 + k0;
+    float acc[8];
+    apply_run<KT>(S, tx, ty, tz * 8, K, ps, q, acc);
+    if (mask) {
+      const uint2 m = __ldg(reinterpret_cast<const uint2 *>(mask + q));
+#pragma unroll
+      for (int c = 0; c < 8; ++c)
+        if (!((c < 4 ? (m.x >> (8 * c)) : (m.y >> (8 * (c - 4)))) & 0xffu)) acc[c] = 0.f;
+    }
+    st8(y + q, acc);
+    if (POOL) {
+#pragma unroll
+      for (int c = 0; c < 4; ++c) pool[c] += acc[2 * c] + acc[2 * c + 1];
+    }
+  }
+  if (POOL) {
+#pragma unroll
+    for (int c = 0; c < 4; ++c) pool[c] += __shfl_xor_sync(0xffffffffu, pool[c], ZT);
+    if (active && (ty & 1) == 0) {
+      const int m2 = n2 / 2, m3 = n3 / 2;
+      const int64_t qc = ((int64_t)(x0 / 2) * m2 + j / 2) * m3 + k0 / 2;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) pool[c] *= 0.125f;
+      st4(ypool + qc, pool);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// post-block with fused trilinear prolongation and level combine
+// ---------------------------------------------------------------------------
+struct Lin1 { int i0, i1; float l0, l1; };
+__device__ __forceinline__ Lin1 lin1(int f, int n) {
+  float src = 0.5f * ((float)f + 0.5f) - 0.5f;
+  if (src < 0.f) src = 0.f;
+  Lin1 r;
+  r.i0 = (int)src;
+  r.i1 = r.i0 + (r.i0 < n - 1 ? 1 : 0);
+  r.l1 = src - (float)r.i0;
+  r.l0 = 1.f - r.l1;
+  return r;
+}
+
+template <typename KT, typename CT, typename YT, typename OT, bool SWAP>
+__global__ void __launch_bounds__(PT)
+k_post_fused(const KT *__restrict__ K, int64_t ps, const CT *__restrict__ xc, const YT *__restrict__ yl,
+             const float *__restrict__ c0p, const float *__restrict__ c1p, OT *__restrict__ out,
+             const uint8_t *__restrict__ bmask, const uint8_t *__restrict__ omask, int n1, int n2, int n3) {
+  __shared__ float S[HX][HY][HZ];
+  __shared__ float Cs[CX][CY][CZ];
+  const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY, x0 = blockIdx.z * TX;
+  const int m1 = n1 / 2, m2 = n2 / 2, m3 = n3 / 2;
+  const int cx0 = x0 / 2 - 1, cy0 = y0 / 2 - 1, cz0 = z0 / 2 - 1;
+  const float c0 = __ldg(c0p), c1 = __ldg(c1p);
+  for (int e = threadIdx.x; e < CX * CY * CZ; e += PT) {
+    const int cz = e % CZ, t = e / CZ, cy = t % CY, cx = t / CY;
+    const int i = cx0 + cx, j = cy0 + cy, k = cz0 + cz;
+    float v = 0.f;
+    if ((unsigned)i < (unsigned)m1 && (unsigned)j < (unsigned)m2 && (unsigned)k < (unsigned)m3)
+      v = ldf(xc + ((int64_t)i * m2 + j) * m3 + k);
+    Cs[cx][cy][cz] = v;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < HX * HY * HZ; e += PT) {
+    const int hz = e % HZ, t = e / HZ, hy = t % HY, hx = t / HY;
+    const int i = x0 + hx - 1, j = y0 + hy - 1, k = z0 + hz - 1;
+    float v = 0.f;
+    if ((unsigned)i < (unsigned)n1 && (unsigned)j < (unsigned)n2 && (unsigned)k < (unsigned)n3) {
+      const Lin1 a = lin1(i, m1), b = lin1(j, m2), c = lin1(k, m3);
+      const int a0 = a.i0 - cx0, a1 = a.i1 - cx0, b0 = b.i0 - cy0, b1 = b.i1 - cy0;
+      const int e0 = c.i0 - cz0, e1 = c.i1 - cz0;
+      v = a.l0 * (b.l0 * (c.l0 * Cs[a0][b0][e0] + c.l1 * Cs[a0][b0][e1]) +
+                  b.l1 * (c.l0 * Cs[a0][b1][e0] + c.l1 * Cs[a0][b1][e1])) +
+          a.l1 * (b.l0 * (c.l0 * Cs[a1][b0][e0] + c.l1 * Cs[a1][b0][e1]) +
+                  b.l1 * (c.l0 * Cs[a1][b1][e0] + c.l1 * Cs[a1][b1][e1]));
+      if (SWAP) v = __fadd_rn(__fmul_rn(c0, ldf(yl + ((int64_t)i * n2 + j) * n3 + k)), __fmul_rn(c1, v));
+    }
+    S[hx][hy][hz] = v;
+  }
+  __syncthreads();
+  const int tz = threadIdx.x % ZT, ty = threadIdx.x / ZT;
+  const int k0 = z0 + tz * 8, j = y0 + ty;
+  if (k0 >= n3 || j >= n2) return;
+#pragma unroll
+  for (int tx = 0; tx < TX; ++tx) {
+    const int i = x0 + tx;
+    if (i >= n1) continue;
+    const int64_t q = ((int64_t)i * n2 + j) * n3 + k0;
+    float acc[8];
+    apply_run<KT>(S, tx, ty, tz * 8, K, ps, q, acc);
+    if (bmask) {
+      const uint2 m = __ldg(reinterpret_cast<const uint2 *>(bmask + q));
+#pragma unroll
+      for (int c = 0; c < 8; ++c)
+        if (!((c < 4 ? (m.x >> (8 * c)) : (m.y >> (8 * (c - 4)))) & 0xffu)) acc[c] = 0.f;
+    }
+    if (!SWAP) {
+      float yv[8];
+      ld8(yl + q, yv);
+#pragma unroll
+      for (int c = 0; c < 8; ++c) acc[c] = __fadd_rn(__fmul_rn(c0, yv[c]), __fmul_rn(c1, acc[c]));
+    }
+    if (omask) {
+      const uint2 m = __ldg(reinterpret_cast<const uint2 *>(omask + q));
+#pragma unroll
+      for (int c = 0; c < 8; ++c)
+        if (!((c < 4 ? (m.x >> (8 * c)) : (m.y >> (8 * (c - 4)))) & 0xffu)) acc[c] = 0.f;
+    }
+    st8(out + q, acc);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// small helpers for the general (ragged-size) path and the plan setup
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_scale_copy(const float *__restrict__ x, const float *__restrict__ s, T *__restrict__ y, int64_t n) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  stf(y + q, x[q] * (s ? s[0] : 1.f));
+}
+
+template <typename T>
+__global__ void k_apply_mask(T *__restrict__ y, const uint8_t *__restrict__ m, int64_t n) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  if (!m[q]) stf(y + q, 0.f);
+}
+
+template <typename TI, typename TO>
+__global__ void k_convert(const TI *__restrict__ x, TO *__restrict__ y, int64_t n) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  stf(y + q, ldf(x + q));
+}
+
+__global__ void k_fluid_mask(const float *__restrict__ img, uint8_t *__restrict__ m, int64_t n) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  m[q] = img[n + q] != 0.f;  // channel 1 = fluid (the reference masks with image[1] == 0)
+}
+
+// ---------------------------------------------------------------------------
+// the plan object (host side; all device memory is the caller's workspace)
+// ---------------------------------------------------------------------------
+int launch_stencil_gen(const float *, int, int, int, int, const float *, const float *, void *, int,
+                       int64_t, cudaStream_t);
+int launch_stencil_apply(const void *, int, int64_t, const void *, int, int, void *, int, int, int,
+                         int, int, int, cudaStream_t);
+int launch_avg_pool2(const void *, void *, int, int, int, int, int, cudaStream_t);
+int launch_upsample2(const void *, void *, int, int, int, int, int, cudaStream_t);
+int launch_axpby(const float *, const void *, const float *, const void *, void *, int, int64_t,
+                 cudaStream_t);
+int launch_linear_forward(const float *, int, int, int, const float *, const float *, int, float *,
+                          float *, void *, size_t, cudaStream_t);
+size_t linear_workspace();
+
+struct PrecondPlan {
+  int n1, n2, n3, L;          // fine sizes, number of levels n (blocks at levels 0..L)
+  int kdt, adt;               // coefficient / activation storage dtypes
+  int swap, mask;
+  struct Level { int n1, n2, n3; int64_t n, ps; bool fast; };
+  std::vector<Level> lv;      // L + 1 levels
+  // device pointers (inside the caller's workspace)
+  std::vector<float *> img;   // level images, [0] unused (caller's image)
+  std::vector<void *> Kpre, Kpost;
+  void *Kl = nullptr;
+  std::vector<void *> y, xin, xout;  // y_l (pre out), x_l inputs (l >= 1), post outputs (l >= 1)
+  float *coef = nullptr;      // c0[0..L-1], c1[0..L-1]
+  uint8_t *fmask = nullptr;   // fluid mask of level 0
+  void *lin_ws = nullptr;
+  float *scratch = nullptr;   // 81 floats (linear means)
+  size_t bytes = 0;
+  bool ready = false;
+};
+
+static size_t al256(size_t b) { return (b + 255) / 256 * 256; }
+
+static size_t plan_layout(PrecondPlan &P, char *base) {
+  size_t off = 0;
+  auto take = [&](size_t b) -> void * {
+    void *p = base ? base + off : nullptr;
+    off += al256(b);
+    return p;
+  };
+  const size_t sk = dtype_size(P.kdt), sa = dtype_size(P.adt);
+  P.img.assign(P.L + 1, nullptr);
+  P.Kpre.assign(P.L, nullptr);
+  P.Kpost.assign(P.L, nullptr);
+  P.y.assign(P.L, nullptr);
+  P.xin.assign(P.L + 1, nullptr);
+  P.xout.assign(P.L + 1, nullptr);
+  for (int l = 1; l <= P.L; ++l) P.img[l] = (float *)take(3 * P.lv[l].n * sizeof(float));
+  for (int l = 0; l < P.L; ++l) {
+    P.Kpre[l] = take(27 * P.lv[l].ps * sk);
+    P.Kpost[l] = take(27 * P.lv[l].ps * sk);
+  }
+  P.Kl = take(27 * P.lv[P.L].ps * sk);
+  for (int l = 0; l < P.L; ++l) P.y[l] = take(P.lv[l].ps * sa);
+  for (int l = 1; l <= P.L; ++l) {
+    P.xin[l] = take(P.lv[l].ps * sa);
+    P.xout[l] = take(P.lv[l].ps * sa);
+  }
+  P.coef = (float *)take(2 * P.L * sizeof(float));
+  P.fmask = (uint8_t *)take(P.lv[0].ps + 64);
+  P.lin_ws = take(linear_workspace());
+  P.scratch = (float *)take(96 * sizeof(float));
+  // scratch for the general path: level-0 scaled input and one activation-sized temp
+  return off;
+}
+
+}  // namespace mlpcg
+
+using namespace mlpcg;
+
+typedef struct mlpcg_precond mlpcg_precond;
+struct mlpcg_precond { PrecondPlan p; };
+
+#define RET_IF(expr) do { int _r = (expr); if (_r != MLPCG_OK) return _r; } while (0)
+
+// launch helpers for the fast kernels ------------------------------------------
+// Stages of one application, in launch order: 0..L-1 = pre-block of level s,
+// L = coarsest block, L+1..2L = post-block of level 2L-s.  [s0, s1] selects a range.
+template <typename KT, typename AT>
+static int run_apply(const PrecondPlan &P, const float *r, const float *rscale, float *z, void *tmp0,
+                     cudaStream_t st, int s0 = 0, int s1 = 1 << 20) {
+  const int L = P.L;
+  auto grid_of = [](const PrecondPlan::Level &v) {
+    return dim3((unsigned)((v.n3 + TZ - 1) / TZ), (unsigned)((v.n2 + TY - 1) / TY), (unsigned)((v.n1 + TX - 1) / TX));
+  };
+  const uint8_t *m0 = P.mask ? P.fmask : nullptr;
+  // ---- down sweep
+  for (int l = 0; l < L; ++l) {
+    const auto &v = P.lv[l];
+    if (l < s0 || l > s1) continue;
+    if (v.fast) {
+      if (l == 0)
+        k_pre_fused<KT, float, AT, true><<<grid_of(v), PT, 0, st>>>(
+            (const KT *)P.Kpre[0], v.ps, r, rscale, (AT *)P.y[0], (AT *)P.xin[1], m0, v.n1, v.n2, v.n3);
+      else
+        k_pre_fused<KT, AT, AT, true><<<grid_of(v), PT, 0, st>>>(
+            (const KT *)P.Kpre[l], v.ps, (const AT *)P.xin[l], nullptr, (AT *)P.y[l], (AT *)P.xin[l + 1],
+            nullptr, v.n1, v.n2, v.n3);
+      MLPCG_LAUNCH_CHECK();
+    } else {
+      const void *src = P.xin[l];
+      int sdt = P.adt;
+      if (l == 0) {
+        k_scale_copy<AT><<<blocks_for(v.n, 256), 256, 0, st>>>(r, rscale, (AT *)tmp0, v.n);
+        MLPCG_LAUNCH_CHECK();
+        src = tmp0;
+      }
+      RET_IF(launch_stencil_apply(P.Kpre[l], P.kdt, v.ps, src, sdt, 0, P.y[l], P.adt, 1, v.n1, v.n2, v.n3, 0, st));
+      if (l == 0 && m0) {
+        k_apply_mask<AT><<<blocks_for(v.n, 256), 256, 0, st>>>((AT *)P.y[0], m0, v.n);
+        MLPCG_LAUNCH_CHECK();
+      }
+      RET_IF(launch_avg_pool2(P.y[l], P.xin[l + 1], P.adt, 1, v.n1, v.n2, v.n3, st));
+    }
+  }
+  // ---- coarsest block
+  if (L >= s0 && L <= s1) {
+    const auto &v = P.lv[L];
+    if (v.fast) {
+      k_pre_fused<KT, AT, AT, false><<<grid_of(v), PT, 0, st>>>(
+          (const KT *)P.Kl, v.ps, (const AT *)P.xin[L], nullptr, (AT *)P.xout[L], nullptr, nullptr, v.n1, v.n2, v.n3);
+      MLPCG_LAUNCH_CHECK();
+    } else {
+      RET_IF(launch_stencil_apply(P.Kl, P.kdt, v.ps, P.xin[L], P.adt, 0, P.xout[L], P.adt, 1, v.n1, v.n2, v.n3, 0, st));
+    }
+  }
+  // ---- up sweep
+  for (int l = L - 1; l >= 0; --l) {
+    const auto &v = P.lv[l];
+    if (2 * L - l < s0 || 2 * L - l > s1) continue;
+    const float *c0 = P.coef + l, *c1 = P.coef + L + l;
+    const uint8_t *bm = (l == 0) ? m0 : nullptr;
+    const uint8_t *om = (l == 0) ? P.fmask : nullptr;
+    if (v.fast) {
+      if (l == 0) {
+        if (P.swap)
+          k_post_fused<KT, AT, AT, float, true><<<grid_of(v), PT, 0, st>>>(
+              (const KT *)P.Kpost[0], v.ps, (const AT *)P.xout[1], (const AT *)P.y[0], c0, c1, z, bm, om, v.n1, v.n2, v.n3);
+        else
+          k_post_fused<KT, AT, AT, float, false><<<grid_of(v), PT, 0, st>>>(
+              (const KT *)P.Kpost[0], v.ps, (const AT *)P.xout[1], (const AT *)P.y[0], c0, c1, z, bm, om, v.n1, v.n2, v.n3);
+      } else {
+        if (P.swap)
+          k_post_fused<KT, AT, AT, AT, true><<<grid_of(v), PT, 0, st>>>(
+              (const KT *)P.Kpost[l], v.ps, (const AT *)P.xout[l + 1], (const AT *)P.y[l], c0, c1, (AT *)P.xout[l],
+              nullptr, nullptr, v.n1, v.n2, v.n3);
+        else
+          k_post_fused<KT, AT, AT, AT, false><<<grid_of(v), PT, 0, st>>>(
+              (const KT *)P.Kpost[l], v.ps, (const AT *)P.xout[l + 1], (const AT *)P.y[l], c0, c1, (AT *)P.xout[l],
+              nullptr, nullptr, v.n1, v.n2, v.n3);
+      }
+      MLPCG_LAUNCH_CHECK();
+    } else {
+      // general path: up -> (combine) -> block -> (combine) with level-sized temporaries
+      void *up = tmp0;                                   // level-l sized, activation dtype
+      void *dst = (l == 0) ? (void *)z : P.xout[l];
+      const int ddt = (l == 0) ? MLPCG_F32 : P.adt;
+      RET_IF(launch_upsample2(P.xout[l + 1], up, P.adt, 1, v.n1 / 2, v.n2 / 2, v.n3 / 2, st));
+      if (P.swap) {
+        RET_IF(launch_axpby(c0, P.y[l], c1, up, up, P.adt, v.n, st));
+        RET_IF(launch_stencil_apply(P.Kpost[l], P.kdt, v.ps, up, P.adt, 0, dst, ddt, 1, v.n1, v.n2, v.n3, 0, st));
+        if (bm) {
+          k_apply_mask<float><<<blocks_for(v.n, 256), 256, 0, st>>>((float *)dst, bm, v.n);
+          MLPCG_LAUNCH_CHECK();
+        }
+      } else {
+        // t = B(up) into up's slot via dst, then combine into dst
+        RET_IF(launch_stencil_apply(P.Kpost[l], P.kdt, v.ps, up, P.adt, 0, dst, ddt, 1, v.n1, v.n2, v.n3, 0, st));
+        if (l == 0) {
+          if (bm) {
+            k_apply_mask<float><<<blocks_for(v.n, 256), 256, 0, st>>>((float *)dst, bm, v.n);
+            MLPCG_LAUNCH_CHECK();
+          }
+          // y0 (activation dtype) -> F32 copy in tmp, then z = c0*y0 + c1*t
+          k_convert<AT, float><<<blocks_for(v.n, 256), 256, 0, st>>>((const AT *)P.y[0], (float *)up, v.n);
+          MLPCG_LAUNCH_CHECK();
+          RET_IF(launch_axpby(c0, up, c1, dst, dst, MLPCG_F32, v.n, st));
+        } else {
+          RET_IF(launch_axpby(c0, P.y[l], c1, dst, dst, P.adt, v.n, st));
+        }
+      }
+      if (l == 0) {
+        k_apply_mask<float><<<blocks_for(v.n, 256), 256, 0, st>>>((float *)dst, P.fmask, v.n);
+        MLPCG_LAUNCH_CHECK();
+      }
+    }
+  }
+  return MLPCG_OK;
+}
+
+extern "C" {
+
+int mlpcg_precond_create(int N1, int N2, int N3, int levels, int k_dtype, int act_dtype,
+                         int swap_sm_order, int mask, mlpcg_precond **out) {
+  clear_error();
+  MLPCG_REQUIRE(out != nullptr, MLPCG_ERR_ARG, "out must not be NULL");
+  *out = nullptr;
+  MLPCG_REQUIRE(levels >= 1 && levels <= 12, MLPCG_ERR_ARG, "levels %d out of [1, 12]", levels);
+  MLPCG_REQUIRE(N1 >= 1 && N2 >= 1 && N3 >= 1, MLPCG_ERR_SHAPE, "grid sizes must be >= 1");
+  const int f = 1 << levels;
+  MLPCG_REQUIRE(N1 % f == 0 && N2 % f == 0 && N3 % f == 0, MLPCG_ERR_SHAPE,
+                "grid %d x %d x %d must be divisible by 2^levels = %d", N1, N2, N3, f);
+  MLPCG_REQUIRE((k_dtype == MLPCG_F32 || k_dtype == MLPCG_BF16) && (act_dtype == MLPCG_F32 || act_dtype == MLPCG_BF16),
+                MLPCG_ERR_UNSUPPORTED, "coefficient / activation storage must be F32 or BF16");
+  auto *h = new mlpcg_precond();
+  PrecondPlan &P = h->p;
+  P.n1 = N1; P.n2 = N2; P.n3 = N3; P.L = levels;
+  P.kdt = k_dtype; P.adt = act_dtype; P.swap = swap_sm_order ? 1 : 0; P.mask = mask ? 1 : 0;
+  for (int l = 0; l <= levels; ++l) {
+    PrecondPlan::Level v;
+    v.n1 = N1 >> l; v.n2 = N2 >> l; v.n3 = N3 >> l;
+    v.n = cells(v.n1, v.n2, v.n3);
+    v.ps = (v.n + 63) / 64 * 64;
+    v.fast = (v.n3 % 8 == 0);
+    P.lv.push_back(v);
+  }
+  P.bytes = plan_layout(P, nullptr);
+  // temporaries of the general path: level-0 sized activation + F32 buffer
+  P.bytes += al256(P.lv[0].ps * 4);
+  *out = h;
+  return MLPCG_OK;
+}
+
+size_t mlpcg_precond_workspace(const mlpcg_precond *h) { return h ? h->p.bytes : 0; }
+
+void mlpcg_precond_destroy(mlpcg_precond *h) { delete h; }
+
+int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_bytes, const float *image,
+                        const float *params, void *stream) {
+  clear_error();
+  MLPCG_REQUIRE(h && workspace && image && params, MLPCG_ERR_ARG, "precond_setup: NULL argument");
+  PrecondPlan &P = h->p;
+  MLPCG_REQUIRE(workspace_bytes >= P.bytes, MLPCG_ERR_WORKSPACE, "precond workspace too small: %zu < %zu",
+                workspace_bytes, P.bytes);
+  MLPCG_REQUIRE(((uintptr_t)workspace & 255) == 0, MLPCG_ERR_ALIGN, "precond workspace must be 256-byte aligned");
+  cudaStream_t st = as_stream(stream);
+  plan_layout(P, (char *)workspace);
+  const int L = P.L;
+  // parameter offsets: pre[0..L-1], post[0..L-1], l (2214 each), c0[0..L-1], c1[0..L-1] (82 each)
+  auto blk_w = [&](int b) { return params + (size_t)b * 2214; };
+  auto blk_b = [&](int b) { return params + (size_t)b * 2214 + 2187; };
+  const float *linp = params + (size_t)(2 * L + 1) * 2214;
+  // image pyramid
+  for (int l = 1; l <= L; ++l) {
+    const auto &v = P.lv[l - 1];
+    const float *src = (l == 1) ? image : P.img[l - 1];
+    RET_IF(launch_avg_pool2(src, P.img[l], MLPCG_F32, 3, v.n1, v.n2, v.n3, st));
+  }
+  k_fluid_mask<<<blocks_for(P.lv[0].n, 256), 256, 0, st>>>(image, P.fmask, P.lv[0].n);
+  MLPCG_LAUNCH_CHECK();
+  // coefficients
+  for (int l = 0; l < L; ++l) {
+    const auto &v = P.lv[l];
+    const float *im = (l == 0) ? image : P.img[l];
+    RET_IF(launch_stencil_gen(im, 0, v.n1, v.n2, v.n3, blk_w(l), blk_b(l), P.Kpre[l], P.kdt, v.ps, st));
+    RET_IF(launch_stencil_gen(im, 0, v.n1, v.n2, v.n3, blk_w(L + l), blk_b(L + l), P.Kpost[l], P.kdt, v.ps, st));
+  }
+  {
+    const auto &v = P.lv[L];
+    RET_IF(launch_stencil_gen(P.img[L], 0, v.n1, v.n2, v.n3, blk_w(2 * L), blk_b(2 * L), P.Kl, P.kdt, v.ps, st));
+  }
+  // c0 / c1 of every level (the linear blocks of sm_model_3d.py:236-239)
+  for (int l = 0; l < L; ++l) {
+    const auto &v = P.lv[l];
+    const float *im = (l == 0) ? image : P.img[l];
+    const float *w0 = linp + (size_t)l * 82, *w1 = linp + (size_t)(L + l) * 82;
+    RET_IF(launch_linear_forward(im, v.n1, v.n2, v.n3, w0, w0 + 81, 1, P.coef + l, nullptr, P.lin_ws,
+                                 linear_workspace(), st));
+    RET_IF(launch_linear_forward(im, v.n1, v.n2, v.n3, w1, w1 + 81, 1, P.coef + L + l, nullptr, P.lin_ws,
+                                 linear_workspace(), st));
+  }
+  P.ready = true;
+  return MLPCG_OK;
+}
+
+int mlpcg_precond_apply(const mlpcg_precond *h, const float *r, const float *r_scale, float *z, void *stream) {
+  clear_error();
+  MLPCG_REQUIRE(h && r && z, MLPCG_ERR_ARG, "precond_apply: NULL argument");
+  const PrecondPlan &P = h->p;
+  MLPCG_REQUIRE(P.ready, MLPCG_ERR_ARG, "precond_apply: plan not set up");
+  MLPCG_REQUIRE(((uintptr_t)r & 15) == 0 && ((uintptr_t)z & 31) == 0, MLPCG_ERR_ALIGN,
+                "precond_apply: r must be 16-byte and z 32-byte aligned");
+  cudaStream_t st = as_stream(stream);
+  void *tmp0 = (char *)P.scratch + al256(96 * sizeof(float));
+  if (P.kdt == MLPCG_BF16 && P.adt == MLPCG_BF16) return run_apply<__nv_bfloat16, __nv_bfloat16>(P, r, r_scale, z, tmp0, st);
+  if (P.kdt == MLPCG_BF16 && P.adt == MLPCG_F32) return run_apply<__nv_bfloat16, float>(P, r, r_scale, z, tmp0, st);
+  if (P.kdt == MLPCG_F32 && P.adt == MLPCG_BF16) return run_apply<float, __nv_bfloat16>(P, r, r_scale, z, tmp0, st);
+  return run_apply<float, float>(P, r, r_scale, z, tmp0, st);
+}
+
+int mlpcg_precond_apply_stages(const mlpcg_precond *h, int first, int last, const float *r, const float *r_scale,
+                               float *z, void *stream) {
+  clear_error();
+  MLPCG_REQUIRE(h && r && z, MLPCG_ERR_ARG, "precond_apply_stages: NULL argument");
+  const PrecondPlan &P = h->p;
+  MLPCG_REQUIRE(P.ready, MLPCG_ERR_ARG, "precond_apply_stages: plan not set up");
+  MLPCG_REQUIRE(first >= 0 && last <= 2 * P.L && first <= last, MLPCG_ERR_ARG,
+                "precond_apply_stages: stage range [%d, %d] outside [0, %d]", first, last, 2 * P.L);
+  cudaStream_t st = as_stream(stream);
+  void *tmp0 = (char *)P.scratch + al256(96 * sizeof(float));
+  if (P.kdt == MLPCG_BF16 && P.adt == MLPCG_BF16)
+    return run_apply<__nv_bfloat16, __nv_bfloat16>(P, r, r_scale, z, tmp0, st, first, last);
+  if (P.kdt == MLPCG_BF16 && P.adt == MLPCG_F32) return run_apply<__nv_bfloat16, float>(P, r, r_scale, z, tmp0, st, first, last);
+  if (P.kdt == MLPCG_F32 && P.adt == MLPCG_BF16) return run_apply<float, __nv_bfloat16>(P, r, r_scale, z, tmp0, st, first, last);
+  return run_apply<float, float>(P, r, r_scale, z, tmp0, st, first, last);
+}
+
+int mlpcg_precond_level_info(const mlpcg_precond *h, int level, int *n1, int *n2, int *n3, int *fast) {
+  clear_error();
+  MLPCG_REQUIRE(h && level >= 0 && level <= h->p.L, MLPCG_ERR_ARG, "precond_level_info: bad level");
+  const auto &v = h->p.lv[level];
+  if (n1) *n1 = v.n1;
+  if (n2) *n2 = v.n2;
+  if (n3) *n3 = v.n3;
+  if (fast) *fast = v.fast ? 1 : 0;
+  return MLPCG_OK;
+}
+
+int mlpcg_precond_coefficients(const mlpcg_precond *h, float *c_out, void *stream) {
+  clear_error();
+  MLPCG_REQUIRE(h && c_out && h->p.ready, MLPCG_ERR_ARG, "precond_coefficients: bad argument");
+  MLPCG_CUDA_CHECK(cudaMemcpyAsync(c_out, h->p.coef, 2 * h->p.L * sizeof(float), cudaMemcpyDeviceToDevice,
+                                   as_stream(stream)));
+  return MLPCG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,610 @@
+// Fused neural-preconditioned solve: the whole iteration on the GPU inside one
+// CUDA graph whose conditional WHILE node loops until convergence, breakdown
+// or max_it -- no host synchronisation per iteration (the reference syncs on
+// .item() every iteration, cg_tests.py:90,266).
+//
+// Two iteration forms with the reference's recurrences:
+//   NPSD (cg_tests.py:189-284): q = M r, A-orthogonalised against the last two
+//        directions, x += (q.r / q.Aq) q.
+//   NPCG (cg_tests.py:26-101): textbook PCG with the network as M.
+// Precision: vectors r, z, p, Ap in FP32 on the full grid (zero off-fluid),
+// x and b in FP64, every dot product reduced in FP64 (FP32 per-thread runs,
+// FP64 across threads, fixed-order across blocks), the residual recomputed
+// as r = b - A x in FP64 every `true_every` iterations and before declaring
+// convergence (the reference recomputes it every iteration, cg_tests.py:83,260).
+//
+// Every reduction kernel ends with a "last block" step: block partials go to
+// scratch, the last block to finish (atomic ticket) sums them in block order
+// and updates the solver state.  Each loop iteration increments the
+// iteration counter unconditionally and the loop stops at max_it, so the
+// WHILE node always terminates.
+#include <vector>
+#include "common.cuh"
+
+struct mlpcg_precond;
+extern "C" int mlpcg_precond_apply(const mlpcg_precond *, const float *, const float *, float *, void *);
+
+namespace mlpcg {
+
+enum { ST_RUNNING = 0, ST_CONVERGED = 1, ST_MAXIT = 2, ST_BREAKDOWN = 3, ST_NONFINITE = 4 };
+enum { M_NPSD = 0, M_NPCG = 1 };
+
+constexpr int RT = 256;          // threads per reduction block
+constexpr int RB_MAX = 1216;     // blocks per reduction kernel (8 x 152 SMs)
+constexpr int NRED = 3;          // dot products per kernel at most
+
+struct State {
+  int it, status, need_true, head;    // head: ring slot of the most recent direction
+  int pp;                             // NPCG: index of the current p buffer
+  int max_it, true_every, method;
+  double tol, bb, rr, rr_true, rel;
+  double alpha[3];                    // NPSD: p_j . A p_j per ring slot
+  double e_last;                      // NPSD: p_recent . A p_previous
+  double c0, c1, beta, rz_old, rz;
+  float rscale;                       // 1/||r|| fed to the preconditioner
+  unsigned ticket[4];
+};
+
+struct Vecs {
+  const uint8_t *flags;
+  const double *b;
+  double *x;
+  float *r, *z;
+  float *p;        // 3 slots (NPSD ring) or 2 (NPCG ping-pong), n each
+  float *Ap;       // 3 slots (NPSD) or 1 (NPCG)
+  double *part;    // NRED * RB_MAX partial sums
+  double *hist;    // max_it + 1 relative residuals
+  State *st;
+  int n1, n2, n3;
+  int64_t n;
+  int nblk;
+};
+
+// ---- block reduction of NR values into partials, last block finalises ----
+template <int NR>
+__device__ __forceinline__ bool reduce_last(double (&v)[NR], const Vecs &V, int slot, double (&out)[NR]) {
+  __shared__ double red[NR][RT / 32];
+  __shared__ bool last;
+#pragma unroll
+  for (int r = 0; r < NR; ++r)
+    for (int o = 16; o > 0; o >>= 1) v[r] += __shfl_xor_sync(0xffffffffu, v[r], o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+#pragma unroll
+    for (int r = 0; r < NR; ++r) red[r][w] = v[r];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int r = 0; r < NR; ++r) {
+      double s = 0.0;
+      for (int ww = 0; ww < RT / 32; ++ww) s += red[r][ww];
+      V.part[r * RB_MAX + blockIdx.x] = s;
+    }
+    __threadfence();
+    const unsigned t = atomicAdd(&V.st->ticket[slot], 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return false;
+  // last block: fixed-order sum of the partials
+  __threadfence();
+#pragma unroll
+  for (int r = 0; r < NR; ++r) {
+    double s = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += RT) s += __ldcg(&V.part[r * RB_MAX + b]);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (l == 0) red[r][w] = s;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < NR; ++r) {
+    double s = 0.0;
+    for (int ww = 0; ww < RT / 32; ++ww) s += red[r][ww];
+    out[r] = s;
+  }
+  if (threadIdx.x == 0) V.st->ticket[slot] = 0u;
+  return true;
+}
+
+__device__ __forceinline__ int64_t gstride() { return (int64_t)gridDim.x * blockDim.x; }
+__device__ __forceinline__ int64_t gtid() { return (int64_t)blockIdx.x * blockDim.x + threadIdx.x; }
+
+// (A v)(q) for FLUID q (0 otherwise), v given as a functor of the cell index
+template <typename F>
+__device__ __forceinline__ float lap_at(const Vecs &V, int64_t q, F vat) {
+  if (V.flags[q] != MLPCG_FLUID) return 0.f;
+  const int k = (int)(q % V.n3);
+  const int64_t t = q / V.n3;
+  const int j = (int)(t % V.n2);
+  const int i = (int)(t / V.n2);
+  const int64_t sx = (int64_t)V.n2 * V.n3, sy = V.n3;
+  float off = 0.f;
+  int d = 0;
+  auto visit = [&](bool inside, int64_t nb) {
+    if (!inside) return;
+    const uint8_t f = V.flags[nb];
+    if (f == MLPCG_FLUID) { off += vat(nb); ++d; }
+    else if (f == MLPCG_AIR) { ++d; }
+  };
+  visit(i > 0, q - sx);
+  visit(j > 0, q - sy);
+  visit(k > 0, q - 1);
+  visit(k < V.n3 - 1, q + 1);
+  visit(j < V.n2 - 1, q + sy);
+  visit(i < V.n1 - 1, q + sx);
+  return (float)d * vat(q) - off;
+}
+
+__device__ __forceinline__ double lap_at_f64(const Vecs &V, int64_t q) {
+  if (V.flags[q] != MLPCG_FLUID) return 0.0;
+  const int k = (int)(q % V.n3);
+  const int64_t t = q / V.n3;
+  const int j = (int)(t % V.n2);
+  const int i = (int)(t / V.n2);
+  const int64_t sx = (int64_t)V.n2 * V.n3, sy = V.n3;
+  double off = 0.0;
+  int d = 0;
+  auto visit = [&](bool inside, int64_t nb) {
+    if (!inside) return;
+    const uint8_t f = V.flags[nb];
+    if (f == MLPCG_FLUID) { off += V.x[nb]; ++d; }
+    else if (f == MLPCG_AIR) { ++d; }
+  };
+  visit(i > 0, q - sx);
+  visit(j > 0, q - sy);
+  visit(k > 0, q - 1);
+  visit(k < V.n3 - 1, q + 1);
+  visit(j < V.n2 - 1, q + sy);
+  visit(i < V.n1 - 1, q + sx);
+  return (double)d * V.x[q] - off;
+}
+
+// ---------------------------------------------------------------------------
+// setup: state reset, then r = b - A x (FP64), bb = b.b, rr = r.r
+// ---------------------------------------------------------------------------
+__global__ void k_reset(State *st, int max_it, int true_every, int method, double tol) {
+  if (threadIdx.x != 0) return;
+  State S{};
+  S.max_it = max_it;
+  S.true_every = true_every;
+  S.method = method;
+  S.tol = tol;
+  *st = S;
+}
+
+__global__ void __launch_bounds__(RT) k_init(Vecs V) {
+  double v[2] = {0.0, 0.0};
+  for (int64_t q = gtid(); q < V.n; q += gstride()) {
+    const double bq = V.flags[q] == MLPCG_FLUID ? V.b[q] : 0.0;
+    const double rq = bq - lap_at_f64(V, q);
+    const float rf = (float)rq;
+    V.r[q] = rf;
+    v[0] += bq * bq;
+    v[1] += (double)rf * rf;
+  }
+  double o[2];
+  if (reduce_last<2>(v, V, 0, o) && threadIdx.x == 0) {
+    State &S = *V.st;
+    S.bb = o[0];
+    S.rr = o[1];
+    S.it = 0;
+    S.head = 2;
+    S.pp = 0;
+    S.need_true = 0;
+    if (!isfinite(o[0]) || !isfinite(o[1])) {
+      S.rel = o[1];
+      S.status = ST_NONFINITE;
+    } else {
+      S.rel = (o[0] > 0.0) ? sqrt(o[1] / o[0]) : 0.0;
+      S.status = (o[0] > 0.0 && S.rel >= S.tol) ? ST_RUNNING : ST_CONVERGED;
+    }
+    S.rscale = (o[1] > 0.0) ? (float)(1.0 / sqrt((double)(float)o[1])) : 1.f;
+    S.alpha[0] = S.alpha[1] = S.alpha[2] = 0.0;
+    S.e_last = 0.0;
+    S.beta = S.c0 = S.c1 = 0.0;
+    S.rz_old = 0.0;
+    V.hist[0] = S.rel;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// NPSD
+// ---------------------------------------------------------------------------
+// d1 = z . A p_recent, d0 = z . A p_previous  ->  c1, c0 of
+// q = z - c1 p_recent - c0 p_previous  (the two sequential projections of
+// cg_tests.py:226-233, with q.A p_previous expanded as d0 - c1 e_last).
+__global__ void __launch_bounds__(RT) k_sd_dots(Vecs V) {
+  const State &S = *V.st;
+  if (S.status != ST_RUNNING) return;
+  const int it = S.it;
+  if (it == 0) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) { V.st->c0 = 0.0; V.st->c1 = 0.0; }
+    return;
+  }
+  const int h = S.head, hp = (h + 2) % 3;
+  const float *A1 = V.Ap + (int64_t)h * V.n, *A0 = V.Ap + (int64_t)hp * V.n;
+  const bool two = it >= 2;
+  double v[2] = {0.0, 0.0};
+  float s1 = 0.f, s0 = 0.f;
+  int cnt = 0;
+  for (int64_t q = gtid(); q < V.n; q += gstride()) {
+    const float zq = V.z[q];
+    s1 = fmaf(zq, A1[q], s1);
+    if (two) s0 = fmaf(zq, A0[q], s0);
+    if (++cnt == 16) { v[0] += s1; v[1] += s0; s1 = s0 = 0.f; cnt = 0; }
+  }
+  v[0] += s1; v[1] += s0;
+  double o[2];
+  if (reduce_last<2>(v, V, 1, o) && threadIdx.x == 0) {
+    State &W = *V.st;
+    const double c1 = o[0] / W.alpha[h];
+    const double c0 = two ? (o[1] - c1 * W.e_last) / W.alpha[hp] : 0.0;
+    W.c1 = c1;
+    W.c0 = c0;
+  }
+}
+
+// q = z - c1 p_recent - c0 p_previous into the next ring slot
+__global__ void __launch_bounds__(RT) k_sd_qform(Vecs V) {
+  const State &S = *V.st;
+  if (S.status != ST_RUNNING) return;
+  const int h = S.head, hp = (h + 2) % 3, hn = (h + 1) % 3;
+  const float c1 = (float)S.c1, c0 = (float)S.c0;
+  const float *P1 = V.p + (int64_t)h * V.n, *P0 = V.p + (int64_t)hp * V.n;
+  float *Q = V.p + (int64_t)hn * V.n;
+  const int it = S.it;
+  for (int64_t q = gtid(); q < V.n; q += gstride()) {
+    float v = V.z[q];
+    if (it >= 1) v = fmaf(-c1, P1[q], v);
+    if (it >= 2) v = fmaf(-c0, P0[q], v);
+    Q[q] = v;
+  }
+}
+
+// Aq, alpha = q.Aq, q.r, e = Aq.p_recent; then beta = q.r / alpha
+__global__ void __launch_bounds__(RT) k_sd_spmv(Vecs V) {
+  const State &S = *V.st;
+  if (S.status != ST_RUNNING) return;
+  const int h = S.head, hn = (h + 1) % 3;
+  const float *Q = V.p + (int64_t)hn * V.n, *P1 = V.p + (int64_t)h * V.n;
+  float *AQ = V.Ap + (int64_t)hn * V.n;
+  const bool has_prev = S.it >= 1;
+  double v[3] = {0.0, 0.0, 0.0};
+  float s[3] = {0.f, 0.f, 0.f};
+  int cnt = 0;
+  for (int64_t q = gtid(); q < V.n; q += gstride()) {
+    const float aq = lap_at(V, q, [&](int64_t m) { return Q[m]; });
+    AQ[q] = aq;
+    const float qq = Q[q];
+    s[0] = fmaf(qq, aq, s[0]);
+    s[1] = fmaf(qq, V.r[q], s[1]);
+    if (has_prev) s[2] = fmaf(aq, P1[q], s[2]);
+    if (++cnt == 16) { v[0] += s[0]; v[1] += s[1]; v[2] += s[2]; s[0] = s[1] = s[2] = 0.f; cnt = 0; }
+  }
+  v[0] += s[0]; v[1] += s[1]; v[2] += s[2];
+  double o[3];
+  if (reduce_last<3>(v, V, 2, o) && threadIdx.x == 0) {
+    State &W = *V.st;
+    W.alpha[hn] = o[0];
+    W.e_last = o[2];
+    W.head = hn;
+    W.beta = o[1] / o[0];
+    if (!(o[0] > 0.0) || !isfinite(W.beta)) W.status = isfinite(o[0]) ? ST_BREAKDOWN : ST_NONFINITE;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// NPCG
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(RT) k_cg_rz(Vecs V) {
+  const State &S = *V.st;
+  if (S.status != ST_RUNNING) return;
+  double v[1] = {0.0};
+  float s = 0.f;
+  int cnt = 0;
+  for (int64_t q = gtid(); q < V.n; q += gstride()) {
+    s = fmaf(V.r[q], V.z[q], s);
+    if (++cnt == 16) { v[0] += s; s = 0.f; cnt = 0; }
+  }
+  v[0] += s;
+  double o[1];
+  if (reduce_last<1>(v, V, 1, o) && threadIdx.x == 0) {
+    State &W = *V.st;
+    W.rz = o[0];
+    W.c1 = (W.it == 0) ? 0.0 : o[0] / W.rz_old;  // beta of the p update
+    W.rz_old = o[0];
+  }
+}
+
+// p_new = z + beta p_old (ping-pong buffers), w = A p_new, pw = p_new . w, alpha = rz / pw
+__global__ void __launch_bounds__(RT) k_cg_pspmv(Vecs V) {
+  const State &S = *V.st;
+  if (S.status != ST_RUNNING) return;
+  const int cur = S.pp, nxt = cur ^ 1;
+  const float *Po = V.p + (int64_t)cur * V.n;
+  float *Pn = V.p + (int64_t)nxt * V.n;
+  const float bt = (float)S.c1;
+  const bool first = S.it == 0;
+  auto pnew = [&](int64_t m) { return first ? V.z[m] : fmaf(bt, Po[m], V.z[m]); };
+  double v[1] = {0.0};
+  float s = 0.f;
+  int cnt = 0;
+  for (int64_t q = gtid(); q < V.n; q += gstride()) {
+    const float pq = pnew(q);
+    Pn[q] = pq;
+    const float w = lap_at(V, q, pnew);
+    V.Ap[q] = w;
+    s = fmaf(pq, w, s);
+    if (++cnt == 16) { v[0] += s; s = 0.f; cnt = 0; }
+  }
+  v[0] += s;
+  double o[1];
+  if (reduce_last<1>(v, V, 2, o) && threadIdx.x == 0) {
+    State &W = *V.st;
+    W.pp = nxt;
+    W.beta = W.rz / o[0];  // the step length alpha of cg_tests.py:81
+    if (!isfinite(W.beta) || o[0] == 0.0) W.status = isfinite(o[0]) ? ST_BREAKDOWN : ST_NONFINITE;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// shared: x += beta d; r -= beta A d; rr = r.r; decide whether a true residual is due
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(RT) k_update(Vecs V) {
+  const State &S = *V.st;
+  if (S.status != ST_RUNNING) return;
+  const float *D, *AD;
+  if (S.method == M_NPSD) {
+    D = V.p + (int64_t)S.head * V.n;
+    AD = V.Ap + (int64_t)S.head * V.n;
+  } else {
+    D = V.p + (int64_t)S.pp * V.n;
+    AD = V.Ap;
+  }
+  const double bd = S.beta;
+  const float bf = (float)S.beta;
+  double v[1] = {0.0};
+  float s = 0.f;
+  int cnt = 0;
+  for (int64_t q = gtid(); q < V.n; q += gstride()) {
+    V.x[q] = fma(bd, (double)D[q], V.x[q]);
+    const float rq = fmaf(-bf, AD[q], V.r[q]);
+    V.r[q] = rq;
+    s = fmaf(rq, rq, s);
+    if (++cnt == 16) { v[0] += s; s = 0.f; cnt = 0; }
+  }
+  v[0] += s;
+  double o[1];
+  if (reduce_last<1>(v, V, 3, o) && threadIdx.x == 0) {
+    State &W = *V.st;
+    W.rr = o[0];
+    const int itn = W.it + 1;
+    const double rel = sqrt(o[0] / W.bb);
+    W.rel = rel;
+    W.need_true = (rel < W.tol) || (W.true_every > 0 && itn % W.true_every == 0) || (itn >= W.max_it) ||
+                  !isfinite(rel);
+  }
+}
+
+// r = b - A x in FP64 when due
+__global__ void __launch_bounds__(RT) k_true_residual(Vecs V) {
+  const State &S = *V.st;
+  if (S.status != ST_RUNNING || !S.need_true) return;
+  double v[1] = {0.0};
+  for (int64_t q = gtid(); q < V.n; q += gstride()) {
+    const double bq = V.flags[q] == MLPCG_FLUID ? V.b[q] : 0.0;
+    const double rq = bq - lap_at_f64(V, q);
+    V.r[q] = (float)rq;
+    v[0] += rq * rq;
+  }
+  double o[1];
+  if (reduce_last<1>(v, V, 0, o) && threadIdx.x == 0) V.st->rr_true = o[0];
+}
+
+// one thread: iteration bookkeeping, convergence, loop condition
+__global__ void k_control(Vecs V, cudaGraphConditionalHandle handle, int use_handle) {
+  State &S = *V.st;
+  if (S.status == ST_RUNNING) {
+    const int itn = S.it + 1;
+    S.it = itn;
+    double rel = S.rel;
+    if (S.need_true) {
+      rel = sqrt(S.rr_true / S.bb);
+      S.rr = S.rr_true;
+      S.rel = rel;
+      S.need_true = 0;
+      if (rel < S.tol) S.status = ST_CONVERGED;
+    }
+    if (!isfinite(rel)) S.status = ST_NONFINITE;
+    V.hist[itn] = rel;
+    if (S.status == ST_RUNNING && itn >= S.max_it) S.status = ST_MAXIT;
+    S.rscale = (S.rr > 0.0) ? (float)(1.0 / sqrt((double)(float)S.rr)) : 1.f;
+  }
+  if (use_handle) cudaGraphSetConditional(handle, S.status == ST_RUNNING ? 1u : 0u);
+}
+
+}  // namespace mlpcg
+
+using namespace mlpcg;
+
+struct mlpcg_solver {
+  int n1, n2, n3, method, max_it, true_every;
+  double tol;
+  const mlpcg_precond *plan = nullptr;
+  Vecs V{};
+  size_t bytes = 0;
+  bool bound = false;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t capture_stream = nullptr;  // graphs are captured here, launched on the caller's stream
+};
+
+static size_t al256s(size_t b) { return (b + 255) / 256 * 256; }
+
+static size_t solver_layout(mlpcg_solver &s, char *base) {
+  size_t off = 0;
+  auto take = [&](size_t b) -> void * {
+    void *p = base ? base + off : nullptr;
+    off += al256s(b);
+    return p;
+  };
+  const int64_t n = cells(s.n1, s.n2, s.n3);
+  const int nslots = s.method == M_NPSD ? 3 : 2;
+  const int naps = s.method == M_NPSD ? 3 : 1;
+  s.V.r = (float *)take(n * 4);
+  s.V.z = (float *)take(n * 4);
+  s.V.p = (float *)take(nslots * n * 4);
+  s.V.Ap = (float *)take(naps * n * 4);
+  s.V.part = (double *)take(NRED * RB_MAX * 8);
+  s.V.hist = (double *)take((s.max_it + 1) * 8);
+  s.V.st = (State *)take(sizeof(State));
+  return off;
+}
+
+static void destroy_graph(mlpcg_solver *s) {
+  if (s->exec) cudaGraphExecDestroy(s->exec);
+  if (s->graph) cudaGraphDestroy(s->graph);
+  s->exec = nullptr;
+  s->graph = nullptr;
+}
+
+static int enqueue_body(mlpcg_solver *s, cudaStream_t st, cudaGraphConditionalHandle h, int use_handle) {
+  Vecs &V = s->V;
+  const unsigned nb = (unsigned)V.nblk;
+  State *S = V.st;
+  // z = M (r / ||r||): the scale is read from the device state
+  int rc = mlpcg_precond_apply(s->plan, V.r, &S->rscale, V.z, st);
+  if (rc) return rc;
+  if (s->method == M_NPSD) {
+    k_sd_dots<<<nb, RT, 0, st>>>(V);
+    k_sd_qform<<<nb, RT, 0, st>>>(V);
+    k_sd_spmv<<<nb, RT, 0, st>>>(V);
+  } else {
+    k_cg_rz<<<nb, RT, 0, st>>>(V);
+    k_cg_pspmv<<<nb, RT, 0, st>>>(V);
+  }
+  k_update<<<nb, RT, 0, st>>>(V);
+  k_true_residual<<<nb, RT, 0, st>>>(V);
+  k_control<<<1, 1, 0, st>>>(V, h, use_handle);
+  MLPCG_LAUNCH_CHECK();
+  return MLPCG_OK;
+}
+
+extern "C" {
+
+int mlpcg_solver_create(int N1, int N2, int N3, const mlpcg_precond *plan, int method, int max_it, double tol,
+                        int true_every, mlpcg_solver **out) {
+  clear_error();
+  MLPCG_REQUIRE(out && plan, MLPCG_ERR_ARG, "solver_create: NULL argument");
+  MLPCG_REQUIRE(method == M_NPSD || method == M_NPCG, MLPCG_ERR_ARG, "solver_create: method must be 0 (npsd) or 1 (npcg)");
+  MLPCG_REQUIRE(max_it >= 1 && max_it <= 1000000, MLPCG_ERR_ARG, "solver_create: max_it out of range");
+  MLPCG_REQUIRE(tol > 0.0, MLPCG_ERR_ARG, "solver_create: tol must be > 0");
+  MLPCG_REQUIRE(N1 >= 1 && N2 >= 1 && N3 >= 1, MLPCG_ERR_SHAPE, "solver_create: bad grid");
+  auto *s = new mlpcg_solver();
+  s->n1 = N1; s->n2 = N2; s->n3 = N3;
+  s->method = method; s->max_it = max_it; s->tol = tol; s->true_every = true_every;
+  s->plan = plan;
+  s->bytes = solver_layout(*s, nullptr);
+  *out = s;
+  return MLPCG_OK;
+}
+
+size_t mlpcg_solver_workspace(const mlpcg_solver *s) { return s ? s->bytes : 0; }
+
+void mlpcg_solver_destroy(mlpcg_solver *s) {
+  if (!s) return;
+  destroy_graph(s);
+  if (s->capture_stream) cudaStreamDestroy(s->capture_stream);
+  delete s;
+}
+
+int mlpcg_solver_bind(mlpcg_solver *s, void *workspace, size_t workspace_bytes, const uint8_t *flags,
+                      const double *b, double *x) {
+  clear_error();
+  MLPCG_REQUIRE(s && workspace && flags && b && x, MLPCG_ERR_ARG, "solver_bind: NULL argument");
+  MLPCG_REQUIRE(workspace_bytes >= s->bytes, MLPCG_ERR_WORKSPACE, "solver workspace too small: %zu < %zu",
+                workspace_bytes, s->bytes);
+  MLPCG_REQUIRE(((uintptr_t)workspace & 255) == 0, MLPCG_ERR_ALIGN, "solver workspace must be 256-byte aligned");
+  destroy_graph(s);
+  solver_layout(*s, (char *)workspace);
+  Vecs &V = s->V;
+  V.flags = flags; V.b = b; V.x = x;
+  V.n1 = s->n1; V.n2 = s->n2; V.n3 = s->n3;
+  V.n = cells(s->n1, s->n2, s->n3);
+  int64_t nb = (V.n + RT * 8 - 1) / (RT * 8);
+  V.nblk = (int)(nb < 1 ? 1 : (nb > RB_MAX ? RB_MAX : nb));
+  s->bound = true;
+  return MLPCG_OK;
+}
+
+// Resets the state and x's residual, then runs the loop: as one CUDA graph
+// (use_graph = 1; built on the first call and reused) or as plain launches
+// with one host check per iteration (use_graph = 0).  Asynchronous for the
+// graph; mlpcg_solver_result() synchronises.
+int mlpcg_solver_solve(mlpcg_solver *s, int use_graph, void *stream) {
+  clear_error();
+  MLPCG_REQUIRE(s && s->bound, MLPCG_ERR_ARG, "solver_solve: solver not bound");
+  cudaStream_t st = as_stream(stream);
+  Vecs &V = s->V;
+  k_reset<<<1, 32, 0, st>>>(V.st, s->max_it, s->true_every, s->method, s->tol);
+  k_init<<<(unsigned)V.nblk, RT, 0, st>>>(V);
+  MLPCG_LAUNCH_CHECK();
+  if (!use_graph) {
+    for (int it = 0; it < s->max_it; ++it) {
+      int status = 0;
+      MLPCG_CUDA_CHECK(cudaMemcpyAsync(&status, &V.st->status, sizeof(int), cudaMemcpyDeviceToHost, st));
+      MLPCG_CUDA_CHECK(cudaStreamSynchronize(st));
+      if (status != ST_RUNNING) break;
+      int rc = enqueue_body(s, st, 0, 0);
+      if (rc) return rc;
+    }
+    return MLPCG_OK;
+  }
+  if (!s->exec) {
+    if (!s->capture_stream)
+      MLPCG_CUDA_CHECK(cudaStreamCreateWithFlags(&s->capture_stream, cudaStreamNonBlocking));
+    MLPCG_CUDA_CHECK(cudaGraphCreate(&s->graph, 0));
+    cudaGraphConditionalHandle h;
+    MLPCG_CUDA_CHECK(cudaGraphConditionalHandleCreate(&h, s->graph, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp{};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    MLPCG_CUDA_CHECK(cudaGraphAddNode(&node, s->graph, nullptr, nullptr, 0, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    cudaStream_t cs = s->capture_stream;
+    MLPCG_CUDA_CHECK(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue_body(s, cs, h, 1);
+    cudaGraph_t captured = nullptr;
+    cudaError_t e = cudaStreamEndCapture(cs, &captured);
+    if (rc) { destroy_graph(s); return rc; }
+    if (e != cudaSuccess) { destroy_graph(s); MLPCG_CUDA_CHECK(e); }
+    MLPCG_CUDA_CHECK(cudaGraphInstantiate(&s->exec, s->graph, 0));
+  }
+  // the loop only starts when the initial residual is not already converged:
+  // the body's first kernels see status != RUNNING and the control kernel
+  // ends the loop after one pass.
+  MLPCG_CUDA_CHECK(cudaGraphLaunch(s->exec, st));
+  return MLPCG_OK;
+}
+
+int mlpcg_solver_result(const mlpcg_solver *s, int *iters, int *status, double *rel_res, double *history,
+                        void *stream) {
+  clear_error();
+  MLPCG_REQUIRE(s && s->bound, MLPCG_ERR_ARG, "solver_result: solver not bound");
+  cudaStream_t st = as_stream(stream);
+  State S;
+  MLPCG_CUDA_CHECK(cudaMemcpyAsync(&S, s->V.st, sizeof(State), cudaMemcpyDeviceToHost, st));
+  if (history)
+    MLPCG_CUDA_CHECK(cudaMemcpyAsync(history, s->V.hist, (s->max_it + 1) * sizeof(double), cudaMemcpyDeviceToHost, st));
+  MLPCG_CUDA_CHECK(cudaStreamSynchronize(st));
+  if (iters) *iters = S.it;
+  if (status) *status = S.status;
+  if (rel_res) *rel_res = S.rel;
+  return MLPCG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,117 @@
+"""PrecondPlan: SmallSMModelDn3D.eval_forward with every block's coefficients
+precomputed once per (image, weights) and fused level kernels.
+
+The reference re-evaluates each block's 27 coefficients from the image inside
+every call (sm_block_3d_kernel.cu:45-65) and caches only the image pyramid and
+c0/c1 (sm_model_3d.py:180-239).  The plan evaluates them once into 27 planes
+(BF16 or FP32) per block, so an application is 2n+1 bandwidth-bound kernels
+(mlpcg_precond_apply).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import torch
+
+from . import _lib
+from ._lib import BF16, F32, call
+from .ops import _check, _p, _stream
+
+_DT = {torch.float32: F32, torch.bfloat16: BF16}
+
+
+def pack_params(model) -> torch.Tensor:
+    """Flat F32 parameter vector in the order mlpcg_precond_setup expects."""
+    n = model.n
+    parts = []
+    for blk in list(model.pre) + list(model.post) + [model.l]:
+        parts += [blk.weight.detach().reshape(-1), blk.bias.detach().reshape(-1)]
+    for lin in list(model.c0) + list(model.c1):
+        parts += [lin.weight.detach().reshape(-1), lin.bias.detach().reshape(-1)]
+    flat = torch.cat([p.float() for p in parts]).contiguous()
+    assert flat.numel() == (2 * n + 1) * 2214 + 2 * n * 82
+    return flat
+
+
+class PrecondPlan:
+    """z = M r for one image; ``apply`` is graph-capturable (no host sync, no allocation with ``out``)."""
+
+    def __init__(self, model, image, storage=torch.bfloat16, act_storage=None):
+        _check(image, "image")
+        if image.dim() != 4 or image.shape[0] != 3:
+            raise RuntimeError("image must have shape (3, N1, N2, N3)")
+        act_storage = storage if act_storage is None else act_storage
+        self.shape = tuple(int(s) for s in image.shape[1:])
+        self.levels = model.n
+        self.storage, self.act_storage = storage, act_storage
+        self.device = image.device
+        lib = _lib.load()
+        h = C.c_void_p()
+        call("mlpcg_precond_create", *self.shape, model.n, _DT[storage], _DT[act_storage],
+             int(bool(model.swap_ord)), int(bool(model.pre[0].mask)), C.byref(h))
+        self._h = h
+        self._lib = lib
+        nbytes = lib.mlpcg_precond_workspace(h)
+        self.workspace = torch.empty(nbytes, dtype=torch.uint8, device=image.device)
+        self.params = pack_params(model).to(image.device)
+        self.image = image
+        call("mlpcg_precond_setup", h, _p(self.workspace), nbytes, _p(image), _p(self.params),
+             _stream(image.device))
+
+    @property
+    def handle(self):
+        return self._h
+
+    def coefficients(self) -> torch.Tensor:
+        c = torch.empty(2 * self.levels, dtype=torch.float32, device=self.device)
+        call("mlpcg_precond_coefficients", self._h, _p(c), _stream(self.device))
+        return c
+
+    def apply(self, r: torch.Tensor, scale: torch.Tensor | None = None, out: torch.Tensor | None = None):
+        """z = M(r * scale) on the full grid; r F32 with the grid's numel."""
+        _check(r, "r")
+        z = torch.empty(self.shape, dtype=torch.float32, device=r.device) if out is None else out
+        call("mlpcg_precond_apply", self._h, _p(r), _p(scale), _p(z), _stream(r.device))
+        return z.reshape(r.shape) if out is None else z
+
+    def apply_stages(self, first: int, last: int, r: torch.Tensor, scale=None, out=None):
+        """Launch stages [first, last] of an application (see mlpcg_precond_apply_stages)."""
+        z = torch.empty(self.shape, dtype=torch.float32, device=r.device) if out is None else out
+        call("mlpcg_precond_apply_stages", self._h, int(first), int(last), _p(r), _p(scale), _p(z),
+             _stream(r.device))
+        return z
+
+    def level_info(self, level: int):
+        n1, n2, n3, fast = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        call("mlpcg_precond_level_info", self._h, int(level), C.byref(n1), C.byref(n2), C.byref(n3),
+             C.byref(fast))
+        return (n1.value, n2.value, n3.value), bool(fast.value)
+
+    def stage_names(self):
+        n = self.levels
+        return [f"pre{l}" for l in range(n)] + [f"l{n}"] + [f"post{2 * n - s}" for s in range(n + 1, 2 * n + 1)]
+
+    def predict(self, fluid_cells):
+        """A model_predict-style callable (test.py:42-51) on compressed FP64 vectors."""
+        n = 1
+        for s in self.shape:
+            n *= s
+
+        def predict(r, timer=None, imgs=None, c0=None, c1=None):
+            r32 = r.to(torch.float32)
+            g = torch.zeros(n, dtype=torch.float32, device=r.device)
+            g[fluid_cells] = r32
+            scale = (1.0 / torch.clamp(r32.norm(), min=1e-12)).reshape(1)
+            z = self.apply(g, scale)
+            return z.reshape(-1)[fluid_cells].double()
+
+        return predict
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                self._lib.mlpcg_precond_destroy(h)
+            except Exception:
+                pass
+            self._h = None

@@ -345,7 +345,7 @@ class SmallSMModelDn3D(BaseModel):
                 x[i - 1] = CombineFunction.apply(c0, x[i - 1], c1, x[i])
         return x[0]
 
-    def precond_plan(self, image, storage=torch.bfloat16, fluid_mask=None):
+    def precond_plan(self, image, storage=torch.bfloat16, act_storage=None):
         """Coefficients of every block precomputed on ``image``: see precond.PrecondPlan."""
         from .precond import PrecondPlan
-        return PrecondPlan(self, image, storage=storage, fluid_mask=fluid_mask)
+        return PrecondPlan(self, image, storage=storage, act_storage=act_storage)

@@ -1,0 +1,108 @@
+"""FusedSolver: npsd / npcg with the network preconditioner, entirely on the GPU.
+
+One CUDA graph per solver: a conditional WHILE node wraps one iteration
+(2n+1 fused preconditioner kernels, the orthogonalisation / SpMV / update
+kernels with FP64 reductions, an FP64 true residual every ``true_every``
+iterations, a one-thread control kernel).  ``solve`` is a single graph
+launch; the host synchronises only to read the result.
+
+The drop-in solvers of ``cg.py`` keep the reference's per-iteration host
+round trips (cg_tests.py:90,266); this is the form they are compared with.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import call
+from .ops import _p, _stream
+from .precond import PrecondPlan, pack_params
+
+METHODS = {"npsd": 0, "npcg": 1}
+STATUS = {0: "running", 1: "converged", 2: "max_it", 3: "breakdown", 4: "nonfinite"}
+
+
+@dataclass
+class SolveResult:
+    x: torch.Tensor             # (N1, N2, N3) FP64, zero off-fluid
+    iterations: int
+    status: str
+    rel_res: float              # final FP64 true relative residual
+    history: np.ndarray         # relative residual after each iteration (index 0 = initial)
+
+
+def flags_to_image(flags: torch.Tensor) -> torch.Tensor:
+    """[air, fluid, non-solid] F32 channels from uint8 flags on the device."""
+    img = torch.empty((3,) + tuple(flags.shape), dtype=torch.float32, device=flags.device)
+    call("mlpcg_flags_to_image", _p(flags), _p(img), flags.numel(), _stream(flags.device))
+    return img
+
+
+class FusedSolver:
+    def __init__(self, model, flags: torch.Tensor, method="npsd", max_it=100, tol=1e-6, true_every=25,
+                 storage=torch.bfloat16, act_storage=None, image=None, plan: PrecondPlan | None = None):
+        if flags.dtype != torch.uint8 or flags.dim() != 3 or not flags.is_cuda:
+            raise ValueError("flags must be a (N1, N2, N3) uint8 CUDA tensor")
+        self.flags = flags.contiguous()
+        self.shape = tuple(int(s) for s in flags.shape)
+        self.method, self.max_it, self.tol, self.true_every = method, int(max_it), float(tol), int(true_every)
+        dev = flags.device
+        if plan is None:
+            image = flags_to_image(self.flags) if image is None else image
+            plan = PrecondPlan(model, image, storage=storage, act_storage=act_storage)
+        self.plan = plan
+        lib = _lib.load()
+        self._lib = lib
+        h = C.c_void_p()
+        call("mlpcg_solver_create", *self.shape, plan.handle, METHODS[method], self.max_it,
+             C.c_double(self.tol), self.true_every, C.byref(h))
+        self._h = h
+        nbytes = lib.mlpcg_solver_workspace(h)
+        self.workspace = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        self.b = torch.zeros(self.shape, dtype=torch.float64, device=dev)
+        self.x = torch.zeros(self.shape, dtype=torch.float64, device=dev)
+        call("mlpcg_solver_bind", h, _p(self.workspace), nbytes, _p(self.flags), _p(self.b), _p(self.x))
+
+    def set_image(self, model, image: torch.Tensor, flags: torch.Tensor | None = None):
+        """New frame: recompute the plan in place (the captured graph stays valid)."""
+        if flags is not None:
+            self.flags.copy_(flags)
+        if model is not None:
+            self.plan.params.copy_(pack_params(model))
+        call("mlpcg_precond_setup", self.plan.handle, _p(self.plan.workspace), self.plan.workspace.numel(),
+             _p(image), _p(self.plan.params), _stream(self.flags.device))
+        self.plan.image = image
+
+    def launch(self, b: torch.Tensor | None = None, x0: torch.Tensor | None = None, use_graph=True):
+        """Enqueue a solve (asynchronous with use_graph)."""
+        if b is not None and b.data_ptr() != self.b.data_ptr():
+            self.b.copy_(b.reshape(self.shape))
+        if x0 is None:
+            self.x.zero_()
+        elif x0.data_ptr() != self.x.data_ptr():
+            self.x.copy_(x0.reshape(self.shape))
+        call("mlpcg_solver_solve", self._h, int(bool(use_graph)), _stream(self.flags.device))
+
+    def result(self, with_history=True) -> SolveResult:
+        it, st, rel = C.c_int(), C.c_int(), C.c_double()
+        hist = np.zeros(self.max_it + 1, dtype=np.float64)
+        call("mlpcg_solver_result", self._h, C.byref(it), C.byref(st), C.byref(rel),
+             hist.ctypes.data_as(C.c_void_p) if with_history else None, _stream(self.flags.device))
+        return SolveResult(self.x, it.value, STATUS[st.value], rel.value, hist[: it.value + 1])
+
+    def solve(self, b: torch.Tensor, x0: torch.Tensor | None = None, use_graph=True) -> SolveResult:
+        self.launch(b, x0, use_graph)
+        return self.result()
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                self._lib.mlpcg_solver_destroy(h)
+            except Exception:
+                pass
+            self._h = None

@@ -1,0 +1,214 @@
+"""Training of SmallSMModelDn3D through the hand-written adjoint kernels (the reference's train.py).
+
+Loss (per right-hand side b of unit norm, x = f(b) restricted to fluid cells):
+  * ``squared`` (default): ||b - A x||^2 / ||b||^2, averaged over the batch;
+  * ``reference``: ||b - A x|| averaged over the batch (residual_loss,
+    loss_functions.py:18-23).
+Right-hand sides: random combinations of the lowest Lanczos Ritz vectors of
+each scene (lanczos.py), plus a fraction of white noise on the fluid cells so
+that the high-frequency end of the spectrum is seen as well.  Optimiser:
+Adam (train.py:219 of the reference uses lr 1e-4 over far more steps; a
+cosine schedule from a larger lr is used here).
+
+    python -m mlpcg_gb300.train --out DIR --size 128 --levels 5 --seeds 10-17 --steps 4000
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import time
+from pathlib import Path
+
+import numpy as np
+import torch
+
+from . import ops
+from .laplacian import FluidLaplacian
+from .lanczos import lanczos_ritz, mix_rhs
+from .scenes import make_scene
+from .sm_model_3d import SmallSMModelDn3D
+from .solver import FusedSolver, flags_to_image
+
+
+class LaplacianFunction(torch.autograd.Function):
+    """y = A x for a batch of full-grid F32 fields; A is symmetric, so the adjoint is A again."""
+
+    @staticmethod
+    def forward(ctx, flags, x):
+        ctx.flags = flags
+        return _lap_batch(flags, x)
+
+    @staticmethod
+    def backward(ctx, g):
+        return None, _lap_batch(ctx.flags, g.contiguous())
+
+
+def _lap_batch(flags, x):
+    shp = x.shape
+    xb = x.reshape(-1, *flags.shape).contiguous()
+    out = torch.stack([ops.laplacian(flags, xb[i]) for i in range(xb.shape[0])])
+    return out.reshape(shp)
+
+
+def residual_loss(model, image, flags, fluid, b, kind="step"):
+    """b: (B, N1, N2, N3) unit-norm on fluid cells, zero elsewhere.
+
+    kind = "squared":   ||b - A x||^2 / ||b||^2
+           "reference": ||b - A x||  (residual_loss, loss_functions.py:18-23)
+           "step":      ||b - beta A x||^2 / ||b||^2 with beta = x.b / x.Ax, the
+                        residual after one exactly line-searched npsd step from 0
+                        (the A-norm scaling of scaled_loss_2, loss_functions.py:45-53);
+                        invariant to the scale of the network output, like npsd.
+    """
+    x = model(image, b[:, None])[:, 0]
+    x = x * fluid
+    Ax = LaplacianFunction.apply(flags, x)
+    bf, xf, Af = b.flatten(1), x.flatten(1), Ax.flatten(1)
+    if kind == "step":
+        beta = (xf * bf).sum(1, keepdim=True) / (xf * Af).sum(1, keepdim=True)
+        r = bf - beta * Af
+        return (r.pow(2).sum(1) / bf.pow(2).sum(1)).mean()
+    r = bf - Af
+    if kind == "reference":
+        return r.norm(dim=1).mean()
+    return (r.pow(2).sum(1) / bf.pow(2).sum(1)).mean()
+
+
+def near_identity_(model, eps=0.1):
+    """Shrink the random weights by eps and add z = x on the direct path (M ~ I at start)."""
+    with torch.no_grad():
+        for p in model.parameters():
+            p.mul_(eps)
+        model.pre[0].bias[13] += 1.0
+        model.c0[0].bias[0] += 1.0
+
+
+class TrainScene:
+    def __init__(self, shape, seed, device, n_ritz=64, lanczos_steps=1600, spheres=3):
+        s = make_scene(shape, seed, spheres)
+        self.seed = seed
+        self.flags = torch.as_tensor(s.flags, device=device)
+        self.image = flags_to_image(self.flags)
+        self.fluid = (self.flags == 2).float()
+        self.A = FluidLaplacian(self.flags)
+        self.rhs = torch.as_tensor(s.rhs, device=device)
+        v0 = self.rhs.reshape(-1)[self.A.fluid_cells]
+        t = time.time()
+        self.ritz_vals, ritz = lanczos_ritz(self.A, v0, lanczos_steps, n_ritz)
+        self.lanczos_s = time.time() - t
+        self.ritz = ritz.float()
+        self.n = self.flags.numel()
+
+    def batch(self, B, noise_frac, gen):
+        nb = int(round(B * noise_frac))
+        parts = []
+        if B - nb > 0:
+            parts.append(mix_rhs(self.ritz, B - nb, generator=gen))
+        if nb > 0:
+            w = torch.randn((nb, self.A.n_fluid), device=self.ritz.device, generator=gen)
+            parts.append(w / w.norm(dim=1, keepdim=True))
+        bf = torch.cat(parts)
+        b = torch.zeros((B, self.n), dtype=torch.float32, device=bf.device)
+        b[:, self.A.fluid_cells] = bf
+        return b.reshape(B, *self.flags.shape)
+
+
+def evaluate(model, scene: TrainScene, max_it=200, tol=1e-6):
+    solver = FusedSolver(model, scene.flags, method="npsd", max_it=max_it, tol=tol, image=scene.image)
+    r = solver.solve(scene.rhs)
+    return r.iterations, r.status, r.rel_res
+
+
+def parse_seeds(s):
+    if "-" in s:
+        a, b = s.split("-")
+        return list(range(int(a), int(b) + 1))
+    return [int(t) for t in s.split(",")]
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--out", required=True)
+    ap.add_argument("--size", type=int, default=128)
+    ap.add_argument("--levels", type=int, default=5)
+    ap.add_argument("--seeds", default="10-17")
+    ap.add_argument("--steps", type=int, default=4000)
+    ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--lr", type=float, default=3e-3)
+    ap.add_argument("--lr-min", type=float, default=1e-4)
+    ap.add_argument("--noise-frac", type=float, default=0.25)
+    ap.add_argument("--loss", default="step", choices=["step", "squared", "reference"])
+    ap.add_argument("--init-mode", default="near-identity", choices=["near-identity", "reference"])
+    ap.add_argument("--init-eps", type=float, default=0.1)
+    ap.add_argument("--lanczos-steps", type=int, default=1600)
+    ap.add_argument("--n-ritz", type=int, default=64)
+    ap.add_argument("--eval-every", type=int, default=500)
+    ap.add_argument("--eval-seed", type=int, default=18)
+    ap.add_argument("--init", default=None, help="npz state dict to start from")
+    ap.add_argument("--time-limit", type=float, default=1e9, help="seconds of training loop at most")
+    args = ap.parse_args(argv)
+
+    dev = torch.device("cuda")
+    out = Path(args.out)
+    out.mkdir(parents=True, exist_ok=True)
+    torch.manual_seed(0)
+    model = SmallSMModelDn3D(args.levels, 3, "trilinear").to(dev)
+    if args.init:
+        d = np.load(args.init)
+        model.load_state_dict({k: torch.from_numpy(d[k]) for k in model.state_dict()})
+    elif args.init_mode == "near-identity":
+        near_identity_(model, args.init_eps)
+    t0 = time.time()
+    scenes = [TrainScene(args.size, s, dev, args.n_ritz, args.lanczos_steps) for s in parse_seeds(args.seeds)]
+    val = TrainScene(args.size, args.eval_seed, dev, 8, 16)
+    prep_s = time.time() - t0
+    print(f"prepared {len(scenes)} scenes in {prep_s:.1f}s (lanczos {[round(s.lanczos_s, 1) for s in scenes]})",
+          flush=True)
+
+    opt = torch.optim.Adam(model.parameters(), lr=args.lr)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(1234)
+    log = {"loss": [], "eval": [], "args": vars(args), "prep_s": prep_s}
+    it0, st0, rel0 = evaluate(model, val)
+    log["eval"].append({"step": 0, "iterations": it0, "status": st0, "rel_res": rel0})
+    print(f"step 0 eval: {it0} its ({st0}, {rel0:.2e})", flush=True)
+    t_train = time.time()
+    ema = None
+    step = 0
+    for step in range(1, args.steps + 1):
+        lr = args.lr_min + 0.5 * (args.lr - args.lr_min) * (1 + math.cos(math.pi * (step - 1) / args.steps))
+        for g in opt.param_groups:
+            g["lr"] = lr
+        sc = scenes[(step - 1) % len(scenes)]
+        b = sc.batch(args.batch, args.noise_frac, gen)
+        loss = residual_loss(model, sc.image, sc.flags, sc.fluid, b, args.loss)
+        opt.zero_grad(set_to_none=True)
+        loss.backward()
+        opt.step()
+        lv = float(loss.detach())
+        ema = lv if ema is None else 0.98 * ema + 0.02 * lv
+        if step % 50 == 0:
+            log["loss"].append({"step": step, "loss": lv, "ema": ema, "lr": lr})
+            print(f"step {step} loss {lv:.4e} ema {ema:.4e} lr {lr:.2e} ({time.time() - t_train:.0f}s)", flush=True)
+        if step % args.eval_every == 0 or step == args.steps:
+            it, st, rel = evaluate(model, val)
+            log["eval"].append({"step": step, "iterations": it, "status": st, "rel_res": rel})
+            print(f"step {step} eval: {it} its ({st}, {rel:.2e})", flush=True)
+            save(model, out, args, log)
+        if time.time() - t_train > args.time_limit:
+            print(f"time limit reached at step {step}", flush=True)
+            break
+    log["train_s"] = time.time() - t_train
+    log["steps_done"] = step
+    save(model, out, args, log)
+
+
+def save(model, out: Path, args, log):
+    sd = {k: v.detach().float().cpu().numpy() for k, v in model.state_dict().items()}
+    np.savez(out / f"smallsm_l{args.levels}.npz", **sd)
+    (out / f"smallsm_l{args.levels}.train.json").write_text(json.dumps(log, indent=1))
+
+
+if __name__ == "__main__":
+    main()

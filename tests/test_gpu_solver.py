@@ -1,0 +1,162 @@
+"""Preconditioner plan and fused graph-captured solver vs the drop-in path and the FP64 oracle (GPU)."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import rel_err
+from oracle import laplacian as olap
+
+pytestmark = pytest.mark.gpu
+
+
+def _model(n, dev, seed=0, swap=False, mask=False):
+    from mlpcg_gb300.sm_model_3d import SmallSMModelDn3D
+    torch.manual_seed(seed)
+    return SmallSMModelDn3D(n, 3, "trilinear", mask=mask, swap_sm_order=swap).to(dev)
+
+
+def _near_identity_model(n, dev, eps=0.02, seed=1):
+    """M = I plus a small non-symmetric perturbation through every block and level."""
+    m = _model(n, dev, seed)
+    with torch.no_grad():
+        for p in m.parameters():
+            p.mul_(eps)
+        m.pre[0].bias[13] += 1.0
+        m.c0[0].bias[0] += 1.0
+    return m
+
+
+def _scene(shape, seed, dev):
+    from mlpcg_gb300.scenes import make_scene
+    s = make_scene(shape, seed)
+    return s, torch.as_tensor(s.flags, device=dev), torch.as_tensor(s.image(), device=dev)
+
+
+@pytest.mark.parametrize("shape,n", [((16, 16, 16), 3), ((32, 16, 24), 3), ((64, 64, 64), 4), ((24, 40, 8), 3)])
+@pytest.mark.parametrize("swap,mask", [(False, False), (True, False), (False, True)])
+def test_plan_fp32_matches_eval_forward(cuda, shape, n, swap, mask):
+    s, flags, img = _scene(shape, 2, cuda)
+    m = _model(n, cuda, swap=swap, mask=mask)
+    plan = m.precond_plan(img, storage=torch.float32)
+    b = torch.randn((1, 1) + shape, device=cuda)
+    ref = m.eval_forward(img, b)
+    ref = torch.where(img[1] == 0, 0.0, ref)          # the fluid gather of test.py:49-50
+    z = plan.apply(b.reshape(-1)).reshape(ref.shape)
+    assert rel_err(z.cpu().numpy(), ref.cpu().numpy()) < 1e-5
+    scale = torch.tensor([0.37], device=cuda)
+    z2 = plan.apply(b.reshape(-1).contiguous(), scale).reshape(ref.shape)
+    assert rel_err(z2.cpu().numpy(), 0.37 * ref.cpu().numpy()) < 1e-5
+
+
+@pytest.mark.parametrize("storage,act", [(torch.bfloat16, torch.bfloat16), (torch.bfloat16, torch.float32),
+                                         (torch.float32, torch.bfloat16)])
+def test_plan_bf16_storage(cuda, storage, act):
+    s, flags, img = _scene((64, 64, 64), 4, cuda)
+    m = _model(4, cuda)
+    ref = m.precond_plan(img, storage=torch.float32).apply(torch.ones(64 ** 3, device=cuda))
+    b = torch.randn(64 ** 3, device=cuda)
+    ref = m.precond_plan(img, storage=torch.float32).apply(b)
+    z = m.precond_plan(img, storage=storage, act_storage=act).apply(b)
+    err = (z - ref).norm() / ref.norm()
+    assert err < 2e-2, float(err)
+
+
+def test_plan_coefficients_match_linear_blocks(cuda):
+    s, flags, img = _scene((32, 32, 32), 5, cuda)
+    m = _model(3, cuda)
+    plan = m.precond_plan(img, storage=torch.float32)
+    c = plan.coefficients().cpu().numpy()
+    imgs = [img]
+    from mlpcg_gb300 import ops
+    for _ in range(2):
+        imgs.append(ops.avg_pool2(imgs[-1]))
+    for l in range(3):
+        c0 = float(m.c0[l].eval_forward(imgs[l]))
+        c1 = float(m.c1[l].eval_forward(imgs[l]))
+        assert abs(c[l] - c0) <= 1e-6 * max(1, abs(c0)) and abs(c[3 + l] - c1) <= 1e-6 * max(1, abs(c1))
+
+
+@pytest.mark.parametrize("method", ["npcg", "npsd"])
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_fused_identity_preconditioner_is_cg(cuda, method, use_graph):
+    """With M = I, npcg is plain CG: converge to 1e-6 and match the FP64 oracle solution."""
+    from mlpcg_gb300.solver import FusedSolver
+    s, flags, img = _scene((24, 24, 24), 3, cuda)
+    m = _near_identity_model(3, cuda, eps=0.0)
+    solver = FusedSolver(m, flags, method=method, max_it=400, tol=1e-6, storage=torch.float32)
+    res = solver.solve(torch.as_tensor(s.rhs, device=cuda), use_graph=use_graph)
+    assert res.status == "converged", (res.status, res.iterations, res.rel_res)
+    A, fluid = olap.assemble(s.flags)
+    b = s.rhs.ravel()[fluid]
+    x = res.x.cpu().numpy().ravel()[fluid]
+    true_rel = np.linalg.norm(b - A @ x) / np.linalg.norm(b)
+    assert true_rel < 1e-6 and abs(true_rel - res.rel_res) <= 1e-3 * true_rel
+    xo, it_o = olap.cg_fp64(A, b, tol=1e-12)
+    assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-4
+    if method == "npcg":
+        _, it_cg = olap.cg_fp64(A, b, tol=1e-6)
+        assert abs(res.iterations - it_cg) <= 3
+    assert np.all(solver.flags.cpu().numpy().ravel()[res.x.cpu().numpy().ravel() != 0] == 2)
+
+
+@pytest.mark.parametrize("method", ["npsd", "npcg"])
+def test_fused_matches_dropin_history(cuda, method):
+    """Fused (FP32 vectors, FP64 reductions) vs drop-in (FP64 vectors, reference recurrences)."""
+    from mlpcg_gb300 import cg
+    from mlpcg_gb300.laplacian import FluidLaplacian
+    from mlpcg_gb300.solver import FusedSolver
+    s, flags, img = _scene((32, 32, 32), 6, cuda)
+    m = _near_identity_model(3, cuda)
+    solver = FusedSolver(m, flags, method=method, max_it=400, tol=1e-6, storage=torch.float32, true_every=1)
+    res = solver.solve(torch.as_tensor(s.rhs, device=cuda))
+    A = FluidLaplacian(flags)
+    b = torch.as_tensor(s.rhs.ravel(), device=cuda)[A.fluid_cells]
+    hist = []
+    pred = cg.model_predict(m, img, A.fluid_cells)
+    getattr(cg, method)(b, A, torch.zeros_like(b), pred, 400, tol=1e-6, atol=1e-20,
+                        callback=lambda nrm, t: hist.append(nrm))
+    k = min(25, len(hist), len(res.history))
+    np.testing.assert_allclose(res.history[:k], np.array(hist[:k]), rtol=2e-3)
+    assert res.status == "converged" and hist[-1] < 1e-6
+    assert abs(res.iterations - (len(hist) - 1)) <= max(3, 0.05 * res.iterations)
+
+
+def test_fused_graph_reuse_is_deterministic(cuda):
+    from mlpcg_gb300.solver import FusedSolver
+    s, flags, img = _scene((32, 32, 32), 7, cuda)
+    m = _near_identity_model(3, cuda)
+    solver = FusedSolver(m, flags, method="npsd", max_it=40, tol=1e-6)
+    r1 = solver.solve(torch.as_tensor(s.rhs, device=cuda))
+    x1 = r1.x.clone()
+    assert r1.status == "max_it" and r1.iterations == 40 and r1.history[-1] < r1.history[0]
+    r2 = solver.solve(torch.as_tensor(s.rhs, device=cuda))
+    assert r2.iterations == r1.iterations and torch.equal(x1, r2.x)  # deterministic reductions
+    r3 = solver.solve(torch.as_tensor(s.rhs, device=cuda), use_graph=False)
+    assert torch.equal(x1, r3.x) and r3.iterations == r1.iterations
+
+
+def test_fused_status_words(cuda):
+    from mlpcg_gb300.solver import FusedSolver
+    s, flags, img = _scene((16, 16, 16), 8, cuda)
+    m = _near_identity_model(2, cuda)
+    solver = FusedSolver(m, flags, method="npsd", max_it=2, tol=1e-6)
+    r = solver.solve(torch.zeros(s.shape, dtype=torch.float64, device=cuda))
+    assert r.status == "converged" and r.iterations == 0
+    r = solver.solve(torch.as_tensor(s.rhs, device=cuda))
+    assert r.status == "max_it" and r.iterations == 2
+    bad = torch.as_tensor(s.rhs, device=cuda).clone()
+    bad.view(-1)[torch.nonzero(flags.view(-1) == 2)[0]] = float("nan")
+    r = solver.solve(bad)
+    assert r.status == "nonfinite"
+    # the solver still works after a non-finite solve
+    r = solver.solve(torch.as_tensor(s.rhs, device=cuda))
+    assert r.status == "max_it" and np.isfinite(r.rel_res)
+
+
+def test_all_solid_grid(cuda):
+    from mlpcg_gb300.solver import FusedSolver
+    flags = torch.full((16, 16, 16), 1, dtype=torch.uint8, device=cuda)
+    m = _near_identity_model(2, cuda)
+    solver = FusedSolver(m, flags, method="npcg", max_it=5, tol=1e-6)
+    r = solver.solve(torch.ones((16, 16, 16), dtype=torch.float64, device=cuda))
+    assert r.status == "converged" and r.iterations == 0

@@ -1,0 +1,63 @@
+"""Training pieces: Lanczos Ritz pairs vs the FP64 oracle matrix, loss adjoint, a few Adam steps (GPU)."""
+import numpy as np
+import pytest
+import scipy.sparse.linalg as sla
+import torch
+
+from oracle import laplacian as olap
+
+pytestmark = pytest.mark.gpu
+
+
+def test_lanczos_ritz_pairs_match_eigsh(cuda):
+    from mlpcg_gb300.lanczos import lanczos_ritz, mix_rhs
+    from mlpcg_gb300.laplacian import FluidLaplacian
+    from mlpcg_gb300.scenes import make_scene
+    s = make_scene(12, 9)
+    A = FluidLaplacian(torch.as_tensor(s.flags, device=cuda))
+    Ac, fluid = olap.assemble(s.flags)
+    v0 = torch.as_tensor(s.rhs.ravel()[fluid], device=cuda)
+    vals, vecs = lanczos_ritz(A, v0, steps=Ac.shape[0], n_ritz=6)
+    ref = np.sort(np.linalg.eigvalsh(Ac.toarray()))[:6]
+    np.testing.assert_allclose(vals, ref, rtol=1e-8, atol=1e-10)
+    V = vecs.cpu().numpy()
+    for k in range(6):
+        res = Ac @ V[k] - vals[k] * V[k]
+        assert np.linalg.norm(res) < 1e-6
+    b = mix_rhs(vecs, 4)
+    assert torch.allclose(b.norm(dim=1), torch.ones(4, dtype=b.dtype, device=cuda))
+
+
+def test_laplacian_function_adjoint(cuda):
+    from mlpcg_gb300.train import LaplacianFunction
+    from mlpcg_gb300.scenes import make_scene
+    s = make_scene(16, 2)
+    flags = torch.as_tensor(s.flags, device=cuda)
+    x = torch.randn((3,) + s.shape, device=cuda, requires_grad=True)
+    g = torch.randn((3,) + s.shape, device=cuda)
+    y = LaplacianFunction.apply(flags, x)
+    (y * g).sum().backward()
+    lhs = float((y.detach().double() * g.double()).sum())
+    rhs = float((x.double() * x.grad.double()).sum())
+    # <A x, g> = <x, A g>
+    assert abs(lhs - rhs) <= 1e-5 * abs(lhs)
+
+
+def test_training_steps_reduce_loss(cuda):
+    from mlpcg_gb300.sm_model_3d import SmallSMModelDn3D
+    from mlpcg_gb300.train import TrainScene, residual_loss
+    torch.manual_seed(0)
+    model = SmallSMModelDn3D(3, 3, "trilinear").to(cuda)
+    sc = TrainScene((32, 32, 32), 10, cuda, n_ritz=16, lanczos_steps=80)
+    opt = torch.optim.Adam(model.parameters(), lr=3e-3)
+    gen = torch.Generator(device=cuda)
+    gen.manual_seed(0)
+    b = sc.batch(8, 0.25, gen)
+    first = None
+    for _ in range(30):
+        loss = residual_loss(model, sc.image, sc.flags, sc.fluid, b)
+        first = float(loss) if first is None else first
+        opt.zero_grad()
+        loss.backward()
+        opt.step()
+    assert float(loss) < 0.8 * first
