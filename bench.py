@@ -65,6 +65,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-reference-solution", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--no-graph", action="store_true",
+                    help="plain launches of the same kernels with a host check per iteration (for profilers)")
     return ap.parse_args()
 
 
@@ -201,7 +203,7 @@ def run_ours(args, rank, world):
     def step():
         img = flags_to_image(flags)
         solver.set_image(None, img)
-        solver.launch(b)
+        solver.launch(b, use_graph=not args.no_graph)
 
     for _ in range(args.warmup):
         step()
@@ -285,7 +287,7 @@ def run_ours(args, rank, world):
         solver.b.copy_(b_h, non_blocking=True)
         img = flags_to_image(solver.flags)
         solver.set_image(None, img)
-        solver.launch(None)
+        solver.launch(None, use_graph=not args.no_graph)
         x_h.copy_(solver.x, non_blocking=True)
 
     for _ in range(2):

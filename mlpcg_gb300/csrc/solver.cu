@@ -45,7 +45,14 @@ struct State {
   unsigned ticket[4];
 };
 
+// q / d for q < 2^31 by multiply and shift (Granlund & Montgomery 1994, fig. 4.1)
+struct FastDiv {
+  uint32_t m, s1, s2;
+};
+
 struct Vecs {
+  FastDiv fd3, fd2;  // division by N3 and by N2
+  uint32_t ngroups;  // n / 4
   const uint8_t *flags;
   const double *b;
   double *x;
@@ -107,57 +114,113 @@ __device__ __forceinline__ bool reduce_last(double (&v)[NR], const Vecs &V, int 
   return true;
 }
 
-__device__ __forceinline__ int64_t gstride() { return (int64_t)gridDim.x * blockDim.x; }
-__device__ __forceinline__ int64_t gtid() { return (int64_t)blockIdx.x * blockDim.x + threadIdx.x; }
-
-// (A v)(q) for FLUID q (0 otherwise), v given as a functor of the cell index
-template <typename F>
-__device__ __forceinline__ float lap_at(const Vecs &V, int64_t q, F vat) {
-  if (V.flags[q] != MLPCG_FLUID) return 0.f;
-  const int k = (int)(q % V.n3);
-  const int64_t t = q / V.n3;
-  const int j = (int)(t % V.n2);
-  const int i = (int)(t / V.n2);
-  const int64_t sx = (int64_t)V.n2 * V.n3, sy = V.n3;
-  float off = 0.f;
-  int d = 0;
-  auto visit = [&](bool inside, int64_t nb) {
-    if (!inside) return;
-    const uint8_t f = V.flags[nb];
-    if (f == MLPCG_FLUID) { off += vat(nb); ++d; }
-    else if (f == MLPCG_AIR) { ++d; }
-  };
-  visit(i > 0, q - sx);
-  visit(j > 0, q - sy);
-  visit(k > 0, q - 1);
-  visit(k < V.n3 - 1, q + 1);
-  visit(j < V.n2 - 1, q + sy);
-  visit(i < V.n1 - 1, q + sx);
-  return (float)d * vat(q) - off;
+// ---------------------------------------------------------------------------
+// Cells are processed in groups of 4 consecutive z cells (N3 % 4 == 0): one
+// 16-byte load per FP32 vector (two for FP64), one 4-byte load of flags.
+// (i, j, k0) of a group come from a multiply-shift division by N3 and N2.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv &f) {
+  const uint32_t t = __umulhi(f.m, n);
+  return (t + ((n - t) >> f.s1)) >> f.s2;
 }
 
-__device__ __forceinline__ double lap_at_f64(const Vecs &V, int64_t q) {
-  if (V.flags[q] != MLPCG_FLUID) return 0.0;
-  const int k = (int)(q % V.n3);
-  const int64_t t = q / V.n3;
-  const int j = (int)(t % V.n2);
-  const int i = (int)(t / V.n2);
-  const int64_t sx = (int64_t)V.n2 * V.n3, sy = V.n3;
-  double off = 0.0;
-  int d = 0;
-  auto visit = [&](bool inside, int64_t nb) {
-    if (!inside) return;
-    const uint8_t f = V.flags[nb];
-    if (f == MLPCG_FLUID) { off += V.x[nb]; ++d; }
-    else if (f == MLPCG_AIR) { ++d; }
+__device__ __forceinline__ uint32_t gstride() { return gridDim.x * blockDim.x; }
+__device__ __forceinline__ uint32_t gtid() { return blockIdx.x * blockDim.x + threadIdx.x; }
+
+__device__ __forceinline__ void ld4(const float *p, float v[4]) {
+  const float4 a = *reinterpret_cast<const float4 *>(p);
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+}
+__device__ __forceinline__ void st4(float *p, const float v[4]) {
+  *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ __forceinline__ void ld4(const double *p, double v[4]) {
+  const double2 a = reinterpret_cast<const double2 *>(p)[0], b = reinterpret_cast<const double2 *>(p)[1];
+  v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+}
+__device__ __forceinline__ void st4(double *p, const double v[4]) {
+  reinterpret_cast<double2 *>(p)[0] = make_double2(v[0], v[1]);
+  reinterpret_cast<double2 *>(p)[1] = make_double2(v[2], v[3]);
+}
+__device__ __forceinline__ uchar4 ldflags4(const uint8_t *p) { return *reinterpret_cast<const uchar4 *>(p); }
+__device__ __forceinline__ uint8_t lane(const uchar4 f, int c) {
+  return c == 0 ? f.x : (c == 1 ? f.y : (c == 2 ? f.z : f.w));
+}
+
+// sources of the vector a stencil is applied to
+struct SrcF32 {
+  const float *a;
+  __device__ __forceinline__ void load4(uint32_t q, float v[4]) const { ld4(a + q, v); }
+  __device__ __forceinline__ float load1(uint32_t q) const { return a[q]; }
+};
+struct SrcF64 {
+  const double *a;
+  __device__ __forceinline__ void load4(uint32_t q, double v[4]) const { ld4(a + q, v); }
+  __device__ __forceinline__ double load1(uint32_t q) const { return a[q]; }
+};
+// p_new = z + beta * p_old, evaluated on the fly (first iteration: p_new = z)
+struct SrcAxpy {
+  const float *z, *p;
+  float beta;
+  bool first;
+  __device__ __forceinline__ void load4(uint32_t q, float v[4]) const {
+    ld4(z + q, v);
+    if (!first) {
+      float w[4];
+      ld4(p + q, w);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) v[c] = fmaf(beta, w[c], v[c]);
+    }
+  }
+  __device__ __forceinline__ float load1(uint32_t q) const { return first ? z[q] : fmaf(beta, p[q], z[q]); }
+};
+
+// (A v) on the 4 cells of the group at q (flat index, q % 4 == 0) at (i, j, k0);
+// cen receives v on those cells.  Neighbours are summed in the column order of
+// the assembled CSR row: i-1, j-1, k-1, k+1, j+1, i+1.
+template <typename T, typename S>
+__device__ __forceinline__ void lap4(const Vecs &V, uint32_t q, int i, int j, int k0, const S &src, T out[4],
+                                     T cen[4]) {
+  const uint32_t sy = (uint32_t)V.n3, sx = (uint32_t)V.n2 * (uint32_t)V.n3;
+  const uchar4 fc = ldflags4(V.flags + q);
+  src.load4(q, cen);
+  T off[4] = {T(0), T(0), T(0), T(0)};
+  int d[4] = {0, 0, 0, 0};
+  auto take = [&](int c, uint8_t f, T v) {
+    if (f == MLPCG_FLUID) { off[c] += v; ++d[c]; }
+    else if (f == MLPCG_AIR) { ++d[c]; }
   };
-  visit(i > 0, q - sx);
-  visit(j > 0, q - sy);
-  visit(k > 0, q - 1);
-  visit(k < V.n3 - 1, q + 1);
-  visit(j < V.n2 - 1, q + sy);
-  visit(i < V.n1 - 1, q + sx);
-  return (double)d * V.x[q] - off;
+  auto row = [&](bool inside, uint32_t qq) {
+    if (!inside) return;
+    const uchar4 f = ldflags4(V.flags + qq);
+    T v[4];
+    src.load4(qq, v);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) take(c, lane(f, c), v[c]);
+  };
+  row(i > 0, q - sx);
+  row(j > 0, q - sy);
+  // k - 1
+  if (k0 > 0) take(0, V.flags[q - 1], src.load1(q - 1));
+#pragma unroll
+  for (int c = 1; c < 4; ++c) take(c, lane(fc, c - 1), cen[c - 1]);
+  // k + 1
+#pragma unroll
+  for (int c = 0; c < 3; ++c) take(c, lane(fc, c + 1), cen[c + 1]);
+  if (k0 + 4 < V.n3) take(3, V.flags[q + 4], src.load1(q + 4));
+  row(j < V.n2 - 1, q + sy);
+  row(i < V.n1 - 1, q + sx);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) out[c] = lane(fc, c) == MLPCG_FLUID ? T(d[c]) * cen[c] - off[c] : T(0);
+}
+
+__device__ __forceinline__ void group_coords(const Vecs &V, uint32_t g, uint32_t &q, int &i, int &j, int &k0) {
+  q = 4u * g;
+  const uint32_t rowi = fdiv(q, V.fd3);
+  k0 = (int)(q - rowi * (uint32_t)V.n3);
+  const uint32_t ii = fdiv(rowi, V.fd2);
+  j = (int)(rowi - ii * (uint32_t)V.n2);
+  i = (int)ii;
 }
 
 // ---------------------------------------------------------------------------
@@ -173,16 +236,31 @@ __global__ void k_reset(State *st, int max_it, int true_every, int method, doubl
   *st = S;
 }
 
+// r = b - A x in FP64 (b read on fluid cells only); returns sum b^2 and sum r^2
+__device__ __forceinline__ void true_residual_pass(const Vecs &V, double &bb, double &rr) {
+  for (uint32_t g = gtid(); g < V.ngroups; g += gstride()) {
+    uint32_t q; int i, j, k0;
+    group_coords(V, g, q, i, j, k0);
+    double ax[4], xc[4], bq[4];
+    lap4<double>(V, q, i, j, k0, SrcF64{V.x}, ax, xc);
+    ld4(V.b + q, bq);
+    const uchar4 fc = ldflags4(V.flags + q);
+    float rf[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const double b = lane(fc, c) == MLPCG_FLUID ? bq[c] : 0.0;
+      const double r = b - ax[c];
+      rf[c] = (float)r;
+      bb += b * b;
+      rr += r * r;
+    }
+    st4(V.r + q, rf);
+  }
+}
+
 __global__ void __launch_bounds__(RT) k_init(Vecs V) {
   double v[2] = {0.0, 0.0};
-  for (int64_t q = gtid(); q < V.n; q += gstride()) {
-    const double bq = V.flags[q] == MLPCG_FLUID ? V.b[q] : 0.0;
-    const double rq = bq - lap_at_f64(V, q);
-    const float rf = (float)rq;
-    V.r[q] = rf;
-    v[0] += bq * bq;
-    v[1] += (double)rf * rf;
-  }
+  true_residual_pass(V, v[0], v[1]);
   double o[2];
   if (reduce_last<2>(v, V, 0, o) && threadIdx.x == 0) {
     State &S = *V.st;
@@ -223,16 +301,23 @@ __global__ void __launch_bounds__(RT) k_sd_dots(Vecs V) {
     return;
   }
   const int h = S.head, hp = (h + 2) % 3;
-  const float *A1 = V.Ap + (int64_t)h * V.n, *A0 = V.Ap + (int64_t)hp * V.n;
+  const float *A1 = V.Ap + (size_t)h * V.n, *A0 = V.Ap + (size_t)hp * V.n;
   const bool two = it >= 2;
   double v[2] = {0.0, 0.0};
-  float s1 = 0.f, s0 = 0.f;
   int cnt = 0;
-  for (int64_t q = gtid(); q < V.n; q += gstride()) {
-    const float zq = V.z[q];
-    s1 = fmaf(zq, A1[q], s1);
-    if (two) s0 = fmaf(zq, A0[q], s0);
-    if (++cnt == 16) { v[0] += s1; v[1] += s0; s1 = s0 = 0.f; cnt = 0; }
+  float s1 = 0.f, s0 = 0.f;
+  for (uint32_t g = gtid(); g < V.ngroups; g += gstride()) {
+    float z[4], a[4];
+    ld4(V.z + 4 * g, z);
+    ld4(A1 + 4 * g, a);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) s1 = fmaf(z[c], a[c], s1);
+    if (two) {
+      ld4(A0 + 4 * g, a);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) s0 = fmaf(z[c], a[c], s0);
+    }
+    if (++cnt == 8) { v[0] += s1; v[1] += s0; s1 = s0 = 0.f; cnt = 0; }
   }
   v[0] += s1; v[1] += s0;
   double o[2];
@@ -251,14 +336,23 @@ __global__ void __launch_bounds__(RT) k_sd_qform(Vecs V) {
   if (S.status != ST_RUNNING) return;
   const int h = S.head, hp = (h + 2) % 3, hn = (h + 1) % 3;
   const float c1 = (float)S.c1, c0 = (float)S.c0;
-  const float *P1 = V.p + (int64_t)h * V.n, *P0 = V.p + (int64_t)hp * V.n;
-  float *Q = V.p + (int64_t)hn * V.n;
+  const float *P1 = V.p + (size_t)h * V.n, *P0 = V.p + (size_t)hp * V.n;
+  float *Q = V.p + (size_t)hn * V.n;
   const int it = S.it;
-  for (int64_t q = gtid(); q < V.n; q += gstride()) {
-    float v = V.z[q];
-    if (it >= 1) v = fmaf(-c1, P1[q], v);
-    if (it >= 2) v = fmaf(-c0, P0[q], v);
-    Q[q] = v;
+  for (uint32_t g = gtid(); g < V.ngroups; g += gstride()) {
+    float v[4], w[4];
+    ld4(V.z + 4 * g, v);
+    if (it >= 1) {
+      ld4(P1 + 4 * g, w);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) v[c] = fmaf(-c1, w[c], v[c]);
+    }
+    if (it >= 2) {
+      ld4(P0 + 4 * g, w);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) v[c] = fmaf(-c0, w[c], v[c]);
+    }
+    st4(Q + 4 * g, v);
   }
 }
 
@@ -267,20 +361,31 @@ __global__ void __launch_bounds__(RT) k_sd_spmv(Vecs V) {
   const State &S = *V.st;
   if (S.status != ST_RUNNING) return;
   const int h = S.head, hn = (h + 1) % 3;
-  const float *Q = V.p + (int64_t)hn * V.n, *P1 = V.p + (int64_t)h * V.n;
-  float *AQ = V.Ap + (int64_t)hn * V.n;
+  const float *Q = V.p + (size_t)hn * V.n, *P1 = V.p + (size_t)h * V.n;
+  float *AQ = V.Ap + (size_t)hn * V.n;
   const bool has_prev = S.it >= 1;
   double v[3] = {0.0, 0.0, 0.0};
   float s[3] = {0.f, 0.f, 0.f};
   int cnt = 0;
-  for (int64_t q = gtid(); q < V.n; q += gstride()) {
-    const float aq = lap_at(V, q, [&](int64_t m) { return Q[m]; });
-    AQ[q] = aq;
-    const float qq = Q[q];
-    s[0] = fmaf(qq, aq, s[0]);
-    s[1] = fmaf(qq, V.r[q], s[1]);
-    if (has_prev) s[2] = fmaf(aq, P1[q], s[2]);
-    if (++cnt == 16) { v[0] += s[0]; v[1] += s[1]; v[2] += s[2]; s[0] = s[1] = s[2] = 0.f; cnt = 0; }
+  for (uint32_t g = gtid(); g < V.ngroups; g += gstride()) {
+    uint32_t q; int i, j, k0;
+    group_coords(V, g, q, i, j, k0);
+    float aq[4], qq[4], rq[4];
+    lap4<float>(V, q, i, j, k0, SrcF32{Q}, aq, qq);
+    st4(AQ + q, aq);
+    ld4(V.r + q, rq);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      s[0] = fmaf(qq[c], aq[c], s[0]);
+      s[1] = fmaf(qq[c], rq[c], s[1]);
+    }
+    if (has_prev) {
+      float p1[4];
+      ld4(P1 + q, p1);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) s[2] = fmaf(aq[c], p1[c], s[2]);
+    }
+    if (++cnt == 8) { v[0] += s[0]; v[1] += s[1]; v[2] += s[2]; s[0] = s[1] = s[2] = 0.f; cnt = 0; }
   }
   v[0] += s[0]; v[1] += s[1]; v[2] += s[2];
   double o[3];
@@ -303,9 +408,13 @@ __global__ void __launch_bounds__(RT) k_cg_rz(Vecs V) {
   double v[1] = {0.0};
   float s = 0.f;
   int cnt = 0;
-  for (int64_t q = gtid(); q < V.n; q += gstride()) {
-    s = fmaf(V.r[q], V.z[q], s);
-    if (++cnt == 16) { v[0] += s; s = 0.f; cnt = 0; }
+  for (uint32_t g = gtid(); g < V.ngroups; g += gstride()) {
+    float r[4], z[4];
+    ld4(V.r + 4 * g, r);
+    ld4(V.z + 4 * g, z);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) s = fmaf(r[c], z[c], s);
+    if (++cnt == 8) { v[0] += s; s = 0.f; cnt = 0; }
   }
   v[0] += s;
   double o[1];
@@ -322,21 +431,21 @@ __global__ void __launch_bounds__(RT) k_cg_pspmv(Vecs V) {
   const State &S = *V.st;
   if (S.status != ST_RUNNING) return;
   const int cur = S.pp, nxt = cur ^ 1;
-  const float *Po = V.p + (int64_t)cur * V.n;
-  float *Pn = V.p + (int64_t)nxt * V.n;
-  const float bt = (float)S.c1;
-  const bool first = S.it == 0;
-  auto pnew = [&](int64_t m) { return first ? V.z[m] : fmaf(bt, Po[m], V.z[m]); };
+  float *Pn = V.p + (size_t)nxt * V.n;
+  const SrcAxpy src{V.z, V.p + (size_t)cur * V.n, (float)S.c1, S.it == 0};
   double v[1] = {0.0};
   float s = 0.f;
   int cnt = 0;
-  for (int64_t q = gtid(); q < V.n; q += gstride()) {
-    const float pq = pnew(q);
-    Pn[q] = pq;
-    const float w = lap_at(V, q, pnew);
-    V.Ap[q] = w;
-    s = fmaf(pq, w, s);
-    if (++cnt == 16) { v[0] += s; s = 0.f; cnt = 0; }
+  for (uint32_t g = gtid(); g < V.ngroups; g += gstride()) {
+    uint32_t q; int i, j, k0;
+    group_coords(V, g, q, i, j, k0);
+    float w[4], pc[4];
+    lap4<float>(V, q, i, j, k0, src, w, pc);
+    st4(Pn + q, pc);
+    st4(V.Ap + q, w);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) s = fmaf(pc[c], w[c], s);
+    if (++cnt == 8) { v[0] += s; s = 0.f; cnt = 0; }
   }
   v[0] += s;
   double o[1];
@@ -356,10 +465,10 @@ __global__ void __launch_bounds__(RT) k_update(Vecs V) {
   if (S.status != ST_RUNNING) return;
   const float *D, *AD;
   if (S.method == M_NPSD) {
-    D = V.p + (int64_t)S.head * V.n;
-    AD = V.Ap + (int64_t)S.head * V.n;
+    D = V.p + (size_t)S.head * V.n;
+    AD = V.Ap + (size_t)S.head * V.n;
   } else {
-    D = V.p + (int64_t)S.pp * V.n;
+    D = V.p + (size_t)S.pp * V.n;
     AD = V.Ap;
   }
   const double bd = S.beta;
@@ -367,12 +476,23 @@ __global__ void __launch_bounds__(RT) k_update(Vecs V) {
   double v[1] = {0.0};
   float s = 0.f;
   int cnt = 0;
-  for (int64_t q = gtid(); q < V.n; q += gstride()) {
-    V.x[q] = fma(bd, (double)D[q], V.x[q]);
-    const float rq = fmaf(-bf, AD[q], V.r[q]);
-    V.r[q] = rq;
-    s = fmaf(rq, rq, s);
-    if (++cnt == 16) { v[0] += s; s = 0.f; cnt = 0; }
+  for (uint32_t g = gtid(); g < V.ngroups; g += gstride()) {
+    const uint32_t q = 4u * g;
+    float d[4], ad[4], r[4];
+    double x[4];
+    ld4(D + q, d);
+    ld4(AD + q, ad);
+    ld4(V.r + q, r);
+    ld4(V.x + q, x);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      x[c] = fma(bd, (double)d[c], x[c]);
+      r[c] = fmaf(-bf, ad[c], r[c]);
+      s = fmaf(r[c], r[c], s);
+    }
+    st4(V.x + q, x);
+    st4(V.r + q, r);
+    if (++cnt == 8) { v[0] += s; s = 0.f; cnt = 0; }
   }
   v[0] += s;
   double o[1];
@@ -391,15 +511,10 @@ __global__ void __launch_bounds__(RT) k_update(Vecs V) {
 __global__ void __launch_bounds__(RT) k_true_residual(Vecs V) {
   const State &S = *V.st;
   if (S.status != ST_RUNNING || !S.need_true) return;
-  double v[1] = {0.0};
-  for (int64_t q = gtid(); q < V.n; q += gstride()) {
-    const double bq = V.flags[q] == MLPCG_FLUID ? V.b[q] : 0.0;
-    const double rq = bq - lap_at_f64(V, q);
-    V.r[q] = (float)rq;
-    v[0] += rq * rq;
-  }
-  double o[1];
-  if (reduce_last<1>(v, V, 0, o) && threadIdx.x == 0) V.st->rr_true = o[0];
+  double v[2] = {0.0, 0.0};
+  true_residual_pass(V, v[0], v[1]);
+  double o[2];
+  if (reduce_last<2>(v, V, 0, o) && threadIdx.x == 0) V.st->rr_true = o[1];
 }
 
 // one thread: iteration bookkeeping, convergence, loop condition
@@ -441,6 +556,17 @@ struct mlpcg_solver {
 };
 
 static size_t al256s(size_t b) { return (b + 255) / 256 * 256; }
+
+static FastDiv make_fastdiv(uint32_t d) {
+  int l = 0;
+  while ((1ull << l) < d) ++l;  // ceil(log2 d)
+  const uint64_t m = ((1ull << 32) * ((1ull << l) - d)) / d + 1;
+  FastDiv f;
+  f.m = (uint32_t)m;
+  f.s1 = l < 1 ? (uint32_t)l : 1u;
+  f.s2 = l > 1 ? (uint32_t)(l - 1) : 0u;
+  return f;
+}
 
 static size_t solver_layout(mlpcg_solver &s, char *base) {
   size_t off = 0;
@@ -501,6 +627,8 @@ int mlpcg_solver_create(int N1, int N2, int N3, const mlpcg_precond *plan, int m
   MLPCG_REQUIRE(max_it >= 1 && max_it <= 1000000, MLPCG_ERR_ARG, "solver_create: max_it out of range");
   MLPCG_REQUIRE(tol > 0.0, MLPCG_ERR_ARG, "solver_create: tol must be > 0");
   MLPCG_REQUIRE(N1 >= 1 && N2 >= 1 && N3 >= 1, MLPCG_ERR_SHAPE, "solver_create: bad grid");
+  MLPCG_REQUIRE(N3 % 4 == 0, MLPCG_ERR_SHAPE, "solver_create: N3 (%d) must be a multiple of 4", N3);
+  MLPCG_REQUIRE(cells(N1, N2, N3) < ((int64_t)1 << 31), MLPCG_ERR_SHAPE, "solver_create: grid must have < 2^31 cells");
   auto *s = new mlpcg_solver();
   s->n1 = N1; s->n2 = N2; s->n3 = N3;
   s->method = method; s->max_it = max_it; s->tol = tol; s->true_every = true_every;
@@ -532,7 +660,10 @@ int mlpcg_solver_bind(mlpcg_solver *s, void *workspace, size_t workspace_bytes, 
   V.flags = flags; V.b = b; V.x = x;
   V.n1 = s->n1; V.n2 = s->n2; V.n3 = s->n3;
   V.n = cells(s->n1, s->n2, s->n3);
-  int64_t nb = (V.n + RT * 8 - 1) / (RT * 8);
+  V.ngroups = (uint32_t)(V.n / 4);
+  V.fd3 = make_fastdiv((uint32_t)s->n3);
+  V.fd2 = make_fastdiv((uint32_t)s->n2);
+  int64_t nb = ((int64_t)V.ngroups + RT * 2 - 1) / (RT * 2);
   V.nblk = (int)(nb < 1 ? 1 : (nb > RB_MAX ? RB_MAX : nb));
   s->bound = true;
   return MLPCG_OK;

@@ -1,7 +1,9 @@
 """Training of SmallSMModelDn3D through the hand-written adjoint kernels (the reference's train.py).
 
 Loss (per right-hand side b of unit norm, x = f(b) restricted to fluid cells):
-  * ``squared`` (default): ||b - A x||^2 / ||b||^2, averaged over the batch;
+  * ``angle`` (default): 1 - cos^2(b, A x), the squared relative residual at
+    the best output scale (npsd / npcg do not see the scale of M);
+  * ``squared``: ||b - A x||^2 / ||b||^2, averaged over the batch;
   * ``reference``: ||b - A x|| averaged over the batch (residual_loss,
     loss_functions.py:18-23).
 Right-hand sides: random combinations of the lowest Lanczos Ritz vectors of
@@ -51,24 +53,24 @@ def _lap_batch(flags, x):
     return out.reshape(shp)
 
 
-def residual_loss(model, image, flags, fluid, b, kind="step"):
+def residual_loss(model, image, flags, fluid, b, kind="angle"):
     """b: (B, N1, N2, N3) unit-norm on fluid cells, zero elsewhere.
 
     kind = "squared":   ||b - A x||^2 / ||b||^2
            "reference": ||b - A x||  (residual_loss, loss_functions.py:18-23)
-           "step":      ||b - beta A x||^2 / ||b||^2 with beta = x.b / x.Ax, the
-                        residual after one exactly line-searched npsd step from 0
-                        (the A-norm scaling of scaled_loss_2, loss_functions.py:45-53);
-                        invariant to the scale of the network output, like npsd.
+           "angle":     min_s ||b - s A x||^2 / ||b||^2 = 1 - cos^2(b, A x): the
+                        squared relative residual at the best scale of the output,
+                        in [0, 1]; invariant to the scale of the network output,
+                        like npsd and npcg are.
     """
     x = model(image, b[:, None])[:, 0]
     x = x * fluid
     Ax = LaplacianFunction.apply(flags, x)
-    bf, xf, Af = b.flatten(1), x.flatten(1), Ax.flatten(1)
-    if kind == "step":
-        beta = (xf * bf).sum(1, keepdim=True) / (xf * Af).sum(1, keepdim=True)
-        r = bf - beta * Af
-        return (r.pow(2).sum(1) / bf.pow(2).sum(1)).mean()
+    bf, Af = b.flatten(1), Ax.flatten(1)
+    if kind == "angle":
+        num = (Af * bf).sum(1).pow(2)
+        den = Af.pow(2).sum(1) * bf.pow(2).sum(1)
+        return (1.0 - num / den.clamp_min(1e-30)).mean()
     r = bf - Af
     if kind == "reference":
         return r.norm(dim=1).mean()
@@ -85,7 +87,7 @@ def near_identity_(model, eps=0.1):
 
 
 class TrainScene:
-    def __init__(self, shape, seed, device, n_ritz=64, lanczos_steps=1600, spheres=3):
+    def __init__(self, shape, seed, device, n_ritz=64, lanczos_steps=1600, spheres=3, cache_dir=None):
         s = make_scene(shape, seed, spheres)
         self.seed = seed
         self.flags = torch.as_tensor(s.flags, device=device)
@@ -95,7 +97,17 @@ class TrainScene:
         self.rhs = torch.as_tensor(s.rhs, device=device)
         v0 = self.rhs.reshape(-1)[self.A.fluid_cells]
         t = time.time()
-        self.ritz_vals, ritz = lanczos_ritz(self.A, v0, lanczos_steps, n_ritz)
+        shp = "x".join(str(d) for d in self.flags.shape)
+        cache = Path(cache_dir) / f"ritz_{shp}_s{seed}_k{n_ritz}_m{lanczos_steps}.pt" if cache_dir else None
+        if cache is not None and cache.exists():
+            d = torch.load(cache, map_location=device)
+            self.ritz_vals, ritz = d["vals"].cpu().numpy(), d["vecs"]
+        else:
+            self.ritz_vals, ritz = lanczos_ritz(self.A, v0, lanczos_steps, n_ritz)
+            ritz = ritz.float()
+            if cache is not None:
+                cache.parent.mkdir(parents=True, exist_ok=True)
+                torch.save({"vals": torch.as_tensor(self.ritz_vals), "vecs": ritz}, cache)
         self.lanczos_s = time.time() - t
         self.ritz = ritz.float()
         self.n = self.flags.numel()
@@ -138,7 +150,7 @@ def main(argv=None):
     ap.add_argument("--lr", type=float, default=3e-3)
     ap.add_argument("--lr-min", type=float, default=1e-4)
     ap.add_argument("--noise-frac", type=float, default=0.25)
-    ap.add_argument("--loss", default="step", choices=["step", "squared", "reference"])
+    ap.add_argument("--loss", default="angle", choices=["angle", "squared", "reference"])
     ap.add_argument("--init-mode", default="near-identity", choices=["near-identity", "reference"])
     ap.add_argument("--init-eps", type=float, default=0.1)
     ap.add_argument("--lanczos-steps", type=int, default=1600)
@@ -147,6 +159,7 @@ def main(argv=None):
     ap.add_argument("--eval-seed", type=int, default=18)
     ap.add_argument("--init", default=None, help="npz state dict to start from")
     ap.add_argument("--time-limit", type=float, default=1e9, help="seconds of training loop at most")
+    ap.add_argument("--ritz-cache", default=None, help="directory caching the Lanczos Ritz vectors")
     args = ap.parse_args(argv)
 
     dev = torch.device("cuda")
@@ -160,7 +173,8 @@ def main(argv=None):
     elif args.init_mode == "near-identity":
         near_identity_(model, args.init_eps)
     t0 = time.time()
-    scenes = [TrainScene(args.size, s, dev, args.n_ritz, args.lanczos_steps) for s in parse_seeds(args.seeds)]
+    scenes = [TrainScene(args.size, s, dev, args.n_ritz, args.lanczos_steps, cache_dir=args.ritz_cache)
+              for s in parse_seeds(args.seeds)]
     val = TrainScene(args.size, args.eval_seed, dev, 8, 16)
     prep_s = time.time() - t0
     print(f"prepared {len(scenes)} scenes in {prep_s:.1f}s (lanczos {[round(s.lanczos_s, 1) for s in scenes]})",
