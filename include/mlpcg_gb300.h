@@ -330,6 +330,25 @@ size_t mlpcg_dot_workspace(int64_t n);
 int mlpcg_dot(const void *x, const void *y, int dtype, int64_t n, double *out,
               void *workspace, size_t workspace_bytes, void *stream);
 
+/*
+ * mlpcg_dot without a workspace (no counterpart in the reference).  For
+ * callers that cannot allocate device memory: code running while a stream
+ * is captured in global or thread-local mode (where cudaMalloc is not
+ * permitted), real-time loops that must not enter an allocator, and host
+ * runtimes that own all device memory and forbid library allocations.
+ * The block partial sums live in a 64 KiB file-scope device array of this
+ * library (one partial per 2048 elements), so n <= 16,777,216; larger n is
+ * rejected with MLPCG_ERR_SHAPE and a message.  It calls no cudaMalloc,
+ * cudaFree or allocating routine.  The first call on each device looks up
+ * the array's device address (cudaGetSymbolAddress, with that device
+ * current): make that first call before any stream capture.  Every call
+ * shares the one array, so calls that overlap on the GPU (different streams
+ * without ordering) race; nothing in it needs clearing between calls, since
+ * each call writes every partial it reads.  Every GPU that loads the library
+ * holds the 64 KiB until the process exits.
+ */
+int mlpcg_dot_noalloc(const void *x, const void *y, int dtype, int64_t n, double *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -59,6 +59,7 @@ _PROTOS = {
     "mlpcg_flags_to_image": (_i, [_u8p, _fp, _i64, _vp]),
     "mlpcg_dot_workspace": (_sz, [_i64]),
     "mlpcg_dot": (_i, [_vp, _vp, _i, _i64, _vp, _vp, _sz, _vp]),
+    "mlpcg_dot_noalloc": (_i, [_vp, _vp, _i, _i64, _vp, _vp]),
 }
 
 

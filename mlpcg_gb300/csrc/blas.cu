@@ -1,5 +1,6 @@
 // Deterministic reductions: per-thread FP32 partial sums over short runs,
 // FP64 across threads and blocks, block partials summed in a fixed order.
+#include <mutex>
 #include "common.cuh"
 
 namespace mlpcg {
@@ -70,4 +71,74 @@ int launch_dot(const void *x, const void *y, int dt, int64_t n, double *out, voi
   return MLPCG_OK;
 }
 
+// ---------------------------------------------------------------------------
+// mlpcg_dot_noalloc: the same reduction with its block partials in a
+// file-scope device array instead of a caller workspace, for callers that
+// cannot allocate device memory: code that runs while a stream is being
+// captured in global or thread-local mode (cudaMalloc is not permitted
+// there), real-time loops that must never enter the allocator, and host
+// runtimes that own all device memory through their own arena and forbid
+// libraries from allocating.  One partial per 2048 elements, at most 8192
+// partials (64 KiB), so n <= 16,777,216 (a 256^3 grid).  Every GPU that
+// loads this library holds the 64 KiB until the process exits.
+// ---------------------------------------------------------------------------
+constexpr int kNoAllocPartials = 8192;
+constexpr int kNoAllocPerBlock = 2048;
+constexpr int64_t kNoAllocMaxN = (int64_t)kNoAllocPartials * kNoAllocPerBlock;
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) double g_noalloc_partials[kNoAllocPartials];
+
+// Device address of g_noalloc_partials, looked up once per device.  In host
+// code the array's name is only a host-side stand-in, so the address must
+// come from cudaGetSymbolAddress with that device current.
+static std::mutex g_noalloc_mu;
+static double *g_noalloc_ptr[kNoAllocMaxDevices];
+
+static int noalloc_scratch(double **out) {
+  int dev = 0;
+  MLPCG_CUDA_CHECK(cudaGetDevice(&dev));
+  MLPCG_REQUIRE(dev >= 0 && dev < kNoAllocMaxDevices, MLPCG_ERR_UNSUPPORTED,
+                "dot_noalloc: device ordinal %d beyond %d", dev, kNoAllocMaxDevices);
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void *p = nullptr;
+    MLPCG_CUDA_CHECK(cudaGetSymbolAddress(&p, g_noalloc_partials));
+    g_noalloc_ptr[dev] = static_cast<double *>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return MLPCG_OK;
+}
+
+int launch_dot_noalloc(const void *x, const void *y, int dt, int64_t n, double *out, cudaStream_t st) {
+  MLPCG_REQUIRE(n <= kNoAllocMaxN, MLPCG_ERR_SHAPE,
+                "dot_noalloc: n = %lld exceeds the maximum of %lld elements (%d partial sums in the "
+                "library's static scratch); use mlpcg_dot with a workspace",
+                (long long)n, (long long)kNoAllocMaxN, kNoAllocPartials);
+  double *part = nullptr;
+  const int rc = noalloc_scratch(&part);
+  if (rc != MLPCG_OK) return rc;
+  // every one of the nb partials is written before it is read: nothing to clear
+  const int nb = (int)((n + kNoAllocPerBlock - 1) / kNoAllocPerBlock);
+  if (dt == MLPCG_F32)
+    k_dot_partial<float><<<nb, kDotThreads, 0, st>>>((const float *)x, (const float *)y, n, part);
+  else if (dt == MLPCG_F64)
+    k_dot_partial<double><<<nb, kDotThreads, 0, st>>>((const double *)x, (const double *)y, n, part);
+  else
+    k_dot_partial<__nv_bfloat16><<<nb, kDotThreads, 0, st>>>((const __nv_bfloat16 *)x, (const __nv_bfloat16 *)y,
+                                                            n, part);
+  MLPCG_LAUNCH_CHECK();
+  k_sum_partials<<<1, 256, 0, st>>>(part, nb, out);
+  MLPCG_LAUNCH_CHECK();
+  return MLPCG_OK;
+}
+
 }  // namespace mlpcg
+
+extern "C" int mlpcg_dot_noalloc(const void *x, const void *y, int dtype, int64_t n, double *out, void *stream) {
+  mlpcg::clear_error();
+  MLPCG_REQUIRE(x && y && out, MLPCG_ERR_ARG, "dot_noalloc: NULL argument");
+  MLPCG_REQUIRE(mlpcg::valid_dtype(dtype), MLPCG_ERR_UNSUPPORTED, "dot_noalloc: bad dtype %d", dtype);
+  MLPCG_REQUIRE(n >= 1, MLPCG_ERR_ARG, "dot_noalloc: n must be >= 1");
+  return mlpcg::launch_dot_noalloc(x, y, dtype, n, out, mlpcg::as_stream(stream));
+}
