@@ -261,7 +261,8 @@ def run_ours(args, rank, world):
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     hbm = peaks.get("hbm_gbs", 6800.0)
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    bytes_pre0 = n * (27 * 2 + 4 + 2 + 0.25)   # K (bf16), r in (f32), y out (bf16), pooled out (bf16)
+    gen = [plan.general_cells(l) for l in range(plan.levels + 1)]
+    bytes_pre0 = coeff_bytes(plan, 0, n, gen[0]) + n * (4 + 2 + 0.25)   # coefficients, r in, y out, pooled out
     achieved = bytes_pre0 / (stage_ms["pre0"] * 1e-3) / 1e9
     traffic = None
     tp = ROOT / "profiles" / "traffic.json"
@@ -269,12 +270,12 @@ def run_ours(args, rank, world):
         tj = json.loads(tp.read_text())
         if "pre0_bytes_per_cell" in tj:
             traffic = tj["pre0_bytes_per_cell"] * n
-    roofline = {"kernel": "k_pre_fused (level 0, bf16 coefficients)", "bound": "hbm",
+    roofline = {"kernel": f"k_pre_fused (level 0, {plan.layout} bf16 coefficients)", "bound": "hbm",
                 "achieved": round(achieved, 1), "peak": hbm, "peak_source": peak_src, "unit": "GB/s",
                 "frac": round(achieved / hbm, 4), "traffic": traffic,
-                "algorithmic_bytes": bytes_pre0}
+                "algorithmic_bytes": bytes_pre0, "general_cells": gen}
     # whole-iteration bytes (compulsory traffic of the fused algorithm)
-    per_iter_bytes = iteration_bytes(plan, n)
+    per_iter_bytes = iteration_bytes(plan, n, gen)
     it_mean = statistics.mean(its)
 
     # ---- e2e: public API from pinned host buffers ----
@@ -313,17 +314,26 @@ def run_ours(args, rank, world):
     return out
 
 
-def iteration_bytes(plan, n0):
+def coeff_bytes(plan, level, n_level, general):
+    """Coefficient bytes one block application reads at a level (bf16)."""
+    if general is None or general < 0:
+        return n_level * 27 * 2                         # dense planes
+    tiles = math.ceil(n_level / (2 * 16 * 64))
+    return n_level * 1 + general * 32 * 2 + tiles * 4   # class bytes, general-cell records, tile offsets
+
+
+def iteration_bytes(plan, n0, gen):
     """Compulsory HBM bytes of one fused npsd iteration (bf16 coefficients and activations)."""
     total = 0.0
     L = plan.levels
     for l in range(L):
         nl = n0 / 8 ** l
+        kb = coeff_bytes(plan, l, nl, gen[l])
         sv_in = 4 if l == 0 else 2
-        total += nl * (27 * 2 + sv_in + 2 + 2 / 8)        # pre: K, x in, y out, pooled out
-        total += nl * (27 * 2 + 2 / 8 + 2 + (4 + 1 if l == 0 else 2))  # post: K, coarse, y, out (+mask)
-    total += (n0 / 8 ** L) * (27 * 2 + 2 + 2)
-    total += n0 * (12 + 16 + 25 + 32)                   # dots, qform, spmv+dots, update (f32 vectors, f64 x)
+        total += kb + nl * (sv_in + 2 + 2 / 8)                  # pre: coefficients, x in, y out, pooled out
+        total += kb + nl * (2 / 8 + 2 + (4 + 1 if l == 0 else 2))  # post: coefficients, coarse, y, out (+mask)
+    total += coeff_bytes(plan, L, n0 / 8 ** L, gen[L]) + (n0 / 8 ** L) * (2 + 2)
+    total += n0 * (12 + 16 + 18 + 32)                   # dots, qform, spmv+dots, update (f32 vectors, f64 x)
     return total
 
 

@@ -238,12 +238,26 @@ int mlpcg_laplacian_apply(const uint8_t *flags, const void *x, void *y, int dtyp
  * ========================================================================= */
 typedef struct mlpcg_precond mlpcg_precond;
 
+/* Coefficient layouts of a plan.
+ * DENSE:   27 planes per block (27 values per cell).
+ * CLASSED: one class byte per cell; cells whose 3x3x3 image neighbourhood is
+ *          a single one-hot material (solid or outside, air, fluid) use that
+ *          material's constant coefficient vector, the others ("general"
+ *          cells, near interfaces) a 32-value record.  Bit-identical results,
+ *          far less coefficient traffic on scenes made of large regions. */
+#define MLPCG_COEFF_DENSE   0
+#define MLPCG_COEFF_CLASSED 1
+
 /* Host-side plan for an N1 x N2 x N3 grid (each divisible by 2^levels).
  * k_dtype / act_dtype: storage of coefficients / level activations, F32 or
  * BF16 (arithmetic is FP32).  swap_sm_order and mask have the meaning of the
- * SmallSMModelDn3D constructor arguments. */
+ * SmallSMModelDn3D constructor arguments.  coeff_layout: MLPCG_COEFF_*
+ * (levels whose z size is not a multiple of 8 always use dense planes). */
 int mlpcg_precond_create(int N1, int N2, int N3, int levels, int k_dtype, int act_dtype,
-                         int swap_sm_order, int mask, mlpcg_precond **out);
+                         int swap_sm_order, int mask, int coeff_layout, mlpcg_precond **out);
+/* Number of general cells of a classed level after setup (synchronises
+ * `stream`); -1 for a dense level. */
+int mlpcg_precond_general_cells(const mlpcg_precond *plan, int level, int64_t *count, void *stream);
 /* Device bytes the plan needs (caller allocates, 256-byte aligned). */
 size_t mlpcg_precond_workspace(const mlpcg_precond *plan);
 void mlpcg_precond_destroy(mlpcg_precond *plan);

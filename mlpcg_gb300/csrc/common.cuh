@@ -94,4 +94,49 @@ struct FieldGeom {
   }
 };
 
+// ---------------------------------------------------------------------------
+// The 27 coefficients of one cell: acc[p] = bias[p] + sum_{s,m,n,o} W[p][s][m][n][o] * v(s,m,n,o)
+// with v the image patch around the cell (v(s,m,n,o) = img(s, q + (m-1,n-1,o-1))).
+// sW[(s*27 + 9m+3n+o)*7 + pp] holds W[4pp..4pp+3][s][m][n][o] (p padded to 28),
+// sb[p] the bias.  The summation order (bias, then s, m, n, o) is the order of
+// the reference's loop (sm_block_3d_kernel.cu:53-64); every kernel that
+// produces coefficients goes through this one function, so equal patches give
+// bit-identical coefficients whichever kernel computed them.
+// ---------------------------------------------------------------------------
+template <typename Patch>
+__device__ __forceinline__ void coeffs_of_patch(const float4 *sW, const float *sb, Patch v, float acc[28]) {
+#pragma unroll
+  for (int p = 0; p < 28; ++p) acc[p] = sb[p];
+  for (int s = 0; s < 3; ++s) {
+#pragma unroll
+    for (int m = 0; m < 3; ++m)
+#pragma unroll
+      for (int nn = 0; nn < 3; ++nn)
+#pragma unroll
+        for (int o = 0; o < 3; ++o) {
+          const float x = v(s, m, nn, o);
+          const float4 *w = sW + (s * 27 + m * 9 + nn * 3 + o) * 7;
+#pragma unroll
+          for (int pp = 0; pp < 7; ++pp) {
+            const float4 wv = w[pp];
+            acc[4 * pp + 0] = fmaf(wv.x, x, acc[4 * pp + 0]);
+            acc[4 * pp + 1] = fmaf(wv.y, x, acc[4 * pp + 1]);
+            acc[4 * pp + 2] = fmaf(wv.z, x, acc[4 * pp + 2]);
+            acc[4 * pp + 3] = fmaf(wv.w, x, acc[4 * pp + 3]);
+          }
+        }
+  }
+}
+
+// Loads W (27 x 81) and bias (27) into the shared-memory layout of coeffs_of_patch.
+__device__ __forceinline__ void load_weights_smem(const float *__restrict__ W, const float *__restrict__ bias,
+                                                  float4 *sW, float *sb) {
+  float *sWf = reinterpret_cast<float *>(sW);
+  for (int t = threadIdx.x; t < 81 * 28; t += blockDim.x) {
+    const int so = t / 28, p = t % 28;
+    sWf[t] = p < 27 ? W[p * 81 + so] : 0.f;
+  }
+  if (threadIdx.x < 28) sb[threadIdx.x] = threadIdx.x < 27 ? bias[threadIdx.x] : 0.f;
+}
+
 }  // namespace mlpcg

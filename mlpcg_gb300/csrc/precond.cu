@@ -103,14 +103,333 @@ __device__ __forceinline__ void apply_run(const float (*S)[HY][HZ], int tx, int 
 }
 
 // ---------------------------------------------------------------------------
+// Classed coefficients.  A block's 27 coefficients at a cell depend only on
+// the 3 x 27 image values around it.  Where those are all one of the three
+// one-hot materials -- solid (or outside the grid) (0,0,0), air (1,0,1),
+// fluid (0,1,1) -- the coefficients are the block's constant vector for that
+// material; only the remaining ("general") cells, near material interfaces,
+// need their own 27 values.  A classed level stores one class byte per cell
+// (shared by the level's blocks), per tile the index of its first general
+// cell, and per block the 3 uniform vectors plus one 32-wide record per
+// general cell, laid out tile by tile in the apply kernels' thread/cell order.
+// Results equal those of the dense planes bit for bit: coeffs_of_patch
+// produces every value and the 27 taps are summed in the same order.
+// ---------------------------------------------------------------------------
+enum { CLS_SOLID = 0, CLS_AIR = 1, CLS_FLUID = 2, CLS_GENERAL = 3 };
+constexpr int KREC = 32;
+
+__device__ __forceinline__ int material_of(float a, float f, float s) {
+  if (a == 0.f && f == 0.f && s == 0.f) return CLS_SOLID;
+  if (a == 1.f && f == 0.f && s == 1.f) return CLS_AIR;
+  if (a == 0.f && f == 1.f && s == 1.f) return CLS_FLUID;
+  return CLS_GENERAL;
+}
+// channel s of the one-hot image value of material cls
+__device__ __forceinline__ float material_channel(int cls, int s) {
+  if (cls == CLS_AIR) return s != 1 ? 1.f : 0.f;
+  if (cls == CLS_FLUID) return s != 0 ? 1.f : 0.f;
+  return 0.f;
+}
+
+__device__ __forceinline__ int cell_class(const float *__restrict__ img, int n1, int n2, int n3, int64_t n, int i,
+                                          int j, int k) {
+  int cls = -1;
+  for (int o = 0; o < 27; ++o) {
+    const int ii = i + o / 9 - 1, jj = j + (o / 3) % 3 - 1, kk = k + o % 3 - 1;
+    int c = CLS_SOLID;
+    if ((unsigned)ii < (unsigned)n1 && (unsigned)jj < (unsigned)n2 && (unsigned)kk < (unsigned)n3) {
+      const int64_t q = ((int64_t)ii * n2 + jj) * n3 + kk;
+      c = material_of(img[q], img[n + q], img[2 * n + q]);
+    }
+    if (c == CLS_GENERAL) return CLS_GENERAL;
+    if (cls < 0) cls = c;
+    else if (c != cls) return CLS_GENERAL;
+  }
+  return cls;
+}
+
+// exclusive scan of one int per thread over the PT threads of a CTA
+__device__ __forceinline__ int cta_excl_scan(int v, int &total) {
+  __shared__ int ws[PT / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) ws[w] = x;
+  __syncthreads();
+  int off = 0, tot = 0;
+#pragma unroll
+  for (int i = 0; i < PT / 32; ++i) {
+    if (i < w) off += ws[i];
+    tot += ws[i];
+  }
+  __syncthreads();
+  total = tot;
+  return off + x - v;
+}
+
+__device__ __forceinline__ unsigned tile_id() { return blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z); }
+
+// number of general cells among the 8-cell runs this thread owns
+__device__ __forceinline__ int count_general(const uint8_t *__restrict__ cls, int n1, int n2, int n3) {
+  const int tz = threadIdx.x % ZT, ty = threadIdx.x / ZT;
+  const int k0 = blockIdx.x * TZ + tz * 8, j = blockIdx.y * TY + ty, x0 = blockIdx.z * TX;
+  int cnt = 0;
+  if (k0 < n3 && j < n2) {
+#pragma unroll
+    for (int tx = 0; tx < TX; ++tx) {
+      const int i = x0 + tx;
+      if (i >= n1) continue;
+      const uint2 c = __ldg(reinterpret_cast<const uint2 *>(cls + ((int64_t)i * n2 + j) * n3 + k0));
+#pragma unroll
+      for (int b = 0; b < 4; ++b) {
+        cnt += ((c.x >> (8 * b)) & 0xffu) == CLS_GENERAL;
+        cnt += ((c.y >> (8 * b)) & 0xffu) == CLS_GENERAL;
+      }
+    }
+  }
+  return cnt;
+}
+
+// class byte of every cell, number of general cells per tile
+__global__ void __launch_bounds__(PT)
+k_classify(const float *__restrict__ img, int n1, int n2, int n3, uint8_t *__restrict__ cls,
+           uint32_t *__restrict__ tcount) {
+  const int tz = threadIdx.x % ZT, ty = threadIdx.x / ZT;
+  const int k0 = blockIdx.x * TZ + tz * 8, j = blockIdx.y * TY + ty, x0 = blockIdx.z * TX;
+  const int64_t n = cells(n1, n2, n3);
+  int cnt = 0;
+  if (k0 < n3 && j < n2) {
+    for (int tx = 0; tx < TX; ++tx) {
+      const int i = x0 + tx;
+      if (i >= n1) continue;
+      const int64_t q = ((int64_t)i * n2 + j) * n3 + k0;
+      for (int c = 0; c < 8; ++c) {
+        const int cl = cell_class(img, n1, n2, n3, n, i, j, k0 + c);
+        cls[q + c] = (uint8_t)cl;
+        cnt += cl == CLS_GENERAL;
+      }
+    }
+  }
+  int tot;
+  cta_excl_scan(cnt, tot);
+  if (threadIdx.x == 0) tcount[tile_id()] = (uint32_t)tot;
+}
+
+// exclusive prefix sum of the tile counts (one CTA of 1024 threads)
+__global__ void __launch_bounds__(1024)
+k_scan_tiles(const uint32_t *__restrict__ cnt, uint32_t *__restrict__ base, int ntiles) {
+  __shared__ uint32_t ws[32];
+  __shared__ uint32_t carry;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int start = 0; start < ntiles; start += 1024) {
+    const int idx = start + threadIdx.x;
+    const uint32_t v = idx < ntiles ? cnt[idx] : 0u;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[w] = x;
+    __syncthreads();
+    if (w == 0) {
+      uint32_t s = ws[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+        if (lane >= o) s += y;
+      }
+      ws[lane] = s;
+    }
+    __syncthreads();
+    const uint32_t prefix = carry + (w > 0 ? ws[w - 1] : 0u) + x - v;
+    if (idx < ntiles) base[idx] = prefix;
+    __syncthreads();
+    if (threadIdx.x == 1023) carry = prefix + v;
+    __syncthreads();
+  }
+}
+
+// v rounded to the storage type of the first argument's pointee
+__device__ __forceinline__ float round_as(const float *, float v) { return v; }
+__device__ __forceinline__ float round_as(const __nv_bfloat16 *, float v) {
+  return __bfloat162float(__float2bfloat16_rn(v));
+}
+
+// the block's coefficient vector of each uniform material (rounded like the stored dtype)
+template <typename KT>
+__global__ void k_kgen_uniform(const float *__restrict__ W, const float *__restrict__ bias, float *__restrict__ kuni) {
+  __shared__ float4 sW[81 * 7];
+  __shared__ float sb[28];
+  load_weights_smem(W, bias, sW, sb);
+  __syncthreads();
+  if (threadIdx.x >= 3) return;
+  const int c = threadIdx.x;
+  float acc[28];
+  coeffs_of_patch(sW, sb, [&](int s, int, int, int) { return material_channel(c, s); }, acc);
+#pragma unroll
+  for (int p = 0; p < KREC; ++p) kuni[c * KREC + p] = p < 27 ? round_as((const KT *)nullptr, acc[p]) : 0.f;
+}
+
+// one 32-wide record per general cell, tile by tile in thread/cell order
+template <typename KT>
+__global__ void __launch_bounds__(PT)
+k_kgen_cls(const float *__restrict__ img, int n1, int n2, int n3, const float *__restrict__ W,
+           const float *__restrict__ bias, const uint8_t *__restrict__ cls, const uint32_t *__restrict__ tbase,
+           KT *__restrict__ rec) {
+  __shared__ float4 sW[81 * 7];
+  __shared__ float sb[28];
+  load_weights_smem(W, bias, sW, sb);
+  __syncthreads();
+  int tot;
+  uint32_t rank = tbase[tile_id()] + (uint32_t)cta_excl_scan(count_general(cls, n1, n2, n3), tot);
+  const int tz = threadIdx.x % ZT, ty = threadIdx.x / ZT;
+  const int k0 = blockIdx.x * TZ + tz * 8, j = blockIdx.y * TY + ty, x0 = blockIdx.z * TX;
+  if (k0 >= n3 || j >= n2) return;
+  const FieldGeom g = FieldGeom::make(n1, n2, n3, 0);
+  for (int tx = 0; tx < TX; ++tx) {
+    const int i = x0 + tx;
+    if (i >= n1) continue;
+    const int64_t q = ((int64_t)i * n2 + j) * n3 + k0;
+    for (int c = 0; c < 8; ++c) {
+      if (cls[q + c] != CLS_GENERAL) continue;
+      float acc[28];
+      const int k = k0 + c;
+      coeffs_of_patch(sW, sb, [&](int s, int m, int nn, int o) {
+        return g.at(img + s * g.bstride, i + m - 1, j + nn - 1, k + o - 1);
+      }, acc);
+      KT *r = rec + (size_t)rank * KREC;
+#pragma unroll
+      for (int p = 0; p < KREC; ++p) stf(r + p, p < 27 ? acc[p] : 0.f);
+      ++rank;
+    }
+  }
+}
+
+// coefficients of one general cell's record as floats
+__device__ __forceinline__ void ld_record(const float *r, float k[KREC]) {
+#pragma unroll
+  for (int v = 0; v < KREC / 4; ++v) {
+    const float4 a = __ldg(reinterpret_cast<const float4 *>(r) + v);
+    k[4 * v] = a.x; k[4 * v + 1] = a.y; k[4 * v + 2] = a.z; k[4 * v + 3] = a.w;
+  }
+}
+__device__ __forceinline__ void ld_record(const __nv_bfloat16 *r, float k[KREC]) {
+#pragma unroll
+  for (int v = 0; v < KREC / 8; ++v) {
+    const uint4 u = __ldg(reinterpret_cast<const uint4 *>(r) + v);
+    unpack_bf16x2(u.x, k[8 * v + 0], k[8 * v + 1]); unpack_bf16x2(u.y, k[8 * v + 2], k[8 * v + 3]);
+    unpack_bf16x2(u.z, k[8 * v + 4], k[8 * v + 5]); unpack_bf16x2(u.w, k[8 * v + 6], k[8 * v + 7]);
+  }
+}
+
+template <typename KT>
+struct CoefArgs {
+  const KT *K;             // dense: 27 planes ...
+  int64_t ps;              // ... of this stride
+  const KT *rec;           // classed: general-cell records
+  const float *kuni;       // classed: 3 x KREC uniform vectors
+  const uint8_t *cls;      // classed: class byte per cell
+  const uint32_t *tbase;   // classed: first record index per tile
+};
+
+// classed 27-tap application of one 8-cell run; rank = record index of the
+// run's first general cell, advanced past the run's general cells
+template <typename KT>
+__device__ __forceinline__ void apply_run_cls(const float (*S)[HY][HZ], const float (*Ku)[KREC], int tx, int ty,
+                                              int tz8, const uint8_t *__restrict__ clsrun,
+                                              const KT *__restrict__ rec, uint32_t &rank, float acc[8]) {
+  const uint2 cw = __ldg(reinterpret_cast<const uint2 *>(clsrun));
+  int cl[8];
+#pragma unroll
+  for (int b = 0; b < 4; ++b) {
+    cl[b] = (cw.x >> (8 * b)) & 0xffu;
+    cl[4 + b] = (cw.y >> (8 * b)) & 0xffu;
+  }
+  bool uni = cl[0] != CLS_GENERAL;
+#pragma unroll
+  for (int c = 1; c < 8; ++c) uni = uni && cl[c] == cl[0];
+  if (uni) {
+    const float *ku = Ku[cl[0]];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) acc[c] = 0.f;
+#pragma unroll
+    for (int dx = 0; dx < 3; ++dx)
+#pragma unroll
+      for (int dy = 0; dy < 3; ++dy) {
+        float xr[10];
+        const float *row = &S[tx + dx][ty + dy][tz8];
+#pragma unroll
+        for (int c = 0; c < 10; ++c) xr[c] = row[c];
+#pragma unroll
+        for (int dz = 0; dz < 3; ++dz) {
+          const float kv = ku[dx * 9 + dy * 3 + dz];
+#pragma unroll
+          for (int c = 0; c < 8; ++c) acc[c] = fmaf(kv, xr[c + dz], acc[c]);
+        }
+      }
+    return;
+  }
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    float k[KREC];
+    if (cl[c] == CLS_GENERAL) {
+      ld_record(rec + (size_t)rank * KREC, k);
+      ++rank;
+    } else {
+#pragma unroll
+      for (int p = 0; p < 27; ++p) k[p] = Ku[cl[c]][p];
+    }
+    float a = 0.f;
+#pragma unroll
+    for (int dx = 0; dx < 3; ++dx)
+#pragma unroll
+      for (int dy = 0; dy < 3; ++dy)
+#pragma unroll
+        for (int dz = 0; dz < 3; ++dz) a = fmaf(k[dx * 9 + dy * 3 + dz], S[tx + dx][ty + dy][tz8 + c + dz], a);
+    acc[c] = a;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // pre-block (and the coarsest l-block): y = B(x), optional fused avg-pool
 // ---------------------------------------------------------------------------
-template <typename KT, typename XT, typename YT, bool POOL>
+// uniform coefficient vectors of a classed block into shared memory
+template <bool CLS>
+__device__ __forceinline__ void stage_uniform(float (*Ku)[KREC], const float *__restrict__ kuni) {
+  if (CLS)
+    for (int e = threadIdx.x; e < 3 * KREC; e += PT) Ku[e / KREC][e % KREC] = __ldg(kuni + e);
+}
+
+// record index of this thread's first general cell (all threads of the CTA must call)
+template <typename KT, bool CLS>
+__device__ __forceinline__ uint32_t first_rank(const CoefArgs<KT> &C, int n1, int n2, int n3) {
+  if (!CLS) return 0u;
+  int tot;
+  return __ldg(C.tbase + tile_id()) + (uint32_t)cta_excl_scan(count_general(C.cls, n1, n2, n3), tot);
+}
+
+template <typename KT, bool CLS>
+__device__ __forceinline__ void apply_any(const float (*S)[HY][HZ], const float (*Ku)[KREC], int tx, int ty,
+                                          int tz8, const CoefArgs<KT> &C, int64_t q, uint32_t &rank,
+                                          float acc[8]) {
+  if (CLS) apply_run_cls<KT>(S, Ku, tx, ty, tz8, C.cls + q, C.rec, rank, acc);
+  else apply_run<KT>(S, tx, ty, tz8, C.K, C.ps, q, acc);
+}
+
+template <typename KT, typename XT, typename YT, bool POOL, bool CLS>
 __global__ void __launch_bounds__(PT)
-k_pre_fused(const KT *__restrict__ K, int64_t ps, const XT *__restrict__ x,
+k_pre_fused(const CoefArgs<KT> C, const XT *__restrict__ x,
             const float *__restrict__ xscale, YT *__restrict__ y, YT *__restrict__ ypool,
             const uint8_t *__restrict__ mask, int n1, int n2, int n3) {
   __shared__ float S[HX][HY][HZ];
+  __shared__ float Ku[CLS ? 3 : 1][KREC];
   const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY, x0 = blockIdx.z * TX;
   const float sc = xscale ? __ldg(xscale) : 1.f;
   for (int e = threadIdx.x; e < HX * HY * HZ; e += PT) {
@@ -121,7 +440,9 @@ k_pre_fused(const KT *__restrict__ K, int64_t ps, const XT *__restrict__ x,
       v = ldf(x + ((int64_t)i * n2 + j) * n3 + k) * sc;
     S[hx][hy][hz] = v;
   }
+  stage_uniform<CLS>(Ku, C.kuni);
   __syncthreads();
+  uint32_t rank = first_rank<KT, CLS>(C, n1, n2, n3);
   const int tz = threadIdx.x % ZT, ty = threadIdx.x / ZT;
   const int k0 = z0 + tz * 8, j = y0 + ty;
   const bool active = k0 < n3 && j < n2;  // n3 % 8 == 0: a run is all in or all out
@@ -132,7 +453,7 @@ k_pre_fused(const KT *__restrict__ K, int64_t ps, const XT *__restrict__ x,
     if (!active || i >= n1) continue;
     const int64_t q = ((int64_t)i * n2 + j) * n3 + k0;
     float acc[8];
-    apply_run<KT>(S, tx, ty, tz * 8, K, ps, q, acc);
+    apply_any<KT, CLS>(S, Ku, tx, ty, tz * 8, C, q, rank, acc);
     if (mask) {
       const uint2 m = __ldg(reinterpret_cast<const uint2 *>(mask + q));
 #pragma unroll
@@ -173,13 +494,15 @@ __device__ __forceinline__ Lin1 lin1(int f, int n) {
   return r;
 }
 
-template <typename KT, typename CT, typename YT, typename OT, bool SWAP>
+template <typename KT, typename CT, typename YT, typename OT, bool SWAP, bool CLS>
 __global__ void __launch_bounds__(PT)
-k_post_fused(const KT *__restrict__ K, int64_t ps, const CT *__restrict__ xc, const YT *__restrict__ yl,
+k_post_fused(const CoefArgs<KT> C, const CT *__restrict__ xc, const YT *__restrict__ yl,
              const float *__restrict__ c0p, const float *__restrict__ c1p, OT *__restrict__ out,
              const uint8_t *__restrict__ bmask, const uint8_t *__restrict__ omask, int n1, int n2, int n3) {
   __shared__ float S[HX][HY][HZ];
   __shared__ float Cs[CX][CY][CZ];
+  __shared__ float Ku[CLS ? 3 : 1][KREC];
+  stage_uniform<CLS>(Ku, C.kuni);
   const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY, x0 = blockIdx.z * TX;
   const int m1 = n1 / 2, m2 = n2 / 2, m3 = n3 / 2;
   const int cx0 = x0 / 2 - 1, cy0 = y0 / 2 - 1, cz0 = z0 / 2 - 1;
@@ -210,6 +533,7 @@ k_post_fused(const KT *__restrict__ K, int64_t ps, const CT *__restrict__ xc, co
     S[hx][hy][hz] = v;
   }
   __syncthreads();
+  uint32_t rank = first_rank<KT, CLS>(C, n1, n2, n3);
   const int tz = threadIdx.x % ZT, ty = threadIdx.x / ZT;
   const int k0 = z0 + tz * 8, j = y0 + ty;
   if (k0 >= n3 || j >= n2) return;
@@ -219,7 +543,7 @@ k_post_fused(const KT *__restrict__ K, int64_t ps, const CT *__restrict__ xc, co
     if (i >= n1) continue;
     const int64_t q = ((int64_t)i * n2 + j) * n3 + k0;
     float acc[8];
-    apply_run<KT>(S, tx, ty, tz * 8, K, ps, q, acc);
+    apply_any<KT, CLS>(S, Ku, tx, ty, tz * 8, C, q, rank, acc);
     if (bmask) {
       const uint2 m = __ldg(reinterpret_cast<const uint2 *>(bmask + q));
 #pragma unroll
@@ -291,12 +615,17 @@ struct PrecondPlan {
   int n1, n2, n3, L;          // fine sizes, number of levels n (blocks at levels 0..L)
   int kdt, adt;               // coefficient / activation storage dtypes
   int swap, mask;
-  struct Level { int n1, n2, n3; int64_t n, ps; bool fast; };
+  int layout;                 // MLPCG_COEFF_DENSE or MLPCG_COEFF_CLASSED
+  struct Level { int n1, n2, n3; int64_t n, ps; bool fast, cls; unsigned ntiles; };
   std::vector<Level> lv;      // L + 1 levels
   // device pointers (inside the caller's workspace)
   std::vector<float *> img;   // level images, [0] unused (caller's image)
-  std::vector<void *> Kpre, Kpost;
+  std::vector<void *> Kpre, Kpost;   // dense planes, or general-cell records on classed levels
   void *Kl = nullptr;
+  std::vector<float *> Upre, Upost;  // classed levels: 3 x KREC uniform vectors per block
+  float *Ul = nullptr;
+  std::vector<uint8_t *> cls;        // classed levels: class byte per cell
+  std::vector<uint32_t *> tcount, tbase;
   std::vector<void *> y, xin, xout;  // y_l (pre out), x_l inputs (l >= 1), post outputs (l >= 1)
   float *coef = nullptr;      // c0[0..L-1], c1[0..L-1]
   uint8_t *fmask = nullptr;   // fluid mask of level 0
@@ -323,11 +652,34 @@ static size_t plan_layout(PrecondPlan &P, char *base) {
   P.xin.assign(P.L + 1, nullptr);
   P.xout.assign(P.L + 1, nullptr);
   for (int l = 1; l <= P.L; ++l) P.img[l] = (float *)take(3 * P.lv[l].n * sizeof(float));
+  // coefficient storage of one block: dense planes, or (worst case: every cell general) records
+  auto kbytes = [&](int l) {
+    const auto &v = P.lv[l];
+    return v.cls ? (size_t)v.n * KREC * sk : (size_t)27 * v.ps * sk;
+  };
   for (int l = 0; l < P.L; ++l) {
-    P.Kpre[l] = take(27 * P.lv[l].ps * sk);
-    P.Kpost[l] = take(27 * P.lv[l].ps * sk);
+    P.Kpre[l] = take(kbytes(l));
+    P.Kpost[l] = take(kbytes(l));
   }
-  P.Kl = take(27 * P.lv[P.L].ps * sk);
+  P.Kl = take(kbytes(P.L));
+  P.Upre.assign(P.L, nullptr);
+  P.Upost.assign(P.L, nullptr);
+  P.cls.assign(P.L + 1, nullptr);
+  P.tcount.assign(P.L + 1, nullptr);
+  P.tbase.assign(P.L + 1, nullptr);
+  for (int l = 0; l <= P.L; ++l) {
+    const auto &v = P.lv[l];
+    if (!v.cls) continue;
+    P.cls[l] = (uint8_t *)take(v.ps);
+    P.tcount[l] = (uint32_t *)take(v.ntiles * sizeof(uint32_t));
+    P.tbase[l] = (uint32_t *)take(v.ntiles * sizeof(uint32_t));
+    if (l < P.L) {
+      P.Upre[l] = (float *)take(3 * KREC * sizeof(float));
+      P.Upost[l] = (float *)take(3 * KREC * sizeof(float));
+    } else {
+      P.Ul = (float *)take(3 * KREC * sizeof(float));
+    }
+  }
   for (int l = 0; l < P.L; ++l) P.y[l] = take(P.lv[l].ps * sa);
   for (int l = 1; l <= P.L; ++l) {
     P.xin[l] = take(P.lv[l].ps * sa);
@@ -351,28 +703,50 @@ struct mlpcg_precond { PrecondPlan p; };
 #define RET_IF(expr) do { int _r = (expr); if (_r != MLPCG_OK) return _r; } while (0)
 
 // launch helpers for the fast kernels ------------------------------------------
+static dim3 grid_of(const PrecondPlan::Level &v) {
+  return dim3((unsigned)((v.n3 + TZ - 1) / TZ), (unsigned)((v.n2 + TY - 1) / TY), (unsigned)((v.n1 + TX - 1) / TX));
+}
+
+template <typename KT>
+static CoefArgs<KT> coef_args(const PrecondPlan &P, int l, void *K, float *uni) {
+  CoefArgs<KT> C;
+  C.K = (const KT *)K;
+  C.ps = P.lv[l].ps;
+  C.rec = (const KT *)K;
+  C.kuni = uni;
+  C.cls = P.cls[l];
+  C.tbase = P.tbase[l];
+  return C;
+}
+
 // Stages of one application, in launch order: 0..L-1 = pre-block of level s,
 // L = coarsest block, L+1..2L = post-block of level 2L-s.  [s0, s1] selects a range.
 template <typename KT, typename AT>
 static int run_apply(const PrecondPlan &P, const float *r, const float *rscale, float *z, void *tmp0,
                      cudaStream_t st, int s0 = 0, int s1 = 1 << 20) {
   const int L = P.L;
-  auto grid_of = [](const PrecondPlan::Level &v) {
-    return dim3((unsigned)((v.n3 + TZ - 1) / TZ), (unsigned)((v.n2 + TY - 1) / TY), (unsigned)((v.n1 + TX - 1) / TX));
-  };
   const uint8_t *m0 = P.mask ? P.fmask : nullptr;
   // ---- down sweep
   for (int l = 0; l < L; ++l) {
     const auto &v = P.lv[l];
     if (l < s0 || l > s1) continue;
     if (v.fast) {
-      if (l == 0)
-        k_pre_fused<KT, float, AT, true><<<grid_of(v), PT, 0, st>>>(
-            (const KT *)P.Kpre[0], v.ps, r, rscale, (AT *)P.y[0], (AT *)P.xin[1], m0, v.n1, v.n2, v.n3);
-      else
-        k_pre_fused<KT, AT, AT, true><<<grid_of(v), PT, 0, st>>>(
-            (const KT *)P.Kpre[l], v.ps, (const AT *)P.xin[l], nullptr, (AT *)P.y[l], (AT *)P.xin[l + 1],
-            nullptr, v.n1, v.n2, v.n3);
+      const CoefArgs<KT> C = coef_args<KT>(P, l, P.Kpre[l], v.cls ? P.Upre[l] : nullptr);
+      if (l == 0) {
+        if (v.cls)
+          k_pre_fused<KT, float, AT, true, true><<<grid_of(v), PT, 0, st>>>(
+              C, r, rscale, (AT *)P.y[0], (AT *)P.xin[1], m0, v.n1, v.n2, v.n3);
+        else
+          k_pre_fused<KT, float, AT, true, false><<<grid_of(v), PT, 0, st>>>(
+              C, r, rscale, (AT *)P.y[0], (AT *)P.xin[1], m0, v.n1, v.n2, v.n3);
+      } else {
+        if (v.cls)
+          k_pre_fused<KT, AT, AT, true, true><<<grid_of(v), PT, 0, st>>>(
+              C, (const AT *)P.xin[l], nullptr, (AT *)P.y[l], (AT *)P.xin[l + 1], nullptr, v.n1, v.n2, v.n3);
+        else
+          k_pre_fused<KT, AT, AT, true, false><<<grid_of(v), PT, 0, st>>>(
+              C, (const AT *)P.xin[l], nullptr, (AT *)P.y[l], (AT *)P.xin[l + 1], nullptr, v.n1, v.n2, v.n3);
+      }
       MLPCG_LAUNCH_CHECK();
     } else {
       const void *src = P.xin[l];
@@ -394,8 +768,13 @@ static int run_apply(const PrecondPlan &P, const float *r, const float *rscale, 
   if (L >= s0 && L <= s1) {
     const auto &v = P.lv[L];
     if (v.fast) {
-      k_pre_fused<KT, AT, AT, false><<<grid_of(v), PT, 0, st>>>(
-          (const KT *)P.Kl, v.ps, (const AT *)P.xin[L], nullptr, (AT *)P.xout[L], nullptr, nullptr, v.n1, v.n2, v.n3);
+      const CoefArgs<KT> C = coef_args<KT>(P, L, P.Kl, v.cls ? P.Ul : nullptr);
+      if (v.cls)
+        k_pre_fused<KT, AT, AT, false, true><<<grid_of(v), PT, 0, st>>>(
+            C, (const AT *)P.xin[L], nullptr, (AT *)P.xout[L], nullptr, nullptr, v.n1, v.n2, v.n3);
+      else
+        k_pre_fused<KT, AT, AT, false, false><<<grid_of(v), PT, 0, st>>>(
+            C, (const AT *)P.xin[L], nullptr, (AT *)P.xout[L], nullptr, nullptr, v.n1, v.n2, v.n3);
       MLPCG_LAUNCH_CHECK();
     } else {
       RET_IF(launch_stencil_apply(P.Kl, P.kdt, v.ps, P.xin[L], P.adt, 0, P.xout[L], P.adt, 1, v.n1, v.n2, v.n3, 0, st));
@@ -409,22 +788,26 @@ static int run_apply(const PrecondPlan &P, const float *r, const float *rscale, 
     const uint8_t *bm = (l == 0) ? m0 : nullptr;
     const uint8_t *om = (l == 0) ? P.fmask : nullptr;
     if (v.fast) {
+      const CoefArgs<KT> C = coef_args<KT>(P, l, P.Kpost[l], v.cls ? P.Upost[l] : nullptr);
+      const AT *xc = (const AT *)P.xout[l + 1], *yl = (const AT *)P.y[l];
+      const dim3 g = grid_of(v);
       if (l == 0) {
-        if (P.swap)
-          k_post_fused<KT, AT, AT, float, true><<<grid_of(v), PT, 0, st>>>(
-              (const KT *)P.Kpost[0], v.ps, (const AT *)P.xout[1], (const AT *)P.y[0], c0, c1, z, bm, om, v.n1, v.n2, v.n3);
-        else
-          k_post_fused<KT, AT, AT, float, false><<<grid_of(v), PT, 0, st>>>(
-              (const KT *)P.Kpost[0], v.ps, (const AT *)P.xout[1], (const AT *)P.y[0], c0, c1, z, bm, om, v.n1, v.n2, v.n3);
+        if (P.swap) {
+          if (v.cls) k_post_fused<KT, AT, AT, float, true, true><<<g, PT, 0, st>>>(C, xc, yl, c0, c1, z, bm, om, v.n1, v.n2, v.n3);
+          else k_post_fused<KT, AT, AT, float, true, false><<<g, PT, 0, st>>>(C, xc, yl, c0, c1, z, bm, om, v.n1, v.n2, v.n3);
+        } else {
+          if (v.cls) k_post_fused<KT, AT, AT, float, false, true><<<g, PT, 0, st>>>(C, xc, yl, c0, c1, z, bm, om, v.n1, v.n2, v.n3);
+          else k_post_fused<KT, AT, AT, float, false, false><<<g, PT, 0, st>>>(C, xc, yl, c0, c1, z, bm, om, v.n1, v.n2, v.n3);
+        }
       } else {
-        if (P.swap)
-          k_post_fused<KT, AT, AT, AT, true><<<grid_of(v), PT, 0, st>>>(
-              (const KT *)P.Kpost[l], v.ps, (const AT *)P.xout[l + 1], (const AT *)P.y[l], c0, c1, (AT *)P.xout[l],
-              nullptr, nullptr, v.n1, v.n2, v.n3);
-        else
-          k_post_fused<KT, AT, AT, AT, false><<<grid_of(v), PT, 0, st>>>(
-              (const KT *)P.Kpost[l], v.ps, (const AT *)P.xout[l + 1], (const AT *)P.y[l], c0, c1, (AT *)P.xout[l],
-              nullptr, nullptr, v.n1, v.n2, v.n3);
+        AT *o = (AT *)P.xout[l];
+        if (P.swap) {
+          if (v.cls) k_post_fused<KT, AT, AT, AT, true, true><<<g, PT, 0, st>>>(C, xc, yl, c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3);
+          else k_post_fused<KT, AT, AT, AT, true, false><<<g, PT, 0, st>>>(C, xc, yl, c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3);
+        } else {
+          if (v.cls) k_post_fused<KT, AT, AT, AT, false, true><<<g, PT, 0, st>>>(C, xc, yl, c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3);
+          else k_post_fused<KT, AT, AT, AT, false, false><<<g, PT, 0, st>>>(C, xc, yl, c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3);
+        }
       }
       MLPCG_LAUNCH_CHECK();
     } else {
@@ -468,7 +851,7 @@ static int run_apply(const PrecondPlan &P, const float *r, const float *rscale, 
 extern "C" {
 
 int mlpcg_precond_create(int N1, int N2, int N3, int levels, int k_dtype, int act_dtype,
-                         int swap_sm_order, int mask, mlpcg_precond **out) {
+                         int swap_sm_order, int mask, int coeff_layout, mlpcg_precond **out) {
   clear_error();
   MLPCG_REQUIRE(out != nullptr, MLPCG_ERR_ARG, "out must not be NULL");
   *out = nullptr;
@@ -482,13 +865,19 @@ int mlpcg_precond_create(int N1, int N2, int N3, int levels, int k_dtype, int ac
   auto *h = new mlpcg_precond();
   PrecondPlan &P = h->p;
   P.n1 = N1; P.n2 = N2; P.n3 = N3; P.L = levels;
+  MLPCG_REQUIRE(coeff_layout == MLPCG_COEFF_DENSE || coeff_layout == MLPCG_COEFF_CLASSED, MLPCG_ERR_ARG,
+                "coeff_layout must be MLPCG_COEFF_DENSE or MLPCG_COEFF_CLASSED");
   P.kdt = k_dtype; P.adt = act_dtype; P.swap = swap_sm_order ? 1 : 0; P.mask = mask ? 1 : 0;
+  P.layout = coeff_layout;
   for (int l = 0; l <= levels; ++l) {
     PrecondPlan::Level v;
     v.n1 = N1 >> l; v.n2 = N2 >> l; v.n3 = N3 >> l;
     v.n = cells(v.n1, v.n2, v.n3);
     v.ps = (v.n + 63) / 64 * 64;
     v.fast = (v.n3 % 8 == 0);
+    v.cls = v.fast && coeff_layout == MLPCG_COEFF_CLASSED;
+    const dim3 g = grid_of(v);
+    v.ntiles = g.x * g.y * g.z;
     P.lv.push_back(v);
   }
   P.bytes = plan_layout(P, nullptr);
@@ -525,17 +914,37 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
   }
   k_fluid_mask<<<blocks_for(P.lv[0].n, 256), 256, 0, st>>>(image, P.fmask, P.lv[0].n);
   MLPCG_LAUNCH_CHECK();
-  // coefficients
-  for (int l = 0; l < L; ++l) {
+  // coefficients: dense planes, or class map + uniform vectors + general-cell records
+  auto gen = [&](int l, const float *im, int blk, void *K, float *U) -> int {
     const auto &v = P.lv[l];
+    if (!v.cls) return launch_stencil_gen(im, 0, v.n1, v.n2, v.n3, blk_w(blk), blk_b(blk), K, P.kdt, v.ps, st);
+    if (P.kdt == MLPCG_BF16) {
+      k_kgen_uniform<__nv_bfloat16><<<1, 32, 0, st>>>(blk_w(blk), blk_b(blk), U);
+      k_kgen_cls<__nv_bfloat16><<<grid_of(v), PT, 0, st>>>(im, v.n1, v.n2, v.n3, blk_w(blk), blk_b(blk), P.cls[l],
+                                                           P.tbase[l], (__nv_bfloat16 *)K);
+    } else {
+      k_kgen_uniform<float><<<1, 32, 0, st>>>(blk_w(blk), blk_b(blk), U);
+      k_kgen_cls<float><<<grid_of(v), PT, 0, st>>>(im, v.n1, v.n2, v.n3, blk_w(blk), blk_b(blk), P.cls[l], P.tbase[l],
+                                                   (float *)K);
+    }
+    MLPCG_LAUNCH_CHECK();
+    return MLPCG_OK;
+  };
+  for (int l = 0; l <= L; ++l) {
+    const auto &v = P.lv[l];
+    if (!v.cls) continue;
     const float *im = (l == 0) ? image : P.img[l];
-    RET_IF(launch_stencil_gen(im, 0, v.n1, v.n2, v.n3, blk_w(l), blk_b(l), P.Kpre[l], P.kdt, v.ps, st));
-    RET_IF(launch_stencil_gen(im, 0, v.n1, v.n2, v.n3, blk_w(L + l), blk_b(L + l), P.Kpost[l], P.kdt, v.ps, st));
+    k_classify<<<grid_of(v), PT, 0, st>>>(im, v.n1, v.n2, v.n3, P.cls[l], P.tcount[l]);
+    MLPCG_LAUNCH_CHECK();
+    k_scan_tiles<<<1, 1024, 0, st>>>(P.tcount[l], P.tbase[l], (int)v.ntiles);
+    MLPCG_LAUNCH_CHECK();
   }
-  {
-    const auto &v = P.lv[L];
-    RET_IF(launch_stencil_gen(P.img[L], 0, v.n1, v.n2, v.n3, blk_w(2 * L), blk_b(2 * L), P.Kl, P.kdt, v.ps, st));
+  for (int l = 0; l < L; ++l) {
+    const float *im = (l == 0) ? image : P.img[l];
+    RET_IF(gen(l, im, l, P.Kpre[l], P.Upre[l]));
+    RET_IF(gen(l, im, L + l, P.Kpost[l], P.Upost[l]));
   }
+  RET_IF(gen(L, P.img[L], 2 * L, P.Kl, P.Ul));
   // c0 / c1 of every level (the linear blocks of sm_model_3d.py:236-239)
   for (int l = 0; l < L; ++l) {
     const auto &v = P.lv[l];
@@ -580,6 +989,22 @@ int mlpcg_precond_apply_stages(const mlpcg_precond *h, int first, int last, cons
   if (P.kdt == MLPCG_BF16 && P.adt == MLPCG_F32) return run_apply<__nv_bfloat16, float>(P, r, r_scale, z, tmp0, st, first, last);
   if (P.kdt == MLPCG_F32 && P.adt == MLPCG_BF16) return run_apply<float, __nv_bfloat16>(P, r, r_scale, z, tmp0, st, first, last);
   return run_apply<float, float>(P, r, r_scale, z, tmp0, st, first, last);
+}
+
+int mlpcg_precond_general_cells(const mlpcg_precond *h, int level, int64_t *count, void *stream) {
+  clear_error();
+  MLPCG_REQUIRE(h && count && level >= 0 && level <= h->p.L, MLPCG_ERR_ARG, "precond_general_cells: bad argument");
+  const PrecondPlan &P = h->p;
+  MLPCG_REQUIRE(P.ready, MLPCG_ERR_ARG, "precond_general_cells: plan not set up");
+  const auto &v = P.lv[level];
+  if (!v.cls) { *count = -1; return MLPCG_OK; }
+  uint32_t last[2] = {0, 0};
+  cudaStream_t st = as_stream(stream);
+  MLPCG_CUDA_CHECK(cudaMemcpyAsync(&last[0], P.tbase[level] + v.ntiles - 1, 4, cudaMemcpyDeviceToHost, st));
+  MLPCG_CUDA_CHECK(cudaMemcpyAsync(&last[1], P.tcount[level] + v.ntiles - 1, 4, cudaMemcpyDeviceToHost, st));
+  MLPCG_CUDA_CHECK(cudaStreamSynchronize(st));
+  *count = (int64_t)last[0] + last[1];
+  return MLPCG_OK;
 }
 
 int mlpcg_precond_level_info(const mlpcg_precond *h, int level, int *n1, int *n2, int *n3, int *fast) {

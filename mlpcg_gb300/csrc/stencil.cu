@@ -26,12 +26,7 @@ k_stencil_gen(const float *__restrict__ img, FieldGeom g, const float *__restric
               const float *__restrict__ bias, KT *__restrict__ K, int64_t ps) {
   __shared__ float4 sW[81 * 7];
   __shared__ float sb[28];
-  float *sWf = reinterpret_cast<float *>(sW);
-  for (int t = threadIdx.x; t < 81 * 28; t += blockDim.x) {
-    int so = t / 28, p = t % 28;
-    sWf[t] = p < 27 ? W[p * 81 + so] : 0.f;
-  }
-  if (threadIdx.x < 28) sb[threadIdx.x] = threadIdx.x < 27 ? bias[threadIdx.x] : 0.f;
+  load_weights_smem(W, bias, sW, sb);
   __syncthreads();
 
   const int64_t n = cells(g.n1, g.n2, g.n3);
@@ -43,29 +38,9 @@ k_stencil_gen(const float *__restrict__ img, FieldGeom g, const float *__restric
   const int i = (int)(t / g.n2);
 
   float acc[28];
-#pragma unroll
-  for (int p = 0; p < 28; ++p) acc[p] = sb[p];
-  // Same summation order as the reference: bias, then s, m, n, o.
-  for (int s = 0; s < 3; ++s) {
-    const float *ch = img + s * g.bstride;
-#pragma unroll
-    for (int m = 0; m < 3; ++m)
-#pragma unroll
-      for (int nn = 0; nn < 3; ++nn)
-#pragma unroll
-        for (int o = 0; o < 3; ++o) {
-          const float v = g.at(ch, i + m - 1, j + nn - 1, k + o - 1);
-          const float4 *w = sW + (s * 27 + m * 9 + nn * 3 + o) * 7;
-#pragma unroll
-          for (int pp = 0; pp < 7; ++pp) {
-            const float4 wv = w[pp];
-            acc[4 * pp + 0] = fmaf(wv.x, v, acc[4 * pp + 0]);
-            acc[4 * pp + 1] = fmaf(wv.y, v, acc[4 * pp + 1]);
-            acc[4 * pp + 2] = fmaf(wv.z, v, acc[4 * pp + 2]);
-            acc[4 * pp + 3] = fmaf(wv.w, v, acc[4 * pp + 3]);
-          }
-        }
-  }
+  coeffs_of_patch(sW, sb, [&](int s, int m, int nn, int o) {
+    return g.at(img + s * g.bstride, i + m - 1, j + nn - 1, k + o - 1);
+  }, acc);
 #pragma unroll
   for (int p = 0; p < 27; ++p) stf(K + p * ps + q, acc[p]);
 }

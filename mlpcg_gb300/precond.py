@@ -36,19 +36,21 @@ def pack_params(model) -> torch.Tensor:
 class PrecondPlan:
     """z = M r for one image; ``apply`` is graph-capturable (no host sync, no allocation with ``out``)."""
 
-    def __init__(self, model, image, storage=torch.bfloat16, act_storage=None):
+    LAYOUTS = {"dense": 0, "classed": 1}
+
+    def __init__(self, model, image, storage=torch.bfloat16, act_storage=None, layout="classed"):
         _check(image, "image")
         if image.dim() != 4 or image.shape[0] != 3:
             raise RuntimeError("image must have shape (3, N1, N2, N3)")
         act_storage = storage if act_storage is None else act_storage
         self.shape = tuple(int(s) for s in image.shape[1:])
         self.levels = model.n
-        self.storage, self.act_storage = storage, act_storage
+        self.storage, self.act_storage, self.layout = storage, act_storage, layout
         self.device = image.device
         lib = _lib.load()
         h = C.c_void_p()
         call("mlpcg_precond_create", *self.shape, model.n, _DT[storage], _DT[act_storage],
-             int(bool(model.swap_ord)), int(bool(model.pre[0].mask)), C.byref(h))
+             int(bool(model.swap_ord)), int(bool(model.pre[0].mask)), self.LAYOUTS[layout], C.byref(h))
         self._h = h
         self._lib = lib
         nbytes = lib.mlpcg_precond_workspace(h)
@@ -80,6 +82,12 @@ class PrecondPlan:
         call("mlpcg_precond_apply_stages", self._h, int(first), int(last), _p(r), _p(scale), _p(z),
              _stream(r.device))
         return z
+
+    def general_cells(self, level: int) -> int:
+        """Cells of a classed level that need their own coefficients (-1 on dense levels)."""
+        c = C.c_int64()
+        call("mlpcg_precond_general_cells", self._h, int(level), C.byref(c), _stream(self.device))
+        return c.value
 
     def level_info(self, level: int):
         n1, n2, n3, fast = C.c_int(), C.c_int(), C.c_int(), C.c_int()

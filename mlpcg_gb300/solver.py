@@ -44,7 +44,8 @@ def flags_to_image(flags: torch.Tensor) -> torch.Tensor:
 
 class FusedSolver:
     def __init__(self, model, flags: torch.Tensor, method="npsd", max_it=100, tol=1e-6, true_every=25,
-                 storage=torch.bfloat16, act_storage=None, image=None, plan: PrecondPlan | None = None):
+                 storage=torch.bfloat16, act_storage=None, image=None, plan: PrecondPlan | None = None,
+                 layout="classed"):
         if flags.dtype != torch.uint8 or flags.dim() != 3 or not flags.is_cuda:
             raise ValueError("flags must be a (N1, N2, N3) uint8 CUDA tensor")
         self.flags = flags.contiguous()
@@ -53,7 +54,7 @@ class FusedSolver:
         dev = flags.device
         if plan is None:
             image = flags_to_image(self.flags) if image is None else image
-            plan = PrecondPlan(model, image, storage=storage, act_storage=act_storage)
+            plan = PrecondPlan(model, image, storage=storage, act_storage=act_storage, layout=layout)
         self.plan = plan
         lib = _lib.load()
         self._lib = lib

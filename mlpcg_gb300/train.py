@@ -112,24 +112,62 @@ class TrainScene:
         self.ritz = ritz.float()
         self.n = self.flags.numel()
 
-    def batch(self, B, noise_frac, gen):
+        self.harvested = []       # residuals met by npsd with the current network (fluid cells, unit norm)
+        self.plan = None
+        self.solvers = {}
+
+    def batch(self, B, noise_frac, gen, harvest_frac=0.0):
+        nh = min(int(round(B * harvest_frac)), len(self.harvested) and B)
         nb = int(round(B * noise_frac))
+        nr = max(B - nb - nh, 0)
         parts = []
-        if B - nb > 0:
-            parts.append(mix_rhs(self.ritz, B - nb, generator=gen))
+        if nr > 0:
+            parts.append(mix_rhs(self.ritz, nr, generator=gen))
         if nb > 0:
             w = torch.randn((nb, self.A.n_fluid), device=self.ritz.device, generator=gen)
             parts.append(w / w.norm(dim=1, keepdim=True))
+        if nh > 0:
+            idx = torch.randint(len(self.harvested), (nh,), generator=gen, device=self.ritz.device).tolist()
+            parts.append(torch.stack([self.harvested[i] for i in idx]))
         bf = torch.cat(parts)
-        b = torch.zeros((B, self.n), dtype=torch.float32, device=bf.device)
+        b = torch.zeros((bf.shape[0], self.n), dtype=torch.float32, device=bf.device)
         b[:, self.A.fluid_cells] = bf
-        return b.reshape(B, *self.flags.shape)
+        return b.reshape(bf.shape[0], *self.flags.shape)
+
+    def harvest(self, model, gen, depths=(2, 5, 10, 20), keep=48):
+        """Residuals after a few fused npsd iterations with the current network, from a random rhs."""
+        from .precond import PrecondPlan
+        if self.plan is None:
+            self.plan = PrecondPlan(model, self.image)
+            for d in depths:
+                self.solvers[d] = FusedSolver(model, self.flags, method="npsd", max_it=d, tol=1e-12,
+                                              plan=self.plan)
+        else:
+            next(iter(self.solvers.values())).set_image(model, self.image)
+        b0 = self.batch(1, 0.5, gen)[0].double()
+        for d, s in self.solvers.items():
+            res = s.solve(b0)
+            r = (b0 - self.A.matvec_grid(res.x)).reshape(-1)[self.A.fluid_cells].float()
+            nrm = r.norm()
+            if torch.isfinite(nrm) and nrm > 0:
+                self.harvested.append(r / nrm)
+        self.harvested = self.harvested[-keep:]
 
 
-def evaluate(model, scene: TrainScene, max_it=200, tol=1e-6):
-    solver = FusedSolver(model, scene.flags, method="npsd", max_it=max_it, tol=tol, image=scene.image)
-    r = solver.solve(scene.rhs)
-    return r.iterations, r.status, r.rel_res
+class Validator:
+    """npsd iterations to 1e-6 on a held-out scene (one solver, re-planned with the current weights)."""
+
+    def __init__(self, model, size, seed, spheres, device, max_it=200, tol=1e-6):
+        s = make_scene(size, seed, spheres)
+        self.flags = torch.as_tensor(s.flags, device=device)
+        self.rhs = torch.as_tensor(s.rhs, device=device)
+        self.image = flags_to_image(self.flags)
+        self.solver = FusedSolver(model, self.flags, method="npsd", max_it=max_it, tol=tol, image=self.image)
+
+    def __call__(self, model):
+        self.solver.set_image(model, self.image)
+        r = self.solver.solve(self.rhs)
+        return r.iterations, r.status, r.rel_res
 
 
 def parse_seeds(s):
@@ -156,7 +194,11 @@ def main(argv=None):
     ap.add_argument("--lanczos-steps", type=int, default=1600)
     ap.add_argument("--n-ritz", type=int, default=64)
     ap.add_argument("--eval-every", type=int, default=500)
-    ap.add_argument("--eval-seed", type=int, default=18)
+    ap.add_argument("--val-size", type=int, default=256)
+    ap.add_argument("--val-seed", type=int, default=19)
+    ap.add_argument("--val-spheres", type=int, default=6)
+    ap.add_argument("--harvest-every", type=int, default=250, help="0 disables solver-in-the-loop rhs")
+    ap.add_argument("--harvest-frac", type=float, default=0.25)
     ap.add_argument("--init", default=None, help="npz state dict to start from")
     ap.add_argument("--time-limit", type=float, default=1e9, help="seconds of training loop at most")
     ap.add_argument("--ritz-cache", default=None, help="directory caching the Lanczos Ritz vectors")
@@ -175,7 +217,7 @@ def main(argv=None):
     t0 = time.time()
     scenes = [TrainScene(args.size, s, dev, args.n_ritz, args.lanczos_steps, cache_dir=args.ritz_cache)
               for s in parse_seeds(args.seeds)]
-    val = TrainScene(args.size, args.eval_seed, dev, 8, 16)
+    val = Validator(model, args.val_size, args.val_seed, args.val_spheres, dev)
     prep_s = time.time() - t0
     print(f"prepared {len(scenes)} scenes in {prep_s:.1f}s (lanczos {[round(s.lanczos_s, 1) for s in scenes]})",
           flush=True)
@@ -184,8 +226,10 @@ def main(argv=None):
     gen = torch.Generator(device=dev)
     gen.manual_seed(1234)
     log = {"loss": [], "eval": [], "args": vars(args), "prep_s": prep_s}
-    it0, st0, rel0 = evaluate(model, val)
+    it0, st0, rel0 = val(model)
     log["eval"].append({"step": 0, "iterations": it0, "status": st0, "rel_res": rel0})
+    best = (it0 if st0 == "converged" else 10 ** 9, rel0)
+    save(model, out, args, log, best=True)
     print(f"step 0 eval: {it0} its ({st0}, {rel0:.2e})", flush=True)
     t_train = time.time()
     ema = None
@@ -194,8 +238,12 @@ def main(argv=None):
         lr = args.lr_min + 0.5 * (args.lr - args.lr_min) * (1 + math.cos(math.pi * (step - 1) / args.steps))
         for g in opt.param_groups:
             g["lr"] = lr
+        if args.harvest_every and (step - 1) % args.harvest_every == 0:
+            with torch.no_grad():
+                for sc in scenes:
+                    sc.harvest(model, gen)
         sc = scenes[(step - 1) % len(scenes)]
-        b = sc.batch(args.batch, args.noise_frac, gen)
+        b = sc.batch(args.batch, args.noise_frac, gen, args.harvest_frac if args.harvest_every else 0.0)
         loss = residual_loss(model, sc.image, sc.flags, sc.fluid, b, args.loss)
         opt.zero_grad(set_to_none=True)
         loss.backward()
@@ -206,21 +254,29 @@ def main(argv=None):
             log["loss"].append({"step": step, "loss": lv, "ema": ema, "lr": lr})
             print(f"step {step} loss {lv:.4e} ema {ema:.4e} lr {lr:.2e} ({time.time() - t_train:.0f}s)", flush=True)
         if step % args.eval_every == 0 or step == args.steps:
-            it, st, rel = evaluate(model, val)
+            it, st, rel = val(model)
             log["eval"].append({"step": step, "iterations": it, "status": st, "rel_res": rel})
-            print(f"step {step} eval: {it} its ({st}, {rel:.2e})", flush=True)
-            save(model, out, args, log)
+            score = (it if st == "converged" else 10 ** 9, rel)
+            is_best = score < best
+            if is_best:
+                best = score
+            print(f"step {step} eval: {it} its ({st}, {rel:.2e}){' best' if is_best else ''}", flush=True)
+            save(model, out, args, log, best=is_best)
         if time.time() - t_train > args.time_limit:
             print(f"time limit reached at step {step}", flush=True)
             break
     log["train_s"] = time.time() - t_train
     log["steps_done"] = step
-    save(model, out, args, log)
+    log["best"] = {"iterations": best[0], "rel_res": best[1]}
+    save(model, out, args, log, best=False)
 
 
-def save(model, out: Path, args, log):
+def save(model, out: Path, args, log, best: bool):
+    """The best weights so far (by validation iterations) go to smallsm_l{n}.npz, the latest to *.last.npz."""
     sd = {k: v.detach().float().cpu().numpy() for k, v in model.state_dict().items()}
-    np.savez(out / f"smallsm_l{args.levels}.npz", **sd)
+    if best:
+        np.savez(out / f"smallsm_l{args.levels}.npz", **sd)
+    np.savez(out / f"smallsm_l{args.levels}.last.npz", **sd)
     (out / f"smallsm_l{args.levels}.train.json").write_text(json.dumps(log, indent=1))
 
 

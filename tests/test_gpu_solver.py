@@ -61,6 +61,47 @@ def test_plan_bf16_storage(cuda, storage, act):
     assert err < 2e-2, float(err)
 
 
+@pytest.mark.parametrize("shape,n,seed", [((64, 64, 64), 4, 4), ((32, 48, 64), 3, 9), ((128, 128, 128), 5, 7)])
+@pytest.mark.parametrize("storage", [torch.float32, torch.bfloat16])
+@pytest.mark.parametrize("swap,mask", [(False, False), (True, True)])
+def test_plan_classed_is_bit_identical_to_dense(cuda, shape, n, seed, storage, swap, mask):
+    """Class map + uniform vectors + general-cell records give exactly the dense planes' output."""
+    from mlpcg_gb300.precond import PrecondPlan
+    s, flags, img = _scene(shape, seed, cuda)
+    m = _model(n, cuda, seed=3, swap=swap, mask=mask)
+    dense = PrecondPlan(m, img, storage=storage, layout="dense")
+    cls = PrecondPlan(m, img, storage=storage, layout="classed")
+    g0 = cls.general_cells(0)
+    n0 = int(np.prod(shape))
+    assert 0 < g0 < n0 // 2, g0
+    b = torch.randn(n0, device=cuda)
+    scale = torch.tensor([0.5], device=cuda)
+    zd = dense.apply(b, scale)
+    zc = cls.apply(b, scale)
+    assert torch.equal(zd, zc), float((zd - zc).abs().max())
+    # every stage on its own as well
+    for st in range(2 * n + 1):
+        a = dense.apply_stages(st, st, b, scale)
+        c = cls.apply_stages(st, st, b, scale)
+    torch.cuda.synchronize()
+
+
+def test_plan_classed_uniform_grid(cuda):
+    """An all-fluid interior (only the wall layer differs) is almost entirely uniform."""
+    from mlpcg_gb300.precond import PrecondPlan
+    flags = torch.full((32, 32, 32), 2, dtype=torch.uint8, device=cuda)
+    flags[0], flags[-1], flags[:, 0], flags[:, -1], flags[:, :, 0], flags[:, :, -1] = 0, 0, 0, 0, 0, 0
+    from mlpcg_gb300.solver import flags_to_image
+    img = flags_to_image(flags)
+    m = _model(3, cuda, seed=5)
+    dense = PrecondPlan(m, img, storage=torch.float32, layout="dense")
+    cls = PrecondPlan(m, img, storage=torch.float32, layout="classed")
+    interior = 28 ** 3
+    assert cls.general_cells(0) == 32 ** 3 - interior
+    b = torch.randn(32 ** 3, device=cuda)
+    assert torch.equal(dense.apply(b), cls.apply(b))
+
+
 def test_plan_coefficients_match_linear_blocks(cuda):
     s, flags, img = _scene((32, 32, 32), 5, cuda)
     m = _model(3, cuda)
