@@ -154,6 +154,21 @@ class ClockSampler:
                 "samples": len(rows), "reasons": sorted(reasons)}
 
 
+def max_over_ranks(value: float, world: int, device="cpu") -> float:
+    """Max of a per-rank time over the replicas (each rank solves its own scene)."""
+    if world <= 1:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t)
+
+
+def replica_seed(base_seed: int, rank: int) -> int:
+    """Scene seed of a replica: rank r solves scene base_seed + r."""
+    return base_seed + rank
+
+
 # ----------------------------------------------------------------------------
 # launch accounting
 # ----------------------------------------------------------------------------
@@ -189,7 +204,7 @@ def run_ours(args, rank, world):
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(dev)
     N = args.size
-    scene = make_scene(N, args.seed + rank, args.spheres)
+    scene = make_scene(N, replica_seed(args.seed, rank), args.spheres)
     model, meta = load_model(args, dev)
     flags = torch.as_tensor(scene.flags, device=dev)
     b = torch.as_tensor(scene.rhs, device=dev)
@@ -233,11 +248,7 @@ def run_ours(args, rank, world):
         t_wall = time.perf_counter() - t_wall
     clocks = clk.summary()
     times = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    ms = statistics.mean(times)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t)
+    ms = max_over_ranks(statistics.mean(times), world, dev)
     last = r
     x_fused = last.x.clone()
 

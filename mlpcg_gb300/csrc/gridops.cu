@@ -152,7 +152,7 @@ __global__ void k_axpby(const float *__restrict__ c0, const T *__restrict__ x,
 // pass computes 27 x 3 class sums and the 81 shifted sums follow by
 // inclusion (deterministic: per-block FP64 partials summed in fixed order).
 // ---------------------------------------------------------------------------
-constexpr int kLinBlocks = 128;
+constexpr int kLinBlocks = 512;
 constexpr int kLinThreads = 256;
 
 struct Range1 { int lo, hi; };  // [lo, hi)
@@ -206,9 +206,11 @@ k_class_sums(const float *__restrict__ img, int n1, int n2, int n3, double *__re
 }
 
 // One block of 128 threads: class sums -> 81 shifted means y -> nlin outputs z.
+// Output j uses weights W + j*wstride (81 values), bias[j*bstride], and goes to z[j*zstride].
 __global__ void k_linear_finalize(const double *__restrict__ partial, int nblk, int n1, int n2, int n3,
-                                  const float *__restrict__ W, const float *__restrict__ bias,
-                                  int nlin, float *__restrict__ z, float *__restrict__ yout) {
+                                  const float *__restrict__ W, int64_t wstride, const float *__restrict__ bias,
+                                  int64_t bstride, int nlin, float *__restrict__ z, int64_t zstride,
+                                  float *__restrict__ yout) {
   __shared__ double cs[27 * 3];
   __shared__ double ym[81];
   const int t = threadIdx.x;
@@ -247,8 +249,8 @@ __global__ void k_linear_finalize(const double *__restrict__ partial, int nblk, 
   // z_j = w_j . y + b_j   (w . y in float like the reference's dot, then + bias)
   if (t < nlin) {
     double acc = 0.0;
-    for (int e = 0; e < 81; ++e) acc += (double)W[t * 81 + e] * ym[e];
-    z[t] = (float)(acc + (double)bias[t]);
+    for (int e = 0; e < 81; ++e) acc += (double)W[t * wstride + e] * ym[e];
+    z[t * zstride] = (float)(acc + (double)bias[t * bstride]);
   }
 }
 
@@ -382,15 +384,22 @@ int launch_axpby(const float *c0, const void *x, const float *c1, const void *y,
 
 size_t linear_workspace() { return (size_t)27 * 3 * kLinBlocks * sizeof(double); }
 
-int launch_linear_forward(const float *img, int n1, int n2, int n3, const float *W, const float *bias,
-                          int nlin, float *z, float *y, void *ws, size_t ws_bytes, cudaStream_t st) {
+int launch_linear_forward_strided(const float *img, int n1, int n2, int n3, const float *W, int64_t wstride,
+                                  const float *bias, int64_t bstride, int nlin, float *z, int64_t zstride, float *y,
+                                  void *ws, size_t ws_bytes, cudaStream_t st) {
   MLPCG_REQUIRE(ws_bytes >= linear_workspace(), MLPCG_ERR_WORKSPACE,
                 "sm_linear_3d workspace too small: %zu < %zu", ws_bytes, linear_workspace());
   k_class_sums<<<dim3(kLinBlocks, 27), kLinThreads, 0, st>>>(img, n1, n2, n3, (double *)ws);
   MLPCG_LAUNCH_CHECK();
-  k_linear_finalize<<<1, 128, 0, st>>>((const double *)ws, kLinBlocks, n1, n2, n3, W, bias, nlin, z, y);
+  k_linear_finalize<<<1, 128, 0, st>>>((const double *)ws, kLinBlocks, n1, n2, n3, W, wstride, bias, bstride, nlin,
+                                       z, zstride, y);
   MLPCG_LAUNCH_CHECK();
   return MLPCG_OK;
+}
+
+int launch_linear_forward(const float *img, int n1, int n2, int n3, const float *W, const float *bias,
+                          int nlin, float *z, float *y, void *ws, size_t ws_bytes, cudaStream_t st) {
+  return launch_linear_forward_strided(img, n1, n2, n3, W, 81, bias, 1, nlin, z, 1, y, ws, ws_bytes, st);
 }
 
 int launch_linear_backward(const float *g, const float *y, float *gw, float *gb, cudaStream_t st) {

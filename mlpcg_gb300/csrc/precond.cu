@@ -12,9 +12,13 @@
 //
 // Tile: 2 (x) x 16 (y) x 64 (z) outputs per 128-thread CTA; each thread owns
 // a run of 8 consecutive z cells in 2 x-planes.  The input with its one-cell
-// halo is staged in shared memory (4 x 18 x 66 floats); coefficients stream
-// from HBM as 16-byte vectors (8 BF16 or 4 FP32 values) with the
-// cache-streaming hint, since each is read exactly once per application.
+// halo is staged in shared memory (4 x 18 x 66 floats in rows of 76): the
+// staging issues all of a thread's global loads (16-byte vectors) before its
+// first shared store, and each run reads its 9 input rows as three 16-byte
+// shared loads apiece.  Coefficients stream from HBM as 16-byte vectors
+// (8 BF16 or 4 FP32 values) with the cache-streaming hint, since each is
+// read exactly once per application.
+#include <type_traits>
 #include <vector>
 #include "common.cuh"
 
@@ -24,7 +28,86 @@ constexpr int TZ = 64, TY = 16, TX = 2;
 constexpr int ZT = 8;                 // threads along z, 8 cells each
 constexpr int PT = ZT * TY;           // 128 threads
 constexpr int HZ = TZ + 2, HY = TY + 2, HX = TX + 2;
+constexpr int HZP = 76;               // shared row stride: 16-byte aligned, = 12 (mod 32) floats
 constexpr int CZ = TZ / 2 + 2, CY = TY / 2 + 2, CX = TX / 2 + 2;
+constexpr int NVR = TZ / 4;           // 4-wide vectors in a row's interior
+
+// Thread t owns the runs (tx, run_ty(t), 8 run_tz(t) .. +7).  Each group of 8
+// consecutive lanes covers 4 tz by 2 ty, so with the row stride above the
+// group's 16-byte shared loads of one tile row fall in 8 distinct bank quads.
+__device__ __forceinline__ int run_tz(int t) { return (t & 3) | ((t >> 1) & 4); }
+__device__ __forceinline__ int run_ty(int t) { return ((t >> 2) & 1) | ((t >> 3) & 2) | ((t >> 5) << 2); }
+constexpr unsigned kTyPairLane = 4;   // lane distance between the runs of ty and ty ^ 1
+
+// 4 consecutive values as floats (16-byte / 8-byte aligned vector load)
+__device__ __forceinline__ float4 ldv4(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
+__device__ __forceinline__ float4 ldv4(const __nv_bfloat16 *p) {
+  const uint2 u = __ldg(reinterpret_cast<const uint2 *>(p));
+  return make_float4(__uint_as_float(u.x << 16), __uint_as_float(u.x & 0xffff0000u),
+                     __uint_as_float(u.y << 16), __uint_as_float(u.y & 0xffff0000u));
+}
+
+// The 12 tile values S[row][z .. z + 11] (z a multiple of 4) by three 16-byte loads
+__device__ __forceinline__ void ld_row12(const float *row, float xr[12]) {
+  const float4 a = reinterpret_cast<const float4 *>(row)[0];
+  const float4 b = reinterpret_cast<const float4 *>(row)[1];
+  const float4 c = reinterpret_cast<const float4 *>(row)[2];
+  xr[0] = a.x; xr[1] = a.y; xr[2] = a.z; xr[3] = a.w;
+  xr[4] = b.x; xr[5] = b.y; xr[6] = b.z; xr[7] = b.w;
+  xr[8] = c.x; xr[9] = c.y; xr[10] = c.z; xr[11] = c.w;
+}
+
+// Fine-tile staging in two halves: load() issues every global load of the
+// thread (its 9 interior vectors and at most 2 z-halo values), put() writes
+// them to the tile.  Row r = hx * HY + hy; interior vector v of a row covers
+// k = z0 + 4 v .. + 3 (tile z index 4 v + 1 ..), the halo values k = z0 - 1
+// and z0 + TZ (tile z index 0 and HZ - 1).  Outside the grid the value is 0.
+constexpr int kStageVec = HX * HY * NVR / PT;  // 9
+constexpr int kStageHalo = 2;                  // 2 * HX * HY = 144 halo values over 128 threads
+static_assert(HX * HY * NVR % PT == 0 && 2 * HX * HY <= kStageHalo * PT, "staging split");
+struct FineStage {
+  float4 v[kStageVec];
+  float h[kStageHalo];
+};
+__device__ __forceinline__ int stage_vec_row(int m) { return threadIdx.x / NVR + m * (PT / NVR); }
+__device__ __forceinline__ int stage_halo_id(int m) { return threadIdx.x + m * PT; }
+
+template <typename F4, typename F1>
+__device__ __forceinline__ void stage_load(FineStage &st, int n1, int n2, int n3, F4 ld4, F1 ld1) {
+  const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY, x0 = blockIdx.z * TX;
+  const int k = z0 + 4 * (threadIdx.x % NVR);
+#pragma unroll
+  for (int m = 0; m < kStageVec; ++m) {
+    const int r = stage_vec_row(m), i = x0 + r / HY - 1, j = y0 + r % HY - 1;
+    st.v[m] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if ((unsigned)i < (unsigned)n1 && (unsigned)j < (unsigned)n2 && k < n3)
+      st.v[m] = ld4(i, j, k, ((int64_t)i * n2 + j) * n3 + k);
+  }
+#pragma unroll
+  for (int m = 0; m < kStageHalo; ++m) {
+    const int e = stage_halo_id(m), r = e >> 1;
+    const int i = x0 + r / HY - 1, j = y0 + r % HY - 1, kk = (e & 1) ? z0 + TZ : z0 - 1;
+    st.h[m] = 0.f;
+    if (e < 2 * HX * HY && (unsigned)i < (unsigned)n1 && (unsigned)j < (unsigned)n2 && (unsigned)kk < (unsigned)n3)
+      st.h[m] = ld1(i, j, kk, ((int64_t)i * n2 + j) * n3 + kk);
+  }
+}
+__device__ __forceinline__ void stage_put(float (*S)[HY][HZP], const FineStage &st) {
+  const int v = threadIdx.x % NVR;
+#pragma unroll
+  for (int m = 0; m < kStageVec; ++m) {
+    const int r = stage_vec_row(m);
+    float *row = &S[r / HY][r % HY][4 * v + 1];
+    row[0] = st.v[m].x;
+    *reinterpret_cast<float2 *>(row + 1) = make_float2(st.v[m].y, st.v[m].z);
+    row[3] = st.v[m].w;
+  }
+#pragma unroll
+  for (int m = 0; m < kStageHalo; ++m) {
+    const int e = stage_halo_id(m), r = e >> 1;
+    if (e < 2 * HX * HY) S[r / HY][r % HY][(e & 1) ? HZ - 1 : 0] = st.h[m];
+  }
+}
 
 // ---- 8-wide vector access --------------------------------------------------
 __device__ __forceinline__ void ld8cs(const float *p, float v[8]) {
@@ -76,9 +159,9 @@ __device__ __forceinline__ void st4(__nv_bfloat16 *p, const float v[4]) {
 }
 
 // 27-tap application of one 8-cell run from the staged tile.
-// S is the (HX, HY, HZ) tile, (tx, ty, tz8) the run's position in the tile.
+// S is the (HX, HY, HZP) tile, (tx, ty, tz8) the run's position in the tile.
 template <typename KT>
-__device__ __forceinline__ void apply_run(const float (*S)[HY][HZ], int tx, int ty, int tz8,
+__device__ __forceinline__ void apply_run(const float (*S)[HY][HZP], int tx, int ty, int tz8,
                                           const KT *__restrict__ K, int64_t ps, int64_t q,
                                           float acc[8]) {
 #pragma unroll
@@ -87,10 +170,8 @@ __device__ __forceinline__ void apply_run(const float (*S)[HY][HZ], int tx, int 
   for (int dx = 0; dx < 3; ++dx)
 #pragma unroll
     for (int dy = 0; dy < 3; ++dy) {
-      float xr[10];
-      const float *row = &S[tx + dx][ty + dy][tz8];
-#pragma unroll
-      for (int c = 0; c < 10; ++c) xr[c] = row[c];
+      float xr[12];
+      ld_row12(&S[tx + dx][ty + dy][tz8], xr);
 #pragma unroll
       for (int dz = 0; dz < 3; ++dz) {
         const int p = dx * 9 + dy * 3 + dz;  // the reference's tap order
@@ -124,6 +205,19 @@ __device__ __forceinline__ int material_of(float a, float f, float s) {
   if (a == 0.f && f == 1.f && s == 1.f) return CLS_FLUID;
   return CLS_GENERAL;
 }
+__device__ __forceinline__ uint32_t general_mask(uint2 cw) {
+  uint32_t m = 0;
+#pragma unroll
+  for (int b = 0; b < 4; ++b) {
+    m |= (((cw.x >> (8 * b)) & 0xffu) == CLS_GENERAL ? 1u : 0u) << b;
+    m |= (((cw.y >> (8 * b)) & 0xffu) == CLS_GENERAL ? 1u : 0u) << (4 + b);
+  }
+  return m;
+}
+__device__ __forceinline__ int class_of(uint2 cw, int c) {
+  return (int)(((c < 4 ? cw.x : cw.y) >> (8 * (c & 3))) & 0xffu);
+}
+
 // channel s of the one-hot image value of material cls
 __device__ __forceinline__ float material_channel(int cls, int s) {
   if (cls == CLS_AIR) return s != 1 ? 1.f : 0.f;
@@ -173,45 +267,111 @@ __device__ __forceinline__ int cta_excl_scan(int v, int &total) {
 
 __device__ __forceinline__ unsigned tile_id() { return blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z); }
 
-// number of general cells among the 8-cell runs this thread owns
-__device__ __forceinline__ int count_general(const uint8_t *__restrict__ cls, int n1, int n2, int n3) {
-  const int tz = threadIdx.x % ZT, ty = threadIdx.x / ZT;
-  const int k0 = blockIdx.x * TZ + tz * 8, j = blockIdx.y * TY + ty, x0 = blockIdx.z * TX;
-  int cnt = 0;
-  if (k0 < n3 && j < n2) {
+// class words (8 class bytes) of the thread's two runs; 0 (all solid, no
+// general cell) for a run outside the grid
+__device__ __forceinline__ void load_run_cls(const uint8_t *__restrict__ cls, int n1, int n2, int n3, uint2 cw[TX]) {
+  const int k0 = blockIdx.x * TZ + run_tz(threadIdx.x) * 8, j = blockIdx.y * TY + run_ty(threadIdx.x);
 #pragma unroll
-    for (int tx = 0; tx < TX; ++tx) {
-      const int i = x0 + tx;
-      if (i >= n1) continue;
-      const uint2 c = __ldg(reinterpret_cast<const uint2 *>(cls + ((int64_t)i * n2 + j) * n3 + k0));
-#pragma unroll
-      for (int b = 0; b < 4; ++b) {
-        cnt += ((c.x >> (8 * b)) & 0xffu) == CLS_GENERAL;
-        cnt += ((c.y >> (8 * b)) & 0xffu) == CLS_GENERAL;
-      }
-    }
+  for (int tx = 0; tx < TX; ++tx) {
+    const int i = blockIdx.z * TX + tx;
+    cw[tx] = make_uint2(0u, 0u);
+    if (k0 < n3 && j < n2 && i < n1)
+      cw[tx] = __ldg(reinterpret_cast<const uint2 *>(cls + ((int64_t)i * n2 + j) * n3 + k0));
   }
+}
+
+// number of general cells among the thread's runs
+__device__ __forceinline__ int count_general(const uint2 cw[TX]) {
+  int cnt = 0;
+#pragma unroll
+  for (int tx = 0; tx < TX; ++tx) cnt += __popc(general_mask(cw[tx]));
   return cnt;
 }
 
-// class byte of every cell, number of general cells per tile
+// material code of component c of three channel vectors
+__device__ __forceinline__ uint8_t material_at(float4 a, float4 f, float4 s, int c) {
+  const float av = c == 0 ? a.x : c == 1 ? a.y : c == 2 ? a.z : a.w;
+  const float fv = c == 0 ? f.x : c == 1 ? f.y : c == 2 ? f.z : f.w;
+  const float sv = c == 0 ? s.x : c == 1 ? s.y : c == 2 ? s.z : s.w;
+  return (uint8_t)material_of(av, fv, sv);
+}
+
+// class byte of every cell, number of general cells per tile.  The tile's
+// material codes (with a one-cell halo; outside the grid = solid) are staged
+// in shared memory, loaded as 4-wide vectors of the three image channels; a
+// cell is uniform when all 27 codes around it agree.
 __global__ void __launch_bounds__(PT)
 k_classify(const float *__restrict__ img, int n1, int n2, int n3, uint8_t *__restrict__ cls,
            uint32_t *__restrict__ tcount) {
-  const int tz = threadIdx.x % ZT, ty = threadIdx.x / ZT;
-  const int k0 = blockIdx.x * TZ + tz * 8, j = blockIdx.y * TY + ty, x0 = blockIdx.z * TX;
+  __shared__ __align__(16) uint8_t M[HX][HY][HZP];
+  const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY, x0 = blockIdx.z * TX;
   const int64_t n = cells(n1, n2, n3);
+  {
+    const int v = threadIdx.x % NVR, k = z0 + 4 * v;
+    // the interior in 3 batches of 3 vectors per channel, every load of a batch in flight together
+#pragma unroll
+    for (int b = 0; b < kStageVec / 3; ++b) {
+      float4 ch[3][3];
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        const int r = stage_vec_row(3 * b + m), i = x0 + r / HY - 1, j = y0 + r % HY - 1;
+        const bool in = (unsigned)i < (unsigned)n1 && (unsigned)j < (unsigned)n2 && k < n3;
+        const int64_t q = ((int64_t)i * n2 + j) * n3 + k;
+#pragma unroll
+        for (int s = 0; s < 3; ++s)
+          ch[m][s] = in ? __ldg(reinterpret_cast<const float4 *>(img + s * n + q)) : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        const int r = stage_vec_row(3 * b + m);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) M[r / HY][r % HY][4 * v + 1 + c] = material_at(ch[m][0], ch[m][1], ch[m][2], c);
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < kStageHalo; ++m) {
+      const int e = stage_halo_id(m), r = e >> 1;
+      if (e >= 2 * HX * HY) continue;
+      const int i = x0 + r / HY - 1, j = y0 + r % HY - 1, kk = (e & 1) ? z0 + TZ : z0 - 1;
+      int mc = CLS_SOLID;
+      if ((unsigned)i < (unsigned)n1 && (unsigned)j < (unsigned)n2 && (unsigned)kk < (unsigned)n3) {
+        const int64_t q = ((int64_t)i * n2 + j) * n3 + kk;
+        mc = material_of(img[q], img[n + q], img[2 * n + q]);
+      }
+      M[r / HY][r % HY][(e & 1) ? HZ - 1 : 0] = (uint8_t)mc;
+    }
+  }
+  __syncthreads();
+  const int tz = run_tz(threadIdx.x), ty = run_ty(threadIdx.x);
+  const int k0 = z0 + tz * 8, j = y0 + ty;
   int cnt = 0;
   if (k0 < n3 && j < n2) {
+#pragma unroll
     for (int tx = 0; tx < TX; ++tx) {
       const int i = x0 + tx;
       if (i >= n1) continue;
-      const int64_t q = ((int64_t)i * n2 + j) * n3 + k0;
+      // per cell: the set of material codes seen in its 3 x 3 x 3 neighbourhood, as bits
+      uint32_t seen[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+#pragma unroll
+      for (int dx = 0; dx < 3; ++dx)
+#pragma unroll
+        for (int dy = 0; dy < 3; ++dy) {
+          uint32_t rowbits[10];
+#pragma unroll
+          for (int c = 0; c < 10; ++c) rowbits[c] = 1u << M[tx + dx][ty + dy][tz * 8 + c];
+#pragma unroll
+          for (int c = 0; c < 8; ++c) seen[c] |= rowbits[c] | rowbits[c + 1] | rowbits[c + 2];
+        }
+      uint32_t w[2] = {0u, 0u};
+#pragma unroll
       for (int c = 0; c < 8; ++c) {
-        const int cl = cell_class(img, n1, n2, n3, n, i, j, k0 + c);
-        cls[q + c] = (uint8_t)cl;
+        // uniform: exactly one code seen, and it is not the general code
+        const uint32_t sc = seen[c];
+        const int cl = (__popc(sc) == 1 && !(sc & (1u << CLS_GENERAL))) ? (__ffs(sc) - 1) : CLS_GENERAL;
+        w[c >> 2] |= (uint32_t)cl << (8 * (c & 3));
         cnt += cl == CLS_GENERAL;
       }
+      *reinterpret_cast<uint2 *>(cls + ((int64_t)i * n2 + j) * n3 + k0) = make_uint2(w[0], w[1]);
     }
   }
   int tot;
@@ -277,7 +437,9 @@ __global__ void k_kgen_uniform(const float *__restrict__ W, const float *__restr
   for (int p = 0; p < KREC; ++p) kuni[c * KREC + p] = p < 27 ? round_as((const KT *)nullptr, acc[p]) : 0.f;
 }
 
-// one 32-wide record per general cell, tile by tile in thread/cell order
+// one 32-wide record per general cell, tile by tile in thread/cell order.
+// The tile's general cells are listed in that order in shared memory and the
+// coefficient evaluations (2187 FMA each) are spread over all threads.
 template <typename KT>
 __global__ void __launch_bounds__(PT)
 k_kgen_cls(const float *__restrict__ img, int n1, int n2, int n3, const float *__restrict__ W,
@@ -285,30 +447,32 @@ k_kgen_cls(const float *__restrict__ img, int n1, int n2, int n3, const float *_
            KT *__restrict__ rec) {
   __shared__ float4 sW[81 * 7];
   __shared__ float sb[28];
+  __shared__ uint16_t list[TX * TY * TZ];  // tile-local cell index (tx * TY + ty) * TZ + (k - z0)
   load_weights_smem(W, bias, sW, sb);
-  __syncthreads();
+  const int tz = run_tz(threadIdx.x), ty = run_ty(threadIdx.x);
+  const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY, x0 = blockIdx.z * TX;
+  uint2 cw[TX];
+  load_run_cls(cls, n1, n2, n3, cw);
   int tot;
-  uint32_t rank = tbase[tile_id()] + (uint32_t)cta_excl_scan(count_general(cls, n1, n2, n3), tot);
-  const int tz = threadIdx.x % ZT, ty = threadIdx.x / ZT;
-  const int k0 = blockIdx.x * TZ + tz * 8, j = blockIdx.y * TY + ty, x0 = blockIdx.z * TX;
-  if (k0 >= n3 || j >= n2) return;
-  const FieldGeom g = FieldGeom::make(n1, n2, n3, 0);
-  for (int tx = 0; tx < TX; ++tx) {
-    const int i = x0 + tx;
-    if (i >= n1) continue;
-    const int64_t q = ((int64_t)i * n2 + j) * n3 + k0;
-    for (int c = 0; c < 8; ++c) {
-      if (cls[q + c] != CLS_GENERAL) continue;
-      float acc[28];
-      const int k = k0 + c;
-      coeffs_of_patch(sW, sb, [&](int s, int m, int nn, int o) {
-        return g.at(img + s * g.bstride, i + m - 1, j + nn - 1, k + o - 1);
-      }, acc);
-      KT *r = rec + (size_t)rank * KREC;
+  int pos = cta_excl_scan(count_general(cw), tot);  // its barriers also publish sW, sb
 #pragma unroll
-      for (int p = 0; p < KREC; ++p) stf(r + p, p < 27 ? acc[p] : 0.f);
-      ++rank;
-    }
+  for (int tx = 0; tx < TX; ++tx)
+#pragma unroll
+    for (int c = 0; c < 8; ++c)
+      if (class_of(cw[tx], c) == CLS_GENERAL) list[pos++] = (uint16_t)((tx * TY + ty) * TZ + tz * 8 + c);
+  __syncthreads();
+  const uint32_t base = tbase[tile_id()];
+  const FieldGeom g = FieldGeom::make(n1, n2, n3, 0);
+  for (int e = threadIdx.x; e < tot; e += PT) {
+    const int l = list[e];
+    const int k = z0 + l % TZ, jj = y0 + (l / TZ) % TY, i = x0 + l / (TZ * TY);
+    float acc[28];
+    coeffs_of_patch(sW, sb, [&](int s, int m, int nn, int o) {
+      return g.at(img + s * g.bstride, i + m - 1, jj + nn - 1, k + o - 1);
+    }, acc);
+    KT *r = rec + (size_t)(base + e) * KREC;
+#pragma unroll
+    for (int p = 0; p < KREC; ++p) stf(r + p, p < 27 ? acc[p] : 0.f);
   }
 }
 
@@ -339,52 +503,99 @@ struct CoefArgs {
   const uint32_t *tbase;   // classed: first record index per tile
 };
 
-// classed 27-tap application of one 8-cell run; rank = record index of the
-// run's first general cell, advanced past the run's general cells
-template <typename KT>
-__device__ __forceinline__ void apply_run_cls(const float (*S)[HY][HZ], const float (*Ku)[KREC], int tx, int ty,
-                                              int tz8, const uint8_t *__restrict__ clsrun,
-                                              const KT *__restrict__ rec, uint32_t &rank, float acc[8]) {
-  const uint2 cw = __ldg(reinterpret_cast<const uint2 *>(clsrun));
-  int cl[8];
+constexpr int KU = 33;  // row stride of the uniform vectors in shared memory (no bank conflicts)
+constexpr int TZY = TZ + 4;  // row stride of the mixed-run output tile (16-byte reads without conflicts)
+
+// Shared memory of the classed path: uniform vectors, an output tile for the
+// cells of mixed runs, and the CTA's worklist of mixed runs.
+struct ClsSmem {
+  float Ku[3][KU];
+  __align__(16) float Y[TX][TY][TZY];
+  uint2 run_cw[PT * TX];      // class bytes of the run
+  uint32_t run_rank[PT * TX]; // record index of the run's first general cell
+  uint16_t run_id[PT * TX];   // 2 * thread + tx
+  int nmixed;
+};
+
+// 27-tap application of a run whose cells all use the coefficient vector ku
+__device__ __forceinline__ void apply_run_uniform(const float (*S)[HY][HZP], const float *ku, int tx, int ty, int tz8,
+                                                  float acc[8]) {
 #pragma unroll
-  for (int b = 0; b < 4; ++b) {
-    cl[b] = (cw.x >> (8 * b)) & 0xffu;
-    cl[4 + b] = (cw.y >> (8 * b)) & 0xffu;
-  }
-  bool uni = cl[0] != CLS_GENERAL;
+  for (int c = 0; c < 8; ++c) acc[c] = 0.f;
 #pragma unroll
-  for (int c = 1; c < 8; ++c) uni = uni && cl[c] == cl[0];
-  if (uni) {
-    const float *ku = Ku[cl[0]];
+  for (int dx = 0; dx < 3; ++dx)
 #pragma unroll
-    for (int c = 0; c < 8; ++c) acc[c] = 0.f;
+    for (int dy = 0; dy < 3; ++dy) {
+      float xr[12];
+      ld_row12(&S[tx + dx][ty + dy][tz8], xr);
 #pragma unroll
-    for (int dx = 0; dx < 3; ++dx)
+      for (int dz = 0; dz < 3; ++dz) {
+        const float kv = ku[dx * 9 + dy * 3 + dz];
 #pragma unroll
-      for (int dy = 0; dy < 3; ++dy) {
-        float xr[10];
-        const float *row = &S[tx + dx][ty + dy][tz8];
-#pragma unroll
-        for (int c = 0; c < 10; ++c) xr[c] = row[c];
-#pragma unroll
-        for (int dz = 0; dz < 3; ++dz) {
-          const float kv = ku[dx * 9 + dy * 3 + dz];
-#pragma unroll
-          for (int c = 0; c < 8; ++c) acc[c] = fmaf(kv, xr[c + dz], acc[c]);
-        }
+        for (int c = 0; c < 8; ++c) acc[c] = fmaf(kv, xr[c + dz], acc[c]);
       }
+    }
+}
+
+// acc[tx][c] for the thread's two runs (tx = 0, 1).  Dense: coefficient planes.
+// Classed: runs of one uniform material take the broadcast fast path; the
+// cells of the other runs are spread over the whole CTA (one cell per thread)
+// through a shared-memory worklist, so interface cells do not hold whole warps.
+// cw are the runs' class words (load_run_cls), tile_base the tile's first
+// record index.  All threads of the CTA must call this (it synchronises); S
+// (and, classed, sm->Ku and sm->nmixed = 0) must be visible to all threads.
+template <typename KT, bool CLS>
+__device__ __forceinline__ void tile_apply(const float (*S)[HY][HZP], ClsSmem *sm, const CoefArgs<KT> &C,
+                                           const uint2 cw[TX], uint32_t tile_base, int n1, int n2, int n3,
+                                           float acc[TX][8]) {
+  const int tz = run_tz(threadIdx.x), ty = run_ty(threadIdx.x);
+  const int x0 = blockIdx.z * TX, k0 = blockIdx.x * TZ + tz * 8, j = blockIdx.y * TY + ty;
+  const bool active = k0 < n3 && j < n2;
+  if (!CLS) {
+#pragma unroll
+    for (int tx = 0; tx < TX; ++tx) {
+      const int i = x0 + tx;
+      if (!active || i >= n1) continue;
+      apply_run<KT>(S, tx, ty, tz * 8, C.K, C.ps, ((int64_t)i * n2 + j) * n3 + k0, acc[tx]);
+    }
     return;
   }
+  int tot;
+  uint32_t rank = tile_base + (uint32_t)cta_excl_scan(count_general(cw), tot);
+  bool mixed[TX];
 #pragma unroll
-  for (int c = 0; c < 8; ++c) {
+  for (int tx = 0; tx < TX; ++tx) {
+    mixed[tx] = false;
+    const int i = x0 + tx;
+    if (!active || i >= n1) continue;
+    const int c0 = class_of(cw[tx], 0);
+    const bool uni = c0 != CLS_GENERAL && cw[tx].x == cw[tx].y && cw[tx].x == c0 * 0x01010101u;
+    if (uni) {
+      apply_run_uniform(S, sm->Ku[c0], tx, ty, tz * 8, acc[tx]);
+    } else {
+      mixed[tx] = true;
+      const int slot = atomicAdd(&sm->nmixed, 1);
+      sm->run_cw[slot] = cw[tx];
+      sm->run_rank[slot] = rank;
+      sm->run_id[slot] = (uint16_t)(threadIdx.x * TX + tx);
+      rank += __popc(general_mask(cw[tx]));
+    }
+  }
+  __syncthreads();
+  const int nm = sm->nmixed;
+  for (int e = threadIdx.x; e < nm * 8; e += PT) {
+    const int sl = e >> 3, c = e & 7;
+    const int id = sm->run_id[sl];
+    const int t = id / TX, tx = id % TX, tzz = run_tz(t), tyy = run_ty(t);
+    const uint2 w = sm->run_cw[sl];
+    const int cl = class_of(w, c);
     float k[KREC];
-    if (cl[c] == CLS_GENERAL) {
-      ld_record(rec + (size_t)rank * KREC, k);
-      ++rank;
+    if (cl == CLS_GENERAL) {
+      const uint32_t r = sm->run_rank[sl] + __popc(general_mask(w) & ((1u << c) - 1u));
+      ld_record(C.rec + (size_t)r * KREC, k);
     } else {
 #pragma unroll
-      for (int p = 0; p < 27; ++p) k[p] = Ku[cl[c]][p];
+      for (int p = 0; p < 27; ++p) k[p] = sm->Ku[cl][p];
     }
     float a = 0.f;
 #pragma unroll
@@ -392,58 +603,82 @@ __device__ __forceinline__ void apply_run_cls(const float (*S)[HY][HZ], const fl
 #pragma unroll
       for (int dy = 0; dy < 3; ++dy)
 #pragma unroll
-        for (int dz = 0; dz < 3; ++dz) a = fmaf(k[dx * 9 + dy * 3 + dz], S[tx + dx][ty + dy][tz8 + c + dz], a);
-    acc[c] = a;
+        for (int dz = 0; dz < 3; ++dz)
+          a = fmaf(k[dx * 9 + dy * 3 + dz], S[tx + dx][tyy + dy][tzz * 8 + c + dz], a);
+    sm->Y[tx][tyy][tzz * 8 + c] = a;
   }
+  __syncthreads();
+#pragma unroll
+  for (int tx = 0; tx < TX; ++tx)
+    if (mixed[tx]) {
+      const float4 lo = *reinterpret_cast<const float4 *>(&sm->Y[tx][ty][tz * 8]);
+      const float4 hi = *reinterpret_cast<const float4 *>(&sm->Y[tx][ty][tz * 8 + 4]);
+      acc[tx][0] = lo.x; acc[tx][1] = lo.y; acc[tx][2] = lo.z; acc[tx][3] = lo.w;
+      acc[tx][4] = hi.x; acc[tx][5] = hi.y; acc[tx][6] = hi.z; acc[tx][7] = hi.w;
+    }
+}
+
+// uniform coefficient vectors of a classed block into shared memory
+template <bool CLS>
+__device__ __forceinline__ void stage_uniform(ClsSmem *sm, const float *__restrict__ kuni) {
+  if (!CLS) return;
+  for (int e = threadIdx.x; e < 3 * KREC; e += PT) sm->Ku[e / KREC][e % KREC] = __ldg(kuni + e);
+  if (threadIdx.x == 0) sm->nmixed = 0;
+}
+
+// the class words of the thread's runs and the tile's first record index (classed only)
+template <typename KT, bool CLS>
+__device__ __forceinline__ uint32_t load_tile_cls(const CoefArgs<KT> &C, int n1, int n2, int n3, uint2 cw[TX]) {
+  if (!CLS) return 0u;
+  load_run_cls(C.cls, n1, n2, n3, cw);
+  return __ldg(C.tbase + tile_id());
+}
+
+// mask bytes of the thread's runs (all ones without a mask)
+__device__ __forceinline__ void load_run_mask(const uint8_t *__restrict__ m, int n1, int n2, int n3, uint2 mw[TX]) {
+  const int k0 = blockIdx.x * TZ + run_tz(threadIdx.x) * 8, j = blockIdx.y * TY + run_ty(threadIdx.x);
+#pragma unroll
+  for (int tx = 0; tx < TX; ++tx) {
+    const int i = blockIdx.z * TX + tx;
+    mw[tx] = make_uint2(0xffffffffu, 0xffffffffu);
+    if (m && k0 < n3 && j < n2 && i < n1) mw[tx] = __ldg(reinterpret_cast<const uint2 *>(m + ((int64_t)i * n2 + j) * n3 + k0));
+  }
+}
+__device__ __forceinline__ void apply_run_mask(uint2 m, float acc[8]) {
+#pragma unroll
+  for (int c = 0; c < 8; ++c)
+    if (!((c < 4 ? (m.x >> (8 * c)) : (m.y >> (8 * (c - 4)))) & 0xffu)) acc[c] = 0.f;
 }
 
 // ---------------------------------------------------------------------------
 // pre-block (and the coarsest l-block): y = B(x), optional fused avg-pool
 // ---------------------------------------------------------------------------
-// uniform coefficient vectors of a classed block into shared memory
-template <bool CLS>
-__device__ __forceinline__ void stage_uniform(float (*Ku)[KREC], const float *__restrict__ kuni) {
-  if (CLS)
-    for (int e = threadIdx.x; e < 3 * KREC; e += PT) Ku[e / KREC][e % KREC] = __ldg(kuni + e);
-}
-
-// record index of this thread's first general cell (all threads of the CTA must call)
-template <typename KT, bool CLS>
-__device__ __forceinline__ uint32_t first_rank(const CoefArgs<KT> &C, int n1, int n2, int n3) {
-  if (!CLS) return 0u;
-  int tot;
-  return __ldg(C.tbase + tile_id()) + (uint32_t)cta_excl_scan(count_general(C.cls, n1, n2, n3), tot);
-}
-
-template <typename KT, bool CLS>
-__device__ __forceinline__ void apply_any(const float (*S)[HY][HZ], const float (*Ku)[KREC], int tx, int ty,
-                                          int tz8, const CoefArgs<KT> &C, int64_t q, uint32_t &rank,
-                                          float acc[8]) {
-  if (CLS) apply_run_cls<KT>(S, Ku, tx, ty, tz8, C.cls + q, C.rec, rank, acc);
-  else apply_run<KT>(S, tx, ty, tz8, C.K, C.ps, q, acc);
-}
-
 template <typename KT, typename XT, typename YT, bool POOL, bool CLS>
 __global__ void __launch_bounds__(PT)
 k_pre_fused(const CoefArgs<KT> C, const XT *__restrict__ x,
             const float *__restrict__ xscale, YT *__restrict__ y, YT *__restrict__ ypool,
             const uint8_t *__restrict__ mask, int n1, int n2, int n3) {
-  __shared__ float S[HX][HY][HZ];
-  __shared__ float Ku[CLS ? 3 : 1][KREC];
+  __shared__ __align__(16) float S[HX][HY][HZP];
+  __shared__ typename std::conditional<CLS, ClsSmem, int>::type smc_raw;
+  ClsSmem *smc = CLS ? reinterpret_cast<ClsSmem *>(&smc_raw) : nullptr;
   const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY, x0 = blockIdx.z * TX;
   const float sc = xscale ? __ldg(xscale) : 1.f;
-  for (int e = threadIdx.x; e < HX * HY * HZ; e += PT) {
-    const int hz = e % HZ, t = e / HZ, hy = t % HY, hx = t / HY;
-    const int i = x0 + hx - 1, j = y0 + hy - 1, k = z0 + hz - 1;
-    float v = 0.f;
-    if ((unsigned)i < (unsigned)n1 && (unsigned)j < (unsigned)n2 && (unsigned)k < (unsigned)n3)
-      v = ldf(x + ((int64_t)i * n2 + j) * n3 + k) * sc;
-    S[hx][hy][hz] = v;
-  }
-  stage_uniform<CLS>(Ku, C.kuni);
+  uint2 cw[TX], mw[TX];
+  const uint32_t tb = load_tile_cls<KT, CLS>(C, n1, n2, n3, cw);
+  load_run_mask(mask, n1, n2, n3, mw);
+  FineStage fs;
+  stage_load(fs, n1, n2, n3,
+             [&](int, int, int, int64_t q) {
+               const float4 v = ldv4(x + q);
+               return make_float4(v.x * sc, v.y * sc, v.z * sc, v.w * sc);
+             },
+             [&](int, int, int, int64_t q) { return ldf(x + q) * sc; });
+  stage_put(S, fs);
+  stage_uniform<CLS>(smc, C.kuni);
   __syncthreads();
-  uint32_t rank = first_rank<KT, CLS>(C, n1, n2, n3);
-  const int tz = threadIdx.x % ZT, ty = threadIdx.x / ZT;
+  float acc[TX][8];
+  tile_apply<KT, CLS>(S, smc, C, cw, tb, n1, n2, n3, acc);
+  const int tz = run_tz(threadIdx.x), ty = run_ty(threadIdx.x);
   const int k0 = z0 + tz * 8, j = y0 + ty;
   const bool active = k0 < n3 && j < n2;  // n3 % 8 == 0: a run is all in or all out
   float pool[4] = {0.f, 0.f, 0.f, 0.f};
@@ -452,23 +687,16 @@ k_pre_fused(const CoefArgs<KT> C, const XT *__restrict__ x,
     const int i = x0 + tx;
     if (!active || i >= n1) continue;
     const int64_t q = ((int64_t)i * n2 + j) * n3 + k0;
-    float acc[8];
-    apply_any<KT, CLS>(S, Ku, tx, ty, tz * 8, C, q, rank, acc);
-    if (mask) {
-      const uint2 m = __ldg(reinterpret_cast<const uint2 *>(mask + q));
-#pragma unroll
-      for (int c = 0; c < 8; ++c)
-        if (!((c < 4 ? (m.x >> (8 * c)) : (m.y >> (8 * (c - 4)))) & 0xffu)) acc[c] = 0.f;
-    }
-    st8(y + q, acc);
+    apply_run_mask(mw[tx], acc[tx]);
+    st8(y + q, acc[tx]);
     if (POOL) {
 #pragma unroll
-      for (int c = 0; c < 4; ++c) pool[c] += acc[2 * c] + acc[2 * c + 1];
+      for (int c = 0; c < 4; ++c) pool[c] += acc[tx][2 * c] + acc[tx][2 * c + 1];
     }
   }
   if (POOL) {
 #pragma unroll
-    for (int c = 0; c < 4; ++c) pool[c] += __shfl_xor_sync(0xffffffffu, pool[c], ZT);
+    for (int c = 0; c < 4; ++c) pool[c] += __shfl_xor_sync(0xffffffffu, pool[c], kTyPairLane);
     if (active && (ty & 1) == 0) {
       const int m2 = n2 / 2, m3 = n3 / 2;
       const int64_t qc = ((int64_t)(x0 / 2) * m2 + j / 2) * m3 + k0 / 2;
@@ -494,47 +722,118 @@ __device__ __forceinline__ Lin1 lin1(int f, int n) {
   return r;
 }
 
+// trilinear prolongation at fine z index k from the staged coarse tile, the
+// x / y weights (a, b) already relative to the tile
+__device__ __forceinline__ float up_at(const float (*Cs)[CY][CZ], const Lin1 &a, const Lin1 &b, int k, int m3,
+                                       int cz0) {
+  const Lin1 c = lin1(k, m3);
+  const int e0 = c.i0 - cz0, e1 = c.i1 - cz0;
+  return a.l0 * (b.l0 * (c.l0 * Cs[a.i0][b.i0][e0] + c.l1 * Cs[a.i0][b.i0][e1]) +
+                 b.l1 * (c.l0 * Cs[a.i0][b.i1][e0] + c.l1 * Cs[a.i0][b.i1][e1])) +
+         a.l1 * (b.l0 * (c.l0 * Cs[a.i1][b.i0][e0] + c.l1 * Cs[a.i1][b.i0][e1]) +
+                 b.l1 * (c.l0 * Cs[a.i1][b.i1][e0] + c.l1 * Cs[a.i1][b.i1][e1]));
+}
+__device__ __forceinline__ Lin1 lin1_rel(int f, int n, int base) {
+  Lin1 r = lin1(f, n);
+  r.i0 -= base;
+  r.i1 -= base;
+  return r;
+}
+
+constexpr int CNV = (TZ / 2) / 4;                 // coarse interior vectors per row
+constexpr int kCoarseVec = (CX * CY * CNV + PT - 1) / PT;
+
 template <typename KT, typename CT, typename YT, typename OT, bool SWAP, bool CLS>
 __global__ void __launch_bounds__(PT)
 k_post_fused(const CoefArgs<KT> C, const CT *__restrict__ xc, const YT *__restrict__ yl,
              const float *__restrict__ c0p, const float *__restrict__ c1p, OT *__restrict__ out,
              const uint8_t *__restrict__ bmask, const uint8_t *__restrict__ omask, int n1, int n2, int n3) {
-  __shared__ float S[HX][HY][HZ];
+  __shared__ __align__(16) float S[HX][HY][HZP];
   __shared__ float Cs[CX][CY][CZ];
-  __shared__ float Ku[CLS ? 3 : 1][KREC];
-  stage_uniform<CLS>(Ku, C.kuni);
+  __shared__ typename std::conditional<CLS, ClsSmem, int>::type smc_raw;
+  ClsSmem *smc = CLS ? reinterpret_cast<ClsSmem *>(&smc_raw) : nullptr;
+  stage_uniform<CLS>(smc, C.kuni);
   const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY, x0 = blockIdx.z * TX;
   const int m1 = n1 / 2, m2 = n2 / 2, m3 = n3 / 2;
   const int cx0 = x0 / 2 - 1, cy0 = y0 / 2 - 1, cz0 = z0 / 2 - 1;
   const float c0 = __ldg(c0p), c1 = __ldg(c1p);
-  for (int e = threadIdx.x; e < CX * CY * CZ; e += PT) {
-    const int cz = e % CZ, t = e / CZ, cy = t % CY, cx = t / CY;
-    const int i = cx0 + cx, j = cy0 + cy, k = cz0 + cz;
-    float v = 0.f;
-    if ((unsigned)i < (unsigned)m1 && (unsigned)j < (unsigned)m2 && (unsigned)k < (unsigned)m3)
-      v = ldf(xc + ((int64_t)i * m2 + j) * m3 + k);
-    Cs[cx][cy][cz] = v;
+  uint2 cw[TX], bw[TX], ow[TX];
+  const uint32_t tb = load_tile_cls<KT, CLS>(C, n1, n2, n3, cw);
+  load_run_mask(bmask, n1, n2, n3, bw);
+  load_run_mask(omask, n1, n2, n3, ow);
+  // every global load of the staging in flight together: the coarse tile
+  // (vectors + z-halo) and, with swap, the fine y_l tile
+  float4 cv[kCoarseVec];
+  float ch = 0.f;
+#pragma unroll
+  for (int m = 0; m < kCoarseVec; ++m) {
+    const int e = threadIdx.x + m * PT, r = e / CNV;
+    const int i = cx0 + r / CY, j = cy0 + r % CY, k = cz0 + 1 + 4 * (e % CNV);
+    cv[m] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (e < CX * CY * CNV && (unsigned)i < (unsigned)m1 && (unsigned)j < (unsigned)m2 && k < m3)
+      cv[m] = ldv4(xc + ((int64_t)i * m2 + j) * m3 + k);
+  }
+  {
+    const int e = threadIdx.x, r = e >> 1;
+    const int i = cx0 + r / CY, j = cy0 + r % CY, k = (e & 1) ? cz0 + CZ - 1 : cz0;
+    if (e < 2 * CX * CY && (unsigned)i < (unsigned)m1 && (unsigned)j < (unsigned)m2 && (unsigned)k < (unsigned)m3)
+      ch = ldf(xc + ((int64_t)i * m2 + j) * m3 + k);
+  }
+  if (SWAP) {  // y_l goes straight into the fine tile; the combine below reads it back in place
+    FineStage fs;
+    stage_load(fs, n1, n2, n3, [&](int, int, int, int64_t q) { return ldv4(yl + q); },
+               [&](int, int, int, int64_t q) { return ldf(yl + q); });
+    stage_put(S, fs);
+  }
+#pragma unroll
+  for (int m = 0; m < kCoarseVec; ++m) {
+    const int e = threadIdx.x + m * PT, r = e / CNV, v = e % CNV;
+    if (e >= CX * CY * CNV) continue;
+    float *row = &Cs[r / CY][r % CY][1 + 4 * v];
+    row[0] = cv[m].x; row[1] = cv[m].y; row[2] = cv[m].z; row[3] = cv[m].w;
+  }
+  if (threadIdx.x < 2 * CX * CY) {
+    const int r = threadIdx.x >> 1;
+    Cs[r / CY][r % CY][(threadIdx.x & 1) ? CZ - 1 : 0] = ch;
   }
   __syncthreads();
-  for (int e = threadIdx.x; e < HX * HY * HZ; e += PT) {
-    const int hz = e % HZ, t = e / HZ, hy = t % HY, hx = t / HY;
-    const int i = x0 + hx - 1, j = y0 + hy - 1, k = z0 + hz - 1;
-    float v = 0.f;
-    if ((unsigned)i < (unsigned)n1 && (unsigned)j < (unsigned)n2 && (unsigned)k < (unsigned)n3) {
-      const Lin1 a = lin1(i, m1), b = lin1(j, m2), c = lin1(k, m3);
-      const int a0 = a.i0 - cx0, a1 = a.i1 - cx0, b0 = b.i0 - cy0, b1 = b.i1 - cy0;
-      const int e0 = c.i0 - cz0, e1 = c.i1 - cz0;
-      v = a.l0 * (b.l0 * (c.l0 * Cs[a0][b0][e0] + c.l1 * Cs[a0][b0][e1]) +
-                  b.l1 * (c.l0 * Cs[a0][b1][e0] + c.l1 * Cs[a0][b1][e1])) +
-          a.l1 * (b.l0 * (c.l0 * Cs[a1][b0][e0] + c.l1 * Cs[a1][b0][e1]) +
-                  b.l1 * (c.l0 * Cs[a1][b1][e0] + c.l1 * Cs[a1][b1][e1]));
-      if (SWAP) v = __fadd_rn(__fmul_rn(c0, ldf(yl + ((int64_t)i * n2 + j) * n3 + k)), __fmul_rn(c1, v));
+  // the fine tile: up(x_{l+1}) (with swap: c0 y_l + c1 up(x_{l+1})); 0 outside the grid
+  {
+    const int v = threadIdx.x % NVR;
+#pragma unroll
+    for (int m = 0; m < kStageVec; ++m) {
+      const int r = stage_vec_row(m), i = x0 + r / HY - 1, j = y0 + r % HY - 1, k = z0 + 4 * v;
+      float o[4] = {0.f, 0.f, 0.f, 0.f};
+      float *row = &S[r / HY][r % HY][4 * v + 1];
+      if ((unsigned)i < (unsigned)n1 && (unsigned)j < (unsigned)n2 && k < n3) {
+        const Lin1 a = lin1_rel(i, m1, cx0), b = lin1_rel(j, m2, cy0);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          o[c] = up_at(Cs, a, b, k + c, m3, cz0);
+          if (SWAP) o[c] = __fadd_rn(__fmul_rn(c0, row[c]), __fmul_rn(c1, o[c]));
+        }
+      }
+      row[0] = o[0];
+      *reinterpret_cast<float2 *>(row + 1) = make_float2(o[1], o[2]);
+      row[3] = o[3];
     }
-    S[hx][hy][hz] = v;
+#pragma unroll
+    for (int m = 0; m < kStageHalo; ++m) {
+      const int e = stage_halo_id(m), r = e >> 1;
+      if (e >= 2 * HX * HY) continue;
+      const int i = x0 + r / HY - 1, j = y0 + r % HY - 1, k = (e & 1) ? z0 + TZ : z0 - 1;
+      float o = 0.f;
+      if ((unsigned)i < (unsigned)n1 && (unsigned)j < (unsigned)n2 && (unsigned)k < (unsigned)n3) {
+        o = up_at(Cs, lin1_rel(i, m1, cx0), lin1_rel(j, m2, cy0), k, m3, cz0);
+        if (SWAP) o = __fadd_rn(__fmul_rn(c0, S[r / HY][r % HY][(e & 1) ? HZ - 1 : 0]), __fmul_rn(c1, o));
+      }
+      S[r / HY][r % HY][(e & 1) ? HZ - 1 : 0] = o;
+    }
   }
   __syncthreads();
-  uint32_t rank = first_rank<KT, CLS>(C, n1, n2, n3);
-  const int tz = threadIdx.x % ZT, ty = threadIdx.x / ZT;
+  float accs[TX][8];
+  tile_apply<KT, CLS>(S, smc, C, cw, tb, n1, n2, n3, accs);
+  const int tz = run_tz(threadIdx.x), ty = run_ty(threadIdx.x);
   const int k0 = z0 + tz * 8, j = y0 + ty;
   if (k0 >= n3 || j >= n2) return;
 #pragma unroll
@@ -542,26 +841,15 @@ k_post_fused(const CoefArgs<KT> C, const CT *__restrict__ xc, const YT *__restri
     const int i = x0 + tx;
     if (i >= n1) continue;
     const int64_t q = ((int64_t)i * n2 + j) * n3 + k0;
-    float acc[8];
-    apply_any<KT, CLS>(S, Ku, tx, ty, tz * 8, C, q, rank, acc);
-    if (bmask) {
-      const uint2 m = __ldg(reinterpret_cast<const uint2 *>(bmask + q));
-#pragma unroll
-      for (int c = 0; c < 8; ++c)
-        if (!((c < 4 ? (m.x >> (8 * c)) : (m.y >> (8 * (c - 4)))) & 0xffu)) acc[c] = 0.f;
-    }
+    float *acc = accs[tx];
+    apply_run_mask(bw[tx], acc);
     if (!SWAP) {
       float yv[8];
       ld8(yl + q, yv);
 #pragma unroll
       for (int c = 0; c < 8; ++c) acc[c] = __fadd_rn(__fmul_rn(c0, yv[c]), __fmul_rn(c1, acc[c]));
     }
-    if (omask) {
-      const uint2 m = __ldg(reinterpret_cast<const uint2 *>(omask + q));
-#pragma unroll
-      for (int c = 0; c < 8; ++c)
-        if (!((c < 4 ? (m.x >> (8 * c)) : (m.y >> (8 * (c - 4)))) & 0xffu)) acc[c] = 0.f;
-    }
+    apply_run_mask(ow[tx], acc);
     st8(out + q, acc);
   }
 }
@@ -609,6 +897,8 @@ int launch_axpby(const float *, const void *, const float *, const void *, void 
                  cudaStream_t);
 int launch_linear_forward(const float *, int, int, int, const float *, const float *, int, float *,
                           float *, void *, size_t, cudaStream_t);
+int launch_linear_forward_strided(const float *, int, int, int, const float *, int64_t, const float *, int64_t, int,
+                                  float *, int64_t, float *, void *, size_t, cudaStream_t);
 size_t linear_workspace();
 
 struct PrecondPlan {
@@ -949,11 +1239,10 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
   for (int l = 0; l < L; ++l) {
     const auto &v = P.lv[l];
     const float *im = (l == 0) ? image : P.img[l];
-    const float *w0 = linp + (size_t)l * 82, *w1 = linp + (size_t)(L + l) * 82;
-    RET_IF(launch_linear_forward(im, v.n1, v.n2, v.n3, w0, w0 + 81, 1, P.coef + l, nullptr, P.lin_ws,
-                                 linear_workspace(), st));
-    RET_IF(launch_linear_forward(im, v.n1, v.n2, v.n3, w1, w1 + 81, 1, P.coef + L + l, nullptr, P.lin_ws,
-                                 linear_workspace(), st));
+    // c0[l] and c1[l] in one pass over the level image: their weights are L*82 floats apart
+    const float *w0 = linp + (size_t)l * 82;
+    RET_IF(launch_linear_forward_strided(im, v.n1, v.n2, v.n3, w0, (int64_t)L * 82, w0 + 81, (int64_t)L * 82, 2,
+                                         P.coef + l, L, nullptr, P.lin_ws, linear_workspace(), st));
   }
   P.ready = true;
   return MLPCG_OK;

@@ -30,7 +30,7 @@ enum { ST_RUNNING = 0, ST_CONVERGED = 1, ST_MAXIT = 2, ST_BREAKDOWN = 3, ST_NONF
 enum { M_NPSD = 0, M_NPCG = 1 };
 
 constexpr int RT = 256;          // threads per reduction block
-constexpr int RB_MAX = 1216;     // blocks per reduction kernel (8 x 152 SMs)
+constexpr int RB_MAX = 1216;     // blocks per reduction kernel at most (8 per SM): one ticket atomic each
 constexpr int NRED = 3;          // dot products per kernel at most
 
 struct State {
@@ -175,44 +175,77 @@ struct SrcAxpy {
   __device__ __forceinline__ float load1(uint32_t q) const { return first ? z[q] : fmaf(beta, p[q], z[q]); }
 };
 
-// (A v) on the 4 cells of the group at q (flat index, q % 4 == 0) at (i, j, k0);
-// cen receives v on those cells.  Neighbours are summed in the column order of
-// the assembled CSR row: i-1, j-1, k-1, k+1, j+1, i+1.
+// Everything the 7-point operator needs on one 4-cell group, loaded before
+// any arithmetic so that all of a thread's loads are in flight together.
+// Missing neighbours (outside the grid) get SOLID flags.
+template <typename T>
+struct Nbr4 {
+  uchar4 fc, fxm, fym, fyp, fxp;
+  uint8_t fzm, fzp;
+  T c[4], xm[4], ym[4], yp[4], xp[4];
+  T zm, zp;
+};
+
 template <typename T, typename S>
-__device__ __forceinline__ void lap4(const Vecs &V, uint32_t q, int i, int j, int k0, const S &src, T out[4],
-                                     T cen[4]) {
+__device__ __forceinline__ void nbr_load(const Vecs &V, uint32_t q, int i, int j, int k0, const S &src, Nbr4<T> &N) {
   const uint32_t sy = (uint32_t)V.n3, sx = (uint32_t)V.n2 * (uint32_t)V.n3;
-  const uchar4 fc = ldflags4(V.flags + q);
-  src.load4(q, cen);
+  const uchar4 solid = make_uchar4(MLPCG_SOLID, MLPCG_SOLID, MLPCG_SOLID, MLPCG_SOLID);
+  N.fc = ldflags4(V.flags + q);
+  src.load4(q, N.c);
+  N.fxm = N.fym = N.fyp = N.fxp = solid;
+  N.fzm = N.fzp = MLPCG_SOLID;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) N.xm[c] = N.ym[c] = N.yp[c] = N.xp[c] = T(0);
+  N.zm = N.zp = T(0);
+  if (i > 0) { N.fxm = ldflags4(V.flags + q - sx); src.load4(q - sx, N.xm); }
+  if (j > 0) { N.fym = ldflags4(V.flags + q - sy); src.load4(q - sy, N.ym); }
+  if (k0 > 0) { N.fzm = V.flags[q - 1]; N.zm = src.load1(q - 1); }
+  if (k0 + 4 < V.n3) { N.fzp = V.flags[q + 4]; N.zp = src.load1(q + 4); }
+  if (j < V.n2 - 1) { N.fyp = ldflags4(V.flags + q + sy); src.load4(q + sy, N.yp); }
+  if (i < V.n1 - 1) { N.fxp = ldflags4(V.flags + q + sx); src.load4(q + sx, N.xp); }
+}
+
+// (A v) on the group from its loaded neighbourhood.  Neighbours are summed in
+// the column order of the assembled CSR row: i-1, j-1, k-1, k+1, j+1, i+1.
+template <typename T>
+__device__ __forceinline__ void nbr_apply(const Nbr4<T> &N, T out[4]) {
   T off[4] = {T(0), T(0), T(0), T(0)};
   int d[4] = {0, 0, 0, 0};
   auto take = [&](int c, uint8_t f, T v) {
     if (f == MLPCG_FLUID) { off[c] += v; ++d[c]; }
     else if (f == MLPCG_AIR) { ++d[c]; }
   };
-  auto row = [&](bool inside, uint32_t qq) {
-    if (!inside) return;
-    const uchar4 f = ldflags4(V.flags + qq);
-    T v[4];
-    src.load4(qq, v);
 #pragma unroll
-    for (int c = 0; c < 4; ++c) take(c, lane(f, c), v[c]);
-  };
-  row(i > 0, q - sx);
-  row(j > 0, q - sy);
-  // k - 1
-  if (k0 > 0) take(0, V.flags[q - 1], src.load1(q - 1));
+  for (int c = 0; c < 4; ++c) take(c, lane(N.fxm, c), N.xm[c]);
 #pragma unroll
-  for (int c = 1; c < 4; ++c) take(c, lane(fc, c - 1), cen[c - 1]);
-  // k + 1
+  for (int c = 0; c < 4; ++c) take(c, lane(N.fym, c), N.ym[c]);
+  take(0, N.fzm, N.zm);
 #pragma unroll
-  for (int c = 0; c < 3; ++c) take(c, lane(fc, c + 1), cen[c + 1]);
-  if (k0 + 4 < V.n3) take(3, V.flags[q + 4], src.load1(q + 4));
-  row(j < V.n2 - 1, q + sy);
-  row(i < V.n1 - 1, q + sx);
+  for (int c = 1; c < 4; ++c) take(c, lane(N.fc, c - 1), N.c[c - 1]);
 #pragma unroll
-  for (int c = 0; c < 4; ++c) out[c] = lane(fc, c) == MLPCG_FLUID ? T(d[c]) * cen[c] - off[c] : T(0);
+  for (int c = 0; c < 3; ++c) take(c, lane(N.fc, c + 1), N.c[c + 1]);
+  take(3, N.fzp, N.zp);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) take(c, lane(N.fyp, c), N.yp[c]);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) take(c, lane(N.fxp, c), N.xp[c]);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) out[c] = lane(N.fc, c) == MLPCG_FLUID ? T(d[c]) * N.c[c] - off[c] : T(0);
 }
+
+// (A v) on the 4 cells of the group at q (flat index, q % 4 == 0) at (i, j, k0);
+// cen receives v on those cells.
+template <typename T, typename S>
+__device__ __forceinline__ void lap4(const Vecs &V, uint32_t q, int i, int j, int k0, const S &src, T out[4],
+                                     T cen[4]) {
+  Nbr4<T> N;
+  nbr_load<T>(V, q, i, j, k0, src, N);
+  nbr_apply<T>(N, out);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) cen[c] = N.c[c];
+}
+
+constexpr int UNR = 2;  // groups per thread per loop pass in the streaming kernels
 
 __device__ __forceinline__ void group_coords(const Vecs &V, uint32_t g, uint32_t &q, int &i, int &j, int &k0) {
   q = 4u * g;
@@ -304,22 +337,29 @@ __global__ void __launch_bounds__(RT) k_sd_dots(Vecs V) {
   const float *A1 = V.Ap + (size_t)h * V.n, *A0 = V.Ap + (size_t)hp * V.n;
   const bool two = it >= 2;
   double v[2] = {0.0, 0.0};
-  int cnt = 0;
-  float s1 = 0.f, s0 = 0.f;
-  for (uint32_t g = gtid(); g < V.ngroups; g += gstride()) {
-    float z[4], a[4];
-    ld4(V.z + 4 * g, z);
-    ld4(A1 + 4 * g, a);
+  for (uint32_t g0 = blockIdx.x * RT * UNR + threadIdx.x; g0 < V.ngroups; g0 += gridDim.x * RT * UNR) {
+    float z[UNR][4], a1[UNR][4], a0[UNR][4];
 #pragma unroll
-    for (int c = 0; c < 4; ++c) s1 = fmaf(z[c], a[c], s1);
-    if (two) {
-      ld4(A0 + 4 * g, a);
-#pragma unroll
-      for (int c = 0; c < 4; ++c) s0 = fmaf(z[c], a[c], s0);
+    for (int u = 0; u < UNR; ++u) {
+      const uint32_t g = g0 + u * RT;
+      if (g >= V.ngroups) continue;
+      ld4(V.z + 4 * g, z[u]);
+      ld4(A1 + 4 * g, a1[u]);
+      if (two) ld4(A0 + 4 * g, a0[u]);
     }
-    if (++cnt == 8) { v[0] += s1; v[1] += s0; s1 = s0 = 0.f; cnt = 0; }
+    float s1 = 0.f, s0 = 0.f;
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) {
+      if (g0 + u * RT >= V.ngroups) continue;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        s1 = fmaf(z[u][c], a1[u][c], s1);
+        if (two) s0 = fmaf(z[u][c], a0[u][c], s0);
+      }
+    }
+    v[0] += s1;
+    v[1] += s0;
   }
-  v[0] += s1; v[1] += s0;
   double o[2];
   if (reduce_last<2>(v, V, 1, o) && threadIdx.x == 0) {
     State &W = *V.st;
@@ -339,20 +379,27 @@ __global__ void __launch_bounds__(RT) k_sd_qform(Vecs V) {
   const float *P1 = V.p + (size_t)h * V.n, *P0 = V.p + (size_t)hp * V.n;
   float *Q = V.p + (size_t)hn * V.n;
   const int it = S.it;
-  for (uint32_t g = gtid(); g < V.ngroups; g += gstride()) {
-    float v[4], w[4];
-    ld4(V.z + 4 * g, v);
-    if (it >= 1) {
-      ld4(P1 + 4 * g, w);
+  for (uint32_t g0 = blockIdx.x * RT * UNR + threadIdx.x; g0 < V.ngroups; g0 += gridDim.x * RT * UNR) {
+    float z[UNR][4], a[UNR][4], b[UNR][4];
 #pragma unroll
-      for (int c = 0; c < 4; ++c) v[c] = fmaf(-c1, w[c], v[c]);
+    for (int u = 0; u < UNR; ++u) {
+      const uint32_t q = 4u * (g0 + u * RT);
+      if (g0 + u * RT >= V.ngroups) continue;
+      ld4(V.z + q, z[u]);
+      if (it >= 1) ld4(P1 + q, a[u]);
+      if (it >= 2) ld4(P0 + q, b[u]);
     }
-    if (it >= 2) {
-      ld4(P0 + 4 * g, w);
 #pragma unroll
-      for (int c = 0; c < 4; ++c) v[c] = fmaf(-c0, w[c], v[c]);
+    for (int u = 0; u < UNR; ++u) {
+      const uint32_t q = 4u * (g0 + u * RT);
+      if (g0 + u * RT >= V.ngroups) continue;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        if (it >= 1) z[u][c] = fmaf(-c1, a[u][c], z[u][c]);
+        if (it >= 2) z[u][c] = fmaf(-c0, b[u][c], z[u][c]);
+      }
+      st4(Q + q, z[u]);
     }
-    st4(Q + 4 * g, v);
   }
 }
 
@@ -365,29 +412,26 @@ __global__ void __launch_bounds__(RT) k_sd_spmv(Vecs V) {
   float *AQ = V.Ap + (size_t)hn * V.n;
   const bool has_prev = S.it >= 1;
   double v[3] = {0.0, 0.0, 0.0};
-  float s[3] = {0.f, 0.f, 0.f};
-  int cnt = 0;
   for (uint32_t g = gtid(); g < V.ngroups; g += gstride()) {
     uint32_t q; int i, j, k0;
     group_coords(V, g, q, i, j, k0);
-    float aq[4], qq[4], rq[4];
-    lap4<float>(V, q, i, j, k0, SrcF32{Q}, aq, qq);
-    st4(AQ + q, aq);
+    Nbr4<float> N;
+    nbr_load<float>(V, q, i, j, k0, SrcF32{Q}, N);
+    float rq[4], p1[4];
     ld4(V.r + q, rq);
+    if (has_prev) ld4(P1 + q, p1);
+    float aq[4];
+    nbr_apply<float>(N, aq);
+    st4(AQ + q, aq);
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f;
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
-      s[0] = fmaf(qq[c], aq[c], s[0]);
-      s[1] = fmaf(qq[c], rq[c], s[1]);
+      s0 = fmaf(N.c[c], aq[c], s0);
+      s1 = fmaf(N.c[c], rq[c], s1);
+      if (has_prev) s2 = fmaf(aq[c], p1[c], s2);
     }
-    if (has_prev) {
-      float p1[4];
-      ld4(P1 + q, p1);
-#pragma unroll
-      for (int c = 0; c < 4; ++c) s[2] = fmaf(aq[c], p1[c], s[2]);
-    }
-    if (++cnt == 8) { v[0] += s[0]; v[1] += s[1]; v[2] += s[2]; s[0] = s[1] = s[2] = 0.f; cnt = 0; }
+    v[0] += s0; v[1] += s1; v[2] += s2;
   }
-  v[0] += s[0]; v[1] += s[1]; v[2] += s[2];
   double o[3];
   if (reduce_last<3>(v, V, 2, o) && threadIdx.x == 0) {
     State &W = *V.st;
@@ -474,27 +518,34 @@ __global__ void __launch_bounds__(RT) k_update(Vecs V) {
   const double bd = S.beta;
   const float bf = (float)S.beta;
   double v[1] = {0.0};
-  float s = 0.f;
-  int cnt = 0;
-  for (uint32_t g = gtid(); g < V.ngroups; g += gstride()) {
-    const uint32_t q = 4u * g;
-    float d[4], ad[4], r[4];
-    double x[4];
-    ld4(D + q, d);
-    ld4(AD + q, ad);
-    ld4(V.r + q, r);
-    ld4(V.x + q, x);
+  for (uint32_t g0 = blockIdx.x * RT * UNR + threadIdx.x; g0 < V.ngroups; g0 += gridDim.x * RT * UNR) {
+    float d[UNR][4], ad[UNR][4], r[UNR][4];
+    double x[UNR][4];
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      x[c] = fma(bd, (double)d[c], x[c]);
-      r[c] = fmaf(-bf, ad[c], r[c]);
-      s = fmaf(r[c], r[c], s);
+    for (int u = 0; u < UNR; ++u) {
+      const uint32_t q = 4u * (g0 + u * RT);
+      if (g0 + u * RT >= V.ngroups) continue;
+      ld4(D + q, d[u]);
+      ld4(AD + q, ad[u]);
+      ld4(V.r + q, r[u]);
+      ld4(V.x + q, x[u]);
     }
-    st4(V.x + q, x);
-    st4(V.r + q, r);
-    if (++cnt == 8) { v[0] += s; s = 0.f; cnt = 0; }
+    float s = 0.f;
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) {
+      const uint32_t q = 4u * (g0 + u * RT);
+      if (g0 + u * RT >= V.ngroups) continue;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        x[u][c] = fma(bd, (double)d[u][c], x[u][c]);
+        r[u][c] = fmaf(-bf, ad[u][c], r[u][c]);
+        s = fmaf(r[u][c], r[u][c], s);
+      }
+      st4(V.x + q, x[u]);
+      st4(V.r + q, r[u]);
+    }
+    v[0] += s;
   }
-  v[0] += s;
   double o[1];
   if (reduce_last<1>(v, V, 3, o) && threadIdx.x == 0) {
     State &W = *V.st;
@@ -663,7 +714,7 @@ int mlpcg_solver_bind(mlpcg_solver *s, void *workspace, size_t workspace_bytes, 
   V.ngroups = (uint32_t)(V.n / 4);
   V.fd3 = make_fastdiv((uint32_t)s->n3);
   V.fd2 = make_fastdiv((uint32_t)s->n2);
-  int64_t nb = ((int64_t)V.ngroups + RT * 2 - 1) / (RT * 2);
+  int64_t nb = ((int64_t)V.ngroups + RT * UNR - 1) / (RT * UNR);
   V.nblk = (int)(nb < 1 ? 1 : (nb > RB_MAX ? RB_MAX : nb));
   s->bound = true;
   return MLPCG_OK;

@@ -1,0 +1,42 @@
+"""Multi-GPU runs are replicas (one scene per rank, no collective in the solve): the harness'
+cross-rank reduction checked with 2 gloo ranks on the CPU."""
+import os
+import socket
+
+import pytest
+import torch.multiprocessing as mp
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    return port
+
+
+def _worker(rank, world, port, out):
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import bench
+    v = bench.max_over_ranks(10.0 + 5.0 * rank, world)
+    out[rank] = (v, bench.replica_seed(7, rank))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_max_over_ranks_two_gloo_ranks():
+    world = 2
+    port = _free_port()
+    with mp.Manager() as m:
+        out = m.dict()
+        mp.spawn(_worker, args=(world, port, out), nprocs=world, join=True)
+        res = dict(out)
+    assert res[0][0] == res[1][0] == 15.0
+    assert {res[0][1], res[1][1]} == {7, 8}
+
+
+def test_single_rank_is_identity():
+    import bench
+    assert bench.max_over_ranks(3.5, 1) == 3.5
