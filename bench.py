@@ -12,6 +12,7 @@ flushed between steps.  Also reported:
   * plain_ms   -- the plain FP32 drop-in (reference semantics: coefficients
                   re-evaluated in every block call, FP64 CG vectors, a host
                   round trip per iteration), one solve;
+  * setup_ms / solve_ms -- the step split at the end of the plan setup;
   * stages_ms  -- each preconditioner kernel timed alone;
   * roofline   -- the level-0 pre-block kernel (the largest launch of an
                   iteration) against the measured HBM copy bandwidth;
@@ -182,15 +183,22 @@ def precond_launches(plan):
     cnt += 1
     for l in range(n - 1, -1, -1):
         if fast[l]:
-            cnt += 1
+            cnt += 2 if l == 0 else 1                 # level 0: prolongation pass + block
         else:
             cnt += 3 + (2 if l == 0 else 0)
     return cnt
 
 
 def setup_launches(plan):
+    """Kernel launches of flags -> image plus one plan setup (mirrors mlpcg_precond_setup)."""
     n = plan.levels
-    return 1 + n + 1 + (2 * n + 1) + 4 * n   # image, pyramid, fluid mask, coefficients, c0/c1
+    cls = [plan.layout == "classed" and plan.level_info(l)[1] for l in range(n + 1)]
+    cnt = 1 + n + 1                                # image, pyramid, fluid mask
+    cnt += 2 if any(cls) else 0                    # uniform vectors and material records of all blocks
+    for l in range(n + 1):
+        nb = 2 if l < n else 1
+        cnt += 6 if cls[l] else nb                 # classify, 2 tile scans, list, records, fill | dense planes
+    return cnt + 2 * n                             # c0/c1: class sums + finalize per level
 
 
 # ----------------------------------------------------------------------------
@@ -215,9 +223,11 @@ def run_ours(args, rank, world):
     plan = solver.plan
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
-    def step():
+    def step(mid=None):
         img = flags_to_image(flags)
         solver.set_image(None, img)
+        if mid is not None:
+            mid.record()
         solver.launch(b, use_graph=not args.no_graph)
 
     for _ in range(args.warmup):
@@ -227,6 +237,7 @@ def run_ours(args, rank, world):
 
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    mids = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     its, rels, stats = [], [], []
     with ClockSampler(dev.index) as clk:
         if world > 1:
@@ -236,7 +247,7 @@ def run_ours(args, rank, world):
         for i in range(args.steps):
             flush.zero_()
             starts[i].record()
-            step()
+            step(mids[i])
             ends[i].record()
             r = solver.result(with_history=(i == args.steps - 1))
             its.append(r.iterations)
@@ -248,6 +259,8 @@ def run_ours(args, rank, world):
         t_wall = time.perf_counter() - t_wall
     clocks = clk.summary()
     times = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    setup_ms = statistics.mean(s.elapsed_time(m) for s, m in zip(starts, mids))
+    solve_ms = statistics.mean(m.elapsed_time(e) for m, e in zip(mids, ends))
     ms = max_over_ranks(statistics.mean(times), world, dev)
     last = r
     x_fused = last.x.clone()
@@ -272,8 +285,11 @@ def run_ours(args, rank, world):
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     hbm = peaks.get("hbm_gbs", 6800.0)
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    gen = [plan.general_cells(l) for l in range(plan.levels + 1)]
-    bytes_pre0 = coeff_bytes(plan, 0, n, gen[0]) + n * (4 + 2 + 0.25)   # coefficients, r in, y out, pooled out
+    counts = [plan.class_counts(l) for l in range(plan.levels + 1)]
+    gen = [c[0] for c in counts]
+    mixed = [c[1] for c in counts]
+    # coefficients, r in, y out, pooled out (+ the fluid mask)
+    bytes_pre0 = coeff_bytes(plan, 0, n, mixed[0]) + n * (4 + 2 + 0.25 + (1 if plan.masked else 0))
     achieved = bytes_pre0 / (stage_ms["pre0"] * 1e-3) / 1e9
     traffic = None
     tp = ROOT / "profiles" / "traffic.json"
@@ -284,9 +300,9 @@ def run_ours(args, rank, world):
     roofline = {"kernel": f"k_pre_fused (level 0, {plan.layout} bf16 coefficients)", "bound": "hbm",
                 "achieved": round(achieved, 1), "peak": hbm, "peak_source": peak_src, "unit": "GB/s",
                 "frac": round(achieved / hbm, 4), "traffic": traffic,
-                "algorithmic_bytes": bytes_pre0, "general_cells": gen}
+                "algorithmic_bytes": bytes_pre0, "general_cells": gen, "mixed_runs": mixed}
     # whole-iteration bytes (compulsory traffic of the fused algorithm)
-    per_iter_bytes = iteration_bytes(plan, n, gen)
+    per_iter_bytes = iteration_bytes(plan, n, mixed)
     it_mean = statistics.mean(its)
 
     # ---- e2e: public API from pinned host buffers ----
@@ -318,6 +334,7 @@ def run_ours(args, rank, world):
            "d2h_bytes_per_step": n * 8}
 
     out = {"its": its, "rels": rels, "status": stats, "ms": ms, "times": times, "stage_ms": stage_ms,
+           "setup_ms": setup_ms, "solve_ms": solve_ms,
            "roofline": roofline, "clocks": clocks, "e2e": e2e, "meta": meta, "history": last.history.tolist(),
            "per_iter_bytes": per_iter_bytes, "launches": setup_launches(plan) + 2 +
            it_mean * (precond_launches(plan) + 6), "x": x_fused, "scene": scene, "model": model,
@@ -325,25 +342,28 @@ def run_ours(args, rank, world):
     return out
 
 
-def coeff_bytes(plan, level, n_level, general):
+def coeff_bytes(plan, level, n_level, mixed):
     """Coefficient bytes one block application reads at a level (bf16)."""
-    if general is None or general < 0:
-        return n_level * 27 * 2                         # dense planes
+    if mixed is None or mixed < 0:
+        return n_level * 27 * 2                          # dense planes
     tiles = math.ceil(n_level / (2 * 16 * 64))
-    return n_level * 1 + general * 32 * 2 + tiles * 4   # class bytes, general-cell records, tile offsets
+    return n_level / 8 * 4 + mixed * 27 * 8 * 2 + tiles * 4   # run words, mixed-run records, tile offsets
 
 
-def iteration_bytes(plan, n0, gen):
+def iteration_bytes(plan, n0, mixed):
     """Compulsory HBM bytes of one fused npsd iteration (bf16 coefficients and activations)."""
     total = 0.0
     L = plan.levels
     for l in range(L):
         nl = n0 / 8 ** l
-        kb = coeff_bytes(plan, l, nl, gen[l])
+        kb = coeff_bytes(plan, l, nl, mixed[l])
         sv_in = 4 if l == 0 else 2
         total += kb + nl * (sv_in + 2 + 2 / 8)                  # pre: coefficients, x in, y out, pooled out
-        total += kb + nl * (2 / 8 + 2 + (4 + 1 if l == 0 else 2))  # post: coefficients, coarse, y, out (+mask)
-    total += coeff_bytes(plan, L, n0 / 8 ** L, gen[L]) + (n0 / 8 ** L) * (2 + 2)
+        if l == 0:   # prolongation pass (coarse in, u out), then the block (u, y in, z out, masks)
+            total += nl * (2 / 8 + 2) + kb + nl * (2 + 2 + 4 + (2 if plan.masked else 0))
+        else:        # post: coefficients, coarse, y, out
+            total += kb + nl * (2 / 8 + 2 + 2)
+    total += coeff_bytes(plan, L, n0 / 8 ** L, mixed[L]) + (n0 / 8 ** L) * (2 + 2)
     total += n0 * (12 + 16 + 18 + 32)                   # dots, qform, spmv+dots, update (f32 vectors, f64 x)
     return total
 
@@ -488,6 +508,7 @@ def main():
             "iterations": it_mean, "status": r["status"][-1], "rel_res": r["rels"][-1],
             "history": [round(h, 9) for h in r["history"]],
             "per_iteration_hbm_bytes": r["per_iter_bytes"],
+            "setup_ms": round(r["setup_ms"], 3), "solve_ms": round(r["solve_ms"], 3),
             "stages_ms": {k: round(v, 4) for k, v in r["stage_ms"].items()},
             "roofline": r["roofline"], "cpu_baseline": cpu, "e2e": r["e2e"], "clocks": r["clocks"],
             "gpu_launches": int(r["launches"] * args.steps)}

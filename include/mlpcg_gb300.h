@@ -240,11 +240,13 @@ typedef struct mlpcg_precond mlpcg_precond;
 
 /* Coefficient layouts of a plan.
  * DENSE:   27 planes per block (27 values per cell).
- * CLASSED: one class byte per cell; cells whose 3x3x3 image neighbourhood is
- *          a single one-hot material (solid or outside, air, fluid) use that
- *          material's constant coefficient vector, the others ("general"
- *          cells, near interfaces) a 32-value record.  Bit-identical results,
- *          far less coefficient traffic on scenes made of large regions. */
+ * CLASSED: one word per 8-cell z-run.  A cell whose 3x3x3 image neighbourhood
+ *          is a single one-hot material (solid or outside, air, fluid) has
+ *          that material's constant coefficient vector; a run of 8 such cells
+ *          of one material is described by the material alone, any other
+ *          ("mixed") run by a record of its 27 x 8 coefficients.
+ *          Bit-identical results, far less coefficient traffic on scenes
+ *          made of large regions. */
 #define MLPCG_COEFF_DENSE   0
 #define MLPCG_COEFF_CLASSED 1
 
@@ -255,9 +257,10 @@ typedef struct mlpcg_precond mlpcg_precond;
  * (levels whose z size is not a multiple of 8 always use dense planes). */
 int mlpcg_precond_create(int N1, int N2, int N3, int levels, int k_dtype, int act_dtype,
                          int swap_sm_order, int mask, int coeff_layout, mlpcg_precond **out);
-/* Number of general cells of a classed level after setup (synchronises
- * `stream`); -1 for a dense level. */
-int mlpcg_precond_general_cells(const mlpcg_precond *plan, int level, int64_t *count, void *stream);
+/* After setup (synchronises `stream`): the number of general cells and of
+ * mixed runs (records) of a classed level; -1 for both on a dense level. */
+int mlpcg_precond_class_counts(const mlpcg_precond *plan, int level, int64_t *general_cells, int64_t *mixed_runs,
+                               void *stream);
 /* Device bytes the plan needs (caller allocates, 256-byte aligned). */
 size_t mlpcg_precond_workspace(const mlpcg_precond *plan);
 void mlpcg_precond_destroy(mlpcg_precond *plan);

@@ -100,13 +100,20 @@ struct FieldGeom {
 // sW[(s*27 + 9m+3n+o)*7 + pp] holds W[4pp..4pp+3][s][m][n][o] (p padded to 28),
 // sb[p] the bias.  The summation order (bias, then s, m, n, o) is the order of
 // the reference's loop (sm_block_3d_kernel.cu:53-64); every kernel that
-// produces coefficients goes through this one function, so equal patches give
+// produces coefficients goes through coeffs_of_patch_n, so equal patches give
 // bit-identical coefficients whichever kernel computed them.
+// coeffs_of_patch_n evaluates NB blocks on one patch (each patch value read
+// once): block b's weights at sW + b * kSW, its bias at sb + b * 28; each
+// block's accumulation sequence is the single-block one.
 // ---------------------------------------------------------------------------
-template <typename Patch>
-__device__ __forceinline__ void coeffs_of_patch(const float4 *sW, const float *sb, Patch v, float acc[28]) {
+constexpr int kSW = 81 * 7;  // float4 entries of one block's weights in shared memory
+
+template <int NB, typename Patch>
+__device__ __forceinline__ void coeffs_of_patch_n(const float4 *sW, const float *sb, Patch v, float (*acc)[28]) {
 #pragma unroll
-  for (int p = 0; p < 28; ++p) acc[p] = sb[p];
+  for (int b = 0; b < NB; ++b)
+#pragma unroll
+    for (int p = 0; p < 28; ++p) acc[b][p] = sb[b * 28 + p];
   for (int s = 0; s < 3; ++s) {
 #pragma unroll
     for (int m = 0; m < 3; ++m)
@@ -115,17 +122,24 @@ __device__ __forceinline__ void coeffs_of_patch(const float4 *sW, const float *s
 #pragma unroll
         for (int o = 0; o < 3; ++o) {
           const float x = v(s, m, nn, o);
-          const float4 *w = sW + (s * 27 + m * 9 + nn * 3 + o) * 7;
 #pragma unroll
-          for (int pp = 0; pp < 7; ++pp) {
-            const float4 wv = w[pp];
-            acc[4 * pp + 0] = fmaf(wv.x, x, acc[4 * pp + 0]);
-            acc[4 * pp + 1] = fmaf(wv.y, x, acc[4 * pp + 1]);
-            acc[4 * pp + 2] = fmaf(wv.z, x, acc[4 * pp + 2]);
-            acc[4 * pp + 3] = fmaf(wv.w, x, acc[4 * pp + 3]);
+          for (int b = 0; b < NB; ++b) {
+            const float4 *w = sW + b * kSW + (s * 27 + m * 9 + nn * 3 + o) * 7;
+#pragma unroll
+            for (int pp = 0; pp < 7; ++pp) {
+              const float4 wv = w[pp];
+              acc[b][4 * pp + 0] = fmaf(wv.x, x, acc[b][4 * pp + 0]);
+              acc[b][4 * pp + 1] = fmaf(wv.y, x, acc[b][4 * pp + 1]);
+              acc[b][4 * pp + 2] = fmaf(wv.z, x, acc[b][4 * pp + 2]);
+              acc[b][4 * pp + 3] = fmaf(wv.w, x, acc[b][4 * pp + 3]);
+            }
           }
         }
   }
+}
+template <typename Patch>
+__device__ __forceinline__ void coeffs_of_patch(const float4 *sW, const float *sb, Patch v, float acc[28]) {
+  coeffs_of_patch_n<1>(sW, sb, v, reinterpret_cast<float (*)[28]>(acc));
 }
 
 // Loads W (27 x 81) and bias (27) into the shared-memory layout of coeffs_of_patch.

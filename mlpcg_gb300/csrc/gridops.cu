@@ -152,60 +152,82 @@ __global__ void k_axpby(const float *__restrict__ c0, const T *__restrict__ x,
 // pass computes 27 x 3 class sums and the 81 shifted sums follow by
 // inclusion (deterministic: per-block FP64 partials summed in fixed order).
 // ---------------------------------------------------------------------------
-constexpr int kLinBlocks = 512;
+constexpr int kLinBlocks = 304;
 constexpr int kLinThreads = 256;
+constexpr int kLinWarps = kLinThreads / 32;
 
-struct Range1 { int lo, hi; };  // [lo, hi)
-__device__ __forceinline__ Range1 class_range(int cls, int n) {
-  Range1 r;
-  if (n == 1) { r.lo = (cls == 0) ? 0 : 1; r.hi = (cls == 0) ? 1 : 1; return r; }
-  if (cls == 0) { r.lo = 0; r.hi = 1; }
-  else if (cls == 1) { r.lo = 1; r.hi = n - 1; }
-  else { r.lo = n - 1; r.hi = n; }
-  return r;
-}
+// boundary class of coordinate c on an axis of n cells: first plane 0,
+// interior 1, last plane 2 (a single plane is class 0)
+__device__ __forceinline__ int axis_class(int c, int n) { return c == 0 ? 0 : (c == n - 1 ? 2 : 1); }
 
+// Per-block FP64 partial sums of the 3 image channels over each of the 27
+// classes.  Warps take whole z-rows (i, j), which share the row class
+// (x class, y class); a lane sums its cells by z class in FP32 across the rows
+// of one row class, and the sums go through an FP64 warp reduction into the
+// warp's slots whenever the row class changes.  Deterministic: the row
+// assignment and every reduction order are fixed.
 __global__ void __launch_bounds__(kLinThreads)
 k_class_sums(const float *__restrict__ img, int n1, int n2, int n3, double *__restrict__ partial) {
-  // blockIdx.y = class (cx*9 + cy*3 + cz)
-  const int cls = blockIdx.y;
-  const Range1 rx = class_range(cls / 9, n1), ry = class_range((cls / 3) % 3, n2),
-               rz = class_range(cls % 3, n3);
-  const int64_t ex = rx.hi > rx.lo ? rx.hi - rx.lo : 0;
-  const int64_t ey = ry.hi > ry.lo ? ry.hi - ry.lo : 0;
-  const int64_t ez = rz.hi > rz.lo ? rz.hi - rz.lo : 0;
-  const int64_t cnt = ex * ey * ez;
+  __shared__ double ws[kLinWarps][81];  // per warp: (class * 3 + channel)
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int e = lane; e < 81; e += 32) ws[w][e] = 0.0;
+  __syncwarp();
   const int64_t n = cells(n1, n2, n3);
-  float s0 = 0.f, s1 = 0.f, s2 = 0.f;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < cnt;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    const int k = rz.lo + (int)(e % ez);
-    const int64_t t = e / ez;
-    const int j = ry.lo + (int)(t % ey);
-    const int i = rx.lo + (int)(t / ey);
-    const int64_t q = ((int64_t)i * n2 + j) * n3 + k;
-    s0 += img[q];
-    s1 += img[n + q];
-    s2 += img[2 * n + q];
+  const int64_t rows = (int64_t)n1 * n2;
+  const bool vec = (n3 % 4) == 0 && ((uintptr_t)img & 15) == 0;
+  float a[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};  // [channel][z class]
+  int key = -1;  // current row class (x class * 3 + y class), warp-uniform
+  auto flush = [&]() {
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch)
+#pragma unroll
+      for (int cz = 0; cz < 3; ++cz) {
+        double d = a[ch][cz];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+        if (lane == 0) ws[w][(key * 3 + cz) * 3 + ch] += d;
+        a[ch][cz] = 0.f;
+      }
+  };
+  auto add = [&](int k, float v0, float v1, float v2) {
+    const int cz = axis_class(k, n3);
+    if (cz == 1) { a[0][1] += v0; a[1][1] += v1; a[2][1] += v2; }
+    else if (cz == 0) { a[0][0] += v0; a[1][0] += v1; a[2][0] += v2; }
+    else { a[0][2] += v0; a[1][2] += v1; a[2][2] += v2; }
+  };
+  for (int64_t r = (int64_t)blockIdx.x * kLinWarps + w; r < rows; r += (int64_t)gridDim.x * kLinWarps) {
+    const int i = (int)(r / n2), j = (int)(r % n2);
+    const int nk = axis_class(i, n1) * 3 + axis_class(j, n2);
+    if (nk != key) {
+      if (key >= 0) flush();
+      key = nk;
+    }
+    const float *p = img + r * n3;
+    if (vec) {
+      for (int k = 4 * lane; k < n3; k += 128) {
+        const float4 x0 = __ldg(reinterpret_cast<const float4 *>(p + k));
+        const float4 x1 = __ldg(reinterpret_cast<const float4 *>(p + n + k));
+        const float4 x2 = __ldg(reinterpret_cast<const float4 *>(p + 2 * n + k));
+        add(k, x0.x, x1.x, x2.x);
+        add(k + 1, x0.y, x1.y, x2.y);
+        add(k + 2, x0.z, x1.z, x2.z);
+        add(k + 3, x0.w, x1.w, x2.w);
+      }
+    } else {
+      for (int k = lane; k < n3; k += 32) add(k, __ldg(p + k), __ldg(p + n + k), __ldg(p + 2 * n + k));
+    }
   }
-  __shared__ double red[3][kLinThreads / 32];
-  double d0 = s0, d1 = s1, d2 = s2;
-  for (int o = 16; o > 0; o >>= 1) {
-    d0 += __shfl_xor_sync(0xffffffffu, d0, o);
-    d1 += __shfl_xor_sync(0xffffffffu, d1, o);
-    d2 += __shfl_xor_sync(0xffffffffu, d2, o);
-  }
-  const int w = threadIdx.x / 32, l = threadIdx.x % 32;
-  if (l == 0) { red[0][w] = d0; red[1][w] = d1; red[2][w] = d2; }
+  if (key >= 0) flush();
   __syncthreads();
-  if (threadIdx.x < 3) {
+  if (threadIdx.x < 81) {
     double s = 0.0;
-    for (int ww = 0; ww < kLinThreads / 32; ++ww) s += red[threadIdx.x][ww];
-    partial[((int64_t)cls * 3 + threadIdx.x) * gridDim.x + blockIdx.x] = s;
+#pragma unroll
+    for (int ww = 0; ww < kLinWarps; ++ww) s += ws[ww][threadIdx.x];
+    partial[(int64_t)threadIdx.x * gridDim.x + blockIdx.x] = s;
   }
 }
 
-// One block of 128 threads: class sums -> 81 shifted means y -> nlin outputs z.
+// One block of 1024 threads: class sums -> 81 shifted means y -> nlin outputs z.
 // Output j uses weights W + j*wstride (81 values), bias[j*bstride], and goes to z[j*zstride].
 __global__ void k_linear_finalize(const double *__restrict__ partial, int nblk, int n1, int n2, int n3,
                                   const float *__restrict__ W, int64_t wstride, const float *__restrict__ bias,
@@ -214,10 +236,18 @@ __global__ void k_linear_finalize(const double *__restrict__ partial, int nblk, 
   __shared__ double cs[27 * 3];
   __shared__ double ym[81];
   const int t = threadIdx.x;
-  if (t < 81) {
+  // cs[cls * 3 + channel] = the sum of the blocks' partials (a warp per value, fixed order;
+  // every load of a lane issued before its first add)
+  for (int c = t >> 5; c < 81; c += blockDim.x >> 5) {
     double s = 0.0;
-    for (int b = 0; b < nblk; ++b) s += partial[(int64_t)t * nblk + b];
-    cs[t] = s;  // index cls*3 + channel
+#pragma unroll
+    for (int u = 0; u < (kLinBlocks + 31) / 32; ++u) {
+      const int b = (t & 31) + 32 * u;
+      if (b < nblk) s += partial[(int64_t)c * nblk + b];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((t & 31) == 0) cs[c] = s;
   }
   __syncthreads();
   // shift index k in {0,1,2} (offset k-1) keeps classes: k=0 -> {0,1}, k=1 -> all, k=2 -> {1,2};
@@ -389,9 +419,9 @@ int launch_linear_forward_strided(const float *img, int n1, int n2, int n3, cons
                                   void *ws, size_t ws_bytes, cudaStream_t st) {
   MLPCG_REQUIRE(ws_bytes >= linear_workspace(), MLPCG_ERR_WORKSPACE,
                 "sm_linear_3d workspace too small: %zu < %zu", ws_bytes, linear_workspace());
-  k_class_sums<<<dim3(kLinBlocks, 27), kLinThreads, 0, st>>>(img, n1, n2, n3, (double *)ws);
+  k_class_sums<<<kLinBlocks, kLinThreads, 0, st>>>(img, n1, n2, n3, (double *)ws);
   MLPCG_LAUNCH_CHECK();
-  k_linear_finalize<<<1, 128, 0, st>>>((const double *)ws, kLinBlocks, n1, n2, n3, W, wstride, bias, bstride, nlin,
+  k_linear_finalize<<<1, 1024, 0, st>>>((const double *)ws, kLinBlocks, n1, n2, n3, W, wstride, bias, bstride, nlin,
                                        z, zstride, y);
   MLPCG_LAUNCH_CHECK();
   return MLPCG_OK;

@@ -2,11 +2,14 @@
 // (image, weights), applied by fused, tiled, bandwidth-bound kernels.
 //
 // SmallSMModelDn3D.eval_forward (sm_model_3d.py:180-262) on one rhs becomes
-// 2n+1 launches:
+// 2n+2 launches:
 //   pre_l   y_l = B_pre_l(x_l)          fused with x_{l+1} = avg_pool(y_l)
 //   l       x_n = B_l(x_n)
 //   post_l  x_l = c0_l y_l + c1_l B_post_l(up(x_{l+1}))   (prolongation + combine fused)
 // (or, with swap_sm_order, x_l = B_post_l(c0_l y_l + c1_l up(x_{l+1}))).
+// At the finest level the prolongation is a pass of its own (k_up_fine)
+// whose output the post-block stages like any input: interpolating the
+// tile's halo cells inside the block kernel cost more than the extra pass.
 // Levels whose z size is not a multiple of 8 use the general kernels of
 // stencil.cu / gridops.cu instead.
 //
@@ -18,6 +21,7 @@
 // shared loads apiece.  Coefficients stream from HBM as 16-byte vectors
 // (8 BF16 or 4 FP32 values) with the cache-streaming hint, since each is
 // read exactly once per application.
+#include <algorithm>
 #include <type_traits>
 #include <vector>
 #include "common.cuh"
@@ -30,6 +34,7 @@ constexpr int PT = ZT * TY;           // 128 threads
 constexpr int HZ = TZ + 2, HY = TY + 2, HX = TX + 2;
 constexpr int HZP = 76;               // shared row stride: 16-byte aligned, = 12 (mod 32) floats
 constexpr int CZ = TZ / 2 + 2, CY = TY / 2 + 2, CX = TX / 2 + 2;
+constexpr int CZP = 48;               // coarse-tile row stride: 16-byte aligned, = 16 (mod 32) floats
 constexpr int NVR = TZ / 4;           // 4-wide vectors in a row's interior
 
 // Thread t owns the runs (tx, run_ty(t), 8 run_tz(t) .. +7).  Each group of 8
@@ -158,61 +163,33 @@ __device__ __forceinline__ void st4(__nv_bfloat16 *p, const float v[4]) {
   *reinterpret_cast<uint2 *>(p) = u;
 }
 
-// 27-tap application of one 8-cell run from the staged tile.
-// S is the (HX, HY, HZP) tile, (tx, ty, tz8) the run's position in the tile.
-template <typename KT>
-__device__ __forceinline__ void apply_run(const float (*S)[HY][HZP], int tx, int ty, int tz8,
-                                          const KT *__restrict__ K, int64_t ps, int64_t q,
-                                          float acc[8]) {
-#pragma unroll
-  for (int c = 0; c < 8; ++c) acc[c] = 0.f;
-#pragma unroll
-  for (int dx = 0; dx < 3; ++dx)
-#pragma unroll
-    for (int dy = 0; dy < 3; ++dy) {
-      float xr[12];
-      ld_row12(&S[tx + dx][ty + dy][tz8], xr);
-#pragma unroll
-      for (int dz = 0; dz < 3; ++dz) {
-        const int p = dx * 9 + dy * 3 + dz;  // the reference's tap order
-        float kv[8];
-        ld8cs(K + p * ps + q, kv);
-#pragma unroll
-        for (int c = 0; c < 8; ++c) acc[c] = fmaf(kv[c], xr[c + dz], acc[c]);
-      }
-    }
-}
-
 // ---------------------------------------------------------------------------
 // Classed coefficients.  A block's 27 coefficients at a cell depend only on
 // the 3 x 27 image values around it.  Where those are all one of the three
 // one-hot materials -- solid (or outside the grid) (0,0,0), air (1,0,1),
 // fluid (0,1,1) -- the coefficients are the block's constant vector for that
-// material; only the remaining ("general") cells, near material interfaces,
-// need their own 27 values.  A classed level stores one class byte per cell
-// (shared by the level's blocks), per tile the index of its first general
-// cell, and per block the 3 uniform vectors plus one 32-wide record per
-// general cell, laid out tile by tile in the apply kernels' thread/cell order.
-// Results equal those of the dense planes bit for bit: coeffs_of_patch
+// material ("uniform" cells); the other ("general") cells lie near material
+// interfaces.  A classed level describes each 8-cell z-run (the unit a thread
+// applies) by one word: a run whose 8 cells are uniform cells of one
+// material is that material's run; every other run is "mixed" and has a
+// record of its 27 x 8 coefficients.  The R mixed runs of a tile (numbered in
+// thread / run order) keep their records together, tap-major across the
+// runs -- coefficient p of cell c of the tile's mixed run r at
+// (p * R + r) * 8 + c -- so that a warp's loads of one tap are contiguous,
+// as they are in the dense planes.
+// Results equal those of the dense planes bit for bit: coeffs_of_patch_n
 // produces every value and the 27 taps are summed in the same order.
 // ---------------------------------------------------------------------------
 enum { CLS_SOLID = 0, CLS_AIR = 1, CLS_FLUID = 2, CLS_GENERAL = 3 };
-constexpr int KREC = 32;
+constexpr int KREC = 32;        // uniform vectors: 27 values padded to 32
+constexpr int RREC = 27 * 8;    // coefficients of a mixed run's record
+constexpr uint32_t kMixed = 3;  // run word: bits 0-1 material or kMixed, bits 2.. mixed-run index in the tile
 
 __device__ __forceinline__ int material_of(float a, float f, float s) {
   if (a == 0.f && f == 0.f && s == 0.f) return CLS_SOLID;
   if (a == 1.f && f == 0.f && s == 1.f) return CLS_AIR;
   if (a == 0.f && f == 1.f && s == 1.f) return CLS_FLUID;
   return CLS_GENERAL;
-}
-__device__ __forceinline__ uint32_t general_mask(uint2 cw) {
-  uint32_t m = 0;
-#pragma unroll
-  for (int b = 0; b < 4; ++b) {
-    m |= (((cw.x >> (8 * b)) & 0xffu) == CLS_GENERAL ? 1u : 0u) << b;
-    m |= (((cw.y >> (8 * b)) & 0xffu) == CLS_GENERAL ? 1u : 0u) << (4 + b);
-  }
-  return m;
 }
 __device__ __forceinline__ int class_of(uint2 cw, int c) {
   return (int)(((c < 4 ? cw.x : cw.y) >> (8 * (c & 3))) & 0xffu);
@@ -223,23 +200,6 @@ __device__ __forceinline__ float material_channel(int cls, int s) {
   if (cls == CLS_AIR) return s != 1 ? 1.f : 0.f;
   if (cls == CLS_FLUID) return s != 0 ? 1.f : 0.f;
   return 0.f;
-}
-
-__device__ __forceinline__ int cell_class(const float *__restrict__ img, int n1, int n2, int n3, int64_t n, int i,
-                                          int j, int k) {
-  int cls = -1;
-  for (int o = 0; o < 27; ++o) {
-    const int ii = i + o / 9 - 1, jj = j + (o / 3) % 3 - 1, kk = k + o % 3 - 1;
-    int c = CLS_SOLID;
-    if ((unsigned)ii < (unsigned)n1 && (unsigned)jj < (unsigned)n2 && (unsigned)kk < (unsigned)n3) {
-      const int64_t q = ((int64_t)ii * n2 + jj) * n3 + kk;
-      c = material_of(img[q], img[n + q], img[2 * n + q]);
-    }
-    if (c == CLS_GENERAL) return CLS_GENERAL;
-    if (cls < 0) cls = c;
-    else if (c != cls) return CLS_GENERAL;
-  }
-  return cls;
 }
 
 // exclusive scan of one int per thread over the PT threads of a CTA
@@ -267,25 +227,16 @@ __device__ __forceinline__ int cta_excl_scan(int v, int &total) {
 
 __device__ __forceinline__ unsigned tile_id() { return blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z); }
 
-// class words (8 class bytes) of the thread's two runs; 0 (all solid, no
-// general cell) for a run outside the grid
-__device__ __forceinline__ void load_run_cls(const uint8_t *__restrict__ cls, int n1, int n2, int n3, uint2 cw[TX]) {
+// run words of the thread's two runs (uniform solid for a run outside the grid)
+__device__ __forceinline__ void load_run_words(const uint32_t *__restrict__ rw, int n1, int n2, int n3,
+                                               uint32_t w[TX]) {
   const int k0 = blockIdx.x * TZ + run_tz(threadIdx.x) * 8, j = blockIdx.y * TY + run_ty(threadIdx.x);
 #pragma unroll
   for (int tx = 0; tx < TX; ++tx) {
     const int i = blockIdx.z * TX + tx;
-    cw[tx] = make_uint2(0u, 0u);
-    if (k0 < n3 && j < n2 && i < n1)
-      cw[tx] = __ldg(reinterpret_cast<const uint2 *>(cls + ((int64_t)i * n2 + j) * n3 + k0));
+    w[tx] = CLS_SOLID;
+    if (k0 < n3 && j < n2 && i < n1) w[tx] = __ldg(rw + ((((int64_t)i * n2 + j) * n3 + k0) >> 3));
   }
-}
-
-// number of general cells among the thread's runs
-__device__ __forceinline__ int count_general(const uint2 cw[TX]) {
-  int cnt = 0;
-#pragma unroll
-  for (int tx = 0; tx < TX; ++tx) cnt += __popc(general_mask(cw[tx]));
-  return cnt;
 }
 
 // material code of component c of three channel vectors
@@ -296,13 +247,14 @@ __device__ __forceinline__ uint8_t material_at(float4 a, float4 f, float4 s, int
   return (uint8_t)material_of(av, fv, sv);
 }
 
-// class byte of every cell, number of general cells per tile.  The tile's
-// material codes (with a one-cell halo; outside the grid = solid) are staged
-// in shared memory, loaded as 4-wide vectors of the three image channels; a
-// cell is uniform when all 27 codes around it agree.
+// Class byte of every cell, the word of every run, and per tile the numbers
+// of mixed runs (rcount) and of general cells (gcount).  The tile's material
+// codes (with a one-cell halo; outside the grid = solid) are staged in shared
+// memory, loaded as 4-wide vectors of the three image channels; a cell is
+// uniform when all 27 codes around it agree.
 __global__ void __launch_bounds__(PT)
 k_classify(const float *__restrict__ img, int n1, int n2, int n3, uint8_t *__restrict__ cls,
-           uint32_t *__restrict__ tcount) {
+           uint32_t *__restrict__ rw, uint32_t *__restrict__ rcount, uint32_t *__restrict__ gcount) {
   __shared__ __align__(16) uint8_t M[HX][HY][HZP];
   const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY, x0 = blockIdx.z * TX;
   const int64_t n = cells(n1, n2, n3);
@@ -344,7 +296,9 @@ k_classify(const float *__restrict__ img, int n1, int n2, int n3, uint8_t *__res
   __syncthreads();
   const int tz = run_tz(threadIdx.x), ty = run_ty(threadIdx.x);
   const int k0 = z0 + tz * 8, j = y0 + ty;
-  int cnt = 0;
+  int ngen = 0, nmixed = 0;
+  uint32_t word[TX] = {CLS_SOLID, CLS_SOLID};
+  bool mixed[TX] = {false, false};
   if (k0 < n3 && j < n2) {
 #pragma unroll
     for (int tx = 0; tx < TX; ++tx) {
@@ -362,21 +316,38 @@ k_classify(const float *__restrict__ img, int n1, int n2, int n3, uint8_t *__res
 #pragma unroll
           for (int c = 0; c < 8; ++c) seen[c] |= rowbits[c] | rowbits[c + 1] | rowbits[c + 2];
         }
-      uint32_t w[2] = {0u, 0u};
+      uint32_t w[2] = {0u, 0u}, all = 0u;
 #pragma unroll
       for (int c = 0; c < 8; ++c) {
         // uniform: exactly one code seen, and it is not the general code
         const uint32_t sc = seen[c];
         const int cl = (__popc(sc) == 1 && !(sc & (1u << CLS_GENERAL))) ? (__ffs(sc) - 1) : CLS_GENERAL;
         w[c >> 2] |= (uint32_t)cl << (8 * (c & 3));
-        cnt += cl == CLS_GENERAL;
+        ngen += cl == CLS_GENERAL;
+        all |= 1u << cl;
       }
       *reinterpret_cast<uint2 *>(cls + ((int64_t)i * n2 + j) * n3 + k0) = make_uint2(w[0], w[1]);
+      mixed[tx] = __popc(all) != 1 || (all & (1u << CLS_GENERAL));
+      word[tx] = mixed[tx] ? kMixed : (uint32_t)(__ffs(all) - 1);
+      nmixed += mixed[tx];
     }
   }
-  int tot;
-  cta_excl_scan(cnt, tot);
-  if (threadIdx.x == 0) tcount[tile_id()] = (uint32_t)tot;
+  int rtot, gtot;
+  int pos = cta_excl_scan(nmixed, rtot);
+  cta_excl_scan(ngen, gtot);
+  if (k0 < n3 && j < n2) {
+#pragma unroll
+    for (int tx = 0; tx < TX; ++tx) {
+      const int i = x0 + tx;
+      if (i >= n1) continue;
+      if (mixed[tx]) word[tx] |= (uint32_t)(pos++) << 2;
+      rw[(((int64_t)i * n2 + j) * n3 + k0) >> 3] = word[tx];
+    }
+  }
+  if (threadIdx.x == 0) {
+    rcount[tile_id()] = (uint32_t)rtot;
+    gcount[tile_id()] = (uint32_t)gtot;
+  }
 }
 
 // exclusive prefix sum of the tile counts (one CTA of 1024 threads)
@@ -422,74 +393,142 @@ __device__ __forceinline__ float round_as(const __nv_bfloat16 *, float v) {
   return __bfloat162float(__float2bfloat16_rn(v));
 }
 
-// the block's coefficient vector of each uniform material (rounded like the stored dtype)
+// The coefficient vector of each uniform material for every block of the
+// model (blockIdx.x = parameter block b, at params + b * 2214), rounded like
+// the stored dtype: thread (c, p) evaluates output p of material c in the
+// accumulation order of coeffs_of_patch_n, so it equals what that function
+// yields on a patch of material c.
 template <typename KT>
-__global__ void k_kgen_uniform(const float *__restrict__ W, const float *__restrict__ bias, float *__restrict__ kuni) {
-  __shared__ float4 sW[81 * 7];
-  __shared__ float sb[28];
-  load_weights_smem(W, bias, sW, sb);
-  __syncthreads();
-  if (threadIdx.x >= 3) return;
-  const int c = threadIdx.x;
-  float acc[28];
-  coeffs_of_patch(sW, sb, [&](int s, int, int, int) { return material_channel(c, s); }, acc);
+__global__ void __launch_bounds__(3 * KREC)
+k_kgen_uniform_all(const float *__restrict__ params, float *__restrict__ kuni) {
+  const int b = blockIdx.x, c = threadIdx.x / KREC, p = threadIdx.x % KREC;
+  const float *W = params + (size_t)b * 2214, *bias = W + 2187;
+  float acc = 0.f;
+  if (p < 27) {
+    acc = __ldg(bias + p);
+    for (int s = 0; s < 3; ++s) {
+      const float x = material_channel(c, s);
 #pragma unroll
-  for (int p = 0; p < KREC; ++p) kuni[c * KREC + p] = p < 27 ? round_as((const KT *)nullptr, acc[p]) : 0.f;
+      for (int t = 0; t < 27; ++t) acc = fmaf(__ldg(W + p * 81 + s * 27 + t), x, acc);
+    }
+    acc = round_as((const KT *)nullptr, acc);
+  }
+  kuni[(size_t)b * 3 * KREC + threadIdx.x] = acc;
 }
 
-// one 32-wide record per general cell, tile by tile in thread/cell order.
-// The tile's general cells are listed in that order in shared memory and the
-// coefficient evaluations (2187 FMA each) are spread over all threads.
-template <typename KT>
+// The linear index of every general cell, tile by tile in thread / run / cell
+// order: list[gbase[tile] + rank] = q.
 __global__ void __launch_bounds__(PT)
-k_kgen_cls(const float *__restrict__ img, int n1, int n2, int n3, const float *__restrict__ W,
-           const float *__restrict__ bias, const uint8_t *__restrict__ cls, const uint32_t *__restrict__ tbase,
-           KT *__restrict__ rec) {
-  __shared__ float4 sW[81 * 7];
-  __shared__ float sb[28];
-  __shared__ uint16_t list[TX * TY * TZ];  // tile-local cell index (tx * TY + ty) * TZ + (k - z0)
-  load_weights_smem(W, bias, sW, sb);
-  const int tz = run_tz(threadIdx.x), ty = run_ty(threadIdx.x);
-  const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY, x0 = blockIdx.z * TX;
+k_list_general(const uint8_t *__restrict__ cls, int n1, int n2, int n3, const uint32_t *__restrict__ gbase,
+               uint32_t *__restrict__ list) {
+  const int k0 = blockIdx.x * TZ + run_tz(threadIdx.x) * 8, j = blockIdx.y * TY + run_ty(threadIdx.x);
   uint2 cw[TX];
-  load_run_cls(cls, n1, n2, n3, cw);
-  int tot;
-  int pos = cta_excl_scan(count_general(cw), tot);  // its barriers also publish sW, sb
+  uint32_t gm[TX];
+  int cnt = 0;
 #pragma unroll
-  for (int tx = 0; tx < TX; ++tx)
+  for (int tx = 0; tx < TX; ++tx) {
+    const int i = blockIdx.z * TX + tx;
+    cw[tx] = make_uint2(0u, 0u);
+    if (k0 < n3 && j < n2 && i < n1)
+      cw[tx] = __ldg(reinterpret_cast<const uint2 *>(cls + ((int64_t)i * n2 + j) * n3 + k0));
+    gm[tx] = 0u;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) gm[tx] |= (class_of(cw[tx], c) == CLS_GENERAL ? 1u : 0u) << c;
+    cnt += __popc(gm[tx]);
+  }
+  int tot;
+  uint32_t pos = __ldg(gbase + tile_id()) + (uint32_t)cta_excl_scan(cnt, tot);
+#pragma unroll
+  for (int tx = 0; tx < TX; ++tx) {
+    if (!gm[tx]) continue;
+    const uint32_t q0 = (uint32_t)((((int64_t)blockIdx.z * TX + tx) * n2 + j) * n3 + k0);
 #pragma unroll
     for (int c = 0; c < 8; ++c)
-      if (class_of(cw[tx], c) == CLS_GENERAL) list[pos++] = (uint16_t)((tx * TY + ty) * TZ + tz * 8 + c);
-  __syncthreads();
-  const uint32_t base = tbase[tile_id()];
-  const FieldGeom g = FieldGeom::make(n1, n2, n3, 0);
-  for (int e = threadIdx.x; e < tot; e += PT) {
-    const int l = list[e];
-    const int k = z0 + l % TZ, jj = y0 + (l / TZ) % TY, i = x0 + l / (TZ * TY);
-    float acc[28];
-    coeffs_of_patch(sW, sb, [&](int s, int m, int nn, int o) {
-      return g.at(img + s * g.bstride, i + m - 1, jj + nn - 1, k + o - 1);
-    }, acc);
-    KT *r = rec + (size_t)(base + e) * KREC;
-#pragma unroll
-    for (int p = 0; p < KREC; ++p) stf(r + p, p < 27 ? acc[p] : 0.f);
+      if (gm[tx] & (1u << c)) list[pos++] = q0 + c;
   }
 }
 
-// coefficients of one general cell's record as floats
-__device__ __forceinline__ void ld_record(const float *r, float k[KREC]) {
+// Where the coefficients of cell q (in a mixed run) live: coefficient p at
+// offset + p * stride of the level's record array.
+struct RecPos {
+  size_t offset, stride;
+};
+__device__ __forceinline__ RecPos rec_pos(const uint32_t *__restrict__ rw, const uint32_t *__restrict__ rbase,
+                                          const uint32_t *__restrict__ rcount, uint32_t q, int i, int j, int k,
+                                          int n2, int n3) {
+  const uint32_t tile = (uint32_t)(k / TZ) + (uint32_t)((n3 + TZ - 1) / TZ) *
+                        ((uint32_t)(j / TY) + (uint32_t)((n2 + TY - 1) / TY) * (uint32_t)(i / TX));
+  const size_t R = __ldg(rcount + tile);
+  RecPos rp;
+  rp.offset = (size_t)__ldg(rbase + tile) * RREC + (size_t)(__ldg(rw + (q >> 3)) >> 2) * 8 + (q & 7u);
+  rp.stride = R * 8;
+  return rp;
+}
+
+// The coefficients of every general cell for NB blocks of one level at once
+// (the pre- and post-block share the level's image and run words), written
+// into the records of their runs.  Thread e of the grid-stride loop evaluates
+// list[e]; the count of general cells is read on the device.
+template <typename KT, int NB>
+__global__ void __launch_bounds__(PT)
+k_kgen_list(const float *__restrict__ img, int n1, int n2, int n3, const float *__restrict__ params, int b0, int b1,
+            const uint32_t *__restrict__ list, const uint32_t *__restrict__ glast_base,
+            const uint32_t *__restrict__ glast_count, const uint32_t *__restrict__ rw,
+            const uint32_t *__restrict__ rbase, const uint32_t *__restrict__ rcount, KT *__restrict__ rec0,
+            KT *__restrict__ rec1) {
+  __shared__ float4 sW[NB * kSW];
+  __shared__ float sb[NB * 28];
 #pragma unroll
-  for (int v = 0; v < KREC / 4; ++v) {
-    const float4 a = __ldg(reinterpret_cast<const float4 *>(r) + v);
-    k[4 * v] = a.x; k[4 * v + 1] = a.y; k[4 * v + 2] = a.z; k[4 * v + 3] = a.w;
+  for (int b = 0; b < NB; ++b) {
+    const float *W = params + (size_t)(b ? b1 : b0) * 2214;
+    load_weights_smem(W, W + 2187, sW + b * kSW, sb + b * 28);
+  }
+  __syncthreads();
+  const uint32_t G = __ldg(glast_base) + __ldg(glast_count);
+  const FieldGeom g = FieldGeom::make(n1, n2, n3, 0);
+  for (uint32_t e = blockIdx.x * PT + threadIdx.x; e < G; e += gridDim.x * PT) {
+    const uint32_t q = __ldg(list + e);
+    const int k = (int)(q % (uint32_t)n3);
+    const uint32_t t = q / (uint32_t)n3;
+    const int j = (int)(t % (uint32_t)n2), i = (int)(t / (uint32_t)n2);
+    float acc[NB][28];
+    coeffs_of_patch_n<NB>(sW, sb, [&](int s, int m, int nn, int o) {
+      return g.at(img + s * g.bstride, i + m - 1, j + nn - 1, k + o - 1);
+    }, acc);
+    const RecPos rp = rec_pos(rw, rbase, rcount, q, i, j, k, n2, n3);
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      KT *r = (b ? rec1 : rec0) + rp.offset;
+#pragma unroll
+      for (int p = 0; p < 27; ++p) stf(r + p * rp.stride, acc[b][p]);
+    }
   }
 }
-__device__ __forceinline__ void ld_record(const __nv_bfloat16 *r, float k[KREC]) {
+
+// The uniform cells of the mixed runs: their material's vector, for NB blocks
+// (uniform vectors at kuni0 / kuni1).  One thread per cell of the level.
+template <typename KT, int NB>
+__global__ void __launch_bounds__(256)
+k_fill_uniform(const uint8_t *__restrict__ cls, const uint32_t *__restrict__ rw, const uint32_t *__restrict__ rbase,
+               const uint32_t *__restrict__ rcount, int n1, int n2, int n3, const float *__restrict__ kuni0,
+               const float *__restrict__ kuni1, KT *__restrict__ rec0, KT *__restrict__ rec1) {
+  const int64_t n = cells(n1, n2, n3);
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t word = __ldg(rw + (q >> 3));
+    if ((word & 3u) != kMixed) continue;
+    const int cl = cls[q];
+    if (cl == CLS_GENERAL) continue;
+    const int k = (int)(q % n3);
+    const int64_t t = q / n3;
+    const int j = (int)(t % n2), i = (int)(t / n2);
+    const RecPos rp = rec_pos(rw, rbase, rcount, (uint32_t)q, i, j, k, n2, n3);
 #pragma unroll
-  for (int v = 0; v < KREC / 8; ++v) {
-    const uint4 u = __ldg(reinterpret_cast<const uint4 *>(r) + v);
-    unpack_bf16x2(u.x, k[8 * v + 0], k[8 * v + 1]); unpack_bf16x2(u.y, k[8 * v + 2], k[8 * v + 3]);
-    unpack_bf16x2(u.z, k[8 * v + 4], k[8 * v + 5]); unpack_bf16x2(u.w, k[8 * v + 6], k[8 * v + 7]);
+    for (int b = 0; b < NB; ++b) {
+      const float *ku = (b ? kuni1 : kuni0) + cl * KREC;
+      KT *r = (b ? rec1 : rec0) + rp.offset;
+#pragma unroll
+      for (int p = 0; p < 27; ++p) stf(r + p * rp.stride, __ldg(ku + p));
+    }
   }
 }
 
@@ -497,125 +536,117 @@ template <typename KT>
 struct CoefArgs {
   const KT *K;             // dense: 27 planes ...
   int64_t ps;              // ... of this stride
-  const KT *rec;           // classed: general-cell records
+  const KT *rec;           // classed: mixed-run records
+  const KT *mrec;          // classed: a record for each material (its vector, each value 8 times)
   const float *kuni;       // classed: 3 x KREC uniform vectors
-  const uint8_t *cls;      // classed: class byte per cell
-  const uint32_t *tbase;   // classed: first record index per tile
+  const uint32_t *rw;      // classed: run words
+  const uint32_t *rbase;   // classed: first record index per tile
+  const uint32_t *rcount;  // classed: mixed runs per tile
 };
+
+// The material records of every block: block b, material m, coefficient p,
+// cell c at mrec[((b * 3 + m) * 27 + p) * 8 + c] = kuni[b][m][p].
+template <typename KT>
+__global__ void __launch_bounds__(256) k_material_records(const float *__restrict__ kuni, KT *__restrict__ mrec) {
+  const int b = blockIdx.x;
+  for (int e = threadIdx.x; e < 3 * RREC; e += blockDim.x) {
+    const int m = e / RREC, p = (e % RREC) / 8;
+    stf(mrec + (size_t)b * 3 * RREC + e, kuni[((size_t)b * 3 + m) * KREC + p]);
+  }
+}
 
 constexpr int KU = 33;  // row stride of the uniform vectors in shared memory (no bank conflicts)
-constexpr int TZY = TZ + 4;  // row stride of the mixed-run output tile (16-byte reads without conflicts)
 
-// Shared memory of the classed path: uniform vectors, an output tile for the
-// cells of mixed runs, and the CTA's worklist of mixed runs.
+// Shared memory of the classed path: the uniform vectors
 struct ClsSmem {
   float Ku[3][KU];
-  __align__(16) float Y[TX][TY][TZY];
-  uint2 run_cw[PT * TX];      // class bytes of the run
-  uint32_t run_rank[PT * TX]; // record index of the run's first general cell
-  uint16_t run_id[PT * TX];   // 2 * thread + tx
-  int nmixed;
 };
 
-// 27-tap application of a run whose cells all use the coefficient vector ku
-__device__ __forceinline__ void apply_run_uniform(const float (*S)[HY][HZP], const float *ku, int tx, int ty, int tz8,
-                                                  float acc[8]) {
+// The thread's two runs (tx = 0, 1) against the staged tile, rows shared:
+// plane pl = tx + dx of the tile serves run 0 as dx = pl and run 1 as
+// dx = pl - 1, so each of the 12 input rows is read from shared memory once.
+// Per cell the 27 taps are summed in the reference's order (dx, dy, dz).
+// coef(tx, p, kv) yields the 8 coefficients of tap p for run tx.
+template <typename Coef>
+__device__ __forceinline__ void apply_pair(const float (*S)[HY][HZP], int ty, int tz8, Coef coef, float acc[TX][8]) {
 #pragma unroll
-  for (int c = 0; c < 8; ++c) acc[c] = 0.f;
+  for (int tx = 0; tx < TX; ++tx)
 #pragma unroll
-  for (int dx = 0; dx < 3; ++dx)
+    for (int c = 0; c < 8; ++c) acc[tx][c] = 0.f;
+#pragma unroll
+  for (int pl = 0; pl < TX + 2; ++pl)
 #pragma unroll
     for (int dy = 0; dy < 3; ++dy) {
       float xr[12];
-      ld_row12(&S[tx + dx][ty + dy][tz8], xr);
+      ld_row12(&S[pl][ty + dy][tz8], xr);
 #pragma unroll
-      for (int dz = 0; dz < 3; ++dz) {
-        const float kv = ku[dx * 9 + dy * 3 + dz];
+      for (int tx = 0; tx < TX; ++tx) {
+        const int dx = pl - tx;
+        if (dx < 0 || dx > 2) continue;
 #pragma unroll
-        for (int c = 0; c < 8; ++c) acc[c] = fmaf(kv, xr[c + dz], acc[c]);
+        for (int dz = 0; dz < 3; ++dz) {
+          float kv[8];
+          coef(tx, dx * 9 + dy * 3 + dz, kv);
+#pragma unroll
+          for (int c = 0; c < 8; ++c) acc[tx][c] = fmaf(kv[c], xr[c + dz], acc[tx][c]);
+        }
       }
     }
 }
 
-// acc[tx][c] for the thread's two runs (tx = 0, 1).  Dense: coefficient planes.
-// Classed: runs of one uniform material take the broadcast fast path; the
-// cells of the other runs are spread over the whole CTA (one cell per thread)
-// through a shared-memory worklist, so interface cells do not hold whole warps.
-// cw are the runs' class words (load_run_cls), tile_base the tile's first
-// record index.  All threads of the CTA must call this (it synchronises); S
-// (and, classed, sm->Ku and sm->nmixed = 0) must be visible to all threads.
+// acc[tx][c] for the thread's two runs (tx = 0, 1).
+// Dense: coefficient planes streamed from HBM.  Classed: a material run takes
+// the material's uniform vector from shared memory, a mixed run streams its
+// record like a dense run; warps with no mixed run skip the record path.
+// rwd are the runs' words (load_run_words), trec the tile's first record and
+// mixed-run count (load_tile_runs).
 template <typename KT, bool CLS>
-__device__ __forceinline__ void tile_apply(const float (*S)[HY][HZP], ClsSmem *sm, const CoefArgs<KT> &C,
-                                           const uint2 cw[TX], uint32_t tile_base, int n1, int n2, int n3,
+__device__ __forceinline__ void tile_apply(const float (*S)[HY][HZP], const ClsSmem *sm, const CoefArgs<KT> &C,
+                                           const uint32_t rwd[TX], uint2 trec, int n1, int n2, int n3,
                                            float acc[TX][8]) {
   const int tz = run_tz(threadIdx.x), ty = run_ty(threadIdx.x);
   const int x0 = blockIdx.z * TX, k0 = blockIdx.x * TZ + tz * 8, j = blockIdx.y * TY + ty;
   const bool active = k0 < n3 && j < n2;
-  if (!CLS) {
+  bool valid[TX];
 #pragma unroll
-    for (int tx = 0; tx < TX; ++tx) {
-      const int i = x0 + tx;
-      if (!active || i >= n1) continue;
-      apply_run<KT>(S, tx, ty, tz * 8, C.K, C.ps, ((int64_t)i * n2 + j) * n3 + k0, acc[tx]);
-    }
+  for (int tx = 0; tx < TX; ++tx) valid[tx] = active && x0 + tx < n1;
+  if (!CLS) {
+    int64_t q[TX];
+#pragma unroll
+    for (int tx = 0; tx < TX; ++tx) q[tx] = valid[tx] ? ((int64_t)(x0 + tx) * n2 + j) * n3 + k0 : 0;
+    apply_pair(S, ty, tz * 8, [&](int tx, int p, float kv[8]) {
+      if (valid[tx]) ld8cs(C.K + p * C.ps + q[tx], kv);
+      else {
+#pragma unroll
+        for (int c = 0; c < 8; ++c) kv[c] = 0.f;
+      }
+    }, acc);
     return;
   }
-  int tot;
-  uint32_t rank = tile_base + (uint32_t)cta_excl_scan(count_general(cw), tot);
   bool mixed[TX];
 #pragma unroll
-  for (int tx = 0; tx < TX; ++tx) {
-    mixed[tx] = false;
-    const int i = x0 + tx;
-    if (!active || i >= n1) continue;
-    const int c0 = class_of(cw[tx], 0);
-    const bool uni = c0 != CLS_GENERAL && cw[tx].x == cw[tx].y && cw[tx].x == c0 * 0x01010101u;
-    if (uni) {
-      apply_run_uniform(S, sm->Ku[c0], tx, ty, tz * 8, acc[tx]);
-    } else {
-      mixed[tx] = true;
-      const int slot = atomicAdd(&sm->nmixed, 1);
-      sm->run_cw[slot] = cw[tx];
-      sm->run_rank[slot] = rank;
-      sm->run_id[slot] = (uint16_t)(threadIdx.x * TX + tx);
-      rank += __popc(general_mask(cw[tx]));
+  for (int tx = 0; tx < TX; ++tx) mixed[tx] = (rwd[tx] & 3u) == kMixed;
+  if (!__any_sync(0xffffffffu, mixed[0] || mixed[1])) {
+    const float *ku[TX];
+#pragma unroll
+    for (int tx = 0; tx < TX; ++tx) ku[tx] = sm->Ku[rwd[tx] & 3u];
+    apply_pair(S, ty, tz * 8, [&](int tx, int p, float kv[8]) {
+      const float v = ku[tx][p];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) kv[c] = v;
+    }, acc);
+  } else {
+    // every lane streams a record: its run's, or its material's (cached), so
+    // the loads carry no branch and issue ahead of the arithmetic
+    const KT *rp[TX];
+    uint32_t st[TX];
+#pragma unroll
+    for (int tx = 0; tx < TX; ++tx) {
+      rp[tx] = mixed[tx] ? C.rec + (size_t)trec.x * RREC + (rwd[tx] >> 2) * 8 : C.mrec + (rwd[tx] & 3u) * RREC;
+      st[tx] = mixed[tx] ? trec.y * 8 : 8;
     }
+    apply_pair(S, ty, tz * 8, [&](int tx, int p, float kv[8]) { ld8(rp[tx] + p * st[tx], kv); }, acc);
   }
-  __syncthreads();
-  const int nm = sm->nmixed;
-  for (int e = threadIdx.x; e < nm * 8; e += PT) {
-    const int sl = e >> 3, c = e & 7;
-    const int id = sm->run_id[sl];
-    const int t = id / TX, tx = id % TX, tzz = run_tz(t), tyy = run_ty(t);
-    const uint2 w = sm->run_cw[sl];
-    const int cl = class_of(w, c);
-    float k[KREC];
-    if (cl == CLS_GENERAL) {
-      const uint32_t r = sm->run_rank[sl] + __popc(general_mask(w) & ((1u << c) - 1u));
-      ld_record(C.rec + (size_t)r * KREC, k);
-    } else {
-#pragma unroll
-      for (int p = 0; p < 27; ++p) k[p] = sm->Ku[cl][p];
-    }
-    float a = 0.f;
-#pragma unroll
-    for (int dx = 0; dx < 3; ++dx)
-#pragma unroll
-      for (int dy = 0; dy < 3; ++dy)
-#pragma unroll
-        for (int dz = 0; dz < 3; ++dz)
-          a = fmaf(k[dx * 9 + dy * 3 + dz], S[tx + dx][tyy + dy][tzz * 8 + c + dz], a);
-    sm->Y[tx][tyy][tzz * 8 + c] = a;
-  }
-  __syncthreads();
-#pragma unroll
-  for (int tx = 0; tx < TX; ++tx)
-    if (mixed[tx]) {
-      const float4 lo = *reinterpret_cast<const float4 *>(&sm->Y[tx][ty][tz * 8]);
-      const float4 hi = *reinterpret_cast<const float4 *>(&sm->Y[tx][ty][tz * 8 + 4]);
-      acc[tx][0] = lo.x; acc[tx][1] = lo.y; acc[tx][2] = lo.z; acc[tx][3] = lo.w;
-      acc[tx][4] = hi.x; acc[tx][5] = hi.y; acc[tx][6] = hi.z; acc[tx][7] = hi.w;
-    }
 }
 
 // uniform coefficient vectors of a classed block into shared memory
@@ -623,15 +654,14 @@ template <bool CLS>
 __device__ __forceinline__ void stage_uniform(ClsSmem *sm, const float *__restrict__ kuni) {
   if (!CLS) return;
   for (int e = threadIdx.x; e < 3 * KREC; e += PT) sm->Ku[e / KREC][e % KREC] = __ldg(kuni + e);
-  if (threadIdx.x == 0) sm->nmixed = 0;
 }
 
-// the class words of the thread's runs and the tile's first record index (classed only)
+// the run words of the thread's runs and the tile's (first record, mixed runs) (classed only)
 template <typename KT, bool CLS>
-__device__ __forceinline__ uint32_t load_tile_cls(const CoefArgs<KT> &C, int n1, int n2, int n3, uint2 cw[TX]) {
-  if (!CLS) return 0u;
-  load_run_cls(C.cls, n1, n2, n3, cw);
-  return __ldg(C.tbase + tile_id());
+__device__ __forceinline__ uint2 load_tile_runs(const CoefArgs<KT> &C, int n1, int n2, int n3, uint32_t rwd[TX]) {
+  if (!CLS) return make_uint2(0u, 0u);
+  load_run_words(C.rw, n1, n2, n3, rwd);
+  return make_uint2(__ldg(C.rbase + tile_id()), __ldg(C.rcount + tile_id()));
 }
 
 // mask bytes of the thread's runs (all ones without a mask)
@@ -663,8 +693,9 @@ k_pre_fused(const CoefArgs<KT> C, const XT *__restrict__ x,
   ClsSmem *smc = CLS ? reinterpret_cast<ClsSmem *>(&smc_raw) : nullptr;
   const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY, x0 = blockIdx.z * TX;
   const float sc = xscale ? __ldg(xscale) : 1.f;
-  uint2 cw[TX], mw[TX];
-  const uint32_t tb = load_tile_cls<KT, CLS>(C, n1, n2, n3, cw);
+  uint32_t rwd[TX];
+  uint2 mw[TX];
+  const uint2 tb = load_tile_runs<KT, CLS>(C, n1, n2, n3, rwd);
   load_run_mask(mask, n1, n2, n3, mw);
   FineStage fs;
   stage_load(fs, n1, n2, n3,
@@ -677,7 +708,7 @@ k_pre_fused(const CoefArgs<KT> C, const XT *__restrict__ x,
   stage_uniform<CLS>(smc, C.kuni);
   __syncthreads();
   float acc[TX][8];
-  tile_apply<KT, CLS>(S, smc, C, cw, tb, n1, n2, n3, acc);
+  tile_apply<KT, CLS>(S, smc, C, rwd, tb, n1, n2, n3, acc);
   const int tz = run_tz(threadIdx.x), ty = run_ty(threadIdx.x);
   const int k0 = z0 + tz * 8, j = y0 + ty;
   const bool active = k0 < n3 && j < n2;  // n3 % 8 == 0: a run is all in or all out
@@ -724,7 +755,7 @@ __device__ __forceinline__ Lin1 lin1(int f, int n) {
 
 // trilinear prolongation at fine z index k from the staged coarse tile, the
 // x / y weights (a, b) already relative to the tile
-__device__ __forceinline__ float up_at(const float (*Cs)[CY][CZ], const Lin1 &a, const Lin1 &b, int k, int m3,
+__device__ __forceinline__ float up_at(const float (*Cs)[CY][CZP], const Lin1 &a, const Lin1 &b, int k, int m3,
                                        int cz0) {
   const Lin1 c = lin1(k, m3);
   const int e0 = c.i0 - cz0, e1 = c.i1 - cz0;
@@ -743,26 +774,11 @@ __device__ __forceinline__ Lin1 lin1_rel(int f, int n, int base) {
 constexpr int CNV = (TZ / 2) / 4;                 // coarse interior vectors per row
 constexpr int kCoarseVec = (CX * CY * CNV + PT - 1) / PT;
 
-template <typename KT, typename CT, typename YT, typename OT, bool SWAP, bool CLS>
-__global__ void __launch_bounds__(PT)
-k_post_fused(const CoefArgs<KT> C, const CT *__restrict__ xc, const YT *__restrict__ yl,
-             const float *__restrict__ c0p, const float *__restrict__ c1p, OT *__restrict__ out,
-             const uint8_t *__restrict__ bmask, const uint8_t *__restrict__ omask, int n1, int n2, int n3) {
-  __shared__ __align__(16) float S[HX][HY][HZP];
-  __shared__ float Cs[CX][CY][CZ];
-  __shared__ typename std::conditional<CLS, ClsSmem, int>::type smc_raw;
-  ClsSmem *smc = CLS ? reinterpret_cast<ClsSmem *>(&smc_raw) : nullptr;
-  stage_uniform<CLS>(smc, C.kuni);
-  const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY, x0 = blockIdx.z * TX;
-  const int m1 = n1 / 2, m2 = n2 / 2, m3 = n3 / 2;
-  const int cx0 = x0 / 2 - 1, cy0 = y0 / 2 - 1, cz0 = z0 / 2 - 1;
-  const float c0 = __ldg(c0p), c1 = __ldg(c1p);
-  uint2 cw[TX], bw[TX], ow[TX];
-  const uint32_t tb = load_tile_cls<KT, CLS>(C, n1, n2, n3, cw);
-  load_run_mask(bmask, n1, n2, n3, bw);
-  load_run_mask(omask, n1, n2, n3, ow);
-  // every global load of the staging in flight together: the coarse tile
-  // (vectors + z-halo) and, with swap, the fine y_l tile
+// Stages the coarse tile of the CTA's fine tile (x_{l+1} with a one-cell
+// halo; 0 outside the grid): every global load first, then the stores.
+template <typename CT>
+__device__ __forceinline__ void stage_coarse(float (*Cs)[CY][CZP], const CT *__restrict__ xc, int m1, int m2, int m3) {
+  const int cx0 = blockIdx.z * TX / 2 - 1, cy0 = blockIdx.y * TY / 2 - 1, cz0 = blockIdx.x * TZ / 2 - 1;
   float4 cv[kCoarseVec];
   float ch = 0.f;
 #pragma unroll
@@ -779,12 +795,6 @@ k_post_fused(const CoefArgs<KT> C, const CT *__restrict__ xc, const YT *__restri
     if (e < 2 * CX * CY && (unsigned)i < (unsigned)m1 && (unsigned)j < (unsigned)m2 && (unsigned)k < (unsigned)m3)
       ch = ldf(xc + ((int64_t)i * m2 + j) * m3 + k);
   }
-  if (SWAP) {  // y_l goes straight into the fine tile; the combine below reads it back in place
-    FineStage fs;
-    stage_load(fs, n1, n2, n3, [&](int, int, int, int64_t q) { return ldv4(yl + q); },
-               [&](int, int, int, int64_t q) { return ldf(yl + q); });
-    stage_put(S, fs);
-  }
 #pragma unroll
   for (int m = 0; m < kCoarseVec; ++m) {
     const int e = threadIdx.x + m * PT, r = e / CNV, v = e % CNV;
@@ -796,9 +806,122 @@ k_post_fused(const CoefArgs<KT> C, const CT *__restrict__ xc, const YT *__restri
     const int r = threadIdx.x >> 1;
     Cs[r / CY][r % CY][(threadIdx.x & 1) ? CZ - 1 : 0] = ch;
   }
+}
+
+// The prolongation of a large level as its own bandwidth-bound pass: u =
+// up(x_{l+1}) (with swap: c0 y_l + c1 up(x_{l+1})), one value per fine
+// cell in the activation dtype, for the post-block kernel to stage like any
+// input (its tile then needs no interpolation of the halo).  Same tile grid
+// and run ownership as the block kernels.
+template <typename CT, typename YT, typename UT, bool SWAP>
+__global__ void __launch_bounds__(PT)
+k_up_fine(const CT *__restrict__ xc, const YT *__restrict__ yl, const float *__restrict__ c0p,
+          const float *__restrict__ c1p, UT *__restrict__ u, int n1, int n2, int n3) {
+  __shared__ __align__(16) float Cs[CX][CY][CZP];
+  const int m1 = n1 / 2, m2 = n2 / 2, m3 = n3 / 2;
+  const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY, x0 = blockIdx.z * TX;
+  const int cx0 = x0 / 2 - 1, cy0 = y0 / 2 - 1, cz0 = z0 / 2 - 1;
+  const int tz = run_tz(threadIdx.x), ty = run_ty(threadIdx.x);
+  const int k0 = z0 + tz * 8, j = y0 + ty;
+  const bool active = k0 < n3 && j < n2;
+  float yv[TX][8];
+  if (SWAP) {
+#pragma unroll
+    for (int tx = 0; tx < TX; ++tx)
+      if (active && x0 + tx < n1) ld8(yl + ((int64_t)(x0 + tx) * n2 + j) * n3 + k0, yv[tx]);
+  }
+  stage_coarse(Cs, xc, m1, m2, m3);
   __syncthreads();
-  // the fine tile: up(x_{l+1}) (with swap: c0 y_l + c1 up(x_{l+1})); 0 outside the grid
-  {
+  if (!active) return;
+  const float c0 = SWAP ? __ldg(c0p) : 0.f, c1 = SWAP ? __ldg(c1p) : 0.f;
+  const Lin1 b = lin1_rel(j, m2, cy0);
+  // The run's fine cells k0 .. k0 + 7 interpolate along z between the coarse
+  // cells k0/2 - 1 .. k0/2 + 4 (tile z index 4 tz ..), with the weights of
+  // lin1: (1/4, 3/4) for even k, (3/4, 1/4) for odd k; only the first cell
+  // of the grid (clamped source) and the last (clamped upper neighbour)
+  // differ, and take lin1's values.
+  const Lin1 zf = lin1(k0, m3), zl = lin1(k0 + 7, m3);
+  const bool first_lo = zf.i0 - (k0 / 2 - 1) == 1;  // k0 == 0: both taps one cell up
+  const bool last_hi = zl.i1 == zl.i0;             // last cell of the grid: upper tap clamped
+#pragma unroll
+  for (int tx = 0; tx < TX; ++tx) {
+    const int i = x0 + tx;
+    if (i >= n1) continue;
+    const Lin1 a = lin1_rel(i, m1, cx0);
+    float R[2][2][6];
+#pragma unroll
+    for (int ia = 0; ia < 2; ++ia)
+#pragma unroll
+      for (int ib = 0; ib < 2; ++ib) {
+        const float *row = &Cs[ia ? a.i1 : a.i0][ib ? b.i1 : b.i0][4 * tz];
+        const float4 lo = *reinterpret_cast<const float4 *>(row);
+        const float2 hi = *reinterpret_cast<const float2 *>(row + 4);
+        R[ia][ib][0] = lo.x; R[ia][ib][1] = lo.y; R[ia][ib][2] = lo.z; R[ia][ib][3] = lo.w;
+        R[ia][ib][4] = hi.x; R[ia][ib][5] = hi.y;
+      }
+    float o[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      float l0 = (c & 1) ? 0.75f : 0.25f, l1 = (c & 1) ? 0.25f : 0.75f;
+      if (c == 0) { l0 = zf.l0; l1 = zf.l1; }
+      if (c == 7) { l0 = zl.l0; l1 = zl.l1; }
+      const int r0 = (c & 1) ? c / 2 + 1 : c / 2, r1 = r0 + 1;
+      float v[2][2][2];
+#pragma unroll
+      for (int ia = 0; ia < 2; ++ia)
+#pragma unroll
+        for (int ib = 0; ib < 2; ++ib) {
+          float x0v = R[ia][ib][r0], x1v = R[ia][ib][r1];
+          if (c == 0 && first_lo) { x0v = R[ia][ib][1]; x1v = R[ia][ib][2]; }
+          if (c == 7 && last_hi) x1v = R[ia][ib][4];
+          v[ia][ib][0] = x0v;
+          v[ia][ib][1] = x1v;
+        }
+      o[c] = a.l0 * (b.l0 * (l0 * v[0][0][0] + l1 * v[0][0][1]) + b.l1 * (l0 * v[0][1][0] + l1 * v[0][1][1])) +
+             a.l1 * (b.l0 * (l0 * v[1][0][0] + l1 * v[1][0][1]) + b.l1 * (l0 * v[1][1][0] + l1 * v[1][1][1]));
+      if (SWAP) o[c] = __fadd_rn(__fmul_rn(c0, yv[tx][c]), __fmul_rn(c1, o[c]));
+    }
+    st8(u + ((int64_t)i * n2 + j) * n3 + k0, o);
+  }
+}
+
+// UPIN: xc is the level's prolongated input u of k_up_fine (already combined
+// with y_l under swap), staged like a pre-block input.
+template <typename KT, typename CT, typename YT, typename OT, bool SWAP, bool CLS, bool UPIN>
+__global__ void __launch_bounds__(PT)
+k_post_fused(const CoefArgs<KT> C, const CT *__restrict__ xc, const YT *__restrict__ yl,
+             const float *__restrict__ c0p, const float *__restrict__ c1p, OT *__restrict__ out,
+             const uint8_t *__restrict__ bmask, const uint8_t *__restrict__ omask, int n1, int n2, int n3) {
+  __shared__ __align__(16) float S[HX][HY][HZP];
+  __shared__ __align__(16) typename std::conditional<UPIN, int, float[CX][CY][CZP]>::type cs_raw;
+  __shared__ typename std::conditional<CLS, ClsSmem, int>::type smc_raw;
+  float(*Cs)[CY][CZP] = reinterpret_cast<float(*)[CY][CZP]>(&cs_raw);
+  ClsSmem *smc = CLS ? reinterpret_cast<ClsSmem *>(&smc_raw) : nullptr;
+  stage_uniform<CLS>(smc, C.kuni);
+  const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY, x0 = blockIdx.z * TX;
+  const int m1 = n1 / 2, m2 = n2 / 2, m3 = n3 / 2;
+  const int cx0 = x0 / 2 - 1, cy0 = y0 / 2 - 1, cz0 = z0 / 2 - 1;
+  const float c0 = __ldg(c0p), c1 = __ldg(c1p);
+  uint32_t rwd[TX];
+  uint2 bw[TX], ow[TX];
+  const uint2 tb = load_tile_runs<KT, CLS>(C, n1, n2, n3, rwd);
+  load_run_mask(bmask, n1, n2, n3, bw);
+  load_run_mask(omask, n1, n2, n3, ow);
+  if (UPIN) {
+    FineStage fs;
+    stage_load(fs, n1, n2, n3, [&](int, int, int, int64_t q) { return ldv4(xc + q); },
+               [&](int, int, int, int64_t q) { return ldf(xc + q); });
+    stage_put(S, fs);
+  } else {
+    if (SWAP) {  // y_l goes straight into the fine tile; the combine below reads it back in place
+      FineStage fs;
+      stage_load(fs, n1, n2, n3, [&](int, int, int, int64_t q) { return ldv4(yl + q); },
+                 [&](int, int, int, int64_t q) { return ldf(yl + q); });
+      stage_put(S, fs);
+    }
+    stage_coarse(Cs, xc, m1, m2, m3);
+    __syncthreads();
+    // the fine tile: up(x_{l+1}) (with swap: c0 y_l + c1 up(x_{l+1})); 0 outside the grid
     const int v = threadIdx.x % NVR;
 #pragma unroll
     for (int m = 0; m < kStageVec; ++m) {
@@ -832,7 +955,7 @@ k_post_fused(const CoefArgs<KT> C, const CT *__restrict__ xc, const YT *__restri
   }
   __syncthreads();
   float accs[TX][8];
-  tile_apply<KT, CLS>(S, smc, C, cw, tb, n1, n2, n3, accs);
+  tile_apply<KT, CLS>(S, smc, C, rwd, tb, n1, n2, n3, accs);
   const int tz = run_tz(threadIdx.x), ty = run_ty(threadIdx.x);
   const int k0 = z0 + tz * 8, j = y0 + ty;
   if (k0 >= n3 || j >= n2) return;
@@ -910,12 +1033,17 @@ struct PrecondPlan {
   std::vector<Level> lv;      // L + 1 levels
   // device pointers (inside the caller's workspace)
   std::vector<float *> img;   // level images, [0] unused (caller's image)
-  std::vector<void *> Kpre, Kpost;   // dense planes, or general-cell records on classed levels
+  float *Uall = nullptr;      // uniform vectors of all blocks
+  void *Mrec = nullptr;       // material records of all blocks (block order of Uall)
+  void *ufine = nullptr;      // level-0 prolongated post-block input
+  uint32_t *glist = nullptr;  // general-cell list (setup scratch)
+  std::vector<void *> Kpre, Kpost;   // dense planes, or mixed-run records on classed levels
   void *Kl = nullptr;
   std::vector<float *> Upre, Upost;  // classed levels: 3 x KREC uniform vectors per block
   float *Ul = nullptr;
-  std::vector<uint8_t *> cls;        // classed levels: class byte per cell
-  std::vector<uint32_t *> tcount, tbase;
+  std::vector<uint8_t *> cls;        // classed levels: class byte per cell (setup)
+  std::vector<uint32_t *> rw;        // classed levels: word per 8-cell run
+  std::vector<uint32_t *> rcount, rbase, gcount, gbase;  // per tile: mixed runs, general cells
   std::vector<void *> y, xin, xout;  // y_l (pre out), x_l inputs (l >= 1), post outputs (l >= 1)
   float *coef = nullptr;      // c0[0..L-1], c1[0..L-1]
   uint8_t *fmask = nullptr;   // fluid mask of level 0
@@ -926,6 +1054,26 @@ struct PrecondPlan {
 };
 
 static size_t al256(size_t b) { return (b + 255) / 256 * 256; }
+
+// multiprocessors of the current device (grid sizing of persistent kernels)
+static int sm_count() {
+  int dev = 0, v = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0)
+    return 152;
+  return v;
+}
+
+// CTAs of PT threads of kernel f resident per SM (at least 1)
+template <typename F>
+static int resident_ctas(F f) {
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, f, PT, 0) != cudaSuccess || nb < 1) return 1;
+  return nb;
+}
+template <typename KT>
+static KT *kgen_rec_type(void (*)(const float *, int, int, int, const float *, int, int, const uint32_t *,
+                                  const uint32_t *, const uint32_t *, const uint32_t *, const uint32_t *,
+                                  const uint32_t *, KT *, KT *));
 
 static size_t plan_layout(PrecondPlan &P, char *base) {
   size_t off = 0;
@@ -942,10 +1090,10 @@ static size_t plan_layout(PrecondPlan &P, char *base) {
   P.xin.assign(P.L + 1, nullptr);
   P.xout.assign(P.L + 1, nullptr);
   for (int l = 1; l <= P.L; ++l) P.img[l] = (float *)take(3 * P.lv[l].n * sizeof(float));
-  // coefficient storage of one block: dense planes, or (worst case: every cell general) records
+  // coefficient storage of one block: dense planes, or (worst case: every run mixed) run records
   auto kbytes = [&](int l) {
     const auto &v = P.lv[l];
-    return v.cls ? (size_t)v.n * KREC * sk : (size_t)27 * v.ps * sk;
+    return v.cls ? (size_t)(v.n / 8) * RREC * sk : (size_t)27 * v.ps * sk;
   };
   for (int l = 0; l < P.L; ++l) {
     P.Kpre[l] = take(kbytes(l));
@@ -955,26 +1103,41 @@ static size_t plan_layout(PrecondPlan &P, char *base) {
   P.Upre.assign(P.L, nullptr);
   P.Upost.assign(P.L, nullptr);
   P.cls.assign(P.L + 1, nullptr);
-  P.tcount.assign(P.L + 1, nullptr);
-  P.tbase.assign(P.L + 1, nullptr);
+  P.rw.assign(P.L + 1, nullptr);
+  P.rcount.assign(P.L + 1, nullptr);
+  P.rbase.assign(P.L + 1, nullptr);
+  P.gcount.assign(P.L + 1, nullptr);
+  P.gbase.assign(P.L + 1, nullptr);
+  // uniform vectors of all 2L + 1 blocks (block b at U + 3 KREC b, the parameter block order)
+  float *U = (float *)take((size_t)(2 * P.L + 1) * 3 * KREC * sizeof(float));
+  for (int l = 0; l < P.L; ++l) {
+    P.Upre[l] = U + (size_t)l * 3 * KREC;
+    P.Upost[l] = U + (size_t)(P.L + l) * 3 * KREC;
+  }
+  P.Ul = U + (size_t)2 * P.L * 3 * KREC;
+  P.Uall = U;
+  P.Mrec = take((size_t)(2 * P.L + 1) * 3 * RREC * sk);
+  int64_t nlist = 0;
   for (int l = 0; l <= P.L; ++l) {
     const auto &v = P.lv[l];
     if (!v.cls) continue;
     P.cls[l] = (uint8_t *)take(v.ps);
-    P.tcount[l] = (uint32_t *)take(v.ntiles * sizeof(uint32_t));
-    P.tbase[l] = (uint32_t *)take(v.ntiles * sizeof(uint32_t));
-    if (l < P.L) {
-      P.Upre[l] = (float *)take(3 * KREC * sizeof(float));
-      P.Upost[l] = (float *)take(3 * KREC * sizeof(float));
-    } else {
-      P.Ul = (float *)take(3 * KREC * sizeof(float));
-    }
+    P.rw[l] = (uint32_t *)take((v.n / 8) * sizeof(uint32_t));
+    P.rcount[l] = (uint32_t *)take(v.ntiles * sizeof(uint32_t));
+    P.rbase[l] = (uint32_t *)take(v.ntiles * sizeof(uint32_t));
+    P.gcount[l] = (uint32_t *)take(v.ntiles * sizeof(uint32_t));
+    P.gbase[l] = (uint32_t *)take(v.ntiles * sizeof(uint32_t));
+    nlist = std::max<int64_t>(nlist, v.n);
   }
+  // general-cell list of one level at a time (setup only)
+  P.glist = nlist ? (uint32_t *)take((size_t)nlist * sizeof(uint32_t)) : nullptr;
   for (int l = 0; l < P.L; ++l) P.y[l] = take(P.lv[l].ps * sa);
   for (int l = 1; l <= P.L; ++l) {
     P.xin[l] = take(P.lv[l].ps * sa);
     P.xout[l] = take(P.lv[l].ps * sa);
   }
+  // the finest level's prolongated input (fast path only)
+  P.ufine = P.lv[0].fast ? take(P.lv[0].ps * sa) : nullptr;
   P.coef = (float *)take(2 * P.L * sizeof(float));
   P.fmask = (uint8_t *)take(P.lv[0].ps + 64);
   P.lin_ws = take(linear_workspace());
@@ -1000,12 +1163,15 @@ static dim3 grid_of(const PrecondPlan::Level &v) {
 template <typename KT>
 static CoefArgs<KT> coef_args(const PrecondPlan &P, int l, void *K, float *uni) {
   CoefArgs<KT> C;
+  // the block's material records sit at the same block offset as its uniform vectors
+  C.mrec = uni ? (const KT *)P.Mrec + (size_t)((uni - P.Uall) / (3 * KREC)) * 3 * RREC : nullptr;
   C.K = (const KT *)K;
   C.ps = P.lv[l].ps;
   C.rec = (const KT *)K;
   C.kuni = uni;
-  C.cls = P.cls[l];
-  C.tbase = P.tbase[l];
+  C.rw = P.rw[l];
+  C.rbase = P.rbase[l];
+  C.rcount = P.rcount[l];
   return C;
 }
 
@@ -1082,21 +1248,27 @@ static int run_apply(const PrecondPlan &P, const float *r, const float *rscale, 
       const AT *xc = (const AT *)P.xout[l + 1], *yl = (const AT *)P.y[l];
       const dim3 g = grid_of(v);
       if (l == 0) {
+        // the finest level: prolongation as its own pass, then the block on u
+        AT *u = (AT *)P.ufine;
         if (P.swap) {
-          if (v.cls) k_post_fused<KT, AT, AT, float, true, true><<<g, PT, 0, st>>>(C, xc, yl, c0, c1, z, bm, om, v.n1, v.n2, v.n3);
-          else k_post_fused<KT, AT, AT, float, true, false><<<g, PT, 0, st>>>(C, xc, yl, c0, c1, z, bm, om, v.n1, v.n2, v.n3);
+          k_up_fine<AT, AT, AT, true><<<g, PT, 0, st>>>(xc, yl, c0, c1, u, v.n1, v.n2, v.n3);
+          MLPCG_LAUNCH_CHECK();
+          if (v.cls) k_post_fused<KT, AT, AT, float, true, true, true><<<g, PT, 0, st>>>(C, u, yl, c0, c1, z, bm, om, v.n1, v.n2, v.n3);
+          else k_post_fused<KT, AT, AT, float, true, false, true><<<g, PT, 0, st>>>(C, u, yl, c0, c1, z, bm, om, v.n1, v.n2, v.n3);
         } else {
-          if (v.cls) k_post_fused<KT, AT, AT, float, false, true><<<g, PT, 0, st>>>(C, xc, yl, c0, c1, z, bm, om, v.n1, v.n2, v.n3);
-          else k_post_fused<KT, AT, AT, float, false, false><<<g, PT, 0, st>>>(C, xc, yl, c0, c1, z, bm, om, v.n1, v.n2, v.n3);
+          k_up_fine<AT, AT, AT, false><<<g, PT, 0, st>>>(xc, yl, c0, c1, u, v.n1, v.n2, v.n3);
+          MLPCG_LAUNCH_CHECK();
+          if (v.cls) k_post_fused<KT, AT, AT, float, false, true, true><<<g, PT, 0, st>>>(C, u, yl, c0, c1, z, bm, om, v.n1, v.n2, v.n3);
+          else k_post_fused<KT, AT, AT, float, false, false, true><<<g, PT, 0, st>>>(C, u, yl, c0, c1, z, bm, om, v.n1, v.n2, v.n3);
         }
       } else {
         AT *o = (AT *)P.xout[l];
         if (P.swap) {
-          if (v.cls) k_post_fused<KT, AT, AT, AT, true, true><<<g, PT, 0, st>>>(C, xc, yl, c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3);
-          else k_post_fused<KT, AT, AT, AT, true, false><<<g, PT, 0, st>>>(C, xc, yl, c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3);
+          if (v.cls) k_post_fused<KT, AT, AT, AT, true, true, false><<<g, PT, 0, st>>>(C, xc, yl, c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3);
+          else k_post_fused<KT, AT, AT, AT, true, false, false><<<g, PT, 0, st>>>(C, xc, yl, c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3);
         } else {
-          if (v.cls) k_post_fused<KT, AT, AT, AT, false, true><<<g, PT, 0, st>>>(C, xc, yl, c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3);
-          else k_post_fused<KT, AT, AT, AT, false, false><<<g, PT, 0, st>>>(C, xc, yl, c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3);
+          if (v.cls) k_post_fused<KT, AT, AT, AT, false, true, false><<<g, PT, 0, st>>>(C, xc, yl, c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3);
+          else k_post_fused<KT, AT, AT, AT, false, false, false><<<g, PT, 0, st>>>(C, xc, yl, c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3);
         }
       }
       MLPCG_LAUNCH_CHECK();
@@ -1152,11 +1324,14 @@ int mlpcg_precond_create(int N1, int N2, int N3, int levels, int k_dtype, int ac
                 "grid %d x %d x %d must be divisible by 2^levels = %d", N1, N2, N3, f);
   MLPCG_REQUIRE((k_dtype == MLPCG_F32 || k_dtype == MLPCG_BF16) && (act_dtype == MLPCG_F32 || act_dtype == MLPCG_BF16),
                 MLPCG_ERR_UNSUPPORTED, "coefficient / activation storage must be F32 or BF16");
+  MLPCG_REQUIRE(coeff_layout == MLPCG_COEFF_DENSE || coeff_layout == MLPCG_COEFF_CLASSED, MLPCG_ERR_ARG,
+                "coeff_layout must be MLPCG_COEFF_DENSE or MLPCG_COEFF_CLASSED");
+  // classed levels index cells and records with 32-bit integers
+  MLPCG_REQUIRE(coeff_layout == MLPCG_COEFF_DENSE || cells(N1, N2, N3) < ((int64_t)1 << 32), MLPCG_ERR_SHAPE,
+                "the classed layout needs fewer than 2^32 cells (grid %d x %d x %d)", N1, N2, N3);
   auto *h = new mlpcg_precond();
   PrecondPlan &P = h->p;
   P.n1 = N1; P.n2 = N2; P.n3 = N3; P.L = levels;
-  MLPCG_REQUIRE(coeff_layout == MLPCG_COEFF_DENSE || coeff_layout == MLPCG_COEFF_CLASSED, MLPCG_ERR_ARG,
-                "coeff_layout must be MLPCG_COEFF_DENSE or MLPCG_COEFF_CLASSED");
   P.kdt = k_dtype; P.adt = act_dtype; P.swap = swap_sm_order ? 1 : 0; P.mask = mask ? 1 : 0;
   P.layout = coeff_layout;
   for (int l = 0; l <= levels; ++l) {
@@ -1205,36 +1380,58 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
   k_fluid_mask<<<blocks_for(P.lv[0].n, 256), 256, 0, st>>>(image, P.fmask, P.lv[0].n);
   MLPCG_LAUNCH_CHECK();
   // coefficients: dense planes, or class map + uniform vectors + general-cell records
-  auto gen = [&](int l, const float *im, int blk, void *K, float *U) -> int {
-    const auto &v = P.lv[l];
-    if (!v.cls) return launch_stencil_gen(im, 0, v.n1, v.n2, v.n3, blk_w(blk), blk_b(blk), K, P.kdt, v.ps, st);
+  bool any_cls = false;
+  for (int l = 0; l <= L; ++l) any_cls = any_cls || P.lv[l].cls;
+  if (any_cls) {
     if (P.kdt == MLPCG_BF16) {
-      k_kgen_uniform<__nv_bfloat16><<<1, 32, 0, st>>>(blk_w(blk), blk_b(blk), U);
-      k_kgen_cls<__nv_bfloat16><<<grid_of(v), PT, 0, st>>>(im, v.n1, v.n2, v.n3, blk_w(blk), blk_b(blk), P.cls[l],
-                                                           P.tbase[l], (__nv_bfloat16 *)K);
+      k_kgen_uniform_all<__nv_bfloat16><<<2 * L + 1, 3 * KREC, 0, st>>>(params, P.Uall);
+      k_material_records<__nv_bfloat16><<<2 * L + 1, 256, 0, st>>>(P.Uall, (__nv_bfloat16 *)P.Mrec);
     } else {
-      k_kgen_uniform<float><<<1, 32, 0, st>>>(blk_w(blk), blk_b(blk), U);
-      k_kgen_cls<float><<<grid_of(v), PT, 0, st>>>(im, v.n1, v.n2, v.n3, blk_w(blk), blk_b(blk), P.cls[l], P.tbase[l],
-                                                   (float *)K);
+      k_kgen_uniform_all<float><<<2 * L + 1, 3 * KREC, 0, st>>>(params, P.Uall);
+      k_material_records<float><<<2 * L + 1, 256, 0, st>>>(P.Uall, (float *)P.Mrec);
+    }
+    MLPCG_LAUNCH_CHECK();
+  }
+  // one level's blocks b0 (and b1 >= 0): dense planes, or class map + general-cell records
+  auto gen_level = [&](int l, const float *im, int b0, void *K0, int b1, void *K1) -> int {
+    const auto &v = P.lv[l];
+    if (!v.cls) {
+      RET_IF(launch_stencil_gen(im, 0, v.n1, v.n2, v.n3, blk_w(b0), blk_b(b0), K0, P.kdt, v.ps, st));
+      if (b1 >= 0) RET_IF(launch_stencil_gen(im, 0, v.n1, v.n2, v.n3, blk_w(b1), blk_b(b1), K1, P.kdt, v.ps, st));
+      return MLPCG_OK;
+    }
+    k_classify<<<grid_of(v), PT, 0, st>>>(im, v.n1, v.n2, v.n3, P.cls[l], P.rw[l], P.rcount[l], P.gcount[l]);
+    MLPCG_LAUNCH_CHECK();
+    k_scan_tiles<<<1, 1024, 0, st>>>(P.rcount[l], P.rbase[l], (int)v.ntiles);
+    MLPCG_LAUNCH_CHECK();
+    k_scan_tiles<<<1, 1024, 0, st>>>(P.gcount[l], P.gbase[l], (int)v.ntiles);
+    MLPCG_LAUNCH_CHECK();
+    k_list_general<<<grid_of(v), PT, 0, st>>>(P.cls[l], v.n1, v.n2, v.n3, P.gbase[l], P.glist);
+    MLPCG_LAUNCH_CHECK();
+    // general cells: one wave of CTAs (as many as fit on every SM), each looping over its share
+    const uint32_t *lb = P.gbase[l] + v.ntiles - 1, *lc = P.gcount[l] + v.ntiles - 1;
+    const float *u0 = P.Uall + (size_t)b0 * 3 * KREC, *u1 = P.Uall + (size_t)(b1 >= 0 ? b1 : b0) * 3 * KREC;
+    const int fgrid = (int)std::min<int64_t>((int64_t)sm_count() * 8, (v.n + 255) / 256);
+    auto launch = [&](auto kern, auto fill, const void *r0, const void *r1) {
+      using KT = typename std::remove_pointer<decltype(kgen_rec_type(kern))>::type;
+      const int grid = (int)std::min<int64_t>((int64_t)sm_count() * resident_ctas(kern), (v.n + PT - 1) / PT);
+      kern<<<grid, PT, 0, st>>>(im, v.n1, v.n2, v.n3, params, b0, b1 >= 0 ? b1 : b0, P.glist, lb, lc, P.rw[l],
+                                P.rbase[l], P.rcount[l], (KT *)r0, (KT *)r1);
+      fill<<<fgrid, 256, 0, st>>>(P.cls[l], P.rw[l], P.rbase[l], P.rcount[l], v.n1, v.n2, v.n3, u0, u1, (KT *)r0,
+                                  (KT *)r1);
+    };
+    if (P.kdt == MLPCG_BF16) {
+      if (b1 >= 0) launch(k_kgen_list<__nv_bfloat16, 2>, k_fill_uniform<__nv_bfloat16, 2>, K0, K1);
+      else launch(k_kgen_list<__nv_bfloat16, 1>, k_fill_uniform<__nv_bfloat16, 1>, K0, nullptr);
+    } else {
+      if (b1 >= 0) launch(k_kgen_list<float, 2>, k_fill_uniform<float, 2>, K0, K1);
+      else launch(k_kgen_list<float, 1>, k_fill_uniform<float, 1>, K0, nullptr);
     }
     MLPCG_LAUNCH_CHECK();
     return MLPCG_OK;
   };
-  for (int l = 0; l <= L; ++l) {
-    const auto &v = P.lv[l];
-    if (!v.cls) continue;
-    const float *im = (l == 0) ? image : P.img[l];
-    k_classify<<<grid_of(v), PT, 0, st>>>(im, v.n1, v.n2, v.n3, P.cls[l], P.tcount[l]);
-    MLPCG_LAUNCH_CHECK();
-    k_scan_tiles<<<1, 1024, 0, st>>>(P.tcount[l], P.tbase[l], (int)v.ntiles);
-    MLPCG_LAUNCH_CHECK();
-  }
-  for (int l = 0; l < L; ++l) {
-    const float *im = (l == 0) ? image : P.img[l];
-    RET_IF(gen(l, im, l, P.Kpre[l], P.Upre[l]));
-    RET_IF(gen(l, im, L + l, P.Kpost[l], P.Upost[l]));
-  }
-  RET_IF(gen(L, P.img[L], 2 * L, P.Kl, P.Ul));
+  for (int l = 0; l < L; ++l) RET_IF(gen_level(l, (l == 0) ? image : P.img[l], l, P.Kpre[l], L + l, P.Kpost[l]));
+  RET_IF(gen_level(L, P.img[L], 2 * L, P.Kl, -1, nullptr));
   // c0 / c1 of every level (the linear blocks of sm_model_3d.py:236-239)
   for (int l = 0; l < L; ++l) {
     const auto &v = P.lv[l];
@@ -1280,19 +1477,26 @@ int mlpcg_precond_apply_stages(const mlpcg_precond *h, int first, int last, cons
   return run_apply<float, float>(P, r, r_scale, z, tmp0, st, first, last);
 }
 
-int mlpcg_precond_general_cells(const mlpcg_precond *h, int level, int64_t *count, void *stream) {
+int mlpcg_precond_class_counts(const mlpcg_precond *h, int level, int64_t *general_cells, int64_t *mixed_runs,
+                               void *stream) {
   clear_error();
-  MLPCG_REQUIRE(h && count && level >= 0 && level <= h->p.L, MLPCG_ERR_ARG, "precond_general_cells: bad argument");
+  MLPCG_REQUIRE(h && general_cells && mixed_runs && level >= 0 && level <= h->p.L, MLPCG_ERR_ARG,
+                "precond_class_counts: bad argument");
   const PrecondPlan &P = h->p;
-  MLPCG_REQUIRE(P.ready, MLPCG_ERR_ARG, "precond_general_cells: plan not set up");
+  MLPCG_REQUIRE(P.ready, MLPCG_ERR_ARG, "precond_class_counts: plan not set up");
   const auto &v = P.lv[level];
-  if (!v.cls) { *count = -1; return MLPCG_OK; }
-  uint32_t last[2] = {0, 0};
+  if (!v.cls) {
+    *general_cells = *mixed_runs = -1;
+    return MLPCG_OK;
+  }
+  uint32_t last[4] = {0, 0, 0, 0};
   cudaStream_t st = as_stream(stream);
-  MLPCG_CUDA_CHECK(cudaMemcpyAsync(&last[0], P.tbase[level] + v.ntiles - 1, 4, cudaMemcpyDeviceToHost, st));
-  MLPCG_CUDA_CHECK(cudaMemcpyAsync(&last[1], P.tcount[level] + v.ntiles - 1, 4, cudaMemcpyDeviceToHost, st));
+  const uint32_t *src[4] = {P.gbase[level], P.gcount[level], P.rbase[level], P.rcount[level]};
+  for (int t = 0; t < 4; ++t)
+    MLPCG_CUDA_CHECK(cudaMemcpyAsync(&last[t], src[t] + v.ntiles - 1, 4, cudaMemcpyDeviceToHost, st));
   MLPCG_CUDA_CHECK(cudaStreamSynchronize(st));
-  *count = (int64_t)last[0] + last[1];
+  *general_cells = (int64_t)last[0] + last[1];
+  *mixed_runs = (int64_t)last[2] + last[3];
   return MLPCG_OK;
 }
 

@@ -54,6 +54,7 @@ struct Vecs {
   FastDiv fd3, fd2;  // division by N3 and by N2
   uint32_t ngroups;  // n / 4
   const uint8_t *flags;
+  uint8_t *code;     // per cell: fluid -> diagonal (fluid + air neighbours), else kNotFluid
   const double *b;
   double *x;
   float *r, *z;
@@ -233,16 +234,41 @@ __device__ __forceinline__ void nbr_apply(const Nbr4<T> &N, T out[4]) {
   for (int c = 0; c < 4; ++c) out[c] = lane(N.fc, c) == MLPCG_FLUID ? T(d[c]) * N.c[c] - off[c] : T(0);
 }
 
-// (A v) on the 4 cells of the group at q (flat index, q % 4 == 0) at (i, j, k0);
-// cen receives v on those cells.
-template <typename T, typename S>
-__device__ __forceinline__ void lap4(const Vecs &V, uint32_t q, int i, int j, int k0, const S &src, T out[4],
-                                     T cen[4]) {
-  Nbr4<T> N;
-  nbr_load<T>(V, q, i, j, k0, src, N);
-  nbr_apply<T>(N, out);
+// The operator on vectors that vanish off the fluid cells (every CG vector
+// r, z, p, q, Ap does): a fluid cell's row is d v_c - (sum of the 6
+// neighbours), the non-fluid neighbours contributing their zeros, so the
+// stencil needs only the cell's code -- d, the number of fluid or air
+// neighbours (the CSR diagonal), or kNotFluid.  Same terms, same order as
+// nbr_apply.
+constexpr uint8_t kNotFluid = 0x80;
+
+template <typename S>
+__device__ __forceinline__ void lap4_code(const Vecs &V, uint32_t q, int i, int j, int k0, const S &src,
+                                          float out[4], float cen[4]) {
+  const uint32_t sy = (uint32_t)V.n3, sx = (uint32_t)V.n2 * (uint32_t)V.n3;
+  float xm[4] = {0.f, 0.f, 0.f, 0.f}, ym[4] = {0.f, 0.f, 0.f, 0.f};
+  float yp[4] = {0.f, 0.f, 0.f, 0.f}, xp[4] = {0.f, 0.f, 0.f, 0.f};
+  float zm = 0.f, zp = 0.f;
+  const uchar4 cd = ldflags4(V.code + q);
+  src.load4(q, cen);
+  if (i > 0) src.load4(q - sx, xm);
+  if (j > 0) src.load4(q - sy, ym);
+  if (k0 > 0) zm = src.load1(q - 1);
+  if (k0 + 4 < V.n3) zp = src.load1(q + 4);
+  if (j < V.n2 - 1) src.load4(q + sy, yp);
+  if (i < V.n1 - 1) src.load4(q + sx, xp);
 #pragma unroll
-  for (int c = 0; c < 4; ++c) cen[c] = N.c[c];
+  for (int c = 0; c < 4; ++c) {
+    float off = 0.f;
+    off += xm[c];
+    off += ym[c];
+    off += c == 0 ? zm : cen[c - 1];
+    off += c == 3 ? zp : cen[c + 1];
+    off += yp[c];
+    off += xp[c];
+    const uint8_t k = lane(cd, c);
+    out[c] = (k & kNotFluid) ? 0.f : (float)k * cen[c] - off;
+  }
 }
 
 constexpr int UNR = 2;  // groups per thread per loop pass in the streaming kernels
@@ -269,15 +295,30 @@ __global__ void k_reset(State *st, int max_it, int true_every, int method, doubl
   *st = S;
 }
 
-// r = b - A x in FP64 (b read on fluid cells only); returns sum b^2 and sum r^2
+// r = b - A x in FP64 (b read on fluid cells only); returns sum b^2 and sum r^2.
+// With CODES, also writes every cell's operator code (see lap4_code).
+template <bool CODES>
 __device__ __forceinline__ void true_residual_pass(const Vecs &V, double &bb, double &rr) {
   for (uint32_t g = gtid(); g < V.ngroups; g += gstride()) {
     uint32_t q; int i, j, k0;
     group_coords(V, g, q, i, j, k0);
-    double ax[4], xc[4], bq[4];
-    lap4<double>(V, q, i, j, k0, SrcF64{V.x}, ax, xc);
+    double ax[4], bq[4];
+    Nbr4<double> N;
+    nbr_load<double>(V, q, i, j, k0, SrcF64{V.x}, N);
+    nbr_apply<double>(N, ax);
+    if (CODES) {
+      uint8_t cd[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        auto open = [](uint8_t f) { return f == MLPCG_FLUID || f == MLPCG_AIR ? 1 : 0; };
+        const int d = open(lane(N.fxm, c)) + open(lane(N.fym, c)) + open(c == 0 ? N.fzm : lane(N.fc, c - 1)) +
+                      open(c == 3 ? N.fzp : lane(N.fc, c + 1)) + open(lane(N.fyp, c)) + open(lane(N.fxp, c));
+        cd[c] = lane(N.fc, c) == MLPCG_FLUID ? (uint8_t)d : kNotFluid;
+      }
+      *reinterpret_cast<uchar4 *>(V.code + q) = make_uchar4(cd[0], cd[1], cd[2], cd[3]);
+    }
     ld4(V.b + q, bq);
-    const uchar4 fc = ldflags4(V.flags + q);
+    const uchar4 fc = N.fc;
     float rf[4];
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
@@ -293,7 +334,7 @@ __device__ __forceinline__ void true_residual_pass(const Vecs &V, double &bb, do
 
 __global__ void __launch_bounds__(RT) k_init(Vecs V) {
   double v[2] = {0.0, 0.0};
-  true_residual_pass(V, v[0], v[1]);
+  true_residual_pass<true>(V, v[0], v[1]);
   double o[2];
   if (reduce_last<2>(v, V, 0, o) && threadIdx.x == 0) {
     State &S = *V.st;
@@ -415,19 +456,16 @@ __global__ void __launch_bounds__(RT) k_sd_spmv(Vecs V) {
   for (uint32_t g = gtid(); g < V.ngroups; g += gstride()) {
     uint32_t q; int i, j, k0;
     group_coords(V, g, q, i, j, k0);
-    Nbr4<float> N;
-    nbr_load<float>(V, q, i, j, k0, SrcF32{Q}, N);
-    float rq[4], p1[4];
+    float rq[4], p1[4], qc[4], aq[4];
     ld4(V.r + q, rq);
     if (has_prev) ld4(P1 + q, p1);
-    float aq[4];
-    nbr_apply<float>(N, aq);
+    lap4_code(V, q, i, j, k0, SrcF32{Q}, aq, qc);
     st4(AQ + q, aq);
     float s0 = 0.f, s1 = 0.f, s2 = 0.f;
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
-      s0 = fmaf(N.c[c], aq[c], s0);
-      s1 = fmaf(N.c[c], rq[c], s1);
+      s0 = fmaf(qc[c], aq[c], s0);
+      s1 = fmaf(qc[c], rq[c], s1);
       if (has_prev) s2 = fmaf(aq[c], p1[c], s2);
     }
     v[0] += s0; v[1] += s1; v[2] += s2;
@@ -484,7 +522,7 @@ __global__ void __launch_bounds__(RT) k_cg_pspmv(Vecs V) {
     uint32_t q; int i, j, k0;
     group_coords(V, g, q, i, j, k0);
     float w[4], pc[4];
-    lap4<float>(V, q, i, j, k0, src, w, pc);
+    lap4_code(V, q, i, j, k0, src, w, pc);
     st4(Pn + q, pc);
     st4(V.Ap + q, w);
 #pragma unroll
@@ -563,7 +601,7 @@ __global__ void __launch_bounds__(RT) k_true_residual(Vecs V) {
   const State &S = *V.st;
   if (S.status != ST_RUNNING || !S.need_true) return;
   double v[2] = {0.0, 0.0};
-  true_residual_pass(V, v[0], v[1]);
+  true_residual_pass<false>(V, v[0], v[1]);
   double o[2];
   if (reduce_last<2>(v, V, 0, o) && threadIdx.x == 0) V.st->rr_true = o[1];
 }
@@ -629,6 +667,7 @@ static size_t solver_layout(mlpcg_solver &s, char *base) {
   const int64_t n = cells(s.n1, s.n2, s.n3);
   const int nslots = s.method == M_NPSD ? 3 : 2;
   const int naps = s.method == M_NPSD ? 3 : 1;
+  s.V.code = (uint8_t *)take(n);
   s.V.r = (float *)take(n * 4);
   s.V.z = (float *)take(n * 4);
   s.V.p = (float *)take(nslots * n * 4);

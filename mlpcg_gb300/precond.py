@@ -46,6 +46,7 @@ class PrecondPlan:
         self.shape = tuple(int(s) for s in image.shape[1:])
         self.levels = model.n
         self.storage, self.act_storage, self.layout = storage, act_storage, layout
+        self.masked = bool(model.pre[0].mask)
         self.device = image.device
         lib = _lib.load()
         h = C.c_void_p()
@@ -83,11 +84,19 @@ class PrecondPlan:
              _stream(r.device))
         return z
 
+    def class_counts(self, level: int):
+        """(general cells, mixed runs) of a classed level; (-1, -1) on dense levels."""
+        g, r = C.c_int64(), C.c_int64()
+        call("mlpcg_precond_class_counts", self._h, int(level), C.byref(g), C.byref(r), _stream(self.device))
+        return g.value, r.value
+
     def general_cells(self, level: int) -> int:
-        """Cells of a classed level that need their own coefficients (-1 on dense levels)."""
-        c = C.c_int64()
-        call("mlpcg_precond_general_cells", self._h, int(level), C.byref(c), _stream(self.device))
-        return c.value
+        """Cells of a classed level whose neighbourhood is not a single material (-1 on dense levels)."""
+        return self.class_counts(level)[0]
+
+    def mixed_runs(self, level: int) -> int:
+        """8-cell runs of a classed level that carry a coefficient record (-1 on dense levels)."""
+        return self.class_counts(level)[1]
 
     def level_info(self, level: int):
         n1, n2, n3, fast = C.c_int(), C.c_int(), C.c_int(), C.c_int()

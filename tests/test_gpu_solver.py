@@ -65,7 +65,7 @@ def test_plan_bf16_storage(cuda, storage, act):
 @pytest.mark.parametrize("storage", [torch.float32, torch.bfloat16])
 @pytest.mark.parametrize("swap,mask", [(False, False), (True, True)])
 def test_plan_classed_is_bit_identical_to_dense(cuda, shape, n, seed, storage, swap, mask):
-    """Class map + uniform vectors + general-cell records give exactly the dense planes' output."""
+    """Run words + uniform vectors + mixed-run records give exactly the dense planes' output."""
     from mlpcg_gb300.precond import PrecondPlan
     s, flags, img = _scene(shape, seed, cuda)
     m = _model(n, cuda, seed=3, swap=swap, mask=mask)
@@ -98,6 +98,8 @@ def test_plan_classed_uniform_grid(cuda):
     cls = PrecondPlan(m, img, storage=torch.float32, layout="classed")
     interior = 28 ** 3
     assert cls.general_cells(0) == 32 ** 3 - interior
+    # runs of 8 z-cells: uniform where i, j are interior and the run avoids k < 2 and k > 29
+    assert cls.mixed_runs(0) == 32 * 32 * 4 - 28 * 28 * 2
     b = torch.randn(32 ** 3, device=cuda)
     assert torch.equal(dense.apply(b), cls.apply(b))
 
