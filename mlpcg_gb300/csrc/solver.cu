@@ -7,11 +7,16 @@
 //   NPSD (cg_tests.py:189-284): q = M r, A-orthogonalised against the last two
 //        directions, x += (q.r / q.Aq) q.
 //   NPCG (cg_tests.py:26-101): textbook PCG with the network as M.
-// Precision: vectors r, z, p, Ap in FP32 on the full grid (zero off-fluid),
-// x and b in FP64, every dot product reduced in FP64 (FP32 per-thread runs,
-// FP64 across threads, fixed-order across blocks), the residual recomputed
-// as r = b - A x in FP64 every `true_every` iterations and before declaring
-// convergence (the reference recomputes it every iteration, cg_tests.py:83,260).
+// Precision: vectors r, z, p, Ap in FP32 on the full grid (zero off-fluid);
+// the iterate x and the right-hand side b as double-float pairs (hi + lo,
+// two floats, about 48 significant bits) updated with error-free FP32
+// transformations -- GB300's FP64 pipe runs at a small fraction of its FP32
+// rate, so FP64 arithmetic is used only to convert b and x in and x out once
+// per solve; every dot product is summed per thread with a compensated FP32
+// sum and reduced in FP64 across threads and, in fixed order, across blocks;
+// the residual is recomputed as r = b - A x in double-float every
+// `true_every` iterations and before declaring convergence (the reference
+// recomputes it every iteration, cg_tests.py:83,260).
 //
 // Every reduction kernel ends with a "last block" step: block partials go to
 // scratch, the last block to finish (atomic ticket) sums them in block order
@@ -41,6 +46,7 @@ struct State {
   double alpha[3];                    // NPSD: p_j . A p_j per ring slot
   double e_last;                      // NPSD: p_recent . A p_previous
   double c0, c1, beta, rz_old, rz;
+  float beta_hi, beta_lo;             // beta as a double-float pair
   float rscale;                       // 1/||r|| fed to the preconditioner
   unsigned ticket[4];
 };
@@ -55,8 +61,9 @@ struct Vecs {
   uint32_t ngroups;  // n / 4
   const uint8_t *flags;
   uint8_t *code;     // per cell: fluid -> diagonal (fluid + air neighbours), else kNotFluid
-  const double *b;
-  double *x;
+  const double *b;   // caller's right-hand side (FP64), read once per solve
+  double *x;         // caller's iterate (FP64), read at the start and written at the end of a solve
+  float2 *xd, *bd;   // x and b as double-float pairs (x zero off the fluid cells)
   float *r, *z;
   float *p;        // 3 slots (NPSD ring) or 2 (NPCG ping-pong), n each
   float *Ap;       // 3 slots (NPSD) or 1 (NPCG)
@@ -125,6 +132,45 @@ __device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv &f) {
   return (t + ((n - t) >> f.s1)) >> f.s2;
 }
 
+// ---- double-float arithmetic: a value as the unevaluated sum hi + lo of two
+// floats, kept exact by error-free transformations (Knuth's two-sum, Dekker's
+// fast two-sum, FMA two-product); the rounded-to-nearest intrinsics keep the
+// compiler from contracting or reordering them ----
+__device__ __forceinline__ float2 two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
+  return make_float2(s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb)));
+}
+__device__ __forceinline__ float2 fast_two_sum(float a, float b) {  // |a| >= |b| or a == 0
+  const float s = __fadd_rn(a, b);
+  return make_float2(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+  const float2 s = two_sum(a.x, b.x);
+  return fast_two_sum(s.x, __fadd_rn(s.y, __fadd_rn(a.y, b.y)));
+}
+__device__ __forceinline__ float2 df_neg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 df_mul_f(float2 a, float b) {
+  const float p = __fmul_rn(a.x, b);
+  const float e = fmaf(a.y, b, fmaf(a.x, b, -p));
+  return fast_two_sum(p, e);
+}
+__device__ __forceinline__ float2 df_from_double(double v) {
+  const float hi = __double2float_rn(v);
+  return make_float2(hi, __double2float_rn(v - (double)hi));
+}
+__device__ __forceinline__ double df_to_double(float2 a) { return (double)a.x + (double)a.y; }
+
+// Compensated per-thread sum (the running error of every addition is kept)
+struct CSum {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float v) {
+    const float2 t = two_sum(s, v);
+    s = t.x;
+    c = __fadd_rn(c, t.y);
+  }
+  __device__ __forceinline__ double get() const { return (double)s + (double)c; }
+};
+
 __device__ __forceinline__ uint32_t gstride() { return gridDim.x * blockDim.x; }
 __device__ __forceinline__ uint32_t gtid() { return blockIdx.x * blockDim.x + threadIdx.x; }
 
@@ -143,6 +189,14 @@ __device__ __forceinline__ void st4(double *p, const double v[4]) {
   reinterpret_cast<double2 *>(p)[0] = make_double2(v[0], v[1]);
   reinterpret_cast<double2 *>(p)[1] = make_double2(v[2], v[3]);
 }
+__device__ __forceinline__ void ld4(const float2 *p, float2 v[4]) {
+  const float4 a = reinterpret_cast<const float4 *>(p)[0], b = reinterpret_cast<const float4 *>(p)[1];
+  v[0] = make_float2(a.x, a.y); v[1] = make_float2(a.z, a.w); v[2] = make_float2(b.x, b.y); v[3] = make_float2(b.z, b.w);
+}
+__device__ __forceinline__ void st4(float2 *p, const float2 v[4]) {
+  reinterpret_cast<float4 *>(p)[0] = make_float4(v[0].x, v[0].y, v[1].x, v[1].y);
+  reinterpret_cast<float4 *>(p)[1] = make_float4(v[2].x, v[2].y, v[3].x, v[3].y);
+}
 __device__ __forceinline__ uchar4 ldflags4(const uint8_t *p) { return *reinterpret_cast<const uchar4 *>(p); }
 __device__ __forceinline__ uint8_t lane(const uchar4 f, int c) {
   return c == 0 ? f.x : (c == 1 ? f.y : (c == 2 ? f.z : f.w));
@@ -154,10 +208,9 @@ struct SrcF32 {
   __device__ __forceinline__ void load4(uint32_t q, float v[4]) const { ld4(a + q, v); }
   __device__ __forceinline__ float load1(uint32_t q) const { return a[q]; }
 };
-struct SrcF64 {
-  const double *a;
-  __device__ __forceinline__ void load4(uint32_t q, double v[4]) const { ld4(a + q, v); }
-  __device__ __forceinline__ double load1(uint32_t q) const { return a[q]; }
+struct SrcZero {  // no values: loads only the flags of a neighbourhood
+  __device__ __forceinline__ void load4(uint32_t, float v[4]) const { v[0] = v[1] = v[2] = v[3] = 0.f; }
+  __device__ __forceinline__ float load1(uint32_t) const { return 0.f; }
 };
 // p_new = z + beta * p_old, evaluated on the fly (first iteration: p_new = z)
 struct SrcAxpy {
@@ -295,46 +348,104 @@ __global__ void k_reset(State *st, int max_it, int true_every, int method, doubl
   *st = S;
 }
 
-// r = b - A x in FP64 (b read on fluid cells only); returns sum b^2 and sum r^2.
-// With CODES, also writes every cell's operator code (see lap4_code).
-template <bool CODES>
-__device__ __forceinline__ void true_residual_pass(const Vecs &V, double &bb, double &rr) {
+// Once per solve, before the residual: every cell's operator code (see
+// lap4_code), and x, b as double-float pairs on the fluid cells (zero
+// elsewhere; the operator never reads x off the fluid cells).  The only FP64
+// arithmetic of the solve besides the final write of x; cells whose value is
+// exactly zero skip it.
+__global__ void __launch_bounds__(RT) k_prepare(Vecs V) {
   for (uint32_t g = gtid(); g < V.ngroups; g += gstride()) {
     uint32_t q; int i, j, k0;
     group_coords(V, g, q, i, j, k0);
-    double ax[4], bq[4];
-    Nbr4<double> N;
-    nbr_load<double>(V, q, i, j, k0, SrcF64{V.x}, N);
-    nbr_apply<double>(N, ax);
-    if (CODES) {
-      uint8_t cd[4];
+    Nbr4<float> N;
+    nbr_load<float>(V, q, i, j, k0, SrcZero{}, N);
+    uint8_t cd[4];
 #pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        auto open = [](uint8_t f) { return f == MLPCG_FLUID || f == MLPCG_AIR ? 1 : 0; };
-        const int d = open(lane(N.fxm, c)) + open(lane(N.fym, c)) + open(c == 0 ? N.fzm : lane(N.fc, c - 1)) +
-                      open(c == 3 ? N.fzp : lane(N.fc, c + 1)) + open(lane(N.fyp, c)) + open(lane(N.fxp, c));
-        cd[c] = lane(N.fc, c) == MLPCG_FLUID ? (uint8_t)d : kNotFluid;
-      }
-      *reinterpret_cast<uchar4 *>(V.code + q) = make_uchar4(cd[0], cd[1], cd[2], cd[3]);
+    for (int c = 0; c < 4; ++c) {
+      auto open = [](uint8_t f) { return f == MLPCG_FLUID || f == MLPCG_AIR ? 1 : 0; };
+      const int d = open(lane(N.fxm, c)) + open(lane(N.fym, c)) + open(c == 0 ? N.fzm : lane(N.fc, c - 1)) +
+                    open(c == 3 ? N.fzp : lane(N.fc, c + 1)) + open(lane(N.fyp, c)) + open(lane(N.fxp, c));
+      cd[c] = lane(N.fc, c) == MLPCG_FLUID ? (uint8_t)d : kNotFluid;
     }
+    *reinterpret_cast<uchar4 *>(V.code + q) = make_uchar4(cd[0], cd[1], cd[2], cd[3]);
+    double xq[4], bq[4];
+    ld4(V.x + q, xq);
     ld4(V.b + q, bq);
-    const uchar4 fc = N.fc;
+    float2 xd[4], bd[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const bool fl = !(cd[c] & kNotFluid);
+      // zero tests on the bit patterns (integer ops), so zero cells cost no FP64 work
+      xd[c] = (fl && (__double_as_longlong(xq[c]) << 1)) ? df_from_double(xq[c]) : make_float2(0.f, 0.f);
+      bd[c] = (fl && (__double_as_longlong(bq[c]) << 1)) ? df_from_double(bq[c]) : make_float2(0.f, 0.f);
+    }
+    st4(V.xd + q, xd);
+    st4(V.bd + q, bd);
+  }
+}
+
+// r = b - A x in double-float arithmetic (x, b as pairs, zero off the fluid
+// cells), stored rounded to FP32; accumulates sum r^2 (and, with BB, sum b^2)
+// with compensated FP32 sums.  The neighbours are added in the column order
+// of the assembled CSR row (i-1, j-1, k-1, k+1, j+1, i+1).
+template <bool BB>
+__device__ __forceinline__ void residual_pass(const Vecs &V, CSum &bb, CSum &rr) {
+  const uint32_t sy = (uint32_t)V.n3, sx = (uint32_t)V.n2 * (uint32_t)V.n3;
+  const float2 zero = make_float2(0.f, 0.f);
+  for (uint32_t g = gtid(); g < V.ngroups; g += gstride()) {
+    uint32_t q; int i, j, k0;
+    group_coords(V, g, q, i, j, k0);
+    float2 cen[4], xm[4], ym[4], yp[4], xp[4], bq[4];
+    float2 zm = zero, zp = zero;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) xm[c] = ym[c] = yp[c] = xp[c] = zero;
+    const uchar4 cd = ldflags4(V.code + q);
+    ld4(V.xd + q, cen);
+    ld4(V.bd + q, bq);
+    if (i > 0) ld4(V.xd + q - sx, xm);
+    if (j > 0) ld4(V.xd + q - sy, ym);
+    if (k0 > 0) zm = V.xd[q - 1];
+    if (k0 + 4 < V.n3) zp = V.xd[q + 4];
+    if (j < V.n2 - 1) ld4(V.xd + q + sy, yp);
+    if (i < V.n1 - 1) ld4(V.xd + q + sx, xp);
     float rf[4];
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
-      const double b = lane(fc, c) == MLPCG_FLUID ? bq[c] : 0.0;
-      const double r = b - ax[c];
-      rf[c] = (float)r;
-      bb += b * b;
-      rr += r * r;
+      const uint8_t k = lane(cd, c);
+      rf[c] = 0.f;
+      if (k & kNotFluid) continue;
+      float2 off = df_add(xm[c], ym[c]);
+      off = df_add(off, c == 0 ? zm : cen[c - 1]);
+      off = df_add(off, c == 3 ? zp : cen[c + 1]);
+      off = df_add(off, yp[c]);
+      off = df_add(off, xp[c]);
+      const float2 ax = df_add(df_mul_f(cen[c], (float)k), df_neg(off));
+      const float2 rv = df_add(bq[c], df_neg(ax));
+      rf[c] = __fadd_rn(rv.x, rv.y);
+      rr.add(__fmul_rn(rf[c], rf[c]));
+      if (BB) bb.add(__fmul_rn(bq[c].x, bq[c].x));
     }
     st4(V.r + q, rf);
   }
 }
 
+// The caller's x from the pairs, on the fluid cells (the others keep their values)
+__global__ void __launch_bounds__(RT) k_finalize(Vecs V) {
+  for (uint32_t g = gtid(); g < V.ngroups; g += gstride()) {
+    const uint32_t q = 4u * g;
+    const uchar4 cd = ldflags4(V.code + q);
+    float2 xd[4];
+    ld4(V.xd + q, xd);
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+      if (!(lane(cd, c) & kNotFluid)) V.x[q + c] = df_to_double(xd[c]);
+  }
+}
+
 __global__ void __launch_bounds__(RT) k_init(Vecs V) {
-  double v[2] = {0.0, 0.0};
-  true_residual_pass<true>(V, v[0], v[1]);
+  CSum bb, rr;
+  residual_pass<true>(V, bb, rr);
+  double v[2] = {bb.get(), rr.get()};
   double o[2];
   if (reduce_last<2>(v, V, 0, o) && threadIdx.x == 0) {
     State &S = *V.st;
@@ -355,6 +466,7 @@ __global__ void __launch_bounds__(RT) k_init(Vecs V) {
     S.alpha[0] = S.alpha[1] = S.alpha[2] = 0.0;
     S.e_last = 0.0;
     S.beta = S.c0 = S.c1 = 0.0;
+    S.beta_hi = S.beta_lo = 0.f;
     S.rz_old = 0.0;
     V.hist[0] = S.rel;
   }
@@ -377,7 +489,7 @@ __global__ void __launch_bounds__(RT) k_sd_dots(Vecs V) {
   const int h = S.head, hp = (h + 2) % 3;
   const float *A1 = V.Ap + (size_t)h * V.n, *A0 = V.Ap + (size_t)hp * V.n;
   const bool two = it >= 2;
-  double v[2] = {0.0, 0.0};
+  CSum a1s, a0s;
   for (uint32_t g0 = blockIdx.x * RT * UNR + threadIdx.x; g0 < V.ngroups; g0 += gridDim.x * RT * UNR) {
     float z[UNR][4], a1[UNR][4], a0[UNR][4];
 #pragma unroll
@@ -398,9 +510,10 @@ __global__ void __launch_bounds__(RT) k_sd_dots(Vecs V) {
         if (two) s0 = fmaf(z[u][c], a0[u][c], s0);
       }
     }
-    v[0] += s1;
-    v[1] += s0;
+    a1s.add(s1);
+    a0s.add(s0);
   }
+  double v[2] = {a1s.get(), a0s.get()};
   double o[2];
   if (reduce_last<2>(v, V, 1, o) && threadIdx.x == 0) {
     State &W = *V.st;
@@ -452,7 +565,7 @@ __global__ void __launch_bounds__(RT) k_sd_spmv(Vecs V) {
   const float *Q = V.p + (size_t)hn * V.n, *P1 = V.p + (size_t)h * V.n;
   float *AQ = V.Ap + (size_t)hn * V.n;
   const bool has_prev = S.it >= 1;
-  double v[3] = {0.0, 0.0, 0.0};
+  CSum t0, t1, t2;
   for (uint32_t g = gtid(); g < V.ngroups; g += gstride()) {
     uint32_t q; int i, j, k0;
     group_coords(V, g, q, i, j, k0);
@@ -468,8 +581,9 @@ __global__ void __launch_bounds__(RT) k_sd_spmv(Vecs V) {
       s1 = fmaf(qc[c], rq[c], s1);
       if (has_prev) s2 = fmaf(aq[c], p1[c], s2);
     }
-    v[0] += s0; v[1] += s1; v[2] += s2;
+    t0.add(s0); t1.add(s1); t2.add(s2);
   }
+  double v[3] = {t0.get(), t1.get(), t2.get()};
   double o[3];
   if (reduce_last<3>(v, V, 2, o) && threadIdx.x == 0) {
     State &W = *V.st;
@@ -477,6 +591,9 @@ __global__ void __launch_bounds__(RT) k_sd_spmv(Vecs V) {
     W.e_last = o[2];
     W.head = hn;
     W.beta = o[1] / o[0];
+    const float2 bdf = df_from_double(W.beta);
+    W.beta_hi = bdf.x;
+    W.beta_lo = bdf.y;
     if (!(o[0] > 0.0) || !isfinite(W.beta)) W.status = isfinite(o[0]) ? ST_BREAKDOWN : ST_NONFINITE;
   }
 }
@@ -487,18 +604,17 @@ __global__ void __launch_bounds__(RT) k_sd_spmv(Vecs V) {
 __global__ void __launch_bounds__(RT) k_cg_rz(Vecs V) {
   const State &S = *V.st;
   if (S.status != ST_RUNNING) return;
-  double v[1] = {0.0};
-  float s = 0.f;
-  int cnt = 0;
+  CSum t;
   for (uint32_t g = gtid(); g < V.ngroups; g += gstride()) {
     float r[4], z[4];
     ld4(V.r + 4 * g, r);
     ld4(V.z + 4 * g, z);
+    float s = 0.f;
 #pragma unroll
     for (int c = 0; c < 4; ++c) s = fmaf(r[c], z[c], s);
-    if (++cnt == 8) { v[0] += s; s = 0.f; cnt = 0; }
+    t.add(s);
   }
-  v[0] += s;
+  double v[1] = {t.get()};
   double o[1];
   if (reduce_last<1>(v, V, 1, o) && threadIdx.x == 0) {
     State &W = *V.st;
@@ -515,9 +631,7 @@ __global__ void __launch_bounds__(RT) k_cg_pspmv(Vecs V) {
   const int cur = S.pp, nxt = cur ^ 1;
   float *Pn = V.p + (size_t)nxt * V.n;
   const SrcAxpy src{V.z, V.p + (size_t)cur * V.n, (float)S.c1, S.it == 0};
-  double v[1] = {0.0};
-  float s = 0.f;
-  int cnt = 0;
+  CSum t;
   for (uint32_t g = gtid(); g < V.ngroups; g += gstride()) {
     uint32_t q; int i, j, k0;
     group_coords(V, g, q, i, j, k0);
@@ -525,22 +639,26 @@ __global__ void __launch_bounds__(RT) k_cg_pspmv(Vecs V) {
     lap4_code(V, q, i, j, k0, src, w, pc);
     st4(Pn + q, pc);
     st4(V.Ap + q, w);
+    float s = 0.f;
 #pragma unroll
     for (int c = 0; c < 4; ++c) s = fmaf(pc[c], w[c], s);
-    if (++cnt == 8) { v[0] += s; s = 0.f; cnt = 0; }
+    t.add(s);
   }
-  v[0] += s;
+  double v[1] = {t.get()};
   double o[1];
   if (reduce_last<1>(v, V, 2, o) && threadIdx.x == 0) {
     State &W = *V.st;
     W.pp = nxt;
     W.beta = W.rz / o[0];  // the step length alpha of cg_tests.py:81
+    const float2 bdf = df_from_double(W.beta);
+    W.beta_hi = bdf.x;
+    W.beta_lo = bdf.y;
     if (!isfinite(W.beta) || o[0] == 0.0) W.status = isfinite(o[0]) ? ST_BREAKDOWN : ST_NONFINITE;
   }
 }
 
 // ---------------------------------------------------------------------------
-// shared: x += beta d; r -= beta A d; rr = r.r; decide whether a true residual is due
+// shared: x += beta d (double-float); r -= beta A d; rr = r.r; decide whether a true residual is due
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(RT) k_update(Vecs V) {
   const State &S = *V.st;
@@ -553,12 +671,12 @@ __global__ void __launch_bounds__(RT) k_update(Vecs V) {
     D = V.p + (size_t)S.pp * V.n;
     AD = V.Ap;
   }
-  const double bd = S.beta;
+  const float2 bd = make_float2(S.beta_hi, S.beta_lo);
   const float bf = (float)S.beta;
-  double v[1] = {0.0};
+  CSum t;
   for (uint32_t g0 = blockIdx.x * RT * UNR + threadIdx.x; g0 < V.ngroups; g0 += gridDim.x * RT * UNR) {
     float d[UNR][4], ad[UNR][4], r[UNR][4];
-    double x[UNR][4];
+    float2 x[UNR][4];
 #pragma unroll
     for (int u = 0; u < UNR; ++u) {
       const uint32_t q = 4u * (g0 + u * RT);
@@ -566,7 +684,7 @@ __global__ void __launch_bounds__(RT) k_update(Vecs V) {
       ld4(D + q, d[u]);
       ld4(AD + q, ad[u]);
       ld4(V.r + q, r[u]);
-      ld4(V.x + q, x[u]);
+      ld4(V.xd + q, x[u]);
     }
     float s = 0.f;
 #pragma unroll
@@ -575,15 +693,16 @@ __global__ void __launch_bounds__(RT) k_update(Vecs V) {
       if (g0 + u * RT >= V.ngroups) continue;
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
-        x[u][c] = fma(bd, (double)d[u][c], x[u][c]);
+        x[u][c] = df_add(x[u][c], df_mul_f(bd, d[u][c]));
         r[u][c] = fmaf(-bf, ad[u][c], r[u][c]);
         s = fmaf(r[u][c], r[u][c], s);
       }
-      st4(V.x + q, x[u]);
+      st4(V.xd + q, x[u]);
       st4(V.r + q, r[u]);
     }
-    v[0] += s;
+    t.add(s);
   }
+  double v[1] = {t.get()};
   double o[1];
   if (reduce_last<1>(v, V, 3, o) && threadIdx.x == 0) {
     State &W = *V.st;
@@ -596,12 +715,13 @@ __global__ void __launch_bounds__(RT) k_update(Vecs V) {
   }
 }
 
-// r = b - A x in FP64 when due
+// r = b - A x (double-float) when due
 __global__ void __launch_bounds__(RT) k_true_residual(Vecs V) {
   const State &S = *V.st;
   if (S.status != ST_RUNNING || !S.need_true) return;
-  double v[2] = {0.0, 0.0};
-  true_residual_pass<false>(V, v[0], v[1]);
+  CSum bb, rr;
+  residual_pass<false>(V, bb, rr);
+  double v[2] = {0.0, rr.get()};
   double o[2];
   if (reduce_last<2>(v, V, 0, o) && threadIdx.x == 0) V.st->rr_true = o[1];
 }
@@ -668,6 +788,8 @@ static size_t solver_layout(mlpcg_solver &s, char *base) {
   const int nslots = s.method == M_NPSD ? 3 : 2;
   const int naps = s.method == M_NPSD ? 3 : 1;
   s.V.code = (uint8_t *)take(n);
+  s.V.xd = (float2 *)take(n * 8);
+  s.V.bd = (float2 *)take(n * 8);
   s.V.r = (float *)take(n * 4);
   s.V.z = (float *)take(n * 4);
   s.V.p = (float *)take(nslots * n * 4);
@@ -769,6 +891,7 @@ int mlpcg_solver_solve(mlpcg_solver *s, int use_graph, void *stream) {
   cudaStream_t st = as_stream(stream);
   Vecs &V = s->V;
   k_reset<<<1, 32, 0, st>>>(V.st, s->max_it, s->true_every, s->method, s->tol);
+  k_prepare<<<(unsigned)V.nblk, RT, 0, st>>>(V);
   k_init<<<(unsigned)V.nblk, RT, 0, st>>>(V);
   MLPCG_LAUNCH_CHECK();
   if (!use_graph) {
@@ -780,6 +903,8 @@ int mlpcg_solver_solve(mlpcg_solver *s, int use_graph, void *stream) {
       int rc = enqueue_body(s, st, 0, 0);
       if (rc) return rc;
     }
+    k_finalize<<<(unsigned)V.nblk, RT, 0, st>>>(V);
+    MLPCG_LAUNCH_CHECK();
     return MLPCG_OK;
   }
   if (!s->exec) {
@@ -809,6 +934,8 @@ int mlpcg_solver_solve(mlpcg_solver *s, int use_graph, void *stream) {
   // the body's first kernels see status != RUNNING and the control kernel
   // ends the loop after one pass.
   MLPCG_CUDA_CHECK(cudaGraphLaunch(s->exec, st));
+  k_finalize<<<(unsigned)V.nblk, RT, 0, st>>>(V);
+  MLPCG_LAUNCH_CHECK();
   return MLPCG_OK;
 }
 

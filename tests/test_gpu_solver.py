@@ -168,6 +168,30 @@ def test_fused_matches_dropin_history(cuda, method):
         assert abs(np.log10(res.rel_res) - np.log10(hist[-1])) < 1.0
 
 
+def test_fused_warm_start_and_off_fluid_values(cuda):
+    """x0 enters through its double-float pair: restarting from the solution is already converged,
+    a perturbed start converges to the same solution, and x0 off the fluid cells is left as given."""
+    from mlpcg_gb300.solver import FusedSolver
+    s, flags, img = _scene((24, 24, 24), 3, cuda)
+    m = _near_identity_model(3, cuda, eps=0.0)
+    solver = FusedSolver(m, flags, method="npsd", max_it=400, tol=1e-6, storage=torch.float32)
+    b = torch.as_tensor(s.rhs, device=cuda)
+    fluid = flags == 2
+    cold = solver.solve(b)
+    assert cold.status == "converged"
+    xc = cold.x.clone()
+    warm = solver.solve(b, x0=xc.clone())
+    assert warm.status == "converged" and warm.iterations == 0
+    assert rel_err(warm.x[fluid].cpu(), xc[fluid].cpu()) < 1e-12
+    g = torch.Generator(device=cuda).manual_seed(4)
+    x0 = xc + 0.1 * xc.abs().max() * torch.randn(xc.shape, generator=g, device=cuda, dtype=torch.float64)
+    x0[~fluid] = 7.0
+    pert = solver.solve(b, x0=x0)
+    assert pert.status == "converged" and pert.iterations > 0
+    assert torch.all(pert.x[~fluid] == 7.0)
+    assert rel_err(pert.x[fluid].cpu(), xc[fluid].cpu()) < 1e-4
+
+
 def test_fused_graph_reuse_is_deterministic(cuda):
     from mlpcg_gb300.solver import FusedSolver
     s, flags, img = _scene((32, 32, 32), 7, cuda)
