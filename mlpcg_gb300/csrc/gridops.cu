@@ -152,7 +152,7 @@ __global__ void k_axpby(const float *__restrict__ c0, const T *__restrict__ x,
 // pass computes 27 x 3 class sums and the 81 shifted sums follow by
 // inclusion (deterministic: per-block FP64 partials summed in fixed order).
 // ---------------------------------------------------------------------------
-constexpr int kLinBlocks = 304;
+constexpr int kLinBlocks = 1216;
 constexpr int kLinThreads = 256;
 constexpr int kLinWarps = kLinThreads / 32;
 
@@ -160,17 +160,17 @@ constexpr int kLinWarps = kLinThreads / 32;
 // interior 1, last plane 2 (a single plane is class 0)
 __device__ __forceinline__ int axis_class(int c, int n) { return c == 0 ? 0 : (c == n - 1 ? 2 : 1); }
 
-// Per-block FP64 partial sums of the 3 image channels over each of the 27
-// classes.  Warps take whole z-rows (i, j), which share the row class
-// (x class, y class); a lane sums its cells by z class in FP32 across the rows
-// of one row class, and the sums go through an FP64 warp reduction into the
-// warp's slots whenever the row class changes.  Deterministic: the row
-// assignment and every reduction order are fixed.
+// Per-block partial sums (double-float pairs) of the 3 image channels over
+// each of the 27 classes.  Warps take whole z-rows (i, j), which share the
+// row class (x class, y class); a lane sums its cells by z class in FP32
+// across the rows of one row class, and the sums go through a double-float
+// warp reduction into the warp's slots whenever the row class changes.
+// Deterministic: the row assignment and every reduction order are fixed.
 __global__ void __launch_bounds__(kLinThreads)
-k_class_sums(const float *__restrict__ img, int n1, int n2, int n3, double *__restrict__ partial) {
-  __shared__ double ws[kLinWarps][81];  // per warp: (class * 3 + channel)
+k_class_sums(const float *__restrict__ img, int n1, int n2, int n3, float2 *__restrict__ partial) {
+  __shared__ float2 ws[kLinWarps][81];  // per warp: (class * 3 + channel)
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int e = lane; e < 81; e += 32) ws[w][e] = 0.0;
+  for (int e = lane; e < 81; e += 32) ws[w][e] = make_float2(0.f, 0.f);
   __syncwarp();
   const int64_t n = cells(n1, n2, n3);
   const int64_t rows = (int64_t)n1 * n2;
@@ -182,10 +182,10 @@ k_class_sums(const float *__restrict__ img, int n1, int n2, int n3, double *__re
     for (int ch = 0; ch < 3; ++ch)
 #pragma unroll
       for (int cz = 0; cz < 3; ++cz) {
-        double d = a[ch][cz];
+        float2 d = make_float2(a[ch][cz], 0.f);
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
-        if (lane == 0) ws[w][(key * 3 + cz) * 3 + ch] += d;
+        for (int o = 16; o > 0; o >>= 1) d = df_add(d, df_shfl_xor(d, o));
+        if (lane == 0) ws[w][(key * 3 + cz) * 3 + ch] = df_add(ws[w][(key * 3 + cz) * 3 + ch], d);
         a[ch][cz] = 0.f;
       }
   };
@@ -220,34 +220,34 @@ k_class_sums(const float *__restrict__ img, int n1, int n2, int n3, double *__re
   if (key >= 0) flush();
   __syncthreads();
   if (threadIdx.x < 81) {
-    double s = 0.0;
+    float2 s = make_float2(0.f, 0.f);
 #pragma unroll
-    for (int ww = 0; ww < kLinWarps; ++ww) s += ws[ww][threadIdx.x];
+    for (int ww = 0; ww < kLinWarps; ++ww) s = df_add(s, ws[ww][threadIdx.x]);
     partial[(int64_t)threadIdx.x * gridDim.x + blockIdx.x] = s;
   }
 }
 
 // One block of 1024 threads: class sums -> 81 shifted means y -> nlin outputs z.
 // Output j uses weights W + j*wstride (81 values), bias[j*bstride], and goes to z[j*zstride].
-__global__ void k_linear_finalize(const double *__restrict__ partial, int nblk, int n1, int n2, int n3,
+__global__ void k_linear_finalize(const float2 *__restrict__ partial, int nblk, int n1, int n2, int n3,
                                   const float *__restrict__ W, int64_t wstride, const float *__restrict__ bias,
                                   int64_t bstride, int nlin, float *__restrict__ z, int64_t zstride,
                                   float *__restrict__ yout) {
   __shared__ double cs[27 * 3];
   __shared__ double ym[81];
   const int t = threadIdx.x;
-  // cs[cls * 3 + channel] = the sum of the blocks' partials (a warp per value, fixed order;
-  // every load of a lane issued before its first add)
+  // cs[cls * 3 + channel] = the sum of the blocks' partials (a warp per value,
+  // double-float, fixed order; every load of a lane issued before its first add)
   for (int c = t >> 5; c < 81; c += blockDim.x >> 5) {
-    double s = 0.0;
+    float2 s = make_float2(0.f, 0.f);
 #pragma unroll
     for (int u = 0; u < (kLinBlocks + 31) / 32; ++u) {
       const int b = (t & 31) + 32 * u;
-      if (b < nblk) s += partial[(int64_t)c * nblk + b];
+      if (b < nblk) s = df_add(s, partial[(int64_t)c * nblk + b]);
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if ((t & 31) == 0) cs[c] = s;
+    for (int o = 16; o > 0; o >>= 1) s = df_add(s, df_shfl_xor(s, o));
+    if ((t & 31) == 0) cs[c] = df_to_double(s);
   }
   __syncthreads();
   // shift index k in {0,1,2} (offset k-1) keeps classes: k=0 -> {0,1}, k=1 -> all, k=2 -> {1,2};
@@ -412,16 +412,16 @@ int launch_axpby(const float *c0, const void *x, const float *c1, const void *y,
   return MLPCG_OK;
 }
 
-size_t linear_workspace() { return (size_t)27 * 3 * kLinBlocks * sizeof(double); }
+size_t linear_workspace() { return (size_t)27 * 3 * kLinBlocks * sizeof(float2); }
 
 int launch_linear_forward_strided(const float *img, int n1, int n2, int n3, const float *W, int64_t wstride,
                                   const float *bias, int64_t bstride, int nlin, float *z, int64_t zstride, float *y,
                                   void *ws, size_t ws_bytes, cudaStream_t st) {
   MLPCG_REQUIRE(ws_bytes >= linear_workspace(), MLPCG_ERR_WORKSPACE,
                 "sm_linear_3d workspace too small: %zu < %zu", ws_bytes, linear_workspace());
-  k_class_sums<<<kLinBlocks, kLinThreads, 0, st>>>(img, n1, n2, n3, (double *)ws);
+  k_class_sums<<<kLinBlocks, kLinThreads, 0, st>>>(img, n1, n2, n3, (float2 *)ws);
   MLPCG_LAUNCH_CHECK();
-  k_linear_finalize<<<1, 1024, 0, st>>>((const double *)ws, kLinBlocks, n1, n2, n3, W, wstride, bias, bstride, nlin,
+  k_linear_finalize<<<1, 1024, 0, st>>>((const float2 *)ws, kLinBlocks, n1, n2, n3, W, wstride, bias, bstride, nlin,
                                        z, zstride, y);
   MLPCG_LAUNCH_CHECK();
   return MLPCG_OK;

@@ -417,10 +417,12 @@ k_kgen_uniform_all(const float *__restrict__ params, float *__restrict__ kuni) {
 }
 
 // The linear index of every general cell, tile by tile in thread / run / cell
-// order: list[gbase[tile] + rank] = q.
+// order: list[gbase[tile] + rank] = q; and the run index (q / 8) of every
+// mixed run at its record position: rlist[rbase[tile] + local index].
 __global__ void __launch_bounds__(PT)
 k_list_general(const uint8_t *__restrict__ cls, int n1, int n2, int n3, const uint32_t *__restrict__ gbase,
-               uint32_t *__restrict__ list) {
+               uint32_t *__restrict__ list, const uint32_t *__restrict__ rw, const uint32_t *__restrict__ rbase,
+               uint32_t *__restrict__ rlist) {
   const int k0 = blockIdx.x * TZ + run_tz(threadIdx.x) * 8, j = blockIdx.y * TY + run_ty(threadIdx.x);
   uint2 cw[TX];
   uint32_t gm[TX];
@@ -429,8 +431,12 @@ k_list_general(const uint8_t *__restrict__ cls, int n1, int n2, int n3, const ui
   for (int tx = 0; tx < TX; ++tx) {
     const int i = blockIdx.z * TX + tx;
     cw[tx] = make_uint2(0u, 0u);
-    if (k0 < n3 && j < n2 && i < n1)
-      cw[tx] = __ldg(reinterpret_cast<const uint2 *>(cls + ((int64_t)i * n2 + j) * n3 + k0));
+    if (k0 < n3 && j < n2 && i < n1) {
+      const int64_t q0 = ((int64_t)i * n2 + j) * n3 + k0;
+      cw[tx] = __ldg(reinterpret_cast<const uint2 *>(cls + q0));
+      const uint32_t word = __ldg(rw + (q0 >> 3));
+      if ((word & 3u) == kMixed) rlist[__ldg(rbase + tile_id()) + (word >> 2)] = (uint32_t)(q0 >> 3);
+    }
     gm[tx] = 0u;
 #pragma unroll
     for (int c = 0; c < 8; ++c) gm[tx] |= (class_of(cw[tx], c) == CLS_GENERAL ? 1u : 0u) << c;
@@ -506,22 +512,25 @@ k_kgen_list(const float *__restrict__ img, int n1, int n2, int n3, const float *
 }
 
 // The uniform cells of the mixed runs: their material's vector, for NB blocks
-// (uniform vectors at kuni0 / kuni1).  One thread per cell of the level.
+// (uniform vectors at kuni0 / kuni1).  Thread e of the grid-stride loop takes
+// cell e % 8 of mixed run e / 8 (runs from rlist; their count read on the
+// device).
 template <typename KT, int NB>
 __global__ void __launch_bounds__(256)
-k_fill_uniform(const uint8_t *__restrict__ cls, const uint32_t *__restrict__ rw, const uint32_t *__restrict__ rbase,
+k_fill_uniform(const uint8_t *__restrict__ cls, const uint32_t *__restrict__ rlist,
+               const uint32_t *__restrict__ rlast_base, const uint32_t *__restrict__ rlast_count,
+               const uint32_t *__restrict__ rw, const uint32_t *__restrict__ rbase,
                const uint32_t *__restrict__ rcount, int n1, int n2, int n3, const float *__restrict__ kuni0,
                const float *__restrict__ kuni1, KT *__restrict__ rec0, KT *__restrict__ rec1) {
-  const int64_t n = cells(n1, n2, n3);
-  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
-    const uint32_t word = __ldg(rw + (q >> 3));
-    if ((word & 3u) != kMixed) continue;
+  const uint64_t ncell = 8ull * (__ldg(rlast_base) + __ldg(rlast_count));
+  for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < ncell; e += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t q = 8u * __ldg(rlist + (e >> 3)) + (uint32_t)(e & 7);
     const int cl = cls[q];
     if (cl == CLS_GENERAL) continue;
-    const int k = (int)(q % n3);
-    const int64_t t = q / n3;
-    const int j = (int)(t % n2), i = (int)(t / n2);
-    const RecPos rp = rec_pos(rw, rbase, rcount, (uint32_t)q, i, j, k, n2, n3);
+    const int k = (int)(q % (uint32_t)n3);
+    const uint32_t t = q / (uint32_t)n3;
+    const int j = (int)(t % (uint32_t)n2), i = (int)(t / (uint32_t)n2);
+    const RecPos rp = rec_pos(rw, rbase, rcount, q, i, j, k, n2, n3);
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
       const float *ku = (b ? kuni1 : kuni0) + cl * KREC;
@@ -1037,6 +1046,7 @@ struct PrecondPlan {
   void *Mrec = nullptr;       // material records of all blocks (block order of Uall)
   void *ufine = nullptr;      // level-0 prolongated post-block input
   uint32_t *glist = nullptr;  // general-cell list (setup scratch)
+  uint32_t *rlist = nullptr;  // mixed-run list (setup scratch)
   std::vector<void *> Kpre, Kpost;   // dense planes, or mixed-run records on classed levels
   void *Kl = nullptr;
   std::vector<float *> Upre, Upost;  // classed levels: 3 x KREC uniform vectors per block
@@ -1129,8 +1139,9 @@ static size_t plan_layout(PrecondPlan &P, char *base) {
     P.gbase[l] = (uint32_t *)take(v.ntiles * sizeof(uint32_t));
     nlist = std::max<int64_t>(nlist, v.n);
   }
-  // general-cell list of one level at a time (setup only)
+  // general-cell and mixed-run lists of one level at a time (setup only)
   P.glist = nlist ? (uint32_t *)take((size_t)nlist * sizeof(uint32_t)) : nullptr;
+  P.rlist = nlist ? (uint32_t *)take((size_t)(nlist / 8 + 1) * sizeof(uint32_t)) : nullptr;
   for (int l = 0; l < P.L; ++l) P.y[l] = take(P.lv[l].ps * sa);
   for (int l = 1; l <= P.L; ++l) {
     P.xin[l] = take(P.lv[l].ps * sa);
@@ -1406,19 +1417,21 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
     MLPCG_LAUNCH_CHECK();
     k_scan_tiles<<<1, 1024, 0, st>>>(P.gcount[l], P.gbase[l], (int)v.ntiles);
     MLPCG_LAUNCH_CHECK();
-    k_list_general<<<grid_of(v), PT, 0, st>>>(P.cls[l], v.n1, v.n2, v.n3, P.gbase[l], P.glist);
+    k_list_general<<<grid_of(v), PT, 0, st>>>(P.cls[l], v.n1, v.n2, v.n3, P.gbase[l], P.glist, P.rw[l], P.rbase[l],
+                                              P.rlist);
     MLPCG_LAUNCH_CHECK();
     // general cells: one wave of CTAs (as many as fit on every SM), each looping over its share
     const uint32_t *lb = P.gbase[l] + v.ntiles - 1, *lc = P.gcount[l] + v.ntiles - 1;
     const float *u0 = P.Uall + (size_t)b0 * 3 * KREC, *u1 = P.Uall + (size_t)(b1 >= 0 ? b1 : b0) * 3 * KREC;
     const int fgrid = (int)std::min<int64_t>((int64_t)sm_count() * 8, (v.n + 255) / 256);
+    const uint32_t *rlb = P.rbase[l] + v.ntiles - 1, *rlc = P.rcount[l] + v.ntiles - 1;
     auto launch = [&](auto kern, auto fill, const void *r0, const void *r1) {
       using KT = typename std::remove_pointer<decltype(kgen_rec_type(kern))>::type;
       const int grid = (int)std::min<int64_t>((int64_t)sm_count() * resident_ctas(kern), (v.n + PT - 1) / PT);
       kern<<<grid, PT, 0, st>>>(im, v.n1, v.n2, v.n3, params, b0, b1 >= 0 ? b1 : b0, P.glist, lb, lc, P.rw[l],
                                 P.rbase[l], P.rcount[l], (KT *)r0, (KT *)r1);
-      fill<<<fgrid, 256, 0, st>>>(P.cls[l], P.rw[l], P.rbase[l], P.rcount[l], v.n1, v.n2, v.n3, u0, u1, (KT *)r0,
-                                  (KT *)r1);
+      fill<<<fgrid, 256, 0, st>>>(P.cls[l], P.rlist, rlb, rlc, P.rw[l], P.rbase[l], P.rcount[l], v.n1, v.n2, v.n3, u0,
+                                  u1, (KT *)r0, (KT *)r1);
     };
     if (P.kdt == MLPCG_BF16) {
       if (b1 >= 0) launch(k_kgen_list<__nv_bfloat16, 2>, k_fill_uniform<__nv_bfloat16, 2>, K0, K1);

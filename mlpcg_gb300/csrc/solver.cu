@@ -132,45 +132,6 @@ __device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv &f) {
   return (t + ((n - t) >> f.s1)) >> f.s2;
 }
 
-// ---- double-float arithmetic: a value as the unevaluated sum hi + lo of two
-// floats, kept exact by error-free transformations (Knuth's two-sum, Dekker's
-// fast two-sum, FMA two-product); the rounded-to-nearest intrinsics keep the
-// compiler from contracting or reordering them ----
-__device__ __forceinline__ float2 two_sum(float a, float b) {
-  const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
-  return make_float2(s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb)));
-}
-__device__ __forceinline__ float2 fast_two_sum(float a, float b) {  // |a| >= |b| or a == 0
-  const float s = __fadd_rn(a, b);
-  return make_float2(s, __fsub_rn(b, __fsub_rn(s, a)));
-}
-__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
-  const float2 s = two_sum(a.x, b.x);
-  return fast_two_sum(s.x, __fadd_rn(s.y, __fadd_rn(a.y, b.y)));
-}
-__device__ __forceinline__ float2 df_neg(float2 a) { return make_float2(-a.x, -a.y); }
-__device__ __forceinline__ float2 df_mul_f(float2 a, float b) {
-  const float p = __fmul_rn(a.x, b);
-  const float e = fmaf(a.y, b, fmaf(a.x, b, -p));
-  return fast_two_sum(p, e);
-}
-__device__ __forceinline__ float2 df_from_double(double v) {
-  const float hi = __double2float_rn(v);
-  return make_float2(hi, __double2float_rn(v - (double)hi));
-}
-__device__ __forceinline__ double df_to_double(float2 a) { return (double)a.x + (double)a.y; }
-
-// Compensated per-thread sum (the running error of every addition is kept)
-struct CSum {
-  float s = 0.f, c = 0.f;
-  __device__ __forceinline__ void add(float v) {
-    const float2 t = two_sum(s, v);
-    s = t.x;
-    c = __fadd_rn(c, t.y);
-  }
-  __device__ __forceinline__ double get() const { return (double)s + (double)c; }
-};
-
 __device__ __forceinline__ uint32_t gstride() { return gridDim.x * blockDim.x; }
 __device__ __forceinline__ uint32_t gtid() { return blockIdx.x * blockDim.x + threadIdx.x; }
 
