@@ -78,6 +78,53 @@ __device__ __forceinline__ float2 df_from_double(double v) {
   return make_float2(hi, __double2float_rn(v - (double)hi));
 }
 __device__ __forceinline__ double df_to_double(float2 a) { return (double)a.x + (double)a.y; }
+
+// The same two conversions for bulk use with integer operations only (the
+// FP64 pipe is the bottleneck of a pass that converts every cell).  Results
+// equal df_from_double / df_to_double bit for bit; values outside the range
+// handled here (exponents far from 1, zeros, subnormals, Inf, NaN, or a low
+// part tiny against the high part) take the FP64 routine above.
+__device__ __forceinline__ float pow2f(int k) { return __int_as_float((k + 127) << 23); }  // k in [-126, 127]
+
+__device__ __forceinline__ float2 df_from_double_bits(double v) {
+  const uint64_t u = (uint64_t)__double_as_longlong(v);
+  const int E = (int)((u >> 52) & 0x7ff) - 1023;
+  if (E < -74 || E > 120) return df_from_double(v);
+  const uint64_t full = (1ull << 52) | (u & ((1ull << 52) - 1));  // 53-bit significand
+  const uint64_t hm = (full + (1ull << 28) - 1 + ((full >> 29) & 1)) >> 29;  // rounded to 24 bits (nearest even)
+  int rem = (int)((int64_t)full - (int64_t)(hm << 29));  // |rem| <= 2^28: |v| - |hi| in units of 2^(E-52)
+  float hi = __uint2float_rn((uint32_t)hm) * pow2f(E - 23);
+  if (u >> 63) { hi = -hi; rem = -rem; }  // the sign on the integer keeps a zero low part +0, as v - hi gives
+  return make_float2(hi, __int2float_rn(rem) * pow2f(E - 52));
+}
+
+__device__ __forceinline__ double df_to_double_bits(float2 a) {
+  const uint32_t hb = __float_as_uint(a.x), lb = __float_as_uint(a.y);
+  const int eh = (int)((hb >> 23) & 0xff), el = (int)((lb >> 23) & 0xff);
+  if (eh == 0 || eh == 255) return df_to_double(a);
+  // hi as a 53-bit significand in units of 2^(Eh - 52)
+  const int64_t H = (int64_t)((1ull << 23) | (hb & 0x7fffffu)) << 29;
+  int64_t S = (hb >> 31) ? -H : H;
+  if ((lb << 1) != 0) {
+    const int sh = el - eh + 29;  // lo's significand shift into those units (<= 5 for a normalised pair)
+    if (el == 0 || el == 255 || sh < 0 || sh > 5) return df_to_double(a);
+    const int64_t L = (int64_t)((1ull << 23) | (lb & 0x7fffffu)) << sh;
+    S += (lb >> 31) ? -L : L;
+  }
+  const uint64_t neg = S < 0 ? 1ull : 0ull;
+  uint64_t m = neg ? (uint64_t)(-S) : (uint64_t)S;
+  int e = eh - 127 + 1023;  // biased double exponent of 2^(Eh)
+  if (m >= (1ull << 53)) {  // one bit too many: drop it, ties to even
+    const uint64_t half = m >> 1;
+    m = half + ((m & 1ull) & (half & 1ull));
+    e += 1;
+    if (m >= (1ull << 53)) { m >>= 1; e += 1; }
+  } else if (m < (1ull << 52)) {  // |lo| <= 2^29 units: one step restores 53 bits, exactly
+    m <<= 1;
+    e -= 1;
+  }
+  return __longlong_as_double((long long)((neg << 63) | ((uint64_t)e << 52) | (m & ((1ull << 52) - 1))));
+}
 __device__ __forceinline__ float2 df_shfl_xor(float2 a, int o) {
   return make_float2(__shfl_xor_sync(0xffffffffu, a.x, o), __shfl_xor_sync(0xffffffffu, a.y, o));
 }

@@ -311,9 +311,9 @@ __global__ void k_reset(State *st, int max_it, int true_every, int method, doubl
 
 // Once per solve, before the residual: every cell's operator code (see
 // lap4_code), and x, b as double-float pairs on the fluid cells (zero
-// elsewhere; the operator never reads x off the fluid cells).  The only FP64
-// arithmetic of the solve besides the final write of x; cells whose value is
-// exactly zero skip it.
+// elsewhere; the operator never reads x off the fluid cells).  The
+// conversions use integer operations (df_from_double_bits); cells whose value
+// is exactly zero skip them.
 __global__ void __launch_bounds__(RT) k_prepare(Vecs V) {
   for (uint32_t g = gtid(); g < V.ngroups; g += gstride()) {
     uint32_t q; int i, j, k0;
@@ -337,8 +337,8 @@ __global__ void __launch_bounds__(RT) k_prepare(Vecs V) {
     for (int c = 0; c < 4; ++c) {
       const bool fl = !(cd[c] & kNotFluid);
       // zero tests on the bit patterns (integer ops), so zero cells cost no FP64 work
-      xd[c] = (fl && (__double_as_longlong(xq[c]) << 1)) ? df_from_double(xq[c]) : make_float2(0.f, 0.f);
-      bd[c] = (fl && (__double_as_longlong(bq[c]) << 1)) ? df_from_double(bq[c]) : make_float2(0.f, 0.f);
+      xd[c] = (fl && (__double_as_longlong(xq[c]) << 1)) ? df_from_double_bits(xq[c]) : make_float2(0.f, 0.f);
+      bd[c] = (fl && (__double_as_longlong(bq[c]) << 1)) ? df_from_double_bits(bq[c]) : make_float2(0.f, 0.f);
     }
     st4(V.xd + q, xd);
     st4(V.bd + q, bd);
@@ -399,7 +399,7 @@ __global__ void __launch_bounds__(RT) k_finalize(Vecs V) {
     ld4(V.xd + q, xd);
 #pragma unroll
     for (int c = 0; c < 4; ++c)
-      if (!(lane(cd, c) & kNotFluid)) V.x[q + c] = df_to_double(xd[c]);
+      if (!(lane(cd, c) & kNotFluid)) V.x[q + c] = df_to_double_bits(xd[c]);
   }
 }
 
