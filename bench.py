@@ -311,12 +311,7 @@ def run_ours(args, rank, world):
     x_h = torch.empty(scene.rhs.shape, dtype=torch.float64).pin_memory()
 
     def e2e_step():
-        solver.flags.copy_(flags_h, non_blocking=True)
-        solver.b.copy_(b_h, non_blocking=True)
-        img = flags_to_image(solver.flags)
-        solver.set_image(None, img)
-        solver.launch(None, use_graph=not args.no_graph)
-        x_h.copy_(solver.x, non_blocking=True)
+        solver.solve_host(flags_h, b_h, x_h, use_graph=not args.no_graph)
 
     for _ in range(2):
         e2e_step()

@@ -1,10 +1,12 @@
 """FusedSolver: npsd / npcg with the network preconditioner, entirely on the GPU.
 
 One CUDA graph per solver: a conditional WHILE node wraps one iteration
-(2n+1 fused preconditioner kernels, the orthogonalisation / SpMV / update
-kernels with FP64 reductions, an FP64 true residual every ``true_every``
-iterations, a one-thread control kernel).  ``solve`` is a single graph
-launch; the host synchronises only to read the result.
+(the fused preconditioner kernels, the orthogonalisation / SpMV / update
+kernels with FP64 cross-thread reductions, a double-float true residual every
+``true_every`` iterations, a one-thread control kernel).  ``solve`` is a
+single graph launch; the host synchronises only to read the result.
+``solve_host`` is the host-to-host form for a new frame, with the rhs
+transfer overlapped with the preconditioner set-up.
 
 The drop-in solvers of ``cg.py`` keep the reference's per-iteration host
 round trips (cg_tests.py:90,266); this is the form they are compared with.
@@ -67,6 +69,7 @@ class FusedSolver:
         self.b = torch.zeros(self.shape, dtype=torch.float64, device=dev)
         self.x = torch.zeros(self.shape, dtype=torch.float64, device=dev)
         call("mlpcg_solver_bind", h, _p(self.workspace), nbytes, _p(self.flags), _p(self.b), _p(self.x))
+        self._side = None
 
     def set_image(self, model, image: torch.Tensor, flags: torch.Tensor | None = None):
         """New frame: recompute the plan in place (the captured graph stays valid)."""
@@ -87,6 +90,27 @@ class FusedSolver:
         elif x0.data_ptr() != self.x.data_ptr():
             self.x.copy_(x0.reshape(self.shape))
         call("mlpcg_solver_solve", self._h, int(bool(use_graph)), _stream(self.flags.device))
+
+    def solve_host(self, flags_h: torch.Tensor, b_h: torch.Tensor, x_out_h: torch.Tensor | None = None,
+                   model=None, use_graph=True):
+        """A new frame from host memory: flags (uint8) and rhs (FP64) in, the solution into
+        ``x_out_h``.  The rhs is copied on a side stream while the image pyramid and the
+        coefficients are built from the flags, so its transfer hides behind the set-up.  With
+        pinned host buffers every copy is asynchronous; call ``result()`` to wait."""
+        dev = self.flags.device
+        main = torch.cuda.current_stream(dev)
+        if self._side is None:
+            self._side = torch.cuda.Stream(dev)
+        side = self._side
+        side.wait_stream(main)  # the previous solve has finished with self.b
+        with torch.cuda.stream(side):
+            self.b.copy_(b_h.reshape(self.shape), non_blocking=True)
+        self.flags.copy_(flags_h.reshape(self.shape), non_blocking=True)
+        self.set_image(model, flags_to_image(self.flags))
+        main.wait_stream(side)
+        self.launch(None, use_graph=use_graph)
+        if x_out_h is not None:
+            x_out_h.view(self.shape).copy_(self.x, non_blocking=True)
 
     def result(self, with_history=True) -> SolveResult:
         it, st, rel = C.c_int(), C.c_int(), C.c_double()

@@ -192,6 +192,28 @@ def test_fused_warm_start_and_off_fluid_values(cuda):
     assert rel_err(pert.x[fluid].cpu(), xc[fluid].cpu()) < 1e-4
 
 
+def test_solve_host_matches_device_solve(cuda):
+    """The host-to-host form (rhs copied on a side stream during the set-up) gives the device
+    solve's result, also for a new frame whose flags differ from the solver's current ones."""
+    from mlpcg_gb300.solver import FusedSolver, flags_to_image
+    s, flags, img = _scene((32, 32, 32), 5, cuda)
+    s2, flags2, img2 = _scene((32, 32, 32), 6, cuda)
+    m = _near_identity_model(3, cuda)
+    ref = FusedSolver(m, flags2.clone(), method="npsd", max_it=60, tol=1e-6)
+    r_ref = ref.solve(torch.as_tensor(s2.rhs, device=cuda))
+    x_ref = r_ref.x.cpu()
+    solver = FusedSolver(m, flags.clone(), method="npsd", max_it=60, tol=1e-6)
+    solver.solve(torch.as_tensor(s.rhs, device=cuda))
+    flags_h = torch.from_numpy(s2.flags).pin_memory()
+    b_h = torch.from_numpy(s2.rhs).pin_memory()
+    x_h = torch.empty(s2.rhs.shape, dtype=torch.float64).pin_memory()
+    solver.solve_host(flags_h, b_h, x_h)
+    r = solver.result()
+    torch.cuda.synchronize()
+    assert r.iterations == r_ref.iterations and r.status == r_ref.status
+    assert torch.equal(x_h, x_ref)
+
+
 def test_fused_graph_reuse_is_deterministic(cuda):
     from mlpcg_gb300.solver import FusedSolver
     s, flags, img = _scene((32, 32, 32), 7, cuda)
