@@ -336,6 +336,21 @@ int mlpcg_solver_result(const mlpcg_solver *solver, int *iterations, int *status
  * (convert_to_binary_images, lib/read_data.py:28-39). */
 int mlpcg_flags_to_image(const uint8_t *flags, float *image, int64_t n, void *stream);
 
+/* Fluid-DOF vectors: the values of the fluid cells in flat cell order, the
+ * compressed vectors the reference's solvers take and return (test.py:38-50,
+ * lib/read_data.py:110-165).  mlpcg_fluid_order fills `order` (device, uint32,
+ * mlpcg_fluid_order_entries(n) entries) from the flags; scatter writes a
+ * fluid-DOF vector of m values onto the grid (0 off the fluid cells), gather
+ * reads the grid's fluid cells into one; m is the vector's capacity (fluid
+ * cells beyond it are read as 0 / not written).  Recompute the order when the
+ * flags change. */
+size_t mlpcg_fluid_order_entries(int64_t n);
+int mlpcg_fluid_order(const uint8_t *flags, int64_t n, uint32_t *order, void *stream);
+int mlpcg_scatter_fluid(const double *fluid_values, int64_t m, const uint8_t *flags, const uint32_t *order,
+                        int64_t n, double *grid, void *stream);
+int mlpcg_gather_fluid(const double *grid, const uint8_t *flags, const uint32_t *order, int64_t n,
+                       double *fluid_values, int64_t m, void *stream);
+
 /* =========================================================================
  * Reductions
  * ========================================================================= */

@@ -40,6 +40,10 @@ int launch_linear_backward(const float *, const float *, float *, float *, cudaS
 int launch_linear_image_grad(const float *, const float *, float *, int, int, int, cudaStream_t);
 int launch_laplacian(const uint8_t *, const void *, void *, int, int, int, int, cudaStream_t);
 int launch_flags_to_image(const uint8_t *, float *, int64_t, cudaStream_t);
+int64_t fluid_blocks(int64_t n);
+int launch_fluid_order(const uint8_t *, int64_t, uint32_t *, cudaStream_t);
+int launch_scatter_fluid(const double *, int64_t, const uint8_t *, const uint32_t *, int64_t, double *, cudaStream_t);
+int launch_gather_fluid(const double *, const uint8_t *, const uint32_t *, int64_t, double *, int64_t, cudaStream_t);
 // launchers (blas.cu)
 size_t dot_workspace(int64_t);
 int launch_dot(const void *, const void *, int, int64_t, double *, void *, size_t, cudaStream_t);
@@ -297,6 +301,31 @@ int mlpcg_flags_to_image(const uint8_t *flags, float *image, int64_t n, void *st
   CHECK_PTR(flags); CHECK_PTR(image);
   MLPCG_REQUIRE(n >= 1, MLPCG_ERR_ARG, "flags_to_image: n must be >= 1");
   return launch_flags_to_image(flags, image, n, as_stream(stream));
+}
+
+size_t mlpcg_fluid_order_entries(int64_t n) { return n < 1 ? 0 : (size_t)(2 * fluid_blocks(n)); }
+
+int mlpcg_fluid_order(const uint8_t *flags, int64_t n, uint32_t *order, void *stream) {
+  clear_error();
+  CHECK_PTR(flags); CHECK_PTR(order);
+  MLPCG_REQUIRE(n >= 1, MLPCG_ERR_ARG, "fluid_order: n must be >= 1");
+  return launch_fluid_order(flags, n, order, as_stream(stream));
+}
+
+int mlpcg_scatter_fluid(const double *fluid_values, int64_t m, const uint8_t *flags, const uint32_t *order,
+                        int64_t n, double *grid, void *stream) {
+  clear_error();
+  CHECK_PTR(fluid_values); CHECK_PTR(flags); CHECK_PTR(order); CHECK_PTR(grid);
+  MLPCG_REQUIRE(n >= 1 && m >= 0, MLPCG_ERR_ARG, "scatter_fluid: need n >= 1 and m >= 0");
+  return launch_scatter_fluid(fluid_values, m, flags, order, n, grid, as_stream(stream));
+}
+
+int mlpcg_gather_fluid(const double *grid, const uint8_t *flags, const uint32_t *order, int64_t n,
+                       double *fluid_values, int64_t m, void *stream) {
+  clear_error();
+  CHECK_PTR(grid); CHECK_PTR(flags); CHECK_PTR(order); CHECK_PTR(fluid_values);
+  MLPCG_REQUIRE(n >= 1 && m >= 0, MLPCG_ERR_ARG, "gather_fluid: need n >= 1 and m >= 0");
+  return launch_gather_fluid(grid, flags, order, n, fluid_values, m, as_stream(stream));
 }
 
 size_t mlpcg_dot_workspace(int64_t n) { return dot_workspace(n < 1 ? 1 : n); }

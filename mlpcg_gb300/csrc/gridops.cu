@@ -359,6 +359,88 @@ __global__ void k_flags_to_image(const uint8_t *__restrict__ flags, float *__res
 }
 
 // ---------------------------------------------------------------------------
+// Fluid-DOF vectors: the values of the fluid cells in flat cell order (the
+// reference's compressed solver vectors).  Cells are taken in blocks of
+// kFluidBlock; block_base[b] = number of fluid cells before block b, and a
+// cell's position is its block's base plus its rank among the block's fluid
+// cells (recomputed by a block scan in each pass).
+// ---------------------------------------------------------------------------
+constexpr int kFluidThreads = 256, kFluidPer = 4, kFluidBlock = kFluidThreads * kFluidPer;
+
+// exclusive scan of one int per thread over a 256-thread block
+__device__ __forceinline__ int block256_excl_scan(int v, int &total) {
+  __shared__ int ws[kFluidThreads / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) ws[w] = x;
+  __syncthreads();
+  int off = 0, tot = 0;
+#pragma unroll
+  for (int i = 0; i < kFluidThreads / 32; ++i) {
+    if (i < w) off += ws[i];
+    tot += ws[i];
+  }
+  total = tot;
+  return off + x - v;
+}
+
+// fluid bits of the thread's kFluidPer cells
+__device__ __forceinline__ unsigned fluid_bits(const uint8_t *__restrict__ flags, int64_t n, int64_t q0) {
+  unsigned m = 0;
+#pragma unroll
+  for (int u = 0; u < kFluidPer; ++u)
+    if (q0 + u < n && flags[q0 + u] == MLPCG_FLUID) m |= 1u << u;
+  return m;
+}
+
+__global__ void __launch_bounds__(kFluidThreads)
+k_fluid_counts(const uint8_t *__restrict__ flags, int64_t n, uint32_t *__restrict__ cnt) {
+  const int64_t q0 = (int64_t)blockIdx.x * kFluidBlock + kFluidPer * threadIdx.x;
+  int tot;
+  block256_excl_scan(__popc(fluid_bits(flags, n, q0)), tot);
+  if (threadIdx.x == 0) cnt[blockIdx.x] = (uint32_t)tot;
+}
+
+// grid = the fluid values scattered to their cells, 0 elsewhere (and for
+// positions beyond the m values given)
+__global__ void __launch_bounds__(kFluidThreads)
+k_scatter_fluid(const double *__restrict__ vals, int64_t m, const uint8_t *__restrict__ flags,
+                const uint32_t *__restrict__ base, int64_t n, double *__restrict__ grid) {
+  const int64_t q0 = (int64_t)blockIdx.x * kFluidBlock + kFluidPer * threadIdx.x;
+  const unsigned fm = fluid_bits(flags, n, q0);
+  int tot;
+  int64_t pos = (int64_t)__ldg(base + blockIdx.x) + block256_excl_scan(__popc(fm), tot);
+#pragma unroll
+  for (int u = 0; u < kFluidPer; ++u)
+    if (q0 + u < n) {
+      const bool f = (fm >> u) & 1u;
+      grid[q0 + u] = (f && pos < m) ? vals[pos] : 0.0;
+      pos += f;
+    }
+}
+
+// vals = the grid's values on the fluid cells (the first m of them)
+__global__ void __launch_bounds__(kFluidThreads)
+k_gather_fluid(const double *__restrict__ grid, const uint8_t *__restrict__ flags,
+               const uint32_t *__restrict__ base, int64_t n, double *__restrict__ vals, int64_t m) {
+  const int64_t q0 = (int64_t)blockIdx.x * kFluidBlock + kFluidPer * threadIdx.x;
+  const unsigned fm = fluid_bits(flags, n, q0);
+  int tot;
+  int64_t pos = (int64_t)__ldg(base + blockIdx.x) + block256_excl_scan(__popc(fm), tot);
+#pragma unroll
+  for (int u = 0; u < kFluidPer; ++u)
+    if ((fm >> u) & 1u) {
+      if (pos < m) vals[pos] = grid[q0 + u];
+      ++pos;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
 int launch_flags_to_image(const uint8_t *flags, float *img, int64_t n, cudaStream_t st) {
@@ -373,6 +455,33 @@ int launch_flags_to_image(const uint8_t *flags, float *img, int64_t n, cudaStrea
     else if ((dt) == MLPCG_BF16) { using T = __nv_bfloat16; __VA_ARGS__; } \
     else { using T = double; __VA_ARGS__; }                             \
   } while (0)
+
+int launch_scan_u32(const uint32_t *cnt, uint32_t *base, int n, cudaStream_t st);  // precond.cu
+
+int64_t fluid_blocks(int64_t n) { return (n + kFluidBlock - 1) / kFluidBlock; }
+
+int launch_fluid_order(const uint8_t *flags, int64_t n, uint32_t *base, cudaStream_t st) {
+  const int64_t nb = fluid_blocks(n);
+  MLPCG_REQUIRE(nb < (1ll << 31), MLPCG_ERR_SHAPE, "fluid_order: too many cells");
+  uint32_t *cnt = base + nb;  // second half of the caller's array
+  k_fluid_counts<<<(unsigned)nb, kFluidThreads, 0, st>>>(flags, n, cnt);
+  MLPCG_LAUNCH_CHECK();
+  return launch_scan_u32(cnt, base, (int)nb, st);
+}
+
+int launch_scatter_fluid(const double *vals, int64_t m, const uint8_t *flags, const uint32_t *base, int64_t n,
+                         double *grid, cudaStream_t st) {
+  k_scatter_fluid<<<(unsigned)fluid_blocks(n), kFluidThreads, 0, st>>>(vals, m, flags, base, n, grid);
+  MLPCG_LAUNCH_CHECK();
+  return MLPCG_OK;
+}
+
+int launch_gather_fluid(const double *grid, const uint8_t *flags, const uint32_t *base, int64_t n, double *vals,
+                        int64_t m, cudaStream_t st) {
+  k_gather_fluid<<<(unsigned)fluid_blocks(n), kFluidThreads, 0, st>>>(grid, flags, base, n, vals, m);
+  MLPCG_LAUNCH_CHECK();
+  return MLPCG_OK;
+}
 
 int launch_avg_pool2(const void *x, void *y, int dt, int B, int n1, int n2, int n3, cudaStream_t st) {
   dim3 grid(blocks_for(cells(n1 / 2, n2 / 2, n3 / 2), 256), B);

@@ -1186,6 +1186,15 @@ static CoefArgs<KT> coef_args(const PrecondPlan &P, int l, void *K, float *uni) 
   return C;
 }
 
+namespace mlpcg {
+// exclusive prefix sum of n uint32 counts (one CTA)
+int launch_scan_u32(const uint32_t *cnt, uint32_t *base, int n, cudaStream_t st) {
+  k_scan_tiles<<<1, 1024, 0, st>>>(cnt, base, n);
+  MLPCG_LAUNCH_CHECK();
+  return MLPCG_OK;
+}
+}  // namespace mlpcg
+
 // Stages of one application, in launch order: 0..L-1 = pre-block of level s,
 // L = coarsest block, L+1..2L = post-block of level 2L-s.  [s0, s1] selects a range.
 template <typename KT, typename AT>

@@ -69,7 +69,7 @@ class FusedSolver:
         self.b = torch.zeros(self.shape, dtype=torch.float64, device=dev)
         self.x = torch.zeros(self.shape, dtype=torch.float64, device=dev)
         call("mlpcg_solver_bind", h, _p(self.workspace), nbytes, _p(self.flags), _p(self.b), _p(self.x))
-        self._side = None
+        self._side = self._order = self._bf = self._xf = None
 
     def set_image(self, model, image: torch.Tensor, flags: torch.Tensor | None = None):
         """New frame: recompute the plan in place (the captured graph stays valid)."""
@@ -94,23 +94,47 @@ class FusedSolver:
     def solve_host(self, flags_h: torch.Tensor, b_h: torch.Tensor, x_out_h: torch.Tensor | None = None,
                    model=None, use_graph=True):
         """A new frame from host memory: flags (uint8) and rhs (FP64) in, the solution into
-        ``x_out_h``.  The rhs is copied on a side stream while the image pyramid and the
-        coefficients are built from the flags, so its transfer hides behind the set-up.  With
+        ``x_out_h``.  ``b_h`` and ``x_out_h`` are either full grids (N1*N2*N3 values) or fluid-DOF
+        vectors -- one value per fluid cell of ``flags_h`` in flat cell order, the compressed vectors
+        the reference's solvers take -- told apart by their size; fluid-DOF vectors move only the
+        fluid values over the host link.  The rhs is copied on a side stream while the image pyramid
+        and the coefficients are built from the flags, so its transfer hides behind the set-up.  With
         pinned host buffers every copy is asynchronous; call ``result()`` to wait."""
         dev = self.flags.device
+        n = self.b.numel()
+        fluid = b_h.numel() != n
+        if fluid and x_out_h is not None and x_out_h.numel() != b_h.numel():
+            raise ValueError("x_out_h must have the length of b_h")
         main = torch.cuda.current_stream(dev)
         if self._side is None:
             self._side = torch.cuda.Stream(dev)
+            self._order = torch.empty(int(self._lib.mlpcg_fluid_order_entries(n)), dtype=torch.int32, device=dev)
         side = self._side
-        side.wait_stream(main)  # the previous solve has finished with self.b
+        m = b_h.numel()
+        if fluid and (self._bf is None or self._bf.numel() < m):
+            self._bf = torch.empty(max(m, 1), dtype=torch.float64, device=dev)
+            self._xf = torch.empty(max(m, 1), dtype=torch.float64, device=dev)
+        side.wait_stream(main)  # the previous solve has finished with these buffers
         with torch.cuda.stream(side):
-            self.b.copy_(b_h.reshape(self.shape), non_blocking=True)
+            if fluid:
+                self._bf[:m].copy_(b_h.reshape(-1), non_blocking=True)
+            else:
+                self.b.copy_(b_h.reshape(self.shape), non_blocking=True)
         self.flags.copy_(flags_h.reshape(self.shape), non_blocking=True)
+        st = _stream(dev)
+        if fluid:
+            call("mlpcg_fluid_order", _p(self.flags), n, _p(self._order), st)
         self.set_image(model, flags_to_image(self.flags))
         main.wait_stream(side)
+        if fluid:
+            call("mlpcg_scatter_fluid", _p(self._bf), m, _p(self.flags), _p(self._order), n, _p(self.b), st)
         self.launch(None, use_graph=use_graph)
         if x_out_h is not None:
-            x_out_h.view(self.shape).copy_(self.x, non_blocking=True)
+            if fluid:
+                call("mlpcg_gather_fluid", _p(self.x), _p(self.flags), _p(self._order), n, _p(self._xf), m, st)
+                x_out_h.view(-1).copy_(self._xf[:m], non_blocking=True)
+            else:
+                x_out_h.view(self.shape).copy_(self.x, non_blocking=True)
 
     def result(self, with_history=True) -> SolveResult:
         it, st, rel = C.c_int(), C.c_int(), C.c_double()

@@ -214,6 +214,58 @@ def test_solve_host_matches_device_solve(cuda):
     assert torch.equal(x_h, x_ref)
 
 
+@pytest.mark.parametrize("shape", [(16, 16, 16), (7, 13, 29), (64, 64, 64)])
+def test_fluid_vectors_scatter_gather(cuda, shape):
+    """Fluid-DOF order, scatter and gather against torch indexing of the fluid cells (flat order),
+    including a capacity shorter than the fluid count."""
+    from mlpcg_gb300._lib import call, load
+    from mlpcg_gb300.ops import _p, _stream
+    g = torch.Generator(device=cuda).manual_seed(11)
+    flags = torch.randint(0, 4, shape, generator=g, device=cuda, dtype=torch.uint8)
+    n = flags.numel()
+    fluid = torch.nonzero(flags.view(-1) == 2).view(-1)
+    m = fluid.numel()
+    order = torch.empty(int(load().mlpcg_fluid_order_entries(n)), dtype=torch.int32, device=cuda)
+    st = _stream(flags.device)
+    call("mlpcg_fluid_order", _p(flags), n, _p(order), st)
+    vals = torch.randn(m, dtype=torch.float64, device=cuda, generator=g)
+    grid = torch.full((n,), 5.0, dtype=torch.float64, device=cuda)
+    call("mlpcg_scatter_fluid", _p(vals), m, _p(flags), _p(order), n, _p(grid), st)
+    ref = torch.zeros(n, dtype=torch.float64, device=cuda)
+    ref[fluid] = vals
+    assert torch.equal(grid, ref)
+    src = torch.randn(n, dtype=torch.float64, device=cuda, generator=g)
+    out = torch.full((m + 3,), 9.0, dtype=torch.float64, device=cuda)
+    call("mlpcg_gather_fluid", _p(src), _p(flags), _p(order), n, _p(out), m, st)
+    assert torch.equal(out[:m], src[fluid]) and torch.all(out[m:] == 9.0)
+    k = m // 2  # a short vector: the cells beyond it read as 0 / are not written
+    call("mlpcg_scatter_fluid", _p(vals), k, _p(flags), _p(order), n, _p(grid), st)
+    ref2 = torch.zeros(n, dtype=torch.float64, device=cuda)
+    ref2[fluid[:k]] = vals[:k]
+    assert torch.equal(grid, ref2)
+    out.fill_(9.0)
+    call("mlpcg_gather_fluid", _p(src), _p(flags), _p(order), n, _p(out), k, st)
+    assert torch.equal(out[:k], src[fluid[:k]]) and torch.all(out[k:] == 9.0)
+
+
+def test_solve_host_fluid_vectors(cuda):
+    """solve_host with fluid-DOF vectors (the reference's compressed rhs / solution) equals the
+    grid solve on the fluid cells."""
+    from mlpcg_gb300.solver import FusedSolver
+    s, flags, img = _scene((32, 32, 32), 6, cuda)
+    m = _near_identity_model(3, cuda)
+    solver = FusedSolver(m, flags.clone(), method="npsd", max_it=60, tol=1e-6)
+    ref = solver.solve(torch.as_tensor(s.rhs, device=cuda))
+    fl = s.flags.reshape(-1) == 2
+    x_ref = ref.x.cpu().reshape(-1)[torch.from_numpy(fl)]
+    b_h = torch.from_numpy(np.ascontiguousarray(s.rhs.reshape(-1)[fl])).pin_memory()
+    x_h = torch.empty(b_h.numel(), dtype=torch.float64).pin_memory()
+    solver.solve_host(torch.from_numpy(s.flags).pin_memory(), b_h, x_h)
+    r = solver.result()
+    torch.cuda.synchronize()
+    assert r.iterations == ref.iterations and torch.equal(x_h, x_ref)
+
+
 def test_fused_graph_reuse_is_deterministic(cuda):
     from mlpcg_gb300.solver import FusedSolver
     s, flags, img = _scene((32, 32, 32), 7, cuda)
