@@ -15,12 +15,13 @@ What it imports from the reference, unmodified:
   the reference's own module tree, initialisation order and orchestration
   (forward / eval_forward) run on the CPU;
 * model.py          -- BaseModel.reset_parameters;
-* lib/discrete_laplacian.py, lib/read_data.py -- lap_with_bc, compressedMat,
-  convert_to_binary_images;
+* lib/discrete_laplacian.py, lib/read_data.py, lib/write_data.py -- lap_with_bc,
+  compressedMat, convert_to_binary_images, the file readers and writers;
 * cg_tests.py       -- npcg, npcg_flex, npsd (cupy / AMGCL imports stubbed,
   torch.cuda.synchronize made a no-op).
 
-Outputs (FP64 unless noted): ops_*.npz, model_*.npz, laplacian_*.npz, cg_*.npz.
+Outputs (FP64 unless noted): ops_*.npz, model_*.npz, laplacian_*.npz, cg_*.npz, and
+scene_8/ (simulator-format files) with scene_files_8.npz (what the reference reads from them).
 The scenes come from mlpcg_gb300.scenes (seeded), stored in the fixtures.
 """
 from __future__ import annotations
@@ -255,9 +256,42 @@ def make_cg(ref_cg, model, scene, max_it=30):
     return out
 
 
-def main(ref_root: str):
+def make_scene_files(ref_lap, ref_read, shape, seed, frame=1):
+    """A small scene as the reference's simulator files: the matrix and the rhs written by the
+    reference's own writers (lib/write_data.py), the flags in the C++ Serialize layout that
+    lib/read_data.py documents (size_t count + int32); the expected arrays are what the
+    reference's readers return for them."""
+    import struct
+    import write_data as ref_write
+    scene = make_scene(shape, seed)
+    f = scene.flags
+    n = f.shape[0]
+    idx = lambda code: [tuple(int(c) for c in t) for t in np.argwhere(f == code)]
+    A_full = ref_lap.lap_with_bc(n, 3, solid=idx(1), air=idx(3), bd=idx(0), bd_padding=True, dtype=np.float64)
+    d = HERE / f"scene_{n}"
+    d.mkdir(exist_ok=True)
+    with open(d / f"flags_{frame}.bin", "wb") as out:
+        out.write(struct.pack("N", f.size))
+        out.write(struct.pack(f"{f.size}i", *[int(v) for v in f.ravel()]))
+    ref_write.writeA_sparse(A_full.tocsr(), str(d / f"A_{frame}.bin"))
+    ref_write.write_bin_file_from_nparray(str(d / f"div_v_star_{frame}.bin"), scene.rhs.ravel().astype(np.float64))
+    flags = ref_read.read_flags(str(d / f"flags_{frame}.bin"))
+    A = ref_read.readA_sparse(str(d / f"A_{frame}.bin"))
+    Ac = ref_read.compressedMat(A, flags).tocsr()
+    Ac.sort_indices()
+    rhs = ref_read.load_vector(str(d / f"div_v_star_{frame}.bin"))
+    return {"flags": flags, "A_indptr": A.indptr, "A_indices": A.indices, "A_data": A.data,
+            "Ac_indptr": Ac.indptr, "Ac_indices": Ac.indices, "Ac_data": Ac.data, "rhs": rhs,
+            "rhs_fluid": ref_read.compressedVec(rhs, flags)}
+
+
+def main(ref_root: str, only: str | None = None):
     ref = Path(ref_root)
     ref_model, ref_py, ref_lap, ref_read, ref_cg = _import_reference(ref)
+    if only == "scene_files":
+        np.savez_compressed(HERE / "scene_files_8.npz", **make_scene_files(ref_lap, ref_read, (8, 8, 8), 4))
+        print("scene files written to", HERE)
+        return
     torch.set_default_dtype(torch.float32)
     for shape, seed in (((8, 8, 8), 0), ((6, 4, 10), 1), ((16, 16, 16), 2)):
         out = make_ops(ref_py, shape, seed)
@@ -273,8 +307,12 @@ def main(ref_root: str):
                             **{k: v.detach().numpy() for k, v in m.state_dict().items()})
     np.savez_compressed(HERE / "laplacian_12.npz", **make_laplacian(ref_lap, ref_read, (12, 12, 12), 5))
     np.savez_compressed(HERE / "cg_16_l3.npz", **make_cg(ref_cg, model, scene))
+    np.savez_compressed(HERE / "scene_files_8.npz", **make_scene_files(ref_lap, ref_read, (8, 8, 8), 4))
     print("fixtures written to", HERE)
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    # python make_golden.py [reference root] [--only scene_files]
+    args = [a for a in sys.argv[1:] if not a.startswith("--only")]
+    only = next((a.split("=", 1)[1] for a in sys.argv[1:] if a.startswith("--only=")), None)
+    main(args[0] if args else "/root/reference", only)
