@@ -332,6 +332,20 @@ int mlpcg_solver_solve(mlpcg_solver *solver, int use_graph, void *stream);
 int mlpcg_solver_result(const mlpcg_solver *solver, int *iterations, int *status, double *rel_res,
                         double *history, void *stream);
 
+/* Many systems in one launch (no counterpart in the reference, whose solver
+ * takes one system at a time): `count` (<= 64) bound solvers, each with its
+ * own grid size, plan, method, tolerance and max_it, solved together by one
+ * graph launch whose conditional WHILE node runs while any system is running;
+ * inside an iteration every system's kernels form a parallel branch and
+ * return at once for a system that has stopped (per-system convergence
+ * masks).  Each system's result is read with mlpcg_solver_result.  The graph
+ * is built on the first mlpcg_batch_solve; a solver must not be rebound while
+ * it belongs to a batch. */
+typedef struct mlpcg_batch mlpcg_batch;
+int mlpcg_batch_create(mlpcg_solver *const *solvers, int count, mlpcg_batch **out);
+int mlpcg_batch_solve(mlpcg_batch *batch, void *stream);
+void mlpcg_batch_destroy(mlpcg_batch *batch);
+
 /* Image channels [air, fluid, non-solid] (F32, 3 x N) from cell flags
  * (convert_to_binary_images, lib/read_data.py:28-39). */
 int mlpcg_flags_to_image(const uint8_t *flags, float *image, int64_t n, void *stream);

@@ -57,6 +57,9 @@ _PROTOS = {
     "mlpcg_solver_bind": (_i, [_vp, _vp, _sz, _u8p, _vp, _vp]),
     "mlpcg_solver_solve": (_i, [_vp, _i, _vp]),
     "mlpcg_solver_result": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "mlpcg_batch_create": (_i, [_vp, _i, _vp]),
+    "mlpcg_batch_solve": (_i, [_vp, _vp]),
+    "mlpcg_batch_destroy": (None, [_vp]),
     "mlpcg_flags_to_image": (_i, [_u8p, _fp, _i64, _vp]),
     "mlpcg_fluid_order_entries": (_sz, [_i64]),
     "mlpcg_fluid_order": (_i, [_u8p, _i64, _vp, _vp]),

@@ -696,7 +696,8 @@ template <typename KT, typename XT, typename YT, bool POOL, bool CLS>
 __global__ void __launch_bounds__(PT)
 k_pre_fused(const CoefArgs<KT> C, const XT *__restrict__ x,
             const float *__restrict__ xscale, YT *__restrict__ y, YT *__restrict__ ypool,
-            const uint8_t *__restrict__ mask, int n1, int n2, int n3) {
+            const uint8_t *__restrict__ mask, int n1, int n2, int n3, const int *__restrict__ gate) {
+  if (gate && *gate != 0) return;  // batched solves: this system has stopped
   __shared__ __align__(16) float S[HX][HY][HZP];
   __shared__ typename std::conditional<CLS, ClsSmem, int>::type smc_raw;
   ClsSmem *smc = CLS ? reinterpret_cast<ClsSmem *>(&smc_raw) : nullptr;
@@ -825,7 +826,8 @@ __device__ __forceinline__ void stage_coarse(float (*Cs)[CY][CZP], const CT *__r
 template <typename CT, typename YT, typename UT, bool SWAP>
 __global__ void __launch_bounds__(PT)
 k_up_fine(const CT *__restrict__ xc, const YT *__restrict__ yl, const float *__restrict__ c0p,
-          const float *__restrict__ c1p, UT *__restrict__ u, int n1, int n2, int n3) {
+          const float *__restrict__ c1p, UT *__restrict__ u, int n1, int n2, int n3, const int *__restrict__ gate) {
+  if (gate && *gate != 0) return;
   __shared__ __align__(16) float Cs[CX][CY][CZP];
   const int m1 = n1 / 2, m2 = n2 / 2, m3 = n3 / 2;
   const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY, x0 = blockIdx.z * TX;
@@ -900,7 +902,9 @@ template <typename KT, typename CT, typename YT, typename OT, bool SWAP, bool CL
 __global__ void __launch_bounds__(PT)
 k_post_fused(const CoefArgs<KT> C, const CT *__restrict__ xc, const YT *__restrict__ yl,
              const float *__restrict__ c0p, const float *__restrict__ c1p, OT *__restrict__ out,
-             const uint8_t *__restrict__ bmask, const uint8_t *__restrict__ omask, int n1, int n2, int n3) {
+             const uint8_t *__restrict__ bmask, const uint8_t *__restrict__ omask, int n1, int n2, int n3,
+             const int *__restrict__ gate) {
+  if (gate && *gate != 0) return;
   __shared__ __align__(16) float S[HX][HY][HZP];
   __shared__ __align__(16) typename std::conditional<UPIN, int, float[CX][CY][CZP]>::type cs_raw;
   __shared__ typename std::conditional<CLS, ClsSmem, int>::type smc_raw;
@@ -1199,7 +1203,7 @@ int launch_scan_u32(const uint32_t *cnt, uint32_t *base, int n, cudaStream_t st)
 // L = coarsest block, L+1..2L = post-block of level 2L-s.  [s0, s1] selects a range.
 template <typename KT, typename AT>
 static int run_apply(const PrecondPlan &P, const float *r, const float *rscale, float *z, void *tmp0,
-                     cudaStream_t st, int s0 = 0, int s1 = 1 << 20) {
+                     cudaStream_t st, int s0 = 0, int s1 = 1 << 20, const int *gate = nullptr) {
   const int L = P.L;
   const uint8_t *m0 = P.mask ? P.fmask : nullptr;
   // ---- down sweep
@@ -1211,17 +1215,17 @@ static int run_apply(const PrecondPlan &P, const float *r, const float *rscale, 
       if (l == 0) {
         if (v.cls)
           k_pre_fused<KT, float, AT, true, true><<<grid_of(v), PT, 0, st>>>(
-              C, r, rscale, (AT *)P.y[0], (AT *)P.xin[1], m0, v.n1, v.n2, v.n3);
+              C, r, rscale, (AT *)P.y[0], (AT *)P.xin[1], m0, v.n1, v.n2, v.n3, gate);
         else
           k_pre_fused<KT, float, AT, true, false><<<grid_of(v), PT, 0, st>>>(
-              C, r, rscale, (AT *)P.y[0], (AT *)P.xin[1], m0, v.n1, v.n2, v.n3);
+              C, r, rscale, (AT *)P.y[0], (AT *)P.xin[1], m0, v.n1, v.n2, v.n3, gate);
       } else {
         if (v.cls)
           k_pre_fused<KT, AT, AT, true, true><<<grid_of(v), PT, 0, st>>>(
-              C, (const AT *)P.xin[l], nullptr, (AT *)P.y[l], (AT *)P.xin[l + 1], nullptr, v.n1, v.n2, v.n3);
+              C, (const AT *)P.xin[l], nullptr, (AT *)P.y[l], (AT *)P.xin[l + 1], nullptr, v.n1, v.n2, v.n3, gate);
         else
           k_pre_fused<KT, AT, AT, true, false><<<grid_of(v), PT, 0, st>>>(
-              C, (const AT *)P.xin[l], nullptr, (AT *)P.y[l], (AT *)P.xin[l + 1], nullptr, v.n1, v.n2, v.n3);
+              C, (const AT *)P.xin[l], nullptr, (AT *)P.y[l], (AT *)P.xin[l + 1], nullptr, v.n1, v.n2, v.n3, gate);
       }
       MLPCG_LAUNCH_CHECK();
     } else {
@@ -1247,10 +1251,10 @@ static int run_apply(const PrecondPlan &P, const float *r, const float *rscale, 
       const CoefArgs<KT> C = coef_args<KT>(P, L, P.Kl, v.cls ? P.Ul : nullptr);
       if (v.cls)
         k_pre_fused<KT, AT, AT, false, true><<<grid_of(v), PT, 0, st>>>(
-            C, (const AT *)P.xin[L], nullptr, (AT *)P.xout[L], nullptr, nullptr, v.n1, v.n2, v.n3);
+            C, (const AT *)P.xin[L], nullptr, (AT *)P.xout[L], nullptr, nullptr, v.n1, v.n2, v.n3, gate);
       else
         k_pre_fused<KT, AT, AT, false, false><<<grid_of(v), PT, 0, st>>>(
-            C, (const AT *)P.xin[L], nullptr, (AT *)P.xout[L], nullptr, nullptr, v.n1, v.n2, v.n3);
+            C, (const AT *)P.xin[L], nullptr, (AT *)P.xout[L], nullptr, nullptr, v.n1, v.n2, v.n3, gate);
       MLPCG_LAUNCH_CHECK();
     } else {
       RET_IF(launch_stencil_apply(P.Kl, P.kdt, v.ps, P.xin[L], P.adt, 0, P.xout[L], P.adt, 1, v.n1, v.n2, v.n3, 0, st));
@@ -1271,24 +1275,24 @@ static int run_apply(const PrecondPlan &P, const float *r, const float *rscale, 
         // the finest level: prolongation as its own pass, then the block on u
         AT *u = (AT *)P.ufine;
         if (P.swap) {
-          k_up_fine<AT, AT, AT, true><<<g, PT, 0, st>>>(xc, yl, c0, c1, u, v.n1, v.n2, v.n3);
+          k_up_fine<AT, AT, AT, true><<<g, PT, 0, st>>>(xc, yl, c0, c1, u, v.n1, v.n2, v.n3, gate);
           MLPCG_LAUNCH_CHECK();
-          if (v.cls) k_post_fused<KT, AT, AT, float, true, true, true><<<g, PT, 0, st>>>(C, u, yl, c0, c1, z, bm, om, v.n1, v.n2, v.n3);
-          else k_post_fused<KT, AT, AT, float, true, false, true><<<g, PT, 0, st>>>(C, u, yl, c0, c1, z, bm, om, v.n1, v.n2, v.n3);
+          if (v.cls) k_post_fused<KT, AT, AT, float, true, true, true><<<g, PT, 0, st>>>(C, u, yl, c0, c1, z, bm, om, v.n1, v.n2, v.n3, gate);
+          else k_post_fused<KT, AT, AT, float, true, false, true><<<g, PT, 0, st>>>(C, u, yl, c0, c1, z, bm, om, v.n1, v.n2, v.n3, gate);
         } else {
-          k_up_fine<AT, AT, AT, false><<<g, PT, 0, st>>>(xc, yl, c0, c1, u, v.n1, v.n2, v.n3);
+          k_up_fine<AT, AT, AT, false><<<g, PT, 0, st>>>(xc, yl, c0, c1, u, v.n1, v.n2, v.n3, gate);
           MLPCG_LAUNCH_CHECK();
-          if (v.cls) k_post_fused<KT, AT, AT, float, false, true, true><<<g, PT, 0, st>>>(C, u, yl, c0, c1, z, bm, om, v.n1, v.n2, v.n3);
-          else k_post_fused<KT, AT, AT, float, false, false, true><<<g, PT, 0, st>>>(C, u, yl, c0, c1, z, bm, om, v.n1, v.n2, v.n3);
+          if (v.cls) k_post_fused<KT, AT, AT, float, false, true, true><<<g, PT, 0, st>>>(C, u, yl, c0, c1, z, bm, om, v.n1, v.n2, v.n3, gate);
+          else k_post_fused<KT, AT, AT, float, false, false, true><<<g, PT, 0, st>>>(C, u, yl, c0, c1, z, bm, om, v.n1, v.n2, v.n3, gate);
         }
       } else {
         AT *o = (AT *)P.xout[l];
         if (P.swap) {
-          if (v.cls) k_post_fused<KT, AT, AT, AT, true, true, false><<<g, PT, 0, st>>>(C, xc, yl, c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3);
-          else k_post_fused<KT, AT, AT, AT, true, false, false><<<g, PT, 0, st>>>(C, xc, yl, c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3);
+          if (v.cls) k_post_fused<KT, AT, AT, AT, true, true, false><<<g, PT, 0, st>>>(C, xc, yl, c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3, gate);
+          else k_post_fused<KT, AT, AT, AT, true, false, false><<<g, PT, 0, st>>>(C, xc, yl, c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3, gate);
         } else {
-          if (v.cls) k_post_fused<KT, AT, AT, AT, false, true, false><<<g, PT, 0, st>>>(C, xc, yl, c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3);
-          else k_post_fused<KT, AT, AT, AT, false, false, false><<<g, PT, 0, st>>>(C, xc, yl, c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3);
+          if (v.cls) k_post_fused<KT, AT, AT, AT, false, true, false><<<g, PT, 0, st>>>(C, xc, yl, c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3, gate);
+          else k_post_fused<KT, AT, AT, AT, false, false, false><<<g, PT, 0, st>>>(C, xc, yl, c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3, gate);
         }
       }
       MLPCG_LAUNCH_CHECK();
@@ -1329,6 +1333,24 @@ static int run_apply(const PrecondPlan &P, const float *r, const float *rscale, 
   }
   return MLPCG_OK;
 }
+
+namespace mlpcg {
+// mlpcg_precond_apply whose fused kernels return at once while *gate != 0
+// (the batched solver passes each system's status word)
+int precond_apply_gated(const mlpcg_precond *h, const float *r, const float *r_scale, float *z, const int *gate,
+                        void *stream) {
+  const PrecondPlan &P = h->p;
+  cudaStream_t st = as_stream(stream);
+  void *tmp0 = (char *)P.scratch + al256(96 * sizeof(float));
+  if (P.kdt == MLPCG_BF16 && P.adt == MLPCG_BF16)
+    return run_apply<__nv_bfloat16, __nv_bfloat16>(P, r, r_scale, z, tmp0, st, 0, 1 << 20, gate);
+  if (P.kdt == MLPCG_BF16 && P.adt == MLPCG_F32)
+    return run_apply<__nv_bfloat16, float>(P, r, r_scale, z, tmp0, st, 0, 1 << 20, gate);
+  if (P.kdt == MLPCG_F32 && P.adt == MLPCG_BF16)
+    return run_apply<float, __nv_bfloat16>(P, r, r_scale, z, tmp0, st, 0, 1 << 20, gate);
+  return run_apply<float, float>(P, r, r_scale, z, tmp0, st, 0, 1 << 20, gate);
+}
+}  // namespace mlpcg
 
 extern "C" {
 

@@ -27,7 +27,9 @@
 #include "common.cuh"
 
 struct mlpcg_precond;
-extern "C" int mlpcg_precond_apply(const mlpcg_precond *, const float *, const float *, float *, void *);
+namespace mlpcg {
+int precond_apply_gated(const mlpcg_precond *, const float *, const float *, float *, const int *, void *);
+}
 
 namespace mlpcg {
 
@@ -709,6 +711,20 @@ __global__ void k_control(Vecs V, cudaGraphConditionalHandle handle, int use_han
   if (use_handle) cudaGraphSetConditional(handle, S.status == ST_RUNNING ? 1u : 0u);
 }
 
+// Batched solves: one loop for many systems.  Each system's control kernel
+// updates its own state; this one keeps the loop running while any runs.
+constexpr int kMaxBatch = 64;
+struct BatchStates {
+  State *st[kMaxBatch];
+  int count;
+};
+__global__ void k_batch_control(BatchStates B, cudaGraphConditionalHandle handle) {
+  const int t = threadIdx.x;
+  const int running = (t < B.count && B.st[t]->status == ST_RUNNING) ? 1 : 0;
+  const int any = __syncthreads_or(running);
+  if (t == 0) cudaGraphSetConditional(handle, any ? 1u : 0u);
+}
+
 }  // namespace mlpcg
 
 using namespace mlpcg;
@@ -723,6 +739,16 @@ struct mlpcg_solver {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   cudaStream_t capture_stream = nullptr;  // graphs are captured here, launched on the caller's stream
+};
+
+struct mlpcg_batch {
+  std::vector<mlpcg_solver *> solvers;
+  std::vector<cudaStream_t> streams;   // one per system: the graph's parallel branches
+  std::vector<cudaEvent_t> joins;
+  cudaEvent_t fork = nullptr;
+  cudaStream_t capture_stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
 };
 
 static size_t al256s(size_t b) { return (b + 255) / 256 * 256; }
@@ -768,12 +794,23 @@ static void destroy_graph(mlpcg_solver *s) {
   s->graph = nullptr;
 }
 
+// state reset, operator codes, b and x0 as pairs, the initial residual
+static int start_solve(mlpcg_solver *s, cudaStream_t st) {
+  Vecs &V = s->V;
+  k_reset<<<1, 32, 0, st>>>(V.st, s->max_it, s->true_every, s->method, s->tol);
+  k_prepare<<<(unsigned)V.nblk, RT, 0, st>>>(V);
+  k_init<<<(unsigned)V.nblk, RT, 0, st>>>(V);
+  MLPCG_LAUNCH_CHECK();
+  return MLPCG_OK;
+}
+
 static int enqueue_body(mlpcg_solver *s, cudaStream_t st, cudaGraphConditionalHandle h, int use_handle) {
   Vecs &V = s->V;
   const unsigned nb = (unsigned)V.nblk;
   State *S = V.st;
-  // z = M (r / ||r||): the scale is read from the device state
-  int rc = mlpcg_precond_apply(s->plan, V.r, &S->rscale, V.z, st);
+  // z = M (r / ||r||): the scale is read from the device state; the kernels
+  // return at once once this system has stopped (its status word is nonzero)
+  int rc = precond_apply_gated(s->plan, V.r, &S->rscale, V.z, &S->status, st);
   if (rc) return rc;
   if (s->method == M_NPSD) {
     k_sd_dots<<<nb, RT, 0, st>>>(V);
@@ -851,10 +888,7 @@ int mlpcg_solver_solve(mlpcg_solver *s, int use_graph, void *stream) {
   MLPCG_REQUIRE(s && s->bound, MLPCG_ERR_ARG, "solver_solve: solver not bound");
   cudaStream_t st = as_stream(stream);
   Vecs &V = s->V;
-  k_reset<<<1, 32, 0, st>>>(V.st, s->max_it, s->true_every, s->method, s->tol);
-  k_prepare<<<(unsigned)V.nblk, RT, 0, st>>>(V);
-  k_init<<<(unsigned)V.nblk, RT, 0, st>>>(V);
-  MLPCG_LAUNCH_CHECK();
+  if (int rc0 = start_solve(s, st)) return rc0;
   if (!use_graph) {
     for (int it = 0; it < s->max_it; ++it) {
       int status = 0;
@@ -913,6 +947,104 @@ int mlpcg_solver_result(const mlpcg_solver *s, int *iters, int *status, double *
   if (iters) *iters = S.it;
   if (status) *status = S.status;
   if (rel_res) *rel_res = S.rel;
+  return MLPCG_OK;
+}
+
+int mlpcg_batch_create(mlpcg_solver *const *solvers, int count, mlpcg_batch **out) {
+  clear_error();
+  MLPCG_REQUIRE(out && solvers, MLPCG_ERR_ARG, "batch_create: NULL argument");
+  *out = nullptr;
+  MLPCG_REQUIRE(count >= 1 && count <= kMaxBatch, MLPCG_ERR_ARG, "batch_create: count %d out of [1, %d]", count,
+                kMaxBatch);
+  for (int i = 0; i < count; ++i) {
+    MLPCG_REQUIRE(solvers[i] && solvers[i]->bound, MLPCG_ERR_ARG, "batch_create: solver %d is NULL or not bound", i);
+    for (int j = 0; j < i; ++j)
+      MLPCG_REQUIRE(solvers[j] != solvers[i], MLPCG_ERR_ARG, "batch_create: solver %d appears twice", i);
+  }
+  auto *b = new mlpcg_batch();
+  b->solvers.assign(solvers, solvers + count);
+  *out = b;
+  return MLPCG_OK;
+}
+
+static void destroy_batch_graph(mlpcg_batch *b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->exec = nullptr;
+  b->graph = nullptr;
+}
+
+void mlpcg_batch_destroy(mlpcg_batch *b) {
+  if (!b) return;
+  destroy_batch_graph(b);
+  for (auto st : b->streams) cudaStreamDestroy(st);
+  for (auto e : b->joins) cudaEventDestroy(e);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->capture_stream) cudaStreamDestroy(b->capture_stream);
+  delete b;
+}
+
+int mlpcg_batch_solve(mlpcg_batch *b, void *stream) {
+  clear_error();
+  MLPCG_REQUIRE(b, MLPCG_ERR_ARG, "batch_solve: NULL batch");
+  cudaStream_t st = as_stream(stream);
+  const int K = (int)b->solvers.size();
+  for (auto *s : b->solvers) {
+    MLPCG_REQUIRE(s->bound, MLPCG_ERR_ARG, "batch_solve: a solver is no longer bound");
+    if (int rc = start_solve(s, st)) return rc;
+  }
+  if (!b->exec) {
+    if (!b->capture_stream) {
+      MLPCG_CUDA_CHECK(cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking));
+      MLPCG_CUDA_CHECK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+      b->streams.resize(K, nullptr);
+      b->joins.resize(K, nullptr);
+      for (int i = 0; i < K; ++i) {
+        MLPCG_CUDA_CHECK(cudaStreamCreateWithFlags(&b->streams[i], cudaStreamNonBlocking));
+        MLPCG_CUDA_CHECK(cudaEventCreateWithFlags(&b->joins[i], cudaEventDisableTiming));
+      }
+    }
+    MLPCG_CUDA_CHECK(cudaGraphCreate(&b->graph, 0));
+    cudaGraphConditionalHandle h;
+    MLPCG_CUDA_CHECK(cudaGraphConditionalHandleCreate(&h, b->graph, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp{};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    MLPCG_CUDA_CHECK(cudaGraphAddNode(&node, b->graph, nullptr, nullptr, 0, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    cudaStream_t cs = b->capture_stream;
+    MLPCG_CUDA_CHECK(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    // one branch per system: each waits on the fork, runs its iteration, joins
+    int rc = 0;
+    cudaError_t e = cudaEventRecord(b->fork, cs);
+    BatchStates B{};
+    B.count = K;
+    for (int i = 0; i < K && !rc && e == cudaSuccess; ++i) {
+      B.st[i] = b->solvers[i]->V.st;
+      e = cudaStreamWaitEvent(b->streams[i], b->fork, 0);
+      if (e == cudaSuccess) rc = enqueue_body(b->solvers[i], b->streams[i], h, 0);
+      if (!rc && e == cudaSuccess) e = cudaEventRecord(b->joins[i], b->streams[i]);
+      if (!rc && e == cudaSuccess) e = cudaStreamWaitEvent(cs, b->joins[i], 0);
+    }
+    if (!rc && e == cudaSuccess) {
+      k_batch_control<<<1, kMaxBatch, 0, cs>>>(B, h);
+      e = cudaGetLastError();
+    }
+    cudaGraph_t captured = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(cs, &captured);
+    if (rc) { destroy_batch_graph(b); return rc; }
+    if (e != cudaSuccess) { destroy_batch_graph(b); MLPCG_CUDA_CHECK(e); }
+    if (e2 != cudaSuccess) { destroy_batch_graph(b); MLPCG_CUDA_CHECK(e2); }
+    MLPCG_CUDA_CHECK(cudaGraphInstantiate(&b->exec, b->graph, 0));
+  }
+  MLPCG_CUDA_CHECK(cudaGraphLaunch(b->exec, st));
+  for (auto *s : b->solvers) {
+    k_finalize<<<(unsigned)s->V.nblk, RT, 0, st>>>(s->V);
+    MLPCG_LAUNCH_CHECK();
+  }
   return MLPCG_OK;
 }
 

@@ -155,3 +155,52 @@ class FusedSolver:
             except Exception:
                 pass
             self._h = None
+
+
+class BatchSolver:
+    """Several FusedSolvers -- any grid sizes, methods, tolerances and iteration limits -- solved by
+    one graph launch: the loop runs while any system is running, each iteration runs every system as
+    a parallel branch, and a system that has converged (or stopped) skips its kernels from then on.
+    The solvers must stay bound (no new ``set_image`` flags size change) while batched."""
+
+    def __init__(self, solvers):
+        self.solvers = list(solvers)
+        if not self.solvers:
+            raise ValueError("BatchSolver needs at least one solver")
+        dev = self.solvers[0].flags.device
+        if any(s.flags.device != dev for s in self.solvers):
+            raise ValueError("all solvers of a batch must be on one device")
+        self._lib = self.solvers[0]._lib
+        arr = (C.c_void_p * len(self.solvers))(*[s._h.value for s in self.solvers])
+        h = C.c_void_p()
+        call("mlpcg_batch_create", arr, len(self.solvers), C.byref(h))
+        self._h = h
+        self.device = dev
+
+    def launch(self, bs=None, x0s=None):
+        """Enqueue the solves of all systems (b: one rhs per system, or None to keep the current)."""
+        n = len(self.solvers)
+        bs = [None] * n if bs is None else list(bs)
+        x0s = [None] * n if x0s is None else list(x0s)
+        for s, b, x0 in zip(self.solvers, bs, x0s):
+            if b is not None and b.data_ptr() != s.b.data_ptr():
+                s.b.copy_(b.reshape(s.shape))
+            if x0 is None:
+                s.x.zero_()
+            elif x0.data_ptr() != s.x.data_ptr():
+                s.x.copy_(x0.reshape(s.shape))
+        call("mlpcg_batch_solve", self._h, _stream(self.device))
+
+    def solve(self, bs=None, x0s=None):
+        self.launch(bs, x0s)
+        return [s.result() for s in self.solvers]
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                self._lib.mlpcg_batch_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+

@@ -266,6 +266,35 @@ def test_solve_host_fluid_vectors(cuda):
     assert r.iterations == ref.iterations and torch.equal(x_h, x_ref)
 
 
+def test_batch_of_uneven_systems_matches_single_solves(cuda):
+    """Systems of different sizes, methods and limits in one batched launch: every system's
+    iterations, status and solution equal its own solve; a system that starts converged stays at
+    zero iterations while the others run; the batch graph is reusable."""
+    from mlpcg_gb300.solver import BatchSolver, FusedSolver
+    specs = [((16, 16, 16), 3, "npsd", 60, 1e-6, 1), ((24, 16, 32), 3, "npcg", 80, 1e-5, 2),
+             ((32, 32, 32), 3, "npsd", 100, 1e-6, 3), ((16, 24, 16), 2, "npsd", 50, 1e-6, 4)]
+    solvers, rhs, singles = [], [], []
+    for shape, n, method, max_it, tol, seed in specs:
+        s, flags, img = _scene(shape, seed, cuda)
+        m = _near_identity_model(n, cuda, seed=seed)
+        solver = FusedSolver(m, flags, method=method, max_it=max_it, tol=tol)
+        b = torch.as_tensor(s.rhs, device=cuda)
+        if seed == 4:
+            b = torch.zeros_like(b)  # converged from the start
+        r = solver.solve(b)
+        singles.append((r.iterations, r.status, r.x.clone()))
+        solvers.append(solver)
+        rhs.append(b)
+    batch = BatchSolver(solvers)
+    for _ in range(2):
+        res = batch.solve(rhs)
+        for (it, st, x), r in zip(singles, res):
+            assert r.iterations == it and r.status == st
+            assert torch.equal(r.x, x)
+    assert res[3].iterations == 0 and res[3].status == "converged"
+    assert max(r.iterations for r in res) > 0
+
+
 def test_fused_graph_reuse_is_deterministic(cuda):
     from mlpcg_gb300.solver import FusedSolver
     s, flags, img = _scene((32, 32, 32), 7, cuda)
