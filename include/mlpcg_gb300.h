@@ -332,6 +332,13 @@ int mlpcg_solver_solve(mlpcg_solver *solver, int use_graph, void *stream);
 int mlpcg_solver_result(const mlpcg_solver *solver, int *iterations, int *status, double *rel_res,
                         double *history, void *stream);
 
+/* Schedule of the solver's grid-stride kernels (no counterpart in the
+ * reference): `blocks` CTAs of 256 threads (0 = automatic, at most 1216),
+ * picked per grid size by mlpcg_gb300.autotune.  Takes effect on the next
+ * solve (the captured graph is rebuilt); batches already built keep theirs. */
+int mlpcg_solver_set_schedule(mlpcg_solver *solver, int blocks);
+int mlpcg_solver_get_schedule(const mlpcg_solver *solver, int *blocks_in_use);
+
 /* Many systems in one launch (no counterpart in the reference, whose solver
  * takes one system at a time): `count` (<= 64) bound solvers, each with its
  * own grid size, plan, method, tolerance and max_it, solved together by one

@@ -57,6 +57,8 @@ _PROTOS = {
     "mlpcg_solver_bind": (_i, [_vp, _vp, _sz, _u8p, _vp, _vp]),
     "mlpcg_solver_solve": (_i, [_vp, _i, _vp]),
     "mlpcg_solver_result": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "mlpcg_solver_set_schedule": (_i, [_vp, _i]),
+    "mlpcg_solver_get_schedule": (_i, [_vp, _vp]),
     "mlpcg_batch_create": (_i, [_vp, _i, _vp]),
     "mlpcg_batch_solve": (_i, [_vp, _vp]),
     "mlpcg_batch_destroy": (None, [_vp]),

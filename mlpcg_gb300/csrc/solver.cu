@@ -23,6 +23,7 @@
 // and updates the solver state.  Each loop iteration increments the
 // iteration counter unconditionally and the loop stops at max_it, so the
 // WHILE node always terminates.
+#include <algorithm>
 #include <vector>
 #include "common.cuh"
 
@@ -739,6 +740,7 @@ struct mlpcg_solver {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   cudaStream_t capture_stream = nullptr;  // graphs are captured here, launched on the caller's stream
+  int sched_blocks = 0;                    // blocks of the solver's grid-stride kernels (0: automatic)
 };
 
 struct mlpcg_batch {
@@ -874,6 +876,7 @@ int mlpcg_solver_bind(mlpcg_solver *s, void *workspace, size_t workspace_bytes, 
   V.fd3 = make_fastdiv((uint32_t)s->n3);
   V.fd2 = make_fastdiv((uint32_t)s->n2);
   int64_t nb = ((int64_t)V.ngroups + RT * UNR - 1) / (RT * UNR);
+  if (s->sched_blocks > 0) nb = std::min<int64_t>(nb, s->sched_blocks);
   V.nblk = (int)(nb < 1 ? 1 : (nb > RB_MAX ? RB_MAX : nb));
   s->bound = true;
   return MLPCG_OK;
@@ -947,6 +950,29 @@ int mlpcg_solver_result(const mlpcg_solver *s, int *iters, int *status, double *
   if (iters) *iters = S.it;
   if (status) *status = S.status;
   if (rel_res) *rel_res = S.rel;
+  return MLPCG_OK;
+}
+
+int mlpcg_solver_set_schedule(mlpcg_solver *s, int blocks) {
+  clear_error();
+  MLPCG_REQUIRE(s, MLPCG_ERR_ARG, "solver_set_schedule: NULL solver");
+  MLPCG_REQUIRE(blocks >= 0 && blocks <= RB_MAX, MLPCG_ERR_ARG, "solver_set_schedule: blocks %d out of [0, %d]",
+                blocks, RB_MAX);
+  s->sched_blocks = blocks;
+  if (s->bound) {
+    Vecs &V = s->V;
+    int64_t nb = ((int64_t)V.ngroups + RT * UNR - 1) / (RT * UNR);
+    if (blocks > 0) nb = std::min<int64_t>(nb, blocks);
+    V.nblk = (int)(nb < 1 ? 1 : (nb > RB_MAX ? RB_MAX : nb));
+    destroy_graph(s);  // recaptured with the new grid on the next solve
+  }
+  return MLPCG_OK;
+}
+
+int mlpcg_solver_get_schedule(const mlpcg_solver *s, int *blocks_in_use) {
+  clear_error();
+  MLPCG_REQUIRE(s && blocks_in_use, MLPCG_ERR_ARG, "solver_get_schedule: NULL argument");
+  *blocks_in_use = s->bound ? s->V.nblk : s->sched_blocks;
   return MLPCG_OK;
 }
 
