@@ -204,6 +204,19 @@ class Upsample2Function(torch.autograd.Function):
         return ops.upsample2_adjoint(g.contiguous())
 
 
+class Prolong8Function(torch.autograd.Function):
+    """F.interpolate(x, scale_factor=2) / 8 (nearest): the adjoint of the 2x2x2 average pool,
+    the prolongation of the SPD models (sm_model_3d.py:332,378,415)."""
+
+    @staticmethod
+    def forward(ctx, x):
+        return ops.avg_pool2_adjoint(x.contiguous())
+
+    @staticmethod
+    def backward(ctx, g):
+        return ops.avg_pool2(g.contiguous())
+
+
 class CombineFunction(torch.autograd.Function):
     """c0 * x + c1 * y with scalar (1,) tensors c0, c1 (sm_model_3d.py:258,286)."""
 
@@ -349,3 +362,141 @@ class SmallSMModelDn3D(BaseModel):
         """Coefficients of every block precomputed on ``image``: see precond.PrecondPlan."""
         from .precond import PrecondPlan
         return PrecondPlan(self, image, storage=storage, act_storage=act_storage)
+
+
+######################
+# SPD models
+######################
+class _Steps:
+    """The primitive steps of a preconditioner pass: autograd Functions for training, the
+    library calls directly for inference."""
+
+    def __init__(self, train):
+        self.train = train
+        self.pool = AvgPool2Function.apply if train else ops.avg_pool2
+        self.prolong = Prolong8Function.apply if train else ops.avg_pool2_adjoint
+        self.combine = CombineFunction.apply if train else ops.axpby
+
+    def block(self, module, image, x):
+        return module(image, x) if self.train else module.eval_forward(image, x)
+
+    def linear(self, module, image):
+        return module(image) if self.train else module.eval_forward(image)
+
+
+def _spd_pyramid(model, image, steps, imgs, c0, c1):
+    """Image pyramid imgs[0..n] and the per-level c0 / c1; the caller's lists are filled when
+    empty and reused when filled."""
+    if not imgs:
+        imgs.append(image)
+        for _ in range(model.n):
+            imgs.append(steps.pool(imgs[-1]))
+    if not c0:
+        c0.extend(steps.linear(model.c0[i], imgs[i]) for i in range(model.n))
+    if not c1:
+        c1.extend(steps.linear(model.c1[i], imgs[i]) for i in range(model.n))
+    return imgs, c0, c1
+
+
+class SPDSMModelDn3D(BaseModel):
+    """Symmetric multilevel preconditioner (sm_model_3d.py:293-385): a V-cycle with blocks l0
+    (down), l (coarsest) and l1 (up), followed by its mirror image with the transposed blocks
+    l1_t, l_t, l0_t, which share the parameters of l1, l, l0.  Prolongation is nearest x2 / 8,
+    the adjoint of the 2x2x2 average pool.  Module names and creation order are the
+    reference's, so its checkpoints load and a given seed draws its initial weights."""
+
+    def __init__(self, n):
+        super().__init__()
+        self.n = n
+        self.l0 = nn.ModuleList()
+        self.l1 = nn.ModuleList()
+        self.l0_t = nn.ModuleList()
+        self.l1_t = nn.ModuleList()
+        for _ in range(n):
+            self.l0.append(SmallSMBlock3D())
+            self.l1.append(SmallSMBlock3D())
+            self.l0_t.append(SmallSMBlockTrans3D(weight=self.l0[-1].weight, bias=self.l0[-1].bias))
+            self.l1_t.append(SmallSMBlockTrans3D(weight=self.l1[-1].weight, bias=self.l1[-1].bias))
+        self.l = SmallSMBlock3D()
+        self.l_t = SmallSMBlockTrans3D(weight=self.l.weight, bias=self.l.bias)
+        self.c0 = nn.ModuleList([SmallLinearBlock3DNew() for _ in range(n)])
+        self.c1 = nn.ModuleList([SmallLinearBlock3DNew() for _ in range(n)])
+
+    check_grid = SmallSMModelDn3D.check_grid
+
+    def _run(self, image, b, steps, imgs, c0, c1):
+        self.check_grid(image.shape)
+        imgs, c0, c1 = _spd_pyramid(self, image, steps, imgs, c0, c1)
+        n = self.n
+        x = [steps.block(self.l0[0], imgs[0], b)]
+        for i in range(1, n):
+            x.append(steps.block(self.l0[i], imgs[i], steps.pool(x[-1])))
+        x.append(steps.block(self.l, imgs[n], steps.pool(x[-1])))
+        for i in range(n, 0, -1):
+            x[i] = steps.block(self.l1[i - 1], imgs[i - 1], steps.prolong(x[i]))
+            x[i - 1] = steps.combine(c0[i - 1], x[i - 1], c1[i - 1], x[i])
+        x = [x[0]]
+        for i in range(n):
+            x.append(steps.pool(steps.block(self.l1_t[i], imgs[i], x[i])))
+        x[-1] = steps.block(self.l_t, imgs[n], x[-1])
+        for i in range(n - 1, -1, -1):
+            x[i] = steps.combine(c0[i], x[i], c1[i], steps.prolong(x[i + 1]))
+            x[i] = steps.block(self.l0_t[i], imgs[i], x[i])
+        return x[0]
+
+    def forward(self, image, b):
+        """Training pass with autograd (sm_model_3d.py:349-385)."""
+        return self._run(image, b, _Steps(True), [], [], [])
+
+    def eval_forward(self, image, b, timer=None, imgs=None, c0=None, c1=None):
+        """Inference pass (sm_model_3d.py:313-347).  ``imgs``, ``c0``, ``c1`` are optional
+        caller-owned caches of the image pyramid and the level coefficients."""
+        return self._run(image, b, _Steps(False), [] if imgs is None else imgs,
+                         [] if c0 is None else c0, [] if c1 is None else c1)
+
+
+class SmallSPDSMModelDn3D(BaseModel):
+    """Reduced symmetric preconditioner (sm_model_3d.py:388-444): M = S^T S, S the down sweep
+    (blocks l0, pooling, coarsest block l); the up sweep applies l_t, the nearest x2 / 8
+    prolongation, c0^2 x + c1^2 y and the transposed blocks l0_t.  Module names and creation
+    order are the reference's."""
+
+    def __init__(self, n):
+        super().__init__()
+        self.n = n
+        self.l0 = nn.ModuleList()
+        self.l0_t = nn.ModuleList()
+        for _ in range(n):
+            self.l0.append(SmallSMBlock3D())
+            self.l0_t.append(SmallSMBlockTrans3D(weight=self.l0[-1].weight, bias=self.l0[-1].bias))
+        self.l = SmallSMBlock3D()
+        self.l_t = SmallSMBlockTrans3D(weight=self.l.weight, bias=self.l.bias)
+        self.c0 = nn.ModuleList([SmallLinearBlock3DNew() for _ in range(n)])
+        self.c1 = nn.ModuleList([SmallLinearBlock3DNew() for _ in range(n)])
+
+    check_grid = SmallSMModelDn3D.check_grid
+
+    def _run(self, image, b, steps, imgs, c0, c1):
+        self.check_grid(image.shape)
+        imgs, c0, c1 = _spd_pyramid(self, image, steps, imgs, c0, c1)
+        n = self.n
+        x = [steps.block(self.l0[0], imgs[0], b)]
+        for i in range(1, n):
+            x.append(steps.block(self.l0[i], imgs[i], steps.pool(x[-1])))
+        x.append(steps.block(self.l, imgs[n], steps.pool(x[-1])))
+        x[-1] = steps.block(self.l_t, imgs[n], x[-1])
+        for i in range(n, 0, -1):
+            x[i] = steps.prolong(x[i])
+            x[i - 1] = steps.combine(c0[i - 1] * c0[i - 1], x[i - 1], c1[i - 1] * c1[i - 1], x[i])
+            x[i - 1] = steps.block(self.l0_t[i - 1], imgs[i - 1], x[i - 1])
+        return x[0]
+
+    def forward(self, image, b):
+        """Training pass with autograd (sm_model_3d.py:404-423)."""
+        return self._run(image, b, _Steps(True), [], [], [])
+
+    def eval_forward(self, image, b, timer=None, imgs=None, c0=None, c1=None):
+        """Inference pass (sm_model_3d.py:425-444); ``imgs``, ``c0``, ``c1`` as in
+        SPDSMModelDn3D.eval_forward."""
+        return self._run(image, b, _Steps(False), [] if imgs is None else imgs,
+                         [] if c0 is None else c0, [] if c1 is None else c1)

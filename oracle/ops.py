@@ -179,6 +179,15 @@ def upsample2(x) -> np.ndarray:
     return _up1(_up1(_up1(x, -3), -2), -1)
 
 
+def prolong_nearest8(x) -> np.ndarray:
+    """F.interpolate(x, scale_factor=2) / 8 (default 'nearest' mode; sm_model_3d.py:332,378,415):
+    every coarse value copied to its 2x2x2 children, divided by 8 -- the adjoint of avg_pool2."""
+    x = np.asarray(x, dtype=np.float64)
+    for ax in (-3, -2, -1):
+        x = np.repeat(x, 2, axis=ax)
+    return x / 8.0
+
+
 def init_block_params(gen_uniform):
     """BaseModel.reset_parameters on a (27,3,3,3,3) weight and (27,) bias (model.py:22-29):
     kaiming_uniform(a=sqrt(5)) gives bound 1/sqrt(fan_in) = 1/9 for both."""

@@ -9,7 +9,8 @@ What it imports from the reference, unmodified:
 
 * sm_model_3d_py.py -- SmallSMBlock3DPY (Conv3d + unfold) and SmallLinearBlock3DPY,
   the reference's own CPU statement of the block and linear ops;
-* sm_model_3d.py    -- SmallSMModelDn3D and its autograd Functions; its JIT
+* sm_model_3d.py    -- SmallSMModelDn3D, SPDSMModelDn3D, SmallSPDSMModelDn3D and
+  their autograd Functions; its JIT
   extension modules (CUDA, cannot run here) are replaced by thin adapters that
   evaluate the ops with the SmallSMBlock3DPY / SmallLinearBlock3DPY math, so
   the reference's own module tree, initialisation order and orchestration
@@ -20,7 +21,8 @@ What it imports from the reference, unmodified:
 * cg_tests.py       -- npcg, npcg_flex, npsd (cupy / AMGCL imports stubbed,
   torch.cuda.synchronize made a no-op).
 
-Outputs (FP64 unless noted): ops_*.npz, model_*.npz, laplacian_*.npz, cg_*.npz, and
+Outputs (FP64 unless noted): ops_*.npz, model_*.npz, spd_*.npz / small_spd_*.npz (fp32) with\ntheir cg_spd_* / cg_small_spd_* solver histories,
+laplacian_*.npz, cg_*.npz, and
 scene_8/ (simulator-format files) with scene_files_8.npz (what the reference reads from them).
 The scenes come from mlpcg_gb300.scenes (seeded), stored in the fixtures.
 """
@@ -201,6 +203,29 @@ def make_model(ref_model, ref_py, shape, n, seed_scene, seed_init=0):
     return out, model, scene
 
 
+def make_spd(ref_model, ref_py, cls_name, shape, n, seed_scene, seed_init=0):
+    """The reference's SPD preconditioners (SPDSMModelDn3D / SmallSPDSMModelDn3D) under the
+    adapters: state dict under ``torch.manual_seed(seed_init)``, forward on a batch of two and
+    eval_forward on one right-hand side."""
+    ref_model.smblock3d = _BlockAdapter(ref_py, False)
+    ref_model.smblocktrans3d = _BlockAdapter(ref_py, True)
+    ref_model.smlinear3d = _LinearAdapter(ref_py)
+    torch.manual_seed(seed_init)
+    model = getattr(ref_model, cls_name)(n)
+    sd = {k: v.detach().numpy().copy() for k, v in model.state_dict().items()}
+    scene = make_scene(shape, seed_scene)
+    image = torch.from_numpy(scene.image())
+    torch.manual_seed(4321)
+    b = torch.rand(2, 1, *shape)
+    with torch.no_grad():
+        y = model(image, b)
+        ye = model.eval_forward(image, b[:1])
+    out = {"flags": scene.flags, "image": scene.image(), "b": b.numpy(), "y": y.numpy(), "y_eval": ye.numpy(),
+           "n": np.array(n)}
+    out.update({"param:" + k: v for k, v in sd.items()})
+    return out, model, scene
+
+
 def make_laplacian(ref_lap, ref_read, shape, seed):
     scene = make_scene(shape, seed)
     f = scene.flags
@@ -293,6 +318,14 @@ def main(ref_root: str, only: str | None = None):
         print("scene files written to", HERE)
         return
     torch.set_default_dtype(torch.float32)
+    spd = {"spd_16_l2.npz": ("SPDSMModelDn3D", 2), "small_spd_16_l3.npz": ("SmallSPDSMModelDn3D", 3)}
+    for fname, (cls_name, n) in spd.items():
+        out, model, scene = make_spd(ref_model, ref_py, cls_name, (16, 16, 16), n, seed_scene=6)
+        np.savez_compressed(HERE / fname, **out)
+        np.savez_compressed(HERE / ("cg_" + fname), **make_cg(ref_cg, model, scene))
+    if only == "spd":
+        print("SPD fixtures written to", HERE)
+        return
     for shape, seed in (((8, 8, 8), 0), ((6, 4, 10), 1), ((16, 16, 16), 2)):
         out = make_ops(ref_py, shape, seed)
         out = {k: v for k, v in out.items() if v is not None}
@@ -312,7 +345,7 @@ def main(ref_root: str, only: str | None = None):
 
 
 if __name__ == "__main__":
-    # python make_golden.py [reference root] [--only scene_files]
+    # python make_golden.py [reference root] [--only=scene_files | --only=spd]
     args = [a for a in sys.argv[1:] if not a.startswith("--only")]
     only = next((a.split("=", 1)[1] for a in sys.argv[1:] if a.startswith("--only=")), None)
     main(args[0] if args else "/root/reference", only)

@@ -1,0 +1,194 @@
+"""SPD preconditioners SPDSMModelDn3D / SmallSPDSMModelDn3D (sm_model_3d.py:290-444).
+
+CPU: the oracle compositions against the reference's own outputs, the module
+tree against its state dict and initial weights.  GPU: the drop-in classes
+(library kernels) against the oracle and the reference, their gradients against
+FP64 central differences, the operator's symmetry (the reference's self-test,
+sm_model_3d.py:476-485), and the drop-in CG solvers' residual histories against
+the reference's cg_tests.py run with the same network.
+"""
+import numpy as np
+import pytest
+import torch
+
+from conftest import rel_err
+from oracle import cg as ocg
+from oracle import laplacian as olap
+from oracle import model as omodel
+
+MODELS = [("spd_16_l2.npz", "SPDSMModelDn3D", omodel.spd_forward),
+          ("small_spd_16_l3.npz", "SmallSPDSMModelDn3D", omodel.small_spd_forward)]
+IDS = ["SPDSMModelDn3D", "SmallSPDSMModelDn3D"]
+
+
+def _params(d, dt=None):
+    return {k[len("param:"):]: (v if dt is None else v.astype(dt)) for k, v in d.items() if k.startswith("param:")}
+
+
+@pytest.mark.parametrize("fname,cls,fwd", MODELS, ids=IDS)
+def test_oracle_vs_reference(golden, fname, cls, fwd):
+    d = golden(fname)
+    p, n = _params(d), int(d["n"])
+    assert rel_err(fwd(p, d["image"], d["b"][:, 0], n), d["y"][:, 0]) < 1e-5  # reference ran in fp32
+    assert rel_err(fwd(p, d["image"], d["b"][:1, 0], n), d["y_eval"][:, 0]) < 1e-5
+
+
+@pytest.mark.parametrize("fname,cls,fwd", MODELS, ids=IDS)
+def test_init_order_and_keys(golden, fname, cls, fwd):
+    """The module tree draws the reference's initial weights under torch.manual_seed(0) and has its
+    state-dict keys (the transposed blocks list the shared parameters again)."""
+    from mlpcg_gb300 import sm_model_3d
+    d = golden(fname)
+    ref = _params(d)
+    torch.manual_seed(0)
+    m = getattr(sm_model_3d, cls)(int(d["n"]))
+    sd = m.state_dict()
+    assert sorted(sd) == sorted(ref)
+    for k, v in sd.items():
+        np.testing.assert_array_equal(v.numpy(), ref[k])
+    assert m.l0_t[0].weight is m.l0[0].weight and m.l_t.bias is m.l.bias
+    small = cls.startswith("Small")
+    names = omodel.spd_param_names(int(d["n"]), small=small)
+    # drawing in that order reproduces every initial weight
+    torch.manual_seed(0)
+    for name in names:
+        w, bias = torch.ones(27, 3, 3, 3, 3), torch.ones(27)
+        m.reset_parameters(w, bias)
+        if name[0] == "c":  # SmallLinearBlock3DNew keeps the means
+            w, bias = w.mean(0, keepdim=True), bias.mean(0, keepdim=True)
+        np.testing.assert_array_equal(w.numpy(), ref[name + ".weight"])
+        np.testing.assert_array_equal(bias.numpy(), ref[name + ".bias"])
+
+
+@pytest.mark.parametrize("fname,cls,fwd", MODELS, ids=IDS)
+def test_oracle_symmetry(golden, fname, cls, fwd):
+    """<x, M y> = <y, M x> in FP64 for both SPD compositions (M = V^T V, M = S^T S)."""
+    d = golden(fname)
+    p, n = _params(d, np.float64), int(d["n"])
+    rng = np.random.default_rng(3)
+    x, y = rng.standard_normal((2,) + d["image"].shape[1:])
+    a = float((x * fwd(p, d["image"], y, n)).sum())
+    b = float((y * fwd(p, d["image"], x, n)).sum())
+    assert abs(a - b) <= 1e-12 * max(abs(a), 1.0)
+    assert float((x * fwd(p, d["image"], x, n)).sum()) >= 0.0
+
+
+# ---------------------------------------------------------------------------- GPU
+def _t(a, dev, dt=torch.float32):
+    return torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=dev)
+
+
+def _model(d, cls, cuda):
+    from mlpcg_gb300 import sm_model_3d
+    m = getattr(sm_model_3d, cls)(int(d["n"])).to(cuda)
+    m.load_state_dict({k: torch.as_tensor(v) for k, v in _params(d).items()})
+    return m
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("fname,cls,fwd", MODELS, ids=IDS)
+def test_forward_and_eval_forward(golden, cuda, fname, cls, fwd):
+    d = golden(fname)
+    m = _model(d, cls, cuda)
+    img = _t(d["image"], cuda)
+    ref = fwd(_params(d), d["image"], d["b"][:, 0], int(d["n"]))
+    with torch.no_grad():
+        y = m(img, _t(d["b"], cuda))
+    assert rel_err(y.cpu().numpy()[:, 0], ref) < 1e-5
+    assert rel_err(y.cpu().numpy(), d["y"]) < 1e-5
+    imgs, c0, c1 = [], [], []
+    ye = m.eval_forward(img, _t(d["b"][:1], cuda), None, imgs, c0, c1)
+    assert rel_err(ye.cpu().numpy(), d["y_eval"]) < 1e-5
+    # a second call reuses the cached pyramid and level coefficients
+    assert len(imgs) == int(d["n"]) + 1 and len(c0) == len(c1) == int(d["n"])
+    ye2 = m.eval_forward(img, _t(d["b"][1:], cuda), None, imgs, c0, c1)
+    assert rel_err(ye2.cpu().numpy()[:, 0], ref[1:]) < 1e-5
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("fname,cls,fwd", MODELS, ids=IDS)
+def test_gradients_vs_fp64_finite_differences(golden, cuda, fname, cls, fwd):
+    """d<g, M b> / d(theta, b) from the adjoint kernels vs FP64 central differences of the oracle;
+    a shared parameter collects the gradients of the block and of its transpose."""
+    d = golden(fname)
+    m = _model(d, cls, cuda)
+    n = int(d["n"])
+    p = _params(d, np.float64)
+    img_np = d["image"].astype(np.float64)
+    b_np = d["b"][:1, 0].astype(np.float64)
+    g_np = np.random.default_rng(5).standard_normal(b_np.shape)
+    b = _t(b_np[:, None], cuda).requires_grad_(True)
+    out = m(_t(img_np, cuda), b)
+    (out * _t(g_np[:, None], cuda)).sum().backward()
+    grads = {k: v.grad.detach().cpu().numpy() for k, v in m.named_parameters()}
+
+    def loss(pp=p, bb=b_np):
+        return float((fwd(pp, img_np, bb, n) * g_np).sum())
+
+    rng = np.random.default_rng(13)
+    h = 1e-4
+    names = ["l0.0.weight", "l0.1.bias", "l.weight", "c0.0.weight", "c1.1.bias"]
+    if not cls.startswith("Small"):
+        names += ["l1.0.weight", "l1.1.bias"]
+    for name in names:
+        for _ in range(2):
+            idx = tuple(rng.integers(0, s) for s in p[name].shape)
+            pp, pm = dict(p), dict(p)
+            pp[name] = p[name].copy(); pp[name][idx] += h
+            pm[name] = p[name].copy(); pm[name][idx] -= h
+            fd = (loss(pp) - loss(pm)) / (2 * h)
+            assert abs(grads[name][idx] - fd) <= 2e-3 * max(1.0, abs(fd)) + 1e-5, (name, idx, grads[name][idx], fd)
+    v = rng.standard_normal(b_np.shape)
+    fd = (loss(bb=b_np + h * v) - loss(bb=b_np - h * v)) / (2 * h)
+    assert abs(float((b.grad.cpu().numpy()[:, 0] * v).sum()) - fd) <= 1e-4 * max(1.0, abs(fd))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cls,n,shape,batch", [("SmallSPDSMModelDn3D", 4, (64, 64, 64), 8),
+                                               ("SPDSMModelDn3D", 3, (32, 48, 64), 4)])
+def test_symmetry_self_test(cuda, cls, n, shape, batch):
+    """The reference's self-test (sm_model_3d.py:476-485): |x^T M y - y^T M x| over a batch of
+    random vectors on a random image, absolute and relative to sqrt(|a| |b|)."""
+    from mlpcg_gb300 import sm_model_3d
+    torch.manual_seed(0)
+    model = getattr(sm_model_3d, cls)(n).to(cuda)
+    x = torch.rand(batch, 1, *shape, device=cuda)
+    y = torch.rand(batch, 1, *shape, device=cuda)
+    img = torch.rand(3, *shape, device=cuda)
+    with torch.no_grad():
+        z = model(img, x)
+        z1 = model(img, y)
+    a = torch.bmm(x.flatten(2).double(), z1.flatten(1).unsqueeze(-1).double())
+    b = torch.bmm(y.flatten(2).double(), z.flatten(1).unsqueeze(-1).double())
+    rel = ((a - b).norm() / torch.sqrt(a.abs() * b.abs()).norm()).item()
+    assert rel < 1e-5, rel
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("fname,cls,fwd", MODELS, ids=IDS)
+def test_solver_histories_vs_reference(golden, cuda, fname, cls, fwd):
+    """npsd / npcg / npcg_flex with the SPD network through the drop-in solvers vs the
+    reference's cg_tests.py run (30 iterations) and the oracle's."""
+    from mlpcg_gb300 import cg
+    from mlpcg_gb300.laplacian import FluidLaplacian
+    d = golden("cg_" + fname)
+    md = golden(fname)
+    m = _model(md, cls, cuda)
+    flags = torch.as_tensor(d["flags"], device=cuda)
+    A = FluidLaplacian(flags)
+    img = _t(md["image"], cuda)
+    b = _t(d["rhs"].ravel()[A.fluid_cells.cpu().numpy()], cuda, torch.float64)
+    Ao, fluid = olap.assemble(d["flags"])
+    p, n = _params(md, np.float64), int(md["n"])
+    pred_o = ocg.make_predict(lambda g: fwd(p, md["image"], g, n), fluid, d["flags"].shape)
+    for name in ("npsd", "npcg", "npcg_flex"):
+        hist = []
+        pred = cg.model_predict(m, img, A.fluid_cells)
+        getattr(cg, name)(b, A, torch.zeros_like(b), pred, 30, tol=1e-6, atol=1e-20,
+                          callback=lambda nrm, t: hist.append(nrm))
+        ref = d[f"{name}_hist"]
+        k = min(len(hist), len(ref))
+        np.testing.assert_allclose(np.array(hist[:k])[:20], ref[:k][:20], rtol=1e-4)
+        _, _, hist_o = getattr(ocg, name)(d["rhs"].ravel()[fluid], Ao, np.zeros(fluid.size), pred_o, 30,
+                                          tol=1e-6, atol=1e-20)
+        np.testing.assert_allclose(np.array(hist[:20]), np.array(hist_o[:20]), rtol=1e-4)
