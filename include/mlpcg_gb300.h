@@ -257,6 +257,25 @@ typedef struct mlpcg_precond mlpcg_precond;
  * (levels whose z size is not a multiple of 8 always use dense planes). */
 int mlpcg_precond_create(int N1, int N2, int N3, int levels, int k_dtype, int act_dtype,
                          int swap_sm_order, int mask, int coeff_layout, mlpcg_precond **out);
+
+/* Network kinds of a plan. */
+#define MLPCG_PRECOND_SM        0  /* SmallSMModelDn3D (sm_model_3d.py:164-287) */
+#define MLPCG_PRECOND_SMALL_SPD 1  /* SmallSPDSMModelDn3D (sm_model_3d.py:388-444) */
+
+/* Plan for the reduced symmetric network SmallSPDSMModelDn3D(levels)
+ * (sm_model_3d.py:388-444; replaces its eval_forward inside the solver
+ * loop): M = S^T S, S the down sweep of blocks l0[0..n-1] with average
+ * pooling and the coarsest block l.  Application: the down sweep, l then
+ * l_t on the coarsest level, and per level the nearest x2 / 8 prolongation,
+ * c0^2 y + c1^2 u and the transposed block l0_t.  The transposed blocks'
+ * coefficients are gathered from the forward blocks' (B^T has at cell q
+ * the coefficient 26 - p of cell q + offset p), so no image is re-read.
+ * setup's params: l0[0..n-1], l as (weight 2187, bias 27), then c0[0..n-1],
+ * c1[0..n-1] as (weight 81, bias 1); mlpcg_precond_coefficients returns the
+ * squares c0^2, c1^2 for this kind.  Other arguments as mlpcg_precond_create
+ * (no swap / mask options: the network has none). */
+int mlpcg_precond_create_spd(int N1, int N2, int N3, int levels, int k_dtype, int act_dtype, int coeff_layout,
+                             mlpcg_precond **out);
 /* After setup (synchronises `stream`): the number of general cells and of
  * mixed runs (records) of a classed level; -1 for both on a dense level. */
 int mlpcg_precond_class_counts(const mlpcg_precond *plan, int level, int64_t *general_cells, int64_t *mixed_runs,

@@ -43,6 +43,7 @@ _PROTOS = {
     "mlpcg_axpby": (_i, [_fp, _vp, _fp, _vp, _vp, _i, _i64, _vp]),
     "mlpcg_laplacian_apply": (_i, [_u8p, _vp, _vp, _i, _i, _i, _i, _vp]),
     "mlpcg_precond_create": (_i, [_i, _i, _i, _i, _i, _i, _i, _i, _i, _vp]),
+    "mlpcg_precond_create_spd": (_i, [_i, _i, _i, _i, _i, _i, _i, _vp]),
     "mlpcg_precond_class_counts": (_i, [_vp, _i, _vp, _vp, _vp]),
     "mlpcg_precond_workspace": (_sz, [_vp]),
     "mlpcg_precond_destroy": (None, [_vp]),

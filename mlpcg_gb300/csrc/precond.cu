@@ -248,17 +248,49 @@ __device__ __forceinline__ uint8_t material_at(float4 a, float4 f, float4 s, int
 }
 
 // Class byte of every cell, the word of every run, and per tile the numbers
-// of mixed runs (rcount) and of general cells (gcount).  The tile's material
-// codes (with a one-cell halo; outside the grid = solid) are staged in shared
-// memory, loaded as 4-wide vectors of the three image channels; a cell is
-// uniform when all 27 codes around it agree.
+// of mixed runs (rcount) and of general cells (gcount).  The tile's codes
+// (with a one-cell halo; outside the grid = solid) are staged in shared
+// memory; a cell is uniform when all 27 codes around it agree.
+// FROM_CLS = false: the codes are the cells' materials, loaded as 4-wide
+// vectors of the three image channels (the classes of a forward block).
+// FROM_CLS = true: the codes are the forward block's class bytes (src_cls),
+// which gives the classes of the transposed block: its coefficients at q are
+// the forward ones of q's 27 neighbours, uniform when those all are alike.
+template <bool FROM_CLS>
 __global__ void __launch_bounds__(PT)
-k_classify(const float *__restrict__ img, int n1, int n2, int n3, uint8_t *__restrict__ cls,
-           uint32_t *__restrict__ rw, uint32_t *__restrict__ rcount, uint32_t *__restrict__ gcount) {
+k_classify(const float *__restrict__ img, const uint8_t *__restrict__ src_cls, int n1, int n2, int n3,
+           uint8_t *__restrict__ cls, uint32_t *__restrict__ rw, uint32_t *__restrict__ rcount,
+           uint32_t *__restrict__ gcount) {
   __shared__ __align__(16) uint8_t M[HX][HY][HZP];
   const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY, x0 = blockIdx.z * TX;
   const int64_t n = cells(n1, n2, n3);
-  {
+  if (FROM_CLS) {
+    const int v = threadIdx.x % NVR, k = z0 + 4 * v;
+    uint32_t w[kStageVec];
+#pragma unroll
+    for (int m = 0; m < kStageVec; ++m) {
+      const int r = stage_vec_row(m), i = x0 + r / HY - 1, j = y0 + r % HY - 1;
+      const bool in = (unsigned)i < (unsigned)n1 && (unsigned)j < (unsigned)n2 && k < n3;
+      // 4 class bytes (k a multiple of 4, n3 of 8: 4-byte aligned); 0 = CLS_SOLID outside
+      w[m] = in ? __ldg(reinterpret_cast<const uint32_t *>(src_cls + ((int64_t)i * n2 + j) * n3 + k)) : 0u;
+    }
+#pragma unroll
+    for (int m = 0; m < kStageVec; ++m) {
+      const int r = stage_vec_row(m);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) M[r / HY][r % HY][4 * v + 1 + c] = (uint8_t)(w[m] >> (8 * c));
+    }
+#pragma unroll
+    for (int m = 0; m < kStageHalo; ++m) {
+      const int e = stage_halo_id(m), r = e >> 1;
+      if (e >= 2 * HX * HY) continue;
+      const int i = x0 + r / HY - 1, j = y0 + r % HY - 1, kk = (e & 1) ? z0 + TZ : z0 - 1;
+      uint8_t mc = CLS_SOLID;
+      if ((unsigned)i < (unsigned)n1 && (unsigned)j < (unsigned)n2 && (unsigned)kk < (unsigned)n3)
+        mc = src_cls[((int64_t)i * n2 + j) * n3 + kk];
+      M[r / HY][r % HY][(e & 1) ? HZ - 1 : 0] = mc;
+    }
+  } else {
     const int v = threadIdx.x % NVR, k = z0 + 4 * v;
     // the interior in 3 batches of 3 vectors per channel, every load of a batch in flight together
 #pragma unroll
@@ -397,10 +429,13 @@ __device__ __forceinline__ float round_as(const __nv_bfloat16 *, float v) {
 // model (blockIdx.x = parameter block b, at params + b * 2214), rounded like
 // the stored dtype: thread (c, p) evaluates output p of material c in the
 // accumulation order of coeffs_of_patch_n, so it equals what that function
-// yields on a patch of material c.
+// yields on a patch of material c.  Block b's vectors go to slot b; with
+// spd_levels = n > 0 (the SPD kind: parameter blocks l0[0..n-1], l) block b
+// goes to slot b (l: slot 2n) and its transpose, the reversed vector (tap
+// 26 - p), to slot n + b (l_t: slot 2n + 1).
 template <typename KT>
 __global__ void __launch_bounds__(3 * KREC)
-k_kgen_uniform_all(const float *__restrict__ params, float *__restrict__ kuni) {
+k_kgen_uniform_all(const float *__restrict__ params, float *__restrict__ kuni, int spd_levels) {
   const int b = blockIdx.x, c = threadIdx.x / KREC, p = threadIdx.x % KREC;
   const float *W = params + (size_t)b * 2214, *bias = W + 2187;
   float acc = 0.f;
@@ -413,7 +448,13 @@ k_kgen_uniform_all(const float *__restrict__ params, float *__restrict__ kuni) {
     }
     acc = round_as((const KT *)nullptr, acc);
   }
-  kuni[(size_t)b * 3 * KREC + threadIdx.x] = acc;
+  if (spd_levels <= 0) {
+    kuni[(size_t)b * 3 * KREC + threadIdx.x] = acc;
+    return;
+  }
+  const int n = spd_levels, sf = b < n ? b : 2 * n, sr = b < n ? n + b : 2 * n + 1;
+  kuni[(size_t)sf * 3 * KREC + threadIdx.x] = acc;
+  kuni[(size_t)sr * 3 * KREC + c * KREC + (p < 27 ? 26 - p : p)] = acc;
 }
 
 // The linear index of every general cell, tile by tile in thread / run / cell
@@ -539,6 +580,71 @@ k_fill_uniform(const uint8_t *__restrict__ cls, const uint32_t *__restrict__ rli
       for (int p = 0; p < 27; ++p) stf(r + p * rp.stride, __ldg(ku + p));
     }
   }
+}
+
+// The transposed block's coefficients at its general cells, gathered from
+// the forward block of the same weights: B^T at cell q has, for tap p, the
+// forward coefficient 26 - p of the neighbour r = q + offset(p) (its
+// material's uniform value, or its record entry when r is general); 0 where
+// r is outside the grid (the input is 0 there).  Written into q's record of
+// the transposed block.  Thread e of the grid-stride loop takes list[e].
+template <typename KT>
+__global__ void __launch_bounds__(PT)
+k_kgen_t_list(int n1, int n2, int n3, const uint32_t *__restrict__ list, const uint32_t *__restrict__ glast_base,
+              const uint32_t *__restrict__ glast_count, const uint8_t *__restrict__ cls,
+              const uint32_t *__restrict__ rw, const uint32_t *__restrict__ rbase, const uint32_t *__restrict__ rcount,
+              const KT *__restrict__ rec, const float *__restrict__ kuni, const uint32_t *__restrict__ rwT,
+              const uint32_t *__restrict__ rbaseT, const uint32_t *__restrict__ rcountT, KT *__restrict__ recT) {
+  const uint32_t G = __ldg(glast_base) + __ldg(glast_count);
+  for (uint32_t e = blockIdx.x * PT + threadIdx.x; e < G; e += gridDim.x * PT) {
+    const uint32_t q = __ldg(list + e);
+    const int k = (int)(q % (uint32_t)n3);
+    const uint32_t t = q / (uint32_t)n3;
+    const int j = (int)(t % (uint32_t)n2), i = (int)(t / (uint32_t)n2);
+    const RecPos rt = rec_pos(rwT, rbaseT, rcountT, q, i, j, k, n2, n3);
+#pragma unroll 3
+    for (int p = 0; p < 27; ++p) {
+      const int ii = i + tap_dx(p), jj = j + tap_dy(p), kk = k + tap_dz(p);
+      float v = 0.f;
+      if ((unsigned)ii < (unsigned)n1 && (unsigned)jj < (unsigned)n2 && (unsigned)kk < (unsigned)n3) {
+        const uint32_t r = ((uint32_t)ii * (uint32_t)n2 + (uint32_t)jj) * (uint32_t)n3 + (uint32_t)kk;
+        const int cl = __ldg(cls + r);
+        if (cl != CLS_GENERAL) {
+          v = __ldg(kuni + cl * KREC + 26 - p);
+        } else {
+          const RecPos rf = rec_pos(rw, rbase, rcount, r, ii, jj, kk, n2, n3);
+          v = ldf(rec + rf.offset + (size_t)(26 - p) * rf.stride);
+        }
+      }
+      stf(recT + rt.offset + (size_t)p * rt.stride, v);
+    }
+  }
+}
+
+// Dense planes of the transposed block: KT[p][q] = K[26 - p][q + offset(p)], 0 outside the grid.
+template <typename KT>
+__global__ void __launch_bounds__(256)
+k_planes_transpose(const KT *__restrict__ K, KT *__restrict__ Kt, int64_t ps, int n1, int n2, int n3) {
+  const int64_t n = cells(n1, n2, n3);
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int k = (int)(q % n3);
+  const int64_t t = q / n3;
+  const int j = (int)(t % n2), i = (int)(t / n2);
+#pragma unroll
+  for (int p = 0; p < 27; ++p) {
+    const int ii = i + tap_dx(p), jj = j + tap_dy(p), kk = k + tap_dz(p);
+    float v = 0.f;
+    if ((unsigned)ii < (unsigned)n1 && (unsigned)jj < (unsigned)n2 && (unsigned)kk < (unsigned)n3)
+      v = ldf(K + (size_t)(26 - p) * ps + ((int64_t)ii * n2 + jj) * n3 + kk);
+    stf(Kt + (size_t)p * ps + q, v);
+  }
+}
+
+// c[e] = c[e]^2 (the SPD kind's c0^2, c1^2; sm_model_3d.py:421)
+__global__ void k_square(float *__restrict__ c, int n) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n) c[e] = c[e] * c[e];
 }
 
 template <typename KT>
@@ -822,8 +928,10 @@ __device__ __forceinline__ void stage_coarse(float (*Cs)[CY][CZP], const CT *__r
 // up(x_{l+1}) (with swap: c0 y_l + c1 up(x_{l+1})), one value per fine
 // cell in the activation dtype, for the post-block kernel to stage like any
 // input (its tile then needs no interpolation of the halo).  Same tile grid
-// and run ownership as the block kernels.
-template <typename CT, typename YT, typename UT, bool SWAP>
+// and run ownership as the block kernels.  up is the trilinear x2
+// interpolation, or with NEAREST the SPD networks' nearest x2 / 8
+// (F.interpolate(x, scale_factor=2) / 8, sm_model_3d.py:415).
+template <typename CT, typename YT, typename UT, bool SWAP, bool NEAREST = false>
 __global__ void __launch_bounds__(PT)
 k_up_fine(const CT *__restrict__ xc, const YT *__restrict__ yl, const float *__restrict__ c0p,
           const float *__restrict__ c1p, UT *__restrict__ u, int n1, int n2, int n3, const int *__restrict__ gate) {
@@ -845,6 +953,24 @@ k_up_fine(const CT *__restrict__ xc, const YT *__restrict__ yl, const float *__r
   __syncthreads();
   if (!active) return;
   const float c0 = SWAP ? __ldg(c0p) : 0.f, c1 = SWAP ? __ldg(c1p) : 0.f;
+  if constexpr (NEAREST) {
+    // fine cell (i, j, k0 + c) takes coarse cell (i/2, j/2, k0/2 + c/2): tile
+    // indices (1, j/2 - cy0, k0/2 - cz0 + c/2)
+    const float *row = &Cs[1][j / 2 - cy0][k0 / 2 - cz0];
+#pragma unroll
+    for (int tx = 0; tx < TX; ++tx) {
+      const int i = x0 + tx;
+      if (i >= n1) continue;
+      float o[8];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        o[c] = row[c / 2] * 0.125f;
+        if (SWAP) o[c] = __fadd_rn(__fmul_rn(c0, yv[tx][c]), __fmul_rn(c1, o[c]));
+      }
+      st8(u + ((int64_t)i * n2 + j) * n3 + k0, o);
+    }
+    return;
+  }
   const Lin1 b = lin1_rel(j, m2, cy0);
   // The run's fine cells k0 .. k0 + 7 interpolate along z between the coarse
   // cells k0/2 - 1 .. k0/2 + 4 (tile z index 4 tz ..), with the weights of
@@ -1028,6 +1154,7 @@ int launch_stencil_gen(const float *, int, int, int, int, const float *, const f
 int launch_stencil_apply(const void *, int, int64_t, const void *, int, int, void *, int, int, int,
                          int, int, int, cudaStream_t);
 int launch_avg_pool2(const void *, void *, int, int, int, int, int, cudaStream_t);
+int launch_avg_pool2_adjoint(const void *, void *, int, int, int, int, int, cudaStream_t);
 int launch_upsample2(const void *, void *, int, int, int, int, int, cudaStream_t);
 int launch_axpby(const float *, const void *, const float *, const void *, void *, int, int64_t,
                  cudaStream_t);
@@ -1041,6 +1168,7 @@ struct PrecondPlan {
   int n1, n2, n3, L;          // fine sizes, number of levels n (blocks at levels 0..L)
   int kdt, adt;               // coefficient / activation storage dtypes
   int swap, mask;
+  int kind;                   // MLPCG_PRECOND_SM (SmallSMModelDn3D) or MLPCG_PRECOND_SMALL_SPD
   int layout;                 // MLPCG_COEFF_DENSE or MLPCG_COEFF_CLASSED
   struct Level { int n1, n2, n3; int64_t n, ps; bool fast, cls; unsigned ntiles; };
   std::vector<Level> lv;      // L + 1 levels
@@ -1058,6 +1186,13 @@ struct PrecondPlan {
   std::vector<uint8_t *> cls;        // classed levels: class byte per cell (setup)
   std::vector<uint32_t *> rw;        // classed levels: word per 8-cell run
   std::vector<uint32_t *> rcount, rbase, gcount, gbase;  // per tile: mixed runs, general cells
+  // SPD kind: the transposed blocks (post-blocks l0_t, coarsest l_t) have their own class
+  // map, run words and per-tile counts (a cell is uniform when its 27 neighbours are)
+  std::vector<uint8_t *> clsT;
+  std::vector<uint32_t *> rwT, rcountT, rbaseT, gcountT, gbaseT;
+  void *Klt = nullptr;        // coarsest transposed block (SPD kind)
+  float *Ult = nullptr;
+  void *xtmp = nullptr;       // coarsest-level temporary between l and l_t (SPD kind)
   std::vector<void *> y, xin, xout;  // y_l (pre out), x_l inputs (l >= 1), post outputs (l >= 1)
   float *coef = nullptr;      // c0[0..L-1], c1[0..L-1]
   uint8_t *fmask = nullptr;   // fluid mask of level 0
@@ -1089,6 +1224,11 @@ static KT *kgen_rec_type(void (*)(const float *, int, int, int, const float *, i
                                   const uint32_t *, const uint32_t *, const uint32_t *, const uint32_t *,
                                   const uint32_t *, KT *, KT *));
 
+// blocks with uniform vectors / material records: 2L + 1, plus l_t for the SPD kind
+static int uniform_blocks(const PrecondPlan &P) {
+  return 2 * P.L + 1 + (P.kind == MLPCG_PRECOND_SMALL_SPD ? 1 : 0);
+}
+
 static size_t plan_layout(PrecondPlan &P, char *base) {
   size_t off = 0;
   auto take = [&](size_t b) -> void * {
@@ -1114,6 +1254,8 @@ static size_t plan_layout(PrecondPlan &P, char *base) {
     P.Kpost[l] = take(kbytes(l));
   }
   P.Kl = take(kbytes(P.L));
+  const bool spd = P.kind == MLPCG_PRECOND_SMALL_SPD;
+  P.Klt = spd ? take(kbytes(P.L)) : nullptr;
   P.Upre.assign(P.L, nullptr);
   P.Upost.assign(P.L, nullptr);
   P.cls.assign(P.L + 1, nullptr);
@@ -1122,15 +1264,18 @@ static size_t plan_layout(PrecondPlan &P, char *base) {
   P.rbase.assign(P.L + 1, nullptr);
   P.gcount.assign(P.L + 1, nullptr);
   P.gbase.assign(P.L + 1, nullptr);
-  // uniform vectors of all 2L + 1 blocks (block b at U + 3 KREC b, the parameter block order)
-  float *U = (float *)take((size_t)(2 * P.L + 1) * 3 * KREC * sizeof(float));
+  // uniform vectors of all blocks (block b at U + 3 KREC b): pre[0..L-1], post[0..L-1], l
+  // (the parameter block order), and for the SPD kind l_t after l
+  const int nU = uniform_blocks(P);
+  float *U = (float *)take((size_t)nU * 3 * KREC * sizeof(float));
   for (int l = 0; l < P.L; ++l) {
     P.Upre[l] = U + (size_t)l * 3 * KREC;
     P.Upost[l] = U + (size_t)(P.L + l) * 3 * KREC;
   }
   P.Ul = U + (size_t)2 * P.L * 3 * KREC;
+  P.Ult = spd ? U + (size_t)(2 * P.L + 1) * 3 * KREC : nullptr;
   P.Uall = U;
-  P.Mrec = take((size_t)(2 * P.L + 1) * 3 * RREC * sk);
+  P.Mrec = take((size_t)nU * 3 * RREC * sk);
   int64_t nlist = 0;
   for (int l = 0; l <= P.L; ++l) {
     const auto &v = P.lv[l];
@@ -1143,6 +1288,22 @@ static size_t plan_layout(PrecondPlan &P, char *base) {
     P.gbase[l] = (uint32_t *)take(v.ntiles * sizeof(uint32_t));
     nlist = std::max<int64_t>(nlist, v.n);
   }
+  P.clsT.assign(P.L + 1, nullptr);
+  P.rwT.assign(P.L + 1, nullptr);
+  P.rcountT.assign(P.L + 1, nullptr);
+  P.rbaseT.assign(P.L + 1, nullptr);
+  P.gcountT.assign(P.L + 1, nullptr);
+  P.gbaseT.assign(P.L + 1, nullptr);
+  for (int l = 0; spd && l <= P.L; ++l) {
+    const auto &v = P.lv[l];
+    if (!v.cls) continue;
+    P.clsT[l] = (uint8_t *)take(v.ps);
+    P.rwT[l] = (uint32_t *)take((v.n / 8) * sizeof(uint32_t));
+    P.rcountT[l] = (uint32_t *)take(v.ntiles * sizeof(uint32_t));
+    P.rbaseT[l] = (uint32_t *)take(v.ntiles * sizeof(uint32_t));
+    P.gcountT[l] = (uint32_t *)take(v.ntiles * sizeof(uint32_t));
+    P.gbaseT[l] = (uint32_t *)take(v.ntiles * sizeof(uint32_t));
+  }
   // general-cell and mixed-run lists of one level at a time (setup only)
   P.glist = nlist ? (uint32_t *)take((size_t)nlist * sizeof(uint32_t)) : nullptr;
   P.rlist = nlist ? (uint32_t *)take((size_t)(nlist / 8 + 1) * sizeof(uint32_t)) : nullptr;
@@ -1151,8 +1312,9 @@ static size_t plan_layout(PrecondPlan &P, char *base) {
     P.xin[l] = take(P.lv[l].ps * sa);
     P.xout[l] = take(P.lv[l].ps * sa);
   }
-  // the finest level's prolongated input (fast path only)
+  // the finest level's prolongated input (fast path only; the SPD kind uses it on every level)
   P.ufine = P.lv[0].fast ? take(P.lv[0].ps * sa) : nullptr;
+  P.xtmp = spd ? take(P.lv[P.L].ps * sa) : nullptr;
   P.coef = (float *)take(2 * P.L * sizeof(float));
   P.fmask = (uint8_t *)take(P.lv[0].ps + 64);
   P.lin_ws = take(linear_workspace());
@@ -1187,6 +1349,16 @@ static CoefArgs<KT> coef_args(const PrecondPlan &P, int l, void *K, float *uni) 
   C.rw = P.rw[l];
   C.rbase = P.rbase[l];
   C.rcount = P.rcount[l];
+  return C;
+}
+
+// a transposed block of the SPD kind: its own run words and tile counts
+template <typename KT>
+static CoefArgs<KT> coef_args_t(const PrecondPlan &P, int l, void *K, float *uni) {
+  CoefArgs<KT> C = coef_args<KT>(P, l, K, uni);
+  C.rw = P.rwT[l];
+  C.rbase = P.rbaseT[l];
+  C.rcount = P.rcountT[l];
   return C;
 }
 
@@ -1244,20 +1416,34 @@ static int run_apply(const PrecondPlan &P, const float *r, const float *rscale, 
       RET_IF(launch_avg_pool2(P.y[l], P.xin[l + 1], P.adt, 1, v.n1, v.n2, v.n3, st));
     }
   }
-  // ---- coarsest block
+  // ---- coarsest block (SPD kind: l into xtmp, then l_t)
+  const bool spd = P.kind == MLPCG_PRECOND_SMALL_SPD;
   if (L >= s0 && L <= s1) {
     const auto &v = P.lv[L];
+    AT *cdst = (AT *)(spd ? P.xtmp : P.xout[L]);
     if (v.fast) {
       const CoefArgs<KT> C = coef_args<KT>(P, L, P.Kl, v.cls ? P.Ul : nullptr);
       if (v.cls)
         k_pre_fused<KT, AT, AT, false, true><<<grid_of(v), PT, 0, st>>>(
-            C, (const AT *)P.xin[L], nullptr, (AT *)P.xout[L], nullptr, nullptr, v.n1, v.n2, v.n3, gate);
+            C, (const AT *)P.xin[L], nullptr, cdst, nullptr, nullptr, v.n1, v.n2, v.n3, gate);
       else
         k_pre_fused<KT, AT, AT, false, false><<<grid_of(v), PT, 0, st>>>(
-            C, (const AT *)P.xin[L], nullptr, (AT *)P.xout[L], nullptr, nullptr, v.n1, v.n2, v.n3, gate);
+            C, (const AT *)P.xin[L], nullptr, cdst, nullptr, nullptr, v.n1, v.n2, v.n3, gate);
       MLPCG_LAUNCH_CHECK();
+      if (spd) {
+        const CoefArgs<KT> Ct = coef_args_t<KT>(P, L, P.Klt, v.cls ? P.Ult : nullptr);
+        if (v.cls)
+          k_pre_fused<KT, AT, AT, false, true><<<grid_of(v), PT, 0, st>>>(
+              Ct, (const AT *)P.xtmp, nullptr, (AT *)P.xout[L], nullptr, nullptr, v.n1, v.n2, v.n3, gate);
+        else
+          k_pre_fused<KT, AT, AT, false, false><<<grid_of(v), PT, 0, st>>>(
+              Ct, (const AT *)P.xtmp, nullptr, (AT *)P.xout[L], nullptr, nullptr, v.n1, v.n2, v.n3, gate);
+        MLPCG_LAUNCH_CHECK();
+      }
     } else {
-      RET_IF(launch_stencil_apply(P.Kl, P.kdt, v.ps, P.xin[L], P.adt, 0, P.xout[L], P.adt, 1, v.n1, v.n2, v.n3, 0, st));
+      RET_IF(launch_stencil_apply(P.Kl, P.kdt, v.ps, P.xin[L], P.adt, 0, cdst, P.adt, 1, v.n1, v.n2, v.n3, 0, st));
+      if (spd)
+        RET_IF(launch_stencil_apply(P.Kl, P.kdt, v.ps, P.xtmp, P.adt, 0, P.xout[L], P.adt, 1, v.n1, v.n2, v.n3, 1, st));
     }
   }
   // ---- up sweep
@@ -1267,6 +1453,39 @@ static int run_apply(const PrecondPlan &P, const float *r, const float *rscale, 
     const float *c0 = P.coef + l, *c1 = P.coef + L + l;
     const uint8_t *bm = (l == 0) ? m0 : nullptr;
     const uint8_t *om = (l == 0) ? P.fmask : nullptr;
+    if (spd) {
+      // u = c0^2 y_l + c1^2 (nearest x2 / 8)(x_{l+1}) (coef holds the squares), then the
+      // transposed block l0_t on u (sm_model_3d.py:436-443)
+      if (v.fast) {
+        const CoefArgs<KT> C = coef_args_t<KT>(P, l, P.Kpost[l], v.cls ? P.Upost[l] : nullptr);
+        const dim3 g = grid_of(v);
+        AT *u = (AT *)P.ufine;
+        k_up_fine<AT, AT, AT, true, true><<<g, PT, 0, st>>>((const AT *)P.xout[l + 1], (const AT *)P.y[l], c0, c1, u,
+                                                             v.n1, v.n2, v.n3, gate);
+        MLPCG_LAUNCH_CHECK();
+        if (l == 0) {
+          if (v.cls) k_post_fused<KT, AT, AT, float, true, true, true><<<g, PT, 0, st>>>(C, u, (const AT *)P.y[0], c0, c1, z, nullptr, om, v.n1, v.n2, v.n3, gate);
+          else k_post_fused<KT, AT, AT, float, true, false, true><<<g, PT, 0, st>>>(C, u, (const AT *)P.y[0], c0, c1, z, nullptr, om, v.n1, v.n2, v.n3, gate);
+        } else {
+          AT *o = (AT *)P.xout[l];
+          if (v.cls) k_post_fused<KT, AT, AT, AT, true, true, true><<<g, PT, 0, st>>>(C, u, (const AT *)P.y[l], c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3, gate);
+          else k_post_fused<KT, AT, AT, AT, true, false, true><<<g, PT, 0, st>>>(C, u, (const AT *)P.y[l], c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3, gate);
+        }
+        MLPCG_LAUNCH_CHECK();
+      } else {
+        void *up = tmp0;
+        void *dst = (l == 0) ? (void *)z : P.xout[l];
+        const int ddt = (l == 0) ? MLPCG_F32 : P.adt;
+        RET_IF(launch_avg_pool2_adjoint(P.xout[l + 1], up, P.adt, 1, v.n1, v.n2, v.n3, st));
+        RET_IF(launch_axpby(c0, P.y[l], c1, up, up, P.adt, v.n, st));
+        RET_IF(launch_stencil_apply(P.Kpre[l], P.kdt, v.ps, up, P.adt, 0, dst, ddt, 1, v.n1, v.n2, v.n3, 1, st));
+        if (l == 0) {
+          k_apply_mask<float><<<blocks_for(v.n, 256), 256, 0, st>>>((float *)dst, P.fmask, v.n);
+          MLPCG_LAUNCH_CHECK();
+        }
+      }
+      continue;
+    }
     if (v.fast) {
       const CoefArgs<KT> C = coef_args<KT>(P, l, P.Kpost[l], v.cls ? P.Upost[l] : nullptr);
       const AT *xc = (const AT *)P.xout[l + 1], *yl = (const AT *)P.y[l];
@@ -1354,9 +1573,8 @@ int precond_apply_gated(const mlpcg_precond *h, const float *r, const float *r_s
 
 extern "C" {
 
-int mlpcg_precond_create(int N1, int N2, int N3, int levels, int k_dtype, int act_dtype,
-                         int swap_sm_order, int mask, int coeff_layout, mlpcg_precond **out) {
-  clear_error();
+static int precond_create(int N1, int N2, int N3, int levels, int k_dtype, int act_dtype, int swap_sm_order,
+                          int mask, int coeff_layout, int kind, mlpcg_precond **out) {
   MLPCG_REQUIRE(out != nullptr, MLPCG_ERR_ARG, "out must not be NULL");
   *out = nullptr;
   MLPCG_REQUIRE(levels >= 1 && levels <= 12, MLPCG_ERR_ARG, "levels %d out of [1, 12]", levels);
@@ -1376,6 +1594,7 @@ int mlpcg_precond_create(int N1, int N2, int N3, int levels, int k_dtype, int ac
   P.n1 = N1; P.n2 = N2; P.n3 = N3; P.L = levels;
   P.kdt = k_dtype; P.adt = act_dtype; P.swap = swap_sm_order ? 1 : 0; P.mask = mask ? 1 : 0;
   P.layout = coeff_layout;
+  P.kind = kind;
   for (int l = 0; l <= levels; ++l) {
     PrecondPlan::Level v;
     v.n1 = N1 >> l; v.n2 = N2 >> l; v.n3 = N3 >> l;
@@ -1394,6 +1613,19 @@ int mlpcg_precond_create(int N1, int N2, int N3, int levels, int k_dtype, int ac
   return MLPCG_OK;
 }
 
+int mlpcg_precond_create(int N1, int N2, int N3, int levels, int k_dtype, int act_dtype,
+                         int swap_sm_order, int mask, int coeff_layout, mlpcg_precond **out) {
+  clear_error();
+  return precond_create(N1, N2, N3, levels, k_dtype, act_dtype, swap_sm_order, mask, coeff_layout,
+                        MLPCG_PRECOND_SM, out);
+}
+
+int mlpcg_precond_create_spd(int N1, int N2, int N3, int levels, int k_dtype, int act_dtype, int coeff_layout,
+                             mlpcg_precond **out) {
+  clear_error();
+  return precond_create(N1, N2, N3, levels, k_dtype, act_dtype, 0, 0, coeff_layout, MLPCG_PRECOND_SMALL_SPD, out);
+}
+
 size_t mlpcg_precond_workspace(const mlpcg_precond *h) { return h ? h->p.bytes : 0; }
 
 void mlpcg_precond_destroy(mlpcg_precond *h) { delete h; }
@@ -1409,10 +1641,13 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
   cudaStream_t st = as_stream(stream);
   plan_layout(P, (char *)workspace);
   const int L = P.L;
-  // parameter offsets: pre[0..L-1], post[0..L-1], l (2214 each), c0[0..L-1], c1[0..L-1] (82 each)
+  // parameter offsets: pre[0..L-1], post[0..L-1], l (2214 each), c0[0..L-1], c1[0..L-1] (82 each);
+  // SPD kind: l0[0..L-1], l, then the linear blocks
+  const bool spd = P.kind == MLPCG_PRECOND_SMALL_SPD;
+  const int nblk = spd ? L + 1 : 2 * L + 1;
   auto blk_w = [&](int b) { return params + (size_t)b * 2214; };
   auto blk_b = [&](int b) { return params + (size_t)b * 2214 + 2187; };
-  const float *linp = params + (size_t)(2 * L + 1) * 2214;
+  const float *linp = params + (size_t)nblk * 2214;
   // image pyramid
   for (int l = 1; l <= L; ++l) {
     const auto &v = P.lv[l - 1];
@@ -1426,23 +1661,26 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
   for (int l = 0; l <= L; ++l) any_cls = any_cls || P.lv[l].cls;
   if (any_cls) {
     if (P.kdt == MLPCG_BF16) {
-      k_kgen_uniform_all<__nv_bfloat16><<<2 * L + 1, 3 * KREC, 0, st>>>(params, P.Uall);
-      k_material_records<__nv_bfloat16><<<2 * L + 1, 256, 0, st>>>(P.Uall, (__nv_bfloat16 *)P.Mrec);
+      k_kgen_uniform_all<__nv_bfloat16><<<nblk, 3 * KREC, 0, st>>>(params, P.Uall, spd ? L : 0);
+      k_material_records<__nv_bfloat16><<<uniform_blocks(P), 256, 0, st>>>(P.Uall, (__nv_bfloat16 *)P.Mrec);
     } else {
-      k_kgen_uniform_all<float><<<2 * L + 1, 3 * KREC, 0, st>>>(params, P.Uall);
-      k_material_records<float><<<2 * L + 1, 256, 0, st>>>(P.Uall, (float *)P.Mrec);
+      k_kgen_uniform_all<float><<<nblk, 3 * KREC, 0, st>>>(params, P.Uall, spd ? L : 0);
+      k_material_records<float><<<uniform_blocks(P), 256, 0, st>>>(P.Uall, (float *)P.Mrec);
     }
     MLPCG_LAUNCH_CHECK();
   }
-  // one level's blocks b0 (and b1 >= 0): dense planes, or class map + general-cell records
-  auto gen_level = [&](int l, const float *im, int b0, void *K0, int b1, void *K1) -> int {
+  // one level's blocks b0 (and b1 >= 0): dense planes, or class map + general-cell records;
+  // their uniform vectors in slots u0s (and u1s), by default the block indices
+  auto gen_level = [&](int l, const float *im, int b0, void *K0, int b1, void *K1, int u0s = -1,
+                       int u1s = -1) -> int {
     const auto &v = P.lv[l];
     if (!v.cls) {
       RET_IF(launch_stencil_gen(im, 0, v.n1, v.n2, v.n3, blk_w(b0), blk_b(b0), K0, P.kdt, v.ps, st));
       if (b1 >= 0) RET_IF(launch_stencil_gen(im, 0, v.n1, v.n2, v.n3, blk_w(b1), blk_b(b1), K1, P.kdt, v.ps, st));
       return MLPCG_OK;
     }
-    k_classify<<<grid_of(v), PT, 0, st>>>(im, v.n1, v.n2, v.n3, P.cls[l], P.rw[l], P.rcount[l], P.gcount[l]);
+    k_classify<false><<<grid_of(v), PT, 0, st>>>(im, nullptr, v.n1, v.n2, v.n3, P.cls[l], P.rw[l], P.rcount[l],
+                                                 P.gcount[l]);
     MLPCG_LAUNCH_CHECK();
     k_scan_tiles<<<1, 1024, 0, st>>>(P.rcount[l], P.rbase[l], (int)v.ntiles);
     MLPCG_LAUNCH_CHECK();
@@ -1453,7 +1691,9 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
     MLPCG_LAUNCH_CHECK();
     // general cells: one wave of CTAs (as many as fit on every SM), each looping over its share
     const uint32_t *lb = P.gbase[l] + v.ntiles - 1, *lc = P.gcount[l] + v.ntiles - 1;
-    const float *u0 = P.Uall + (size_t)b0 * 3 * KREC, *u1 = P.Uall + (size_t)(b1 >= 0 ? b1 : b0) * 3 * KREC;
+    if (u0s < 0) u0s = b0;
+    if (u1s < 0) u1s = b1 >= 0 ? b1 : b0;
+    const float *u0 = P.Uall + (size_t)u0s * 3 * KREC, *u1 = P.Uall + (size_t)u1s * 3 * KREC;
     const int fgrid = (int)std::min<int64_t>((int64_t)sm_count() * 8, (v.n + 255) / 256);
     const uint32_t *rlb = P.rbase[l] + v.ntiles - 1, *rlc = P.rcount[l] + v.ntiles - 1;
     auto launch = [&](auto kern, auto fill, const void *r0, const void *r1) {
@@ -1474,8 +1714,64 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
     MLPCG_LAUNCH_CHECK();
     return MLPCG_OK;
   };
-  for (int l = 0; l < L; ++l) RET_IF(gen_level(l, (l == 0) ? image : P.img[l], l, P.Kpre[l], L + l, P.Kpost[l]));
-  RET_IF(gen_level(L, P.img[L], 2 * L, P.Kl, -1, nullptr));
+  // the transposed block of forward block (Kf, uniform slot uf) at level l into Kt (slot ut): on
+  // a classed level the class map of the neighbourhoods, then its general cells gathered from
+  // the forward records and its mixed runs' uniform cells; on a dense tiled level the planes
+  // gathered; a general-path level applies the forward planes transposed and needs nothing
+  auto gen_transpose = [&](int l, void *Kf, int uf, void *Kt, int ut) -> int {
+    const auto &v = P.lv[l];
+    if (!v.fast) return MLPCG_OK;
+    if (!v.cls) {
+      if (P.kdt == MLPCG_BF16)
+        k_planes_transpose<__nv_bfloat16><<<blocks_for(v.n, 256), 256, 0, st>>>(
+            (const __nv_bfloat16 *)Kf, (__nv_bfloat16 *)Kt, v.ps, v.n1, v.n2, v.n3);
+      else
+        k_planes_transpose<float><<<blocks_for(v.n, 256), 256, 0, st>>>((const float *)Kf, (float *)Kt, v.ps, v.n1,
+                                                                       v.n2, v.n3);
+      MLPCG_LAUNCH_CHECK();
+      return MLPCG_OK;
+    }
+    k_classify<true><<<grid_of(v), PT, 0, st>>>(nullptr, P.cls[l], v.n1, v.n2, v.n3, P.clsT[l], P.rwT[l],
+                                                P.rcountT[l], P.gcountT[l]);
+    MLPCG_LAUNCH_CHECK();
+    k_scan_tiles<<<1, 1024, 0, st>>>(P.rcountT[l], P.rbaseT[l], (int)v.ntiles);
+    MLPCG_LAUNCH_CHECK();
+    k_scan_tiles<<<1, 1024, 0, st>>>(P.gcountT[l], P.gbaseT[l], (int)v.ntiles);
+    MLPCG_LAUNCH_CHECK();
+    k_list_general<<<grid_of(v), PT, 0, st>>>(P.clsT[l], v.n1, v.n2, v.n3, P.gbaseT[l], P.glist, P.rwT[l],
+                                              P.rbaseT[l], P.rlist);
+    MLPCG_LAUNCH_CHECK();
+    const uint32_t *lb = P.gbaseT[l] + v.ntiles - 1, *lc = P.gcountT[l] + v.ntiles - 1;
+    const uint32_t *rlb = P.rbaseT[l] + v.ntiles - 1, *rlc = P.rcountT[l] + v.ntiles - 1;
+    const float *kf = P.Uall + (size_t)uf * 3 * KREC, *kt = P.Uall + (size_t)ut * 3 * KREC;
+    const int fgrid = (int)std::min<int64_t>((int64_t)sm_count() * 8, (v.n + 255) / 256);
+    auto launch = [&](auto kern, auto fill, auto *kf_rec, auto *kt_rec) {
+      const int grid = (int)std::min<int64_t>((int64_t)sm_count() * resident_ctas(kern), (v.n + PT - 1) / PT);
+      kern<<<grid, PT, 0, st>>>(v.n1, v.n2, v.n3, P.glist, lb, lc, P.cls[l], P.rw[l], P.rbase[l], P.rcount[l], kf_rec,
+                                kf, P.rwT[l], P.rbaseT[l], P.rcountT[l], kt_rec);
+      fill<<<fgrid, 256, 0, st>>>(P.clsT[l], P.rlist, rlb, rlc, P.rwT[l], P.rbaseT[l], P.rcountT[l], v.n1, v.n2, v.n3,
+                                  kt, kt, kt_rec, kt_rec);
+    };
+    if (P.kdt == MLPCG_BF16)
+      launch(k_kgen_t_list<__nv_bfloat16>, k_fill_uniform<__nv_bfloat16, 1>, (const __nv_bfloat16 *)Kf,
+             (__nv_bfloat16 *)Kt);
+    else
+      launch(k_kgen_t_list<float>, k_fill_uniform<float, 1>, (const float *)Kf, (float *)Kt);
+    MLPCG_LAUNCH_CHECK();
+    return MLPCG_OK;
+  };
+  if (spd) {
+    // l0[l] forward (slot l) and transposed (slot L + l); l forward (slot 2L) and transposed (2L + 1)
+    for (int l = 0; l < L; ++l) {
+      RET_IF(gen_level(l, (l == 0) ? image : P.img[l], l, P.Kpre[l], -1, nullptr));
+      RET_IF(gen_transpose(l, P.Kpre[l], l, P.Kpost[l], L + l));
+    }
+    RET_IF(gen_level(L, P.img[L], L, P.Kl, -1, nullptr, 2 * L));
+    RET_IF(gen_transpose(L, P.Kl, 2 * L, P.Klt, 2 * L + 1));
+  } else {
+    for (int l = 0; l < L; ++l) RET_IF(gen_level(l, (l == 0) ? image : P.img[l], l, P.Kpre[l], L + l, P.Kpost[l]));
+    RET_IF(gen_level(L, P.img[L], 2 * L, P.Kl, -1, nullptr));
+  }
   // c0 / c1 of every level (the linear blocks of sm_model_3d.py:236-239)
   for (int l = 0; l < L; ++l) {
     const auto &v = P.lv[l];
@@ -1484,6 +1780,10 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
     const float *w0 = linp + (size_t)l * 82;
     RET_IF(launch_linear_forward_strided(im, v.n1, v.n2, v.n3, w0, (int64_t)L * 82, w0 + 81, (int64_t)L * 82, 2,
                                          P.coef + l, L, nullptr, P.lin_ws, linear_workspace(), st));
+  }
+  if (spd) {
+    k_square<<<1, 64, 0, st>>>(P.coef, 2 * L);
+    MLPCG_LAUNCH_CHECK();
   }
   P.ready = true;
   return MLPCG_OK;

@@ -1,5 +1,6 @@
-"""PrecondPlan: SmallSMModelDn3D.eval_forward with every block's coefficients
-precomputed once per (image, weights) and fused level kernels.
+"""PrecondPlan: SmallSMModelDn3D.eval_forward (or SmallSPDSMModelDn3D's) with
+every block's coefficients precomputed once per (image, weights) and fused
+level kernels.
 
 The reference re-evaluates each block's 27 coefficients from the image inside
 every call (sm_block_3d_kernel.cu:45-65) and caches only the image pyramid and
@@ -20,21 +21,32 @@ from .ops import _check, _p, _stream
 _DT = {torch.float32: F32, torch.bfloat16: BF16}
 
 
+def _is_small_spd(model) -> bool:
+    from .sm_model_3d import SmallSPDSMModelDn3D
+    return isinstance(model, SmallSPDSMModelDn3D)
+
+
 def pack_params(model) -> torch.Tensor:
-    """Flat F32 parameter vector in the order mlpcg_precond_setup expects."""
+    """Flat F32 parameter vector in the order mlpcg_precond_setup expects: blocks pre, post, l
+    (SmallSPDSMModelDn3D: l0, l), then the linear blocks c0, c1."""
     n = model.n
+    blocks = list(model.l0) + [model.l] if _is_small_spd(model) else list(model.pre) + list(model.post) + [model.l]
     parts = []
-    for blk in list(model.pre) + list(model.post) + [model.l]:
+    for blk in blocks:
         parts += [blk.weight.detach().reshape(-1), blk.bias.detach().reshape(-1)]
     for lin in list(model.c0) + list(model.c1):
         parts += [lin.weight.detach().reshape(-1), lin.bias.detach().reshape(-1)]
     flat = torch.cat([p.float() for p in parts]).contiguous()
-    assert flat.numel() == (2 * n + 1) * 2214 + 2 * n * 82
+    assert flat.numel() == len(blocks) * 2214 + 2 * n * 82
     return flat
 
 
 class PrecondPlan:
-    """z = M r for one image; ``apply`` is graph-capturable (no host sync, no allocation with ``out``)."""
+    """z = M r for one image; ``apply`` is graph-capturable (no host sync, no allocation with ``out``).
+
+    ``model`` is a SmallSMModelDn3D or a SmallSPDSMModelDn3D (M = S^T S, for
+    textbook PCG); ``coefficients()`` returns c0, c1 (the squares for the SPD
+    network)."""
 
     LAYOUTS = {"dense": 0, "classed": 1}
 
@@ -46,12 +58,17 @@ class PrecondPlan:
         self.shape = tuple(int(s) for s in image.shape[1:])
         self.levels = model.n
         self.storage, self.act_storage, self.layout = storage, act_storage, layout
-        self.masked = bool(model.pre[0].mask)
+        self.spd = _is_small_spd(model)
+        self.masked = False if self.spd else bool(model.pre[0].mask)
         self.device = image.device
         lib = _lib.load()
         h = C.c_void_p()
-        call("mlpcg_precond_create", *self.shape, model.n, _DT[storage], _DT[act_storage],
-             int(bool(model.swap_ord)), int(bool(model.pre[0].mask)), self.LAYOUTS[layout], C.byref(h))
+        if self.spd:
+            call("mlpcg_precond_create_spd", *self.shape, model.n, _DT[storage], _DT[act_storage],
+                 self.LAYOUTS[layout], C.byref(h))
+        else:
+            call("mlpcg_precond_create", *self.shape, model.n, _DT[storage], _DT[act_storage],
+                 int(bool(model.swap_ord)), int(bool(model.pre[0].mask)), self.LAYOUTS[layout], C.byref(h))
         self._h = h
         self._lib = lib
         nbytes = lib.mlpcg_precond_workspace(h)

@@ -1,8 +1,9 @@
-"""Drop-in for the reference's sm_model_3d.py: autograd Functions, blocks and SmallSMModelDn3D.
+"""Drop-in for the reference's sm_model_3d.py: autograd Functions, blocks,
+SmallSMModelDn3D and the symmetric networks SPDSMModelDn3D / SmallSPDSMModelDn3D.
 
 Class names, constructor signatures, forward / eval_forward signatures and
 parameter names (state-dict keys) are those of the reference
-(sm_model_3d.py:21-287), so reference checkpoints load unchanged
+(sm_model_3d.py:21-444), so reference checkpoints load unchanged
 (``model.load_state_dict(torch.load(f)['model_state_dict'])``).  Every
 numerical step runs in the sm_103a kernels of ``libmlpcg_gb300.so``:
 
@@ -500,3 +501,9 @@ class SmallSPDSMModelDn3D(BaseModel):
         SPDSMModelDn3D.eval_forward."""
         return self._run(image, b, _Steps(False), [] if imgs is None else imgs,
                          [] if c0 is None else c0, [] if c1 is None else c1)
+
+    def precond_plan(self, image, storage=torch.bfloat16, act_storage=None):
+        """Coefficients of every block (and of its transpose) precomputed on ``image``:
+        see precond.PrecondPlan."""
+        from .precond import PrecondPlan
+        return PrecondPlan(self, image, storage=storage, act_storage=act_storage)

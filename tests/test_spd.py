@@ -192,3 +192,106 @@ def test_solver_histories_vs_reference(golden, cuda, fname, cls, fwd):
         _, _, hist_o = getattr(ocg, name)(d["rhs"].ravel()[fluid], Ao, np.zeros(fluid.size), pred_o, 30,
                                           tol=1e-6, atol=1e-20)
         np.testing.assert_allclose(np.array(hist[:20]), np.array(hist_o[:20]), rtol=1e-4)
+
+
+# ---------------------------------------------------------------------------- fused plan (GPU)
+def _spd_model(n, dev, seed=0, eps=0.05):
+    """A SmallSPDSMModelDn3D with small random weights around the identity stencil."""
+    from mlpcg_gb300.sm_model_3d import SmallSPDSMModelDn3D
+    torch.manual_seed(seed)
+    m = SmallSPDSMModelDn3D(n).to(dev)
+    with torch.no_grad():
+        for p in m.parameters():
+            p.mul_(eps)
+        for blk in list(m.l0) + [m.l]:
+            blk.bias[13] += 1.0
+        for c in m.c0:
+            c.bias[0] += 1.0
+    return m
+
+
+def _scene(shape, seed, dev):
+    from mlpcg_gb300.scenes import make_scene
+    s = make_scene(shape, seed)
+    return s, torch.as_tensor(s.flags, device=dev), torch.as_tensor(s.image(), device=dev)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape,n", [((16, 16, 16), 3), ((32, 16, 24), 3), ((64, 64, 64), 4), ((24, 40, 8), 3)])
+def test_plan_matches_eval_forward(cuda, shape, n):
+    """The fused plan (transposed blocks gathered from the forward coefficients, nearest x2 / 8
+    prolongation fused into the combine) against the drop-in eval_forward on the fluid cells."""
+    s, flags, img = _scene(shape, 2, cuda)
+    torch.manual_seed(1)
+    from mlpcg_gb300.sm_model_3d import SmallSPDSMModelDn3D
+    m = SmallSPDSMModelDn3D(n).to(cuda)
+    plan = m.precond_plan(img, storage=torch.float32)
+    b = torch.randn((1, 1) + shape, device=cuda)
+    ref = m.eval_forward(img, b)
+    ref = torch.where(img[1] == 0, 0.0, ref)
+    z = plan.apply(b.reshape(-1)).reshape(ref.shape)
+    assert rel_err(z.cpu().numpy(), ref.cpu().numpy()) < 1e-5
+    c = plan.coefficients()
+    imgs = [img]
+    from mlpcg_gb300 import ops
+    for l in range(n):
+        c0 = float(m.c0[l].eval_forward(imgs[l]))
+        assert abs(float(c[l]) - c0 * c0) <= 1e-6 * max(1.0, c0 * c0)
+        imgs.append(ops.avg_pool2(imgs[-1]))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape,n,seed", [((64, 64, 64), 4, 4), ((32, 48, 64), 3, 9), ((128, 128, 128), 5, 7)])
+@pytest.mark.parametrize("storage", [torch.float32, torch.bfloat16])
+def test_plan_classed_is_bit_identical_to_dense(cuda, shape, n, seed, storage):
+    """The transposed blocks' classed records (radius-2 classes, gathered general cells) give
+    exactly the dense transposed planes' output."""
+    from mlpcg_gb300.precond import PrecondPlan
+    s, flags, img = _scene(shape, seed, cuda)
+    m = _spd_model(n, cuda, seed=3)
+    dense = PrecondPlan(m, img, storage=storage, layout="dense")
+    cls = PrecondPlan(m, img, storage=storage, layout="classed")
+    n0 = int(np.prod(shape))
+    b = torch.randn(n0, device=cuda)
+    scale = torch.tensor([0.5], device=cuda)
+    zd = dense.apply(b, scale)
+    zc = cls.apply(b, scale)
+    assert torch.equal(zd, zc), float((zd - zc).abs().max())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("layout", ["classed", "dense"])
+def test_plan_operator_is_symmetric(cuda, layout):
+    """On fluid-supported vectors the plan's z = D M D r is symmetric positive definite."""
+    from mlpcg_gb300.precond import PrecondPlan
+    shape = (64, 64, 64)
+    s, flags, img = _scene(shape, 5, cuda)
+    m = _spd_model(4, cuda, seed=2, eps=0.2)
+    plan = PrecondPlan(m, img, storage=torch.float32, layout=layout)
+    fluid = (img[1] != 0).reshape(-1)
+    g = torch.Generator(device=cuda).manual_seed(0)
+    x = torch.randn(fluid.numel(), device=cuda, generator=g) * fluid
+    y = torch.randn(fluid.numel(), device=cuda, generator=g) * fluid
+    a = torch.dot(x.double(), plan.apply(y).double())
+    b = torch.dot(y.double(), plan.apply(x).double())
+    assert abs(float(a - b)) <= 1e-5 * float(torch.sqrt(a.abs() * b.abs())), (float(a), float(b))
+    assert float(torch.dot(x.double(), plan.apply(x).double())) > 0.0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("storage", [torch.float32, torch.bfloat16])
+def test_fused_npcg_with_spd_network(cuda, storage):
+    """Textbook PCG (npcg) in the graph-captured solver with the symmetric network converges, and
+    its FP64 residual against the oracle's matrix meets the tolerance."""
+    from mlpcg_gb300.solver import FusedSolver
+    shape = (64, 64, 64)
+    s, flags, img = _scene(shape, 3, cuda)
+    m = _spd_model(4, cuda, seed=4)
+    solver = FusedSolver(m, flags, method="npcg", max_it=500, tol=1e-6, storage=storage)
+    b = torch.as_tensor(s.rhs, device=cuda)
+    res = solver.solve(b)
+    assert res.status == "converged", res
+    A, fluid = olap.assemble(s.flags)
+    x = res.x.reshape(-1).cpu().numpy()[fluid]
+    rhs = s.rhs.reshape(-1)[fluid]
+    assert np.linalg.norm(rhs - A @ x) / np.linalg.norm(rhs) < 2e-6
