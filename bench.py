@@ -22,6 +22,11 @@ flushed between steps.  Also reported:
                   CSR npsd) on this host, a bounded sample of iterations,
                   extrapolated to the iteration count of the solve.
 
+``--model small_spd`` runs the same harness on the symmetric network
+SmallSPDSMModelDn3D (default solver npcg, textbook PCG; weights
+smallspd_l<n>.npz when present); its CPU path is the same torch-CPU blocks
+composed as that network with the reference's npcg.
+
 ``--impl reference`` times only that CPU path and prints its own line.
 Multi-GPU (``--gpus N`` under torchrun): N independent replicas, one scene
 per rank, no collective in the solve; the reported time is the max over ranks.
@@ -58,7 +63,9 @@ def parse():
     ap.add_argument("--levels", type=int, default=5)
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--spheres", type=int, default=6)
-    ap.add_argument("--method", default="npsd", choices=["npsd", "npcg"])
+    ap.add_argument("--model", default="smallsm", choices=["smallsm", "small_spd"])
+    ap.add_argument("--method", default=None, choices=["npsd", "npcg"],
+                    help="default: npsd (smallsm), npcg (small_spd)")
     ap.add_argument("--max-it", type=int, default=100)
     ap.add_argument("--tol", type=float, default=1e-6)
     ap.add_argument("--weights", default=None, help="npz state dict (default: committed trained weights)")
@@ -68,21 +75,31 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-graph", action="store_true",
                     help="plain launches of the same kernels with a host check per iteration (for profilers)")
-    return ap.parse_args()
+    args = ap.parse_args()
+    if args.method is None:
+        args.method = "npcg" if args.model == "small_spd" else "npsd"
+    return args
+
+
+MODEL_NAMES = {"smallsm": "SmallSMModelDn3D", "small_spd": "SmallSPDSMModelDn3D"}
 
 
 def weights_path(args):
     if args.weights:
         return Path(args.weights)
-    p = WEIGHTS_DIR / f"smallsm_l{args.levels}.npz"
+    prefix = "smallspd" if args.model == "small_spd" else "smallsm"
+    p = WEIGHTS_DIR / f"{prefix}_l{args.levels}.npz"
     return p if p.exists() else None
 
 
 def load_model(args, device):
     import torch
-    from mlpcg_gb300.sm_model_3d import SmallSMModelDn3D
+    from mlpcg_gb300.sm_model_3d import SmallSMModelDn3D, SmallSPDSMModelDn3D
     torch.manual_seed(0)
-    m = SmallSMModelDn3D(args.levels, 3, "trilinear")
+    if args.model == "small_spd":
+        m = SmallSPDSMModelDn3D(args.levels)
+    else:
+        m = SmallSMModelDn3D(args.levels, 3, "trilinear")
     wp = weights_path(args)
     meta = {}
     if wp is not None:
@@ -180,9 +197,11 @@ def precond_launches(plan):
     cnt = 0
     for l in range(n):
         cnt += 1 if fast[l] else (2 + (1 if l == 0 else 0))
-    cnt += 1
+    cnt += 2 if plan.spd else 1                       # coarsest l (and l_t)
     for l in range(n - 1, -1, -1):
-        if fast[l]:
+        if plan.spd:
+            cnt += 2 if fast[l] else 3 + (1 if l == 0 else 0)   # prolongation pass + block
+        elif fast[l]:
             cnt += 2 if l == 0 else 1                 # level 0: prolongation pass + block
         else:
             cnt += 3 + (2 if l == 0 else 0)
@@ -196,9 +215,13 @@ def setup_launches(plan):
     cnt = 1 + n + 1                                # image, pyramid, fluid mask
     cnt += 2 if any(cls) else 0                    # uniform vectors and material records of all blocks
     for l in range(n + 1):
+        if plan.spd:                               # forward block, then its transpose gathered from it
+            fast = plan.level_info(l)[1]
+            cnt += 12 if cls[l] else (2 if fast else 1)
+            continue
         nb = 2 if l < n else 1
         cnt += 6 if cls[l] else nb                 # classify, 2 tile scans, list, records, fill | dense planes
-    return cnt + 2 * n                             # c0/c1: class sums + finalize per level
+    return cnt + 2 * n + (1 if plan.spd else 0)    # c0/c1: class sums + finalize per level (+ squares)
 
 
 # ----------------------------------------------------------------------------
@@ -302,7 +325,10 @@ def run_ours(args, rank, world):
                 "frac": round(achieved / hbm, 4), "traffic": traffic,
                 "algorithmic_bytes": bytes_pre0, "general_cells": gen, "mixed_runs": mixed}
     # whole-iteration bytes (compulsory traffic of the fused algorithm)
-    per_iter_bytes = iteration_bytes(plan, n, mixed)
+    mixed_t = [plan.class_counts_transposed(l)[1] for l in range(plan.levels + 1)] if plan.spd else None
+    if plan.spd:
+        roofline["mixed_runs_transposed"] = mixed_t
+    per_iter_bytes = iteration_bytes(plan, n, mixed, mixed_t, args.method)
     it_mean = statistics.mean(its)
 
     # ---- e2e: public API from pinned host buffers ----
@@ -334,7 +360,8 @@ def run_ours(args, rank, world):
            "setup_ms": setup_ms, "solve_ms": solve_ms,
            "roofline": roofline, "clocks": clocks, "e2e": e2e, "meta": meta, "history": last.history.tolist(),
            "per_iter_bytes": per_iter_bytes, "launches": setup_launches(plan) + 2 +
-           it_mean * (precond_launches(plan) + 6), "x": x_fused, "scene": scene, "model": model,
+           it_mean * (precond_launches(plan) + (6 if args.method == "npsd" else 5)), "x": x_fused, "scene": scene,
+           "model": model,
            "flags": flags, "b": b, "wall": t_wall}
     return out
 
@@ -347,10 +374,22 @@ def coeff_bytes(plan, level, n_level, mixed):
     return n_level / 8 * 4 + mixed * 27 * 8 * 2 + tiles * 4   # run words, mixed-run records, tile offsets
 
 
-def iteration_bytes(plan, n0, mixed):
-    """Compulsory HBM bytes of one fused npsd iteration (bf16 coefficients and activations)."""
+def iteration_bytes(plan, n0, mixed, mixed_t=None, method="npsd"):
+    """Compulsory HBM bytes of one fused iteration (bf16 coefficients and activations)."""
     total = 0.0
+    # solver vectors: npsd dots + qform + spmv/dots, or npcg r.z + p/spmv; then update + true residual
+    vec = n0 * (12 + 16 + 18 + 32) if method == "npsd" else n0 * (8 + 17 + 32)
     L = plan.levels
+    if plan.spd:
+        for l in range(L):
+            nl = n0 / 8 ** l
+            sv_in = 4 if l == 0 else 2
+            total += coeff_bytes(plan, l, nl, mixed[l]) + nl * (sv_in + 2 + 2 / 8)   # pre: as below
+            # prolongation pass (coarse in, y in, u out), transposed block (u in, out; level 0: f32 z + mask)
+            total += nl * (2 / 8 + 2 + 2) + coeff_bytes(plan, l, nl, mixed_t[l]) + nl * (2 + (4 + 1 if l == 0 else 2))
+        nL = n0 / 8 ** L
+        total += coeff_bytes(plan, L, nL, mixed[L]) + coeff_bytes(plan, L, nL, mixed_t[L]) + nL * 8
+        return total + vec
     for l in range(L):
         nl = n0 / 8 ** l
         kb = coeff_bytes(plan, l, nl, mixed[l])
@@ -361,8 +400,7 @@ def iteration_bytes(plan, n0, mixed):
         else:        # post: coefficients, coarse, y, out
             total += kb + nl * (2 / 8 + 2 + 2)
     total += coeff_bytes(plan, L, n0 / 8 ** L, mixed[L]) + (n0 / 8 ** L) * (2 + 2)
-    total += n0 * (12 + 16 + 18 + 32)                   # dots, qform, spmv+dots, update (f32 vectors, f64 x)
-    return total
+    return total + vec
 
 
 def reference_solution(flags, b, tol=1e-12, max_it=20000):
@@ -394,7 +432,7 @@ def reference_solution(flags, b, tol=1e-12, max_it=20000):
 
 
 def plain_solve(args, model, scene, dev):
-    """The plain FP32 GPU drop-in: eval_forward per iteration, FP64 vectors, drop-in npsd."""
+    """The plain FP32 GPU drop-in: eval_forward per iteration, FP64 vectors, the drop-in solver."""
     import torch
     from mlpcg_gb300 import cg
     from mlpcg_gb300.laplacian import FluidLaplacian
@@ -402,12 +440,13 @@ def plain_solve(args, model, scene, dev):
     A = FluidLaplacian(flags)
     img = torch.as_tensor(scene.image(), device=dev)
     b = torch.as_tensor(scene.rhs.ravel(), device=dev)[A.fluid_cells]
+    solve = getattr(cg, args.method)
     pred = cg.model_predict(model, img, A.fluid_cells)
-    cg.npsd(b, A, torch.zeros_like(b), pred, 2, tol=args.tol, atol=1e-20)  # warm-up
+    solve(b, A, torch.zeros_like(b), pred, 2, tol=args.tol, atol=1e-20)  # warm-up
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     pred = cg.model_predict(model, img, A.fluid_cells)
-    x, it, timer, res = cg.npsd(b, A, torch.zeros_like(b), pred, args.max_it, tol=args.tol, atol=1e-20)
+    x, it, timer, res = solve(b, A, torch.zeros_like(b), pred, args.max_it, tol=args.tol, atol=1e-20)
     torch.cuda.synchronize()
     return (time.perf_counter() - t0) * 1e3, it, res
 
@@ -416,28 +455,31 @@ def plain_solve(args, model, scene, dev):
 def cpu_baseline(args, model_sd, scene, iterations, budget_s):
     """The reference's CPU path on this host: per-iteration time on a bounded sample."""
     import torch
-    from oracle.cpu_path import CPUModel, npsd_iterations
+    from oracle.cpu_path import CPUModel, CPUSPDModel, npcg_iterations, npsd_iterations
     threads = torch.get_num_threads()
-    m = CPUModel(model_sd, args.levels)
+    cls = CPUSPDModel if args.model == "small_spd" else CPUModel
+    run = npcg_iterations if args.method == "npcg" else npsd_iterations
+    m = cls(model_sd, args.levels)
     img = scene.image()
     # one iteration (includes the pyramid / c0 / c1 cache build) to size the sample
     t0 = time.perf_counter()
-    times, _ = npsd_iterations(m, img, scene.flags, scene.rhs, 1)
+    times, _ = run(m, img, scene.flags, scene.rhs, 1)
     first = times[0]
     k = max(1, min(5, int(budget_s / max(first, 1e-3))))
-    m2 = CPUModel(model_sd, args.levels)
-    times, hist = npsd_iterations(m2, img, scene.flags, scene.rhs, k + 1)
+    m2 = cls(model_sd, args.levels)
+    times, hist = run(m2, img, scene.flags, scene.rhs, k + 1)
     per_it = statistics.mean(times[1:]) if len(times) > 1 else times[0]
     setup = times[0] - per_it
     total_ms = (setup + per_it * iterations) * 1e3
     return {"value": round(total_ms, 1), "unit": "ms", "cores": threads, "kind": "port",
-            "sample": f"{len(times)} npsd iterations at {args.size}^3 (torch-CPU Conv3d blocks, FP64 CSR), "
+            "sample": f"{len(times)} {args.method} iterations at {args.size}^3 (torch-CPU Conv3d blocks, "
+                      f"{MODEL_NAMES[args.model]}, FP64 CSR), "
                       f"{per_it:.2f} s/iteration, extrapolated to {iterations} iterations",
             "host_cpus": os.cpu_count(), "per_iteration_s": round(per_it, 3)}
 
 
 def reference_iterations(meta, args):
-    key = f"npsd_iterations_{args.size}_seed{args.seed}"
+    key = f"{args.method}_iterations_{args.size}_seed{args.seed}"
     return int(meta.get(key, args.max_it))
 
 
@@ -449,8 +491,10 @@ def main():
     if world > 1:
         torch.distributed.init_process_group("nccl" if args.impl == "ours" else "gloo")
     cfg = {"workload": f"single {args.size}^3 scene (seed {args.seed}, {args.spheres} spheres), "
-                       f"{args.levels}-level SmallSMModelDn3D, {args.method} to {args.tol:g} FP64 true rel. residual",
-           "grid": args.size, "levels": args.levels, "method": args.method, "max_it": args.max_it,
+                       f"{args.levels}-level {MODEL_NAMES[args.model]}, {args.method} to {args.tol:g} FP64 true rel. "
+                       f"residual",
+           "grid": args.size, "levels": args.levels, "model": MODEL_NAMES[args.model], "method": args.method,
+           "max_it": args.max_it,
            "precision": "bf16 coefficients+activations, fp32 CG vectors, fp64 x/b/reductions/true residual",
            "l2": "inputs larger than L2; L2 flushed (256 MiB write) between steps",
            "parallelism": f"replicas x{world}"}

@@ -276,6 +276,11 @@ int mlpcg_precond_create(int N1, int N2, int N3, int levels, int k_dtype, int ac
  * (no swap / mask options: the network has none). */
 int mlpcg_precond_create_spd(int N1, int N2, int N3, int levels, int k_dtype, int act_dtype, int coeff_layout,
                              mlpcg_precond **out);
+/* After setup of an SPD plan: mlpcg_precond_class_counts of the transposed
+ * blocks (l0_t[level], or l_t on the coarsest level), whose cells are
+ * uniform when their 27 neighbours are; MLPCG_ERR_ARG for other plans. */
+int mlpcg_precond_class_counts_transposed(const mlpcg_precond *plan, int level, int64_t *general_cells,
+                                          int64_t *mixed_runs, void *stream);
 /* After setup (synchronises `stream`): the number of general cells and of
  * mixed runs (records) of a classed level; -1 for both on a dense level. */
 int mlpcg_precond_class_counts(const mlpcg_precond *plan, int level, int64_t *general_cells, int64_t *mixed_runs,

@@ -1821,13 +1821,14 @@ int mlpcg_precond_apply_stages(const mlpcg_precond *h, int first, int last, cons
   return run_apply<float, float>(P, r, r_scale, z, tmp0, st, first, last);
 }
 
-int mlpcg_precond_class_counts(const mlpcg_precond *h, int level, int64_t *general_cells, int64_t *mixed_runs,
-                               void *stream) {
-  clear_error();
+static int class_counts(const mlpcg_precond *h, int level, bool transposed, int64_t *general_cells,
+                        int64_t *mixed_runs, void *stream) {
   MLPCG_REQUIRE(h && general_cells && mixed_runs && level >= 0 && level <= h->p.L, MLPCG_ERR_ARG,
                 "precond_class_counts: bad argument");
   const PrecondPlan &P = h->p;
   MLPCG_REQUIRE(P.ready, MLPCG_ERR_ARG, "precond_class_counts: plan not set up");
+  MLPCG_REQUIRE(!transposed || P.kind == MLPCG_PRECOND_SMALL_SPD, MLPCG_ERR_ARG,
+                "precond_class_counts_transposed: the plan has no transposed blocks");
   const auto &v = P.lv[level];
   if (!v.cls) {
     *general_cells = *mixed_runs = -1;
@@ -1836,12 +1837,30 @@ int mlpcg_precond_class_counts(const mlpcg_precond *h, int level, int64_t *gener
   uint32_t last[4] = {0, 0, 0, 0};
   cudaStream_t st = as_stream(stream);
   const uint32_t *src[4] = {P.gbase[level], P.gcount[level], P.rbase[level], P.rcount[level]};
+  if (transposed) {
+    src[0] = P.gbaseT[level];
+    src[1] = P.gcountT[level];
+    src[2] = P.rbaseT[level];
+    src[3] = P.rcountT[level];
+  }
   for (int t = 0; t < 4; ++t)
     MLPCG_CUDA_CHECK(cudaMemcpyAsync(&last[t], src[t] + v.ntiles - 1, 4, cudaMemcpyDeviceToHost, st));
   MLPCG_CUDA_CHECK(cudaStreamSynchronize(st));
   *general_cells = (int64_t)last[0] + last[1];
   *mixed_runs = (int64_t)last[2] + last[3];
   return MLPCG_OK;
+}
+
+int mlpcg_precond_class_counts(const mlpcg_precond *h, int level, int64_t *general_cells, int64_t *mixed_runs,
+                               void *stream) {
+  clear_error();
+  return class_counts(h, level, false, general_cells, mixed_runs, stream);
+}
+
+int mlpcg_precond_class_counts_transposed(const mlpcg_precond *h, int level, int64_t *general_cells,
+                                          int64_t *mixed_runs, void *stream) {
+  clear_error();
+  return class_counts(h, level, true, general_cells, mixed_runs, stream);
 }
 
 int mlpcg_precond_level_info(const mlpcg_precond *h, int level, int *n1, int *n2, int *n3, int *fast) {

@@ -107,6 +107,13 @@ class PrecondPlan:
         call("mlpcg_precond_class_counts", self._h, int(level), C.byref(g), C.byref(r), _stream(self.device))
         return g.value, r.value
 
+    def class_counts_transposed(self, level: int):
+        """(general cells, mixed runs) of the transposed block of a classed level (SPD plans)."""
+        g, r = C.c_int64(), C.c_int64()
+        call("mlpcg_precond_class_counts_transposed", self._h, int(level), C.byref(g), C.byref(r),
+             _stream(self.device))
+        return g.value, r.value
+
     def general_cells(self, level: int) -> int:
         """Cells of a classed level whose neighbourhood is not a single material (-1 on dense levels)."""
         return self.class_counts(level)[0]

@@ -1,4 +1,5 @@
-"""Training of SmallSMModelDn3D through the hand-written adjoint kernels (the reference's train.py).
+"""Training of SmallSMModelDn3D (the reference's train.py) or of the symmetric SmallSPDSMModelDn3D
+(train_one_scene.py:176) through the hand-written adjoint kernels.
 
 Loss (per right-hand side b of unit norm, x = f(b) restricted to fluid cells):
   * ``angle`` (default): 1 - cos^2(b, A x), the squared relative residual at
@@ -13,6 +14,7 @@ Adam (train.py:219 of the reference uses lr 1e-4 over far more steps; a
 cosine schedule from a larger lr is used here).
 
     python -m mlpcg_gb300.train --out DIR --size 128 --levels 5 --seeds 10-17 --steps 4000
+    python -m mlpcg_gb300.train --out DIR --model small_spd ...   (validated with npcg)
 """
 from __future__ import annotations
 
@@ -29,7 +31,20 @@ from . import ops
 from .laplacian import FluidLaplacian
 from .lanczos import lanczos_ritz, mix_rhs
 from .scenes import make_scene
-from .sm_model_3d import SmallSMModelDn3D
+from .sm_model_3d import SmallSMModelDn3D, SmallSPDSMModelDn3D
+
+MODELS = {"smallsm": "smallsm", "small_spd": "smallspd"}   # --model -> weight file prefix
+
+
+def make_model(kind, levels):
+    if kind == "small_spd":
+        return SmallSPDSMModelDn3D(levels)
+    return SmallSMModelDn3D(levels, 3, "trilinear")
+
+
+def solve_method(model):
+    """npcg for the symmetric network (textbook PCG is valid), npsd otherwise."""
+    return "npcg" if isinstance(model, SmallSPDSMModelDn3D) else "npsd"
 from .solver import FusedSolver, flags_to_image
 
 
@@ -78,11 +93,13 @@ def residual_loss(model, image, flags, fluid, b, kind="angle"):
 
 
 def near_identity_(model, eps=0.1):
-    """Shrink the random weights by eps and add z = x on the direct path (M ~ I at start)."""
+    """Shrink the random weights by eps and add z = x on the direct path (M ~ I at start; for the
+    symmetric network M = S^T S ~ I with S ~ I on the finest level)."""
     with torch.no_grad():
         for p in model.parameters():
             p.mul_(eps)
-        model.pre[0].bias[13] += 1.0
+        first = model.l0[0] if isinstance(model, SmallSPDSMModelDn3D) else model.pre[0]
+        first.bias[13] += 1.0
         model.c0[0].bias[0] += 1.0
 
 
@@ -140,8 +157,8 @@ class TrainScene:
         if self.plan is None:
             self.plan = PrecondPlan(model, self.image)
             for d in depths:
-                self.solvers[d] = FusedSolver(model, self.flags, method="npsd", max_it=d, tol=1e-12,
-                                              plan=self.plan)
+                self.solvers[d] = FusedSolver(model, self.flags, method=solve_method(model), max_it=d,
+                                              tol=1e-12, plan=self.plan)
         else:
             next(iter(self.solvers.values())).set_image(model, self.image)
         b0 = self.batch(1, 0.5, gen)[0].double()
@@ -155,14 +172,16 @@ class TrainScene:
 
 
 class Validator:
-    """npsd iterations to 1e-6 on a held-out scene (one solver, re-planned with the current weights)."""
+    """npsd (npcg for the symmetric network) iterations to 1e-6 on a held-out scene (one solver,
+    re-planned with the current weights)."""
 
     def __init__(self, model, size, seed, spheres, device, max_it=200, tol=1e-6):
         s = make_scene(size, seed, spheres)
         self.flags = torch.as_tensor(s.flags, device=device)
         self.rhs = torch.as_tensor(s.rhs, device=device)
         self.image = flags_to_image(self.flags)
-        self.solver = FusedSolver(model, self.flags, method="npsd", max_it=max_it, tol=tol, image=self.image)
+        self.solver = FusedSolver(model, self.flags, method=solve_method(model), max_it=max_it, tol=tol,
+                                  image=self.image)
 
     def __call__(self, model):
         self.solver.set_image(model, self.image)
@@ -180,6 +199,7 @@ def parse_seeds(s):
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", required=True)
+    ap.add_argument("--model", default="smallsm", choices=sorted(MODELS))
     ap.add_argument("--size", type=int, default=128)
     ap.add_argument("--levels", type=int, default=5)
     ap.add_argument("--seeds", default="10-17")
@@ -208,7 +228,7 @@ def main(argv=None):
     out = Path(args.out)
     out.mkdir(parents=True, exist_ok=True)
     torch.manual_seed(0)
-    model = SmallSMModelDn3D(args.levels, 3, "trilinear").to(dev)
+    model = make_model(args.model, args.levels).to(dev)
     if args.init:
         d = np.load(args.init)
         model.load_state_dict({k: torch.from_numpy(d[k]) for k in model.state_dict()})
@@ -272,12 +292,14 @@ def main(argv=None):
 
 
 def save(model, out: Path, args, log, best: bool):
-    """The best weights so far (by validation iterations) go to smallsm_l{n}.npz, the latest to *.last.npz."""
+    """The best weights so far (by validation iterations) go to <prefix>_l{n}.npz (prefix smallsm or
+    smallspd), the latest to *.last.npz."""
     sd = {k: v.detach().float().cpu().numpy() for k, v in model.state_dict().items()}
+    stem = f"{MODELS[getattr(args, 'model', 'smallsm')]}_l{args.levels}"
     if best:
-        np.savez(out / f"smallsm_l{args.levels}.npz", **sd)
-    np.savez(out / f"smallsm_l{args.levels}.last.npz", **sd)
-    (out / f"smallsm_l{args.levels}.train.json").write_text(json.dumps(log, indent=1))
+        np.savez(out / f"{stem}.npz", **sd)
+    np.savez(out / f"{stem}.last.npz", **sd)
+    (out / f"{stem}.train.json").write_text(json.dumps(log, indent=1))
 
 
 if __name__ == "__main__":

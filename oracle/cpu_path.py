@@ -5,7 +5,7 @@ coefficients are a Conv3d(3 -> 27, k=3, padding 1) of the image, applied to
 the 27 shifted copies of x (unfold).  They are composed in the order of
 SmallSMModelDn3D.forward (sm_model_3d.py:264-287) with trilinear upsampling
 and the linear blocks of SmallLinearBlock3DPY (sm_model_3d_py.py:24-31) in
-their mean-weight form.  The solver is npsd (cg_tests.py:189-284) with an FP64
+their mean-weight form (CPUSPDModel: SmallSPDSMModelDn3D on the same blocks).  The solver is npsd (cg_tests.py:189-284) with an FP64
 torch CSR matrix and model_predict (test.py:42-51), all on the CPU.
 """
 from __future__ import annotations
@@ -58,6 +58,43 @@ class CPUModel:
         return x[0]
 
 
+class CPUSPDModel(CPUModel):
+    """SmallSPDSMModelDn3D (sm_model_3d.py:425-444) on the same torch-CPU blocks: the transposed
+    block l_t / l0_t scatters K_p(q) x(q) to q + offset(p) (the adjoint of the unfold), the
+    prolongation is nearest x2 / 8, the combine uses c0^2, c1^2."""
+
+    def _block_t(self, name, img, x):
+        W, b = self.p[f"{name}.weight"], self.p[f"{name}.bias"]
+        K = F.conv3d(img[None], W, b, padding=1)[0]          # (27, N1, N2, N3)
+        n1, n2, n3 = x.shape[-3:]
+        y = torch.zeros(x.shape[:-3] + (n1 + 2, n2 + 2, n3 + 2), dtype=x.dtype)
+        for p in range(27):
+            dx, dy, dz = p // 9, (p // 3) % 3, p % 3
+            y[..., dx:dx + n1, dy:dy + n2, dz:dz + n3] += K[p] * x
+        return y[..., 1:-1, 1:-1, 1:-1]
+
+    def __call__(self, img, b):
+        n = self.n
+        if self.cache is None:
+            imgs = [img]
+            for _ in range(n):
+                imgs.append(F.avg_pool3d(imgs[-1][None], 2)[0])
+            c0 = [self._linear(f"c0.{i}", imgs[i]) for i in range(n)]
+            c1 = [self._linear(f"c1.{i}", imgs[i]) for i in range(n)]
+            self.cache = (imgs, c0, c1)
+        imgs, c0, c1 = self.cache
+        x = [self._block("l0.0", imgs[0], b)]
+        for i in range(1, n):
+            x.append(self._block(f"l0.{i}", imgs[i], F.avg_pool3d(x[-1], 2)))
+        x.append(self._block("l", imgs[n], F.avg_pool3d(x[-1], 2)))
+        x[-1] = self._block_t("l", imgs[n], x[-1])
+        for i in range(n, 0, -1):
+            x[i] = F.interpolate(x[i], scale_factor=2) / 8
+            x[i - 1] = c0[i - 1] ** 2 * x[i - 1] + c1[i - 1] ** 2 * x[i]
+            x[i - 1] = self._block_t(f"l0.{i-1}", imgs[i - 1], x[i - 1])
+        return x[0]
+
+
 def csr_cpu(flags):
     from .laplacian import assemble
     A, fluid = assemble(flags)
@@ -65,6 +102,41 @@ def csr_cpu(flags):
                                  torch.from_numpy(A.indices.astype(np.int64)),
                                  torch.from_numpy(A.data), A.shape, dtype=torch.float64)
     return At, torch.from_numpy(fluid)
+
+
+def npcg_iterations(model: CPUModel, img, flags, rhs, iters):
+    """``iters`` iterations of npcg (cg_tests.py:26-101: textbook PCG, the solver of a symmetric
+    network) on the CPU; returns (seconds per iteration list, rel residuals)."""
+    A, fluid = csr_cpu(flags)
+    shape = tuple(flags.shape)
+    n = int(np.prod(shape))
+    b = torch.from_numpy(rhs.ravel()[fluid.numpy()]).double()
+    img_t = torch.as_tensor(img)
+
+    def predict(r):
+        r32 = F.normalize(r.float(), dim=0)
+        g = torch.zeros(n, dtype=torch.float32)
+        g[fluid] = r32
+        return model(img_t, g.view((1, 1) + shape)).flatten().double()[fluid]
+
+    norm_b = b.norm().item()
+    x = torch.zeros_like(b)
+    r = b - A @ x
+    times, hist = [], []
+    p = rz = None
+    for _ in range(iters):
+        t0 = time.perf_counter()
+        z = predict(r)
+        rz_new = r.dot(z)
+        p = z if p is None else z + (rz_new / rz) * p
+        rz = rz_new
+        Ap = A @ p
+        alpha = rz / p.dot(Ap)
+        x = x + alpha * p
+        r = b - A @ x
+        hist.append(r.norm().item() / norm_b)
+        times.append(time.perf_counter() - t0)
+    return times, hist
 
 
 def npsd_iterations(model: CPUModel, img, flags, rhs, iters):

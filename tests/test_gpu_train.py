@@ -61,3 +61,17 @@ def test_training_steps_reduce_loss(cuda):
         loss.backward()
         opt.step()
     assert float(loss) < 0.8 * first
+
+
+def test_training_symmetric_network(cuda, tmp_path):
+    """A few steps of the training loop on SmallSPDSMModelDn3D (near-identity start, npcg
+    validation and harvesting through the fused SPD plan) reduce the loss and save smallspd_l3."""
+    from mlpcg_gb300 import train
+    train.main(["--out", str(tmp_path), "--model", "small_spd", "--size", "32", "--levels", "3", "--seeds", "10",
+                "--steps", "100", "--batch", "4", "--lanczos-steps", "80", "--n-ritz", "16", "--eval-every", "100",
+                "--val-size", "32", "--val-seed", "11", "--harvest-every", "50"])
+    log = __import__("json").loads((tmp_path / "smallspd_l3.train.json").read_text())
+    assert (tmp_path / "smallspd_l3.npz").exists()
+    assert all(0.0 <= e["loss"] <= 1.0 for e in log["loss"]) and len(log["loss"]) == 2
+    first, last = log["eval"][0], log["eval"][-1]
+    assert last["status"] == "converged" and last["iterations"] <= first["iterations"], log["eval"]

@@ -73,6 +73,16 @@ def test_oracle_symmetry(golden, fname, cls, fwd):
     assert float((x * fwd(p, d["image"], x, n)).sum()) >= 0.0
 
 
+def test_cpu_path_small_spd(golden):
+    """The timed CPU baseline's SmallSPDSMModelDn3D (torch-CPU blocks, scatter transpose) against
+    the reference's output."""
+    from oracle.cpu_path import CPUSPDModel
+    d = golden("small_spd_16_l3.npz")
+    m = CPUSPDModel({k: torch.from_numpy(v) for k, v in _params(d).items()}, int(d["n"]))
+    y = m(torch.from_numpy(d["image"]), torch.from_numpy(d["b"][:1])).numpy()
+    assert rel_err(y, d["y_eval"]) < 1e-5
+
+
 # ---------------------------------------------------------------------------- GPU
 def _t(a, dev, dt=torch.float32):
     return torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=dev)
