@@ -771,12 +771,22 @@ __device__ __forceinline__ void stage_uniform(ClsSmem *sm, const float *__restri
   for (int e = threadIdx.x; e < 3 * KREC; e += PT) sm->Ku[e / KREC][e % KREC] = __ldg(kuni + e);
 }
 
-// the run words of the thread's runs and the tile's (first record, mixed runs) (classed only)
+// the run words of the thread's runs and the tile's (first record, mixed runs) (classed only).
+// The tile's mixed-run records are one contiguous block (tap-major across its runs); thread 0
+// asks for the whole block to be brought into L2 with one bulk prefetch, so that the record
+// loads of the block application, issued after the tile is staged, find it there.
 template <typename KT, bool CLS>
 __device__ __forceinline__ uint2 load_tile_runs(const CoefArgs<KT> &C, int n1, int n2, int n3, uint32_t rwd[TX]) {
   if (!CLS) return make_uint2(0u, 0u);
+  const uint2 tb = make_uint2(__ldg(C.rbase + tile_id()), __ldg(C.rcount + tile_id()));
+  if (threadIdx.x == 0 && tb.y > 0) {
+    // record block: RREC values per run, 16-byte aligned (RREC * sizeof(KT) is a multiple of 16)
+    const size_t addr = __cvta_generic_to_global(C.rec + (size_t)tb.x * RREC);
+    const uint32_t bytes = tb.y * (uint32_t)(RREC * sizeof(KT));
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(addr), "r"(bytes) : "memory");
+  }
   load_run_words(C.rw, n1, n2, n3, rwd);
-  return make_uint2(__ldg(C.rbase + tile_id()), __ldg(C.rcount + tile_id()));
+  return tb;
 }
 
 // mask bytes of the thread's runs (all ones without a mask)
