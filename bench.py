@@ -8,7 +8,8 @@ true relative residual of 1e-6, max 100 iterations.
 A step = one whole solve of that scene with inputs resident in HBM: flags ->
 image channels, the preconditioner plan (image pyramid, the coefficients of
 all 11 blocks, c0/c1), then the graph-captured fused iteration.  The L2 is
-flushed between steps.  Also reported:
+flushed between steps.  Before the warm-up (untimed) the solver's CTA count is
+picked by mlpcg_gb300.autotune (config.solver_schedule).  Also reported:
   * plain_ms   -- the plain FP32 drop-in (reference semantics: coefficients
                   re-evaluated in every block call, FP64 CG vectors, a host
                   round trip per iteration), one solve;
@@ -70,6 +71,8 @@ def parse():
     ap.add_argument("--tol", type=float, default=1e-6)
     ap.add_argument("--weights", default=None, help="npz state dict (default: committed trained weights)")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default solver CTA count instead of the autotuned one (tuning is untimed)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-reference-solution", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
@@ -245,6 +248,15 @@ def run_ours(args, rank, world):
                          storage=torch.bfloat16, image=image)
     plan = solver.plan
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    tuned = None
+    if not args.no_autotune:
+        # the solver's CTA count for this device / grid / method, timed before the timed region
+        from mlpcg_gb300 import autotune
+        cache = Path(tempfile.gettempdir()) / f"mlpcg_autotune_{os.getpid()}.json"
+        tuned = autotune.tune_solver(solver, b, reps=5, cache_path=cache, retune=True)
+        tuned = {"solver_ctas": tuned, "ms_by_ctas": autotune.load_cache(cache)[
+            autotune.schedule_key(torch.cuda.get_device_properties(dev).name, solver.shape, solver.method)]["ms"]}
+        cache.unlink(missing_ok=True)
 
     def step(mid=None):
         img = flags_to_image(flags)
@@ -362,7 +374,7 @@ def run_ours(args, rank, world):
            "per_iter_bytes": per_iter_bytes, "launches": setup_launches(plan) + 2 +
            it_mean * (precond_launches(plan) + (6 if args.method == "npsd" else 5)), "x": x_fused, "scene": scene,
            "model": model,
-           "flags": flags, "b": b, "wall": t_wall}
+           "flags": flags, "b": b, "wall": t_wall, "tuned": tuned}
     return out
 
 
@@ -545,7 +557,8 @@ def main():
     line = {"metric": METRIC, "value": round(r["ms"], 3), "unit": "ms", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(r["ms"], 3), "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": dict(cfg, weights=r["meta"].get("weights")),
+            "config": dict(cfg, weights=r["meta"].get("weights"),
+                           solver_schedule=r["tuned"] or "default (8 CTAs per SM)"),
             "iterations": it_mean, "status": r["status"][-1], "rel_res": r["rels"][-1],
             "history": [round(h, 9) for h in r["history"]],
             "per_iteration_hbm_bytes": r["per_iter_bytes"],
