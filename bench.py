@@ -23,10 +23,10 @@ picked by mlpcg_gb300.autotune (config.solver_schedule).  Also reported:
                   CSR npsd) on this host, a bounded sample of iterations,
                   extrapolated to the iteration count of the solve.
 
-``--model small_spd`` runs the same harness on the symmetric network
-SmallSPDSMModelDn3D (default solver npcg, textbook PCG; weights
-smallspd_l<n>.npz when present); its CPU path is the same torch-CPU blocks
-composed as that network with the reference's npcg.
+``--model small_spd`` / ``--model spd`` run the same harness on the symmetric
+networks SmallSPDSMModelDn3D / SPDSMModelDn3D (default solver npcg, textbook
+PCG; weights smallspd_l<n>.npz / spd_l<n>.npz when present); their CPU path is
+the same torch-CPU blocks composed as that network with the reference's npcg.
 
 ``--impl reference`` times only that CPU path and prints its own line.
 Multi-GPU (``--gpus N`` under torchrun): N independent replicas, one scene
@@ -64,9 +64,9 @@ def parse():
     ap.add_argument("--levels", type=int, default=5)
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--spheres", type=int, default=6)
-    ap.add_argument("--model", default="smallsm", choices=["smallsm", "small_spd"])
+    ap.add_argument("--model", default="smallsm", choices=["smallsm", "small_spd", "spd"])
     ap.add_argument("--method", default=None, choices=["npsd", "npcg"],
-                    help="default: npsd (smallsm), npcg (small_spd)")
+                    help="default: npsd (smallsm), npcg (small_spd, spd)")
     ap.add_argument("--max-it", type=int, default=100)
     ap.add_argument("--tol", type=float, default=1e-6)
     ap.add_argument("--weights", default=None, help="npz state dict (default: committed trained weights)")
@@ -80,27 +80,29 @@ def parse():
                     help="plain launches of the same kernels with a host check per iteration (for profilers)")
     args = ap.parse_args()
     if args.method is None:
-        args.method = "npcg" if args.model == "small_spd" else "npsd"
+        args.method = "npsd" if args.model == "smallsm" else "npcg"
     return args
 
 
-MODEL_NAMES = {"smallsm": "SmallSMModelDn3D", "small_spd": "SmallSPDSMModelDn3D"}
+MODEL_NAMES = {"smallsm": "SmallSMModelDn3D", "small_spd": "SmallSPDSMModelDn3D", "spd": "SPDSMModelDn3D"}
 
 
 def weights_path(args):
     if args.weights:
         return Path(args.weights)
-    prefix = "smallspd" if args.model == "small_spd" else "smallsm"
+    prefix = {"smallsm": "smallsm", "small_spd": "smallspd", "spd": "spd"}[args.model]
     p = WEIGHTS_DIR / f"{prefix}_l{args.levels}.npz"
     return p if p.exists() else None
 
 
 def load_model(args, device):
     import torch
-    from mlpcg_gb300.sm_model_3d import SmallSMModelDn3D, SmallSPDSMModelDn3D
+    from mlpcg_gb300.sm_model_3d import SmallSMModelDn3D, SmallSPDSMModelDn3D, SPDSMModelDn3D
     torch.manual_seed(0)
     if args.model == "small_spd":
         m = SmallSPDSMModelDn3D(args.levels)
+    elif args.model == "spd":
+        m = SPDSMModelDn3D(args.levels)
     else:
         m = SmallSMModelDn3D(args.levels, 3, "trilinear")
     wp = weights_path(args)
@@ -194,9 +196,18 @@ def replica_seed(base_seed: int, rank: int) -> int:
 # launch accounting
 # ----------------------------------------------------------------------------
 def precond_launches(plan):
-    """Kernel launches of one preconditioner application (mirrors run_apply in precond.cu)."""
+    """Kernel launches of one preconditioner application (mirrors run_apply / run_apply_spd in
+    precond.cu)."""
     n = plan.levels
     fast = [plan.level_info(l)[1] for l in range(n + 1)]
+    if plan.kind == 2:   # SPDSMModelDn3D: V then V^T
+        cnt = 2                                            # coarsest l, l_t
+        for l in range(n):
+            cnt += 1 if fast[l] else 2 + (1 if l == 0 else 0)  # V down (level 0: scale copy)
+            cnt += 2 if fast[l] else 3                          # V up: prolongation + block
+            cnt += 1 if fast[l] else 2                          # V^T down
+            cnt += 2 if fast[l] else 3 + (1 if l == 0 else 0)  # V^T up (level 0: mask)
+        return cnt
     cnt = 0
     for l in range(n):
         cnt += 1 if fast[l] else (2 + (1 if l == 0 else 0))
@@ -218,13 +229,17 @@ def setup_launches(plan):
     cnt = 1 + n + 1                                # image, pyramid, fluid mask
     cnt += 2 if any(cls) else 0                    # uniform vectors and material records of all blocks
     for l in range(n + 1):
+        fast = plan.level_info(l)[1]
+        if plan.kind == 2:                         # l0 + l1 (or l), then their transposes gathered
+            nb = 2 if l < n else 1
+            cnt += (6 + 4 + 2 * nb) if cls[l] else (nb + (nb if fast else 0))
+            continue
         if plan.spd:                               # forward block, then its transpose gathered from it
-            fast = plan.level_info(l)[1]
             cnt += 12 if cls[l] else (2 if fast else 1)
             continue
         nb = 2 if l < n else 1
         cnt += 6 if cls[l] else nb                 # classify, 2 tile scans, list, records, fill | dense planes
-    return cnt + 2 * n + (1 if plan.spd else 0)    # c0/c1: class sums + finalize per level (+ squares)
+    return cnt + 2 * n + (1 if plan.kind == 1 else 0)   # c0/c1: class sums + finalize per level (+ squares)
 
 
 # ----------------------------------------------------------------------------
@@ -392,6 +407,18 @@ def iteration_bytes(plan, n0, mixed, mixed_t=None, method="npsd"):
     # solver vectors: npsd dots + qform + spmv/dots, or npcg r.z + p/spmv; then update + true residual
     vec = n0 * (12 + 16 + 18 + 32) if method == "npsd" else n0 * (8 + 17 + 32)
     L = plan.levels
+    if plan.kind == 2:   # V (like the non-swap network, prolongation pass on every level), then V^T
+        for l in range(L):
+            nl = n0 / 8 ** l
+            sv_in = 4 if l == 0 else 2
+            kf, kt = coeff_bytes(plan, l, nl, mixed[l]), coeff_bytes(plan, l, nl, mixed_t[l])
+            total += kf + nl * (sv_in + 2 + 2 / 8)                      # V pre: x in, y out, pooled
+            total += nl * (2 / 8 + 2) + kf + nl * (2 + 2 + 2)            # V up pass; V post: u, y in, out
+            total += kt + nl * (2 + 2 / 8)                              # V^T pre: w in, pooled (no y)
+            total += nl * (2 / 8 + 2 + 2) + kt + nl * (2 + (4 + 1 if l == 0 else 2))   # V^T up + post
+        nL = n0 / 8 ** L
+        total += coeff_bytes(plan, L, nL, mixed[L]) + coeff_bytes(plan, L, nL, mixed_t[L]) + nL * 8
+        return total + vec
     if plan.spd:
         for l in range(L):
             nl = n0 / 8 ** l
@@ -467,9 +494,9 @@ def plain_solve(args, model, scene, dev):
 def cpu_baseline(args, model_sd, scene, iterations, budget_s):
     """The reference's CPU path on this host: per-iteration time on a bounded sample."""
     import torch
-    from oracle.cpu_path import CPUModel, CPUSPDModel, npcg_iterations, npsd_iterations
+    from oracle.cpu_path import CPUModel, CPUSPDFullModel, CPUSPDModel, npcg_iterations, npsd_iterations
     threads = torch.get_num_threads()
-    cls = CPUSPDModel if args.model == "small_spd" else CPUModel
+    cls = {"smallsm": CPUModel, "small_spd": CPUSPDModel, "spd": CPUSPDFullModel}[args.model]
     run = npcg_iterations if args.method == "npcg" else npsd_iterations
     m = cls(model_sd, args.levels)
     img = scene.image()

@@ -261,6 +261,7 @@ int mlpcg_precond_create(int N1, int N2, int N3, int levels, int k_dtype, int ac
 /* Network kinds of a plan. */
 #define MLPCG_PRECOND_SM        0  /* SmallSMModelDn3D (sm_model_3d.py:164-287) */
 #define MLPCG_PRECOND_SMALL_SPD 1  /* SmallSPDSMModelDn3D (sm_model_3d.py:388-444) */
+#define MLPCG_PRECOND_SPD       2  /* SPDSMModelDn3D (sm_model_3d.py:290-385) */
 
 /* Plan for the reduced symmetric network SmallSPDSMModelDn3D(levels)
  * (sm_model_3d.py:388-444; replaces its eval_forward inside the solver
@@ -276,9 +277,26 @@ int mlpcg_precond_create(int N1, int N2, int N3, int levels, int k_dtype, int ac
  * (no swap / mask options: the network has none). */
 int mlpcg_precond_create_spd(int N1, int N2, int N3, int levels, int k_dtype, int act_dtype, int coeff_layout,
                              mlpcg_precond **out);
-/* After setup of an SPD plan: mlpcg_precond_class_counts of the transposed
- * blocks (l0_t[level], or l_t on the coarsest level), whose cells are
- * uniform when their 27 neighbours are; MLPCG_ERR_ARG for other plans. */
+/* Plan for network kind MLPCG_PRECOND_SMALL_SPD (as mlpcg_precond_create_spd)
+ * or MLPCG_PRECOND_SPD: SPDSMModelDn3D(levels) (sm_model_3d.py:290-385;
+ * replaces its eval_forward inside the solver loop), M = V^T V with V the
+ * V-cycle of blocks l0 (down, average pooling), l (coarsest), nearest x2 / 8
+ * prolongation, l1 and c0 y + c1 u (up); the application runs V, then V^T:
+ * l1_t and pooling down from V's output, l_t, then per level the
+ * prolongation, c0 x_l + c1 u with x_l the level's input of that down
+ * sweep, and l0_t.  The transposed blocks' coefficients are gathered from
+ * the forward blocks' as for the reduced network.  setup's params for
+ * MLPCG_PRECOND_SPD: l0[0..n-1], l1[0..n-1], l (weight 2187, bias 27 each),
+ * then c0[0..n-1], c1[0..n-1] (weight 81, bias 1) -- the layout of
+ * mlpcg_precond_create's pre / post / l.  Application stages
+ * (mlpcg_precond_apply_stages): 0 .. 2n as for the other networks for V,
+ * 2n + 1 .. 4n + 1 the same sequence for V^T. */
+int mlpcg_precond_create_kind(int N1, int N2, int N3, int levels, int kind, int k_dtype, int act_dtype,
+                              int coeff_layout, mlpcg_precond **out);
+/* After setup of an SPD plan (either kind): mlpcg_precond_class_counts of the
+ * level's transposed blocks (l0_t / l1_t, or l_t on the coarsest level; they
+ * share one class map), whose cells are uniform when their 27 neighbours
+ * are; MLPCG_ERR_ARG for other plans. */
 int mlpcg_precond_class_counts_transposed(const mlpcg_precond *plan, int level, int64_t *general_cells,
                                           int64_t *mixed_runs, void *stream);
 /* After setup (synchronises `stream`): the number of general cells and of
@@ -306,9 +324,10 @@ int mlpcg_precond_setup(mlpcg_precond *plan, void *workspace, size_t workspace_b
 int mlpcg_precond_apply(const mlpcg_precond *plan, const float *r, const float *r_scale, float *z,
                         void *stream);
 /* Runs stages [first, last] of one application (stage s < n: pre-block of
- * level s; s = n: coarsest block; s > n: post-block of level 2n - s), using
- * the plan's own level buffers.  Stage 0 reads r, stage 2n writes z.  Used
- * to time the kernels of an application one by one. */
+ * level s; s = n: coarsest block; s > n: post-block of level 2n - s; the
+ * MLPCG_PRECOND_SPD kind repeats this for V^T as stages 2n + 1 .. 4n + 1),
+ * using the plan's own level buffers.  Stage 0 reads r, the last stage
+ * writes z.  Used to time the kernels of an application one by one. */
 int mlpcg_precond_apply_stages(const mlpcg_precond *plan, int first, int last, const float *r,
                                const float *r_scale, float *z, void *stream);
 /* Sizes of level `level` (0 = finest) and whether it runs the tiled kernels

@@ -429,13 +429,15 @@ __device__ __forceinline__ float round_as(const __nv_bfloat16 *, float v) {
 // model (blockIdx.x = parameter block b, at params + b * 2214), rounded like
 // the stored dtype: thread (c, p) evaluates output p of material c in the
 // accumulation order of coeffs_of_patch_n, so it equals what that function
-// yields on a patch of material c.  Block b's vectors go to slot b; with
-// spd_levels = n > 0 (the SPD kind: parameter blocks l0[0..n-1], l) block b
-// goes to slot b (l: slot 2n) and its transpose, the reversed vector (tap
-// 26 - p), to slot n + b (l_t: slot 2n + 1).
+// yields on a patch of material c.  Block b's vectors go to slot b, and for
+// the symmetric networks its transpose's, the reversed vector (tap 26 - p),
+// to a second slot: kind MLPCG_PRECOND_SMALL_SPD (parameter blocks l0[0..n-1],
+// l) puts l0[b] in slot b and its transpose in n + b, l in 2n and l_t in
+// 2n + 1; kind MLPCG_PRECOND_SPD (blocks l0[0..n-1], l1[0..n-1], l) puts
+// block b in slot b and its transpose in 2n + 1 + b.
 template <typename KT>
 __global__ void __launch_bounds__(3 * KREC)
-k_kgen_uniform_all(const float *__restrict__ params, float *__restrict__ kuni, int spd_levels) {
+k_kgen_uniform_all(const float *__restrict__ params, float *__restrict__ kuni, int n, int kind) {
   const int b = blockIdx.x, c = threadIdx.x / KREC, p = threadIdx.x % KREC;
   const float *W = params + (size_t)b * 2214, *bias = W + 2187;
   float acc = 0.f;
@@ -448,11 +450,15 @@ k_kgen_uniform_all(const float *__restrict__ params, float *__restrict__ kuni, i
     }
     acc = round_as((const KT *)nullptr, acc);
   }
-  if (spd_levels <= 0) {
+  if (kind == MLPCG_PRECOND_SM) {
     kuni[(size_t)b * 3 * KREC + threadIdx.x] = acc;
     return;
   }
-  const int n = spd_levels, sf = b < n ? b : 2 * n, sr = b < n ? n + b : 2 * n + 1;
+  int sf = b, sr = 2 * n + 1 + b;
+  if (kind == MLPCG_PRECOND_SMALL_SPD) {
+    sf = b < n ? b : 2 * n;
+    sr = b < n ? n + b : 2 * n + 1;
+  }
   kuni[(size_t)sf * 3 * KREC + threadIdx.x] = acc;
   kuni[(size_t)sr * 3 * KREC + c * KREC + (p < 27 ? 26 - p : p)] = acc;
 }
@@ -845,7 +851,7 @@ k_pre_fused(const CoefArgs<KT> C, const XT *__restrict__ x,
     if (!active || i >= n1) continue;
     const int64_t q = ((int64_t)i * n2 + j) * n3 + k0;
     apply_run_mask(mw[tx], acc[tx]);
-    st8(y + q, acc[tx]);
+    if (y) st8(y + q, acc[tx]);  // y may be NULL when only the pooled output is wanted
     if (POOL) {
 #pragma unroll
       for (int c = 0; c < 4; ++c) pool[c] += acc[tx][2 * c] + acc[tx][2 * c + 1];
@@ -1178,7 +1184,7 @@ struct PrecondPlan {
   int n1, n2, n3, L;          // fine sizes, number of levels n (blocks at levels 0..L)
   int kdt, adt;               // coefficient / activation storage dtypes
   int swap, mask;
-  int kind;                   // MLPCG_PRECOND_SM (SmallSMModelDn3D) or MLPCG_PRECOND_SMALL_SPD
+  int kind;                   // MLPCG_PRECOND_SM, MLPCG_PRECOND_SMALL_SPD or MLPCG_PRECOND_SPD
   int layout;                 // MLPCG_COEFF_DENSE or MLPCG_COEFF_CLASSED
   struct Level { int n1, n2, n3; int64_t n, ps; bool fast, cls; unsigned ntiles; };
   std::vector<Level> lv;      // L + 1 levels
@@ -1196,13 +1202,17 @@ struct PrecondPlan {
   std::vector<uint8_t *> cls;        // classed levels: class byte per cell (setup)
   std::vector<uint32_t *> rw;        // classed levels: word per 8-cell run
   std::vector<uint32_t *> rcount, rbase, gcount, gbase;  // per tile: mixed runs, general cells
-  // SPD kind: the transposed blocks (post-blocks l0_t, coarsest l_t) have their own class
-  // map, run words and per-tile counts (a cell is uniform when its 27 neighbours are)
+  // SPD kinds: the transposed blocks (l0_t, l1_t, coarsest l_t) have their own class map,
+  // run words and per-tile counts per level (a cell is uniform when its 27 neighbours are)
   std::vector<uint8_t *> clsT;
   std::vector<uint32_t *> rwT, rcountT, rbaseT, gcountT, gbaseT;
-  void *Klt = nullptr;        // coarsest transposed block (SPD kind)
+  void *Klt = nullptr;        // coarsest transposed block
   float *Ult = nullptr;
-  void *xtmp = nullptr;       // coarsest-level temporary between l and l_t (SPD kind)
+  void *xtmp = nullptr;       // coarsest-level temporary between l and l_t (SMALL_SPD kind)
+  // SPD kind (SPDSMModelDn3D): Kpre = l0, Kpost = l1 (forward); KpreT = l0_t, KpostT = l1_t
+  std::vector<void *> KpreT, KpostT;
+  std::vector<float *> UpreT, UpostT;
+  void *v0 = nullptr;         // V's output on the finest level, the input of V^T
   std::vector<void *> y, xin, xout;  // y_l (pre out), x_l inputs (l >= 1), post outputs (l >= 1)
   float *coef = nullptr;      // c0[0..L-1], c1[0..L-1]
   uint8_t *fmask = nullptr;   // fluid mask of level 0
@@ -1234,10 +1244,14 @@ static KT *kgen_rec_type(void (*)(const float *, int, int, int, const float *, i
                                   const uint32_t *, const uint32_t *, const uint32_t *, const uint32_t *,
                                   const uint32_t *, KT *, KT *));
 
-// blocks with uniform vectors / material records: 2L + 1, plus l_t for the SPD kind
+// blocks with uniform vectors / material records: 2L + 1 forward, plus l_t (SMALL_SPD kind) or
+// the 2L + 1 transposes (SPD kind)
 static int uniform_blocks(const PrecondPlan &P) {
-  return 2 * P.L + 1 + (P.kind == MLPCG_PRECOND_SMALL_SPD ? 1 : 0);
+  if (P.kind == MLPCG_PRECOND_SMALL_SPD) return 2 * P.L + 2;
+  if (P.kind == MLPCG_PRECOND_SPD) return 4 * P.L + 2;
+  return 2 * P.L + 1;
 }
+static bool has_transposes(const PrecondPlan &P) { return P.kind != MLPCG_PRECOND_SM; }
 
 static size_t plan_layout(PrecondPlan &P, char *base) {
   size_t off = 0;
@@ -1264,8 +1278,14 @@ static size_t plan_layout(PrecondPlan &P, char *base) {
     P.Kpost[l] = take(kbytes(l));
   }
   P.Kl = take(kbytes(P.L));
-  const bool spd = P.kind == MLPCG_PRECOND_SMALL_SPD;
+  const bool spd = has_transposes(P), full = P.kind == MLPCG_PRECOND_SPD;
   P.Klt = spd ? take(kbytes(P.L)) : nullptr;
+  P.KpreT.assign(P.L, nullptr);
+  P.KpostT.assign(P.L, nullptr);
+  for (int l = 0; full && l < P.L; ++l) {
+    P.KpreT[l] = take(kbytes(l));
+    P.KpostT[l] = take(kbytes(l));
+  }
   P.Upre.assign(P.L, nullptr);
   P.Upost.assign(P.L, nullptr);
   P.cls.assign(P.L + 1, nullptr);
@@ -1283,7 +1303,13 @@ static size_t plan_layout(PrecondPlan &P, char *base) {
     P.Upost[l] = U + (size_t)(P.L + l) * 3 * KREC;
   }
   P.Ul = U + (size_t)2 * P.L * 3 * KREC;
-  P.Ult = spd ? U + (size_t)(2 * P.L + 1) * 3 * KREC : nullptr;
+  P.Ult = spd ? U + (size_t)(full ? 4 * P.L + 1 : 2 * P.L + 1) * 3 * KREC : nullptr;
+  P.UpreT.assign(P.L, nullptr);
+  P.UpostT.assign(P.L, nullptr);
+  for (int l = 0; full && l < P.L; ++l) {
+    P.UpreT[l] = U + (size_t)(2 * P.L + 1 + l) * 3 * KREC;
+    P.UpostT[l] = U + (size_t)(3 * P.L + 1 + l) * 3 * KREC;
+  }
   P.Uall = U;
   P.Mrec = take((size_t)nU * 3 * RREC * sk);
   int64_t nlist = 0;
@@ -1324,7 +1350,8 @@ static size_t plan_layout(PrecondPlan &P, char *base) {
   }
   // the finest level's prolongated input (fast path only; the SPD kind uses it on every level)
   P.ufine = P.lv[0].fast ? take(P.lv[0].ps * sa) : nullptr;
-  P.xtmp = spd ? take(P.lv[P.L].ps * sa) : nullptr;
+  P.xtmp = P.kind == MLPCG_PRECOND_SMALL_SPD ? take(P.lv[P.L].ps * sa) : nullptr;
+  P.v0 = full ? take(P.lv[0].ps * sa) : nullptr;
   P.coef = (float *)take(2 * P.L * sizeof(float));
   P.fmask = (uint8_t *)take(P.lv[0].ps + 64);
   P.lin_ws = take(linear_workspace());
@@ -1381,11 +1408,156 @@ int launch_scan_u32(const uint32_t *cnt, uint32_t *base, int n, cudaStream_t st)
 }
 }  // namespace mlpcg
 
+// One application of the SPD kind (SPDSMModelDn3D.eval_forward, sm_model_3d.py:313-347): the
+// V-cycle V (stages 0 .. 2L) into v0, then V^T (stages 2L + 1 .. 4L + 1) into z.
+//   V:   y_l = l0[l](x_l), x_{l+1} = pool(y_l); x_L = l(x_L);
+//        x_l = c0 y_l + c1 l1[l](P x_{l+1})                       (P = nearest x2 / 8)
+//   V^T: w_0 = v0, w_{l+1} = pool(l1_t[l](w_l)); w_L = l_t(w_L);
+//        w_l = l0_t[l](c0 w_l + c1 P w_{l+1})
+// V^T's skip vector of level l is that level's input w_l (xin[l], v0 on level 0).
+template <typename KT, typename AT>
+static int run_apply_spd(const PrecondPlan &P, const float *r, const float *rscale, float *z, void *tmp0,
+                         cudaStream_t st, int s0, int s1, const int *gate) {
+  const int L = P.L;
+  auto in_range = [&](int s) { return s >= s0 && s <= s1; };
+  // ---- V: down sweep with l0, as the other networks' pre-blocks
+  for (int l = 0; l < L; ++l) {
+    if (!in_range(l)) continue;
+    const auto &v = P.lv[l];
+    if (v.fast) {
+      const CoefArgs<KT> C = coef_args<KT>(P, l, P.Kpre[l], v.cls ? P.Upre[l] : nullptr);
+      if (l == 0) {
+        if (v.cls)
+          k_pre_fused<KT, float, AT, true, true><<<grid_of(v), PT, 0, st>>>(
+              C, r, rscale, (AT *)P.y[0], (AT *)P.xin[1], nullptr, v.n1, v.n2, v.n3, gate);
+        else
+          k_pre_fused<KT, float, AT, true, false><<<grid_of(v), PT, 0, st>>>(
+              C, r, rscale, (AT *)P.y[0], (AT *)P.xin[1], nullptr, v.n1, v.n2, v.n3, gate);
+      } else {
+        if (v.cls)
+          k_pre_fused<KT, AT, AT, true, true><<<grid_of(v), PT, 0, st>>>(
+              C, (const AT *)P.xin[l], nullptr, (AT *)P.y[l], (AT *)P.xin[l + 1], nullptr, v.n1, v.n2, v.n3, gate);
+        else
+          k_pre_fused<KT, AT, AT, true, false><<<grid_of(v), PT, 0, st>>>(
+              C, (const AT *)P.xin[l], nullptr, (AT *)P.y[l], (AT *)P.xin[l + 1], nullptr, v.n1, v.n2, v.n3, gate);
+      }
+      MLPCG_LAUNCH_CHECK();
+    } else {
+      const void *src = P.xin[l];
+      if (l == 0) {
+        k_scale_copy<AT><<<blocks_for(v.n, 256), 256, 0, st>>>(r, rscale, (AT *)tmp0, v.n);
+        MLPCG_LAUNCH_CHECK();
+        src = tmp0;
+      }
+      RET_IF(launch_stencil_apply(P.Kpre[l], P.kdt, v.ps, src, P.adt, 0, P.y[l], P.adt, 1, v.n1, v.n2, v.n3, 0, st));
+      RET_IF(launch_avg_pool2(P.y[l], P.xin[l + 1], P.adt, 1, v.n1, v.n2, v.n3, st));
+    }
+  }
+  // ---- coarsest block l (V), l_t (V^T): xin[L] -> xout[L]
+  auto coarsest = [&](bool transposed) -> int {
+    const auto &v = P.lv[L];
+    if (v.fast) {
+      const CoefArgs<KT> C = transposed ? coef_args_t<KT>(P, L, P.Klt, v.cls ? P.Ult : nullptr)
+                                        : coef_args<KT>(P, L, P.Kl, v.cls ? P.Ul : nullptr);
+      if (v.cls)
+        k_pre_fused<KT, AT, AT, false, true><<<grid_of(v), PT, 0, st>>>(
+            C, (const AT *)P.xin[L], nullptr, (AT *)P.xout[L], nullptr, nullptr, v.n1, v.n2, v.n3, gate);
+      else
+        k_pre_fused<KT, AT, AT, false, false><<<grid_of(v), PT, 0, st>>>(
+            C, (const AT *)P.xin[L], nullptr, (AT *)P.xout[L], nullptr, nullptr, v.n1, v.n2, v.n3, gate);
+      MLPCG_LAUNCH_CHECK();
+      return MLPCG_OK;
+    }
+    return launch_stencil_apply(P.Kl, P.kdt, v.ps, P.xin[L], P.adt, 0, P.xout[L], P.adt, 1, v.n1, v.n2, v.n3,
+                                transposed ? 1 : 0, st);
+  };
+  if (in_range(L)) RET_IF(coarsest(false));
+  // ---- V: up sweep, x_l = c0 y_l + c1 l1[l](P x_{l+1}); level 0 into v0
+  for (int l = L - 1; l >= 0; --l) {
+    if (!in_range(2 * L - l)) continue;
+    const auto &v = P.lv[l];
+    const float *c0 = P.coef + l, *c1 = P.coef + L + l;
+    AT *o = (AT *)(l == 0 ? P.v0 : P.xout[l]);
+    if (v.fast) {
+      const CoefArgs<KT> C = coef_args<KT>(P, l, P.Kpost[l], v.cls ? P.Upost[l] : nullptr);
+      const dim3 g = grid_of(v);
+      AT *u = (AT *)P.ufine;
+      k_up_fine<AT, AT, AT, false, true><<<g, PT, 0, st>>>((const AT *)P.xout[l + 1], (const AT *)P.y[l], c0, c1, u,
+                                                            v.n1, v.n2, v.n3, gate);
+      MLPCG_LAUNCH_CHECK();
+      if (v.cls) k_post_fused<KT, AT, AT, AT, false, true, true><<<g, PT, 0, st>>>(C, u, (const AT *)P.y[l], c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3, gate);
+      else k_post_fused<KT, AT, AT, AT, false, false, true><<<g, PT, 0, st>>>(C, u, (const AT *)P.y[l], c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3, gate);
+      MLPCG_LAUNCH_CHECK();
+    } else {
+      RET_IF(launch_avg_pool2_adjoint(P.xout[l + 1], tmp0, P.adt, 1, v.n1, v.n2, v.n3, st));
+      RET_IF(launch_stencil_apply(P.Kpost[l], P.kdt, v.ps, tmp0, P.adt, 0, o, P.adt, 1, v.n1, v.n2, v.n3, 0, st));
+      RET_IF(launch_axpby(c0, P.y[l], c1, o, o, P.adt, v.n, st));
+    }
+  }
+  // ---- V^T: down sweep with l1_t from v0; only the pooled outputs are kept
+  const int B = 2 * L + 1;
+  for (int l = 0; l < L; ++l) {
+    if (!in_range(B + l)) continue;
+    const auto &v = P.lv[l];
+    const AT *src = (const AT *)(l == 0 ? P.v0 : P.xin[l]);
+    if (v.fast) {
+      const CoefArgs<KT> C = coef_args_t<KT>(P, l, P.KpostT[l], v.cls ? P.UpostT[l] : nullptr);
+      if (v.cls)
+        k_pre_fused<KT, AT, AT, true, true><<<grid_of(v), PT, 0, st>>>(
+            C, src, nullptr, (AT *)nullptr, (AT *)P.xin[l + 1], nullptr, v.n1, v.n2, v.n3, gate);
+      else
+        k_pre_fused<KT, AT, AT, true, false><<<grid_of(v), PT, 0, st>>>(
+            C, src, nullptr, (AT *)nullptr, (AT *)P.xin[l + 1], nullptr, v.n1, v.n2, v.n3, gate);
+      MLPCG_LAUNCH_CHECK();
+    } else {
+      RET_IF(launch_stencil_apply(P.Kpost[l], P.kdt, v.ps, src, P.adt, 0, tmp0, P.adt, 1, v.n1, v.n2, v.n3, 1, st));
+      RET_IF(launch_avg_pool2(tmp0, P.xin[l + 1], P.adt, 1, v.n1, v.n2, v.n3, st));
+    }
+  }
+  if (in_range(B + L)) RET_IF(coarsest(true));
+  // ---- V^T: up sweep, w_l = l0_t[l](c0 w_l + c1 P w_{l+1}); level 0 into z, zero off the fluid cells
+  for (int l = L - 1; l >= 0; --l) {
+    if (!in_range(B + 2 * L - l)) continue;
+    const auto &v = P.lv[l];
+    const float *c0 = P.coef + l, *c1 = P.coef + L + l;
+    const AT *skip = (const AT *)(l == 0 ? P.v0 : P.xin[l]);
+    if (v.fast) {
+      const CoefArgs<KT> C = coef_args_t<KT>(P, l, P.KpreT[l], v.cls ? P.UpreT[l] : nullptr);
+      const dim3 g = grid_of(v);
+      AT *u = (AT *)P.ufine;
+      k_up_fine<AT, AT, AT, true, true><<<g, PT, 0, st>>>((const AT *)P.xout[l + 1], skip, c0, c1, u, v.n1, v.n2,
+                                                           v.n3, gate);
+      MLPCG_LAUNCH_CHECK();
+      if (l == 0) {
+        if (v.cls) k_post_fused<KT, AT, AT, float, true, true, true><<<g, PT, 0, st>>>(C, u, skip, c0, c1, z, nullptr, P.fmask, v.n1, v.n2, v.n3, gate);
+        else k_post_fused<KT, AT, AT, float, true, false, true><<<g, PT, 0, st>>>(C, u, skip, c0, c1, z, nullptr, P.fmask, v.n1, v.n2, v.n3, gate);
+      } else {
+        AT *o = (AT *)P.xout[l];
+        if (v.cls) k_post_fused<KT, AT, AT, AT, true, true, true><<<g, PT, 0, st>>>(C, u, skip, c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3, gate);
+        else k_post_fused<KT, AT, AT, AT, true, false, true><<<g, PT, 0, st>>>(C, u, skip, c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3, gate);
+      }
+      MLPCG_LAUNCH_CHECK();
+    } else {
+      void *dst = (l == 0) ? (void *)z : P.xout[l];
+      const int ddt = (l == 0) ? MLPCG_F32 : P.adt;
+      RET_IF(launch_avg_pool2_adjoint(P.xout[l + 1], tmp0, P.adt, 1, v.n1, v.n2, v.n3, st));
+      RET_IF(launch_axpby(c0, skip, c1, tmp0, tmp0, P.adt, v.n, st));
+      RET_IF(launch_stencil_apply(P.Kpre[l], P.kdt, v.ps, tmp0, P.adt, 0, dst, ddt, 1, v.n1, v.n2, v.n3, 1, st));
+      if (l == 0) {
+        k_apply_mask<float><<<blocks_for(v.n, 256), 256, 0, st>>>((float *)dst, P.fmask, v.n);
+        MLPCG_LAUNCH_CHECK();
+      }
+    }
+  }
+  return MLPCG_OK;
+}
+
 // Stages of one application, in launch order: 0..L-1 = pre-block of level s,
 // L = coarsest block, L+1..2L = post-block of level 2L-s.  [s0, s1] selects a range.
 template <typename KT, typename AT>
 static int run_apply(const PrecondPlan &P, const float *r, const float *rscale, float *z, void *tmp0,
                      cudaStream_t st, int s0 = 0, int s1 = 1 << 20, const int *gate = nullptr) {
+  if (P.kind == MLPCG_PRECOND_SPD) return run_apply_spd<KT, AT>(P, r, rscale, z, tmp0, st, s0, s1, gate);
   const int L = P.L;
   const uint8_t *m0 = P.mask ? P.fmask : nullptr;
   // ---- down sweep
@@ -1636,6 +1808,14 @@ int mlpcg_precond_create_spd(int N1, int N2, int N3, int levels, int k_dtype, in
   return precond_create(N1, N2, N3, levels, k_dtype, act_dtype, 0, 0, coeff_layout, MLPCG_PRECOND_SMALL_SPD, out);
 }
 
+int mlpcg_precond_create_kind(int N1, int N2, int N3, int levels, int kind, int k_dtype, int act_dtype,
+                              int coeff_layout, mlpcg_precond **out) {
+  clear_error();
+  MLPCG_REQUIRE(kind == MLPCG_PRECOND_SMALL_SPD || kind == MLPCG_PRECOND_SPD, MLPCG_ERR_ARG,
+                "precond_create_kind: kind must be MLPCG_PRECOND_SMALL_SPD or MLPCG_PRECOND_SPD");
+  return precond_create(N1, N2, N3, levels, k_dtype, act_dtype, 0, 0, coeff_layout, kind, out);
+}
+
 size_t mlpcg_precond_workspace(const mlpcg_precond *h) { return h ? h->p.bytes : 0; }
 
 void mlpcg_precond_destroy(mlpcg_precond *h) { delete h; }
@@ -1654,7 +1834,7 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
   // parameter offsets: pre[0..L-1], post[0..L-1], l (2214 each), c0[0..L-1], c1[0..L-1] (82 each);
   // SPD kind: l0[0..L-1], l, then the linear blocks
   const bool spd = P.kind == MLPCG_PRECOND_SMALL_SPD;
-  const int nblk = spd ? L + 1 : 2 * L + 1;
+  const int nblk = spd ? L + 1 : 2 * L + 1;  // SPD kind: l0, l1, l like pre, post, l
   auto blk_w = [&](int b) { return params + (size_t)b * 2214; };
   auto blk_b = [&](int b) { return params + (size_t)b * 2214 + 2187; };
   const float *linp = params + (size_t)nblk * 2214;
@@ -1671,10 +1851,10 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
   for (int l = 0; l <= L; ++l) any_cls = any_cls || P.lv[l].cls;
   if (any_cls) {
     if (P.kdt == MLPCG_BF16) {
-      k_kgen_uniform_all<__nv_bfloat16><<<nblk, 3 * KREC, 0, st>>>(params, P.Uall, spd ? L : 0);
+      k_kgen_uniform_all<__nv_bfloat16><<<nblk, 3 * KREC, 0, st>>>(params, P.Uall, L, P.kind);
       k_material_records<__nv_bfloat16><<<uniform_blocks(P), 256, 0, st>>>(P.Uall, (__nv_bfloat16 *)P.Mrec);
     } else {
-      k_kgen_uniform_all<float><<<nblk, 3 * KREC, 0, st>>>(params, P.Uall, spd ? L : 0);
+      k_kgen_uniform_all<float><<<nblk, 3 * KREC, 0, st>>>(params, P.Uall, L, P.kind);
       k_material_records<float><<<uniform_blocks(P), 256, 0, st>>>(P.Uall, (float *)P.Mrec);
     }
     MLPCG_LAUNCH_CHECK();
@@ -1724,11 +1904,28 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
     MLPCG_LAUNCH_CHECK();
     return MLPCG_OK;
   };
-  // the transposed block of forward block (Kf, uniform slot uf) at level l into Kt (slot ut): on
-  // a classed level the class map of the neighbourhoods, then its general cells gathered from
-  // the forward records and its mixed runs' uniform cells; on a dense tiled level the planes
-  // gathered; a general-path level applies the forward planes transposed and needs nothing
-  auto gen_transpose = [&](int l, void *Kf, int uf, void *Kt, int ut) -> int {
+  // The transposed blocks of level l.  classify_t: on a classed level, the class map of the
+  // neighbourhoods (from the forward class bytes), its tile scans and general-cell / mixed-run
+  // lists, shared by every transposed block of the level.  gather_t: the transposed block of
+  // forward block (Kf, uniform slot uf) into Kt (slot ut) -- general cells gathered from the
+  // forward records, the mixed runs' uniform cells filled; on a dense tiled level the planes
+  // gathered; a general-path level applies the forward planes transposed and needs nothing.
+  auto classify_t = [&](int l) -> int {
+    const auto &v = P.lv[l];
+    if (!v.cls) return MLPCG_OK;
+    k_classify<true><<<grid_of(v), PT, 0, st>>>(nullptr, P.cls[l], v.n1, v.n2, v.n3, P.clsT[l], P.rwT[l],
+                                                P.rcountT[l], P.gcountT[l]);
+    MLPCG_LAUNCH_CHECK();
+    k_scan_tiles<<<1, 1024, 0, st>>>(P.rcountT[l], P.rbaseT[l], (int)v.ntiles);
+    MLPCG_LAUNCH_CHECK();
+    k_scan_tiles<<<1, 1024, 0, st>>>(P.gcountT[l], P.gbaseT[l], (int)v.ntiles);
+    MLPCG_LAUNCH_CHECK();
+    k_list_general<<<grid_of(v), PT, 0, st>>>(P.clsT[l], v.n1, v.n2, v.n3, P.gbaseT[l], P.glist, P.rwT[l],
+                                              P.rbaseT[l], P.rlist);
+    MLPCG_LAUNCH_CHECK();
+    return MLPCG_OK;
+  };
+  auto gather_t = [&](int l, void *Kf, int uf, void *Kt, int ut) -> int {
     const auto &v = P.lv[l];
     if (!v.fast) return MLPCG_OK;
     if (!v.cls) {
@@ -1741,16 +1938,6 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
       MLPCG_LAUNCH_CHECK();
       return MLPCG_OK;
     }
-    k_classify<true><<<grid_of(v), PT, 0, st>>>(nullptr, P.cls[l], v.n1, v.n2, v.n3, P.clsT[l], P.rwT[l],
-                                                P.rcountT[l], P.gcountT[l]);
-    MLPCG_LAUNCH_CHECK();
-    k_scan_tiles<<<1, 1024, 0, st>>>(P.rcountT[l], P.rbaseT[l], (int)v.ntiles);
-    MLPCG_LAUNCH_CHECK();
-    k_scan_tiles<<<1, 1024, 0, st>>>(P.gcountT[l], P.gbaseT[l], (int)v.ntiles);
-    MLPCG_LAUNCH_CHECK();
-    k_list_general<<<grid_of(v), PT, 0, st>>>(P.clsT[l], v.n1, v.n2, v.n3, P.gbaseT[l], P.glist, P.rwT[l],
-                                              P.rbaseT[l], P.rlist);
-    MLPCG_LAUNCH_CHECK();
     const uint32_t *lb = P.gbaseT[l] + v.ntiles - 1, *lc = P.gcountT[l] + v.ntiles - 1;
     const uint32_t *rlb = P.rbaseT[l] + v.ntiles - 1, *rlc = P.rcountT[l] + v.ntiles - 1;
     const float *kf = P.Uall + (size_t)uf * 3 * KREC, *kt = P.Uall + (size_t)ut * 3 * KREC;
@@ -1770,17 +1957,29 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
     MLPCG_LAUNCH_CHECK();
     return MLPCG_OK;
   };
-  if (spd) {
+  if (P.kind == MLPCG_PRECOND_SMALL_SPD) {
     // l0[l] forward (slot l) and transposed (slot L + l); l forward (slot 2L) and transposed (2L + 1)
     for (int l = 0; l < L; ++l) {
       RET_IF(gen_level(l, (l == 0) ? image : P.img[l], l, P.Kpre[l], -1, nullptr));
-      RET_IF(gen_transpose(l, P.Kpre[l], l, P.Kpost[l], L + l));
+      RET_IF(classify_t(l));
+      RET_IF(gather_t(l, P.Kpre[l], l, P.Kpost[l], L + l));
     }
     RET_IF(gen_level(L, P.img[L], L, P.Kl, -1, nullptr, 2 * L));
-    RET_IF(gen_transpose(L, P.Kl, 2 * L, P.Klt, 2 * L + 1));
+    RET_IF(classify_t(L));
+    RET_IF(gather_t(L, P.Kl, 2 * L, P.Klt, 2 * L + 1));
   } else {
     for (int l = 0; l < L; ++l) RET_IF(gen_level(l, (l == 0) ? image : P.img[l], l, P.Kpre[l], L + l, P.Kpost[l]));
     RET_IF(gen_level(L, P.img[L], 2 * L, P.Kl, -1, nullptr));
+    if (P.kind == MLPCG_PRECOND_SPD) {
+      // l0[l] (slot l) -> l0_t (slot 2L + 1 + l); l1[l] (slot L + l) -> l1_t (3L + 1 + l); l -> l_t (4L + 1)
+      for (int l = 0; l < L; ++l) {
+        RET_IF(classify_t(l));
+        RET_IF(gather_t(l, P.Kpre[l], l, P.KpreT[l], 2 * L + 1 + l));
+        RET_IF(gather_t(l, P.Kpost[l], L + l, P.KpostT[l], 3 * L + 1 + l));
+      }
+      RET_IF(classify_t(L));
+      RET_IF(gather_t(L, P.Kl, 2 * L, P.Klt, 4 * L + 1));
+    }
   }
   // c0 / c1 of every level (the linear blocks of sm_model_3d.py:236-239)
   for (int l = 0; l < L; ++l) {
@@ -1820,8 +2019,9 @@ int mlpcg_precond_apply_stages(const mlpcg_precond *h, int first, int last, cons
   MLPCG_REQUIRE(h && r && z, MLPCG_ERR_ARG, "precond_apply_stages: NULL argument");
   const PrecondPlan &P = h->p;
   MLPCG_REQUIRE(P.ready, MLPCG_ERR_ARG, "precond_apply_stages: plan not set up");
-  MLPCG_REQUIRE(first >= 0 && last <= 2 * P.L && first <= last, MLPCG_ERR_ARG,
-                "precond_apply_stages: stage range [%d, %d] outside [0, %d]", first, last, 2 * P.L);
+  const int last_stage = P.kind == MLPCG_PRECOND_SPD ? 4 * P.L + 1 : 2 * P.L;
+  MLPCG_REQUIRE(first >= 0 && last <= last_stage && first <= last, MLPCG_ERR_ARG,
+                "precond_apply_stages: stage range [%d, %d] outside [0, %d]", first, last, last_stage);
   cudaStream_t st = as_stream(stream);
   void *tmp0 = (char *)P.scratch + al256(96 * sizeof(float));
   if (P.kdt == MLPCG_BF16 && P.adt == MLPCG_BF16)
@@ -1837,7 +2037,7 @@ static int class_counts(const mlpcg_precond *h, int level, bool transposed, int6
                 "precond_class_counts: bad argument");
   const PrecondPlan &P = h->p;
   MLPCG_REQUIRE(P.ready, MLPCG_ERR_ARG, "precond_class_counts: plan not set up");
-  MLPCG_REQUIRE(!transposed || P.kind == MLPCG_PRECOND_SMALL_SPD, MLPCG_ERR_ARG,
+  MLPCG_REQUIRE(!transposed || has_transposes(P), MLPCG_ERR_ARG,
                 "precond_class_counts_transposed: the plan has no transposed blocks");
   const auto &v = P.lv[level];
   if (!v.cls) {

@@ -21,16 +21,33 @@ from .ops import _check, _p, _stream
 _DT = {torch.float32: F32, torch.bfloat16: BF16}
 
 
+KIND_SM, KIND_SMALL_SPD, KIND_SPD = 0, 1, 2   # MLPCG_PRECOND_* of the header
+
+
+def network_kind(model) -> int:
+    from .sm_model_3d import SmallSPDSMModelDn3D, SPDSMModelDn3D
+    if isinstance(model, SmallSPDSMModelDn3D):
+        return KIND_SMALL_SPD
+    if isinstance(model, SPDSMModelDn3D):
+        return KIND_SPD
+    return KIND_SM
+
+
 def _is_small_spd(model) -> bool:
-    from .sm_model_3d import SmallSPDSMModelDn3D
-    return isinstance(model, SmallSPDSMModelDn3D)
+    return network_kind(model) == KIND_SMALL_SPD
 
 
 def pack_params(model) -> torch.Tensor:
     """Flat F32 parameter vector in the order mlpcg_precond_setup expects: blocks pre, post, l
-    (SmallSPDSMModelDn3D: l0, l), then the linear blocks c0, c1."""
+    (SmallSPDSMModelDn3D: l0, l; SPDSMModelDn3D: l0, l1, l), then the linear blocks c0, c1."""
     n = model.n
-    blocks = list(model.l0) + [model.l] if _is_small_spd(model) else list(model.pre) + list(model.post) + [model.l]
+    kind = network_kind(model)
+    if kind == KIND_SMALL_SPD:
+        blocks = list(model.l0) + [model.l]
+    elif kind == KIND_SPD:
+        blocks = list(model.l0) + list(model.l1) + [model.l]
+    else:
+        blocks = list(model.pre) + list(model.post) + [model.l]
     parts = []
     for blk in blocks:
         parts += [blk.weight.detach().reshape(-1), blk.bias.detach().reshape(-1)]
@@ -44,9 +61,9 @@ def pack_params(model) -> torch.Tensor:
 class PrecondPlan:
     """z = M r for one image; ``apply`` is graph-capturable (no host sync, no allocation with ``out``).
 
-    ``model`` is a SmallSMModelDn3D or a SmallSPDSMModelDn3D (M = S^T S, for
-    textbook PCG); ``coefficients()`` returns c0, c1 (the squares for the SPD
-    network)."""
+    ``model`` is a SmallSMModelDn3D, a SmallSPDSMModelDn3D (M = S^T S) or an
+    SPDSMModelDn3D (M = V^T V) -- the last two for textbook PCG;
+    ``coefficients()`` returns c0, c1 (the squares for SmallSPDSMModelDn3D)."""
 
     LAYOUTS = {"dense": 0, "classed": 1}
 
@@ -58,13 +75,14 @@ class PrecondPlan:
         self.shape = tuple(int(s) for s in image.shape[1:])
         self.levels = model.n
         self.storage, self.act_storage, self.layout = storage, act_storage, layout
-        self.spd = _is_small_spd(model)
+        self.kind = network_kind(model)
+        self.spd = self.kind != KIND_SM
         self.masked = False if self.spd else bool(model.pre[0].mask)
         self.device = image.device
         lib = _lib.load()
         h = C.c_void_p()
         if self.spd:
-            call("mlpcg_precond_create_spd", *self.shape, model.n, _DT[storage], _DT[act_storage],
+            call("mlpcg_precond_create_kind", *self.shape, model.n, self.kind, _DT[storage], _DT[act_storage],
                  self.LAYOUTS[layout], C.byref(h))
         else:
             call("mlpcg_precond_create", *self.shape, model.n, _DT[storage], _DT[act_storage],
@@ -130,7 +148,10 @@ class PrecondPlan:
 
     def stage_names(self):
         n = self.levels
-        return [f"pre{l}" for l in range(n)] + [f"l{n}"] + [f"post{2 * n - s}" for s in range(n + 1, 2 * n + 1)]
+        names = [f"pre{l}" for l in range(n)] + [f"l{n}"] + [f"post{2 * n - s}" for s in range(n + 1, 2 * n + 1)]
+        if self.kind == KIND_SPD:   # V, then V^T
+            names += [f"t_{s}" for s in names]
+        return names
 
     def predict(self, fluid_cells):
         """A model_predict-style callable (test.py:42-51) on compressed FP64 vectors."""

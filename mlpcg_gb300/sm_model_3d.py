@@ -455,6 +455,12 @@ class SPDSMModelDn3D(BaseModel):
         return self._run(image, b, _Steps(False), [] if imgs is None else imgs,
                          [] if c0 is None else c0, [] if c1 is None else c1)
 
+    def precond_plan(self, image, storage=torch.bfloat16, act_storage=None):
+        """Coefficients of every block (and of its transpose) precomputed on ``image``:
+        see precond.PrecondPlan."""
+        from .precond import PrecondPlan
+        return PrecondPlan(self, image, storage=storage, act_storage=act_storage)
+
 
 class SmallSPDSMModelDn3D(BaseModel):
     """Reduced symmetric preconditioner (sm_model_3d.py:388-444): M = S^T S, S the down sweep

@@ -1,5 +1,5 @@
 """Training of SmallSMModelDn3D (the reference's train.py) or of the symmetric SmallSPDSMModelDn3D
-(train_one_scene.py:176) through the hand-written adjoint kernels.
+(train_one_scene.py:176) / SPDSMModelDn3D through the hand-written adjoint kernels.
 
 Loss (per right-hand side b of unit norm, x = f(b) restricted to fluid cells):
   * ``angle`` (default): 1 - cos^2(b, A x), the squared relative residual at
@@ -31,20 +31,22 @@ from . import ops
 from .laplacian import FluidLaplacian
 from .lanczos import lanczos_ritz, mix_rhs
 from .scenes import make_scene
-from .sm_model_3d import SmallSMModelDn3D, SmallSPDSMModelDn3D
+from .sm_model_3d import SmallSMModelDn3D, SmallSPDSMModelDn3D, SPDSMModelDn3D
 
-MODELS = {"smallsm": "smallsm", "small_spd": "smallspd"}   # --model -> weight file prefix
+MODELS = {"smallsm": "smallsm", "small_spd": "smallspd", "spd": "spd"}   # --model -> weight file prefix
 
 
 def make_model(kind, levels):
     if kind == "small_spd":
         return SmallSPDSMModelDn3D(levels)
+    if kind == "spd":
+        return SPDSMModelDn3D(levels)
     return SmallSMModelDn3D(levels, 3, "trilinear")
 
 
 def solve_method(model):
-    """npcg for the symmetric network (textbook PCG is valid), npsd otherwise."""
-    return "npcg" if isinstance(model, SmallSPDSMModelDn3D) else "npsd"
+    """npcg for the symmetric networks (textbook PCG is valid), npsd otherwise."""
+    return "npcg" if isinstance(model, (SmallSPDSMModelDn3D, SPDSMModelDn3D)) else "npsd"
 from .solver import FusedSolver, flags_to_image
 
 
@@ -98,7 +100,7 @@ def near_identity_(model, eps=0.1):
     with torch.no_grad():
         for p in model.parameters():
             p.mul_(eps)
-        first = model.l0[0] if isinstance(model, SmallSPDSMModelDn3D) else model.pre[0]
+        first = model.l0[0] if isinstance(model, (SmallSPDSMModelDn3D, SPDSMModelDn3D)) else model.pre[0]
         first.bias[13] += 1.0
         model.c0[0].bias[0] += 1.0
 

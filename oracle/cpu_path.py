@@ -5,7 +5,8 @@ coefficients are a Conv3d(3 -> 27, k=3, padding 1) of the image, applied to
 the 27 shifted copies of x (unfold).  They are composed in the order of
 SmallSMModelDn3D.forward (sm_model_3d.py:264-287) with trilinear upsampling
 and the linear blocks of SmallLinearBlock3DPY (sm_model_3d_py.py:24-31) in
-their mean-weight form (CPUSPDModel: SmallSPDSMModelDn3D on the same blocks).  The solver is npsd (cg_tests.py:189-284) with an FP64
+their mean-weight form (CPUSPDModel / CPUSPDFullModel: SmallSPDSMModelDn3D / SPDSMModelDn3D on the
+same blocks).  The solver is npsd (cg_tests.py:189-284) with an FP64
 torch CSR matrix and model_predict (test.py:42-51), all on the CPU.
 """
 from __future__ import annotations
@@ -92,6 +93,37 @@ class CPUSPDModel(CPUModel):
             x[i] = F.interpolate(x[i], scale_factor=2) / 8
             x[i - 1] = c0[i - 1] ** 2 * x[i - 1] + c1[i - 1] ** 2 * x[i]
             x[i - 1] = self._block_t(f"l0.{i-1}", imgs[i - 1], x[i - 1])
+        return x[0]
+
+
+class CPUSPDFullModel(CPUSPDModel):
+    """SPDSMModelDn3D (sm_model_3d.py:313-347) on the same torch-CPU blocks: the V-cycle with l0,
+    l, l1 and then its transpose with l1_t, l_t, l0_t."""
+
+    def __call__(self, img, b):
+        n = self.n
+        if self.cache is None:
+            imgs = [img]
+            for _ in range(n):
+                imgs.append(F.avg_pool3d(imgs[-1][None], 2)[0])
+            c0 = [self._linear(f"c0.{i}", imgs[i]) for i in range(n)]
+            c1 = [self._linear(f"c1.{i}", imgs[i]) for i in range(n)]
+            self.cache = (imgs, c0, c1)
+        imgs, c0, c1 = self.cache
+        x = [self._block("l0.0", imgs[0], b)]
+        for i in range(1, n):
+            x.append(self._block(f"l0.{i}", imgs[i], F.avg_pool3d(x[-1], 2)))
+        x.append(self._block("l", imgs[n], F.avg_pool3d(x[-1], 2)))
+        for i in range(n, 0, -1):
+            x[i] = self._block(f"l1.{i-1}", imgs[i - 1], F.interpolate(x[i], scale_factor=2) / 8)
+            x[i - 1] = c0[i - 1] * x[i - 1] + c1[i - 1] * x[i]
+        x = [x[0]]
+        for i in range(n):
+            x.append(F.avg_pool3d(self._block_t(f"l1.{i}", imgs[i], x[i]), 2))
+        x[-1] = self._block_t("l", imgs[n], x[-1])
+        for i in range(n - 1, -1, -1):
+            x[i] = c0[i] * x[i] + c1[i] * (F.interpolate(x[i + 1], scale_factor=2) / 8)
+            x[i] = self._block_t(f"l0.{i}", imgs[i], x[i])
         return x[0]
 
 

@@ -73,12 +73,13 @@ def test_oracle_symmetry(golden, fname, cls, fwd):
     assert float((x * fwd(p, d["image"], x, n)).sum()) >= 0.0
 
 
-def test_cpu_path_small_spd(golden):
-    """The timed CPU baseline's SmallSPDSMModelDn3D (torch-CPU blocks, scatter transpose) against
+@pytest.mark.parametrize("fname,cpu_cls", [("small_spd_16_l3.npz", "CPUSPDModel"), ("spd_16_l2.npz", "CPUSPDFullModel")])
+def test_cpu_path_spd(golden, fname, cpu_cls):
+    """The timed CPU baseline's symmetric networks (torch-CPU blocks, scatter transpose) against
     the reference's output."""
-    from oracle.cpu_path import CPUSPDModel
-    d = golden("small_spd_16_l3.npz")
-    m = CPUSPDModel({k: torch.from_numpy(v) for k, v in _params(d).items()}, int(d["n"]))
+    from oracle import cpu_path
+    d = golden(fname)
+    m = getattr(cpu_path, cpu_cls)({k: torch.from_numpy(v) for k, v in _params(d).items()}, int(d["n"]))
     y = m(torch.from_numpy(d["image"]), torch.from_numpy(d["b"][:1])).numpy()
     assert rel_err(y, d["y_eval"]) < 1e-5
 
@@ -205,15 +206,18 @@ def test_solver_histories_vs_reference(golden, cuda, fname, cls, fwd):
 
 
 # ---------------------------------------------------------------------------- fused plan (GPU)
-def _spd_model(n, dev, seed=0, eps=0.05):
-    """A SmallSPDSMModelDn3D with small random weights around the identity stencil."""
-    from mlpcg_gb300.sm_model_3d import SmallSPDSMModelDn3D
+PLAN_CLASSES = ["SmallSPDSMModelDn3D", "SPDSMModelDn3D"]
+
+
+def _spd_model(n, dev, seed=0, eps=0.05, cls="SmallSPDSMModelDn3D"):
+    """A symmetric network with small random weights around the identity stencil."""
+    from mlpcg_gb300 import sm_model_3d
     torch.manual_seed(seed)
-    m = SmallSPDSMModelDn3D(n).to(dev)
+    m = getattr(sm_model_3d, cls)(n).to(dev)
     with torch.no_grad():
         for p in m.parameters():
             p.mul_(eps)
-        for blk in list(m.l0) + [m.l]:
+        for blk in list(m.l0) + list(getattr(m, "l1", [])) + [m.l]:
             blk.bias[13] += 1.0
         for c in m.c0:
             c.bias[0] += 1.0
@@ -227,38 +231,48 @@ def _scene(shape, seed, dev):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("cls", PLAN_CLASSES)
 @pytest.mark.parametrize("shape,n", [((16, 16, 16), 3), ((32, 16, 24), 3), ((64, 64, 64), 4), ((24, 40, 8), 3)])
-def test_plan_matches_eval_forward(cuda, shape, n):
+def test_plan_matches_eval_forward(cuda, shape, n, cls):
     """The fused plan (transposed blocks gathered from the forward coefficients, nearest x2 / 8
     prolongation fused into the combine) against the drop-in eval_forward on the fluid cells."""
     s, flags, img = _scene(shape, 2, cuda)
     torch.manual_seed(1)
-    from mlpcg_gb300.sm_model_3d import SmallSPDSMModelDn3D
-    m = SmallSPDSMModelDn3D(n).to(cuda)
+    from mlpcg_gb300 import sm_model_3d
+    m = getattr(sm_model_3d, cls)(n).to(cuda)
     plan = m.precond_plan(img, storage=torch.float32)
     b = torch.randn((1, 1) + shape, device=cuda)
     ref = m.eval_forward(img, b)
     ref = torch.where(img[1] == 0, 0.0, ref)
     z = plan.apply(b.reshape(-1)).reshape(ref.shape)
     assert rel_err(z.cpu().numpy(), ref.cpu().numpy()) < 1e-5
+    # the stages one at a time give the same output
+    names = plan.stage_names()
+    assert len(names) == (4 * n + 2 if cls == "SPDSMModelDn3D" else 2 * n + 1)
+    zs = torch.empty_like(z.reshape(-1))
+    for st in range(len(names)):
+        plan.apply_stages(st, st, b.reshape(-1), None, zs)
+    assert torch.equal(zs, z.reshape(-1))
     c = plan.coefficients()
     imgs = [img]
     from mlpcg_gb300 import ops
     for l in range(n):
         c0 = float(m.c0[l].eval_forward(imgs[l]))
-        assert abs(float(c[l]) - c0 * c0) <= 1e-6 * max(1.0, c0 * c0)
+        want = c0 * c0 if cls == "SmallSPDSMModelDn3D" else c0
+        assert abs(float(c[l]) - want) <= 1e-6 * max(1.0, abs(want))
         imgs.append(ops.avg_pool2(imgs[-1]))
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("cls", PLAN_CLASSES)
 @pytest.mark.parametrize("shape,n,seed", [((64, 64, 64), 4, 4), ((32, 48, 64), 3, 9), ((128, 128, 128), 5, 7)])
 @pytest.mark.parametrize("storage", [torch.float32, torch.bfloat16])
-def test_plan_classed_is_bit_identical_to_dense(cuda, shape, n, seed, storage):
+def test_plan_classed_is_bit_identical_to_dense(cuda, shape, n, seed, storage, cls):
     """The transposed blocks' classed records (radius-2 classes, gathered general cells) give
     exactly the dense transposed planes' output."""
     from mlpcg_gb300.precond import PrecondPlan
     s, flags, img = _scene(shape, seed, cuda)
-    m = _spd_model(n, cuda, seed=3)
+    m = _spd_model(n, cuda, seed=3, cls=cls)
     dense = PrecondPlan(m, img, storage=storage, layout="dense")
     cls = PrecondPlan(m, img, storage=storage, layout="classed")
     n0 = int(np.prod(shape))
@@ -270,13 +284,14 @@ def test_plan_classed_is_bit_identical_to_dense(cuda, shape, n, seed, storage):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("cls", PLAN_CLASSES)
 @pytest.mark.parametrize("layout", ["classed", "dense"])
-def test_plan_operator_is_symmetric(cuda, layout):
+def test_plan_operator_is_symmetric(cuda, layout, cls):
     """On fluid-supported vectors the plan's z = D M D r is symmetric positive definite."""
     from mlpcg_gb300.precond import PrecondPlan
     shape = (64, 64, 64)
     s, flags, img = _scene(shape, 5, cuda)
-    m = _spd_model(4, cuda, seed=2, eps=0.2)
+    m = _spd_model(4, cuda, seed=2, eps=0.2, cls=cls)
     plan = PrecondPlan(m, img, storage=torch.float32, layout=layout)
     fluid = (img[1] != 0).reshape(-1)
     g = torch.Generator(device=cuda).manual_seed(0)
@@ -289,14 +304,15 @@ def test_plan_operator_is_symmetric(cuda, layout):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("cls", PLAN_CLASSES)
 @pytest.mark.parametrize("storage", [torch.float32, torch.bfloat16])
-def test_fused_npcg_with_spd_network(cuda, storage):
+def test_fused_npcg_with_spd_network(cuda, storage, cls):
     """Textbook PCG (npcg) in the graph-captured solver with the symmetric network converges, and
     its FP64 residual against the oracle's matrix meets the tolerance."""
     from mlpcg_gb300.solver import FusedSolver
     shape = (64, 64, 64)
     s, flags, img = _scene(shape, 3, cuda)
-    m = _spd_model(4, cuda, seed=4)
+    m = _spd_model(4, cuda, seed=4, cls=cls)
     solver = FusedSolver(m, flags, method="npcg", max_it=500, tol=1e-6, storage=storage)
     b = torch.as_tensor(s.rhs, device=cuda)
     res = solver.solve(b)
