@@ -268,12 +268,12 @@ def test_npsd_npcg_residual_histories(golden, cuda):
     for name in ("npsd", "npcg", "npcg_flex"):
         hist = []
         pred = cg.model_predict(m, img, A.fluid_cells)
-        x, it, timer, res = getattr(cg, name)(b, A, torch.zeros_like(b), pred, 30, tol=1e-6, atol=1e-20,
+        x, it, timer, res = getattr(cg, name)(b, A, torch.zeros_like(b), pred, 50, tol=1e-6, atol=1e-20,
                                               callback=lambda nrm, t: hist.append(nrm))
         ref = d[f"{name}_hist"]
         k = min(len(hist), len(ref))
         h, r = np.array(hist[:k]), ref[:k]
         ok = np.isfinite(r) & (r < 1e3)
-        np.testing.assert_allclose(h[ok][:20], r[ok][:20], rtol=1e-4)
+        np.testing.assert_allclose(h[ok], r[ok], rtol=1e-4)   # the first 50 iterations
         if name != "npcg_flex":
             assert it == int(d[f"{name}_iters"])

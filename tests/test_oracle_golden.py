@@ -126,7 +126,7 @@ def test_product_csr_builder_matches_reference(golden):
 
 
 def test_cg_histories(golden):
-    """npsd / npcg / npcg_flex restated vs the reference's cg_tests.py run (30 its)."""
+    """npsd / npcg / npcg_flex restated vs the reference's cg_tests.py run (50 its)."""
     d = golden("cg_16_l3.npz")
     m = golden("model_16_l3.npz")
     p = _params(m)
@@ -137,12 +137,12 @@ def test_cg_histories(golden):
     pred = ocg.make_predict(lambda g: omodel.forward(p, img, g, n), fluid, flags.shape)
     b = d["rhs"].ravel()[fluid]
     for name, fn in (("npsd", ocg.npsd), ("npcg", ocg.npcg), ("npcg_flex", ocg.npcg_flex)):
-        x, it, hist = fn(b, A, np.zeros_like(b), pred, 30, tol=1e-6, atol=1e-20)
+        x, it, hist = fn(b, A, np.zeros_like(b), pred, 50, tol=1e-6, atol=1e-20)
         ref = d[f"{name}_hist"]
         k = min(len(hist), len(ref))
         h, r = np.array(hist[:k]), ref[:k]
         ok = np.isfinite(r) & (r < 1e3)
-        np.testing.assert_allclose(h[ok][:20], r[ok][:20], rtol=1e-4)
+        np.testing.assert_allclose(h[ok], r[ok], rtol=1e-4)   # every iteration, up to 50
         assert it == int(d[f"{name}_iters"]) or name == "npcg_flex"
 
 
