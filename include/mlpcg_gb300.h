@@ -330,6 +330,11 @@ int mlpcg_precond_apply(const mlpcg_precond *plan, const float *r, const float *
  * writes z.  Used to time the kernels of an application one by one. */
 int mlpcg_precond_apply_stages(const mlpcg_precond *plan, int first, int last, const float *r,
                                const float *r_scale, float *z, void *stream);
+/* After applications (synchronises `stream`): *copy_failed = 1 if a tile
+ * copy of the level-0 pre-block (loaded by the tensor-memory accelerator)
+ * did not complete within the kernel's bounded wait -- the outputs of such
+ * an application are not valid -- else 0. */
+int mlpcg_precond_check(const mlpcg_precond *plan, int *copy_failed, void *stream);
 /* Sizes of level `level` (0 = finest) and whether it runs the tiled kernels
  * (z size a multiple of 8) or the general ones. */
 int mlpcg_precond_level_info(const mlpcg_precond *plan, int level, int *n1, int *n2, int *n3,

@@ -45,6 +45,7 @@ _PROTOS = {
     "mlpcg_precond_create": (_i, [_i, _i, _i, _i, _i, _i, _i, _i, _i, _vp]),
     "mlpcg_precond_create_spd": (_i, [_i, _i, _i, _i, _i, _i, _i, _vp]),
     "mlpcg_precond_create_kind": (_i, [_i, _i, _i, _i, _i, _i, _i, _i, _vp]),
+    "mlpcg_precond_check": (_i, [_vp, _vp, _vp]),
     "mlpcg_precond_class_counts": (_i, [_vp, _i, _vp, _vp, _vp]),
     "mlpcg_precond_class_counts_transposed": (_i, [_vp, _i, _vp, _vp, _vp]),
     "mlpcg_precond_workspace": (_sz, [_vp]),

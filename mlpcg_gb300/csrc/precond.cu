@@ -21,6 +21,9 @@
 // shared loads apiece.  Coefficients stream from HBM as 16-byte vectors
 // (8 BF16 or 4 FP32 values) with the cache-streaming hint, since each is
 // read exactly once per application.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <algorithm>
 #include <type_traits>
 #include <vector>
@@ -50,6 +53,15 @@ __device__ __forceinline__ float4 ldv4(const __nv_bfloat16 *p) {
   const uint2 u = __ldg(reinterpret_cast<const uint2 *>(p));
   return make_float4(__uint_as_float(u.x << 16), __uint_as_float(u.x & 0xffff0000u),
                      __uint_as_float(u.y << 16), __uint_as_float(u.y & 0xffff0000u));
+}
+
+// The 16 tile values S[row][z .. z + 15] (z a multiple of 4) by four 16-byte loads
+__device__ __forceinline__ void ld_row16(const float *row, float xr[16]) {
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const float4 a = reinterpret_cast<const float4 *>(row)[q];
+    xr[4 * q] = a.x; xr[4 * q + 1] = a.y; xr[4 * q + 2] = a.z; xr[4 * q + 3] = a.w;
+  }
 }
 
 // The 12 tile values S[row][z .. z + 11] (z a multiple of 4) by three 16-byte loads
@@ -687,8 +699,11 @@ struct ClsSmem {
 // plane pl = tx + dx of the tile serves run 0 as dx = pl and run 1 as
 // dx = pl - 1, so each of the 12 input rows is read from shared memory once.
 // Per cell the 27 taps are summed in the reference's order (dx, dy, dz).
-// coef(tx, p, kv) yields the 8 coefficients of tap p for run tx.
-template <typename Coef>
+// coef(tx, p, kv) yields the 8 coefficients of tap p for run tx.  OFF is the
+// tile index of the run's z - 1 neighbour relative to 8 tz: 0 for the staged
+// layout (interior from index 1), 3 for the TMA layout (interior from index 4;
+// the row is then read as 16 values from 8 tz, all 16-byte aligned).
+template <int OFF = 0, typename Coef>
 __device__ __forceinline__ void apply_pair(const float (*S)[HY][HZP], int ty, int tz8, Coef coef, float acc[TX][8]) {
 #pragma unroll
   for (int tx = 0; tx < TX; ++tx)
@@ -698,8 +713,9 @@ __device__ __forceinline__ void apply_pair(const float (*S)[HY][HZP], int ty, in
   for (int pl = 0; pl < TX + 2; ++pl)
 #pragma unroll
     for (int dy = 0; dy < 3; ++dy) {
-      float xr[12];
-      ld_row12(&S[pl][ty + dy][tz8], xr);
+      float xr[OFF ? 16 : 12];
+      if constexpr (OFF != 0) ld_row16(&S[pl][ty + dy][tz8], xr);
+      else ld_row12(&S[pl][ty + dy][tz8], xr);
 #pragma unroll
       for (int tx = 0; tx < TX; ++tx) {
         const int dx = pl - tx;
@@ -709,7 +725,7 @@ __device__ __forceinline__ void apply_pair(const float (*S)[HY][HZP], int ty, in
           float kv[8];
           coef(tx, dx * 9 + dy * 3 + dz, kv);
 #pragma unroll
-          for (int c = 0; c < 8; ++c) acc[tx][c] = fmaf(kv[c], xr[c + dz], acc[tx][c]);
+          for (int c = 0; c < 8; ++c) acc[tx][c] = fmaf(kv[c], xr[c + dz + OFF], acc[tx][c]);
         }
       }
     }
@@ -721,7 +737,7 @@ __device__ __forceinline__ void apply_pair(const float (*S)[HY][HZP], int ty, in
 // record like a dense run; warps with no mixed run skip the record path.
 // rwd are the runs' words (load_run_words), trec the tile's first record and
 // mixed-run count (load_tile_runs).
-template <typename KT, bool CLS>
+template <typename KT, bool CLS, int OFF = 0>
 __device__ __forceinline__ void tile_apply(const float (*S)[HY][HZP], const ClsSmem *sm, const CoefArgs<KT> &C,
                                            const uint32_t rwd[TX], uint2 trec, int n1, int n2, int n3,
                                            float acc[TX][8]) {
@@ -735,7 +751,7 @@ __device__ __forceinline__ void tile_apply(const float (*S)[HY][HZP], const ClsS
     int64_t q[TX];
 #pragma unroll
     for (int tx = 0; tx < TX; ++tx) q[tx] = valid[tx] ? ((int64_t)(x0 + tx) * n2 + j) * n3 + k0 : 0;
-    apply_pair(S, ty, tz * 8, [&](int tx, int p, float kv[8]) {
+    apply_pair<OFF>(S, ty, tz * 8, [&](int tx, int p, float kv[8]) {
       if (valid[tx]) ld8cs(C.K + p * C.ps + q[tx], kv);
       else {
 #pragma unroll
@@ -751,7 +767,7 @@ __device__ __forceinline__ void tile_apply(const float (*S)[HY][HZP], const ClsS
     const float *ku[TX];
 #pragma unroll
     for (int tx = 0; tx < TX; ++tx) ku[tx] = sm->Ku[rwd[tx] & 3u];
-    apply_pair(S, ty, tz * 8, [&](int tx, int p, float kv[8]) {
+    apply_pair<OFF>(S, ty, tz * 8, [&](int tx, int p, float kv[8]) {
       const float v = ku[tx][p];
 #pragma unroll
       for (int c = 0; c < 8; ++c) kv[c] = v;
@@ -766,7 +782,7 @@ __device__ __forceinline__ void tile_apply(const float (*S)[HY][HZP], const ClsS
       rp[tx] = mixed[tx] ? C.rec + (size_t)trec.x * RREC + (rwd[tx] >> 2) * 8 : C.mrec + (rwd[tx] & 3u) * RREC;
       st[tx] = mixed[tx] ? trec.y * 8 : 8;
     }
-    apply_pair(S, ty, tz * 8, [&](int tx, int p, float kv[8]) { ld8(rp[tx] + p * st[tx], kv); }, acc);
+    apply_pair<OFF>(S, ty, tz * 8, [&](int tx, int p, float kv[8]) { ld8(rp[tx] + p * st[tx], kv); }, acc);
   }
 }
 
@@ -814,33 +830,70 @@ __device__ __forceinline__ void apply_run_mask(uint2 m, float acc[8]) {
 // ---------------------------------------------------------------------------
 // pre-block (and the coarsest l-block): y = B(x), optional fused avg-pool
 // ---------------------------------------------------------------------------
-template <typename KT, typename XT, typename YT, bool POOL, bool CLS>
-__global__ void __launch_bounds__(PT)
-k_pre_fused(const CoefArgs<KT> C, const XT *__restrict__ x,
-            const float *__restrict__ xscale, YT *__restrict__ y, YT *__restrict__ ypool,
-            const uint8_t *__restrict__ mask, int n1, int n2, int n3, const int *__restrict__ gate) {
-  if (gate && *gate != 0) return;  // batched solves: this system has stopped
-  __shared__ __align__(16) float S[HX][HY][HZP];
+// The body of the pre-block kernels.  Staged: every thread loads its share of
+// the input tile (scaled by xscale) and stores it to shared memory.  TMA
+// (XT = float): thread 0 has the tensor-memory accelerator copy the whole
+// 4 x 18 x 76 box of the input (z from z0 - 4, outside the grid read as 0)
+// into the tile, completing on an mbarrier; the scale is applied to the
+// block's output instead (the block is linear in x).
+template <typename KT, typename XT, typename YT, bool POOL, bool CLS, bool TMA>
+__device__ __forceinline__ void pre_fused_body(const CoefArgs<KT> &C, const XT *__restrict__ x,
+                                               const float *__restrict__ xscale, YT *__restrict__ y,
+                                               YT *__restrict__ ypool, const uint8_t *__restrict__ mask, int n1,
+                                               int n2, int n3, const CUtensorMap *tmap, int *err) {
+  __shared__ __align__(128) float S[HX][HY][HZP];
   __shared__ typename std::conditional<CLS, ClsSmem, int>::type smc_raw;
+  __shared__ __align__(8) uint64_t mbar;
   ClsSmem *smc = CLS ? reinterpret_cast<ClsSmem *>(&smc_raw) : nullptr;
   const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY, x0 = blockIdx.z * TX;
   const float sc = xscale ? __ldg(xscale) : 1.f;
+  const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&mbar);
+  if constexpr (TMA) {
+    if (threadIdx.x == 0) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
+                   "r"((uint32_t)sizeof(S)) : "memory");
+      const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&S[0][0][0]);
+      asm volatile(
+          "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+          ::"r"(dst), "l"(reinterpret_cast<uint64_t>(tmap)), "r"(z0 - 4), "r"(y0 - 1), "r"(x0 - 1), "r"(bar)
+          : "memory");
+    }
+  }
   uint32_t rwd[TX];
   uint2 mw[TX];
   const uint2 tb = load_tile_runs<KT, CLS>(C, n1, n2, n3, rwd);
   load_run_mask(mask, n1, n2, n3, mw);
-  FineStage fs;
-  stage_load(fs, n1, n2, n3,
-             [&](int, int, int, int64_t q) {
-               const float4 v = ldv4(x + q);
-               return make_float4(v.x * sc, v.y * sc, v.z * sc, v.w * sc);
-             },
-             [&](int, int, int, int64_t q) { return ldf(x + q) * sc; });
-  stage_put(S, fs);
+  if constexpr (!TMA) {
+    FineStage fs;
+    stage_load(fs, n1, n2, n3,
+               [&](int, int, int, int64_t q) {
+                 const float4 v = ldv4(x + q);
+                 return make_float4(v.x * sc, v.y * sc, v.z * sc, v.w * sc);
+               },
+               [&](int, int, int, int64_t q) { return ldf(x + q) * sc; });
+    stage_put(S, fs);
+  }
   stage_uniform<CLS>(smc, C.kuni);
-  __syncthreads();
+  __syncthreads();  // also orders the mbarrier initialisation before the other threads' waits
+  if constexpr (TMA) {
+    // bounded wait for the tile (phase 0): a copy that has not landed after about a second of
+    // polling is reported through *err; the CTA then waits (bounded again) and leaves
+    uint32_t done = 0;
+    for (uint32_t it = 0; it < (1u << 22) && !done; ++it)
+      asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0; selp.u32 %0, 1, 0, p; }"
+                   : "=r"(done) : "r"(bar) : "memory");
+    if (!done) {
+      if (threadIdx.x == 0) atomicExch(err, 1);
+      for (uint32_t it = 0; it < (1u << 22) && !done; ++it)
+        asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0; selp.u32 %0, 1, 0, p; }"
+                     : "=r"(done) : "r"(bar) : "memory");
+      return;
+    }
+  }
   float acc[TX][8];
-  tile_apply<KT, CLS>(S, smc, C, rwd, tb, n1, n2, n3, acc);
+  tile_apply<KT, CLS, TMA ? 3 : 0>(S, smc, C, rwd, tb, n1, n2, n3, acc);
   const int tz = run_tz(threadIdx.x), ty = run_ty(threadIdx.x);
   const int k0 = z0 + tz * 8, j = y0 + ty;
   const bool active = k0 < n3 && j < n2;  // n3 % 8 == 0: a run is all in or all out
@@ -850,6 +903,10 @@ k_pre_fused(const CoefArgs<KT> C, const XT *__restrict__ x,
     const int i = x0 + tx;
     if (!active || i >= n1) continue;
     const int64_t q = ((int64_t)i * n2 + j) * n3 + k0;
+    if constexpr (TMA) {
+#pragma unroll
+      for (int c = 0; c < 8; ++c) acc[tx][c] *= sc;
+    }
     apply_run_mask(mw[tx], acc[tx]);
     if (y) st8(y + q, acc[tx]);  // y may be NULL when only the pooled output is wanted
     if (POOL) {
@@ -868,6 +925,27 @@ k_pre_fused(const CoefArgs<KT> C, const XT *__restrict__ x,
       st4(ypool + qc, pool);
     }
   }
+}
+
+// pre-block (and the coarsest l-block): y = B(x), optional fused avg-pool
+template <typename KT, typename XT, typename YT, bool POOL, bool CLS>
+__global__ void __launch_bounds__(PT)
+k_pre_fused(const CoefArgs<KT> C, const XT *__restrict__ x,
+            const float *__restrict__ xscale, YT *__restrict__ y, YT *__restrict__ ypool,
+            const uint8_t *__restrict__ mask, int n1, int n2, int n3, const int *__restrict__ gate) {
+  if (gate && *gate != 0) return;  // batched solves: this system has stopped
+  pre_fused_body<KT, XT, YT, POOL, CLS, false>(C, x, xscale, y, ypool, mask, n1, n2, n3, nullptr, nullptr);
+}
+
+// the level-0 pre-block with its FP32 input tile loaded by TMA through tmap (x only for the
+// pointer-free parts); err receives 1 if a tile copy did not complete
+template <typename KT, typename YT, bool CLS>
+__global__ void __launch_bounds__(PT)
+k_pre_fused_tma(const CoefArgs<KT> C, const __grid_constant__ CUtensorMap tmap, const float *__restrict__ xscale,
+                YT *__restrict__ y, YT *__restrict__ ypool, const uint8_t *__restrict__ mask, int n1, int n2, int n3,
+                const int *__restrict__ gate, int *__restrict__ err) {
+  if (gate && *gate != 0) return;
+  pre_fused_body<KT, float, YT, true, CLS, true>(C, nullptr, xscale, y, ypool, mask, n1, n2, n3, &tmap, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -1218,6 +1296,7 @@ struct PrecondPlan {
   uint8_t *fmask = nullptr;   // fluid mask of level 0
   void *lin_ws = nullptr;
   float *scratch = nullptr;   // 81 floats (linear means)
+  int *err = nullptr;         // set to 1 by a level-0 TMA tile copy that did not complete
   size_t bytes = 0;
   bool ready = false;
 };
@@ -1356,6 +1435,7 @@ static size_t plan_layout(PrecondPlan &P, char *base) {
   P.fmask = (uint8_t *)take(P.lv[0].ps + 64);
   P.lin_ws = take(linear_workspace());
   P.scratch = (float *)take(96 * sizeof(float));
+  P.err = (int *)take(sizeof(int));
   // scratch for the general path: level-0 scaled input and one activation-sized temp
   return off;
 }
@@ -1408,6 +1488,54 @@ int launch_scan_u32(const uint32_t *cnt, uint32_t *base, int n, cudaStream_t st)
 }
 }  // namespace mlpcg
 
+// cuTensorMapEncodeTiled of the driver, looked up once through the runtime (no link to libcuda)
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }();
+  return fn;
+}
+
+// Tensor map of the FP32 fine-grid input r for the level-0 TMA tile loads: dims (N3, N2, N1),
+// box 76 (z) x 18 (y) x 4 (x) = the shared tile, zero fill outside.  The tile's z origin
+// z0 - 4 is a multiple of 4 floats (16 bytes) as TMA requires; N3 % 8 == 0 on a tiled level
+// makes the row strides multiples of 16 bytes.  false if the encoder is unavailable.
+static bool encode_input_map(CUtensorMap *m, const float *r, const PrecondPlan::Level &v) {
+  const auto enc = tensor_map_encoder();
+  if (!enc || ((uintptr_t)r & 15) || v.n3 % 4) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)v.n3, (cuuint64_t)v.n2, (cuuint64_t)v.n1};
+  const cuuint64_t strides[2] = {(cuuint64_t)v.n3 * 4, (cuuint64_t)v.n3 * (cuuint64_t)v.n2 * 4};
+  const cuuint32_t box[3] = {(cuuint32_t)HZP, (cuuint32_t)HY, (cuuint32_t)HX};
+  const cuuint32_t es[3] = {1, 1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(r), dims, strides, box, es,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// The level-0 pre-block (FP32 input r, scaled by rscale): TMA-staged when the tensor map
+// encodes, else the thread-staged kernel.
+template <typename KT, typename AT>
+static int launch_pre0(const PrecondPlan &P, const CoefArgs<KT> &C, const float *r, const float *rscale, AT *y,
+                       AT *ypool, const uint8_t *mask, cudaStream_t st, const int *gate) {
+  const auto &v = P.lv[0];
+  const dim3 g = grid_of(v);
+  CUtensorMap tm;
+  if (encode_input_map(&tm, r, v)) {
+    if (v.cls) k_pre_fused_tma<KT, AT, true><<<g, PT, 0, st>>>(C, tm, rscale, y, ypool, mask, v.n1, v.n2, v.n3, gate, P.err);
+    else k_pre_fused_tma<KT, AT, false><<<g, PT, 0, st>>>(C, tm, rscale, y, ypool, mask, v.n1, v.n2, v.n3, gate, P.err);
+  } else {
+    if (v.cls) k_pre_fused<KT, float, AT, true, true><<<g, PT, 0, st>>>(C, r, rscale, y, ypool, mask, v.n1, v.n2, v.n3, gate);
+    else k_pre_fused<KT, float, AT, true, false><<<g, PT, 0, st>>>(C, r, rscale, y, ypool, mask, v.n1, v.n2, v.n3, gate);
+  }
+  MLPCG_LAUNCH_CHECK();
+  return MLPCG_OK;
+}
+
 // One application of the SPD kind (SPDSMModelDn3D.eval_forward, sm_model_3d.py:313-347): the
 // V-cycle V (stages 0 .. 2L) into v0, then V^T (stages 2L + 1 .. 4L + 1) into z.
 //   V:   y_l = l0[l](x_l), x_{l+1} = pool(y_l); x_L = l(x_L);
@@ -1427,12 +1555,7 @@ static int run_apply_spd(const PrecondPlan &P, const float *r, const float *rsca
     if (v.fast) {
       const CoefArgs<KT> C = coef_args<KT>(P, l, P.Kpre[l], v.cls ? P.Upre[l] : nullptr);
       if (l == 0) {
-        if (v.cls)
-          k_pre_fused<KT, float, AT, true, true><<<grid_of(v), PT, 0, st>>>(
-              C, r, rscale, (AT *)P.y[0], (AT *)P.xin[1], nullptr, v.n1, v.n2, v.n3, gate);
-        else
-          k_pre_fused<KT, float, AT, true, false><<<grid_of(v), PT, 0, st>>>(
-              C, r, rscale, (AT *)P.y[0], (AT *)P.xin[1], nullptr, v.n1, v.n2, v.n3, gate);
+        RET_IF((launch_pre0<KT, AT>(P, C, r, rscale, (AT *)P.y[0], (AT *)P.xin[1], nullptr, st, gate)));
       } else {
         if (v.cls)
           k_pre_fused<KT, AT, AT, true, true><<<grid_of(v), PT, 0, st>>>(
@@ -1567,12 +1690,7 @@ static int run_apply(const PrecondPlan &P, const float *r, const float *rscale, 
     if (v.fast) {
       const CoefArgs<KT> C = coef_args<KT>(P, l, P.Kpre[l], v.cls ? P.Upre[l] : nullptr);
       if (l == 0) {
-        if (v.cls)
-          k_pre_fused<KT, float, AT, true, true><<<grid_of(v), PT, 0, st>>>(
-              C, r, rscale, (AT *)P.y[0], (AT *)P.xin[1], m0, v.n1, v.n2, v.n3, gate);
-        else
-          k_pre_fused<KT, float, AT, true, false><<<grid_of(v), PT, 0, st>>>(
-              C, r, rscale, (AT *)P.y[0], (AT *)P.xin[1], m0, v.n1, v.n2, v.n3, gate);
+        RET_IF((launch_pre0<KT, AT>(P, C, r, rscale, (AT *)P.y[0], (AT *)P.xin[1], m0, st, gate)));
       } else {
         if (v.cls)
           k_pre_fused<KT, AT, AT, true, true><<<grid_of(v), PT, 0, st>>>(
@@ -1830,6 +1948,7 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
   MLPCG_REQUIRE(((uintptr_t)workspace & 255) == 0, MLPCG_ERR_ALIGN, "precond workspace must be 256-byte aligned");
   cudaStream_t st = as_stream(stream);
   plan_layout(P, (char *)workspace);
+  MLPCG_CUDA_CHECK(cudaMemsetAsync(P.err, 0, sizeof(int), st));
   const int L = P.L;
   // parameter offsets: pre[0..L-1], post[0..L-1], l (2214 each), c0[0..L-1], c1[0..L-1] (82 each);
   // SPD kind: l0[0..L-1], l, then the linear blocks
@@ -2071,6 +2190,17 @@ int mlpcg_precond_class_counts_transposed(const mlpcg_precond *h, int level, int
                                           int64_t *mixed_runs, void *stream) {
   clear_error();
   return class_counts(h, level, true, general_cells, mixed_runs, stream);
+}
+
+int mlpcg_precond_check(const mlpcg_precond *h, int *copy_failed, void *stream) {
+  clear_error();
+  MLPCG_REQUIRE(h && copy_failed && h->p.ready, MLPCG_ERR_ARG, "precond_check: bad argument");
+  cudaStream_t st = as_stream(stream);
+  int v = 0;
+  MLPCG_CUDA_CHECK(cudaMemcpyAsync(&v, h->p.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  MLPCG_CUDA_CHECK(cudaStreamSynchronize(st));
+  *copy_failed = v;
+  return MLPCG_OK;
 }
 
 int mlpcg_precond_level_info(const mlpcg_precond *h, int level, int *n1, int *n2, int *n3, int *fast) {

@@ -125,6 +125,12 @@ class PrecondPlan:
         call("mlpcg_precond_class_counts", self._h, int(level), C.byref(g), C.byref(r), _stream(self.device))
         return g.value, r.value
 
+    def copy_failed(self) -> bool:
+        """True if a level-0 tile copy of an application so far did not complete (mlpcg_precond_check)."""
+        v = C.c_int()
+        call("mlpcg_precond_check", self._h, C.byref(v), _stream(self.device))
+        return bool(v.value)
+
     def class_counts_transposed(self, level: int):
         """(general cells, mixed runs) of the transposed block of a classed level (SPD plans)."""
         g, r = C.c_int64(), C.c_int64()

@@ -281,6 +281,27 @@ def make_cg(ref_cg, model, scene, max_it=50):
     return out
 
 
+def make_cg_near_identity(ref_cg, ref_model, ref_py, shape, n, seed_scene, max_it=50):
+    """Solver histories over max_it iterations with the reference's SmallSMModelDn3D(n) drawn under
+    torch.manual_seed(0) and moved near the identity (weights x 0.1, centre tap of pre[0] and the
+    bias of c0[0] + 1), so that the residual falls steadily instead of stagnating."""
+    ref_model.smblock3d = _BlockAdapter(ref_py, False)
+    ref_model.smblocktrans3d = _BlockAdapter(ref_py, True)
+    ref_model.smlinear3d = _LinearAdapter(ref_py)
+    torch.manual_seed(0)
+    model = ref_model.SmallSMModelDn3D(n, 3, "trilinear")
+    with torch.no_grad():
+        for p in model.parameters():
+            p.mul_(0.1)
+        model.pre[0].bias[13] += 1.0
+        model.c0[0].bias[0] += 1.0
+    scene = make_scene(shape, seed_scene)
+    out = make_cg(ref_cg, model, scene, max_it=max_it)
+    out.update({"param:" + k: v.detach().numpy().copy() for k, v in model.state_dict().items()})
+    out.update(image=scene.image(), n=np.array(n))
+    return out
+
+
 def make_scene_files(ref_lap, ref_read, shape, seed, frame=1):
     """A small scene as the reference's simulator files: the matrix and the rhs written by the
     reference's own writers (lib/write_data.py), the flags in the C++ Serialize layout that
@@ -326,6 +347,11 @@ def main(ref_root: str, only: str | None = None):
     if only == "spd":
         print("SPD fixtures written to", HERE)
         return
+    if only == "near_identity":
+        np.savez_compressed(HERE / "cg_16_l3_near_identity.npz",
+                            **make_cg_near_identity(ref_cg, ref_model, ref_py, (16, 16, 16), 3, seed_scene=3))
+        print("near-identity solver fixture written to", HERE)
+        return
     for shape, seed in (((8, 8, 8), 0), ((6, 4, 10), 1), ((16, 16, 16), 2)):
         out = make_ops(ref_py, shape, seed)
         out = {k: v for k, v in out.items() if v is not None}
@@ -340,12 +366,14 @@ def main(ref_root: str, only: str | None = None):
                             **{k: v.detach().numpy() for k, v in m.state_dict().items()})
     np.savez_compressed(HERE / "laplacian_12.npz", **make_laplacian(ref_lap, ref_read, (12, 12, 12), 5))
     np.savez_compressed(HERE / "cg_16_l3.npz", **make_cg(ref_cg, model, scene))
+    np.savez_compressed(HERE / "cg_16_l3_near_identity.npz",
+                        **make_cg_near_identity(ref_cg, ref_model, ref_py, (16, 16, 16), 3, seed_scene=3))
     np.savez_compressed(HERE / "scene_files_8.npz", **make_scene_files(ref_lap, ref_read, (8, 8, 8), 4))
     print("fixtures written to", HERE)
 
 
 if __name__ == "__main__":
-    # python make_golden.py [reference root] [--only=scene_files | --only=spd]
+    # python make_golden.py [reference root] [--only=scene_files | --only=spd | --only=near_identity]
     args = [a for a in sys.argv[1:] if not a.startswith("--only")]
     only = next((a.split("=", 1)[1] for a in sys.argv[1:] if a.startswith("--only=")), None)
     main(args[0] if args else "/root/reference", only)

@@ -334,3 +334,18 @@ def test_all_solid_grid(cuda):
     solver = FusedSolver(m, flags, method="npcg", max_it=5, tol=1e-6)
     r = solver.solve(torch.ones((16, 16, 16), dtype=torch.float64, device=cuda))
     assert r.status == "converged" and r.iterations == 0
+
+
+def test_tile_copies_complete(cuda):
+    """The level-0 pre-block's input tiles (loaded by the tensor-memory accelerator) all land: the
+    plan's copy-failure flag stays clear over applications and a graph-captured solve."""
+    from mlpcg_gb300.solver import FusedSolver
+    s, flags, img = _scene((64, 64, 64), 3, cuda)
+    m = _near_identity_model(4, cuda)
+    solver = FusedSolver(m, flags, method="npsd", max_it=60, tol=1e-6, storage=torch.bfloat16)
+    for _ in range(3):
+        solver.plan.apply(torch.randn(64 ** 3, device=cuda))
+    res = solver.solve(torch.as_tensor(s.rhs, device=cuda))
+    assert res.status in ("converged", "max_it") and np.isfinite(res.rel_res)
+    assert res.history[-1] < 0.1 * res.history[0]
+    assert not solver.plan.copy_failed()

@@ -146,6 +146,21 @@ def test_cg_histories(golden):
         assert it == int(d[f"{name}_iters"]) or name == "npcg_flex"
 
 
+def test_cg_histories_near_identity_50(golden):
+    """The oracle's solvers against the reference's over 50 iterations with the near-identity
+    network (the fixture also pins the plain GPU path)."""
+    d = golden("cg_16_l3_near_identity.npz")
+    p = _params(d)
+    n = int(d["n"])
+    flags = d["flags"]
+    A, fluid = olap.assemble(flags)
+    pred = ocg.make_predict(lambda g: omodel.forward(p, d["image"], g, n), fluid, flags.shape)
+    b = d["rhs"].ravel()[fluid]
+    for name, fn in (("npsd", ocg.npsd), ("npcg", ocg.npcg), ("npcg_flex", ocg.npcg_flex)):
+        x, it, hist = fn(b, A, np.zeros_like(b), pred, 50, tol=1e-6, atol=1e-20)
+        np.testing.assert_allclose(np.array(hist), d[f"{name}_hist"], rtol=1e-4, err_msg=name)
+
+
 def test_fp64_cg_oracle_converges():
     from mlpcg_gb300.scenes import make_scene
     s = make_scene(12, 4)
