@@ -830,6 +830,41 @@ __device__ __forceinline__ void apply_run_mask(uint2 m, float acc[8]) {
 // ---------------------------------------------------------------------------
 // pre-block (and the coarsest l-block): y = B(x), optional fused avg-pool
 // ---------------------------------------------------------------------------
+// Thread 0: initialise the tile's mbarrier (one arrival + the byte count) and have the
+// tensor-memory accelerator copy the 4 x 18 x 76 FP32 box of the tile's input -- z from
+// z0 - 4 (a multiple of 4 floats, 16 bytes), y from y0 - 1, x from x0 - 1, zero outside
+// the grid -- into S (interior cell z0 + c at row index c + 4).
+__device__ __forceinline__ void tma_tile_issue(float (*S)[HY][HZP], uint32_t bar, const CUtensorMap *tmap) {
+  if (threadIdx.x != 0) return;
+  const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY, x0 = blockIdx.z * TX;
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
+               "r"((uint32_t)(HX * HY * HZP * sizeof(float))) : "memory");
+  const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&S[0][0][0]);
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+      ::"r"(dst), "l"(reinterpret_cast<uint64_t>(tmap)), "r"(z0 - 4), "r"(y0 - 1), "r"(x0 - 1), "r"(bar)
+      : "memory");
+}
+
+// All threads, after a __syncthreads that follows tma_tile_issue: wait for the tile (phase 0)
+// with a bounded poll.  A copy that has not landed after about a second is reported through
+// *err; the thread then waits once more (bounded) and the caller leaves.  Returns true when
+// the tile is in place.
+__device__ __forceinline__ bool tma_tile_wait(uint32_t bar, int *err) {
+  uint32_t done = 0;
+  for (uint32_t it = 0; it < (1u << 22) && !done; ++it)
+    asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0; selp.u32 %0, 1, 0, p; }"
+                 : "=r"(done) : "r"(bar) : "memory");
+  if (done) return true;
+  if (threadIdx.x == 0) atomicExch(err, 1);
+  for (uint32_t it = 0; it < (1u << 22) && !done; ++it)
+    asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0; selp.u32 %0, 1, 0, p; }"
+                 : "=r"(done) : "r"(bar) : "memory");
+  return false;
+}
+
 // The body of the pre-block kernels.  Staged: every thread loads its share of
 // the input tile (scaled by xscale) and stores it to shared memory.  TMA
 // (XT = float): thread 0 has the tensor-memory accelerator copy the whole
@@ -848,19 +883,7 @@ __device__ __forceinline__ void pre_fused_body(const CoefArgs<KT> &C, const XT *
   const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY, x0 = blockIdx.z * TX;
   const float sc = xscale ? __ldg(xscale) : 1.f;
   const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&mbar);
-  if constexpr (TMA) {
-    if (threadIdx.x == 0) {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
-      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
-                   "r"((uint32_t)sizeof(S)) : "memory");
-      const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&S[0][0][0]);
-      asm volatile(
-          "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
-          ::"r"(dst), "l"(reinterpret_cast<uint64_t>(tmap)), "r"(z0 - 4), "r"(y0 - 1), "r"(x0 - 1), "r"(bar)
-          : "memory");
-    }
-  }
+  if constexpr (TMA) tma_tile_issue(S, bar, tmap);
   uint32_t rwd[TX];
   uint2 mw[TX];
   const uint2 tb = load_tile_runs<KT, CLS>(C, n1, n2, n3, rwd);
@@ -878,19 +901,7 @@ __device__ __forceinline__ void pre_fused_body(const CoefArgs<KT> &C, const XT *
   stage_uniform<CLS>(smc, C.kuni);
   __syncthreads();  // also orders the mbarrier initialisation before the other threads' waits
   if constexpr (TMA) {
-    // bounded wait for the tile (phase 0): a copy that has not landed after about a second of
-    // polling is reported through *err; the CTA then waits (bounded again) and leaves
-    uint32_t done = 0;
-    for (uint32_t it = 0; it < (1u << 22) && !done; ++it)
-      asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0; selp.u32 %0, 1, 0, p; }"
-                   : "=r"(done) : "r"(bar) : "memory");
-    if (!done) {
-      if (threadIdx.x == 0) atomicExch(err, 1);
-      for (uint32_t it = 0; it < (1u << 22) && !done; ++it)
-        asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0; selp.u32 %0, 1, 0, p; }"
-                     : "=r"(done) : "r"(bar) : "memory");
-      return;
-    }
+    if (!tma_tile_wait(bar, err)) return;
   }
   float acc[TX][8];
   tile_apply<KT, CLS, TMA ? 3 : 0>(S, smc, C, rwd, tb, n1, n2, n3, acc);
@@ -1118,16 +1129,22 @@ k_up_fine(const CT *__restrict__ xc, const YT *__restrict__ yl, const float *__r
 
 // UPIN: xc is the level's prolongated input u of k_up_fine (already combined
 // with y_l under swap), staged like a pre-block input.
-template <typename KT, typename CT, typename YT, typename OT, bool SWAP, bool CLS, bool UPIN>
-__global__ void __launch_bounds__(PT)
-k_post_fused(const CoefArgs<KT> C, const CT *__restrict__ xc, const YT *__restrict__ yl,
-             const float *__restrict__ c0p, const float *__restrict__ c1p, OT *__restrict__ out,
-             const uint8_t *__restrict__ bmask, const uint8_t *__restrict__ omask, int n1, int n2, int n3,
-             const int *__restrict__ gate) {
-  if (gate && *gate != 0) return;
-  __shared__ __align__(16) float S[HX][HY][HZP];
+// TMA (UPIN, CT = float): the FP32 input u arrives by the tensor-memory accelerator as in the
+// level-0 pre-block (tma_tile_issue / tma_tile_wait).
+template <typename KT, typename CT, typename YT, typename OT, bool SWAP, bool CLS, bool UPIN, bool TMA>
+__device__ __forceinline__ void post_fused_body(const CoefArgs<KT> &C, const CT *__restrict__ xc,
+                                                const YT *__restrict__ yl, const float *__restrict__ c0p,
+                                                const float *__restrict__ c1p, OT *__restrict__ out,
+                                                const uint8_t *__restrict__ bmask,
+                                                const uint8_t *__restrict__ omask, int n1, int n2, int n3,
+                                                const CUtensorMap *tmap, int *err) {
+  static_assert(!TMA || UPIN, "TMA staging needs the prolongated input");
+  __shared__ __align__(128) float S[HX][HY][HZP];
   __shared__ __align__(16) typename std::conditional<UPIN, int, float[CX][CY][CZP]>::type cs_raw;
   __shared__ typename std::conditional<CLS, ClsSmem, int>::type smc_raw;
+  __shared__ __align__(8) uint64_t mbar;
+  const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&mbar);
+  if constexpr (TMA) tma_tile_issue(S, bar, tmap);
   float(*Cs)[CY][CZP] = reinterpret_cast<float(*)[CY][CZP]>(&cs_raw);
   ClsSmem *smc = CLS ? reinterpret_cast<ClsSmem *>(&smc_raw) : nullptr;
   stage_uniform<CLS>(smc, C.kuni);
@@ -1141,10 +1158,12 @@ k_post_fused(const CoefArgs<KT> C, const CT *__restrict__ xc, const YT *__restri
   load_run_mask(bmask, n1, n2, n3, bw);
   load_run_mask(omask, n1, n2, n3, ow);
   if (UPIN) {
-    FineStage fs;
-    stage_load(fs, n1, n2, n3, [&](int, int, int, int64_t q) { return ldv4(xc + q); },
-               [&](int, int, int, int64_t q) { return ldf(xc + q); });
-    stage_put(S, fs);
+    if constexpr (!TMA) {
+      FineStage fs;
+      stage_load(fs, n1, n2, n3, [&](int, int, int, int64_t q) { return ldv4(xc + q); },
+                 [&](int, int, int, int64_t q) { return ldf(xc + q); });
+      stage_put(S, fs);
+    }
   } else {
     if (SWAP) {  // y_l goes straight into the fine tile; the combine below reads it back in place
       FineStage fs;
@@ -1187,8 +1206,11 @@ k_post_fused(const CoefArgs<KT> C, const CT *__restrict__ xc, const YT *__restri
     }
   }
   __syncthreads();
+  if constexpr (TMA) {
+    if (!tma_tile_wait(bar, err)) return;
+  }
   float accs[TX][8];
-  tile_apply<KT, CLS>(S, smc, C, rwd, tb, n1, n2, n3, accs);
+  tile_apply<KT, CLS, TMA ? 3 : 0>(S, smc, C, rwd, tb, n1, n2, n3, accs);
   const int tz = run_tz(threadIdx.x), ty = run_ty(threadIdx.x);
   const int k0 = z0 + tz * 8, j = y0 + ty;
   if (k0 >= n3 || j >= n2) return;
@@ -1208,6 +1230,29 @@ k_post_fused(const CoefArgs<KT> C, const CT *__restrict__ xc, const YT *__restri
     apply_run_mask(ow[tx], acc);
     st8(out + q, acc);
   }
+}
+
+template <typename KT, typename CT, typename YT, typename OT, bool SWAP, bool CLS, bool UPIN>
+__global__ void __launch_bounds__(PT)
+k_post_fused(const CoefArgs<KT> C, const CT *__restrict__ xc, const YT *__restrict__ yl,
+             const float *__restrict__ c0p, const float *__restrict__ c1p, OT *__restrict__ out,
+             const uint8_t *__restrict__ bmask, const uint8_t *__restrict__ omask, int n1, int n2, int n3,
+             const int *__restrict__ gate) {
+  if (gate && *gate != 0) return;
+  post_fused_body<KT, CT, YT, OT, SWAP, CLS, UPIN, false>(C, xc, yl, c0p, c1p, out, bmask, omask, n1, n2, n3,
+                                                          nullptr, nullptr);
+}
+
+// the post-block on an FP32 prolongated input u loaded by TMA through tmap
+template <typename KT, typename YT, typename OT, bool SWAP, bool CLS>
+__global__ void __launch_bounds__(PT)
+k_post_fused_tma(const CoefArgs<KT> C, const __grid_constant__ CUtensorMap tmap, const YT *__restrict__ yl,
+                 const float *__restrict__ c0p, const float *__restrict__ c1p, OT *__restrict__ out,
+                 const uint8_t *__restrict__ bmask, const uint8_t *__restrict__ omask, int n1, int n2, int n3,
+                 const int *__restrict__ gate, int *__restrict__ err) {
+  if (gate && *gate != 0) return;
+  post_fused_body<KT, float, YT, OT, SWAP, CLS, true, true>(C, nullptr, yl, c0p, c1p, out, bmask, omask, n1, n2,
+                                                            n3, &tmap, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -1428,7 +1473,7 @@ static size_t plan_layout(PrecondPlan &P, char *base) {
     P.xout[l] = take(P.lv[l].ps * sa);
   }
   // the finest level's prolongated input (fast path only; the SPD kind uses it on every level)
-  P.ufine = P.lv[0].fast ? take(P.lv[0].ps * sa) : nullptr;
+  P.ufine = P.lv[0].fast ? take(P.lv[0].ps * sizeof(float)) : nullptr;  // FP32 on level 0 (TMA-staged)
   P.xtmp = P.kind == MLPCG_PRECOND_SMALL_SPD ? take(P.lv[P.L].ps * sa) : nullptr;
   P.v0 = full ? take(P.lv[0].ps * sa) : nullptr;
   P.coef = (float *)take(2 * P.L * sizeof(float));
@@ -1536,6 +1581,26 @@ static int launch_pre0(const PrecondPlan &P, const CoefArgs<KT> &C, const float 
   return MLPCG_OK;
 }
 
+// The finest level's post-block on its prolongated input u (FP32, in P.ufine): TMA-staged when
+// the tensor map encodes, else the thread-staged kernel.
+template <typename KT, typename AT, typename OT, bool SWAP>
+static int launch_post0(const PrecondPlan &P, const CoefArgs<KT> &C, const AT *yl, const float *c0, const float *c1,
+                        OT *out, const uint8_t *bm, const uint8_t *om, cudaStream_t st, const int *gate) {
+  const auto &v = P.lv[0];
+  const dim3 g = grid_of(v);
+  const float *u = (const float *)P.ufine;
+  CUtensorMap tm;
+  if (encode_input_map(&tm, u, v)) {
+    if (v.cls) k_post_fused_tma<KT, AT, OT, SWAP, true><<<g, PT, 0, st>>>(C, tm, yl, c0, c1, out, bm, om, v.n1, v.n2, v.n3, gate, P.err);
+    else k_post_fused_tma<KT, AT, OT, SWAP, false><<<g, PT, 0, st>>>(C, tm, yl, c0, c1, out, bm, om, v.n1, v.n2, v.n3, gate, P.err);
+  } else {
+    if (v.cls) k_post_fused<KT, float, AT, OT, SWAP, true, true><<<g, PT, 0, st>>>(C, u, yl, c0, c1, out, bm, om, v.n1, v.n2, v.n3, gate);
+    else k_post_fused<KT, float, AT, OT, SWAP, false, true><<<g, PT, 0, st>>>(C, u, yl, c0, c1, out, bm, om, v.n1, v.n2, v.n3, gate);
+  }
+  MLPCG_LAUNCH_CHECK();
+  return MLPCG_OK;
+}
+
 // One application of the SPD kind (SPDSMModelDn3D.eval_forward, sm_model_3d.py:313-347): the
 // V-cycle V (stages 0 .. 2L) into v0, then V^T (stages 2L + 1 .. 4L + 1) into z.
 //   V:   y_l = l0[l](x_l), x_{l+1} = pool(y_l); x_L = l(x_L);
@@ -1604,13 +1669,20 @@ static int run_apply_spd(const PrecondPlan &P, const float *r, const float *rsca
     if (v.fast) {
       const CoefArgs<KT> C = coef_args<KT>(P, l, P.Kpost[l], v.cls ? P.Upost[l] : nullptr);
       const dim3 g = grid_of(v);
-      AT *u = (AT *)P.ufine;
-      k_up_fine<AT, AT, AT, false, true><<<g, PT, 0, st>>>((const AT *)P.xout[l + 1], (const AT *)P.y[l], c0, c1, u,
-                                                            v.n1, v.n2, v.n3, gate);
-      MLPCG_LAUNCH_CHECK();
-      if (v.cls) k_post_fused<KT, AT, AT, AT, false, true, true><<<g, PT, 0, st>>>(C, u, (const AT *)P.y[l], c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3, gate);
-      else k_post_fused<KT, AT, AT, AT, false, false, true><<<g, PT, 0, st>>>(C, u, (const AT *)P.y[l], c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3, gate);
-      MLPCG_LAUNCH_CHECK();
+      if (l == 0) {
+        k_up_fine<AT, AT, float, false, true><<<g, PT, 0, st>>>((const AT *)P.xout[1], (const AT *)P.y[0], c0, c1,
+                                                                 (float *)P.ufine, v.n1, v.n2, v.n3, gate);
+        MLPCG_LAUNCH_CHECK();
+        RET_IF((launch_post0<KT, AT, AT, false>(P, C, (const AT *)P.y[0], c0, c1, o, nullptr, nullptr, st, gate)));
+      } else {
+        AT *u = (AT *)P.ufine;
+        k_up_fine<AT, AT, AT, false, true><<<g, PT, 0, st>>>((const AT *)P.xout[l + 1], (const AT *)P.y[l], c0, c1, u,
+                                                              v.n1, v.n2, v.n3, gate);
+        MLPCG_LAUNCH_CHECK();
+        if (v.cls) k_post_fused<KT, AT, AT, AT, false, true, true><<<g, PT, 0, st>>>(C, u, (const AT *)P.y[l], c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3, gate);
+        else k_post_fused<KT, AT, AT, AT, false, false, true><<<g, PT, 0, st>>>(C, u, (const AT *)P.y[l], c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3, gate);
+        MLPCG_LAUNCH_CHECK();
+      }
     } else {
       RET_IF(launch_avg_pool2_adjoint(P.xout[l + 1], tmp0, P.adt, 1, v.n1, v.n2, v.n3, st));
       RET_IF(launch_stencil_apply(P.Kpost[l], P.kdt, v.ps, tmp0, P.adt, 0, o, P.adt, 1, v.n1, v.n2, v.n3, 0, st));
@@ -1647,14 +1719,16 @@ static int run_apply_spd(const PrecondPlan &P, const float *r, const float *rsca
     if (v.fast) {
       const CoefArgs<KT> C = coef_args_t<KT>(P, l, P.KpreT[l], v.cls ? P.UpreT[l] : nullptr);
       const dim3 g = grid_of(v);
-      AT *u = (AT *)P.ufine;
-      k_up_fine<AT, AT, AT, true, true><<<g, PT, 0, st>>>((const AT *)P.xout[l + 1], skip, c0, c1, u, v.n1, v.n2,
-                                                           v.n3, gate);
-      MLPCG_LAUNCH_CHECK();
       if (l == 0) {
-        if (v.cls) k_post_fused<KT, AT, AT, float, true, true, true><<<g, PT, 0, st>>>(C, u, skip, c0, c1, z, nullptr, P.fmask, v.n1, v.n2, v.n3, gate);
-        else k_post_fused<KT, AT, AT, float, true, false, true><<<g, PT, 0, st>>>(C, u, skip, c0, c1, z, nullptr, P.fmask, v.n1, v.n2, v.n3, gate);
+        k_up_fine<AT, AT, float, true, true><<<g, PT, 0, st>>>((const AT *)P.xout[1], skip, c0, c1, (float *)P.ufine,
+                                                                v.n1, v.n2, v.n3, gate);
+        MLPCG_LAUNCH_CHECK();
+        RET_IF((launch_post0<KT, AT, float, true>(P, C, skip, c0, c1, z, nullptr, P.fmask, st, gate)));
       } else {
+        AT *u = (AT *)P.ufine;
+        k_up_fine<AT, AT, AT, true, true><<<g, PT, 0, st>>>((const AT *)P.xout[l + 1], skip, c0, c1, u, v.n1, v.n2,
+                                                             v.n3, gate);
+        MLPCG_LAUNCH_CHECK();
         AT *o = (AT *)P.xout[l];
         if (v.cls) k_post_fused<KT, AT, AT, AT, true, true, true><<<g, PT, 0, st>>>(C, u, skip, c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3, gate);
         else k_post_fused<KT, AT, AT, AT, true, false, true><<<g, PT, 0, st>>>(C, u, skip, c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3, gate);
@@ -1759,14 +1833,16 @@ static int run_apply(const PrecondPlan &P, const float *r, const float *rscale, 
       if (v.fast) {
         const CoefArgs<KT> C = coef_args_t<KT>(P, l, P.Kpost[l], v.cls ? P.Upost[l] : nullptr);
         const dim3 g = grid_of(v);
-        AT *u = (AT *)P.ufine;
-        k_up_fine<AT, AT, AT, true, true><<<g, PT, 0, st>>>((const AT *)P.xout[l + 1], (const AT *)P.y[l], c0, c1, u,
-                                                             v.n1, v.n2, v.n3, gate);
-        MLPCG_LAUNCH_CHECK();
         if (l == 0) {
-          if (v.cls) k_post_fused<KT, AT, AT, float, true, true, true><<<g, PT, 0, st>>>(C, u, (const AT *)P.y[0], c0, c1, z, nullptr, om, v.n1, v.n2, v.n3, gate);
-          else k_post_fused<KT, AT, AT, float, true, false, true><<<g, PT, 0, st>>>(C, u, (const AT *)P.y[0], c0, c1, z, nullptr, om, v.n1, v.n2, v.n3, gate);
+          k_up_fine<AT, AT, float, true, true><<<g, PT, 0, st>>>((const AT *)P.xout[1], (const AT *)P.y[0], c0, c1,
+                                                                  (float *)P.ufine, v.n1, v.n2, v.n3, gate);
+          MLPCG_LAUNCH_CHECK();
+          RET_IF((launch_post0<KT, AT, float, true>(P, C, (const AT *)P.y[0], c0, c1, z, nullptr, om, st, gate)));
         } else {
+          AT *u = (AT *)P.ufine;
+          k_up_fine<AT, AT, AT, true, true><<<g, PT, 0, st>>>((const AT *)P.xout[l + 1], (const AT *)P.y[l], c0, c1, u,
+                                                               v.n1, v.n2, v.n3, gate);
+          MLPCG_LAUNCH_CHECK();
           AT *o = (AT *)P.xout[l];
           if (v.cls) k_post_fused<KT, AT, AT, AT, true, true, true><<<g, PT, 0, st>>>(C, u, (const AT *)P.y[l], c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3, gate);
           else k_post_fused<KT, AT, AT, AT, true, false, true><<<g, PT, 0, st>>>(C, u, (const AT *)P.y[l], c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3, gate);
@@ -1791,18 +1867,16 @@ static int run_apply(const PrecondPlan &P, const float *r, const float *rscale, 
       const AT *xc = (const AT *)P.xout[l + 1], *yl = (const AT *)P.y[l];
       const dim3 g = grid_of(v);
       if (l == 0) {
-        // the finest level: prolongation as its own pass, then the block on u
-        AT *u = (AT *)P.ufine;
+        // the finest level: prolongation as its own pass (FP32 u), then the block on u
+        float *u = (float *)P.ufine;
         if (P.swap) {
-          k_up_fine<AT, AT, AT, true><<<g, PT, 0, st>>>(xc, yl, c0, c1, u, v.n1, v.n2, v.n3, gate);
+          k_up_fine<AT, AT, float, true><<<g, PT, 0, st>>>(xc, yl, c0, c1, u, v.n1, v.n2, v.n3, gate);
           MLPCG_LAUNCH_CHECK();
-          if (v.cls) k_post_fused<KT, AT, AT, float, true, true, true><<<g, PT, 0, st>>>(C, u, yl, c0, c1, z, bm, om, v.n1, v.n2, v.n3, gate);
-          else k_post_fused<KT, AT, AT, float, true, false, true><<<g, PT, 0, st>>>(C, u, yl, c0, c1, z, bm, om, v.n1, v.n2, v.n3, gate);
+          RET_IF((launch_post0<KT, AT, float, true>(P, C, yl, c0, c1, z, bm, om, st, gate)));
         } else {
-          k_up_fine<AT, AT, AT, false><<<g, PT, 0, st>>>(xc, yl, c0, c1, u, v.n1, v.n2, v.n3, gate);
+          k_up_fine<AT, AT, float, false><<<g, PT, 0, st>>>(xc, yl, c0, c1, u, v.n1, v.n2, v.n3, gate);
           MLPCG_LAUNCH_CHECK();
-          if (v.cls) k_post_fused<KT, AT, AT, float, false, true, true><<<g, PT, 0, st>>>(C, u, yl, c0, c1, z, bm, om, v.n1, v.n2, v.n3, gate);
-          else k_post_fused<KT, AT, AT, float, false, false, true><<<g, PT, 0, st>>>(C, u, yl, c0, c1, z, bm, om, v.n1, v.n2, v.n3, gate);
+          RET_IF((launch_post0<KT, AT, float, false>(P, C, yl, c0, c1, z, bm, om, st, gate)));
         }
       } else {
         AT *o = (AT *)P.xout[l];
