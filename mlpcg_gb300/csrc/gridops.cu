@@ -229,26 +229,40 @@ k_class_sums(const float *__restrict__ img, int n1, int n2, int n3, float2 *__re
 
 // One block of 1024 threads: class sums -> 81 shifted means y -> nlin outputs z.
 // Output j uses weights W + j*wstride (81 values), bias[j*bstride], and goes to z[j*zstride].
-__global__ void k_linear_finalize(const float2 *__restrict__ partial, int nblk, int n1, int n2, int n3,
+// cs[c] (c = cls * 3 + channel) = the sum of the blocks' partials of value c: one CTA per value,
+// double-float, in a fixed order (thread t takes blocks t, t + 256, ..., then a fixed tree).
+__global__ void __launch_bounds__(256) k_linear_reduce(const float2 *__restrict__ partial, int nblk,
+                                                       double *__restrict__ cs) {
+  __shared__ float2 ws[8];
+  const int c = blockIdx.x, t = threadIdx.x;
+  float2 v[(kLinBlocks + 255) / 256];
+#pragma unroll
+  for (int u = 0; u < (kLinBlocks + 255) / 256; ++u) {
+    const int b = t + 256 * u;
+    v[u] = b < nblk ? partial[(int64_t)c * nblk + b] : make_float2(0.f, 0.f);
+  }
+  float2 s = v[0];
+#pragma unroll
+  for (int u = 1; u < (kLinBlocks + 255) / 256; ++u) s = df_add(s, v[u]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s = df_add(s, df_shfl_xor(s, o));
+  if ((t & 31) == 0) ws[t >> 5] = s;
+  __syncthreads();
+  if (t == 0) {
+    float2 a = ws[0];
+    for (int w = 1; w < 8; ++w) a = df_add(a, ws[w]);
+    cs[c] = df_to_double(a);
+  }
+}
+
+__global__ void k_linear_finalize(const double *__restrict__ cs_g, int n1, int n2, int n3,
                                   const float *__restrict__ W, int64_t wstride, const float *__restrict__ bias,
                                   int64_t bstride, int nlin, float *__restrict__ z, int64_t zstride,
                                   float *__restrict__ yout) {
   __shared__ double cs[27 * 3];
   __shared__ double ym[81];
   const int t = threadIdx.x;
-  // cs[cls * 3 + channel] = the sum of the blocks' partials (a warp per value,
-  // double-float, fixed order; every load of a lane issued before its first add)
-  for (int c = t >> 5; c < 81; c += blockDim.x >> 5) {
-    float2 s = make_float2(0.f, 0.f);
-#pragma unroll
-    for (int u = 0; u < (kLinBlocks + 31) / 32; ++u) {
-      const int b = (t & 31) + 32 * u;
-      if (b < nblk) s = df_add(s, partial[(int64_t)c * nblk + b]);
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s = df_add(s, df_shfl_xor(s, o));
-    if ((t & 31) == 0) cs[c] = df_to_double(s);
-  }
+  if (t < 81) cs[t] = cs_g[t];
   __syncthreads();
   // shift index k in {0,1,2} (offset k-1) keeps classes: k=0 -> {0,1}, k=1 -> all, k=2 -> {1,2};
   // for an axis of size 1 the single plane is class 0 and only k=1 keeps it.
@@ -521,7 +535,8 @@ int launch_axpby(const float *c0, const void *x, const float *c1, const void *y,
   return MLPCG_OK;
 }
 
-size_t linear_workspace() { return (size_t)27 * 3 * kLinBlocks * sizeof(float2); }
+// the blocks' partials (81 x kLinBlocks double-float pairs), then the 81 reduced sums (FP64)
+size_t linear_workspace() { return (size_t)27 * 3 * kLinBlocks * sizeof(float2) + 81 * sizeof(double); }
 
 int launch_linear_forward_strided(const float *img, int n1, int n2, int n3, const float *W, int64_t wstride,
                                   const float *bias, int64_t bstride, int nlin, float *z, int64_t zstride, float *y,
@@ -530,8 +545,10 @@ int launch_linear_forward_strided(const float *img, int n1, int n2, int n3, cons
                 "sm_linear_3d workspace too small: %zu < %zu", ws_bytes, linear_workspace());
   k_class_sums<<<kLinBlocks, kLinThreads, 0, st>>>(img, n1, n2, n3, (float2 *)ws);
   MLPCG_LAUNCH_CHECK();
-  k_linear_finalize<<<1, 1024, 0, st>>>((const float2 *)ws, kLinBlocks, n1, n2, n3, W, wstride, bias, bstride, nlin,
-                                       z, zstride, y);
+  double *cs = reinterpret_cast<double *>((char *)ws + (size_t)27 * 3 * kLinBlocks * sizeof(float2));
+  k_linear_reduce<<<81, 256, 0, st>>>((const float2 *)ws, kLinBlocks, cs);
+  MLPCG_LAUNCH_CHECK();
+  k_linear_finalize<<<1, 128, 0, st>>>(cs, n1, n2, n3, W, wstride, bias, bstride, nlin, z, zstride, y);
   MLPCG_LAUNCH_CHECK();
   return MLPCG_OK;
 }
