@@ -361,6 +361,7 @@ typedef struct mlpcg_solver mlpcg_solver;
 #define MLPCG_STATUS_MAXIT      2
 #define MLPCG_STATUS_BREAKDOWN  3  /* p.Ap <= 0 */
 #define MLPCG_STATUS_NONFINITE  4  /* NaN / Inf met */
+#define MLPCG_STATUS_COPY_FAILED 5 /* a TMA tile copy did not complete within its bounded wait */
 
 /* The solver keeps `plan` (not owned) as its preconditioner. */
 int mlpcg_solver_create(int N1, int N2, int N3, const mlpcg_precond *plan, int method,

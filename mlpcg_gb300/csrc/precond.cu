@@ -1546,20 +1546,28 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   return fn;
 }
 
-// Tensor map of the FP32 fine-grid input r for the level-0 TMA tile loads: dims (N3, N2, N1),
-// box 76 (z) x 18 (y) x 4 (x) = the shared tile, zero fill outside.  The tile's z origin
-// z0 - 4 is a multiple of 4 floats (16 bytes) as TMA requires; N3 % 8 == 0 on a tiled level
-// makes the row strides multiples of 16 bytes.  false if the encoder is unavailable.
-static bool encode_input_map(CUtensorMap *m, const float *r, const PrecondPlan::Level &v) {
+namespace mlpcg {
+// Tensor map of an FP32 N1 x N2 x N3 grid vector (z fastest) for TMA tile loads of boxes
+// box_z x box_y x box_x, zero fill outside the grid.  The callers' box z origins are multiples
+// of 4 floats (16 bytes) as TMA requires; N3 % 4 == 0 makes the row strides multiples of 16
+// bytes.  false if the encoder is unavailable or the base is not 16-byte aligned.
+bool encode_grid_map(CUtensorMap *m, const float *base, int n1, int n2, int n3, int box_z, int box_y, int box_x) {
   const auto enc = tensor_map_encoder();
-  if (!enc || ((uintptr_t)r & 15) || v.n3 % 4) return false;
-  const cuuint64_t dims[3] = {(cuuint64_t)v.n3, (cuuint64_t)v.n2, (cuuint64_t)v.n1};
-  const cuuint64_t strides[2] = {(cuuint64_t)v.n3 * 4, (cuuint64_t)v.n3 * (cuuint64_t)v.n2 * 4};
-  const cuuint32_t box[3] = {(cuuint32_t)HZP, (cuuint32_t)HY, (cuuint32_t)HX};
+  if (!enc || ((uintptr_t)base & 15) || n3 % 4) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)n3, (cuuint64_t)n2, (cuuint64_t)n1};
+  const cuuint64_t strides[2] = {(cuuint64_t)n3 * 4, (cuuint64_t)n3 * (cuuint64_t)n2 * 4};
+  const cuuint32_t box[3] = {(cuuint32_t)box_z, (cuuint32_t)box_y, (cuuint32_t)box_x};
   const cuuint32_t es[3] = {1, 1, 1};
-  return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(r), dims, strides, box, es,
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(base), dims, strides, box, es,
              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+}  // namespace mlpcg
+
+// Tensor map of the FP32 fine-grid input r (or u) for the level-0 TMA tile loads: box
+// 76 (z) x 18 (y) x 4 (x) = the shared tile.
+static bool encode_input_map(CUtensorMap *m, const float *r, const PrecondPlan::Level &v) {
+  return encode_grid_map(m, r, v.n1, v.n2, v.n3, HZP, HY, HX);
 }
 
 // The level-0 pre-block (FP32 input r, scaled by rscale): TMA-staged when the tensor map

@@ -23,6 +23,8 @@
 // and updates the solver state.  Each loop iteration increments the
 // iteration counter unconditionally and the loop stops at max_it, so the
 // WHILE node always terminates.
+#include <cuda.h>
+
 #include <algorithm>
 #include <vector>
 #include "common.cuh"
@@ -30,11 +32,12 @@
 struct mlpcg_precond;
 namespace mlpcg {
 int precond_apply_gated(const mlpcg_precond *, const float *, const float *, float *, const int *, void *);
+bool encode_grid_map(CUtensorMap *m, const float *base, int n1, int n2, int n3, int box_z, int box_y, int box_x);
 }
 
 namespace mlpcg {
 
-enum { ST_RUNNING = 0, ST_CONVERGED = 1, ST_MAXIT = 2, ST_BREAKDOWN = 3, ST_NONFINITE = 4 };
+enum { ST_RUNNING = 0, ST_CONVERGED = 1, ST_MAXIT = 2, ST_BREAKDOWN = 3, ST_NONFINITE = 4, ST_COPYFAIL = 5 };
 enum { M_NPSD = 0, M_NPCG = 1 };
 
 constexpr int RT = 256;          // threads per reduction block
@@ -562,6 +565,157 @@ __global__ void __launch_bounds__(RT) k_sd_spmv(Vecs V) {
   }
 }
 
+// The same step with q staged in shared memory by TMA: each CTA loops over 4 (x) x 16 (y) x 64 (z)
+// output tiles; thread 0 has the tensor-memory accelerator copy the tile's q box with a one-cell
+// halo (6 x 18 x 76 floats, z from z0 - 4: 16-byte aligned; zero outside the grid) while every
+// thread loads its two 8-cell z-runs' codes, r and p_recent; the 7-point operator then reads the
+// box (same terms, same order as lap4_code).  Thread t takes x planes 2 (t >> 7) + {0, 1} and the
+// (y, z) run of lane pattern run_ty / run_tz, whose 16-byte shared loads of a row are
+// conflict-free with the 76-float row pitch.  Requires N3 % 8 == 0.
+constexpr int SPX = 4, SPY = 16, SPZ = 64;        // output tile
+constexpr int SBX = SPX + 2, SBY = SPY + 2, SBZ = 76;  // q box
+__device__ __forceinline__ int sp_tz(int t) { return (t & 3) | ((t >> 1) & 4); }
+__device__ __forceinline__ int sp_ty(int t) { return ((t >> 2) & 1) | ((t >> 3) & 2) | ((t >> 5) << 2); }
+
+__global__ void __launch_bounds__(RT, 3) k_sd_spmv_tma(Vecs V, const __grid_constant__ CUtensorMap tq0,
+                                                   const __grid_constant__ CUtensorMap tq1,
+                                                   const __grid_constant__ CUtensorMap tq2) {
+  const State &S = *V.st;
+  if (S.status != ST_RUNNING) return;
+  __shared__ __align__(128) float T[SBX][SBY][SBZ];
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ int copy_failed;
+  const int h = S.head, hn = (h + 1) % 3;
+  const CUtensorMap *tm = hn == 0 ? &tq0 : (hn == 1 ? &tq1 : &tq2);
+  const float *P1 = V.p + (size_t)h * V.n;
+  float *AQ = V.Ap + (size_t)hn * V.n;
+  const bool has_prev = S.it >= 1;
+  const int n1 = V.n1, n2 = V.n2, n3 = V.n3;
+  const int tiles_z = (n3 + SPZ - 1) / SPZ, tiles_y = (n2 + SPY - 1) / SPY, tiles_x = (n1 + SPX - 1) / SPX;
+  const int ntiles = tiles_z * tiles_y * tiles_x;
+  const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&mbar);
+  if (threadIdx.x == 0) {
+    copy_failed = 0;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const int tt = threadIdx.x & 127, hx = threadIdx.x >> 7;
+  const int tz = sp_tz(tt), ty = sp_ty(tt);
+  CSum t0, t1, t2;
+  uint32_t phase = 0;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, phase ^= 1u) {
+    const int bz = tile % tiles_z, rest = tile / tiles_z, by = rest % tiles_y, bx = rest / tiles_y;
+    const int z0 = bz * SPZ, y0 = by * SPY, x0 = bx * SPX;
+    if (threadIdx.x == 0) {
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
+                   "r"((uint32_t)sizeof(T)) : "memory");
+      asm volatile(
+          "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+          ::"r"((uint32_t)__cvta_generic_to_shared(&T[0][0][0])), "l"(reinterpret_cast<uint64_t>(tm)), "r"(z0 - 4),
+          "r"(y0 - 1), "r"(x0 - 1), "r"(bar)
+          : "memory");
+    }
+    const int k0 = z0 + 8 * tz, j = y0 + ty;
+    bool valid[2];
+    uint32_t q0[2];
+    uint2 cd[2];
+    float rq[2][8], p1[2][8];
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      const int i = x0 + 2 * hx + r;
+      valid[r] = i < n1 && j < n2 && k0 < n3;
+      q0[r] = valid[r] ? ((uint32_t)i * (uint32_t)n2 + (uint32_t)j) * (uint32_t)n3 + (uint32_t)k0 : 0u;
+      cd[r] = make_uint2(0u, 0u);
+      if (valid[r]) {
+        cd[r] = *reinterpret_cast<const uint2 *>(V.code + q0[r]);
+        ld4(V.r + q0[r], rq[r]);
+        ld4(V.r + q0[r] + 4, rq[r] + 4);
+        if (has_prev) {
+          ld4(P1 + q0[r], p1[r]);
+          ld4(P1 + q0[r] + 4, p1[r] + 4);
+        }
+      }
+    }
+    // bounded wait for the box (phase `phase`); a copy that never lands stops the solve
+    uint32_t done = 0;
+    for (uint32_t it = 0; it < (1u << 22) && !done; ++it)
+      asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+                   : "=r"(done) : "r"(bar), "r"(phase) : "memory");
+    if (!done) {
+      copy_failed = 1;
+      for (uint32_t it = 0; it < (1u << 22) && !done; ++it)  // let a late copy land before leaving
+        asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+                     : "=r"(done) : "r"(bar), "r"(phase) : "memory");
+    }
+    __syncthreads();
+    if (copy_failed) break;
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      if (!valid[r]) continue;
+      const int lx = 2 * hx + r + 1;  // box plane of the run
+      const float *C = &T[lx][ty + 1][8 * tz];
+      float c16[16];
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        const float4 a = reinterpret_cast<const float4 *>(C)[m];
+        c16[4 * m] = a.x; c16[4 * m + 1] = a.y; c16[4 * m + 2] = a.z; c16[4 * m + 3] = a.w;
+      }
+      auto row8 = [&](const float *row, float v[8]) {
+        const float4 a = reinterpret_cast<const float4 *>(row + 4)[0];
+        const float4 b = reinterpret_cast<const float4 *>(row + 4)[1];
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+      };
+      float xm[8], xp[8], ym[8], yp[8];
+      row8(&T[lx - 1][ty + 1][8 * tz], xm);
+      row8(&T[lx + 1][ty + 1][8 * tz], xp);
+      row8(&T[lx][ty][8 * tz], ym);
+      row8(&T[lx][ty + 2][8 * tz], yp);
+      float aq[8];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        float off = 0.f;
+        off += xm[c];
+        off += ym[c];
+        off += c16[c + 3];  // z - 1
+        off += c16[c + 5];  // z + 1
+        off += yp[c];
+        off += xp[c];
+        const uint8_t k = (uint8_t)((c < 4 ? cd[r].x : cd[r].y) >> (8 * (c & 3)));
+        aq[c] = (k & kNotFluid) ? 0.f : (float)k * c16[c + 4] - off;
+      }
+      st4(AQ + q0[r], aq);
+      st4(AQ + q0[r] + 4, aq + 4);
+#pragma unroll
+      for (int gq = 0; gq < 2; ++gq) {
+        float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+#pragma unroll
+        for (int c = 4 * gq; c < 4 * gq + 4; ++c) {
+          s0 = fmaf(c16[c + 4], aq[c], s0);
+          s1 = fmaf(c16[c + 4], rq[r][c], s1);
+          if (has_prev) s2 = fmaf(aq[c], p1[r][c], s2);
+        }
+        t0.add(s0); t1.add(s1); t2.add(s2);
+      }
+    }
+    __syncthreads();  // every thread is done with the box before the next tile's copy
+  }
+  double v[3] = {t0.get(), t1.get(), t2.get()};
+  double o[3];
+  if (reduce_last<3>(v, V, 2, o) && threadIdx.x == 0) {
+    State &W = *V.st;
+    W.alpha[hn] = o[0];
+    W.e_last = o[2];
+    W.head = hn;
+    W.beta = o[1] / o[0];
+    const float2 bdf = df_from_double(W.beta);
+    W.beta_hi = bdf.x;
+    W.beta_lo = bdf.y;
+    if (!(o[0] > 0.0) || !isfinite(W.beta)) W.status = isfinite(o[0]) ? ST_BREAKDOWN : ST_NONFINITE;
+  }
+  if (copy_failed && threadIdx.x == 0) V.st->status = ST_COPYFAIL;
+}
+
 // ---------------------------------------------------------------------------
 // NPCG
 // ---------------------------------------------------------------------------
@@ -741,6 +895,8 @@ struct mlpcg_solver {
   cudaGraphExec_t exec = nullptr;
   cudaStream_t capture_stream = nullptr;  // graphs are captured here, launched on the caller's stream
   int sched_blocks = 0;                    // blocks of the solver's grid-stride kernels (0: automatic)
+  CUtensorMap qmap[3];                     // the three search-direction buffers, for the TMA SpMV
+  bool qmap_ok = false;
 };
 
 struct mlpcg_batch {
@@ -817,7 +973,8 @@ static int enqueue_body(mlpcg_solver *s, cudaStream_t st, cudaGraphConditionalHa
   if (s->method == M_NPSD) {
     k_sd_dots<<<nb, RT, 0, st>>>(V);
     k_sd_qform<<<nb, RT, 0, st>>>(V);
-    k_sd_spmv<<<nb, RT, 0, st>>>(V);
+    if (s->qmap_ok) k_sd_spmv_tma<<<nb, RT, 0, st>>>(V, s->qmap[0], s->qmap[1], s->qmap[2]);
+    else k_sd_spmv<<<nb, RT, 0, st>>>(V);
   } else {
     k_cg_rz<<<nb, RT, 0, st>>>(V);
     k_cg_pspmv<<<nb, RT, 0, st>>>(V);
@@ -878,6 +1035,10 @@ int mlpcg_solver_bind(mlpcg_solver *s, void *workspace, size_t workspace_bytes, 
   int64_t nb = ((int64_t)V.ngroups + RT * UNR - 1) / (RT * UNR);
   if (s->sched_blocks > 0) nb = std::min<int64_t>(nb, s->sched_blocks);
   V.nblk = (int)(nb < 1 ? 1 : (nb > RB_MAX ? RB_MAX : nb));
+  // tensor maps of the three search-direction buffers for the TMA-tiled npsd SpMV
+  s->qmap_ok = V.n3 % 8 == 0;
+  for (int k = 0; k < 3 && s->qmap_ok; ++k)
+    s->qmap_ok = encode_grid_map(&s->qmap[k], V.p + (size_t)k * V.n, V.n1, V.n2, V.n3, SBZ, SBY, SBX);
   s->bound = true;
   return MLPCG_OK;
 }

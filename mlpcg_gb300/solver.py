@@ -25,7 +25,7 @@ from .ops import _p, _stream
 from .precond import PrecondPlan, pack_params
 
 METHODS = {"npsd": 0, "npcg": 1}
-STATUS = {0: "running", 1: "converged", 2: "max_it", 3: "breakdown", 4: "nonfinite"}
+STATUS = {0: "running", 1: "converged", 2: "max_it", 3: "breakdown", 4: "nonfinite", 5: "copy_failed"}
 
 
 @dataclass
