@@ -404,8 +404,9 @@ def coeff_bytes(plan, level, n_level, mixed):
 def iteration_bytes(plan, n0, mixed, mixed_t=None, method="npsd"):
     """Compulsory HBM bytes of one fused iteration (bf16 coefficients and activations)."""
     total = 0.0
-    # solver vectors: npsd dots + qform + spmv/dots, or npcg r.z + p/spmv; then update + true residual
-    vec = n0 * (12 + 16 + 18 + 32) if method == "npsd" else n0 * (8 + 17 + 32)
+    # solver vectors: npsd dots + qform + spmv/dots, or npcg r.z + p/spmv; then the update (r every
+    # iteration, 12 B; the double-float iterate with two directions every other one, 24 B)
+    vec = n0 * (12 + 16 + 18 + 24) if method == "npsd" else n0 * (8 + 17 + 24)
     L = plan.levels
     if plan.kind == 2:   # V (like the non-swap network, prolongation pass on every level), then V^T
         for l in range(L):

@@ -54,6 +54,11 @@ struct State {
   double c0, c1, beta, rz_old, rz;
   float beta_hi, beta_lo;             // beta as a double-float pair
   float rscale;                       // 1/||r|| fed to the preconditioner
+  // x is updated every other iteration: the pending term beta_k d_k (pend = 1) is added together
+  // with the next iteration's (same double-float operations, same order), or on the fly by the
+  // true residual and the final conversion; d_k stays in its buffer slot pend_buf until then
+  int pend, pend_buf;
+  float pend_hi, pend_lo;
   unsigned ticket[4];
 };
 
@@ -355,10 +360,35 @@ __global__ void __launch_bounds__(RT) k_prepare(Vecs V) {
 // cells), stored rounded to FP32; accumulates sum r^2 (and, with BB, sum b^2)
 // with compensated FP32 sums.  The neighbours are added in the column order
 // of the assembled CSR row (i-1, j-1, k-1, k+1, j+1, i+1).
+// x with a pending update beta_p d_p (pd == nullptr: none), per cell exactly as k_update adds it
+struct XEff {
+  const float2 *x;
+  const float *pd;
+  float2 bp;
+  __device__ __forceinline__ float2 at(uint32_t q) const {
+    return pd ? df_add(x[q], df_mul_f(bp, pd[q])) : x[q];
+  }
+  __device__ __forceinline__ void at4(uint32_t q, float2 v[4]) const {
+    ld4(x + q, v);
+    if (pd) {
+      float d[4];
+      ld4(pd + q, d);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) v[c] = df_add(v[c], df_mul_f(bp, d[c]));
+    }
+  }
+};
+__device__ __forceinline__ XEff x_eff(const Vecs &V) {
+  const State &S = *V.st;
+  XEff e{V.xd, S.pend ? V.p + (size_t)S.pend_buf * V.n : nullptr, make_float2(S.pend_hi, S.pend_lo)};
+  return e;
+}
+
 template <bool BB>
 __device__ __forceinline__ void residual_pass(const Vecs &V, CSum &bb, CSum &rr) {
   const uint32_t sy = (uint32_t)V.n3, sx = (uint32_t)V.n2 * (uint32_t)V.n3;
   const float2 zero = make_float2(0.f, 0.f);
+  const XEff X = x_eff(V);
   for (uint32_t g = gtid(); g < V.ngroups; g += gstride()) {
     uint32_t q; int i, j, k0;
     group_coords(V, g, q, i, j, k0);
@@ -367,14 +397,14 @@ __device__ __forceinline__ void residual_pass(const Vecs &V, CSum &bb, CSum &rr)
 #pragma unroll
     for (int c = 0; c < 4; ++c) xm[c] = ym[c] = yp[c] = xp[c] = zero;
     const uchar4 cd = ldflags4(V.code + q);
-    ld4(V.xd + q, cen);
+    X.at4(q, cen);
     ld4(V.bd + q, bq);
-    if (i > 0) ld4(V.xd + q - sx, xm);
-    if (j > 0) ld4(V.xd + q - sy, ym);
-    if (k0 > 0) zm = V.xd[q - 1];
-    if (k0 + 4 < V.n3) zp = V.xd[q + 4];
-    if (j < V.n2 - 1) ld4(V.xd + q + sy, yp);
-    if (i < V.n1 - 1) ld4(V.xd + q + sx, xp);
+    if (i > 0) X.at4(q - sx, xm);
+    if (j > 0) X.at4(q - sy, ym);
+    if (k0 > 0) zm = X.at(q - 1);
+    if (k0 + 4 < V.n3) zp = X.at(q + 4);
+    if (j < V.n2 - 1) X.at4(q + sy, yp);
+    if (i < V.n1 - 1) X.at4(q + sx, xp);
     float rf[4];
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
@@ -398,11 +428,12 @@ __device__ __forceinline__ void residual_pass(const Vecs &V, CSum &bb, CSum &rr)
 
 // The caller's x from the pairs, on the fluid cells (the others keep their values)
 __global__ void __launch_bounds__(RT) k_finalize(Vecs V) {
+  const XEff X = x_eff(V);  // with a still pending update of the iterate
   for (uint32_t g = gtid(); g < V.ngroups; g += gstride()) {
     const uint32_t q = 4u * g;
     const uchar4 cd = ldflags4(V.code + q);
     float2 xd[4];
-    ld4(V.xd + q, xd);
+    X.at4(q, xd);
 #pragma unroll
     for (int c = 0; c < 4; ++c)
       if (!(lane(cd, c) & kNotFluid)) V.x[q + c] = df_to_double_bits(xd[c]);
@@ -791,18 +822,25 @@ __global__ void __launch_bounds__(RT) k_update(Vecs V) {
   }
   const float2 bd = make_float2(S.beta_hi, S.beta_lo);
   const float bf = (float)S.beta;
+  // every other iteration x += beta_prev d_prev + beta d in one pass; in between only r moves
+  const bool commit = S.pend != 0;
+  const float *DP = V.p + (size_t)S.pend_buf * V.n;
+  const float2 bp = make_float2(S.pend_hi, S.pend_lo);
   CSum t;
   for (uint32_t g0 = blockIdx.x * RT * UNR + threadIdx.x; g0 < V.ngroups; g0 += gridDim.x * RT * UNR) {
-    float d[UNR][4], ad[UNR][4], r[UNR][4];
+    float d[UNR][4], dp[UNR][4], ad[UNR][4], r[UNR][4];
     float2 x[UNR][4];
 #pragma unroll
     for (int u = 0; u < UNR; ++u) {
       const uint32_t q = 4u * (g0 + u * RT);
       if (g0 + u * RT >= V.ngroups) continue;
-      ld4(D + q, d[u]);
       ld4(AD + q, ad[u]);
       ld4(V.r + q, r[u]);
-      ld4(V.xd + q, x[u]);
+      if (commit) {
+        ld4(D + q, d[u]);
+        ld4(DP + q, dp[u]);
+        ld4(V.xd + q, x[u]);
+      }
     }
     float s = 0.f;
 #pragma unroll
@@ -811,11 +849,11 @@ __global__ void __launch_bounds__(RT) k_update(Vecs V) {
       if (g0 + u * RT >= V.ngroups) continue;
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
-        x[u][c] = df_add(x[u][c], df_mul_f(bd, d[u][c]));
+        if (commit) x[u][c] = df_add(df_add(x[u][c], df_mul_f(bp, dp[u][c])), df_mul_f(bd, d[u][c]));
         r[u][c] = fmaf(-bf, ad[u][c], r[u][c]);
         s = fmaf(r[u][c], r[u][c], s);
       }
-      st4(V.xd + q, x[u]);
+      if (commit) st4(V.xd + q, x[u]);
       st4(V.r + q, r[u]);
     }
     t.add(s);
@@ -825,6 +863,15 @@ __global__ void __launch_bounds__(RT) k_update(Vecs V) {
   if (reduce_last<1>(v, V, 3, o) && threadIdx.x == 0) {
     State &W = *V.st;
     W.rr = o[0];
+    // every block has read the pending state before the ticket: safe to move it on
+    if (commit) {
+      W.pend = 0;
+    } else {
+      W.pend = 1;
+      W.pend_buf = W.method == M_NPSD ? W.head : W.pp;
+      W.pend_hi = W.beta_hi;
+      W.pend_lo = W.beta_lo;
+    }
     const int itn = W.it + 1;
     const double rel = sqrt(o[0] / W.bb);
     W.rel = rel;
