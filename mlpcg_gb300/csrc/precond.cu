@@ -1475,7 +1475,8 @@ static size_t plan_layout(PrecondPlan &P, char *base) {
   // the finest level's prolongated input (fast path only; the SPD kind uses it on every level)
   P.ufine = P.lv[0].fast ? take(P.lv[0].ps * sizeof(float)) : nullptr;  // FP32 on level 0 (TMA-staged)
   P.xtmp = P.kind == MLPCG_PRECOND_SMALL_SPD ? take(P.lv[P.L].ps * sa) : nullptr;
-  P.v0 = full ? take(P.lv[0].ps * sa) : nullptr;
+  // FP32 on a tiled finest level (the V^T pre-block loads it by TMA), else the activation dtype
+  P.v0 = full ? take(P.lv[0].ps * (P.lv[0].fast ? sizeof(float) : sa)) : nullptr;
   P.coef = (float *)take(2 * P.L * sizeof(float));
   P.fmask = (uint8_t *)take(P.lv[0].ps + 64);
   P.lin_ws = take(linear_workspace());
@@ -1668,7 +1669,7 @@ static int run_apply_spd(const PrecondPlan &P, const float *r, const float *rsca
                                 transposed ? 1 : 0, st);
   };
   if (in_range(L)) RET_IF(coarsest(false));
-  // ---- V: up sweep, x_l = c0 y_l + c1 l1[l](P x_{l+1}); level 0 into v0
+  // ---- V: up sweep, x_l = c0 y_l + c1 l1[l](P x_{l+1}); level 0 into v0 (FP32 when tiled)
   for (int l = L - 1; l >= 0; --l) {
     if (!in_range(2 * L - l)) continue;
     const auto &v = P.lv[l];
@@ -1681,7 +1682,8 @@ static int run_apply_spd(const PrecondPlan &P, const float *r, const float *rsca
         k_up_fine<AT, AT, float, false, true><<<g, PT, 0, st>>>((const AT *)P.xout[1], (const AT *)P.y[0], c0, c1,
                                                                  (float *)P.ufine, v.n1, v.n2, v.n3, gate);
         MLPCG_LAUNCH_CHECK();
-        RET_IF((launch_post0<KT, AT, AT, false>(P, C, (const AT *)P.y[0], c0, c1, o, nullptr, nullptr, st, gate)));
+        RET_IF((launch_post0<KT, AT, float, false>(P, C, (const AT *)P.y[0], c0, c1, (float *)P.v0, nullptr, nullptr,
+                                                    st, gate)));
       } else {
         AT *u = (AT *)P.ufine;
         k_up_fine<AT, AT, AT, false, true><<<g, PT, 0, st>>>((const AT *)P.xout[l + 1], (const AT *)P.y[l], c0, c1, u,
@@ -1703,7 +1705,11 @@ static int run_apply_spd(const PrecondPlan &P, const float *r, const float *rsca
     if (!in_range(B + l)) continue;
     const auto &v = P.lv[l];
     const AT *src = (const AT *)(l == 0 ? P.v0 : P.xin[l]);
-    if (v.fast) {
+    if (v.fast && l == 0) {  // v0 is FP32: the TMA-staged pre-block, unscaled
+      const CoefArgs<KT> C = coef_args_t<KT>(P, 0, P.KpostT[0], v.cls ? P.UpostT[0] : nullptr);
+      RET_IF((launch_pre0<KT, AT>(P, C, (const float *)P.v0, nullptr, (AT *)nullptr, (AT *)P.xin[1], nullptr, st,
+                                  gate)));
+    } else if (v.fast) {
       const CoefArgs<KT> C = coef_args_t<KT>(P, l, P.KpostT[l], v.cls ? P.UpostT[l] : nullptr);
       if (v.cls)
         k_pre_fused<KT, AT, AT, true, true><<<grid_of(v), PT, 0, st>>>(
@@ -1727,11 +1733,11 @@ static int run_apply_spd(const PrecondPlan &P, const float *r, const float *rsca
     if (v.fast) {
       const CoefArgs<KT> C = coef_args_t<KT>(P, l, P.KpreT[l], v.cls ? P.UpreT[l] : nullptr);
       const dim3 g = grid_of(v);
-      if (l == 0) {
-        k_up_fine<AT, AT, float, true, true><<<g, PT, 0, st>>>((const AT *)P.xout[1], skip, c0, c1, (float *)P.ufine,
-                                                                v.n1, v.n2, v.n3, gate);
+      if (l == 0) {  // skip vector v0 in FP32
+        k_up_fine<AT, float, float, true, true><<<g, PT, 0, st>>>((const AT *)P.xout[1], (const float *)P.v0, c0, c1,
+                                                                   (float *)P.ufine, v.n1, v.n2, v.n3, gate);
         MLPCG_LAUNCH_CHECK();
-        RET_IF((launch_post0<KT, AT, float, true>(P, C, skip, c0, c1, z, nullptr, P.fmask, st, gate)));
+        RET_IF((launch_post0<KT, AT, float, true>(P, C, (const AT *)nullptr, c0, c1, z, nullptr, P.fmask, st, gate)));
       } else {
         AT *u = (AT *)P.ufine;
         k_up_fine<AT, AT, AT, true, true><<<g, PT, 0, st>>>((const AT *)P.xout[l + 1], skip, c0, c1, u, v.n1, v.n2,
