@@ -958,6 +958,13 @@ struct mlpcg_batch {
 
 static size_t al256s(size_t b) { return (b + 255) / 256 * 256; }
 
+// CTAs of the once-per-solve kernels (prepare, initial and true residual, finalize): the full
+// reduction grid whatever the schedule of the iteration kernels, so that these single passes
+// keep enough loads in flight
+static unsigned full_grid(const Vecs &V) {
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(RB_MAX, ((int64_t)V.ngroups + RT - 1) / RT));
+}
+
 static FastDiv make_fastdiv(uint32_t d) {
   int l = 0;
   while ((1ull << l) < d) ++l;  // ceil(log2 d)
@@ -1003,8 +1010,8 @@ static void destroy_graph(mlpcg_solver *s) {
 static int start_solve(mlpcg_solver *s, cudaStream_t st) {
   Vecs &V = s->V;
   k_reset<<<1, 32, 0, st>>>(V.st, s->max_it, s->true_every, s->method, s->tol);
-  k_prepare<<<(unsigned)V.nblk, RT, 0, st>>>(V);
-  k_init<<<(unsigned)V.nblk, RT, 0, st>>>(V);
+  k_prepare<<<full_grid(V), RT, 0, st>>>(V);
+  k_init<<<full_grid(V), RT, 0, st>>>(V);
   MLPCG_LAUNCH_CHECK();
   return MLPCG_OK;
 }
@@ -1027,7 +1034,7 @@ static int enqueue_body(mlpcg_solver *s, cudaStream_t st, cudaGraphConditionalHa
     k_cg_pspmv<<<nb, RT, 0, st>>>(V);
   }
   k_update<<<nb, RT, 0, st>>>(V);
-  k_true_residual<<<nb, RT, 0, st>>>(V);
+  k_true_residual<<<full_grid(V), RT, 0, st>>>(V);
   k_control<<<1, 1, 0, st>>>(V, h, use_handle);
   MLPCG_LAUNCH_CHECK();
   return MLPCG_OK;
@@ -1109,7 +1116,7 @@ int mlpcg_solver_solve(mlpcg_solver *s, int use_graph, void *stream) {
       int rc = enqueue_body(s, st, 0, 0);
       if (rc) return rc;
     }
-    k_finalize<<<(unsigned)V.nblk, RT, 0, st>>>(V);
+    k_finalize<<<full_grid(V), RT, 0, st>>>(V);
     MLPCG_LAUNCH_CHECK();
     return MLPCG_OK;
   }
@@ -1140,7 +1147,7 @@ int mlpcg_solver_solve(mlpcg_solver *s, int use_graph, void *stream) {
   // the body's first kernels see status != RUNNING and the control kernel
   // ends the loop after one pass.
   MLPCG_CUDA_CHECK(cudaGraphLaunch(s->exec, st));
-  k_finalize<<<(unsigned)V.nblk, RT, 0, st>>>(V);
+  k_finalize<<<full_grid(V), RT, 0, st>>>(V);
   MLPCG_LAUNCH_CHECK();
   return MLPCG_OK;
 }
@@ -1276,7 +1283,7 @@ int mlpcg_batch_solve(mlpcg_batch *b, void *stream) {
   }
   MLPCG_CUDA_CHECK(cudaGraphLaunch(b->exec, st));
   for (auto *s : b->solvers) {
-    k_finalize<<<(unsigned)s->V.nblk, RT, 0, st>>>(s->V);
+    k_finalize<<<full_grid(s->V), RT, 0, st>>>(s->V);
     MLPCG_LAUNCH_CHECK();
   }
   return MLPCG_OK;
