@@ -369,7 +369,8 @@ int mlpcg_solver_create(int N1, int N2, int N3, const mlpcg_precond *plan, int m
 size_t mlpcg_solver_workspace(const mlpcg_solver *solver);
 void mlpcg_solver_destroy(mlpcg_solver *solver);
 /* flags: N uint8 cell codes; b: N FP64 rhs (read on FLUID cells only);
- * x: N FP64, the initial guess on entry to solve and the solution after. */
+ * x: N FP64, the initial guess on entry to solve and the solution after.
+ * flags 4-byte, b and x 16-byte aligned (MLPCG_ERR_ALIGN otherwise). */
 int mlpcg_solver_bind(mlpcg_solver *solver, void *workspace, size_t workspace_bytes,
                       const uint8_t *flags, const double *b, double *x);
 /* Enqueues the solve on `stream`.  use_graph = 1: one graph launch (the graph

@@ -434,9 +434,16 @@ __global__ void __launch_bounds__(RT) k_finalize(Vecs V) {
     const uchar4 cd = ldflags4(V.code + q);
     float2 xd[4];
     X.at4(q, xd);
+    const bool all_fluid = !((cd.x | cd.y | cd.z | cd.w) & kNotFluid);
+    if (all_fluid) {  // the common case: two 16-byte stores
+      double2 *o = reinterpret_cast<double2 *>(V.x + q);
+      o[0] = make_double2(df_to_double_bits(xd[0]), df_to_double_bits(xd[1]));
+      o[1] = make_double2(df_to_double_bits(xd[2]), df_to_double_bits(xd[3]));
+    } else {
 #pragma unroll
-    for (int c = 0; c < 4; ++c)
-      if (!(lane(cd, c) & kNotFluid)) V.x[q + c] = df_to_double_bits(xd[c]);
+      for (int c = 0; c < 4; ++c)
+        if (!(lane(cd, c) & kNotFluid)) V.x[q + c] = df_to_double_bits(xd[c]);
+    }
   }
 }
 
@@ -1077,6 +1084,9 @@ int mlpcg_solver_bind(mlpcg_solver *s, void *workspace, size_t workspace_bytes, 
   MLPCG_REQUIRE(workspace_bytes >= s->bytes, MLPCG_ERR_WORKSPACE, "solver workspace too small: %zu < %zu",
                 workspace_bytes, s->bytes);
   MLPCG_REQUIRE(((uintptr_t)workspace & 255) == 0, MLPCG_ERR_ALIGN, "solver workspace must be 256-byte aligned");
+  // the kernels read flags 4 cells and b, x 2 doubles at a time
+  MLPCG_REQUIRE(((uintptr_t)flags & 3) == 0 && ((uintptr_t)b & 15) == 0 && ((uintptr_t)x & 15) == 0, MLPCG_ERR_ALIGN,
+                "solver_bind: flags must be 4-byte and b, x 16-byte aligned");
   destroy_graph(s);
   solver_layout(*s, (char *)workspace);
   Vecs &V = s->V;

@@ -73,3 +73,25 @@ def test_workspace_queries(lib):
     assert query("mlpcg_sm_block_3d_workspace", 8, 8, 8) >= 27 * 512 * 4
     assert query("mlpcg_sm_linear_3d_workspace", 8, 8, 8) > 0
     assert query("mlpcg_dot_workspace", 1 << 20) >= 8
+
+
+def test_solver_bind_rejects_misaligned_vectors(lib):
+    """Binding checks the caller's pointers before any kernel reads them (no device work)."""
+    import ctypes as C2
+    from mlpcg_gb300._lib import MLPCGError, call
+    plan, solver = C2.c_void_p(), C2.c_void_p()
+    call("mlpcg_precond_create", 16, 16, 16, 2, 1, 1, 0, 0, 1, C2.byref(plan))
+    try:
+        call("mlpcg_solver_create", 16, 16, 16, plan, 0, 10, C2.c_double(1e-6), 25, C2.byref(solver))
+        try:
+            nbytes = lib.mlpcg_solver_workspace(solver)
+            ws = C2.c_void_p(1 << 20)   # 256-byte aligned, never dereferenced
+            good = C2.c_void_p(1 << 21)
+            with pytest.raises(MLPCGError, match="16-byte"):
+                call("mlpcg_solver_bind", solver, ws, nbytes, good, C2.c_void_p((1 << 21) + 8), good)
+            with pytest.raises(MLPCGError, match="4-byte"):
+                call("mlpcg_solver_bind", solver, ws, nbytes, C2.c_void_p((1 << 21) + 1), good, good)
+        finally:
+            lib.mlpcg_solver_destroy(solver)
+    finally:
+        lib.mlpcg_precond_destroy(plan)
