@@ -239,6 +239,15 @@ class CombineFunction(torch.autograd.Function):
         return gc0, gx, gc1, gy
 
 
+def _direct(fn, *args):
+    return fn(*args)
+
+
+def _checkpointed(fn, *args):
+    from torch.utils.checkpoint import checkpoint
+    return checkpoint(fn, *args, use_reentrant=False)
+
+
 def _check_mode(mode):
     if mode != "trilinear":
         raise ValueError(f"interpolation_mode {mode!r}: only 'trilinear' is provided by the sm_103a kernels")
@@ -335,28 +344,35 @@ class SmallSMModelDn3D(BaseModel):
                 x[i - 1] = ops.axpby(c0[i - 1], x[i - 1], c1[i - 1], x[i])
         return x[0]
 
+    #: Training memory: when True, forward keeps only each level's input and output (the down
+    #: sweep's outputs are the up sweep's skip vectors); the pooled block inputs, the prolongated
+    #: vectors and the post-block outputs are recomputed level by level in the backward pass
+    #: (torch.utils.checkpoint, non-reentrant).  Same gradients, one more forward's work.
+    recompute = False
+
     def forward(self, image, b):
         """Training pass with autograd (sm_model_3d.py:264-287)."""
         self.check_grid(image.shape)
-        x = [self.pre[0](image, b)]
+        n = self.n
+        ck = _checkpointed if (self.recompute and torch.is_grad_enabled()) else _direct
         imgs = [image]
-        for i in range(1, self.n):
-            x.append(AvgPool2Function.apply(x[-1]))
+        for _ in range(n):
             imgs.append(AvgPool2Function.apply(imgs[-1]))
-            x[-1] = self.pre[i](imgs[-1], x[-1])
-        x.append(AvgPool2Function.apply(x[-1]))
-        imgs.append(AvgPool2Function.apply(imgs[-1]))
-        x[-1] = self.l(imgs[-1], x[-1])
-        for i in range(self.n, 0, -1):
-            x[i] = Upsample2Function.apply(x[i])
+        x = [ck(lambda bb: self.pre[0](image, bb), b)]
+        for i in range(1, n):
+            x.append(ck(lambda xp, i=i: self.pre[i](imgs[i], AvgPool2Function.apply(xp)), x[-1]))
+        x.append(ck(lambda xp: self.l(imgs[n], AvgPool2Function.apply(xp)), x[-1]))
+        for i in range(n, 0, -1):
             c0 = self.c0[i - 1](imgs[i - 1])
             c1 = self.c1[i - 1](imgs[i - 1])
-            if self.swap_ord:
-                x[i - 1] = CombineFunction.apply(c0, x[i - 1], c1, x[i])
-                x[i - 1] = self.post[i - 1](imgs[i - 1], x[i - 1])
-            else:
-                x[i] = self.post[i - 1](imgs[i - 1], x[i])
-                x[i - 1] = CombineFunction.apply(c0, x[i - 1], c1, x[i])
+
+            def up(xc, yl, c0, c1, i=i):
+                u = Upsample2Function.apply(xc)
+                if self.swap_ord:
+                    return self.post[i - 1](imgs[i - 1], CombineFunction.apply(c0, yl, c1, u))
+                return CombineFunction.apply(c0, yl, c1, self.post[i - 1](imgs[i - 1], u))
+
+            x[i - 1] = ck(up, x[i], x[i - 1], c0, c1)
         return x[0]
 
     def precond_plan(self, image, storage=torch.bfloat16, act_storage=None):

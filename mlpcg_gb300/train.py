@@ -222,6 +222,8 @@ def main(argv=None):
     ap.add_argument("--harvest-every", type=int, default=250, help="0 disables solver-in-the-loop rhs")
     ap.add_argument("--harvest-frac", type=float, default=0.25)
     ap.add_argument("--init", default=None, help="npz state dict to start from")
+    ap.add_argument("--recompute", action="store_true",
+                    help="recompute per-level activations in the backward pass (large grids, SmallSMModelDn3D)")
     ap.add_argument("--time-limit", type=float, default=1e9, help="seconds of training loop at most")
     ap.add_argument("--ritz-cache", default=None, help="directory caching the Lanczos Ritz vectors")
     args = ap.parse_args(argv)
@@ -231,6 +233,8 @@ def main(argv=None):
     out.mkdir(parents=True, exist_ok=True)
     torch.manual_seed(0)
     model = make_model(args.model, args.levels).to(dev)
+    if args.recompute:
+        model.recompute = True
     if args.init:
         d = np.load(args.init)
         model.load_state_dict({k: torch.from_numpy(d[k]) for k in model.state_dict()})

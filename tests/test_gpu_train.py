@@ -75,3 +75,39 @@ def test_training_symmetric_network(cuda, tmp_path):
     assert all(0.0 <= e["loss"] <= 1.0 for e in log["loss"]) and len(log["loss"]) == 2
     first, last = log["eval"][0], log["eval"][-1]
     assert last["status"] == "converged" and last["iterations"] <= first["iterations"], log["eval"]
+
+
+def test_recompute_gives_the_same_gradients_with_less_memory(cuda):
+    """SmallSMModelDn3D.recompute: per-level activations recomputed in the backward pass -- the
+    same loss and gradients (input, image, every parameter), a lower peak of stored activations."""
+    from mlpcg_gb300.sm_model_3d import SmallSMModelDn3D
+    torch.manual_seed(0)
+    model = SmallSMModelDn3D(3, 3, "trilinear").to(cuda)
+    shape = (64, 64, 64)
+    torch.manual_seed(1)
+    img = (torch.rand((3,) + shape, device=cuda) > 0.5).float()
+    b0 = torch.randn((4, 1) + shape, device=cuda)
+    g = torch.randn_like(b0)
+    out = {}
+    for rec in (False, True):
+        model.recompute = rec
+        model.zero_grad(set_to_none=True)
+        b = b0.clone().requires_grad_(True)
+        im = img.clone().requires_grad_(True)
+        torch.cuda.synchronize()
+        torch.cuda.reset_peak_memory_stats(cuda)
+        base = torch.cuda.memory_allocated(cuda)
+        y = model(im, b)
+        kept = torch.cuda.memory_allocated(cuda) - base   # what the forward keeps for the backward
+        (y * g).sum().backward()
+        torch.cuda.synchronize()
+        out[rec] = (y.detach(), b.grad, im.grad, {k: p.grad.clone() for k, p in model.named_parameters()}, kept)
+    model.recompute = False
+    y0, gb0, gi0, gp0, kept0 = out[False]
+    y1, gb1, gi1, gp1, kept1 = out[True]
+    assert torch.equal(y0, y1) and torch.equal(gb0, gb1)
+    # the image gradient sums contributions of several paths, possibly in another order
+    torch.testing.assert_close(gi1, gi0, rtol=1e-5, atol=1e-7)
+    for k in gp0:
+        assert torch.equal(gp0[k], gp1[k]), k
+    assert kept1 < 0.75 * kept0, (kept0, kept1)
