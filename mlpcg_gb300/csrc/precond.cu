@@ -747,7 +747,7 @@ __device__ __forceinline__ void tile_apply(const float (*S)[HY][HZP], const ClsS
   bool valid[TX];
 #pragma unroll
   for (int tx = 0; tx < TX; ++tx) valid[tx] = active && x0 + tx < n1;
-  if (!CLS) {
+  if constexpr (!CLS) {
     int64_t q[TX];
 #pragma unroll
     for (int tx = 0; tx < TX; ++tx) q[tx] = valid[tx] ? ((int64_t)(x0 + tx) * n2 + j) * n3 + k0 : 0;
@@ -759,38 +759,40 @@ __device__ __forceinline__ void tile_apply(const float (*S)[HY][HZP], const ClsS
       }
     }, acc);
     return;
-  }
-  bool mixed[TX];
-#pragma unroll
-  for (int tx = 0; tx < TX; ++tx) mixed[tx] = (rwd[tx] & 3u) == kMixed;
-  if (!__any_sync(0xffffffffu, mixed[0] || mixed[1])) {
-    const float *ku[TX];
-#pragma unroll
-    for (int tx = 0; tx < TX; ++tx) ku[tx] = sm->Ku[rwd[tx] & 3u];
-    apply_pair<OFF>(S, ty, tz * 8, [&](int tx, int p, float kv[8]) {
-      const float v = ku[tx][p];
-#pragma unroll
-      for (int c = 0; c < 8; ++c) kv[c] = v;
-    }, acc);
   } else {
-    // every lane streams a record: its run's, or its material's (cached), so
-    // the loads carry no branch and issue ahead of the arithmetic
-    const KT *rp[TX];
-    uint32_t st[TX];
+    bool mixed[TX];
 #pragma unroll
-    for (int tx = 0; tx < TX; ++tx) {
-      rp[tx] = mixed[tx] ? C.rec + (size_t)trec.x * RREC + (rwd[tx] >> 2) * 8 : C.mrec + (rwd[tx] & 3u) * RREC;
-      st[tx] = mixed[tx] ? trec.y * 8 : 8;
+    for (int tx = 0; tx < TX; ++tx) mixed[tx] = (rwd[tx] & 3u) == kMixed;
+    if (!__any_sync(0xffffffffu, mixed[0] || mixed[1])) {
+      const float *ku[TX];
+#pragma unroll
+      for (int tx = 0; tx < TX; ++tx) ku[tx] = sm->Ku[rwd[tx] & 3u];
+      apply_pair<OFF>(S, ty, tz * 8, [&](int tx, int p, float kv[8]) {
+        const float v = ku[tx][p];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) kv[c] = v;
+      }, acc);
+    } else {
+      // every lane streams a record: its run's, or its material's (cached), so
+      // the loads carry no branch and issue ahead of the arithmetic
+      const KT *rp[TX];
+      uint32_t st[TX];
+#pragma unroll
+      for (int tx = 0; tx < TX; ++tx) {
+        rp[tx] = mixed[tx] ? C.rec + (size_t)trec.x * RREC + (rwd[tx] >> 2) * 8 : C.mrec + (rwd[tx] & 3u) * RREC;
+        st[tx] = mixed[tx] ? trec.y * 8 : 8;
+      }
+      apply_pair<OFF>(S, ty, tz * 8, [&](int tx, int p, float kv[8]) { ld8(rp[tx] + p * st[tx], kv); }, acc);
     }
-    apply_pair<OFF>(S, ty, tz * 8, [&](int tx, int p, float kv[8]) { ld8(rp[tx] + p * st[tx], kv); }, acc);
   }
 }
 
 // uniform coefficient vectors of a classed block into shared memory
 template <bool CLS>
 __device__ __forceinline__ void stage_uniform(ClsSmem *sm, const float *__restrict__ kuni) {
-  if (!CLS) return;
-  for (int e = threadIdx.x; e < 3 * KREC; e += PT) sm->Ku[e / KREC][e % KREC] = __ldg(kuni + e);
+  if constexpr (CLS) {
+    for (int e = threadIdx.x; e < 3 * KREC; e += PT) sm->Ku[e / KREC][e % KREC] = __ldg(kuni + e);
+  }
 }
 
 // the run words of the thread's runs and the tile's (first record, mixed runs) (classed only).
@@ -1480,8 +1482,9 @@ static size_t plan_layout(PrecondPlan &P, char *base) {
   P.coef = (float *)take(2 * P.L * sizeof(float));
   P.fmask = (uint8_t *)take(P.lv[0].ps + 64);
   P.lin_ws = take(linear_workspace());
-  P.scratch = (float *)take(96 * sizeof(float));
   P.err = (int *)take(sizeof(int));
+  // scratch last: the general path's temporaries (sized in the plan's byte count) follow it
+  P.scratch = (float *)take(96 * sizeof(float));
   // scratch for the general path: level-0 scaled input and one activation-sized temp
   return off;
 }

@@ -349,3 +349,17 @@ def test_tile_copies_complete(cuda):
     assert res.status in ("converged", "max_it") and np.isfinite(res.rel_res)
     assert res.history[-1] < 0.1 * res.history[0]
     assert not solver.plan.copy_failed()
+
+
+@pytest.mark.parametrize("n", [16, 24, 48])
+def test_copy_flag_clear_with_general_path_levels(cuda, n):
+    """Plans whose coarse levels run the general (untiled) kernels keep the tile-copy flag clear
+    (their temporaries must not overlap it) and still match eval_forward."""
+    s, flags, img = _scene((n, n, n), 3, cuda)
+    m = _model(3, cuda)
+    plan = m.precond_plan(img, storage=torch.float32)
+    b = torch.randn((1, 1, n, n, n), device=cuda)
+    z = plan.apply(b.reshape(-1)).reshape(b.shape)
+    ref = torch.where(img[1] == 0, 0.0, m.eval_forward(img, b))
+    assert rel_err(z.cpu().numpy(), ref.cpu().numpy()) < 1e-5
+    assert not plan.copy_failed()
