@@ -98,41 +98,36 @@ __device__ __forceinline__ float2 df_from_double_bits(double v) {
   return make_float2(hi, __int2float_rn(rem) * pow2f(E - 52));
 }
 
+// the FP64 routine as a real call, so that the rare lanes that need it do not make the compiler
+// evaluate it for every cell
+static __device__ __noinline__ double df_to_double_call(float2 a) { return df_to_double(a); }
+
 __device__ __forceinline__ double df_to_double_bits(float2 a) {
   const uint32_t hb = __float_as_uint(a.x), lb = __float_as_uint(a.y);
   const int eh = (int)((hb >> 23) & 0xff), el = (int)((lb >> 23) & 0xff);
-  if (eh == 0 || eh == 255) return df_to_double(a);
-  // hi as an integer in units of 2^(Eh - 60): its 24-bit significand shifted up by 37, which
-  // leaves room for a low part down to 2^-37 |hi| without losing a bit
-  const int64_t H = (int64_t)((1ull << 23) | (hb & 0x7fffffu)) << 37;
+  if (eh == 0 || eh == 255) return df_to_double_call(a);
+  // hi as a 53-bit significand in units of 2^(Eh - 52)
+  const int64_t H = (int64_t)((1ull << 23) | (hb & 0x7fffffu)) << 29;
   int64_t S = (hb >> 31) ? -H : H;
   if ((lb << 1) != 0) {
-    const int sh = el - eh + 37;  // lo's significand shift into those units (<= 13 for a normalised pair)
-    if (el == 0 || el == 255 || sh < 0 || sh > 24) return df_to_double(a);
+    const int sh = el - eh + 29;  // lo's significand shift into those units (<= 5 for a normalised pair)
+    if (el == 0 || el == 255 || sh < 0 || sh > 5) return df_to_double_call(a);
     const int64_t L = (int64_t)((1ull << 23) | (lb & 0x7fffffu)) << sh;
     S += (lb >> 31) ? -L : L;
   }
-  // S is hi + lo exactly (|S| < 2^62); its magnitude rounded once to 53 bits, ties to even,
-  // as the FP64 sum rounds it
   const uint64_t neg = S < 0 ? 1ull : 0ull;
-  const uint64_t m = neg ? (uint64_t)(-S) : (uint64_t)S;
-  if (m == 0) return df_to_double(a);
-  const int len = 64 - __clzll((long long)m);
-  int e = eh - 127 + len - 61 + 1023;  // biased exponent of the leading bit
-  uint64_t q;
-  if (len > 53) {
-    const int drop = len - 53;
-    q = m >> drop;
-    const uint64_t rem = m & ((1ull << drop) - 1), half = 1ull << (drop - 1);
-    q += (rem > half || (rem == half && (q & 1ull))) ? 1ull : 0ull;
-    if (q == (1ull << 53)) {
-      q >>= 1;
-      e += 1;
-    }
-  } else {
-    q = m << (53 - len);
+  uint64_t m = neg ? (uint64_t)(-S) : (uint64_t)S;
+  int e = eh - 127 + 1023;  // biased double exponent of 2^(Eh)
+  if (m >= (1ull << 53)) {  // one bit too many: drop it, ties to even
+    const uint64_t half = m >> 1;
+    m = half + ((m & 1ull) & (half & 1ull));
+    e += 1;
+    if (m >= (1ull << 53)) { m >>= 1; e += 1; }
+  } else if (m < (1ull << 52)) {  // |lo| <= 2^29 units: one step restores 53 bits, exactly
+    m <<= 1;
+    e -= 1;
   }
-  return __longlong_as_double((long long)((neg << 63) | ((uint64_t)e << 52) | (q & ((1ull << 52) - 1))));
+  return __longlong_as_double((long long)((neg << 63) | ((uint64_t)e << 52) | (m & ((1ull << 52) - 1))));
 }
 __device__ __forceinline__ float2 df_shfl_xor(float2 a, int o) {
   return make_float2(__shfl_xor_sync(0xffffffffu, a.x, o), __shfl_xor_sync(0xffffffffu, a.y, o));
