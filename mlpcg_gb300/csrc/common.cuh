@@ -86,10 +86,15 @@ __device__ __forceinline__ double df_to_double(float2 a) { return (double)a.x + 
 // part tiny against the high part) take the FP64 routine above.
 __device__ __forceinline__ float pow2f(int k) { return __int_as_float((k + 127) << 23); }  // k in [-126, 127]
 
+// the FP64 routines as real calls, so that the rare values that need them do not make the
+// compiler evaluate them for every cell
+static __device__ __noinline__ float2 df_from_double_call(double v) { return df_from_double(v); }
+static __device__ __noinline__ double df_to_double_call(float2 a) { return df_to_double(a); }
+
 __device__ __forceinline__ float2 df_from_double_bits(double v) {
   const uint64_t u = (uint64_t)__double_as_longlong(v);
   const int E = (int)((u >> 52) & 0x7ff) - 1023;
-  if (E < -74 || E > 120) return df_from_double(v);
+  if (E < -74 || E > 120) return df_from_double_call(v);
   const uint64_t full = (1ull << 52) | (u & ((1ull << 52) - 1));  // 53-bit significand
   const uint64_t hm = (full + (1ull << 28) - 1 + ((full >> 29) & 1)) >> 29;  // rounded to 24 bits (nearest even)
   int rem = (int)((int64_t)full - (int64_t)(hm << 29));  // |rem| <= 2^28: |v| - |hi| in units of 2^(E-52)
@@ -97,10 +102,6 @@ __device__ __forceinline__ float2 df_from_double_bits(double v) {
   if (u >> 63) { hi = -hi; rem = -rem; }  // the sign on the integer keeps a zero low part +0, as v - hi gives
   return make_float2(hi, __int2float_rn(rem) * pow2f(E - 52));
 }
-
-// the FP64 routine as a real call, so that the rare lanes that need it do not make the compiler
-// evaluate it for every cell
-static __device__ __noinline__ double df_to_double_call(float2 a) { return df_to_double(a); }
 
 __device__ __forceinline__ double df_to_double_bits(float2 a) {
   const uint32_t hb = __float_as_uint(a.x), lb = __float_as_uint(a.y);
