@@ -2211,10 +2211,10 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
 int mlpcg_precond_apply(const mlpcg_precond *h, const float *r, const float *r_scale, float *z, void *stream) {
   clear_error();
   MLPCG_REQUIRE(h && r && z, MLPCG_ERR_ARG, "precond_apply: NULL argument");
-  const PrecondPlan &P = h->p;
-  MLPCG_REQUIRE(P.ready, MLPCG_ERR_ARG, "precond_apply: plan not set up");
   MLPCG_REQUIRE(((uintptr_t)r & 15) == 0 && ((uintptr_t)z & 31) == 0, MLPCG_ERR_ALIGN,
                 "precond_apply: r must be 16-byte and z 32-byte aligned");
+  const PrecondPlan &P = h->p;
+  MLPCG_REQUIRE(P.ready, MLPCG_ERR_ARG, "precond_apply: plan not set up");
   cudaStream_t st = as_stream(stream);
   void *tmp0 = (char *)P.scratch + al256(96 * sizeof(float));
   if (P.kdt == MLPCG_BF16 && P.adt == MLPCG_BF16) return run_apply<__nv_bfloat16, __nv_bfloat16>(P, r, r_scale, z, tmp0, st);
@@ -2227,6 +2227,8 @@ int mlpcg_precond_apply_stages(const mlpcg_precond *h, int first, int last, cons
                                float *z, void *stream) {
   clear_error();
   MLPCG_REQUIRE(h && r && z, MLPCG_ERR_ARG, "precond_apply_stages: NULL argument");
+  MLPCG_REQUIRE(((uintptr_t)r & 15) == 0 && ((uintptr_t)z & 31) == 0, MLPCG_ERR_ALIGN,
+                "precond_apply_stages: r must be 16-byte and z 32-byte aligned");
   const PrecondPlan &P = h->p;
   MLPCG_REQUIRE(P.ready, MLPCG_ERR_ARG, "precond_apply_stages: plan not set up");
   const int last_stage = P.kind == MLPCG_PRECOND_SPD ? 4 * P.L + 1 : 2 * P.L;

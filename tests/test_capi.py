@@ -95,3 +95,23 @@ def test_solver_bind_rejects_misaligned_vectors(lib):
             lib.mlpcg_solver_destroy(solver)
     finally:
         lib.mlpcg_precond_destroy(plan)
+
+
+def test_precond_apply_rejects_misaligned_vectors(lib):
+    """Both application entry points check r (16 bytes) and z (32 bytes) before the plan's state
+    and before any kernel reads them (no device work)."""
+    from mlpcg_gb300._lib import MLPCGError, call
+    plan = C.c_void_p()
+    call("mlpcg_precond_create", 16, 16, 16, 2, 1, 1, 0, 0, 1, C.byref(plan))
+    try:
+        good, st = C.c_void_p(1 << 21), C.c_void_p(0)
+        for name, lead in (("mlpcg_precond_apply", ()), ("mlpcg_precond_apply_stages", (0, 0))):
+            with pytest.raises(MLPCGError, match="16-byte"):
+                call(name, plan, *lead, C.c_void_p((1 << 21) + 4), None, good, st)
+            with pytest.raises(MLPCGError, match="32-byte"):
+                call(name, plan, *lead, good, None, C.c_void_p((1 << 21) + 16), st)
+            with pytest.raises(MLPCGError, match="not set up"):  # aligned: the next check fires
+                call(name, plan, *lead, good, None, good, st)
+    finally:
+        lib.mlpcg_precond_destroy(plan)
+
