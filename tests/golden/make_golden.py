@@ -244,7 +244,6 @@ def make_laplacian(ref_lap, ref_read, shape, seed):
 
 def make_cg(ref_cg, model, scene, max_it=50):
     import scipy.sparse as sp
-    from mlpcg_gb300.laplacian import csr_from_flags  # noqa: F401 (not used: reference matrix below)
     lap = sys.modules["discrete_laplacian"]
     rd = sys.modules["read_data"]
     f = scene.flags

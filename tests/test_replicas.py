@@ -3,7 +3,6 @@ cross-rank reduction checked with 2 gloo ranks on the CPU."""
 import os
 import socket
 
-import pytest
 import torch.multiprocessing as mp
 
 

@@ -9,7 +9,6 @@ Kept in a file that pytest collects last; it passes alone or after the rest.
 """
 import ctypes as C
 
-import numpy as np
 import pytest
 import torch
 
