@@ -105,15 +105,31 @@ class PrecondPlan:
         call("mlpcg_precond_coefficients", self._h, _p(c), _stream(self.device))
         return c
 
+    def _check_vectors(self, r, scale, out):
+        """r and out: contiguous F32 with one value per cell of the plan's grid on its device;
+        scale: None or an F32 value there.  The kernels index them by the plan's grid alone."""
+        n = self.shape[0] * self.shape[1] * self.shape[2]
+        for t, name in ((r, "r"), (out, "out")):
+            if t is None:
+                continue
+            _check(t, name)
+            if t.numel() != n or t.device != self.device:
+                raise RuntimeError(f"{name} must hold {n} values on {self.device} (got {t.numel()} on {t.device})")
+        if scale is not None:
+            _check(scale, "scale")
+            if scale.numel() < 1 or scale.device != self.device:
+                raise RuntimeError(f"scale must hold one value on {self.device}")
+
     def apply(self, r: torch.Tensor, scale: torch.Tensor | None = None, out: torch.Tensor | None = None):
         """z = M(r * scale) on the full grid; r F32 with the grid's numel."""
-        _check(r, "r")
+        self._check_vectors(r, scale, out)
         z = torch.empty(self.shape, dtype=torch.float32, device=r.device) if out is None else out
         call("mlpcg_precond_apply", self._h, _p(r), _p(scale), _p(z), _stream(r.device))
         return z.reshape(r.shape) if out is None else z
 
     def apply_stages(self, first: int, last: int, r: torch.Tensor, scale=None, out=None):
         """Launch stages [first, last] of an application (see mlpcg_precond_apply_stages)."""
+        self._check_vectors(r, scale, out)
         z = torch.empty(self.shape, dtype=torch.float32, device=r.device) if out is None else out
         call("mlpcg_precond_apply_stages", self._h, int(first), int(last), _p(r), _p(scale), _p(z),
              _stream(r.device))

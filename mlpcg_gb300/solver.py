@@ -21,7 +21,7 @@ import torch
 
 from . import _lib
 from ._lib import call
-from .ops import _p, _stream
+from .ops import _check, _p, _stream
 from .precond import PrecondPlan, pack_params
 
 METHODS = {"npsd": 0, "npcg": 1}
@@ -73,6 +73,10 @@ class FusedSolver:
 
     def set_image(self, model, image: torch.Tensor, flags: torch.Tensor | None = None):
         """New frame: recompute the plan in place (the captured graph stays valid)."""
+        _check(image, "image")
+        if tuple(image.shape) != (3,) + self.shape or image.device != self.flags.device:
+            raise RuntimeError(f"image must have shape {(3,) + self.shape} on {self.flags.device} "
+                               f"(got {tuple(image.shape)} on {image.device})")
         if flags is not None:
             self.flags.copy_(flags)
         if model is not None:

@@ -380,3 +380,30 @@ def test_fused_solve_on_uneven_grids(cuda, shape):
     b = s.rhs.reshape(-1)[fluid]
     assert np.linalg.norm(b - A @ x) / np.linalg.norm(b) < 2e-6
     assert not solver.plan.copy_failed()
+
+
+def test_plan_and_solver_refuse_mis_sized_tensors(cuda):
+    """Wrong sizes, dtypes or empty scales are refused in Python before any kernel sees them
+    (the kernels index by the plan's grid alone); a valid call still works afterwards."""
+    from mlpcg_gb300.precond import PrecondPlan
+    from mlpcg_gb300.solver import FusedSolver
+    s, flags, img = _scene((16, 16, 16), 2, cuda)
+    m = _model(2, cuda)
+    plan = PrecondPlan(m, img, storage=torch.float32)
+    n = 16 ** 3
+    good = torch.ones(n, device=cuda)
+    with pytest.raises(RuntimeError):
+        plan.apply(torch.zeros(n - 8, device=cuda))
+    with pytest.raises(RuntimeError):
+        plan.apply(good, out=torch.empty(n // 2, device=cuda))
+    with pytest.raises(RuntimeError):
+        plan.apply(good.double())
+    with pytest.raises(RuntimeError):
+        plan.apply_stages(0, 0, torch.zeros(2 * n, device=cuda))
+    with pytest.raises(RuntimeError):
+        plan.apply(good, scale=torch.zeros(0, device=cuda))
+    solver = FusedSolver(m, flags, plan=plan)
+    with pytest.raises(RuntimeError):
+        solver.set_image(None, torch.zeros((3, 8, 16, 16), device=cuda))
+    z = plan.apply(good)
+    assert z.shape == good.shape and bool(torch.isfinite(z).all())
