@@ -69,6 +69,13 @@ def _out_shape(x: torch.Tensor, dims, padded: bool):
     return tuple(x.shape[:-3]) + tuple(dims)
 
 
+def _block_params(weight: torch.Tensor, bias: torch.Tensor):
+    """A block's W (27, 3, 3, 3, 3) and b (27,), by element count (the kernels read exactly these)."""
+    if weight.numel() != 27 * 81 or bias.numel() != 27:
+        raise RuntimeError(f"weight must hold 27 x 3 x 3 x 3 x 3 values and bias 27 "
+                           f"(got {weight.numel()} and {bias.numel()})")
+
+
 # ----------------------------------------------------------------------------
 # stencil blocks (reference semantics: coefficients evaluated per call)
 # ----------------------------------------------------------------------------
@@ -76,6 +83,7 @@ def block_forward(image, x, weight, bias, transpose=False, padded=False):
     """y = smblock3d(image, x) (transpose=False) or smblocktrans3d(image, x)."""
     for t, n in ((image, "image"), (x, "x"), (weight, "weight"), (bias, "bias")):
         _check(t, n)
+    _block_params(weight, bias)
     dims = _spatial(image, padded)
     B = _batch(x, dims, padded)
     y = torch.empty(_out_shape(x, dims, padded), dtype=torch.float32, device=x.device)
@@ -90,8 +98,11 @@ def block_backward(grad_out, image, x, weight, bias, transpose=False, padded=Fal
     grad_out = grad_out.contiguous()
     for t, n in ((grad_out, "grad_output"), (image, "image"), (x, "x"), (weight, "weight"), (bias, "bias")):
         _check(t, n)
+    _block_params(weight, bias)
     dims = _spatial(image, padded)
     B = _batch(x, dims, padded)
+    if grad_out.numel() != B * math.prod(dims):
+        raise RuntimeError(f"grad_output must hold {B} x {tuple(dims)} values (got {tuple(grad_out.shape)})")
     gx = torch.empty(_out_shape(x, dims, padded), dtype=torch.float32, device=x.device)
     gw = torch.empty((27, 3, 3, 3, 3), dtype=torch.float32, device=x.device)
     gb = torch.empty((27,), dtype=torch.float32, device=x.device)
@@ -147,8 +158,13 @@ def stencil_gen(image, weight, bias, dtype=torch.float32, out=None):
     """K planes (27, plane_stride(n)) of one block on ``image`` (3, N1, N2, N3)."""
     for t, n in ((image, "image"), (weight, "weight"), (bias, "bias")):
         _check(t, n)
+    _block_params(weight, bias)
     dims = _spatial(image, False)
     ps = plane_stride(math.prod(dims))
+    if out is not None:
+        _check(out, "out", (torch.float32, torch.bfloat16))
+        if out.numel() < 27 * ps:
+            raise RuntimeError(f"out must hold 27 planes of {ps} values (got {out.numel()} values)")
     K = out if out is not None else torch.empty((27, ps), dtype=dtype, device=image.device)
     call("mlpcg_stencil_gen", _p(image), 0, *dims, _p(weight), _p(bias), _p(K), _DT[K.dtype], ps,
          _stream(image.device))
@@ -159,6 +175,10 @@ def stencil_apply(K, x, dims, transpose=False, out_dtype=torch.float32):
     _check(K, "K", (torch.float32, torch.bfloat16))
     _check(x, "x", (torch.float32, torch.bfloat16))
     n = math.prod(dims)
+    if K.dim() != 2 or K.shape[0] != 27 or K.shape[1] < n:
+        raise RuntimeError(f"K must be 27 planes of at least {n} values (got {tuple(K.shape)})")
+    if x.numel() == 0 or x.numel() % n:
+        raise RuntimeError(f"x must hold a whole number of {tuple(dims)} grids (got {x.numel()} values)")
     B = x.numel() // n
     y = torch.empty(x.shape, dtype=out_dtype, device=x.device)
     call("mlpcg_stencil_apply", _p(K), _DT[K.dtype], K.shape[-1], _p(x), _DT[x.dtype], 0, _p(y),
@@ -208,7 +228,9 @@ def upsample2_adjoint(y):
 def axpby(c0, x, c1, y):
     """c0 * x + c1 * y with c0, c1 one-element device tensors."""
     _check(x, "x", (torch.float32, torch.bfloat16))
-    _check(y, "y", (torch.float32, torch.bfloat16))
+    _check(y, "y", (x.dtype,))
+    if x.numel() != y.numel():
+        raise RuntimeError(f"axpby: x and y sizes differ ({x.numel()} vs {y.numel()})")
     c0 = c0.reshape(1).to(torch.float32).contiguous()
     c1 = c1.reshape(1).to(torch.float32).contiguous()
     out = torch.empty_like(x)
@@ -220,6 +242,9 @@ def laplacian(flags, x):
     """Matrix-free mixed-boundary Poisson operator on full-grid vectors (F32 or F64)."""
     _check(flags, "flags", (torch.uint8,))
     _check(x, "x", (torch.float32, torch.float64))
+    if flags.dim() < 3 or x.numel() != flags.numel():
+        raise RuntimeError(f"laplacian: x must hold one value per cell of flags (got {x.numel()} for "
+                           f"{tuple(flags.shape)})")
     dims = tuple(flags.shape[-3:])
     y = torch.empty_like(x)
     call("mlpcg_laplacian_apply", _p(flags), _p(x), _p(y), _DT[x.dtype], *dims, _stream(x.device))

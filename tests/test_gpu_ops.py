@@ -305,3 +305,28 @@ def test_npsd_npcg_residual_histories(golden, cuda):
         np.testing.assert_allclose(h[ok][:31], r[ok][:31], rtol=1e-4)
         if name != "npcg_flex":
             assert it == int(d[f"{name}_iters"])
+
+
+def test_ops_refuse_mismatched_sizes(cuda):
+    """The size relations the kernels rely on (weights, gradients, plane strides, operand lengths)
+    are checked before any launch; a valid call still runs afterwards."""
+    from mlpcg_gb300 import ops
+    img = torch.zeros((3, 8, 8, 8), device=cuda)
+    x = torch.zeros((1, 1, 8, 8, 8), device=cuda)
+    W, b = torch.zeros((27, 3, 3, 3, 3), device=cuda), torch.zeros(27, device=cuda)
+    one = torch.ones(1, device=cuda)
+    with pytest.raises(RuntimeError):
+        ops.block_forward(img, x, W[:20], b)
+    with pytest.raises(RuntimeError):
+        ops.block_backward(torch.zeros((1, 1, 8, 8, 4), device=cuda), img, x, W, b)
+    with pytest.raises(RuntimeError):
+        ops.axpby(one, torch.zeros(10, device=cuda), one, torch.zeros(9, device=cuda))
+    with pytest.raises(RuntimeError):
+        ops.laplacian(torch.zeros((8, 8, 8), dtype=torch.uint8, device=cuda), torch.zeros(100, device=cuda))
+    K = ops.stencil_gen(img, W, b)
+    with pytest.raises(RuntimeError):
+        ops.stencil_apply(K, torch.zeros(100, device=cuda), (8, 8, 8))
+    with pytest.raises(RuntimeError):
+        ops.stencil_apply(K[:20].contiguous(), x, (8, 8, 8))
+    y = ops.block_forward(img, x, W, b)
+    assert y.shape == x.shape
