@@ -1,0 +1,27 @@
+"""bench.py's reference arm (the reference's CPU path on the host cores) prints exactly one JSON
+line with the benchmark contract's keys; run at 32^3 on the CPU so that it takes seconds."""
+import json
+import subprocess
+import sys
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def test_reference_arm_prints_one_contract_line():
+    cmd = [sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--size", "32", "--levels", "3",
+           "--cpu-seconds", "1", "--steps", "1", "--warmup", "0"]
+    r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.strip()]
+    assert len(lines) == 1, r.stdout
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 1 and d["higher_is_better"] is False
+    assert isinstance(d["metric"], str) and d["unit"] == "ms" and d["value"] > 0
+    assert d["ms_per_step"] == d["value"] and d["data"] == "synthetic" and "workload" in d["config"]
+    cb = d["cpu_baseline"]
+    assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["unit"] == "ms"
+    assert cb["value"] == d["value"] and "iterations at 32^3" in cb["sample"]
+    e2e = d["e2e"]
+    assert e2e["value"] == d["value"] and e2e["unit"] == "ms"
+    assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
