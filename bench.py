@@ -402,43 +402,50 @@ def coeff_bytes(plan, level, n_level, mixed):
 
 
 def iteration_bytes(plan, n0, mixed, mixed_t=None, method="npsd"):
-    """Compulsory HBM bytes of one fused iteration (bf16 coefficients and activations)."""
+    """Compulsory HBM bytes of one fused iteration (bf16 coefficients and activations; at level 0
+    the input r, the prolongated input u, the output z and, for SPDSMModelDn3D, V's output v0 are
+    FP32, and the fluid mask is read once per application; mirrors run_apply / run_apply_spd)."""
     total = 0.0
     # solver vectors: npsd dots + qform + spmv/dots, or npcg r.z + p/spmv; then the update (r every
     # iteration, 12 B; the double-float iterate with two directions every other one, 24 B)
     vec = n0 * (12 + 16 + 18 + 24) if method == "npsd" else n0 * (8 + 17 + 24)
     L = plan.levels
-    if plan.kind == 2:   # V (like the non-swap network, prolongation pass on every level), then V^T
+    if plan.kind == 2:   # V (prolongation pass on every level), then V^T
         for l in range(L):
             nl = n0 / 8 ** l
-            sv_in = 4 if l == 0 else 2
+            f = 4 if l == 0 else 2                                       # r, u, v0 at level 0: FP32
             kf, kt = coeff_bytes(plan, l, nl, mixed[l]), coeff_bytes(plan, l, nl, mixed_t[l])
-            total += kf + nl * (sv_in + 2 + 2 / 8)                      # V pre: x in, y out, pooled
-            total += nl * (2 / 8 + 2) + kf + nl * (2 + 2 + 2)            # V up pass; V post: u, y in, out
-            total += kt + nl * (2 + 2 / 8)                              # V^T pre: w in, pooled (no y)
-            total += nl * (2 / 8 + 2 + 2) + kt + nl * (2 + (4 + 1 if l == 0 else 2))   # V^T up + post
+            total += kf + nl * (f + 2 + 2 / 8)                          # V pre: x in, y out, pooled
+            total += nl * (2 / 8 + f) + kf + nl * (f + 2 + f)           # V up pass (u out); V post: u, y, out
+            total += kt + nl * (f + 2 / 8)                              # V^T pre: w in, pooled (no y)
+            total += nl * (2 / 8 + f + f)                               # V^T up pass: coarse, skip, u out
+            total += kt + nl * (f + (4 + 1 if l == 0 else 2))           # V^T post: u in, out (+ fluid mask)
         nL = n0 / 8 ** L
         total += coeff_bytes(plan, L, nL, mixed[L]) + coeff_bytes(plan, L, nL, mixed_t[L]) + nL * 8
         return total + vec
     if plan.spd:
         for l in range(L):
             nl = n0 / 8 ** l
-            sv_in = 4 if l == 0 else 2
-            total += coeff_bytes(plan, l, nl, mixed[l]) + nl * (sv_in + 2 + 2 / 8)   # pre: as below
-            # prolongation pass (coarse in, y in, u out), transposed block (u in, out; level 0: f32 z + mask)
-            total += nl * (2 / 8 + 2 + 2) + coeff_bytes(plan, l, nl, mixed_t[l]) + nl * (2 + (4 + 1 if l == 0 else 2))
+            f = 4 if l == 0 else 2
+            total += coeff_bytes(plan, l, nl, mixed[l]) + nl * (f + 2 + 2 / 8)   # pre: as below
+            # prolongation pass (coarse in, y in, u out), transposed block (u in, out; level 0: z + mask)
+            total += nl * (2 / 8 + 2 + f) + coeff_bytes(plan, l, nl, mixed_t[l]) + nl * (f + (4 + 1 if l == 0 else 2))
         nL = n0 / 8 ** L
         total += coeff_bytes(plan, L, nL, mixed[L]) + coeff_bytes(plan, L, nL, mixed_t[L]) + nL * 8
         return total + vec
+    m = 1 if plan.masked else 0
     for l in range(L):
         nl = n0 / 8 ** l
         kb = coeff_bytes(plan, l, nl, mixed[l])
-        sv_in = 4 if l == 0 else 2
-        total += kb + nl * (sv_in + 2 + 2 / 8)                  # pre: coefficients, x in, y out, pooled out
-        if l == 0:   # prolongation pass (coarse in, u out), then the block (u, y in, z out, masks)
-            total += nl * (2 / 8 + 2) + kb + nl * (2 + 2 + 4 + (2 if plan.masked else 0))
-        else:        # post: coefficients, coarse, y, out
-            total += kb + nl * (2 / 8 + 2 + 2)
+        if l == 0:
+            total += kb + nl * (4 + 2 + 2 / 8 + m)              # pre: coefficients, r in, y out, pooled out, mask
+            # prolongation pass (coarse in, u out; with swap also y in), then the block (u in, y in
+            # without swap, z out, the fluid mask and the optional block mask)
+            y_pass, y_block = (2, 0) if plan.swap else (0, 2)
+            total += nl * (2 / 8 + 4 + y_pass) + kb + nl * (4 + y_block + 4 + 1 + m)
+        else:
+            total += kb + nl * (2 + 2 + 2 / 8)                  # pre: coefficients, x in, y out, pooled out
+            total += kb + nl * (2 / 8 + 2 + 2)                  # post: coefficients, coarse, y, out
     total += coeff_bytes(plan, L, n0 / 8 ** L, mixed[L]) + (n0 / 8 ** L) * (2 + 2)
     return total + vec
 

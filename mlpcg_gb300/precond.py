@@ -78,6 +78,7 @@ class PrecondPlan:
         self.kind = network_kind(model)
         self.spd = self.kind != KIND_SM
         self.masked = False if self.spd else bool(model.pre[0].mask)
+        self.swap = False if self.spd else bool(model.swap_ord)
         self.device = image.device
         lib = _lib.load()
         h = C.c_void_p()
