@@ -68,6 +68,11 @@ class PrecondPlan:
     LAYOUTS = {"dense": 0, "classed": 1}
 
     def __init__(self, model, image, storage=torch.bfloat16, act_storage=None, layout="classed"):
+        if layout not in self.LAYOUTS:
+            raise ValueError(f"layout must be one of {sorted(self.LAYOUTS)} (got {layout!r})")
+        for dt in (storage, act_storage):
+            if dt is not None and dt not in _DT:
+                raise ValueError(f"storage dtypes must be torch.float32 or torch.bfloat16 (got {dt})")
         _check(image, "image")
         if image.dim() != 4 or image.shape[0] != 3:
             raise RuntimeError("image must have shape (3, N1, N2, N3)")

@@ -48,6 +48,8 @@ class FusedSolver:
     def __init__(self, model, flags: torch.Tensor, method="npsd", max_it=100, tol=1e-6, true_every=25,
                  storage=torch.bfloat16, act_storage=None, image=None, plan: PrecondPlan | None = None,
                  layout="classed"):
+        if method not in METHODS:
+            raise ValueError(f"method must be one of {sorted(METHODS)} (got {method!r})")
         if flags.dtype != torch.uint8 or flags.dim() != 3 or not flags.is_cuda:
             raise ValueError("flags must be a (N1, N2, N3) uint8 CUDA tensor")
         self.flags = flags.contiguous()

@@ -115,3 +115,18 @@ def test_precond_apply_rejects_misaligned_vectors(lib):
     finally:
         lib.mlpcg_precond_destroy(plan)
 
+
+
+def test_python_constructors_refuse_unknown_options():
+    """Unknown solver methods, coefficient layouts and storage dtypes are refused up front with a
+    ValueError naming the option (no device work)."""
+    import torch
+    from mlpcg_gb300.precond import PrecondPlan
+    from mlpcg_gb300.solver import FusedSolver
+    with pytest.raises(ValueError, match="method"):
+        FusedSolver(None, torch.zeros((4, 4, 4), dtype=torch.uint8), method="cg")
+    img = torch.zeros((3, 4, 4, 4))
+    with pytest.raises(ValueError, match="layout"):
+        PrecondPlan(None, img, layout="sparse")
+    with pytest.raises(ValueError, match="storage"):
+        PrecondPlan(None, img, storage=torch.float16)
