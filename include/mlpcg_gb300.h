@@ -435,10 +435,10 @@ int mlpcg_dot(const void *x, const void *y, int dtype, int64_t n, double *out,
 
 /*
  * mlpcg_dot without a workspace (no counterpart in the reference).  For
- * callers that cannot allocate device memory: code running while a stream
- * is captured in global or thread-local mode (where cudaMalloc is not
- * permitted), real-time loops that must not enter an allocator, and host
- * runtimes that own all device memory and forbid library allocations.
+ * callers that cannot allocate device memory: real-time loops that must not
+ * enter an allocator (its latency is unbounded), and host runtimes or
+ * plug-in hosts that own all device memory through their own arena and give
+ * a library only the buffers of its inputs and outputs.
  * The block partial sums live in a 64 KiB file-scope device array of this
  * library (one partial per 2048 elements), so n <= 16,777,216; larger n is
  * rejected with MLPCG_ERR_SHAPE and a message.  It calls no cudaMalloc,

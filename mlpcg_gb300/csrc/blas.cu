@@ -74,11 +74,10 @@ int launch_dot(const void *x, const void *y, int dt, int64_t n, double *out, voi
 // ---------------------------------------------------------------------------
 // mlpcg_dot_noalloc: the same reduction with its block partials in a
 // file-scope device array instead of a caller workspace, for callers that
-// cannot allocate device memory: code that runs while a stream is being
-// captured in global or thread-local mode (cudaMalloc is not permitted
-// there), real-time loops that must never enter the allocator, and host
-// runtimes that own all device memory through their own arena and forbid
-// libraries from allocating.  One partial per 2048 elements, at most 8192
+// cannot allocate device memory: real-time loops that must never enter the
+// allocator (its latency is unbounded), and host runtimes or plug-in hosts
+// that own all device memory through their own arena and give a library
+// only the buffers of its inputs and outputs.  One partial per 2048 elements, at most 8192
 // partials (64 KiB), so n <= 16,777,216 (a 256^3 grid).  Every GPU that
 // loads this library holds the 64 KiB until the process exits.
 // ---------------------------------------------------------------------------
