@@ -335,6 +335,23 @@ int mlpcg_precond_apply_stages(const mlpcg_precond *plan, int first, int last, c
  * did not complete within the kernel's bounded wait -- the outputs of such
  * an application are not valid -- else 0. */
 int mlpcg_precond_check(const mlpcg_precond *plan, int *copy_failed, void *stream);
+/* The coarse levels of a SmallSMModelDn3D plan (no counterpart in the
+ * reference, which launches every block and transfer separately): from
+ * *first_level on, an application runs the pre-blocks, the coarsest block
+ * and the post-blocks in one launch of one thread-block cluster of *ctas
+ * CTAs, stage after stage.  *first_level = -1 (and *ctas = 0) when no two
+ * coarsest levels qualify (they must all run the tiled kernels), for the
+ * symmetric kinds, or when the device runs no cluster of 8 or 16 CTAs.
+ * mlpcg_precond_apply_stages uses it only when [first, last] covers all of
+ * its stages (first_level .. 2n - first_level). */
+int mlpcg_precond_coarse_cluster(const mlpcg_precond *plan, int *first_level, int *ctas);
+/* Test knob of the bounded TMA waits (no counterpart in the reference):
+ * with on != 0 the level-0 tile kernels first wait on a barrier that nothing
+ * arrives on (256 polls), so the wait runs out on an ordinary copy, whose
+ * completion they then wait for before leaving; the plan's applications
+ * then report copy_failed.  Every call also clears the copy-failed word;
+ * on = 0 restores normal waits.  Off after every mlpcg_precond_setup. */
+int mlpcg_precond_set_copy_stall(mlpcg_precond *plan, int on, void *stream);
 /* Sizes of level `level` (0 = finest) and whether it runs the tiled kernels
  * (z size a multiple of 8) or the general ones. */
 int mlpcg_precond_level_info(const mlpcg_precond *plan, int level, int *n1, int *n2, int *n3,
@@ -377,6 +394,10 @@ int mlpcg_solver_bind(mlpcg_solver *solver, void *workspace, size_t workspace_by
  * is captured on the first call and reused until the next bind); 0: plain
  * launches with a host status check per iteration. */
 int mlpcg_solver_solve(mlpcg_solver *solver, int use_graph, void *stream);
+/* mlpcg_solver_solve with the initial guess x0 = 0, the reference's call
+ * (test.py:328 passes torch.zeros_like(rhs) to npsd): x is not read, and
+ * every cell of x is written by the solve (0 off the fluid cells). */
+int mlpcg_solver_solve_zero_guess(mlpcg_solver *solver, int use_graph, void *stream);
 /* Synchronises `stream`, then returns iterations, status, the final relative
  * residual and (if history != NULL) max_it+1 relative residuals (host). */
 int mlpcg_solver_result(const mlpcg_solver *solver, int *iterations, int *status, double *rel_res,
@@ -388,6 +409,14 @@ int mlpcg_solver_result(const mlpcg_solver *solver, int *iterations, int *status
  * solve (the captured graph is rebuilt); batches already built keep theirs. */
 int mlpcg_solver_set_schedule(mlpcg_solver *solver, int blocks);
 int mlpcg_solver_get_schedule(const mlpcg_solver *solver, int *blocks_in_use);
+
+/* Test knob of the SpMV's bounded TMA waits (no counterpart in the
+ * reference), taking effect from the next solve: with on != 0 the npsd
+ * SpMV's first tile wait polls a barrier that nothing arrives on (256 polls)
+ * and runs out while the real copy completes, so the solve ends with
+ * MLPCG_STATUS_COPY_FAILED.  A solve also ends so when the plan's tile copies
+ * failed (mlpcg_precond_set_copy_stall).  on = 0 restores normal waits. */
+int mlpcg_solver_set_copy_stall(mlpcg_solver *solver, int on);
 
 /* Many systems in one launch (no counterpart in the reference, whose solver
  * takes one system at a time): `count` (<= 64) bound solvers, each with its

@@ -46,6 +46,8 @@ _PROTOS = {
     "mlpcg_precond_create_spd": (_i, [_i, _i, _i, _i, _i, _i, _i, _vp]),
     "mlpcg_precond_create_kind": (_i, [_i, _i, _i, _i, _i, _i, _i, _i, _vp]),
     "mlpcg_precond_check": (_i, [_vp, _vp, _vp]),
+    "mlpcg_precond_set_copy_stall": (_i, [_vp, _i, _vp]),
+    "mlpcg_precond_coarse_cluster": (_i, [_vp, _vp, _vp]),
     "mlpcg_precond_class_counts": (_i, [_vp, _i, _vp, _vp, _vp]),
     "mlpcg_precond_class_counts_transposed": (_i, [_vp, _i, _vp, _vp, _vp]),
     "mlpcg_precond_workspace": (_sz, [_vp]),
@@ -60,8 +62,10 @@ _PROTOS = {
     "mlpcg_solver_destroy": (None, [_vp]),
     "mlpcg_solver_bind": (_i, [_vp, _vp, _sz, _u8p, _vp, _vp]),
     "mlpcg_solver_solve": (_i, [_vp, _i, _vp]),
+    "mlpcg_solver_solve_zero_guess": (_i, [_vp, _i, _vp]),
     "mlpcg_solver_result": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "mlpcg_solver_set_schedule": (_i, [_vp, _i]),
+    "mlpcg_solver_set_copy_stall": (_i, [_vp, _i]),
     "mlpcg_solver_get_schedule": (_i, [_vp, _vp]),
     "mlpcg_batch_create": (_i, [_vp, _i, _vp]),
     "mlpcg_batch_solve": (_i, [_vp, _vp]),

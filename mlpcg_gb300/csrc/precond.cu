@@ -55,6 +55,38 @@ __device__ __forceinline__ float4 ldv4(const __nv_bfloat16 *p) {
                      __uint_as_float(u.y << 16), __uint_as_float(u.y & 0xffff0000u));
 }
 
+// Activation loads of the block bodies.  COH = false: the read-only data path (__ldg), for inputs
+// written by earlier kernels; COH = true: through L2 only (__ldcg), for inputs that other CTAs of
+// the same launch wrote before a cluster barrier (the coarse-level cluster kernel).
+template <bool COH> __device__ __forceinline__ float4 ldv4c(const float *p) {
+  return COH ? __ldcg(reinterpret_cast<const float4 *>(p)) : __ldg(reinterpret_cast<const float4 *>(p));
+}
+template <bool COH> __device__ __forceinline__ float4 ldv4c(const __nv_bfloat16 *p) {
+  const uint2 u = COH ? __ldcg(reinterpret_cast<const uint2 *>(p)) : __ldg(reinterpret_cast<const uint2 *>(p));
+  return make_float4(__uint_as_float(u.x << 16), __uint_as_float(u.x & 0xffff0000u),
+                     __uint_as_float(u.y << 16), __uint_as_float(u.y & 0xffff0000u));
+}
+template <bool COH> __device__ __forceinline__ float ldfc(const float *p) { return COH ? __ldcg(p) : __ldg(p); }
+template <bool COH> __device__ __forceinline__ float ldfc(const __nv_bfloat16 *p) {
+  if (COH) {
+    const unsigned short u = __ldcg(reinterpret_cast<const unsigned short *>(p));
+    return __uint_as_float((uint32_t)u << 16);
+  }
+  return __bfloat162float(*p);
+}
+
+// The tile a CTA works on: tile coordinates (bx: z, by: y, bz: x, in units of TZ, TY, TX) and the
+// linear tile index bx + gx (by + gy bz).  A kernel launched over the tile grid takes its own block
+// index (grid_tile); the coarse-level cluster kernel walks the tiles of each level itself.
+struct Tile {
+  int bx, by, bz;
+  unsigned id;
+};
+__device__ __forceinline__ Tile grid_tile() {
+  return Tile{(int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z,
+              blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)};
+}
+
 // The 16 tile values S[row][z .. z + 15] (z a multiple of 4) by four 16-byte loads
 __device__ __forceinline__ void ld_row16(const float *row, float xr[16]) {
 #pragma unroll
@@ -90,8 +122,8 @@ __device__ __forceinline__ int stage_vec_row(int m) { return threadIdx.x / NVR +
 __device__ __forceinline__ int stage_halo_id(int m) { return threadIdx.x + m * PT; }
 
 template <typename F4, typename F1>
-__device__ __forceinline__ void stage_load(FineStage &st, int n1, int n2, int n3, F4 ld4, F1 ld1) {
-  const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY, x0 = blockIdx.z * TX;
+__device__ __forceinline__ void stage_load(FineStage &st, const Tile &t, int n1, int n2, int n3, F4 ld4, F1 ld1) {
+  const int z0 = t.bx * TZ, y0 = t.by * TY, x0 = t.bz * TX;
   const int k = z0 + 4 * (threadIdx.x % NVR);
 #pragma unroll
   for (int m = 0; m < kStageVec; ++m) {
@@ -148,6 +180,19 @@ __device__ __forceinline__ void ld8(const float *p, float v[8]) {
 }
 __device__ __forceinline__ void ld8(const __nv_bfloat16 *p, float v[8]) {
   const uint4 u = __ldg(reinterpret_cast<const uint4 *>(p));
+  unpack_bf16x2(u.x, v[0], v[1]); unpack_bf16x2(u.y, v[2], v[3]);
+  unpack_bf16x2(u.z, v[4], v[5]); unpack_bf16x2(u.w, v[6], v[7]);
+}
+// ld8 for activations: through L2 only (COH) or the read-only path
+template <bool COH> __device__ __forceinline__ void ld8c(const float *p, float v[8]) {
+  if (!COH) return ld8(p, v);
+  const float4 a = __ldcg(reinterpret_cast<const float4 *>(p));
+  const float4 b = __ldcg(reinterpret_cast<const float4 *>(p) + 1);
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+template <bool COH> __device__ __forceinline__ void ld8c(const __nv_bfloat16 *p, float v[8]) {
+  if (!COH) return ld8(p, v);
+  const uint4 u = __ldcg(reinterpret_cast<const uint4 *>(p));
   unpack_bf16x2(u.x, v[0], v[1]); unpack_bf16x2(u.y, v[2], v[3]);
   unpack_bf16x2(u.z, v[4], v[5]); unpack_bf16x2(u.w, v[6], v[7]);
 }
@@ -240,12 +285,12 @@ __device__ __forceinline__ int cta_excl_scan(int v, int &total) {
 __device__ __forceinline__ unsigned tile_id() { return blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z); }
 
 // run words of the thread's two runs (uniform solid for a run outside the grid)
-__device__ __forceinline__ void load_run_words(const uint32_t *__restrict__ rw, int n1, int n2, int n3,
-                                               uint32_t w[TX]) {
-  const int k0 = blockIdx.x * TZ + run_tz(threadIdx.x) * 8, j = blockIdx.y * TY + run_ty(threadIdx.x);
+__device__ __forceinline__ void load_run_words(const uint32_t *__restrict__ rw, const Tile &t, int n1, int n2,
+                                               int n3, uint32_t w[TX]) {
+  const int k0 = t.bx * TZ + run_tz(threadIdx.x) * 8, j = t.by * TY + run_ty(threadIdx.x);
 #pragma unroll
   for (int tx = 0; tx < TX; ++tx) {
-    const int i = blockIdx.z * TX + tx;
+    const int i = t.bz * TX + tx;
     w[tx] = CLS_SOLID;
     if (k0 < n3 && j < n2 && i < n1) w[tx] = __ldg(rw + ((((int64_t)i * n2 + j) * n3 + k0) >> 3));
   }
@@ -739,10 +784,10 @@ __device__ __forceinline__ void apply_pair(const float (*S)[HY][HZP], int ty, in
 // mixed-run count (load_tile_runs).
 template <typename KT, bool CLS, int OFF = 0>
 __device__ __forceinline__ void tile_apply(const float (*S)[HY][HZP], const ClsSmem *sm, const CoefArgs<KT> &C,
-                                           const uint32_t rwd[TX], uint2 trec, int n1, int n2, int n3,
-                                           float acc[TX][8]) {
+                                           const uint32_t rwd[TX], uint2 trec, const Tile &t, int n1, int n2,
+                                           int n3, float acc[TX][8]) {
   const int tz = run_tz(threadIdx.x), ty = run_ty(threadIdx.x);
-  const int x0 = blockIdx.z * TX, k0 = blockIdx.x * TZ + tz * 8, j = blockIdx.y * TY + ty;
+  const int x0 = t.bz * TX, k0 = t.bx * TZ + tz * 8, j = t.by * TY + ty;
   const bool active = k0 < n3 && j < n2;
   bool valid[TX];
 #pragma unroll
@@ -800,25 +845,27 @@ __device__ __forceinline__ void stage_uniform(ClsSmem *sm, const float *__restri
 // asks for the whole block to be brought into L2 with one bulk prefetch, so that the record
 // loads of the block application, issued after the tile is staged, find it there.
 template <typename KT, bool CLS>
-__device__ __forceinline__ uint2 load_tile_runs(const CoefArgs<KT> &C, int n1, int n2, int n3, uint32_t rwd[TX]) {
+__device__ __forceinline__ uint2 load_tile_runs(const CoefArgs<KT> &C, const Tile &t, int n1, int n2, int n3,
+                                                uint32_t rwd[TX]) {
   if (!CLS) return make_uint2(0u, 0u);
-  const uint2 tb = make_uint2(__ldg(C.rbase + tile_id()), __ldg(C.rcount + tile_id()));
+  const uint2 tb = make_uint2(__ldg(C.rbase + t.id), __ldg(C.rcount + t.id));
   if (threadIdx.x == 0 && tb.y > 0) {
     // record block: RREC values per run, 16-byte aligned (RREC * sizeof(KT) is a multiple of 16)
     const size_t addr = __cvta_generic_to_global(C.rec + (size_t)tb.x * RREC);
     const uint32_t bytes = tb.y * (uint32_t)(RREC * sizeof(KT));
     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(addr), "r"(bytes) : "memory");
   }
-  load_run_words(C.rw, n1, n2, n3, rwd);
+  load_run_words(C.rw, t, n1, n2, n3, rwd);
   return tb;
 }
 
 // mask bytes of the thread's runs (all ones without a mask)
-__device__ __forceinline__ void load_run_mask(const uint8_t *__restrict__ m, int n1, int n2, int n3, uint2 mw[TX]) {
-  const int k0 = blockIdx.x * TZ + run_tz(threadIdx.x) * 8, j = blockIdx.y * TY + run_ty(threadIdx.x);
+__device__ __forceinline__ void load_run_mask(const uint8_t *__restrict__ m, const Tile &t, int n1, int n2, int n3,
+                                              uint2 mw[TX]) {
+  const int k0 = t.bx * TZ + run_tz(threadIdx.x) * 8, j = t.by * TY + run_ty(threadIdx.x);
 #pragma unroll
   for (int tx = 0; tx < TX; ++tx) {
-    const int i = blockIdx.z * TX + tx;
+    const int i = t.bz * TX + tx;
     mw[tx] = make_uint2(0xffffffffu, 0xffffffffu);
     if (m && k0 < n3 && j < n2 && i < n1) mw[tx] = __ldg(reinterpret_cast<const uint2 *>(m + ((int64_t)i * n2 + j) * n3 + k0));
   }
@@ -836,9 +883,10 @@ __device__ __forceinline__ void apply_run_mask(uint2 m, float acc[8]) {
 // tensor-memory accelerator copy the 4 x 18 x 76 FP32 box of the tile's input -- z from
 // z0 - 4 (a multiple of 4 floats, 16 bytes), y from y0 - 1, x from x0 - 1, zero outside
 // the grid -- into S (interior cell z0 + c at row index c + 4).
-__device__ __forceinline__ void tma_tile_issue(float (*S)[HY][HZP], uint32_t bar, const CUtensorMap *tmap) {
+__device__ __forceinline__ void tma_tile_issue(float (*S)[HY][HZP], uint32_t bar, const CUtensorMap *tmap,
+                                               const Tile &t) {
   if (threadIdx.x != 0) return;
-  const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY, x0 = blockIdx.z * TX;
+  const int z0 = t.bx * TZ, y0 = t.by * TY, x0 = t.bz * TX;
   asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
@@ -850,21 +898,69 @@ __device__ __forceinline__ void tma_tile_issue(float (*S)[HY][HZP], uint32_t bar
       : "memory");
 }
 
-// All threads, after a __syncthreads that follows tma_tile_issue: wait for the tile (phase 0)
-// with a bounded poll.  A copy that has not landed after about a second is reported through
-// *err; the thread then waits once more (bounded) and the caller leaves.  Returns true when
-// the tile is in place.
-__device__ __forceinline__ bool tma_tile_wait(uint32_t bar, int *err) {
+// Shared state of a TMA-staged tile's wait: the copy's mbarrier, a second mbarrier that nothing
+// ever arrives on (initialised for one arrival; the copy-stall test waits on it so that the bounded
+// wait runs out while the real copy completes normally), and the CTA's copy-failed flag.
+struct TileWait {
+  uint64_t bar, never;
+  int failed;
+};
+
+// Thread 0, before the __syncthreads that precedes tma_tile_wait: the second barrier and the flag.
+__device__ __forceinline__ void tile_wait_init(TileWait &w) {
+  if (threadIdx.x != 0) return;
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((uint32_t)__cvta_generic_to_shared(&w.never))
+               : "memory");
+  w.failed = 0;
+}
+
+__device__ __forceinline__ uint32_t mbar_poll(uint32_t bar, uint32_t limit) {
   uint32_t done = 0;
-  for (uint32_t it = 0; it < (1u << 22) && !done; ++it)
+  for (uint32_t it = 0; it < limit && !done; ++it)
     asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0; selp.u32 %0, 1, 0, p; }"
                  : "=r"(done) : "r"(bar) : "memory");
-  if (done) return true;
-  if (threadIdx.x == 0) atomicExch(err, 1);
-  for (uint32_t it = 0; it < (1u << 22) && !done; ++it)
-    asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0; selp.u32 %0, 1, 0, p; }"
-                 : "=r"(done) : "r"(bar) : "memory");
-  return false;
+  return done;
+}
+
+// All threads, after a __syncthreads that follows tma_tile_issue and tile_wait_init: wait for the
+// tile (phase 0) with a bounded poll (2^22 tries, about a second).  A thread whose poll runs out
+// raises the CTA's flag and *err, then waits once more (bounded) so that a late copy lands before the
+// CTA leaves; the CTA then agrees on the flag (one __syncthreads), so every thread returns the same
+// verdict: true when the tile is in place.  err[1] != 0 (the copy-stall test knob) makes the first
+// poll wait on the barrier that never completes, 256 tries, so the timeout path runs on an ordinary
+// copy; the second poll then waits for the real copy as usual.
+__device__ __forceinline__ bool tma_tile_wait(TileWait &w, int *err) {
+  const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&w.bar);
+  const bool stall = err[1] != 0;
+  const uint32_t first = stall ? (uint32_t)__cvta_generic_to_shared(&w.never) : bar;
+  if (!mbar_poll(first, stall ? 256u : (1u << 22))) {
+    w.failed = 1;
+    atomicExch(err, 1);
+    mbar_poll(bar, 1u << 22);
+  }
+  __syncthreads();
+  return !w.failed;
+}
+
+// Shared memory of the block bodies, one object per kernel whichever bodies it runs: the fine
+// input tile, the classed path's uniform vectors, the tile copy's wait state and the post-block's
+// coarse tile.  A kernel that runs several bodies one after the other (the coarse-level cluster
+// kernel) reuses them, separating the bodies with barriers.
+__device__ __forceinline__ float (*fine_tile_smem())[HY][HZP] {
+  __shared__ __align__(128) float S[HX][HY][HZP];
+  return S;
+}
+__device__ __forceinline__ ClsSmem *cls_smem() {
+  __shared__ ClsSmem smc;
+  return &smc;
+}
+__device__ __forceinline__ TileWait &tile_wait_smem() {
+  __shared__ __align__(8) TileWait tw;
+  return tw;
+}
+__device__ __forceinline__ float (*coarse_tile_smem())[CY][CZP] {
+  __shared__ __align__(16) float Cs[CX][CY][CZP];
+  return Cs;
 }
 
 // The body of the pre-block kernels.  Staged: every thread loads its share of
@@ -873,40 +969,41 @@ __device__ __forceinline__ bool tma_tile_wait(uint32_t bar, int *err) {
 // 4 x 18 x 76 box of the input (z from z0 - 4, outside the grid read as 0)
 // into the tile, completing on an mbarrier; the scale is applied to the
 // block's output instead (the block is linear in x).
-template <typename KT, typename XT, typename YT, bool POOL, bool CLS, bool TMA>
+template <typename KT, typename XT, typename YT, bool POOL, bool CLS, bool TMA, bool COH = false>
 __device__ __forceinline__ void pre_fused_body(const CoefArgs<KT> &C, const XT *__restrict__ x,
                                                const float *__restrict__ xscale, YT *__restrict__ y,
                                                YT *__restrict__ ypool, const uint8_t *__restrict__ mask, int n1,
-                                               int n2, int n3, const CUtensorMap *tmap, int *err) {
-  __shared__ __align__(128) float S[HX][HY][HZP];
-  __shared__ typename std::conditional<CLS, ClsSmem, int>::type smc_raw;
-  __shared__ __align__(8) uint64_t mbar;
-  ClsSmem *smc = CLS ? reinterpret_cast<ClsSmem *>(&smc_raw) : nullptr;
-  const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY, x0 = blockIdx.z * TX;
+                                               int n2, int n3, const CUtensorMap *tmap, int *err, const Tile &t) {
+  float(*S)[HY][HZP] = fine_tile_smem();
+  ClsSmem *smc = CLS ? cls_smem() : nullptr;
+  TileWait &tw = tile_wait_smem();
+  const int z0 = t.bx * TZ, y0 = t.by * TY, x0 = t.bz * TX;
   const float sc = xscale ? __ldg(xscale) : 1.f;
-  const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&mbar);
-  if constexpr (TMA) tma_tile_issue(S, bar, tmap);
+  if constexpr (TMA) {
+    tile_wait_init(tw);
+    tma_tile_issue(S, (uint32_t)__cvta_generic_to_shared(&tw.bar), tmap, t);
+  }
   uint32_t rwd[TX];
   uint2 mw[TX];
-  const uint2 tb = load_tile_runs<KT, CLS>(C, n1, n2, n3, rwd);
-  load_run_mask(mask, n1, n2, n3, mw);
+  const uint2 tb = load_tile_runs<KT, CLS>(C, t, n1, n2, n3, rwd);
+  load_run_mask(mask, t, n1, n2, n3, mw);
   if constexpr (!TMA) {
     FineStage fs;
-    stage_load(fs, n1, n2, n3,
+    stage_load(fs, t, n1, n2, n3,
                [&](int, int, int, int64_t q) {
-                 const float4 v = ldv4(x + q);
+                 const float4 v = ldv4c<COH>(x + q);
                  return make_float4(v.x * sc, v.y * sc, v.z * sc, v.w * sc);
                },
-               [&](int, int, int, int64_t q) { return ldf(x + q) * sc; });
+               [&](int, int, int, int64_t q) { return ldfc<COH>(x + q) * sc; });
     stage_put(S, fs);
   }
   stage_uniform<CLS>(smc, C.kuni);
   __syncthreads();  // also orders the mbarrier initialisation before the other threads' waits
   if constexpr (TMA) {
-    if (!tma_tile_wait(bar, err)) return;
+    if (!tma_tile_wait(tw, err)) return;
   }
   float acc[TX][8];
-  tile_apply<KT, CLS, TMA ? 3 : 0>(S, smc, C, rwd, tb, n1, n2, n3, acc);
+  tile_apply<KT, CLS, TMA ? 3 : 0>(S, smc, C, rwd, tb, t, n1, n2, n3, acc);
   const int tz = run_tz(threadIdx.x), ty = run_ty(threadIdx.x);
   const int k0 = z0 + tz * 8, j = y0 + ty;
   const bool active = k0 < n3 && j < n2;  // n3 % 8 == 0: a run is all in or all out
@@ -930,7 +1027,8 @@ __device__ __forceinline__ void pre_fused_body(const CoefArgs<KT> &C, const XT *
   if (POOL) {
 #pragma unroll
     for (int c = 0; c < 4; ++c) pool[c] += __shfl_xor_sync(0xffffffffu, pool[c], kTyPairLane);
-    if (active && (ty & 1) == 0) {
+    // (the cluster kernel also runs its coarsest block through this body, with no pooled output)
+    if (active && (ty & 1) == 0 && (!COH || ypool)) {
       const int m2 = n2 / 2, m3 = n3 / 2;
       const int64_t qc = ((int64_t)(x0 / 2) * m2 + j / 2) * m3 + k0 / 2;
 #pragma unroll
@@ -947,7 +1045,8 @@ k_pre_fused(const CoefArgs<KT> C, const XT *__restrict__ x,
             const float *__restrict__ xscale, YT *__restrict__ y, YT *__restrict__ ypool,
             const uint8_t *__restrict__ mask, int n1, int n2, int n3, const int *__restrict__ gate) {
   if (gate && *gate != 0) return;  // batched solves: this system has stopped
-  pre_fused_body<KT, XT, YT, POOL, CLS, false>(C, x, xscale, y, ypool, mask, n1, n2, n3, nullptr, nullptr);
+  pre_fused_body<KT, XT, YT, POOL, CLS, false>(C, x, xscale, y, ypool, mask, n1, n2, n3, nullptr, nullptr,
+                                              grid_tile());
 }
 
 // the level-0 pre-block with its FP32 input tile loaded by TMA through tmap (x only for the
@@ -958,7 +1057,8 @@ k_pre_fused_tma(const CoefArgs<KT> C, const __grid_constant__ CUtensorMap tmap, 
                 YT *__restrict__ y, YT *__restrict__ ypool, const uint8_t *__restrict__ mask, int n1, int n2, int n3,
                 const int *__restrict__ gate, int *__restrict__ err) {
   if (gate && *gate != 0) return;
-  pre_fused_body<KT, float, YT, true, CLS, true>(C, nullptr, xscale, y, ypool, mask, n1, n2, n3, &tmap, err);
+  pre_fused_body<KT, float, YT, true, CLS, true>(C, nullptr, xscale, y, ypool, mask, n1, n2, n3, &tmap, err,
+                                                grid_tile());
 }
 
 // ---------------------------------------------------------------------------
@@ -999,9 +1099,10 @@ constexpr int kCoarseVec = (CX * CY * CNV + PT - 1) / PT;
 
 // Stages the coarse tile of the CTA's fine tile (x_{l+1} with a one-cell
 // halo; 0 outside the grid): every global load first, then the stores.
-template <typename CT>
-__device__ __forceinline__ void stage_coarse(float (*Cs)[CY][CZP], const CT *__restrict__ xc, int m1, int m2, int m3) {
-  const int cx0 = blockIdx.z * TX / 2 - 1, cy0 = blockIdx.y * TY / 2 - 1, cz0 = blockIdx.x * TZ / 2 - 1;
+template <typename CT, bool COH = false>
+__device__ __forceinline__ void stage_coarse(float (*Cs)[CY][CZP], const CT *__restrict__ xc, const Tile &t, int m1,
+                                             int m2, int m3) {
+  const int cx0 = t.bz * TX / 2 - 1, cy0 = t.by * TY / 2 - 1, cz0 = t.bx * TZ / 2 - 1;
   float4 cv[kCoarseVec];
   float ch = 0.f;
 #pragma unroll
@@ -1010,13 +1111,13 @@ __device__ __forceinline__ void stage_coarse(float (*Cs)[CY][CZP], const CT *__r
     const int i = cx0 + r / CY, j = cy0 + r % CY, k = cz0 + 1 + 4 * (e % CNV);
     cv[m] = make_float4(0.f, 0.f, 0.f, 0.f);
     if (e < CX * CY * CNV && (unsigned)i < (unsigned)m1 && (unsigned)j < (unsigned)m2 && k < m3)
-      cv[m] = ldv4(xc + ((int64_t)i * m2 + j) * m3 + k);
+      cv[m] = ldv4c<COH>(xc + ((int64_t)i * m2 + j) * m3 + k);
   }
   {
     const int e = threadIdx.x, r = e >> 1;
     const int i = cx0 + r / CY, j = cy0 + r % CY, k = (e & 1) ? cz0 + CZ - 1 : cz0;
     if (e < 2 * CX * CY && (unsigned)i < (unsigned)m1 && (unsigned)j < (unsigned)m2 && (unsigned)k < (unsigned)m3)
-      ch = ldf(xc + ((int64_t)i * m2 + j) * m3 + k);
+      ch = ldfc<COH>(xc + ((int64_t)i * m2 + j) * m3 + k);
   }
 #pragma unroll
   for (int m = 0; m < kCoarseVec; ++m) {
@@ -1056,7 +1157,7 @@ k_up_fine(const CT *__restrict__ xc, const YT *__restrict__ yl, const float *__r
     for (int tx = 0; tx < TX; ++tx)
       if (active && x0 + tx < n1) ld8(yl + ((int64_t)(x0 + tx) * n2 + j) * n3 + k0, yv[tx]);
   }
-  stage_coarse(Cs, xc, m1, m2, m3);
+  stage_coarse(Cs, xc, grid_tile(), m1, m2, m3);
   __syncthreads();
   if (!active) return;
   const float c0 = SWAP ? __ldg(c0p) : 0.f, c1 = SWAP ? __ldg(c1p) : 0.f;
@@ -1133,47 +1234,49 @@ k_up_fine(const CT *__restrict__ xc, const YT *__restrict__ yl, const float *__r
 // with y_l under swap), staged like a pre-block input.
 // TMA (UPIN, CT = float): the FP32 input u arrives by the tensor-memory accelerator as in the
 // level-0 pre-block (tma_tile_issue / tma_tile_wait).
-template <typename KT, typename CT, typename YT, typename OT, bool SWAP, bool CLS, bool UPIN, bool TMA>
+template <typename KT, typename CT, typename YT, typename OT, bool SWAP, bool CLS, bool UPIN, bool TMA,
+          bool COH = false>
 __device__ __forceinline__ void post_fused_body(const CoefArgs<KT> &C, const CT *__restrict__ xc,
                                                 const YT *__restrict__ yl, const float *__restrict__ c0p,
                                                 const float *__restrict__ c1p, OT *__restrict__ out,
                                                 const uint8_t *__restrict__ bmask,
                                                 const uint8_t *__restrict__ omask, int n1, int n2, int n3,
-                                                const CUtensorMap *tmap, int *err) {
+                                                const CUtensorMap *tmap, int *err, const Tile &t) {
   static_assert(!TMA || UPIN, "TMA staging needs the prolongated input");
-  __shared__ __align__(128) float S[HX][HY][HZP];
-  __shared__ __align__(16) typename std::conditional<UPIN, int, float[CX][CY][CZP]>::type cs_raw;
-  __shared__ typename std::conditional<CLS, ClsSmem, int>::type smc_raw;
-  __shared__ __align__(8) uint64_t mbar;
-  const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&mbar);
-  if constexpr (TMA) tma_tile_issue(S, bar, tmap);
-  float(*Cs)[CY][CZP] = reinterpret_cast<float(*)[CY][CZP]>(&cs_raw);
-  ClsSmem *smc = CLS ? reinterpret_cast<ClsSmem *>(&smc_raw) : nullptr;
+  float(*S)[HY][HZP] = fine_tile_smem();
+  TileWait &tw = tile_wait_smem();
+  if constexpr (TMA) {
+    tile_wait_init(tw);
+    tma_tile_issue(S, (uint32_t)__cvta_generic_to_shared(&tw.bar), tmap, t);
+  }
+  float(*Cs)[CY][CZP] = nullptr;
+  if constexpr (!UPIN) Cs = coarse_tile_smem();
+  ClsSmem *smc = CLS ? cls_smem() : nullptr;
   stage_uniform<CLS>(smc, C.kuni);
-  const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY, x0 = blockIdx.z * TX;
+  const int z0 = t.bx * TZ, y0 = t.by * TY, x0 = t.bz * TX;
   const int m1 = n1 / 2, m2 = n2 / 2, m3 = n3 / 2;
   const int cx0 = x0 / 2 - 1, cy0 = y0 / 2 - 1, cz0 = z0 / 2 - 1;
   const float c0 = __ldg(c0p), c1 = __ldg(c1p);
   uint32_t rwd[TX];
   uint2 bw[TX], ow[TX];
-  const uint2 tb = load_tile_runs<KT, CLS>(C, n1, n2, n3, rwd);
-  load_run_mask(bmask, n1, n2, n3, bw);
-  load_run_mask(omask, n1, n2, n3, ow);
+  const uint2 tb = load_tile_runs<KT, CLS>(C, t, n1, n2, n3, rwd);
+  load_run_mask(bmask, t, n1, n2, n3, bw);
+  load_run_mask(omask, t, n1, n2, n3, ow);
   if (UPIN) {
     if constexpr (!TMA) {
       FineStage fs;
-      stage_load(fs, n1, n2, n3, [&](int, int, int, int64_t q) { return ldv4(xc + q); },
-                 [&](int, int, int, int64_t q) { return ldf(xc + q); });
+      stage_load(fs, t, n1, n2, n3, [&](int, int, int, int64_t q) { return ldv4c<COH>(xc + q); },
+                 [&](int, int, int, int64_t q) { return ldfc<COH>(xc + q); });
       stage_put(S, fs);
     }
   } else {
     if (SWAP) {  // y_l goes straight into the fine tile; the combine below reads it back in place
       FineStage fs;
-      stage_load(fs, n1, n2, n3, [&](int, int, int, int64_t q) { return ldv4(yl + q); },
-                 [&](int, int, int, int64_t q) { return ldf(yl + q); });
+      stage_load(fs, t, n1, n2, n3, [&](int, int, int, int64_t q) { return ldv4c<COH>(yl + q); },
+                 [&](int, int, int, int64_t q) { return ldfc<COH>(yl + q); });
       stage_put(S, fs);
     }
-    stage_coarse(Cs, xc, m1, m2, m3);
+    stage_coarse<CT, COH>(Cs, xc, t, m1, m2, m3);
     __syncthreads();
     // the fine tile: up(x_{l+1}) (with swap: c0 y_l + c1 up(x_{l+1})); 0 outside the grid
     const int v = threadIdx.x % NVR;
@@ -1209,10 +1312,10 @@ __device__ __forceinline__ void post_fused_body(const CoefArgs<KT> &C, const CT 
   }
   __syncthreads();
   if constexpr (TMA) {
-    if (!tma_tile_wait(bar, err)) return;
+    if (!tma_tile_wait(tw, err)) return;
   }
   float accs[TX][8];
-  tile_apply<KT, CLS, TMA ? 3 : 0>(S, smc, C, rwd, tb, n1, n2, n3, accs);
+  tile_apply<KT, CLS, TMA ? 3 : 0>(S, smc, C, rwd, tb, t, n1, n2, n3, accs);
   const int tz = run_tz(threadIdx.x), ty = run_ty(threadIdx.x);
   const int k0 = z0 + tz * 8, j = y0 + ty;
   if (k0 >= n3 || j >= n2) return;
@@ -1225,7 +1328,7 @@ __device__ __forceinline__ void post_fused_body(const CoefArgs<KT> &C, const CT 
     apply_run_mask(bw[tx], acc);
     if (!SWAP) {
       float yv[8];
-      ld8(yl + q, yv);
+      ld8c<COH>(yl + q, yv);
 #pragma unroll
       for (int c = 0; c < 8; ++c) acc[c] = __fadd_rn(__fmul_rn(c0, yv[c]), __fmul_rn(c1, acc[c]));
     }
@@ -1242,7 +1345,7 @@ k_post_fused(const CoefArgs<KT> C, const CT *__restrict__ xc, const YT *__restri
              const int *__restrict__ gate) {
   if (gate && *gate != 0) return;
   post_fused_body<KT, CT, YT, OT, SWAP, CLS, UPIN, false>(C, xc, yl, c0p, c1p, out, bmask, omask, n1, n2, n3,
-                                                          nullptr, nullptr);
+                                                          nullptr, nullptr, grid_tile());
 }
 
 // the post-block on an FP32 prolongated input u loaded by TMA through tmap
@@ -1254,7 +1357,72 @@ k_post_fused_tma(const CoefArgs<KT> C, const __grid_constant__ CUtensorMap tmap,
                  const int *__restrict__ gate, int *__restrict__ err) {
   if (gate && *gate != 0) return;
   post_fused_body<KT, float, YT, OT, SWAP, CLS, true, true>(C, nullptr, yl, c0p, c1p, out, bmask, omask, n1, n2,
-                                                            n3, &tmap, err);
+                                                            n3, &tmap, err, grid_tile());
+}
+
+// ---------------------------------------------------------------------------
+// The coarse levels of one application in one launch: one thread-block
+// cluster (16 CTAs, or 8 where 16 are not available) runs the pre-blocks of
+// levels lc .. L-1, the coarsest block and the post-blocks of levels L-1 .. lc
+// (sm_model_3d.py:204-260 from level lc on) as stages separated by cluster
+// barriers.  In a stage, CTA r takes the level's tiles r, r + 16, ... through
+// the same bodies as the per-level kernels, so every value is computed by the
+// same arithmetic; activations written by one stage are read by the next
+// through L2 (the bodies' COH loads).  These levels hold at most a few tens
+// of tiles each, so as separate kernels they cost a launch and one CTA's
+// load -> compute chain apiece; here the chains follow each other inside one
+// launch.  Only the SmallSMModelDn3D kind (SM) uses it.
+// ---------------------------------------------------------------------------
+constexpr int kCoarseMaxLev = 6;
+template <typename KT, typename AT>
+struct CoarseArgs {
+  int nlev;                              // levels lc .. L (index i: level lc + i)
+  int n1[kCoarseMaxLev], n2[kCoarseMaxLev], n3[kCoarseMaxLev];
+  int tz[kCoarseMaxLev], ty[kCoarseMaxLev];  // tiles along z and y
+  unsigned ntiles[kCoarseMaxLev];
+  CoefArgs<KT> pre[kCoarseMaxLev];       // pre-blocks; pre[nlev - 1]: the coarsest block
+  CoefArgs<KT> post[kCoarseMaxLev];      // post-blocks of levels lc .. L-1
+  AT *x[kCoarseMaxLev];                  // pre-block inputs; x[0] written by the previous kernel
+  AT *y[kCoarseMaxLev];                  // pre-block outputs
+  AT *xo[kCoarseMaxLev];                 // post-block outputs; xo[nlev - 1]: the coarsest block's
+  const float *c0[kCoarseMaxLev], *c1[kCoarseMaxLev];
+};
+
+__device__ __forceinline__ Tile tile_of(unsigned id, int tz, int ty) {
+  return Tile{(int)(id % (unsigned)tz), (int)((id / (unsigned)tz) % (unsigned)ty), (int)(id / (unsigned)(tz * ty)),
+              id};
+}
+
+// all threads of the cluster: the stage's global writes become visible to the next stage's reads
+__device__ __forceinline__ void cluster_stage_barrier() {
+  __threadfence();
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+template <typename KT, typename AT, bool CLS, bool SWAP>
+__global__ void __launch_bounds__(PT)
+k_coarse_cluster(const __grid_constant__ CoarseArgs<KT, AT> A, const int *__restrict__ gate) {
+  if (gate && *gate != 0) return;  // read alike by every CTA: the whole cluster leaves
+  const unsigned r = blockIdx.x, nc = gridDim.x;
+  for (int i = 0; i < A.nlev; ++i) {
+    const bool last = i == A.nlev - 1;
+    for (unsigned id = r; id < A.ntiles[i]; id += nc) {
+      pre_fused_body<KT, AT, AT, true, CLS, false, true>(A.pre[i], A.x[i], nullptr, last ? A.xo[i] : A.y[i],
+                                                        last ? nullptr : A.x[i + 1], nullptr, A.n1[i], A.n2[i],
+                                                        A.n3[i], nullptr, nullptr, tile_of(id, A.tz[i], A.ty[i]));
+      __syncthreads();  // the next tile restages the shared tile
+    }
+    cluster_stage_barrier();
+  }
+  for (int i = A.nlev - 2; i >= 0; --i) {
+    for (unsigned id = r; id < A.ntiles[i]; id += nc) {
+      post_fused_body<KT, AT, AT, AT, SWAP, CLS, false, false, true>(
+          A.post[i], A.xo[i + 1], A.y[i], A.c0[i], A.c1[i], A.xo[i], nullptr, nullptr, A.n1[i], A.n2[i], A.n3[i],
+          nullptr, nullptr, tile_of(id, A.tz[i], A.ty[i]));
+      __syncthreads();
+    }
+    if (i > 0) cluster_stage_barrier();
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1320,6 +1488,11 @@ struct PrecondPlan {
   void *ufine = nullptr;      // level-0 prolongated post-block input
   uint32_t *glist = nullptr;  // general-cell list (setup scratch)
   uint32_t *rlist = nullptr;  // mixed-run list (setup scratch)
+  uint32_t *glist2 = nullptr, *rlist2 = nullptr;  // the same for levels >= 1 (SM kind, side stream)
+  // setup: level 0's coefficient chain runs on the caller's stream, levels >= 1 and the linear
+  // blocks on this stream beside it (forked and joined with the two events)
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   std::vector<void *> Kpre, Kpost;   // dense planes, or mixed-run records on classed levels
   void *Kl = nullptr;
   std::vector<float *> Upre, Upost;  // classed levels: 3 x KREC uniform vectors per block
@@ -1344,6 +1517,7 @@ struct PrecondPlan {
   void *lin_ws = nullptr;
   float *scratch = nullptr;   // 81 floats (linear means)
   int *err = nullptr;         // set to 1 by a level-0 TMA tile copy that did not complete
+  bool coarse_cluster = true; // SM kind: the coarse levels in one cluster launch where the device allows
   size_t bytes = 0;
   bool ready = false;
 };
@@ -1438,7 +1612,7 @@ static size_t plan_layout(PrecondPlan &P, char *base) {
   }
   P.Uall = U;
   P.Mrec = take((size_t)nU * 3 * RREC * sk);
-  int64_t nlist = 0;
+  int64_t nlist = 0, nlist2 = 0;
   for (int l = 0; l <= P.L; ++l) {
     const auto &v = P.lv[l];
     if (!v.cls) continue;
@@ -1449,6 +1623,7 @@ static size_t plan_layout(PrecondPlan &P, char *base) {
     P.gcount[l] = (uint32_t *)take(v.ntiles * sizeof(uint32_t));
     P.gbase[l] = (uint32_t *)take(v.ntiles * sizeof(uint32_t));
     nlist = std::max<int64_t>(nlist, v.n);
+    if (l >= 1) nlist2 = std::max<int64_t>(nlist2, v.n);
   }
   P.clsT.assign(P.L + 1, nullptr);
   P.rwT.assign(P.L + 1, nullptr);
@@ -1469,6 +1644,10 @@ static size_t plan_layout(PrecondPlan &P, char *base) {
   // general-cell and mixed-run lists of one level at a time (setup only)
   P.glist = nlist ? (uint32_t *)take((size_t)nlist * sizeof(uint32_t)) : nullptr;
   P.rlist = nlist ? (uint32_t *)take((size_t)(nlist / 8 + 1) * sizeof(uint32_t)) : nullptr;
+  // the lists of levels >= 1 (SmallSMModelDn3D kind), built on the side stream beside level 0's
+  const bool par = P.kind == MLPCG_PRECOND_SM && nlist2 > 0;
+  P.glist2 = par ? (uint32_t *)take((size_t)nlist2 * sizeof(uint32_t)) : nullptr;
+  P.rlist2 = par ? (uint32_t *)take((size_t)(nlist2 / 8 + 1) * sizeof(uint32_t)) : nullptr;
   for (int l = 0; l < P.L; ++l) P.y[l] = take(P.lv[l].ps * sa);
   for (int l = 1; l <= P.L; ++l) {
     P.xin[l] = take(P.lv[l].ps * sa);
@@ -1482,7 +1661,7 @@ static size_t plan_layout(PrecondPlan &P, char *base) {
   P.coef = (float *)take(2 * P.L * sizeof(float));
   P.fmask = (uint8_t *)take(P.lv[0].ps + 64);
   P.lin_ws = take(linear_workspace());
-  P.err = (int *)take(sizeof(int));
+  P.err = (int *)take(2 * sizeof(int));  // [0]: a tile copy did not complete, [1]: copy-stall test knob
   // scratch last: the general path's temporaries (sized in the plan's byte count) follow it
   P.scratch = (float *)take(96 * sizeof(float));
   // scratch for the general path: level-0 scaled input and one activation-sized temp
@@ -1494,7 +1673,14 @@ static size_t plan_layout(PrecondPlan &P, char *base) {
 using namespace mlpcg;
 
 typedef struct mlpcg_precond mlpcg_precond;
-struct mlpcg_precond { PrecondPlan p; };
+struct mlpcg_precond {
+  PrecondPlan p;
+  ~mlpcg_precond() {
+    if (p.side) cudaStreamDestroy(p.side);
+    if (p.fork_ev) cudaEventDestroy(p.fork_ev);
+    if (p.join_ev) cudaEventDestroy(p.join_ev);
+  }
+};
 
 #define RET_IF(expr) do { int _r = (expr); if (_r != MLPCG_OK) return _r; } while (0)
 
@@ -1768,16 +1954,122 @@ static int run_apply_spd(const PrecondPlan &P, const float *r, const float *rsca
 
 // Stages of one application, in launch order: 0..L-1 = pre-block of level s,
 // L = coarsest block, L+1..2L = post-block of level 2L-s.  [s0, s1] selects a range.
+// CTAs of the coarse-level cluster kernel this device runs as one cluster: 16 (non-portable
+// size) or 8, 0 if neither (the per-level kernels are used then).  Looked up once per
+// instantiation.
+template <typename KT, typename AT, bool CLS, bool SWAP>
+static int coarse_cluster_ctas() {
+  static const int ctas = [] {
+    auto kern = k_coarse_cluster<KT, AT, CLS, SWAP>;
+    for (int c : {16, 8}) {
+      if (c > 8 && cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+        (void)cudaGetLastError();
+        continue;
+      }
+      cudaLaunchConfig_t cfg{};
+      cfg.gridDim = dim3((unsigned)c);
+      cfg.blockDim = dim3(PT);
+      cudaLaunchAttribute at{};
+      at.id = cudaLaunchAttributeClusterDimension;
+      at.val.clusterDim.x = (unsigned)c;
+      at.val.clusterDim.y = 1;
+      at.val.clusterDim.z = 1;
+      cfg.attrs = &at;
+      cfg.numAttrs = 1;
+      int n = 0;
+      if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) == cudaSuccess && n >= 1) return c;
+      (void)cudaGetLastError();
+    }
+    return 0;
+  }();
+  return ctas;
+}
+
+// The first level of the coarse-level cluster kernel for a SmallSMModelDn3D plan: the smallest
+// l >= 1 from which every level down to the coarsest runs the tiled kernels in one coefficient
+// layout, with at most 4 tiles per CTA at level l; -1 when no two levels qualify.
+static int coarse_cluster_level(const PrecondPlan &P, int ctas) {
+  if (P.kind != MLPCG_PRECOND_SM || ctas <= 0) return -1;
+  const int L = P.L;
+  int lc = -1;
+  for (int l = L - 1; l >= 1 && L - l + 1 <= kCoarseMaxLev; --l) {
+    bool ok = true;
+    for (int m = l; m <= L; ++m) ok = ok && P.lv[m].fast && P.lv[m].cls == P.lv[L].cls;
+    if (!ok || P.lv[l].ntiles > (unsigned)(4 * ctas)) break;
+    lc = l;
+  }
+  return lc;
+}
+
+template <typename KT, typename AT, bool CLS, bool SWAP>
+static int launch_coarse_cluster(const PrecondPlan &P, int lc, int ctas, cudaStream_t st, const int *gate) {
+  const int L = P.L;
+  CoarseArgs<KT, AT> A{};
+  A.nlev = L - lc + 1;
+  for (int i = 0; i < A.nlev; ++i) {
+    const int l = lc + i;
+    const auto &v = P.lv[l];
+    const dim3 g = grid_of(v);
+    A.n1[i] = v.n1; A.n2[i] = v.n2; A.n3[i] = v.n3;
+    A.tz[i] = (int)g.x; A.ty[i] = (int)g.y;
+    A.ntiles[i] = v.ntiles;
+    A.x[i] = (AT *)P.xin[l];
+    A.xo[i] = (AT *)P.xout[l];
+    if (l < L) {
+      A.pre[i] = coef_args<KT>(P, l, P.Kpre[l], CLS ? P.Upre[l] : nullptr);
+      A.post[i] = coef_args<KT>(P, l, P.Kpost[l], CLS ? P.Upost[l] : nullptr);
+      A.y[i] = (AT *)P.y[l];
+      A.c0[i] = P.coef + l;
+      A.c1[i] = P.coef + L + l;
+    } else {
+      A.pre[i] = coef_args<KT>(P, L, P.Kl, CLS ? P.Ul : nullptr);
+    }
+  }
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3((unsigned)ctas);
+  cfg.blockDim = dim3(PT);
+  cfg.stream = st;
+  cudaLaunchAttribute at{};
+  at.id = cudaLaunchAttributeClusterDimension;
+  at.val.clusterDim.x = (unsigned)ctas;
+  at.val.clusterDim.y = 1;
+  at.val.clusterDim.z = 1;
+  cfg.attrs = &at;
+  cfg.numAttrs = 1;
+  MLPCG_CUDA_CHECK(cudaLaunchKernelEx(&cfg, k_coarse_cluster<KT, AT, CLS, SWAP>, A, gate));
+  return MLPCG_OK;
+}
+
+template <typename KT, typename AT>
+static int run_coarse_cluster(const PrecondPlan &P, int lc, int ctas, cudaStream_t st, const int *gate) {
+  const bool cls = P.lv[P.L].cls;
+  if (P.swap) return cls ? launch_coarse_cluster<KT, AT, true, true>(P, lc, ctas, st, gate)
+                         : launch_coarse_cluster<KT, AT, false, true>(P, lc, ctas, st, gate);
+  return cls ? launch_coarse_cluster<KT, AT, true, false>(P, lc, ctas, st, gate)
+             : launch_coarse_cluster<KT, AT, false, false>(P, lc, ctas, st, gate);
+}
+
+template <typename KT, typename AT>
+static int cluster_ctas_for(const PrecondPlan &P) {
+  const bool cls = P.lv[P.L].cls;
+  if (P.swap) return cls ? coarse_cluster_ctas<KT, AT, true, true>() : coarse_cluster_ctas<KT, AT, false, true>();
+  return cls ? coarse_cluster_ctas<KT, AT, true, false>() : coarse_cluster_ctas<KT, AT, false, false>();
+}
+
 template <typename KT, typename AT>
 static int run_apply(const PrecondPlan &P, const float *r, const float *rscale, float *z, void *tmp0,
                      cudaStream_t st, int s0 = 0, int s1 = 1 << 20, const int *gate = nullptr) {
   if (P.kind == MLPCG_PRECOND_SPD) return run_apply_spd<KT, AT>(P, r, rscale, z, tmp0, st, s0, s1, gate);
   const int L = P.L;
   const uint8_t *m0 = P.mask ? P.fmask : nullptr;
+  // levels lc .. L in one cluster launch when the range covers all of their stages
+  const int ctas = P.kind == MLPCG_PRECOND_SM && P.coarse_cluster ? cluster_ctas_for<KT, AT>(P) : 0;
+  const int lc = coarse_cluster_level(P, ctas);
+  const bool cluster = lc > 0 && s0 <= lc && s1 >= 2 * L - lc;
   // ---- down sweep
   for (int l = 0; l < L; ++l) {
     const auto &v = P.lv[l];
-    if (l < s0 || l > s1) continue;
+    if (l < s0 || l > s1 || (cluster && l >= lc)) continue;
     if (v.fast) {
       const CoefArgs<KT> C = coef_args<KT>(P, l, P.Kpre[l], v.cls ? P.Upre[l] : nullptr);
       if (l == 0) {
@@ -1807,9 +2099,10 @@ static int run_apply(const PrecondPlan &P, const float *r, const float *rscale, 
       RET_IF(launch_avg_pool2(P.y[l], P.xin[l + 1], P.adt, 1, v.n1, v.n2, v.n3, st));
     }
   }
+  if (cluster) RET_IF((run_coarse_cluster<KT, AT>(P, lc, ctas, st, gate)));
   // ---- coarsest block (SPD kind: l into xtmp, then l_t)
   const bool spd = P.kind == MLPCG_PRECOND_SMALL_SPD;
-  if (L >= s0 && L <= s1) {
+  if (L >= s0 && L <= s1 && !cluster) {
     const auto &v = P.lv[L];
     AT *cdst = (AT *)(spd ? P.xtmp : P.xout[L]);
     if (v.fast) {
@@ -1840,7 +2133,7 @@ static int run_apply(const PrecondPlan &P, const float *r, const float *rscale, 
   // ---- up sweep
   for (int l = L - 1; l >= 0; --l) {
     const auto &v = P.lv[l];
-    if (2 * L - l < s0 || 2 * L - l > s1) continue;
+    if (2 * L - l < s0 || 2 * L - l > s1 || (cluster && l >= lc)) continue;
     const float *c0 = P.coef + l, *c1 = P.coef + L + l;
     const uint8_t *bm = (l == 0) ? m0 : nullptr;
     const uint8_t *om = (l == 0) ? P.fmask : nullptr;
@@ -1945,6 +2238,9 @@ static int run_apply(const PrecondPlan &P, const float *r, const float *rscale, 
 }
 
 namespace mlpcg {
+// the plan's copy-failed word (device memory; valid once the plan is set up)
+const int *precond_copy_flag(const mlpcg_precond *h) { return h->p.ready ? h->p.err : nullptr; }
+
 // mlpcg_precond_apply whose fused kernels return at once while *gate != 0
 // (the batched solver passes each system's status word)
 int precond_apply_gated(const mlpcg_precond *h, const float *r, const float *r_scale, float *z, const int *gate,
@@ -2039,7 +2335,7 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
   MLPCG_REQUIRE(((uintptr_t)workspace & 255) == 0, MLPCG_ERR_ALIGN, "precond workspace must be 256-byte aligned");
   cudaStream_t st = as_stream(stream);
   plan_layout(P, (char *)workspace);
-  MLPCG_CUDA_CHECK(cudaMemsetAsync(P.err, 0, sizeof(int), st));
+  MLPCG_CUDA_CHECK(cudaMemsetAsync(P.err, 0, 2 * sizeof(int), st));
   const int L = P.L;
   // parameter offsets: pre[0..L-1], post[0..L-1], l (2214 each), c0[0..L-1], c1[0..L-1] (82 each);
   // SPD kind: l0[0..L-1], l, then the linear blocks
@@ -2071,23 +2367,40 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
   }
   // one level's blocks b0 (and b1 >= 0): dense planes, or class map + general-cell records;
   // their uniform vectors in slots u0s (and u1s), by default the block indices
+  // c0 / c1 of every level (the linear blocks of sm_model_3d.py:236-239), on stream ls
+  auto setup_linear = [&](cudaStream_t ls) -> int {
+    for (int l = 0; l < L; ++l) {
+      const auto &v = P.lv[l];
+      const float *im = (l == 0) ? image : P.img[l];
+      // c0[l] and c1[l] in one pass over the level image: their weights are L*82 floats apart
+      const float *w0 = linp + (size_t)l * 82;
+      RET_IF(launch_linear_forward_strided(im, v.n1, v.n2, v.n3, w0, (int64_t)L * 82, w0 + 81, (int64_t)L * 82, 2,
+                                           P.coef + l, L, nullptr, P.lin_ws, linear_workspace(), ls));
+    }
+    return MLPCG_OK;
+  };
+  bool linear_done = false;
+  // gen_level enqueues on gs with the list scratch gl / rl (level 0: the caller's stream and the
+  // first lists; the SM kind's levels >= 1: the side stream and the second lists)
+  cudaStream_t gs = st;
+  uint32_t *gl = P.glist, *rl = P.rlist;
   auto gen_level = [&](int l, const float *im, int b0, void *K0, int b1, void *K1, int u0s = -1,
                        int u1s = -1) -> int {
     const auto &v = P.lv[l];
     if (!v.cls) {
-      RET_IF(launch_stencil_gen(im, 0, v.n1, v.n2, v.n3, blk_w(b0), blk_b(b0), K0, P.kdt, v.ps, st));
-      if (b1 >= 0) RET_IF(launch_stencil_gen(im, 0, v.n1, v.n2, v.n3, blk_w(b1), blk_b(b1), K1, P.kdt, v.ps, st));
+      RET_IF(launch_stencil_gen(im, 0, v.n1, v.n2, v.n3, blk_w(b0), blk_b(b0), K0, P.kdt, v.ps, gs));
+      if (b1 >= 0) RET_IF(launch_stencil_gen(im, 0, v.n1, v.n2, v.n3, blk_w(b1), blk_b(b1), K1, P.kdt, v.ps, gs));
       return MLPCG_OK;
     }
-    k_classify<false><<<grid_of(v), PT, 0, st>>>(im, nullptr, v.n1, v.n2, v.n3, P.cls[l], P.rw[l], P.rcount[l],
+    k_classify<false><<<grid_of(v), PT, 0, gs>>>(im, nullptr, v.n1, v.n2, v.n3, P.cls[l], P.rw[l], P.rcount[l],
                                                  P.gcount[l]);
     MLPCG_LAUNCH_CHECK();
-    k_scan_tiles<<<1, 1024, 0, st>>>(P.rcount[l], P.rbase[l], (int)v.ntiles);
+    k_scan_tiles<<<1, 1024, 0, gs>>>(P.rcount[l], P.rbase[l], (int)v.ntiles);
     MLPCG_LAUNCH_CHECK();
-    k_scan_tiles<<<1, 1024, 0, st>>>(P.gcount[l], P.gbase[l], (int)v.ntiles);
+    k_scan_tiles<<<1, 1024, 0, gs>>>(P.gcount[l], P.gbase[l], (int)v.ntiles);
     MLPCG_LAUNCH_CHECK();
-    k_list_general<<<grid_of(v), PT, 0, st>>>(P.cls[l], v.n1, v.n2, v.n3, P.gbase[l], P.glist, P.rw[l], P.rbase[l],
-                                              P.rlist);
+    k_list_general<<<grid_of(v), PT, 0, gs>>>(P.cls[l], v.n1, v.n2, v.n3, P.gbase[l], gl, P.rw[l], P.rbase[l],
+                                              rl);
     MLPCG_LAUNCH_CHECK();
     // general cells: one wave of CTAs (as many as fit on every SM), each looping over its share
     const uint32_t *lb = P.gbase[l] + v.ntiles - 1, *lc = P.gcount[l] + v.ntiles - 1;
@@ -2099,9 +2412,9 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
     auto launch = [&](auto kern, auto fill, const void *r0, const void *r1) {
       using KT = typename std::remove_pointer<decltype(kgen_rec_type(kern))>::type;
       const int grid = (int)std::min<int64_t>((int64_t)sm_count() * resident_ctas(kern), (v.n + PT - 1) / PT);
-      kern<<<grid, PT, 0, st>>>(im, v.n1, v.n2, v.n3, params, b0, b1 >= 0 ? b1 : b0, P.glist, lb, lc, P.rw[l],
+      kern<<<grid, PT, 0, gs>>>(im, v.n1, v.n2, v.n3, params, b0, b1 >= 0 ? b1 : b0, gl, lb, lc, P.rw[l],
                                 P.rbase[l], P.rcount[l], (KT *)r0, (KT *)r1);
-      fill<<<fgrid, 256, 0, st>>>(P.cls[l], P.rlist, rlb, rlc, P.rw[l], P.rbase[l], P.rcount[l], v.n1, v.n2, v.n3, u0,
+      fill<<<fgrid, 256, 0, gs>>>(P.cls[l], rl, rlb, rlc, P.rw[l], P.rbase[l], P.rcount[l], v.n1, v.n2, v.n3, u0,
                                   u1, (KT *)r0, (KT *)r1);
     };
     if (P.kdt == MLPCG_BF16) {
@@ -2177,6 +2490,28 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
     RET_IF(gen_level(L, P.img[L], L, P.Kl, -1, nullptr, 2 * L));
     RET_IF(classify_t(L));
     RET_IF(gather_t(L, P.Kl, 2 * L, P.Klt, 2 * L + 1));
+  } else if (P.kind == MLPCG_PRECOND_SM && P.glist2) {
+    // levels >= 1 and then every level's c0 / c1 on the side stream, level 0 on the caller's
+    if (!P.side) {
+      MLPCG_CUDA_CHECK(cudaStreamCreateWithFlags(&P.side, cudaStreamNonBlocking));
+      MLPCG_CUDA_CHECK(cudaEventCreateWithFlags(&P.fork_ev, cudaEventDisableTiming));
+      MLPCG_CUDA_CHECK(cudaEventCreateWithFlags(&P.join_ev, cudaEventDisableTiming));
+    }
+    MLPCG_CUDA_CHECK(cudaEventRecord(P.fork_ev, st));
+    MLPCG_CUDA_CHECK(cudaStreamWaitEvent(P.side, P.fork_ev, 0));
+    gs = P.side;
+    gl = P.glist2;
+    rl = P.rlist2;
+    for (int l = 1; l < L; ++l) RET_IF(gen_level(l, P.img[l], l, P.Kpre[l], L + l, P.Kpost[l]));
+    RET_IF(gen_level(L, P.img[L], 2 * L, P.Kl, -1, nullptr));
+    RET_IF(setup_linear(P.side));
+    MLPCG_CUDA_CHECK(cudaEventRecord(P.join_ev, P.side));
+    gs = st;
+    gl = P.glist;
+    rl = P.rlist;
+    RET_IF(gen_level(0, image, 0, P.Kpre[0], L, P.Kpost[0]));
+    MLPCG_CUDA_CHECK(cudaStreamWaitEvent(st, P.join_ev, 0));
+    linear_done = true;
   } else {
     for (int l = 0; l < L; ++l) RET_IF(gen_level(l, (l == 0) ? image : P.img[l], l, P.Kpre[l], L + l, P.Kpost[l]));
     RET_IF(gen_level(L, P.img[L], 2 * L, P.Kl, -1, nullptr));
@@ -2191,15 +2526,7 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
       RET_IF(gather_t(L, P.Kl, 2 * L, P.Klt, 4 * L + 1));
     }
   }
-  // c0 / c1 of every level (the linear blocks of sm_model_3d.py:236-239)
-  for (int l = 0; l < L; ++l) {
-    const auto &v = P.lv[l];
-    const float *im = (l == 0) ? image : P.img[l];
-    // c0[l] and c1[l] in one pass over the level image: their weights are L*82 floats apart
-    const float *w0 = linp + (size_t)l * 82;
-    RET_IF(launch_linear_forward_strided(im, v.n1, v.n2, v.n3, w0, (int64_t)L * 82, w0 + 81, (int64_t)L * 82, 2,
-                                         P.coef + l, L, nullptr, P.lin_ws, linear_workspace(), st));
-  }
+  if (!linear_done) RET_IF(setup_linear(st));
   if (spd) {
     k_square<<<1, 64, 0, st>>>(P.coef, 2 * L);
     MLPCG_LAUNCH_CHECK();
@@ -2293,6 +2620,32 @@ int mlpcg_precond_check(const mlpcg_precond *h, int *copy_failed, void *stream) 
   MLPCG_CUDA_CHECK(cudaMemcpyAsync(&v, h->p.err, sizeof(int), cudaMemcpyDeviceToHost, st));
   MLPCG_CUDA_CHECK(cudaStreamSynchronize(st));
   *copy_failed = v;
+  return MLPCG_OK;
+}
+
+int mlpcg_precond_coarse_cluster(const mlpcg_precond *h, int *first_level, int *ctas) {
+  clear_error();
+  MLPCG_REQUIRE(h && first_level, MLPCG_ERR_ARG, "precond_coarse_cluster: NULL argument");
+  const PrecondPlan &P = h->p;
+  int c = 0;
+  if (P.kind == MLPCG_PRECOND_SM && P.coarse_cluster) {
+    if (P.kdt == MLPCG_BF16 && P.adt == MLPCG_BF16) c = cluster_ctas_for<__nv_bfloat16, __nv_bfloat16>(P);
+    else if (P.kdt == MLPCG_BF16) c = cluster_ctas_for<__nv_bfloat16, float>(P);
+    else if (P.adt == MLPCG_BF16) c = cluster_ctas_for<float, __nv_bfloat16>(P);
+    else c = cluster_ctas_for<float, float>(P);
+  }
+  *first_level = coarse_cluster_level(P, c);
+  if (ctas) *ctas = *first_level > 0 ? c : 0;
+  return MLPCG_OK;
+}
+
+int mlpcg_precond_set_copy_stall(mlpcg_precond *h, int on, void *stream) {
+  clear_error();
+  MLPCG_REQUIRE(h && h->p.ready, MLPCG_ERR_ARG, "precond_set_copy_stall: plan not set up");
+  // clears the copy-failed word and sets (any non-zero byte pattern) or clears the knob
+  cudaStream_t st = as_stream(stream);
+  MLPCG_CUDA_CHECK(cudaMemsetAsync(h->p.err, 0, sizeof(int), st));
+  MLPCG_CUDA_CHECK(cudaMemsetAsync(h->p.err + 1, on ? 1 : 0, sizeof(int), st));
   return MLPCG_OK;
 }
 

@@ -32,6 +32,7 @@
 struct mlpcg_precond;
 namespace mlpcg {
 int precond_apply_gated(const mlpcg_precond *, const float *, const float *, float *, const int *, void *);
+const int *precond_copy_flag(const mlpcg_precond *);
 bool encode_grid_map(CUtensorMap *m, const float *base, int n1, int n2, int n3, int box_z, int box_y, int box_x);
 }
 
@@ -59,6 +60,7 @@ struct State {
   // true residual and the final conversion; d_k stays in its buffer slot pend_buf until then
   int pend, pend_buf;
   float pend_hi, pend_lo;
+  int stall_copies;                   // copy-stall test knob: the SpMV's first tile wait runs out
   unsigned ticket[4];
 };
 
@@ -81,6 +83,8 @@ struct Vecs {
   double *part;    // NRED * RB_MAX partial sums
   double *hist;    // max_it + 1 relative residuals
   State *st;
+  const int *perr; // the preconditioner plan's copy-failed word (its level-0 TMA tiles)
+  int zero_guess;  // x0 = 0: k_prepare does not read x, k_finalize writes every cell (0 off the fluid)
   int n1, n2, n3;
   int64_t n;
   int nblk;
@@ -310,13 +314,14 @@ __device__ __forceinline__ void group_coords(const Vecs &V, uint32_t g, uint32_t
 // ---------------------------------------------------------------------------
 // setup: state reset, then r = b - A x (FP64), bb = b.b, rr = r.r
 // ---------------------------------------------------------------------------
-__global__ void k_reset(State *st, int max_it, int true_every, int method, double tol) {
+__global__ void k_reset(State *st, int max_it, int true_every, int method, double tol, int stall_copies) {
   if (threadIdx.x != 0) return;
   State S{};
   S.max_it = max_it;
   S.true_every = true_every;
   S.method = method;
   S.tol = tol;
+  S.stall_copies = stall_copies;
   *st = S;
 }
 
@@ -340,8 +345,8 @@ __global__ void __launch_bounds__(RT) k_prepare(Vecs V) {
       cd[c] = lane(N.fc, c) == MLPCG_FLUID ? (uint8_t)d : kNotFluid;
     }
     *reinterpret_cast<uchar4 *>(V.code + q) = make_uchar4(cd[0], cd[1], cd[2], cd[3]);
-    double xq[4], bq[4];
-    ld4(V.x + q, xq);
+    double xq[4] = {0.0, 0.0, 0.0, 0.0}, bq[4];
+    if (!V.zero_guess) ld4(V.x + q, xq);
     ld4(V.b + q, bq);
     float2 xd[4], bd[4];
 #pragma unroll
@@ -439,6 +444,13 @@ __global__ void __launch_bounds__(RT) k_finalize(Vecs V) {
       double2 *o = reinterpret_cast<double2 *>(V.x + q);
       o[0] = make_double2(df_to_double_bits(xd[0]), df_to_double_bits(xd[1]));
       o[1] = make_double2(df_to_double_bits(xd[2]), df_to_double_bits(xd[3]));
+    } else if (V.zero_guess) {  // x was not read: every cell is written, 0 off the fluid
+      double v[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) v[c] = (lane(cd, c) & kNotFluid) ? 0.0 : df_to_double_bits(xd[c]);
+      double2 *o = reinterpret_cast<double2 *>(V.x + q);
+      o[0] = make_double2(v[0], v[1]);
+      o[1] = make_double2(v[2], v[3]);
     } else {
 #pragma unroll
       for (int c = 0; c < 4; ++c)
@@ -622,6 +634,7 @@ __global__ void __launch_bounds__(RT, 3) k_sd_spmv_tma(Vecs V, const __grid_cons
   if (S.status != ST_RUNNING) return;
   __shared__ __align__(128) float T[SBX][SBY][SBZ];
   __shared__ __align__(8) uint64_t mbar;
+  __shared__ __align__(8) uint64_t never;  // nothing arrives on it: the copy-stall test waits here
   __shared__ int copy_failed;
   const int h = S.head, hn = (h + 1) % 3;
   const CUtensorMap *tm = hn == 0 ? &tq0 : (hn == 1 ? &tq1 : &tq2);
@@ -632,9 +645,12 @@ __global__ void __launch_bounds__(RT, 3) k_sd_spmv_tma(Vecs V, const __grid_cons
   const int tiles_z = (n3 + SPZ - 1) / SPZ, tiles_y = (n2 + SPY - 1) / SPY, tiles_x = (n1 + SPX - 1) / SPX;
   const int ntiles = tiles_z * tiles_y * tiles_x;
   const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&mbar);
+  const uint32_t nbar = (uint32_t)__cvta_generic_to_shared(&never);
+  const bool stall = S.stall_copies != 0;
   if (threadIdx.x == 0) {
     copy_failed = 0;
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(nbar) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
@@ -675,11 +691,14 @@ __global__ void __launch_bounds__(RT, 3) k_sd_spmv_tma(Vecs V, const __grid_cons
         }
       }
     }
-    // bounded wait for the box (phase `phase`); a copy that never lands stops the solve
+    // bounded wait for the box (phase `phase`); a copy that never lands stops the solve.  With the
+    // copy-stall knob the first wait polls the barrier nothing arrives on (256 tries), so it runs
+    // out while the real copy completes; the second wait then lets that copy land
     uint32_t done = 0;
-    for (uint32_t it = 0; it < (1u << 22) && !done; ++it)
+    const uint32_t wbar = stall ? nbar : bar, lim = stall ? 256u : (1u << 22);
+    for (uint32_t it = 0; it < lim && !done; ++it)
       asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
-                   : "=r"(done) : "r"(bar), "r"(phase) : "memory");
+                   : "=r"(done) : "r"(wbar), "r"(stall ? 0u : phase) : "memory");
     if (!done) {
       copy_failed = 1;
       for (uint32_t it = 0; it < (1u << 22) && !done; ++it)  // let a late copy land before leaving
@@ -917,6 +936,10 @@ __global__ void k_control(Vecs V, cudaGraphConditionalHandle handle, int use_han
     if (S.status == ST_RUNNING && itn >= S.max_it) S.status = ST_MAXIT;
     S.rscale = (S.rr > 0.0) ? (float)(1.0 / sqrt((double)(float)S.rr)) : 1.f;
   }
+  // a preconditioner tile copy that did not complete left z invalid: that, not the breakdown or
+  // non-finite value it may have caused, ends the solve (a converged or max_it result stands, its
+  // residual being the true one)
+  if (V.perr && *V.perr && S.status != ST_CONVERGED && S.status != ST_MAXIT) S.status = ST_COPYFAIL;
   if (use_handle) cudaGraphSetConditional(handle, S.status == ST_RUNNING ? 1u : 0u);
 }
 
@@ -949,6 +972,7 @@ struct mlpcg_solver {
   cudaGraphExec_t exec = nullptr;
   cudaStream_t capture_stream = nullptr;  // graphs are captured here, launched on the caller's stream
   int sched_blocks = 0;                    // blocks of the solver's grid-stride kernels (0: automatic)
+  int stall_copies = 0;                    // copy-stall test knob (mlpcg_solver_set_copy_stall)
   CUtensorMap qmap[3];                     // the three search-direction buffers, for the TMA SpMV
   bool qmap_ok = false;
 };
@@ -1016,7 +1040,8 @@ static void destroy_graph(mlpcg_solver *s) {
 // state reset, operator codes, b and x0 as pairs, the initial residual
 static int start_solve(mlpcg_solver *s, cudaStream_t st) {
   Vecs &V = s->V;
-  k_reset<<<1, 32, 0, st>>>(V.st, s->max_it, s->true_every, s->method, s->tol);
+  V.perr = precond_copy_flag(s->plan);
+  k_reset<<<1, 32, 0, st>>>(V.st, s->max_it, s->true_every, s->method, s->tol, s->stall_copies);
   k_prepare<<<full_grid(V), RT, 0, st>>>(V);
   k_init<<<full_grid(V), RT, 0, st>>>(V);
   MLPCG_LAUNCH_CHECK();
@@ -1111,11 +1136,9 @@ int mlpcg_solver_bind(mlpcg_solver *s, void *workspace, size_t workspace_bytes, 
 // (use_graph = 1; built on the first call and reused) or as plain launches
 // with one host check per iteration (use_graph = 0).  Asynchronous for the
 // graph; mlpcg_solver_result() synchronises.
-int mlpcg_solver_solve(mlpcg_solver *s, int use_graph, void *stream) {
-  clear_error();
-  MLPCG_REQUIRE(s && s->bound, MLPCG_ERR_ARG, "solver_solve: solver not bound");
-  cudaStream_t st = as_stream(stream);
+static int solve_impl(mlpcg_solver *s, int use_graph, int zero_guess, cudaStream_t st) {
   Vecs &V = s->V;
+  V.zero_guess = zero_guess;  // read by k_prepare and k_finalize, which run outside the graph
   if (int rc0 = start_solve(s, st)) return rc0;
   if (!use_graph) {
     for (int it = 0; it < s->max_it; ++it) {
@@ -1162,6 +1185,18 @@ int mlpcg_solver_solve(mlpcg_solver *s, int use_graph, void *stream) {
   return MLPCG_OK;
 }
 
+int mlpcg_solver_solve(mlpcg_solver *s, int use_graph, void *stream) {
+  clear_error();
+  MLPCG_REQUIRE(s && s->bound, MLPCG_ERR_ARG, "solver_solve: solver not bound");
+  return solve_impl(s, use_graph, 0, as_stream(stream));
+}
+
+int mlpcg_solver_solve_zero_guess(mlpcg_solver *s, int use_graph, void *stream) {
+  clear_error();
+  MLPCG_REQUIRE(s && s->bound, MLPCG_ERR_ARG, "solver_solve_zero_guess: solver not bound");
+  return solve_impl(s, use_graph, 1, as_stream(stream));
+}
+
 int mlpcg_solver_result(const mlpcg_solver *s, int *iters, int *status, double *rel_res, double *history,
                         void *stream) {
   clear_error();
@@ -1191,6 +1226,13 @@ int mlpcg_solver_set_schedule(mlpcg_solver *s, int blocks) {
     V.nblk = (int)(nb < 1 ? 1 : (nb > RB_MAX ? RB_MAX : nb));
     destroy_graph(s);  // recaptured with the new grid on the next solve
   }
+  return MLPCG_OK;
+}
+
+int mlpcg_solver_set_copy_stall(mlpcg_solver *s, int on) {
+  clear_error();
+  MLPCG_REQUIRE(s, MLPCG_ERR_ARG, "solver_set_copy_stall: NULL solver");
+  s->stall_copies = on ? 1 : 0;
   return MLPCG_OK;
 }
 
@@ -1242,6 +1284,7 @@ int mlpcg_batch_solve(mlpcg_batch *b, void *stream) {
   const int K = (int)b->solvers.size();
   for (auto *s : b->solvers) {
     MLPCG_REQUIRE(s->bound, MLPCG_ERR_ARG, "batch_solve: a solver is no longer bound");
+    s->V.zero_guess = 0;  // batches start from each solver's x
     if (int rc = start_solve(s, st)) return rc;
   }
   if (!b->exec) {

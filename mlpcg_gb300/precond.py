@@ -153,6 +153,19 @@ class PrecondPlan:
         call("mlpcg_precond_check", self._h, C.byref(v), _stream(self.device))
         return bool(v.value)
 
+    def coarse_cluster(self):
+        """(first level, CTAs) of the coarse levels run as one thread-block cluster launch, or (-1, 0)
+        (mlpcg_precond_coarse_cluster)."""
+        lc, c = C.c_int(), C.c_int()
+        call("mlpcg_precond_coarse_cluster", self._h, C.byref(lc), C.byref(c))
+        return lc.value, c.value
+
+    def set_copy_stall(self, on: bool):
+        """Test knob of the bounded TMA waits (mlpcg_precond_set_copy_stall): with ``on`` the level-0
+        tile kernels' first wait runs out on an ordinary copy and ``copy_failed()`` turns true; every
+        call clears the copy-failed word."""
+        call("mlpcg_precond_set_copy_stall", self._h, int(bool(on)), _stream(self.device))
+
     def class_counts_transposed(self, level: int):
         """(general cells, mixed runs) of the transposed block of a classed level (SPD plans)."""
         g, r = C.c_int64(), C.c_int64()

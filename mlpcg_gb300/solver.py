@@ -91,9 +91,10 @@ class FusedSolver:
         """Enqueue a solve (asynchronous with use_graph)."""
         if b is not None and b.data_ptr() != self.b.data_ptr():
             self.b.copy_(b.reshape(self.shape))
-        if x0 is None:
-            self.x.zero_()
-        elif x0.data_ptr() != self.x.data_ptr():
+        if x0 is None:  # x0 = 0 without a memset: the solve does not read x and writes all of it
+            call("mlpcg_solver_solve_zero_guess", self._h, int(bool(use_graph)), _stream(self.flags.device))
+            return
+        if x0.data_ptr() != self.x.data_ptr():
             self.x.copy_(x0.reshape(self.shape))
         call("mlpcg_solver_solve", self._h, int(bool(use_graph)), _stream(self.flags.device))
 
@@ -141,6 +142,11 @@ class FusedSolver:
                 x_out_h.view(-1).copy_(self._xf[:m], non_blocking=True)
             else:
                 x_out_h.view(self.shape).copy_(self.x, non_blocking=True)
+
+    def set_copy_stall(self, on: bool):
+        """Test knob of the bounded TMA waits (mlpcg_solver_set_copy_stall): from the next solve the
+        npsd SpMV's first tile wait runs out on an ordinary copy and the solve ends 'copy_failed'."""
+        call("mlpcg_solver_set_copy_stall", self._h, int(bool(on)))
 
     def result(self, with_history=True) -> SolveResult:
         it, st, rel = C.c_int(), C.c_int(), C.c_double()

@@ -136,9 +136,11 @@ def csr_cpu(flags):
     return At, torch.from_numpy(fluid)
 
 
-def npcg_iterations(model: CPUModel, img, flags, rhs, iters):
-    """``iters`` iterations of npcg (cg_tests.py:26-101: textbook PCG, the solver of a symmetric
-    network) on the CPU; returns (seconds per iteration list, rel residuals)."""
+def npcg_iterations(model: CPUModel, img, flags, rhs, iters, tol=None):
+    """Up to ``iters`` iterations of npcg (cg_tests.py:26-101: textbook PCG, the solver of a
+    symmetric network) on the CPU, stopping once the relative residual is at most ``tol`` (the
+    reference's rule with atol = 1e-20; None: run all ``iters``); returns (seconds per iteration
+    list, rel residuals)."""
     A, fluid = csr_cpu(flags)
     shape = tuple(flags.shape)
     n = int(np.prod(shape))
@@ -168,11 +170,15 @@ def npcg_iterations(model: CPUModel, img, flags, rhs, iters):
         r = b - A @ x
         hist.append(r.norm().item() / norm_b)
         times.append(time.perf_counter() - t0)
+        if tol is not None and not hist[-1] > max(tol, 1e-20 / norm_b):
+            break
     return times, hist
 
 
-def npsd_iterations(model: CPUModel, img, flags, rhs, iters):
-    """Run ``iters`` iterations of npsd on the CPU; returns (seconds per iteration list, rel residuals)."""
+def npsd_iterations(model: CPUModel, img, flags, rhs, iters, tol=None):
+    """Up to ``iters`` iterations of npsd (cg_tests.py:189-284) on the CPU, stopping once the
+    relative residual is below ``tol`` (the reference's rule with atol = 1e-20, test.py:328; None:
+    run all ``iters``); returns (seconds per iteration list, rel residuals)."""
     A, fluid = csr_cpu(flags)
     shape = tuple(flags.shape)
     n = int(np.prod(shape))
@@ -211,4 +217,6 @@ def npsd_iterations(model: CPUModel, img, flags, rhs, iters):
         r = b - A @ x
         hist.append(r.norm().item() / norm_b)
         times.append(time.perf_counter() - t0)
+        if tol is not None and hist[-1] < max(tol, 1e-20 / norm_b):
+            break
     return times, hist

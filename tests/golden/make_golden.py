@@ -280,6 +280,92 @@ def make_cg(ref_cg, model, scene, max_it=50):
     return out
 
 
+def _fluid_matrix(f, use_reference_assembly):
+    """The compressed FP64 matrix of flags f: the reference's lap_with_bc + compressedMat, or, where
+    their LIL assembly cannot run (at 64^3 it grew past 48 GB of host memory before it was stopped),
+    the oracle's assembly, which is pinned entry for entry to the reference's at 12^3
+    (laplacian_12.npz) and evaluates the same formula."""
+    if use_reference_assembly:
+        lap = sys.modules["discrete_laplacian"]
+        rd = sys.modules["read_data"]
+        n = f.shape[0]
+        idx = lambda code: [tuple(int(c) for c in t) for t in np.argwhere(f == code)]
+        A = lap.lap_with_bc(n, 3, solid=idx(1), air=idx(3), bd=idx(0), bd_padding=True, dtype=np.float64)
+        A = rd.compressedMat(A, f).tocsr()
+    else:
+        from oracle.laplacian import assemble
+        A, _ = assemble(f)
+    A.sort_indices()
+    assert A.shape[0] == int((f == 2).sum()), "scene must have no sphere touching the wall layer"
+    return A
+
+
+def make_config_scene(ref_cg, ref_model, ref_py, size, seed, n, max_it=100, state=None, n_spheres=3,
+                      use_reference_assembly=False):
+    """A BASELINE-style scene solved by the reference: make_scene(size, seed) (one wall layer, a
+    height-field fluid, n_spheres spheres), the reference's SmallSMModelDn3D(n, 3, 'trilinear') in
+    FP32 -- drawn under torch.manual_seed(0) (random init), or given weights ``state`` -- and the
+    reference's npsd / npcg / npcg_flex (cg_tests.py) with test.py's model_predict and its call
+    (max_it 100, tol 1e-6, atol 1e-20).  Records the weights, the preconditioner output on the
+    normalised right-hand side (what model_predict feeds the network first), each solver's residual
+    history, iteration count and a few moments of its solution."""
+    ref_model.smblock3d = _BlockAdapter(ref_py, False)
+    ref_model.smblocktrans3d = _BlockAdapter(ref_py, True)
+    ref_model.smlinear3d = _LinearAdapter(ref_py)
+    torch.manual_seed(0)
+    model = ref_model.SmallSMModelDn3D(n, 3, "trilinear")
+    if state is not None:
+        model.load_state_dict({k: torch.as_tensor(v, dtype=torch.float32) for k, v in state.items()})
+    scene = make_scene(size, seed, n_spheres)
+    f = scene.flags
+    A = _fluid_matrix(f, use_reference_assembly)
+    At = torch.sparse_csr_tensor(A.indptr, A.indices, A.data, A.shape, dtype=torch.float64)
+    fluid = torch.from_numpy(np.flatnonzero(f.ravel() == 2))
+    rhs = torch.from_numpy(scene.rhs.ravel()[fluid.numpy()]).double()
+    image = torch.from_numpy(scene.image())
+    shape = tuple(f.shape)
+    from global_clock import GlobalClock
+
+    def predict(r, timer, imgs=[], c0=[], c1=[]):  # test.py:42-51 restated (test.py cannot be imported)
+        with torch.no_grad():
+            r = F.normalize(r.to(torch.float32), dim=0)
+            bb = torch.zeros(int(np.prod(shape)), dtype=torch.float32)
+            bb[fluid] = r
+            x = model.eval_forward(image, bb.view((1, 1) + shape), timer, imgs, c0, c1).flatten().double()
+        return x[fluid]
+
+    with torch.no_grad():
+        r0 = F.normalize(rhs.to(torch.float32), dim=0)
+        b0 = torch.zeros(int(np.prod(shape)), dtype=torch.float32)
+        b0[fluid] = r0
+        y0 = model.eval_forward(image, b0.view((1, 1) + shape), GlobalClock(), [], [], [])
+    out = {"size": np.array(size), "seed": np.array(seed), "n": np.array(n), "spheres": np.array(n_spheres),
+           "flags_sum": np.array(int(f.astype(np.int64).sum())), "rhs_norm": np.array(float(rhs.norm())),
+           "max_it": np.array(max_it), "assembly": np.array("reference" if use_reference_assembly else "oracle")}
+    if size <= 64:
+        out.update(b0=b0.numpy().reshape(shape), y0=y0.numpy().reshape(shape))
+    else:
+        # larger grids: the output at 65,536 cells drawn without replacement (the input b0 is the
+        # normalised rhs, rebuilt from the scene), to keep the fixture small
+        idx = np.sort(np.random.default_rng(7).choice(int(np.prod(shape)), 65536, replace=False))
+        out.update(y0_index=idx.astype(np.int64), y0_sample=y0.numpy().reshape(-1)[idx],
+                   y0_norm=np.array(float(y0.double().norm())))
+    out.update({"param:" + k: v.detach().numpy().copy() for k, v in model.state_dict().items()})
+    w = np.random.default_rng(99).standard_normal(fluid.numel())
+    for name in ("npsd", "npcg", "npcg_flex"):
+        hist = []
+        solver = getattr(ref_cg, name)
+        pred = predict if name == "npsd" else (lambda r, timer, _p=predict, _c=([], [], []): _p(r, timer, *_c))
+        x, iters, _, res = solver(rhs, At, torch.zeros_like(rhs), pred, max_it, tol=1e-6, atol=1e-20,
+                                  callback=lambda nrm, t: hist.append(nrm))
+        xn = x.numpy()
+        out[f"{name}_hist"] = np.array(hist)
+        out[f"{name}_iters"] = np.array(iters)
+        out[f"{name}_x_moments"] = np.array([np.linalg.norm(xn), float(xn @ w), float(xn.sum())])
+        print(f"{size}^3 seed {seed}: {name} {iters} iterations, rel res {res:.3e}", flush=True)
+    return out
+
+
 def make_cg_near_identity(ref_cg, ref_model, ref_py, shape, n, seed_scene, max_it=50):
     """Solver histories over max_it iterations with the reference's SmallSMModelDn3D(n) drawn under
     torch.manual_seed(0) and moved near the identity (weights x 0.1, centre tap of pre[0] and the
@@ -338,6 +424,19 @@ def main(ref_root: str, only: str | None = None):
         print("scene files written to", HERE)
         return
     torch.set_default_dtype(torch.float32)
+    if only == "config0":
+        # 64^3, seed 0, 3 spheres, 4 levels, random init from torch seed 0, FP32, max 100 iterations
+        np.savez_compressed(HERE / "cg_64_l4_seed0.npz",
+                            **make_config_scene(ref_cg, ref_model, ref_py, 64, 0, 4))
+        print("64^3 scene fixture written to", HERE)
+        return
+    if only == "config1":
+        # 128^3, seed 1, 3 spheres, 4 levels, the committed trained weights smallsm_l4.npz
+        w = np.load(REPO / "mlpcg_gb300" / "weights" / "smallsm_l4.npz")
+        np.savez_compressed(HERE / "cg_128_l4_seed1.npz",
+                            **make_config_scene(ref_cg, ref_model, ref_py, 128, 1, 4, state=dict(w)))
+        print("128^3 scene fixture written to", HERE)
+        return
     spd = {"spd_16_l2.npz": ("SPDSMModelDn3D", 2), "small_spd_16_l3.npz": ("SmallSPDSMModelDn3D", 3)}
     for fname, (cls_name, n) in spd.items():
         out, model, scene = make_spd(ref_model, ref_py, cls_name, (16, 16, 16), n, seed_scene=6)
@@ -372,7 +471,8 @@ def main(ref_root: str, only: str | None = None):
 
 
 if __name__ == "__main__":
-    # python make_golden.py [reference root] [--only=scene_files | --only=spd | --only=near_identity]
+    # python make_golden.py [reference root] [--only=scene_files | --only=spd | --only=near_identity |
+    #                                          --only=config0 | --only=config1]
     args = [a for a in sys.argv[1:] if not a.startswith("--only")]
     only = next((a.split("=", 1)[1] for a in sys.argv[1:] if a.startswith("--only=")), None)
     main(args[0] if args else "/root/reference", only)

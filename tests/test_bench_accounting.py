@@ -10,9 +10,10 @@ import bench
 N0 = 64 ** 3
 
 
-def _plan(kind, levels=1, masked=False, swap=False):
+def _plan(kind, levels=1, masked=False, swap=False, cluster=-1):
     return SimpleNamespace(levels=levels, kind=kind, spd=kind != 0, masked=masked, swap=swap, layout="classed",
-                           level_info=lambda l: (0, True, False))
+                           level_info=lambda l: (0, True, False),
+                           coarse_cluster=lambda: (cluster, 16 if cluster > 0 else 0))
 
 
 def test_smallsm_iteration_bytes_dense():
@@ -45,3 +46,11 @@ def test_launch_counters_run(kind):
     assert bench.precond_launches(p) > 0 and bench.setup_launches(p) > 0
     mixed = [1000, 500, 100, 50, 10, 4]
     assert bench.iteration_bytes(p, 256 ** 3, mixed, mixed if kind else None) > 0
+
+
+def test_launch_count_with_the_coarse_cluster():
+    # SmallSMModelDn3D, 5 tiled levels: 5 pre-blocks, the coarsest block, the level-0 prolongation
+    # pass + post-block and 4 post-blocks = 12 launches; with levels 3..5 in one cluster launch:
+    # pre 0-2, the cluster, post 2, post 1, prolongation + post 0 = 8
+    assert bench.precond_launches(_plan(0, levels=5)) == 12
+    assert bench.precond_launches(_plan(0, levels=5, cluster=3)) == 8

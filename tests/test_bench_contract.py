@@ -1,9 +1,12 @@
-"""bench.py's reference arm (the reference's CPU path on the host cores) prints exactly one JSON
-line with the benchmark contract's keys; run at 32^3 on the CPU so that it takes seconds."""
+"""bench.py's reference arm (the reference's CPU path on the host cores, run to convergence) prints
+exactly one JSON line with the benchmark contract's keys; run at 32^3 on the CPU so that it takes
+seconds."""
 import json
 import subprocess
 import sys
 from pathlib import Path
+
+import pytest
 
 ROOT = Path(__file__).resolve().parent.parent
 
@@ -21,7 +24,10 @@ def test_reference_arm_prints_one_contract_line():
     assert d["ms_per_step"] == d["value"] and d["data"] == "synthetic" and "workload" in d["config"]
     cb = d["cpu_baseline"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["unit"] == "ms"
-    assert cb["value"] == d["value"] and "iterations at 32^3" in cb["sample"]
+    assert cb["value"] == d["value"] and "solve at 32^3" in cb["sample"] and cb["measured"] is True
+    # a run to convergence (or to max_it), not an extrapolation: its own count and final residual
+    assert d["iterations"] == len(d["history"]) and d["rel_res"] == pytest.approx(d["history"][-1], rel=1e-6)
+    assert d["status"] in ("converged", "max_it")
     e2e = d["e2e"]
     assert e2e["value"] == d["value"] and e2e["unit"] == "ms"
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0

@@ -48,6 +48,30 @@ def test_plan_fp32_matches_eval_forward(cuda, shape, n, swap, mask):
     assert rel_err(z2.cpu().numpy(), 0.37 * ref.cpu().numpy()) < 1e-5
 
 
+@pytest.mark.parametrize("shape,n", [((128, 128, 128), 4), ((96, 64, 128), 4), ((256, 256, 256), 5)])
+@pytest.mark.parametrize("storage", [torch.float32, torch.bfloat16])
+@pytest.mark.parametrize("swap,mask,layout", [(False, False, "classed"), (True, True, "classed"),
+                                              (False, False, "dense")])
+def test_coarse_cluster_equals_per_level_kernels(cuda, shape, n, storage, swap, mask, layout):
+    """A whole application runs the coarse levels (from the first level with at most four tiles per
+    CTA down to the coarsest) in one thread-block cluster launch; the application split into
+    stages [0, n] and [n + 1, 2n] runs the per-level kernels instead.  Same bodies, same arithmetic:
+    the outputs agree bit for bit."""
+    s, flags, img = _scene(shape, 3, cuda)
+    m = _model(n, cuda, seed=2, swap=swap, mask=mask)
+    plan = m.precond_plan(img, storage=storage) if layout == "classed" else None
+    if plan is None:
+        from mlpcg_gb300.precond import PrecondPlan
+        plan = PrecondPlan(m, img, storage=storage, layout="dense")
+    r = torch.randn(int(np.prod(shape)), device=cuda, generator=torch.Generator(device=cuda).manual_seed(5))
+    z_cluster = plan.apply(r).clone()
+    z_levels = torch.empty_like(z_cluster)
+    plan.apply_stages(0, n, r, None, z_levels)
+    plan.apply_stages(n + 1, 2 * n, r, None, z_levels)
+    assert torch.equal(z_cluster, z_levels)
+    assert bool(torch.isfinite(z_cluster).all()) and float(z_cluster.abs().max()) > 0
+
+
 @pytest.mark.parametrize("storage,act", [(torch.bfloat16, torch.bfloat16), (torch.bfloat16, torch.float32),
                                          (torch.float32, torch.bfloat16)])
 def test_plan_bf16_storage(cuda, storage, act):
@@ -349,6 +373,61 @@ def test_tile_copies_complete(cuda):
     assert res.status in ("converged", "max_it") and np.isfinite(res.rel_res)
     assert res.history[-1] < 0.1 * res.history[0]
     assert not solver.plan.copy_failed()
+
+
+def test_tma_wait_timeout_reports_copy_failed(cuda):
+    """The bounded waits on the tensor-memory accelerator's tile copies, made to run out on ordinary
+    copies by the copy-stall knob (the first wait polls a barrier that nothing arrives on; the real
+    copy still completes and is waited for before the CTA leaves): the plan reports copy_failed, a
+    solve using it ends with status 'copy_failed', and so does a solve whose SpMV waits run out.
+    With the knobs off, the same plan and solver give the same results as before, bit for bit."""
+    from mlpcg_gb300.solver import FusedSolver
+    s, flags, img = _scene((64, 64, 64), 3, cuda)
+    m = _near_identity_model(4, cuda)
+    solver = FusedSolver(m, flags, method="npsd", max_it=60, tol=1e-6, storage=torch.bfloat16)
+    plan = solver.plan
+    b = torch.as_tensor(s.rhs, device=cuda)
+    r = torch.randn(64 ** 3, device=cuda, generator=torch.Generator(device=cuda).manual_seed(3))
+    z_ok = plan.apply(r).clone()
+    ok = solver.solve(b)
+    x_ok = ok.x.clone()
+    assert ok.status in ("converged", "max_it") and not plan.copy_failed()
+    # the plan's level-0 tile waits run out
+    plan.set_copy_stall(True)
+    plan.apply(r)
+    assert plan.copy_failed()
+    res = solver.solve(b)
+    assert res.status == "copy_failed"
+    plan.set_copy_stall(False)
+    assert not plan.copy_failed()
+    z = plan.apply(r)
+    assert not plan.copy_failed() and torch.equal(z, z_ok)
+    # the SpMV's tile waits run out
+    solver.set_copy_stall(True)
+    res = solver.solve(b)
+    assert res.status == "copy_failed" and res.iterations <= 1
+    solver.set_copy_stall(False)
+    res = solver.solve(b)
+    assert res.status == ok.status and res.iterations == ok.iterations and torch.equal(res.x, x_ok)
+    assert not plan.copy_failed()
+
+
+def test_zero_guess_solve_writes_every_cell(cuda):
+    """solve(b) without x0 starts from x0 = 0 without reading or clearing x: the result equals the
+    solve from an explicit zero guess, and the cells off the fluid hold 0 even if x held other
+    values before."""
+    from mlpcg_gb300.solver import FusedSolver
+    s, flags, img = _scene((32, 32, 32), 5, cuda)
+    m = _near_identity_model(3, cuda)
+    solver = FusedSolver(m, flags, method="npsd", max_it=100, tol=1e-6, storage=torch.bfloat16)
+    b = torch.as_tensor(s.rhs, device=cuda)
+    ref = solver.solve(b, x0=torch.zeros_like(b))
+    xr = ref.x.clone()
+    solver.x.fill_(3.0)
+    out = solver.solve(b)
+    assert out.status == ref.status and out.iterations == ref.iterations
+    assert torch.equal(out.x, xr)
+    assert torch.all(out.x[flags != 2] == 0)
 
 
 @pytest.mark.parametrize("n", [16, 24, 48])
