@@ -341,10 +341,18 @@ int mlpcg_precond_check(const mlpcg_precond *plan, int *copy_failed, void *strea
  * and the post-blocks in one launch of one thread-block cluster of *ctas
  * CTAs, stage after stage.  *first_level = -1 (and *ctas = 0) when no two
  * coarsest levels qualify (they must all run the tiled kernels), for the
- * symmetric kinds, or when the device runs no cluster of 8 or 16 CTAs.
+ * symmetric kinds, when the device runs no cluster of 8 or 16 CTAs, or when
+ * the plan has it switched off (mlpcg_precond_set_coarse_cluster).
  * mlpcg_precond_apply_stages uses it only when [first, last] covers all of
  * its stages (first_level .. 2n - first_level). */
 int mlpcg_precond_coarse_cluster(const mlpcg_precond *plan, int *first_level, int *ctas);
+/* on = 1: the plan's applications run the coarse levels as one cluster
+ * launch where the device and the plan allow it; on = 0 (the default): one
+ * kernel per stage.  Same arithmetic, same outputs.  Off by default: on a
+ * GB300 the 256^3 npsd solve takes 8.64 ms with it and 8.46 ms without (a
+ * stage's tiles share 16 SMs instead of spreading over the GPU, and each
+ * stage still waits on its tiles' load -> compute chain). */
+int mlpcg_precond_set_coarse_cluster(mlpcg_precond *plan, int on);
 /* Test knob of the bounded TMA waits (no counterpart in the reference):
  * with on != 0 the level-0 tile kernels first wait on a barrier that nothing
  * arrives on (256 polls), so the wait runs out on an ordinary copy, whose

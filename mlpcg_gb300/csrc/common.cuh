@@ -193,24 +193,83 @@ struct FieldGeom {
 
 // ---------------------------------------------------------------------------
 // The 27 coefficients of one cell: acc[p] = bias[p] + sum_{s,m,n,o} W[p][s][m][n][o] * v(s,m,n,o)
-// with v the image patch around the cell (v(s,m,n,o) = img(s, q + (m-1,n-1,o-1))).
-// sW[(s*27 + 9m+3n+o)*7 + pp] holds W[4pp..4pp+3][s][m][n][o] (p padded to 28),
-// sb[p] the bias.  The summation order (bias, then s, m, n, o) is the order of
-// the reference's loop (sm_block_3d_kernel.cu:53-64); every kernel that
-// produces coefficients goes through coeffs_of_patch_n, so equal patches give
+// with v the image patch around the cell (v(s,m,n,o) = img(s, q + (m-1,n-1,o-1))),
+// the contraction of sm_block_3d_kernel.cu:53-64.
+//
+// Two forms, chosen per cell:
+// * material form, when each of the 27 positions of the patch holds one of the
+//   three one-hot materials of the image channels [air, fluid, non-solid]
+//   (lib/read_data.py:35-39): solid or outside the grid (0,0,0), air (1,0,1),
+//   fluid (0,1,1).  A position's three products then sum to a table entry,
+//   Wm[material][position][p] = W[p][0][pos] + W[p][2][pos] (air) or
+//   W[p][1][pos] + W[p][2][pos] (fluid), 0 (solid), and the coefficients are
+//   acc[p] = bias[p] + sum over the 27 positions, in position order, of the
+//   entry of the position's material: 27 additions instead of 81 products.
+//   Every cell of a finest-level image made from flags takes this form.
+// * product form otherwise (the coarse levels' averaged images): bias, then
+//   the 81 products in the reference's loop order (s, m, n, o).
+// Both forms add in FP32 (round to nearest); their sums differ from the
+// reference's sequence only by rounding.  Every kernel that produces
+// coefficients (dense planes, classed records, the uniform vectors of the
+// classed layout) goes through these definitions, so equal patches give
 // bit-identical coefficients whichever kernel computed them.
-// coeffs_of_patch_n evaluates NB blocks on one patch (each patch value read
-// once): block b's weights at sW + b * kSW, its bias at sb + b * 28; each
-// block's accumulation sequence is the single-block one.
+//
+// Shared-memory layout: sW[(s*27 + 9m+3n+o)*7 + pp] holds W[4pp..4pp+3][s][m][n][o]
+// (p padded to 28), sWm[(mat*27 + pos)*7 + pp] the material table, sb[p] the
+// bias.  coeffs_of_patch_n evaluates NB blocks on one patch (each patch value
+// read once per form): block b at sW / sWm + b * kSW, its bias at sb + b * 28.
 // ---------------------------------------------------------------------------
-constexpr int kSW = 81 * 7;  // float4 entries of one block's weights in shared memory
+constexpr int kSW = 81 * 7;  // float4 entries of one block's weights (and of its material table)
+
+// material of one patch position: 0 solid / outside, 1 air, 2 fluid, 3 none of the three
+__device__ __forceinline__ int patch_material(float a, float f, float s) {
+  if (a == 0.f && f == 0.f && s == 0.f) return 0;
+  if (a == 1.f && f == 0.f && s == 1.f) return 1;
+  if (a == 0.f && f == 1.f && s == 1.f) return 2;
+  return 3;
+}
+
+// the material table entry of weights W (27 x 81, row p) for material mat at position pos
+__device__ __forceinline__ float material_weight(const float *__restrict__ W, int p, int mat, int pos) {
+  if (mat == 0) return 0.f;
+  return __fadd_rn(W[p * 81 + (mat == 1 ? 0 : 27) + pos], W[p * 81 + 54 + pos]);
+}
 
 template <int NB, typename Patch>
-__device__ __forceinline__ void coeffs_of_patch_n(const float4 *sW, const float *sb, Patch v, float (*acc)[28]) {
+__device__ __forceinline__ void coeffs_of_patch_n(const float4 *sW, const float4 *sWm, const float *sb, Patch v,
+                                                  float (*acc)[28]) {
 #pragma unroll
   for (int b = 0; b < NB; ++b)
 #pragma unroll
     for (int p = 0; p < 28; ++p) acc[b][p] = sb[b * 28 + p];
+  uint64_t mats = 0;
+  bool material = true;
+#pragma unroll
+  for (int pos = 0; pos < 27; ++pos) {
+    const int m = pos / 9, nn = (pos / 3) % 3, o = pos % 3;
+    const int mt = patch_material(v(0, m, nn, o), v(1, m, nn, o), v(2, m, nn, o));
+    material = material && mt != 3;
+    mats |= (uint64_t)(mt & 3) << (2 * pos);
+  }
+  if (material) {
+#pragma unroll
+    for (int pos = 0; pos < 27; ++pos) {
+      const int mt = (int)((mats >> (2 * pos)) & 3u);
+#pragma unroll
+      for (int b = 0; b < NB; ++b) {
+        const float4 *w = sWm + b * kSW + (mt * 27 + pos) * 7;
+#pragma unroll
+        for (int pp = 0; pp < 7; ++pp) {
+          const float4 wv = w[pp];
+          acc[b][4 * pp + 0] = __fadd_rn(acc[b][4 * pp + 0], wv.x);
+          acc[b][4 * pp + 1] = __fadd_rn(acc[b][4 * pp + 1], wv.y);
+          acc[b][4 * pp + 2] = __fadd_rn(acc[b][4 * pp + 2], wv.z);
+          acc[b][4 * pp + 3] = __fadd_rn(acc[b][4 * pp + 3], wv.w);
+        }
+      }
+    }
+    return;
+  }
   for (int s = 0; s < 3; ++s) {
 #pragma unroll
     for (int m = 0; m < 3; ++m)
@@ -235,17 +294,30 @@ __device__ __forceinline__ void coeffs_of_patch_n(const float4 *sW, const float 
   }
 }
 template <typename Patch>
-__device__ __forceinline__ void coeffs_of_patch(const float4 *sW, const float *sb, Patch v, float acc[28]) {
-  coeffs_of_patch_n<1>(sW, sb, v, reinterpret_cast<float (*)[28]>(acc));
+__device__ __forceinline__ void coeffs_of_patch(const float4 *sW, const float4 *sWm, const float *sb, Patch v,
+                                                float acc[28]) {
+  coeffs_of_patch_n<1>(sW, sWm, sb, v, reinterpret_cast<float (*)[28]>(acc));
 }
 
-// Loads W (27 x 81) and bias (27) into the shared-memory layout of coeffs_of_patch.
+// The coefficients of a patch whose 27 positions all hold material mat (the
+// uniform vectors of the classed layout): the material form, from global W.
+__device__ __forceinline__ float uniform_coeff(const float *__restrict__ W, const float *__restrict__ bias, int p,
+                                               int mat) {
+  float acc = bias[p];
+  for (int pos = 0; pos < 27; ++pos) acc = __fadd_rn(acc, material_weight(W, p, mat, pos));
+  return acc;
+}
+
+// Loads W (27 x 81), its material table and the bias (27) into the shared-memory layout of
+// coeffs_of_patch.
 __device__ __forceinline__ void load_weights_smem(const float *__restrict__ W, const float *__restrict__ bias,
-                                                  float4 *sW, float *sb) {
+                                                  float4 *sW, float4 *sWm, float *sb) {
   float *sWf = reinterpret_cast<float *>(sW);
+  float *sWmf = reinterpret_cast<float *>(sWm);
   for (int t = threadIdx.x; t < 81 * 28; t += blockDim.x) {
     const int so = t / 28, p = t % 28;
     sWf[t] = p < 27 ? W[p * 81 + so] : 0.f;
+    sWmf[t] = p < 27 ? material_weight(W, p, so / 27, so % 27) : 0.f;
   }
   if (threadIdx.x < 28) sb[threadIdx.x] = threadIdx.x < 27 ? bias[threadIdx.x] : 0.f;
 }

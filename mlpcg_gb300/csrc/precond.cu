@@ -235,28 +235,19 @@ __device__ __forceinline__ void st4(__nv_bfloat16 *p, const float v[4]) {
 // (p * R + r) * 8 + c -- so that a warp's loads of one tap are contiguous,
 // as they are in the dense planes.
 // Results equal those of the dense planes bit for bit: coeffs_of_patch_n
-// produces every value and the 27 taps are summed in the same order.
+// (material or product form, per patch) produces every value and the 27 taps
+// are summed in the same order.
 // ---------------------------------------------------------------------------
 enum { CLS_SOLID = 0, CLS_AIR = 1, CLS_FLUID = 2, CLS_GENERAL = 3 };
 constexpr int KREC = 32;        // uniform vectors: 27 values padded to 32
 constexpr int RREC = 27 * 8;    // coefficients of a mixed run's record
 constexpr uint32_t kMixed = 3;  // run word: bits 0-1 material or kMixed, bits 2.. mixed-run index in the tile
 
-__device__ __forceinline__ int material_of(float a, float f, float s) {
-  if (a == 0.f && f == 0.f && s == 0.f) return CLS_SOLID;
-  if (a == 1.f && f == 0.f && s == 1.f) return CLS_AIR;
-  if (a == 0.f && f == 1.f && s == 1.f) return CLS_FLUID;
-  return CLS_GENERAL;
-}
+// the class codes of the materials are patch_material's
+static_assert(CLS_SOLID == 0 && CLS_AIR == 1 && CLS_FLUID == 2 && CLS_GENERAL == 3, "material codes");
+__device__ __forceinline__ int material_of(float a, float f, float s) { return patch_material(a, f, s); }
 __device__ __forceinline__ int class_of(uint2 cw, int c) {
   return (int)(((c < 4 ? cw.x : cw.y) >> (8 * (c & 3))) & 0xffu);
-}
-
-// channel s of the one-hot image value of material cls
-__device__ __forceinline__ float material_channel(int cls, int s) {
-  if (cls == CLS_AIR) return s != 1 ? 1.f : 0.f;
-  if (cls == CLS_FLUID) return s != 0 ? 1.f : 0.f;
-  return 0.f;
 }
 
 // exclusive scan of one int per thread over the PT threads of a CTA
@@ -485,8 +476,8 @@ __device__ __forceinline__ float round_as(const __nv_bfloat16 *, float v) {
 // The coefficient vector of each uniform material for every block of the
 // model (blockIdx.x = parameter block b, at params + b * 2214), rounded like
 // the stored dtype: thread (c, p) evaluates output p of material c in the
-// accumulation order of coeffs_of_patch_n, so it equals what that function
-// yields on a patch of material c.  Block b's vectors go to slot b, and for
+// material form of coeffs_of_patch_n (uniform_coeff), so it equals what that
+// function yields on a patch of material c.  Block b's vectors go to slot b, and for
 // the symmetric networks its transpose's, the reversed vector (tap 26 - p),
 // to a second slot: kind MLPCG_PRECOND_SMALL_SPD (parameter blocks l0[0..n-1],
 // l) puts l0[b] in slot b and its transpose in n + b, l in 2n and l_t in
@@ -498,15 +489,7 @@ k_kgen_uniform_all(const float *__restrict__ params, float *__restrict__ kuni, i
   const int b = blockIdx.x, c = threadIdx.x / KREC, p = threadIdx.x % KREC;
   const float *W = params + (size_t)b * 2214, *bias = W + 2187;
   float acc = 0.f;
-  if (p < 27) {
-    acc = __ldg(bias + p);
-    for (int s = 0; s < 3; ++s) {
-      const float x = material_channel(c, s);
-#pragma unroll
-      for (int t = 0; t < 27; ++t) acc = fmaf(__ldg(W + p * 81 + s * 27 + t), x, acc);
-    }
-    acc = round_as((const KT *)nullptr, acc);
-  }
+  if (p < 27) acc = round_as((const KT *)nullptr, uniform_coeff(W, bias, p, c));
   if (kind == MLPCG_PRECOND_SM) {
     kuni[(size_t)b * 3 * KREC + threadIdx.x] = acc;
     return;
@@ -587,11 +570,12 @@ k_kgen_list(const float *__restrict__ img, int n1, int n2, int n3, const float *
             const uint32_t *__restrict__ rbase, const uint32_t *__restrict__ rcount, KT *__restrict__ rec0,
             KT *__restrict__ rec1) {
   __shared__ float4 sW[NB * kSW];
+  __shared__ float4 sWm[NB * kSW];
   __shared__ float sb[NB * 28];
 #pragma unroll
   for (int b = 0; b < NB; ++b) {
     const float *W = params + (size_t)(b ? b1 : b0) * 2214;
-    load_weights_smem(W, W + 2187, sW + b * kSW, sb + b * 28);
+    load_weights_smem(W, W + 2187, sW + b * kSW, sWm + b * kSW, sb + b * 28);
   }
   __syncthreads();
   const uint32_t G = __ldg(glast_base) + __ldg(glast_count);
@@ -602,7 +586,7 @@ k_kgen_list(const float *__restrict__ img, int n1, int n2, int n3, const float *
     const uint32_t t = q / (uint32_t)n3;
     const int j = (int)(t % (uint32_t)n2), i = (int)(t / (uint32_t)n2);
     float acc[NB][28];
-    coeffs_of_patch_n<NB>(sW, sb, [&](int s, int m, int nn, int o) {
+    coeffs_of_patch_n<NB>(sW, sWm, sb, [&](int s, int m, int nn, int o) {
       return g.at(img + s * g.bstride, i + m - 1, j + nn - 1, k + o - 1);
     }, acc);
     const RecPos rp = rec_pos(rw, rbase, rcount, q, i, j, k, n2, n3);
@@ -1394,9 +1378,19 @@ __device__ __forceinline__ Tile tile_of(unsigned id, int tz, int ty) {
 }
 
 // all threads of the cluster: the stage's global writes become visible to the next stage's reads
+// (release / acquire at cluster scope; the next stage reads them through L2)
 __device__ __forceinline__ void cluster_stage_barrier() {
-  __threadfence();
   asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// one tile's mixed-run record block into L2 (classed levels)
+template <typename KT>
+__device__ __forceinline__ void prefetch_tile_records(const CoefArgs<KT> &C, unsigned tile) {
+  const uint32_t base = __ldg(C.rbase + tile), cnt = __ldg(C.rcount + tile);
+  if (cnt == 0) return;
+  const size_t addr = __cvta_generic_to_global(C.rec + (size_t)base * RREC);
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(addr), "r"(cnt * (uint32_t)(RREC * sizeof(KT)))
+               : "memory");
 }
 
 template <typename KT, typename AT, bool CLS, bool SWAP>
@@ -1404,6 +1398,16 @@ __global__ void __launch_bounds__(PT)
 k_coarse_cluster(const __grid_constant__ CoarseArgs<KT, AT> A, const int *__restrict__ gate) {
   if (gate && *gate != 0) return;  // read alike by every CTA: the whole cluster leaves
   const unsigned r = blockIdx.x, nc = gridDim.x;
+  if constexpr (CLS) {
+    // the record blocks of every tile this CTA takes in any stage, asked into L2 up front (one
+    // thread per block), so that the later stages' coefficient loads find them there
+    int item = 0;
+    for (int i = 0; i < A.nlev; ++i)
+      for (unsigned id = r; id < A.ntiles[i]; id += nc) {
+        if (item++ == (int)threadIdx.x) prefetch_tile_records(A.pre[i], id);
+        if (i < A.nlev - 1 && item++ == (int)threadIdx.x) prefetch_tile_records(A.post[i], id);
+      }
+  }
   for (int i = 0; i < A.nlev; ++i) {
     const bool last = i == A.nlev - 1;
     for (unsigned id = r; id < A.ntiles[i]; id += nc) {
@@ -1517,7 +1521,7 @@ struct PrecondPlan {
   void *lin_ws = nullptr;
   float *scratch = nullptr;   // 81 floats (linear means)
   int *err = nullptr;         // set to 1 by a level-0 TMA tile copy that did not complete
-  bool coarse_cluster = true; // SM kind: the coarse levels in one cluster launch where the device allows
+  bool coarse_cluster = false; // SM kind: the coarse levels in one cluster launch (off: slower, see notes)
   size_t bytes = 0;
   bool ready = false;
 };
@@ -2620,6 +2624,13 @@ int mlpcg_precond_check(const mlpcg_precond *h, int *copy_failed, void *stream) 
   MLPCG_CUDA_CHECK(cudaMemcpyAsync(&v, h->p.err, sizeof(int), cudaMemcpyDeviceToHost, st));
   MLPCG_CUDA_CHECK(cudaStreamSynchronize(st));
   *copy_failed = v;
+  return MLPCG_OK;
+}
+
+int mlpcg_precond_set_coarse_cluster(mlpcg_precond *h, int on) {
+  clear_error();
+  MLPCG_REQUIRE(h, MLPCG_ERR_ARG, "precond_set_coarse_cluster: NULL plan");
+  h->p.coarse_cluster = on != 0;
   return MLPCG_OK;
 }
 

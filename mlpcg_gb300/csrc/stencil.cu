@@ -24,9 +24,10 @@ template <typename KT>
 __global__ void __launch_bounds__(kGenThreads)
 k_stencil_gen(const float *__restrict__ img, FieldGeom g, const float *__restrict__ W,
               const float *__restrict__ bias, KT *__restrict__ K, int64_t ps) {
-  __shared__ float4 sW[81 * 7];
+  __shared__ float4 sW[kSW];
+  __shared__ float4 sWm[kSW];
   __shared__ float sb[28];
-  load_weights_smem(W, bias, sW, sb);
+  load_weights_smem(W, bias, sW, sWm, sb);
   __syncthreads();
 
   const int64_t n = cells(g.n1, g.n2, g.n3);
@@ -38,7 +39,7 @@ k_stencil_gen(const float *__restrict__ img, FieldGeom g, const float *__restric
   const int i = (int)(t / g.n2);
 
   float acc[28];
-  coeffs_of_patch(sW, sb, [&](int s, int m, int nn, int o) {
+  coeffs_of_patch(sW, sWm, sb, [&](int s, int m, int nn, int o) {
     return g.at(img + s * g.bstride, i + m - 1, j + nn - 1, k + o - 1);
   }, acc);
 #pragma unroll

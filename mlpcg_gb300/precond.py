@@ -160,6 +160,11 @@ class PrecondPlan:
         call("mlpcg_precond_coarse_cluster", self._h, C.byref(lc), C.byref(c))
         return lc.value, c.value
 
+    def set_coarse_cluster(self, on: bool):
+        """Run the coarse levels as one cluster launch or as one kernel per stage (the default)
+        (mlpcg_precond_set_coarse_cluster); the outputs are the same."""
+        call("mlpcg_precond_set_coarse_cluster", self._h, int(bool(on)))
+
     def set_copy_stall(self, on: bool):
         """Test knob of the bounded TMA waits (mlpcg_precond_set_copy_stall): with ``on`` the level-0
         tile kernels' first wait runs out on an ordinary copy and ``copy_failed()`` turns true; every

@@ -81,7 +81,13 @@ def residual_loss(model, image, flags, fluid, b, kind="angle"):
                         like npsd and npcg are.
     """
     x = model(image, b[:, None])[:, 0]
-    x = x * fluid
+    return loss_of_outputs(x * fluid, b, flags, kind)
+
+
+def loss_of_outputs(x, b, flags, kind="angle"):
+    """The loss of network outputs x (B, N1, N2, N3; zero off the fluid cells) for right-hand sides b
+    (same shape): see residual_loss.  kind="reference" is loss_functions.py:18-23 with mean=True,
+    the mean over the batch of ||b - A x||."""
     Ax = LaplacianFunction.apply(flags, x)
     bf, Af = b.flatten(1), Ax.flatten(1)
     if kind == "angle":

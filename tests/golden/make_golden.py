@@ -416,6 +416,24 @@ def make_scene_files(ref_lap, ref_read, shape, seed, frame=1):
             "rhs_fluid": ref_read.compressedVec(rhs, flags)}
 
 
+def make_residual_loss(ref: Path, shape=(16, 16, 16), seed=3, B=4):
+    """The reference's residual_loss (loss_functions.py:18-23: y - x A row by row, the mean and the
+    sum of the norms) on FP64 batches over the fluid cells of a scene, with the reference's own
+    matrix (lap_with_bc + compressedMat, as CSC)."""
+    sys.path.insert(0, str(ref))
+    import loss_functions as ref_loss
+    scene = make_scene(shape, seed)
+    f = scene.flags
+    A = _fluid_matrix(f, True).tocsc()
+    At = torch.sparse_csc_tensor(A.indptr, A.indices, A.data, A.shape, dtype=torch.float64)
+    rng = np.random.default_rng(seed)
+    x = torch.from_numpy(rng.standard_normal((B, A.shape[0])))
+    y = torch.from_numpy(rng.standard_normal((B, A.shape[0])))
+    return {"flags": f, "x": x.numpy(), "y": y.numpy(),
+            "loss_mean": np.array(float(ref_loss.residual_loss(x, y, At))),
+            "loss_sum": np.array(float(ref_loss.residual_loss(x, y, At, mean=False)))}
+
+
 def main(ref_root: str, only: str | None = None):
     ref = Path(ref_root)
     ref_model, ref_py, ref_lap, ref_read, ref_cg = _import_reference(ref)
@@ -424,6 +442,10 @@ def main(ref_root: str, only: str | None = None):
         print("scene files written to", HERE)
         return
     torch.set_default_dtype(torch.float32)
+    if only == "residual_loss":
+        np.savez_compressed(HERE / "residual_loss_16.npz", **make_residual_loss(ref))
+        print("residual_loss fixture written to", HERE)
+        return
     if only == "config0":
         # 64^3, seed 0, 3 spheres, 4 levels, random init from torch seed 0, FP32, max 100 iterations
         np.savez_compressed(HERE / "cg_64_l4_seed0.npz",
@@ -472,7 +494,7 @@ def main(ref_root: str, only: str | None = None):
 
 if __name__ == "__main__":
     # python make_golden.py [reference root] [--only=scene_files | --only=spd | --only=near_identity |
-    #                                          --only=config0 | --only=config1]
+    #                                          --only=config0 | --only=config1 | --only=residual_loss]
     args = [a for a in sys.argv[1:] if not a.startswith("--only")]
     only = next((a.split("=", 1)[1] for a in sys.argv[1:] if a.startswith("--only=")), None)
     main(args[0] if args else "/root/reference", only)

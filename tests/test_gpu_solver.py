@@ -53,16 +53,19 @@ def test_plan_fp32_matches_eval_forward(cuda, shape, n, swap, mask):
 @pytest.mark.parametrize("swap,mask,layout", [(False, False, "classed"), (True, True, "classed"),
                                               (False, False, "dense")])
 def test_coarse_cluster_equals_per_level_kernels(cuda, shape, n, storage, swap, mask, layout):
-    """A whole application runs the coarse levels (from the first level with at most four tiles per
-    CTA down to the coarsest) in one thread-block cluster launch; the application split into
-    stages [0, n] and [n + 1, 2n] runs the per-level kernels instead.  Same bodies, same arithmetic:
-    the outputs agree bit for bit."""
+    """With the cluster switched on, a whole application runs the coarse levels (from the first level
+    with at most four tiles per CTA down to the coarsest) in one thread-block cluster launch; the
+    application split into stages [0, n] and [n + 1, 2n] runs the per-level kernels instead.  Same
+    bodies, same arithmetic: the outputs agree bit for bit."""
     s, flags, img = _scene(shape, 3, cuda)
     m = _model(n, cuda, seed=2, swap=swap, mask=mask)
     plan = m.precond_plan(img, storage=storage) if layout == "classed" else None
     if plan is None:
         from mlpcg_gb300.precond import PrecondPlan
         plan = PrecondPlan(m, img, storage=storage, layout="dense")
+    assert plan.coarse_cluster()[0] == -1  # off by default
+    plan.set_coarse_cluster(True)
+    assert plan.coarse_cluster()[0] > 0
     r = torch.randn(int(np.prod(shape)), device=cuda, generator=torch.Generator(device=cuda).manual_seed(5))
     z_cluster = plan.apply(r).clone()
     z_levels = torch.empty_like(z_cluster)

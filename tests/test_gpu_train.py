@@ -112,3 +112,23 @@ def test_recompute_gives_the_same_gradients_with_less_memory(cuda):
     for k in gp0:
         assert torch.equal(gp0[k], gp1[k]), k
     assert kept1 < 0.75 * kept0, (kept0, kept1)
+
+
+def test_residual_loss_reference_kind_matches_the_reference(golden, cuda):
+    """train.loss_of_outputs(kind="reference") -- the loss of residual_loss(kind="reference") -- against
+    the reference's loss_functions.residual_loss (loss_functions.py:18-23, mean over the batch of
+    ||y - x A||, CSC matrix) on the same FP64 batch of a 16^3 scene (fixture from the reference)."""
+    from mlpcg_gb300.train import loss_of_outputs
+    d = golden("residual_loss_16.npz")
+    flags = torch.as_tensor(d["flags"], device=cuda)
+    fluid = torch.nonzero(flags.reshape(-1) == 2).reshape(-1)
+    B = d["x"].shape[0]
+    n = flags.numel()
+    xg = torch.zeros((B, n), dtype=torch.float64, device=cuda)
+    yg = torch.zeros((B, n), dtype=torch.float64, device=cuda)
+    xg[:, fluid] = torch.as_tensor(d["x"], device=cuda)
+    yg[:, fluid] = torch.as_tensor(d["y"], device=cuda)
+    shp = (B,) + tuple(flags.shape)
+    loss = float(loss_of_outputs(xg.reshape(shp), yg.reshape(shp), flags, kind="reference"))
+    assert loss == pytest.approx(float(d["loss_mean"]), rel=1e-12)
+    assert loss * B == pytest.approx(float(d["loss_sum"]), rel=1e-12)

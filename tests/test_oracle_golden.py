@@ -168,3 +168,14 @@ def test_fp64_cg_oracle_converges():
     b = s.rhs.ravel()[fluid]
     x, it = olap.cg_fp64(A, b, tol=1e-12)
     assert np.linalg.norm(b - A @ x) <= 1e-12 * np.linalg.norm(b) * 1.0001
+
+
+def test_residual_loss_restated(golden):
+    """The reference's residual_loss (loss_functions.py:18-23) with the oracle's matrix: the mean and
+    the sum over the batch of ||y - A x|| equal the reference's on its fixture."""
+    d = golden("residual_loss_16.npz")
+    A, fluid = olap.assemble(d["flags"])
+    r = d["y"] - (A @ d["x"].T).T
+    norms = np.linalg.norm(r, axis=1)
+    assert norms.mean() == pytest.approx(float(d["loss_mean"]), rel=1e-12)
+    assert norms.sum() == pytest.approx(float(d["loss_sum"]), rel=1e-12)
