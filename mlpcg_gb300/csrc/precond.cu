@@ -558,6 +558,45 @@ __device__ __forceinline__ RecPos rec_pos(const uint32_t *__restrict__ rw, const
   return rp;
 }
 
+// The uniform cells of every mixed run, for NB blocks (uniform vectors at
+// kuni0 / kuni1): thread (p, e) writes tap p of the record of mixed run e --
+// the run's 8 cells, contiguous in the record -- as one vector store, its
+// uniform cells taking their material's value and its general cells 0 until
+// k_kgen_list / k_kgen_t_list (launched after it) write theirs.  Consecutive
+// threads take consecutive runs of one tap, which sit side by side in a tile's
+// record block.  Run indices from rlist, their count read on the device.
+template <typename KT, int NB>
+__global__ void __launch_bounds__(256)
+k_fill_runs(const uint8_t *__restrict__ cls, const uint32_t *__restrict__ rlist,
+            const uint32_t *__restrict__ rlast_base, const uint32_t *__restrict__ rlast_count,
+            const uint32_t *__restrict__ rw, const uint32_t *__restrict__ rbase, const uint32_t *__restrict__ rcount,
+            int n2, int n3, const float *__restrict__ kuni0, const float *__restrict__ kuni1, KT *__restrict__ rec0,
+            KT *__restrict__ rec1) {
+  const uint64_t nrun = (uint64_t)__ldg(rlast_base) + __ldg(rlast_count);
+  for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < 27 * nrun;
+       t += (uint64_t)gridDim.x * blockDim.x) {
+    const int p = (int)(t / nrun);
+    const uint32_t e = (uint32_t)(t - (uint64_t)p * nrun);
+    const uint32_t q = 8u * __ldg(rlist + e);
+    const int k = (int)(q % (uint32_t)n3);
+    const uint32_t r = q / (uint32_t)n3;
+    const int j = (int)(r % (uint32_t)n2), i = (int)(r / (uint32_t)n2);
+    const RecPos rp = rec_pos(rw, rbase, rcount, q, i, j, k, n2, n3);
+    const uint2 cw = __ldg(reinterpret_cast<const uint2 *>(cls + q));
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      const float *ku = (b ? kuni1 : kuni0) + p;
+      float v[8];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        const int cl = class_of(cw, c);
+        v[c] = cl == CLS_GENERAL ? 0.f : __ldg(ku + cl * KREC);
+      }
+      st8((b ? rec1 : rec0) + rp.offset + (size_t)p * rp.stride, v);
+    }
+  }
+}
+
 // The coefficients of every general cell for NB blocks of one level at once
 // (the pre- and post-block share the level's image and run words), written
 // into the records of their runs.  Thread e of the grid-stride loop evaluates
@@ -595,36 +634,6 @@ k_kgen_list(const float *__restrict__ img, int n1, int n2, int n3, const float *
       KT *r = (b ? rec1 : rec0) + rp.offset;
 #pragma unroll
       for (int p = 0; p < 27; ++p) stf(r + p * rp.stride, acc[b][p]);
-    }
-  }
-}
-
-// The uniform cells of the mixed runs: their material's vector, for NB blocks
-// (uniform vectors at kuni0 / kuni1).  Thread e of the grid-stride loop takes
-// cell e % 8 of mixed run e / 8 (runs from rlist; their count read on the
-// device).
-template <typename KT, int NB>
-__global__ void __launch_bounds__(256)
-k_fill_uniform(const uint8_t *__restrict__ cls, const uint32_t *__restrict__ rlist,
-               const uint32_t *__restrict__ rlast_base, const uint32_t *__restrict__ rlast_count,
-               const uint32_t *__restrict__ rw, const uint32_t *__restrict__ rbase,
-               const uint32_t *__restrict__ rcount, int n1, int n2, int n3, const float *__restrict__ kuni0,
-               const float *__restrict__ kuni1, KT *__restrict__ rec0, KT *__restrict__ rec1) {
-  const uint64_t ncell = 8ull * (__ldg(rlast_base) + __ldg(rlast_count));
-  for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < ncell; e += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t q = 8u * __ldg(rlist + (e >> 3)) + (uint32_t)(e & 7);
-    const int cl = cls[q];
-    if (cl == CLS_GENERAL) continue;
-    const int k = (int)(q % (uint32_t)n3);
-    const uint32_t t = q / (uint32_t)n3;
-    const int j = (int)(t % (uint32_t)n2), i = (int)(t / (uint32_t)n2);
-    const RecPos rp = rec_pos(rw, rbase, rcount, q, i, j, k, n2, n3);
-#pragma unroll
-    for (int b = 0; b < NB; ++b) {
-      const float *ku = (b ? kuni1 : kuni0) + cl * KREC;
-      KT *r = (b ? rec1 : rec0) + rp.offset;
-#pragma unroll
-      for (int p = 0; p < 27; ++p) stf(r + p * rp.stride, __ldg(ku + p));
     }
   }
 }
@@ -816,6 +825,79 @@ __device__ __forceinline__ void tile_apply(const float (*S)[HY][HZP], const ClsS
   }
 }
 
+// tile_apply for the small levels (the grid fits in one wave, so registers do not limit the
+// resident CTAs): each run's 27 coefficient vectors are loaded before any of them is used --
+// one round of memory latency per run instead of one per group of taps -- and the runs are
+// applied one after the other, each cell summing its taps in the same order with the same
+// operands as tile_apply, so the results are identical.  BF16 coefficients (8 values per
+// 16-byte load); warps without a mixed run take tile_apply's shared-memory path.
+template <typename KT, bool CLS, int OFF = 0>
+__device__ __forceinline__ void tile_apply_pref(const float (*S)[HY][HZP], const ClsSmem *sm, const CoefArgs<KT> &C,
+                                                const uint32_t rwd[TX], uint2 trec, const Tile &t, int n1, int n2,
+                                                int n3, float acc[TX][8]) {
+  static_assert(sizeof(KT) == 2, "prefetched application: BF16 coefficients only");
+  const int tz = run_tz(threadIdx.x), ty = run_ty(threadIdx.x);
+  const int x0 = t.bz * TX, k0 = t.bx * TZ + tz * 8, j = t.by * TY + ty;
+  const bool active = k0 < n3 && j < n2;
+  if constexpr (CLS) {
+    const bool m0 = (rwd[0] & 3u) == kMixed, m1 = (rwd[1] & 3u) == kMixed;
+    if (!__any_sync(0xffffffffu, m0 || m1)) {
+      tile_apply<KT, CLS, OFF>(S, sm, C, rwd, trec, t, n1, n2, n3, acc);
+      return;
+    }
+  }
+#pragma unroll
+  for (int tx = 0; tx < TX; ++tx) {
+    const bool valid = active && x0 + tx < n1;
+    const KT *base;
+    size_t st;
+    bool load = true;
+    if constexpr (CLS) {
+      const bool mixed = (rwd[tx] & 3u) == kMixed;
+      base = mixed ? C.rec + (size_t)trec.x * RREC + (rwd[tx] >> 2) * 8 : C.mrec + (rwd[tx] & 3u) * RREC;
+      st = mixed ? (size_t)trec.y * 8 : 8;
+    } else {
+      base = C.K + (valid ? ((int64_t)(x0 + tx) * n2 + j) * n3 + k0 : 0);
+      st = (size_t)C.ps;
+      load = valid;
+    }
+    // all 27 loads issued before the first use (volatile: kept in this order, ahead of the FMAs)
+    uint4 kr[27];
+#pragma unroll
+    for (int p = 0; p < 27; ++p) {
+      kr[p] = make_uint4(0u, 0u, 0u, 0u);
+      if (load)
+        asm volatile("ld.global.nc.v4.u32 {%0, %1, %2, %3}, [%4];"
+                     : "=r"(kr[p].x), "=r"(kr[p].y), "=r"(kr[p].z), "=r"(kr[p].w)
+                     : "l"(base + (size_t)p * st));
+    }
+    // keep every use after the last load: each vector passes through an (empty) volatile statement,
+    // and those statements follow the loads in program order
+#pragma unroll
+    for (int p = 0; p < 27; ++p)
+      asm volatile("" : "+r"(kr[p].x), "+r"(kr[p].y), "+r"(kr[p].z), "+r"(kr[p].w));
+#pragma unroll
+    for (int c = 0; c < 8; ++c) acc[tx][c] = 0.f;
+#pragma unroll
+    for (int dx = 0; dx < 3; ++dx)
+#pragma unroll
+      for (int dy = 0; dy < 3; ++dy) {
+        float xr[OFF ? 16 : 12];
+        if constexpr (OFF != 0) ld_row16(&S[tx + dx][ty + dy][tz * 8], xr);
+        else ld_row12(&S[tx + dx][ty + dy][tz * 8], xr);
+#pragma unroll
+        for (int dz = 0; dz < 3; ++dz) {
+          const uint4 u = kr[dx * 9 + dy * 3 + dz];
+          float kv[8];
+          unpack_bf16x2(u.x, kv[0], kv[1]); unpack_bf16x2(u.y, kv[2], kv[3]);
+          unpack_bf16x2(u.z, kv[4], kv[5]); unpack_bf16x2(u.w, kv[6], kv[7]);
+#pragma unroll
+          for (int c = 0; c < 8; ++c) acc[tx][c] = fmaf(kv[c], xr[c + dz + OFF], acc[tx][c]);
+        }
+      }
+  }
+}
+
 // uniform coefficient vectors of a classed block into shared memory
 template <bool CLS>
 __device__ __forceinline__ void stage_uniform(ClsSmem *sm, const float *__restrict__ kuni) {
@@ -953,7 +1035,7 @@ __device__ __forceinline__ float (*coarse_tile_smem())[CY][CZP] {
 // 4 x 18 x 76 box of the input (z from z0 - 4, outside the grid read as 0)
 // into the tile, completing on an mbarrier; the scale is applied to the
 // block's output instead (the block is linear in x).
-template <typename KT, typename XT, typename YT, bool POOL, bool CLS, bool TMA, bool COH = false>
+template <typename KT, typename XT, typename YT, bool POOL, bool CLS, bool TMA, bool COH = false, bool PREF = false>
 __device__ __forceinline__ void pre_fused_body(const CoefArgs<KT> &C, const XT *__restrict__ x,
                                                const float *__restrict__ xscale, YT *__restrict__ y,
                                                YT *__restrict__ ypool, const uint8_t *__restrict__ mask, int n1,
@@ -987,7 +1069,8 @@ __device__ __forceinline__ void pre_fused_body(const CoefArgs<KT> &C, const XT *
     if (!tma_tile_wait(tw, err)) return;
   }
   float acc[TX][8];
-  tile_apply<KT, CLS, TMA ? 3 : 0>(S, smc, C, rwd, tb, t, n1, n2, n3, acc);
+  if constexpr (PREF) tile_apply_pref<KT, CLS, TMA ? 3 : 0>(S, smc, C, rwd, tb, t, n1, n2, n3, acc);
+  else tile_apply<KT, CLS, TMA ? 3 : 0>(S, smc, C, rwd, tb, t, n1, n2, n3, acc);
   const int tz = run_tz(threadIdx.x), ty = run_ty(threadIdx.x);
   const int k0 = z0 + tz * 8, j = y0 + ty;
   const bool active = k0 < n3 && j < n2;  // n3 % 8 == 0: a run is all in or all out
@@ -1031,6 +1114,17 @@ k_pre_fused(const CoefArgs<KT> C, const XT *__restrict__ x,
   if (gate && *gate != 0) return;  // batched solves: this system has stopped
   pre_fused_body<KT, XT, YT, POOL, CLS, false>(C, x, xscale, y, ypool, mask, n1, n2, n3, nullptr, nullptr,
                                               grid_tile());
+}
+
+// the small levels' pre-block: each run's coefficients loaded up front (tile_apply_pref); one
+// CTA per SM is all such a grid needs, so the kernel may use the registers that takes
+template <typename KT, typename XT, typename YT, bool POOL, bool CLS>
+__global__ void __launch_bounds__(PT, 1)
+k_pre_fused_small(const CoefArgs<KT> C, const XT *__restrict__ x, YT *__restrict__ y, YT *__restrict__ ypool,
+                  int n1, int n2, int n3, const int *__restrict__ gate) {
+  if (gate && *gate != 0) return;
+  pre_fused_body<KT, XT, YT, POOL, CLS, false, false, true>(C, x, nullptr, y, ypool, nullptr, n1, n2, n3, nullptr,
+                                                            nullptr, grid_tile());
 }
 
 // the level-0 pre-block with its FP32 input tile loaded by TMA through tmap (x only for the
@@ -1219,7 +1313,7 @@ k_up_fine(const CT *__restrict__ xc, const YT *__restrict__ yl, const float *__r
 // TMA (UPIN, CT = float): the FP32 input u arrives by the tensor-memory accelerator as in the
 // level-0 pre-block (tma_tile_issue / tma_tile_wait).
 template <typename KT, typename CT, typename YT, typename OT, bool SWAP, bool CLS, bool UPIN, bool TMA,
-          bool COH = false>
+          bool COH = false, bool PREF = false>
 __device__ __forceinline__ void post_fused_body(const CoefArgs<KT> &C, const CT *__restrict__ xc,
                                                 const YT *__restrict__ yl, const float *__restrict__ c0p,
                                                 const float *__restrict__ c1p, OT *__restrict__ out,
@@ -1299,7 +1393,8 @@ __device__ __forceinline__ void post_fused_body(const CoefArgs<KT> &C, const CT 
     if (!tma_tile_wait(tw, err)) return;
   }
   float accs[TX][8];
-  tile_apply<KT, CLS, TMA ? 3 : 0>(S, smc, C, rwd, tb, t, n1, n2, n3, accs);
+  if constexpr (PREF) tile_apply_pref<KT, CLS, TMA ? 3 : 0>(S, smc, C, rwd, tb, t, n1, n2, n3, accs);
+  else tile_apply<KT, CLS, TMA ? 3 : 0>(S, smc, C, rwd, tb, t, n1, n2, n3, accs);
   const int tz = run_tz(threadIdx.x), ty = run_ty(threadIdx.x);
   const int k0 = z0 + tz * 8, j = y0 + ty;
   if (k0 >= n3 || j >= n2) return;
@@ -1330,6 +1425,17 @@ k_post_fused(const CoefArgs<KT> C, const CT *__restrict__ xc, const YT *__restri
   if (gate && *gate != 0) return;
   post_fused_body<KT, CT, YT, OT, SWAP, CLS, UPIN, false>(C, xc, yl, c0p, c1p, out, bmask, omask, n1, n2, n3,
                                                           nullptr, nullptr, grid_tile());
+}
+
+// the small levels' post-block (fused prolongation and combine), coefficients loaded up front
+template <typename KT, typename AT, bool SWAP, bool CLS>
+__global__ void __launch_bounds__(PT, 1)
+k_post_fused_small(const CoefArgs<KT> C, const AT *__restrict__ xc, const AT *__restrict__ yl,
+                   const float *__restrict__ c0p, const float *__restrict__ c1p, AT *__restrict__ out, int n1,
+                   int n2, int n3, const int *__restrict__ gate) {
+  if (gate && *gate != 0) return;
+  post_fused_body<KT, AT, AT, AT, SWAP, CLS, false, false, false, true>(C, xc, yl, c0p, c1p, out, nullptr, nullptr,
+                                                                        n1, n2, n3, nullptr, nullptr, grid_tile());
 }
 
 // the post-block on an FP32 prolongated input u loaded by TMA through tmap
@@ -2060,6 +2166,40 @@ static int cluster_ctas_for(const PrecondPlan &P) {
   return cls ? coarse_cluster_ctas<KT, AT, true, false>() : coarse_cluster_ctas<KT, AT, false, false>();
 }
 
+// The small levels (their tiles fit in one wave of CTAs) run the block kernels' prefetching
+// variant when the coefficients are BF16.
+template <typename KT>
+static bool small_level(const PrecondPlan::Level &v) {
+  return std::is_same<KT, __nv_bfloat16>::value && v.ntiles <= 2u * (unsigned)sm_count();
+}
+
+template <typename KT, typename AT, bool POOL, bool CLS>
+static void launch_pre_level(const PrecondPlan::Level &v, const CoefArgs<KT> &C, const AT *x, AT *y, AT *yp,
+                             cudaStream_t st, const int *gate) {
+  if constexpr (std::is_same<KT, __nv_bfloat16>::value) {
+    if (small_level<KT>(v)) {
+      k_pre_fused_small<KT, AT, AT, POOL, CLS><<<grid_of(v), PT, 0, st>>>(C, x, y, yp, v.n1, v.n2, v.n3, gate);
+      return;
+    }
+  }
+  k_pre_fused<KT, AT, AT, POOL, CLS><<<grid_of(v), PT, 0, st>>>(C, x, nullptr, y, yp, nullptr, v.n1, v.n2, v.n3,
+                                                                gate);
+}
+
+template <typename KT, typename AT, bool SWAP, bool CLS>
+static void launch_post_level(const PrecondPlan::Level &v, const CoefArgs<KT> &C, const AT *xc, const AT *yl,
+                              const float *c0, const float *c1, AT *o, cudaStream_t st, const int *gate) {
+  if constexpr (std::is_same<KT, __nv_bfloat16>::value) {
+    if (small_level<KT>(v)) {
+      k_post_fused_small<KT, AT, SWAP, CLS><<<grid_of(v), PT, 0, st>>>(C, xc, yl, c0, c1, o, v.n1, v.n2, v.n3,
+                                                                         gate);
+      return;
+    }
+  }
+  k_post_fused<KT, AT, AT, AT, SWAP, CLS, false><<<grid_of(v), PT, 0, st>>>(C, xc, yl, c0, c1, o, nullptr, nullptr,
+                                                                           v.n1, v.n2, v.n3, gate);
+}
+
 template <typename KT, typename AT>
 static int run_apply(const PrecondPlan &P, const float *r, const float *rscale, float *z, void *tmp0,
                      cudaStream_t st, int s0 = 0, int s1 = 1 << 20, const int *gate = nullptr) {
@@ -2080,11 +2220,10 @@ static int run_apply(const PrecondPlan &P, const float *r, const float *rscale, 
         RET_IF((launch_pre0<KT, AT>(P, C, r, rscale, (AT *)P.y[0], (AT *)P.xin[1], m0, st, gate)));
       } else {
         if (v.cls)
-          k_pre_fused<KT, AT, AT, true, true><<<grid_of(v), PT, 0, st>>>(
-              C, (const AT *)P.xin[l], nullptr, (AT *)P.y[l], (AT *)P.xin[l + 1], nullptr, v.n1, v.n2, v.n3, gate);
+          launch_pre_level<KT, AT, true, true>(v, C, (const AT *)P.xin[l], (AT *)P.y[l], (AT *)P.xin[l + 1], st, gate);
         else
-          k_pre_fused<KT, AT, AT, true, false><<<grid_of(v), PT, 0, st>>>(
-              C, (const AT *)P.xin[l], nullptr, (AT *)P.y[l], (AT *)P.xin[l + 1], nullptr, v.n1, v.n2, v.n3, gate);
+          launch_pre_level<KT, AT, true, false>(v, C, (const AT *)P.xin[l], (AT *)P.y[l], (AT *)P.xin[l + 1], st,
+                                                gate);
       }
       MLPCG_LAUNCH_CHECK();
     } else {
@@ -2111,12 +2250,8 @@ static int run_apply(const PrecondPlan &P, const float *r, const float *rscale, 
     AT *cdst = (AT *)(spd ? P.xtmp : P.xout[L]);
     if (v.fast) {
       const CoefArgs<KT> C = coef_args<KT>(P, L, P.Kl, v.cls ? P.Ul : nullptr);
-      if (v.cls)
-        k_pre_fused<KT, AT, AT, false, true><<<grid_of(v), PT, 0, st>>>(
-            C, (const AT *)P.xin[L], nullptr, cdst, nullptr, nullptr, v.n1, v.n2, v.n3, gate);
-      else
-        k_pre_fused<KT, AT, AT, false, false><<<grid_of(v), PT, 0, st>>>(
-            C, (const AT *)P.xin[L], nullptr, cdst, nullptr, nullptr, v.n1, v.n2, v.n3, gate);
+      if (v.cls) launch_pre_level<KT, AT, false, true>(v, C, (const AT *)P.xin[L], cdst, nullptr, st, gate);
+      else launch_pre_level<KT, AT, false, false>(v, C, (const AT *)P.xin[L], cdst, nullptr, st, gate);
       MLPCG_LAUNCH_CHECK();
       if (spd) {
         const CoefArgs<KT> Ct = coef_args_t<KT>(P, L, P.Klt, v.cls ? P.Ult : nullptr);
@@ -2195,11 +2330,11 @@ static int run_apply(const PrecondPlan &P, const float *r, const float *rscale, 
       } else {
         AT *o = (AT *)P.xout[l];
         if (P.swap) {
-          if (v.cls) k_post_fused<KT, AT, AT, AT, true, true, false><<<g, PT, 0, st>>>(C, xc, yl, c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3, gate);
-          else k_post_fused<KT, AT, AT, AT, true, false, false><<<g, PT, 0, st>>>(C, xc, yl, c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3, gate);
+          if (v.cls) launch_post_level<KT, AT, true, true>(v, C, xc, yl, c0, c1, o, st, gate);
+          else launch_post_level<KT, AT, true, false>(v, C, xc, yl, c0, c1, o, st, gate);
         } else {
-          if (v.cls) k_post_fused<KT, AT, AT, AT, false, true, false><<<g, PT, 0, st>>>(C, xc, yl, c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3, gate);
-          else k_post_fused<KT, AT, AT, AT, false, false, false><<<g, PT, 0, st>>>(C, xc, yl, c0, c1, o, nullptr, nullptr, v.n1, v.n2, v.n3, gate);
+          if (v.cls) launch_post_level<KT, AT, false, true>(v, C, xc, yl, c0, c1, o, st, gate);
+          else launch_post_level<KT, AT, false, false>(v, C, xc, yl, c0, c1, o, st, gate);
         }
       }
       MLPCG_LAUNCH_CHECK();
@@ -2411,22 +2546,23 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
     if (u0s < 0) u0s = b0;
     if (u1s < 0) u1s = b1 >= 0 ? b1 : b0;
     const float *u0 = P.Uall + (size_t)u0s * 3 * KREC, *u1 = P.Uall + (size_t)u1s * 3 * KREC;
-    const int fgrid = (int)std::min<int64_t>((int64_t)sm_count() * 8, (v.n + 255) / 256);
+    const int fgrid = (int)std::min<int64_t>((int64_t)sm_count() * 8, (27 * (v.n / 8) + 255) / 256);
     const uint32_t *rlb = P.rbase[l] + v.ntiles - 1, *rlc = P.rcount[l] + v.ntiles - 1;
+    // the mixed runs' uniform cells first (whole taps per vector store), then the general cells
     auto launch = [&](auto kern, auto fill, const void *r0, const void *r1) {
       using KT = typename std::remove_pointer<decltype(kgen_rec_type(kern))>::type;
+      fill<<<fgrid, 256, 0, gs>>>(P.cls[l], rl, rlb, rlc, P.rw[l], P.rbase[l], P.rcount[l], v.n2, v.n3, u0, u1,
+                                  (KT *)r0, (KT *)r1);
       const int grid = (int)std::min<int64_t>((int64_t)sm_count() * resident_ctas(kern), (v.n + PT - 1) / PT);
       kern<<<grid, PT, 0, gs>>>(im, v.n1, v.n2, v.n3, params, b0, b1 >= 0 ? b1 : b0, gl, lb, lc, P.rw[l],
                                 P.rbase[l], P.rcount[l], (KT *)r0, (KT *)r1);
-      fill<<<fgrid, 256, 0, gs>>>(P.cls[l], rl, rlb, rlc, P.rw[l], P.rbase[l], P.rcount[l], v.n1, v.n2, v.n3, u0,
-                                  u1, (KT *)r0, (KT *)r1);
     };
     if (P.kdt == MLPCG_BF16) {
-      if (b1 >= 0) launch(k_kgen_list<__nv_bfloat16, 2>, k_fill_uniform<__nv_bfloat16, 2>, K0, K1);
-      else launch(k_kgen_list<__nv_bfloat16, 1>, k_fill_uniform<__nv_bfloat16, 1>, K0, nullptr);
+      if (b1 >= 0) launch(k_kgen_list<__nv_bfloat16, 2>, k_fill_runs<__nv_bfloat16, 2>, K0, K1);
+      else launch(k_kgen_list<__nv_bfloat16, 1>, k_fill_runs<__nv_bfloat16, 1>, K0, nullptr);
     } else {
-      if (b1 >= 0) launch(k_kgen_list<float, 2>, k_fill_uniform<float, 2>, K0, K1);
-      else launch(k_kgen_list<float, 1>, k_fill_uniform<float, 1>, K0, nullptr);
+      if (b1 >= 0) launch(k_kgen_list<float, 2>, k_fill_runs<float, 2>, K0, K1);
+      else launch(k_kgen_list<float, 1>, k_fill_runs<float, 1>, K0, nullptr);
     }
     MLPCG_LAUNCH_CHECK();
     return MLPCG_OK;
@@ -2468,19 +2604,19 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
     const uint32_t *lb = P.gbaseT[l] + v.ntiles - 1, *lc = P.gcountT[l] + v.ntiles - 1;
     const uint32_t *rlb = P.rbaseT[l] + v.ntiles - 1, *rlc = P.rcountT[l] + v.ntiles - 1;
     const float *kf = P.Uall + (size_t)uf * 3 * KREC, *kt = P.Uall + (size_t)ut * 3 * KREC;
-    const int fgrid = (int)std::min<int64_t>((int64_t)sm_count() * 8, (v.n + 255) / 256);
+    const int fgrid = (int)std::min<int64_t>((int64_t)sm_count() * 8, (27 * (v.n / 8) + 255) / 256);
     auto launch = [&](auto kern, auto fill, auto *kf_rec, auto *kt_rec) {
+      fill<<<fgrid, 256, 0, st>>>(P.clsT[l], P.rlist, rlb, rlc, P.rwT[l], P.rbaseT[l], P.rcountT[l], v.n2, v.n3, kt,
+                                  kt, kt_rec, kt_rec);
       const int grid = (int)std::min<int64_t>((int64_t)sm_count() * resident_ctas(kern), (v.n + PT - 1) / PT);
       kern<<<grid, PT, 0, st>>>(v.n1, v.n2, v.n3, P.glist, lb, lc, P.cls[l], P.rw[l], P.rbase[l], P.rcount[l], kf_rec,
                                 kf, P.rwT[l], P.rbaseT[l], P.rcountT[l], kt_rec);
-      fill<<<fgrid, 256, 0, st>>>(P.clsT[l], P.rlist, rlb, rlc, P.rwT[l], P.rbaseT[l], P.rcountT[l], v.n1, v.n2, v.n3,
-                                  kt, kt, kt_rec, kt_rec);
     };
     if (P.kdt == MLPCG_BF16)
-      launch(k_kgen_t_list<__nv_bfloat16>, k_fill_uniform<__nv_bfloat16, 1>, (const __nv_bfloat16 *)Kf,
+      launch(k_kgen_t_list<__nv_bfloat16>, k_fill_runs<__nv_bfloat16, 1>, (const __nv_bfloat16 *)Kf,
              (__nv_bfloat16 *)Kt);
     else
-      launch(k_kgen_t_list<float>, k_fill_uniform<float, 1>, (const float *)Kf, (float *)Kt);
+      launch(k_kgen_t_list<float>, k_fill_runs<float, 1>, (const float *)Kf, (float *)Kt);
     MLPCG_LAUNCH_CHECK();
     return MLPCG_OK;
   };
