@@ -276,6 +276,12 @@ def run_ours(args, rank, world):
         tuned = autotune.tune_solver(solver, b, reps=5, cache_path=cache, retune=True)
         tuned = {"solver_ctas": tuned, "ms_by_ctas": autotune.load_cache(cache)[
             autotune.schedule_key(torch.cuda.get_device_properties(dev).name, solver.shape, solver.method)]["ms"]}
+        # the preconditioner's block schedule (small-level kernels, coarse cluster)
+        small, cluster = autotune.tune_plan(solver, b, reps=3, cache_path=cache, retune=True)
+        pk = autotune.plan_key(torch.cuda.get_device_properties(dev).name, solver.shape, plan.levels, "bfloat16",
+                               solver.method)
+        tuned.update({"small_level_tiles_per_sm": small, "coarse_cluster": bool(cluster),
+                      "ms_by_block_schedule": autotune.load_cache(cache)[pk]["ms"]})
         cache.unlink(missing_ok=True)
 
     def step(mid=None):

@@ -353,6 +353,14 @@ int mlpcg_precond_coarse_cluster(const mlpcg_precond *plan, int *first_level, in
  * stage's tiles share 16 SMs instead of spreading over the GPU, and each
  * stage still waits on its tiles' load -> compute chain). */
 int mlpcg_precond_set_coarse_cluster(mlpcg_precond *plan, int on);
+/* Block schedule of the plan's applications (no counterpart in the
+ * reference): a level whose tiles number at most tiles_per_sm per SM runs the
+ * block kernels that load each run's coefficients up front (BF16
+ * coefficients only; 0 = never; default 2).  Same outputs either way; picked
+ * per device and grid by mlpcg_gb300.autotune.  A solver bound to the plan
+ * picks the change up once its graph is recaptured (mlpcg_solver_set_schedule
+ * recaptures it). */
+int mlpcg_precond_set_small_levels(mlpcg_precond *plan, int tiles_per_sm);
 /* Test knob of the bounded TMA waits (no counterpart in the reference):
  * with on != 0 the level-0 tile kernels first wait on a barrier that nothing
  * arrives on (256 polls), so the wait runs out on an ordinary copy, whose

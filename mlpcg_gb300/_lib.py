@@ -49,6 +49,7 @@ _PROTOS = {
     "mlpcg_precond_set_copy_stall": (_i, [_vp, _i, _vp]),
     "mlpcg_precond_coarse_cluster": (_i, [_vp, _vp, _vp]),
     "mlpcg_precond_set_coarse_cluster": (_i, [_vp, _i]),
+    "mlpcg_precond_set_small_levels": (_i, [_vp, _i]),
     "mlpcg_precond_class_counts": (_i, [_vp, _i, _vp, _vp, _vp]),
     "mlpcg_precond_class_counts_transposed": (_i, [_vp, _i, _vp, _vp, _vp]),
     "mlpcg_precond_workspace": (_sz, [_vp]),

@@ -1,11 +1,18 @@
 """Schedule autotuning for the fused solver.
 
-The solver's grid-stride kernels (dot products, q-form, SpMV, update, true
-residual) run a fixed number of 256-thread CTAs; the best count depends on the
-grid size and the device.  ``tune_solver`` times whole solves for a set of
-candidate counts (multiples of the SM count) with CUDA events and applies the
-fastest; choices are cached in a JSON file keyed by device name, grid shape and
-method, so a later process applies them without timing.
+Two schedules, each tuned by timing whole solves with CUDA events and cached
+in a JSON file so that a later process applies the choice without timing:
+
+* ``tune_solver``: the number of 256-thread CTAs of the solver's grid-stride
+  kernels (dot products, q-form, SpMV, update, true residual), candidates 1-8
+  per SM; keyed by device name, grid shape and method.
+* ``tune_plan``: the preconditioner's block schedule -- from how many tiles per
+  SM down a level runs the block kernels that load each run's coefficients up
+  front (0, 1, 2 or 4), and whether the coarse levels run as one thread-block
+  cluster launch; keyed by device name, grid shape, levels, coefficient dtype
+  and method.  Every choice gives the same outputs.
+
+The block kernels' tile shape (2 x 16 x 64) is fixed at build time.
 """
 from __future__ import annotations
 
@@ -102,5 +109,51 @@ def tune_solver(solver, b: torch.Tensor | None = None, reps: int = 5, cache_path
     best = pick_best(timings)
     set_schedule(solver, best)
     cache[key] = {"blocks": best, "ms": {str(k): round(v, 4) for k, v in timings.items()}}
+    save_cache(cache, cache_path)
+    return best
+
+
+def plan_key(device_name: str, shape, levels: int, dtype: str, method: str) -> str:
+    return f"plan|{device_name}|{'x'.join(str(int(v)) for v in shape)}|L{int(levels)}|{dtype}|{method}"
+
+
+def plan_candidates(cluster_available: bool):
+    """(small-level tiles per SM, coarse cluster) pairs to try."""
+    out = [(k, 0) for k in (0, 1, 2, 4)]
+    if cluster_available:
+        out += [(k, 1) for k in (0, 2)]
+    return out
+
+
+def apply_plan_schedule(solver, small: int, cluster: int) -> None:
+    solver.plan.set_small_levels(small)
+    solver.plan.set_coarse_cluster(bool(cluster))
+    set_schedule(solver, get_schedule(solver))  # recapture the solver's graph with the new launches
+
+
+def tune_plan(solver, b: torch.Tensor | None = None, reps: int = 5, cache_path: Path | None = None,
+              retune: bool = False, measure=None):
+    """Apply the fastest block schedule of the solver's preconditioner (cached); returns
+    (small-level tiles per SM, coarse cluster).  ``measure(solver, choice) -> ms`` replaces the
+    CUDA-event timing (for tests)."""
+    dev = solver.flags.device
+    props = torch.cuda.get_device_properties(dev)
+    plan = solver.plan
+    key = plan_key(props.name, solver.shape, plan.levels, str(plan.storage).replace("torch.", ""), solver.method)
+    cache = load_cache(cache_path)
+    if not retune and key in cache:
+        choice = tuple(cache[key]["choice"])
+        apply_plan_schedule(solver, *choice)
+        return choice
+    plan.set_coarse_cluster(True)
+    cluster_ok = plan.coarse_cluster()[0] > 0
+    b = solver.b if b is None else b
+    timings = {}
+    for choice in plan_candidates(cluster_ok):
+        apply_plan_schedule(solver, *choice)
+        timings[choice] = measure(solver, choice) if measure is not None else _time_solve(solver, b, reps)
+    best = min(sorted(timings), key=lambda c: timings[c])
+    apply_plan_schedule(solver, *best)
+    cache[key] = {"choice": list(best), "ms": {f"{k[0]},{k[1]}": round(v, 4) for k, v in timings.items()}}
     save_cache(cache, cache_path)
     return best

@@ -196,7 +196,7 @@ struct FieldGeom {
 // with v the image patch around the cell (v(s,m,n,o) = img(s, q + (m-1,n-1,o-1))),
 // the contraction of sm_block_3d_kernel.cu:53-64.
 //
-// Three forms, chosen per cell:
+// Two forms, chosen per cell:
 // * material form, when each of the 27 positions of the patch holds one of the
 //   three one-hot materials of the image channels [air, fluid, non-solid]
 //   (lib/read_data.py:35-39): solid or outside the grid (0,0,0), air (1,0,1),
@@ -206,14 +206,9 @@ struct FieldGeom {
 //   acc[p] = bias[p] + sum over the 27 positions, in position order, of the
 //   entry of the position's material: 27 additions instead of 81 products.
 //   Every cell of a finest-level image made from flags takes this form.
-// * two-channel form, when the non-solid channel equals air + fluid (exactly,
-//   in FP32) at every position -- the coarse levels' images, averages of the
-//   one-hot channels: the same table weighted by the position's air and fluid
-//   values, acc[p] = bias[p] + sum over positions of
-//   a * Wm[air][pos][p] + f * Wm[fluid][pos][p] (54 products instead of 81);
-// * product form otherwise: bias, then the 81 products in the reference's
-//   loop order (s, m, n, o).
-// All forms add in FP32 (round to nearest); their sums differ from the
+// * product form otherwise (the coarse levels' averaged images): bias, then
+//   the 81 products in the reference's loop order (s, m, n, o).
+// Both forms add in FP32 (round to nearest); their sums differ from the
 // reference's sequence only by rounding.  Every kernel that produces
 // coefficients (dense planes, classed records, the uniform vectors of the
 // classed layout) goes through these definitions, so equal patches give
@@ -248,14 +243,12 @@ __device__ __forceinline__ void coeffs_of_patch_n(const float4 *sW, const float4
 #pragma unroll
     for (int p = 0; p < 28; ++p) acc[b][p] = sb[b * 28 + p];
   uint64_t mats = 0;
-  bool material = true, two = true;
+  bool material = true;
 #pragma unroll
   for (int pos = 0; pos < 27; ++pos) {
     const int m = pos / 9, nn = (pos / 3) % 3, o = pos % 3;
-    const float a = v(0, m, nn, o), f = v(1, m, nn, o), sn = v(2, m, nn, o);
-    const int mt = patch_material(a, f, sn);
+    const int mt = patch_material(v(0, m, nn, o), v(1, m, nn, o), v(2, m, nn, o));
     material = material && mt != 3;
-    two = two && sn == __fadd_rn(a, f);
     mats |= (uint64_t)(mt & 3) << (2 * pos);
   }
   if (material) {
@@ -272,28 +265,6 @@ __device__ __forceinline__ void coeffs_of_patch_n(const float4 *sW, const float4
           acc[b][4 * pp + 1] = __fadd_rn(acc[b][4 * pp + 1], wv.y);
           acc[b][4 * pp + 2] = __fadd_rn(acc[b][4 * pp + 2], wv.z);
           acc[b][4 * pp + 3] = __fadd_rn(acc[b][4 * pp + 3], wv.w);
-        }
-      }
-    }
-    return;
-  }
-  if (two) {
-    // averaged one-hot channels (non-solid = air + fluid at every position, exactly): the three
-    // products of a position are a * Wm[air] + f * Wm[fluid]
-#pragma unroll
-    for (int pos = 0; pos < 27; ++pos) {
-      const int m = pos / 9, nn = (pos / 3) % 3, o = pos % 3;
-      const float a = v(0, m, nn, o), f = v(1, m, nn, o);
-#pragma unroll
-      for (int b = 0; b < NB; ++b) {
-        const float4 *wa = sWm + b * kSW + (27 + pos) * 7, *wf = sWm + b * kSW + (54 + pos) * 7;
-#pragma unroll
-        for (int pp = 0; pp < 7; ++pp) {
-          const float4 va = wa[pp], vf = wf[pp];
-          acc[b][4 * pp + 0] = fmaf(vf.x, f, fmaf(va.x, a, acc[b][4 * pp + 0]));
-          acc[b][4 * pp + 1] = fmaf(vf.y, f, fmaf(va.y, a, acc[b][4 * pp + 1]));
-          acc[b][4 * pp + 2] = fmaf(vf.z, f, fmaf(va.z, a, acc[b][4 * pp + 2]));
-          acc[b][4 * pp + 3] = fmaf(vf.w, f, fmaf(va.w, a, acc[b][4 * pp + 3]));
         }
       }
     }

@@ -1628,6 +1628,7 @@ struct PrecondPlan {
   float *scratch = nullptr;   // 81 floats (linear means)
   int *err = nullptr;         // set to 1 by a level-0 TMA tile copy that did not complete
   bool coarse_cluster = false; // SM kind: the coarse levels in one cluster launch (off: slower, see notes)
+  int small_tiles_per_sm = 2;  // a level with at most this many tiles per SM runs the prefetching kernels
   size_t bytes = 0;
   bool ready = false;
 };
@@ -2166,18 +2167,19 @@ static int cluster_ctas_for(const PrecondPlan &P) {
   return cls ? coarse_cluster_ctas<KT, AT, true, false>() : coarse_cluster_ctas<KT, AT, false, false>();
 }
 
-// The small levels (their tiles fit in one wave of CTAs) run the block kernels' prefetching
-// variant when the coefficients are BF16.
+// The small levels (their tiles fit in one wave of CTAs: at most P.small_tiles_per_sm per SM)
+// run the block kernels' prefetching variant when the coefficients are BF16.
 template <typename KT>
-static bool small_level(const PrecondPlan::Level &v) {
-  return std::is_same<KT, __nv_bfloat16>::value && v.ntiles <= 2u * (unsigned)sm_count();
+static bool small_level(const PrecondPlan &P, const PrecondPlan::Level &v) {
+  return std::is_same<KT, __nv_bfloat16>::value &&
+         v.ntiles <= (unsigned)P.small_tiles_per_sm * (unsigned)sm_count();
 }
 
 template <typename KT, typename AT, bool POOL, bool CLS>
-static void launch_pre_level(const PrecondPlan::Level &v, const CoefArgs<KT> &C, const AT *x, AT *y, AT *yp,
-                             cudaStream_t st, const int *gate) {
+static void launch_pre_level(const PrecondPlan &P, const PrecondPlan::Level &v, const CoefArgs<KT> &C, const AT *x,
+                             AT *y, AT *yp, cudaStream_t st, const int *gate) {
   if constexpr (std::is_same<KT, __nv_bfloat16>::value) {
-    if (small_level<KT>(v)) {
+    if (small_level<KT>(P, v)) {
       k_pre_fused_small<KT, AT, AT, POOL, CLS><<<grid_of(v), PT, 0, st>>>(C, x, y, yp, v.n1, v.n2, v.n3, gate);
       return;
     }
@@ -2187,10 +2189,11 @@ static void launch_pre_level(const PrecondPlan::Level &v, const CoefArgs<KT> &C,
 }
 
 template <typename KT, typename AT, bool SWAP, bool CLS>
-static void launch_post_level(const PrecondPlan::Level &v, const CoefArgs<KT> &C, const AT *xc, const AT *yl,
-                              const float *c0, const float *c1, AT *o, cudaStream_t st, const int *gate) {
+static void launch_post_level(const PrecondPlan &P, const PrecondPlan::Level &v, const CoefArgs<KT> &C,
+                              const AT *xc, const AT *yl, const float *c0, const float *c1, AT *o, cudaStream_t st,
+                              const int *gate) {
   if constexpr (std::is_same<KT, __nv_bfloat16>::value) {
-    if (small_level<KT>(v)) {
+    if (small_level<KT>(P, v)) {
       k_post_fused_small<KT, AT, SWAP, CLS><<<grid_of(v), PT, 0, st>>>(C, xc, yl, c0, c1, o, v.n1, v.n2, v.n3,
                                                                          gate);
       return;
@@ -2220,9 +2223,9 @@ static int run_apply(const PrecondPlan &P, const float *r, const float *rscale, 
         RET_IF((launch_pre0<KT, AT>(P, C, r, rscale, (AT *)P.y[0], (AT *)P.xin[1], m0, st, gate)));
       } else {
         if (v.cls)
-          launch_pre_level<KT, AT, true, true>(v, C, (const AT *)P.xin[l], (AT *)P.y[l], (AT *)P.xin[l + 1], st, gate);
+          launch_pre_level<KT, AT, true, true>(P, v, C, (const AT *)P.xin[l], (AT *)P.y[l], (AT *)P.xin[l + 1], st, gate);
         else
-          launch_pre_level<KT, AT, true, false>(v, C, (const AT *)P.xin[l], (AT *)P.y[l], (AT *)P.xin[l + 1], st,
+          launch_pre_level<KT, AT, true, false>(P, v, C, (const AT *)P.xin[l], (AT *)P.y[l], (AT *)P.xin[l + 1], st,
                                                 gate);
       }
       MLPCG_LAUNCH_CHECK();
@@ -2250,8 +2253,8 @@ static int run_apply(const PrecondPlan &P, const float *r, const float *rscale, 
     AT *cdst = (AT *)(spd ? P.xtmp : P.xout[L]);
     if (v.fast) {
       const CoefArgs<KT> C = coef_args<KT>(P, L, P.Kl, v.cls ? P.Ul : nullptr);
-      if (v.cls) launch_pre_level<KT, AT, false, true>(v, C, (const AT *)P.xin[L], cdst, nullptr, st, gate);
-      else launch_pre_level<KT, AT, false, false>(v, C, (const AT *)P.xin[L], cdst, nullptr, st, gate);
+      if (v.cls) launch_pre_level<KT, AT, false, true>(P, v, C, (const AT *)P.xin[L], cdst, nullptr, st, gate);
+      else launch_pre_level<KT, AT, false, false>(P, v, C, (const AT *)P.xin[L], cdst, nullptr, st, gate);
       MLPCG_LAUNCH_CHECK();
       if (spd) {
         const CoefArgs<KT> Ct = coef_args_t<KT>(P, L, P.Klt, v.cls ? P.Ult : nullptr);
@@ -2330,11 +2333,11 @@ static int run_apply(const PrecondPlan &P, const float *r, const float *rscale, 
       } else {
         AT *o = (AT *)P.xout[l];
         if (P.swap) {
-          if (v.cls) launch_post_level<KT, AT, true, true>(v, C, xc, yl, c0, c1, o, st, gate);
-          else launch_post_level<KT, AT, true, false>(v, C, xc, yl, c0, c1, o, st, gate);
+          if (v.cls) launch_post_level<KT, AT, true, true>(P, v, C, xc, yl, c0, c1, o, st, gate);
+          else launch_post_level<KT, AT, true, false>(P, v, C, xc, yl, c0, c1, o, st, gate);
         } else {
-          if (v.cls) launch_post_level<KT, AT, false, true>(v, C, xc, yl, c0, c1, o, st, gate);
-          else launch_post_level<KT, AT, false, false>(v, C, xc, yl, c0, c1, o, st, gate);
+          if (v.cls) launch_post_level<KT, AT, false, true>(P, v, C, xc, yl, c0, c1, o, st, gate);
+          else launch_post_level<KT, AT, false, false>(P, v, C, xc, yl, c0, c1, o, st, gate);
         }
       }
       MLPCG_LAUNCH_CHECK();
@@ -2633,7 +2636,11 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
   } else if (P.kind == MLPCG_PRECOND_SM && P.glist2) {
     // levels >= 1 and then every level's c0 / c1 on the side stream, level 0 on the caller's
     if (!P.side) {
-      MLPCG_CUDA_CHECK(cudaStreamCreateWithFlags(&P.side, cudaStreamNonBlocking));
+      // the side chain's kernels are small and latency-bound: the highest priority lets their CTAs
+      // start as soon as level 0's free a slot
+      int lo = 0, hi = 0;
+      MLPCG_CUDA_CHECK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+      MLPCG_CUDA_CHECK(cudaStreamCreateWithPriority(&P.side, cudaStreamNonBlocking, hi));
       MLPCG_CUDA_CHECK(cudaEventCreateWithFlags(&P.fork_ev, cudaEventDisableTiming));
       MLPCG_CUDA_CHECK(cudaEventCreateWithFlags(&P.join_ev, cudaEventDisableTiming));
     }
@@ -2760,6 +2767,15 @@ int mlpcg_precond_check(const mlpcg_precond *h, int *copy_failed, void *stream) 
   MLPCG_CUDA_CHECK(cudaMemcpyAsync(&v, h->p.err, sizeof(int), cudaMemcpyDeviceToHost, st));
   MLPCG_CUDA_CHECK(cudaStreamSynchronize(st));
   *copy_failed = v;
+  return MLPCG_OK;
+}
+
+int mlpcg_precond_set_small_levels(mlpcg_precond *h, int tiles_per_sm) {
+  clear_error();
+  MLPCG_REQUIRE(h, MLPCG_ERR_ARG, "precond_set_small_levels: NULL plan");
+  MLPCG_REQUIRE(tiles_per_sm >= 0 && tiles_per_sm <= 64, MLPCG_ERR_ARG,
+                "precond_set_small_levels: tiles_per_sm %d out of [0, 64]", tiles_per_sm);
+  h->p.small_tiles_per_sm = tiles_per_sm;
   return MLPCG_OK;
 }
 

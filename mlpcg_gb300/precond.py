@@ -165,6 +165,11 @@ class PrecondPlan:
         (mlpcg_precond_set_coarse_cluster); the outputs are the same."""
         call("mlpcg_precond_set_coarse_cluster", self._h, int(bool(on)))
 
+    def set_small_levels(self, tiles_per_sm: int):
+        """Levels with at most ``tiles_per_sm`` tiles per SM run the prefetching block kernels
+        (mlpcg_precond_set_small_levels; 0 = never); the outputs are the same."""
+        call("mlpcg_precond_set_small_levels", self._h, int(tiles_per_sm))
+
     def set_copy_stall(self, on: bool):
         """Test knob of the bounded TMA waits (mlpcg_precond_set_copy_stall): with ``on`` the level-0
         tile kernels' first wait runs out on an ordinary copy and ``copy_failed()`` turns true; every

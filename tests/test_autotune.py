@@ -57,3 +57,45 @@ def test_tune_solver_applies_and_caches(cuda, tmp_path):
     assert autotune.tune_solver(solver, b, cache_path=cache, measure=lambda *a: 1 / 0) == best
     # the real timing path runs too
     assert autotune.tune_solver(solver, b, cache_path=cache, retune=True, reps=1) in autotune.candidates(n_sm)
+
+
+def test_plan_candidates_and_key():
+    assert autotune.plan_candidates(False) == [(0, 0), (1, 0), (2, 0), (4, 0)]
+    assert autotune.plan_candidates(True)[-2:] == [(0, 1), (2, 1)]
+    assert autotune.plan_key("NVIDIA GB300", (256, 256, 256), 5, "bfloat16", "npsd") == \
+        "plan|NVIDIA GB300|256x256x256|L5|bfloat16|npsd"
+
+
+@pytest.mark.gpu
+def test_tune_plan_applies_caches_and_keeps_results(cuda, tmp_path):
+    """Every block schedule gives the same solve bit for bit; the chosen one is applied and cached."""
+    import torch
+    from mlpcg_gb300.scenes import make_scene
+    from mlpcg_gb300.sm_model_3d import SmallSMModelDn3D
+    from mlpcg_gb300.solver import FusedSolver
+    s = make_scene((128, 128, 128), 3)
+    torch.manual_seed(0)
+    m = SmallSMModelDn3D(4, 3, "trilinear").to(cuda)
+    with torch.no_grad():
+        for p in m.parameters():
+            p.mul_(0.05)
+        m.pre[0].bias[13] += 1.0
+        m.c0[0].bias[0] += 1.0
+    solver = FusedSolver(m, torch.as_tensor(s.flags, device=cuda), method="npsd", max_it=40, tol=1e-6)
+    b = torch.as_tensor(s.rhs, device=cuda)
+    ref = solver.solve(b)
+    xref = ref.x.clone()
+    seen = []
+
+    def measure(sv, choice):
+        r = sv.solve(b)
+        assert r.iterations == ref.iterations and torch.equal(r.x, xref), choice
+        seen.append(choice)
+        return 1.0 if choice == (1, 0) else 2.0
+
+    cache = tmp_path / "plan.json"
+    best = autotune.tune_plan(solver, b, cache_path=cache, measure=measure)
+    assert best == (1, 0) and (2, 0) in seen and (0, 0) in seen
+    assert autotune.tune_plan(solver, b, cache_path=cache, measure=lambda *a: 1 / 0) == best
+    r = solver.solve(b)
+    assert torch.equal(r.x, xref)
