@@ -186,6 +186,43 @@ def stencil_apply(K, x, dims, transpose=False, out_dtype=torch.float32):
     return y
 
 
+def coeff_grad(grad_out, x, dims, transpose=False):
+    """dK (27 planes, FP32): the gradient of the block output with respect to its coefficients,
+    dK_p(q) = sum_b g_b(q) x_b(q + off_p) (transposed: the adjoint relation)."""
+    _check(grad_out, "grad_output")
+    _check(x, "x")
+    n = math.prod(dims)
+    if grad_out.numel() != x.numel() or x.numel() % n:
+        raise RuntimeError(f"grad_output and x must hold the same whole number of {tuple(dims)} grids")
+    ps = plane_stride(n)
+    dK = torch.empty((27, ps), dtype=torch.float32, device=x.device)
+    call("mlpcg_stencil_coeff_grad", _p(grad_out), _p(x), 0, _p(dK), ps, x.numel() // n, *dims, int(transpose),
+         _stream(x.device))
+    return dK
+
+
+def weight_grad(dK, image):
+    """(grad_weight (27, 3, 3, 3, 3), grad_bias (27)) from the coefficient gradient dK."""
+    _check(dK, "dK")
+    _check(image, "image")
+    dims = _spatial(image, False)
+    gw = torch.empty((27, 3, 3, 3, 3), dtype=torch.float32, device=image.device)
+    gb = torch.empty((27,), dtype=torch.float32, device=image.device)
+    ws = _workspace(query("mlpcg_stencil_wgrad_workspace", *dims), image.device)
+    call("mlpcg_stencil_wgrad", _p(dK), dK.shape[-1], _p(image), 0, *dims, _p(gw), _p(gb), _p(ws), ws.numel(),
+         _stream(image.device))
+    return gw, gb
+
+
+def image_grad(dK, weight, dims):
+    """grad_image (3, N1, N2, N3) from the coefficient gradient dK."""
+    _check(dK, "dK")
+    _check(weight, "weight")
+    gi = torch.empty((3,) + tuple(dims), dtype=torch.float32, device=dK.device)
+    call("mlpcg_stencil_image_grad", _p(dK), dK.shape[-1], _p(weight), _p(gi), *dims, _stream(dK.device))
+    return gi
+
+
 # ----------------------------------------------------------------------------
 # level transfer
 # ----------------------------------------------------------------------------

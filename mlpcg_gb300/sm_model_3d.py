@@ -68,6 +68,55 @@ class SMBlockFunction3D(torch.autograd.Function):
         return gi, gx, gw, gb
 
 
+class SMBlockBF16Function3D(torch.autograd.Function):
+    """The block (or its transpose) for training with BF16 storage: the coefficient planes and the
+    input saved for the backward pass in BF16, every sum accumulated in FP32, outputs and gradients
+    in FP32.  Backward through the same adjoint kernels as SMBlockFunction3D: dx by the transposed
+    application of the BF16 planes, dK from the FP32 output gradient and the saved input, dW / db
+    and the image gradient from dK (sm_block_3d_kernel.cu:122-326)."""
+
+    @staticmethod
+    def forward(ctx, image, x, weights, bias, transpose):
+        dims = tuple(image.shape[1:])
+        K = ops.stencil_gen(image, weights, bias, dtype=torch.bfloat16)
+        xb = x.contiguous().to(torch.bfloat16)
+        y = ops.stencil_apply(K, xb, dims, transpose=transpose)
+        ctx.save_for_backward(image, xb, weights, bias)
+        ctx.transpose = transpose
+        return y.reshape(x.shape)
+
+    @staticmethod
+    def backward(ctx, grad_output):
+        image, xb, weights, bias = ctx.saved_tensors
+        dims = tuple(image.shape[1:])
+        g = grad_output.contiguous()
+        K = ops.stencil_gen(image, weights, bias, dtype=torch.bfloat16)
+        gx = ops.stencil_apply(K, g, dims, transpose=not ctx.transpose)
+        dK = ops.coeff_grad(g, xb.float(), dims, transpose=ctx.transpose)
+        gw, gb = ops.weight_grad(dK, image)
+        gi = ops.image_grad(dK, weights, dims) if ctx.needs_input_grad[0] else None
+        return gi, gx.reshape(g.shape), gw, gb, None
+
+
+def set_training_storage(model, dtype=torch.bfloat16):
+    """Every block of ``model`` trains with BF16 coefficient planes and BF16 saved inputs
+    (torch.bfloat16; FP32 accumulation) or in FP32 (torch.float32, the default).  Inference
+    (eval_forward, the fused plans) is unaffected."""
+    if dtype not in (torch.float32, torch.bfloat16):
+        raise ValueError(f"training storage must be torch.float32 or torch.bfloat16 (got {dtype})")
+    for m in model.modules():
+        if isinstance(m, (SmallSMBlock3D, SmallSMBlockTrans3D)):
+            m.storage = dtype
+    return model
+
+
+def _block_apply(module, image, x, transpose):
+    if getattr(module, "storage", torch.float32) == torch.bfloat16 and torch.is_grad_enabled():
+        return SMBlockBF16Function3D.apply(image, x, module.weight, module.bias, transpose)
+    fn = SMBlockTransFunction3D if transpose else SMBlockFunction3D
+    return fn.apply(image, x, module.weight, module.bias)
+
+
 class SMBlockTransFunction3D(torch.autograd.Function):
     """Transpose of SMBlockFunction3D (sm_model_3d.py:50-76)."""
 
@@ -103,7 +152,7 @@ class SmallSMBlock3D(BaseModel):
         self.reset_parameters(self.weight, self.bias)
 
     def forward(self, image, x):
-        y = SMBlockFunction3D.apply(image, x, self.weight, self.bias)
+        y = _block_apply(self, image, x, False)
         if self.mask:
             y = torch.where(image[1] == 0, 0.0, y)
         return y
@@ -126,7 +175,7 @@ class SmallSMBlockTrans3D(BaseModel):
             self.reset_parameters(self.weight, self.bias)
 
     def forward(self, image, x):
-        return SMBlockTransFunction3D.apply(image, x, self.weight, self.bias)
+        return _block_apply(self, image, x, True)
 
     def eval_forward(self, image, x, timer=None):
         return SMBlockTransFunction3D.inference(image, x, self.weight, self.bias, timer)

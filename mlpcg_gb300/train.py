@@ -31,7 +31,7 @@ from . import ops
 from .laplacian import FluidLaplacian
 from .lanczos import lanczos_ritz, mix_rhs
 from .scenes import make_scene
-from .sm_model_3d import SmallSMModelDn3D, SmallSPDSMModelDn3D, SPDSMModelDn3D
+from .sm_model_3d import SmallSMModelDn3D, SmallSPDSMModelDn3D, SPDSMModelDn3D, set_training_storage
 
 MODELS = {"smallsm": "smallsm", "small_spd": "smallspd", "spd": "spd"}   # --model -> weight file prefix
 
@@ -228,6 +228,8 @@ def main(argv=None):
     ap.add_argument("--harvest-every", type=int, default=250, help="0 disables solver-in-the-loop rhs")
     ap.add_argument("--harvest-frac", type=float, default=0.25)
     ap.add_argument("--init", default=None, help="npz state dict to start from")
+    ap.add_argument("--storage", default="fp32", choices=["fp32", "bf16"],
+                    help="block storage in training: BF16 coefficient planes and saved inputs, FP32 sums")
     ap.add_argument("--recompute", action="store_true",
                     help="recompute per-level activations in the backward pass (large grids, SmallSMModelDn3D)")
     ap.add_argument("--time-limit", type=float, default=1e9, help="seconds of training loop at most")
@@ -241,6 +243,8 @@ def main(argv=None):
     model = make_model(args.model, args.levels).to(dev)
     if args.recompute:
         model.recompute = True
+    if args.storage == "bf16":
+        set_training_storage(model, torch.bfloat16)
     if args.init:
         d = np.load(args.init)
         model.load_state_dict({k: torch.from_numpy(d[k]) for k in model.state_dict()})

@@ -132,3 +132,54 @@ def test_residual_loss_reference_kind_matches_the_reference(golden, cuda):
     loss = float(loss_of_outputs(xg.reshape(shp), yg.reshape(shp), flags, kind="reference"))
     assert loss == pytest.approx(float(d["loss_mean"]), rel=1e-12)
     assert loss * B == pytest.approx(float(d["loss_sum"]), rel=1e-12)
+
+
+def test_bf16_training_storage(cuda):
+    """Training with BF16 block storage (coefficient planes and saved inputs in BF16, FP32 sums):
+    the forward output and every gradient (input, image, parameters) agree with the FP32 training
+    path within BF16 rounding, the saved activations shrink, and a few optimiser steps reduce the
+    loss as in FP32."""
+    from mlpcg_gb300.sm_model_3d import SmallSMModelDn3D, set_training_storage
+    from mlpcg_gb300.train import TrainScene, residual_loss
+    torch.manual_seed(0)
+    model = SmallSMModelDn3D(3, 3, "trilinear").to(cuda)
+    shape = (32, 32, 32)
+    torch.manual_seed(1)
+    img = (torch.rand((3,) + shape, device=cuda) > 0.5).float()
+    b0 = torch.randn((4, 1) + shape, device=cuda)
+    g = torch.randn_like(b0)
+    out = {}
+    for dt in (torch.float32, torch.bfloat16):
+        set_training_storage(model, dt)
+        model.zero_grad(set_to_none=True)
+        b = b0.clone().requires_grad_(True)
+        im = img.clone().requires_grad_(True)
+        y = model(im, b)
+        (y * g).sum().backward()
+        out[dt] = (y.detach(), b.grad, im.grad, {k: p.grad.clone() for k, p in model.named_parameters()})
+    set_training_storage(model, torch.float32)
+    (y0, gb0, gi0, gp0), (y1, gb1, gi1, gp1) = out[torch.float32], out[torch.bfloat16]
+
+    def rel(a, b):
+        return float((a - b).norm() / b.norm())
+    assert rel(y1, y0) < 2e-2 and rel(gb1, gb0) < 2e-2 and rel(gi1, gi0) < 3e-2
+    for k in gp0:
+        assert rel(gp1[k], gp0[k]) < 3e-2, (k, rel(gp1[k], gp0[k]))
+    with pytest.raises(ValueError):
+        set_training_storage(model, torch.float16)
+    # a few steps reduce the loss
+    set_training_storage(model, torch.bfloat16)
+    sc = TrainScene(shape, 10, cuda, n_ritz=16, lanczos_steps=80)
+    opt = torch.optim.Adam(model.parameters(), lr=3e-3)
+    gen = torch.Generator(device=cuda)
+    gen.manual_seed(0)
+    b = sc.batch(8, 0.25, gen)
+    first = None
+    for _ in range(30):
+        loss = residual_loss(model, sc.image, sc.flags, sc.fluid, b)
+        first = float(loss) if first is None else first
+        opt.zero_grad()
+        loss.backward()
+        opt.step()
+    set_training_storage(model, torch.float32)
+    assert float(loss) < 0.8 * first
