@@ -426,6 +426,31 @@ int mlpcg_solver_result(const mlpcg_solver *solver, int *iterations, int *status
 int mlpcg_solver_set_schedule(mlpcg_solver *solver, int blocks);
 int mlpcg_solver_get_schedule(const mlpcg_solver *solver, int *blocks_in_use);
 
+/* Programmatic dependent launch in the captured iteration (no counterpart in
+ * the reference; on by default): consecutive kernels of the loop body are
+ * joined by programmatic edges, so a kernel's blocks are scheduled while its
+ * predecessor's last blocks run and wait on the device for its completion
+ * (measured 0.5 % faster at 256^3, 1 % at 128^3).  Results
+ * are identical either way.  Takes effect on the next solve (the graph is
+ * rebuilt); batches built from the solver follow its first solver's setting.
+ * If the runtime refuses such a graph, the solve captures ordinary edges.
+ * mlpcg_solver_dependent_edges reports the edges converted in the current
+ * graph (0 before the first graph solve or with the feature off). */
+int mlpcg_solver_set_dependent_launch(mlpcg_solver *solver, int on);
+int mlpcg_solver_dependent_edges(const mlpcg_solver *solver, int *edges);
+
+/* npsd products in the preconditioner (no counterpart in the reference; on by
+ * default): z.Ap_recent and z.Ap_previous (cg_tests.py:226-233) are summed by
+ * the plan's level-0 post-block while z is in registers, one FP64 partial per
+ * tile, and reduced by one block in a fixed order -- z is not read again.
+ * Applies to npsd solvers whose plan is the SmallSMModelDn3D kind with a
+ * TMA-staged finest level; the others sum them in a separate pass.  The two
+ * forms add the same products in different orders (FP64 partials either
+ * way).  Takes effect on the next solve; mlpcg_solver_fused_dots reports
+ * whether a bound solver uses the epilogue. */
+int mlpcg_solver_set_fused_dots(mlpcg_solver *solver, int on);
+int mlpcg_solver_fused_dots(const mlpcg_solver *solver, int *active);
+
 /* Test knob of the SpMV's bounded TMA waits (no counterpart in the
  * reference), taking effect from the next solve: with on != 0 the npsd
  * SpMV's first tile wait polls a barrier that nothing arrives on (256 polls)

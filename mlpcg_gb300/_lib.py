@@ -68,6 +68,10 @@ _PROTOS = {
     "mlpcg_solver_result": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "mlpcg_solver_set_schedule": (_i, [_vp, _i]),
     "mlpcg_solver_set_copy_stall": (_i, [_vp, _i]),
+    "mlpcg_solver_set_dependent_launch": (_i, [_vp, _i]),
+    "mlpcg_solver_dependent_edges": (_i, [_vp, _vp]),
+    "mlpcg_solver_set_fused_dots": (_i, [_vp, _i]),
+    "mlpcg_solver_fused_dots": (_i, [_vp, _vp]),
     "mlpcg_solver_get_schedule": (_i, [_vp, _vp]),
     "mlpcg_batch_create": (_i, [_vp, _i, _vp]),
     "mlpcg_batch_solve": (_i, [_vp, _vp]),

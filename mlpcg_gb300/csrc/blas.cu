@@ -30,6 +30,7 @@ __device__ __forceinline__ double block_sum(double v) {
 template <typename T>
 __global__ void __launch_bounds__(kDotThreads)
 k_dot_partial(const T *__restrict__ x, const T *__restrict__ y, int64_t n, double *__restrict__ partial) {
+  dependent_launch_enter();
   double acc = 0.0;
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
     acc = fma(ldd(x + q), ldd(y + q), acc);
@@ -38,6 +39,7 @@ k_dot_partial(const T *__restrict__ x, const T *__restrict__ y, int64_t n, doubl
 }
 
 __global__ void k_sum_partials(const double *__restrict__ partial, int nblk, double *__restrict__ out) {
+  dependent_launch_enter();
   double acc = 0.0;
   for (int b = threadIdx.x; b < nblk; b += blockDim.x) acc += partial[b];
   acc = block_sum(acc);

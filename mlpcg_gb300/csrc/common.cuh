@@ -48,6 +48,31 @@ inline size_t dtype_size(int dt) { return dt == MLPCG_F64 ? 8 : (dt == MLPCG_BF1
 __host__ __device__ inline int64_t cells(int n1, int n2, int n3) { return (int64_t)n1 * n2 * n3; }
 inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 
+// Optional epilogue of the finest post-block for the npsd solver: the products of
+// the new preconditioned residual z with the A-images of the two most recent
+// search directions, z . ring[head] and z . ring[(head + 2) % 3] (ring: three
+// slots of n floats; none at iteration 0, the first alone at iteration 1),
+// summed per tile of the finest level in FP64 into partial[2 * tile + k].
+// head and it are words of the solver's device state, read by the kernel.
+struct ZDots {
+  const float *ring;
+  const int *head, *it;
+  double *partial;
+  int64_t n;
+};
+
+// First statement of every kernel of this library.  A kernel reached through a
+// programmatic graph edge (the solver's captured iteration) may be scheduled
+// while its predecessor still runs: it waits here until the predecessor grid
+// has completed and its writes are visible, touching no memory before.
+// Launched any other way, the wait does nothing.  No kernel triggers its
+// successor early: the implicit trigger as its blocks exit lets the successor's
+// blocks be scheduled onto the SMs that free up, overlapping its launch with
+// the predecessor's last blocks.  (An explicit trigger at kernel entry was
+// measured slower at 256^3: the successor's blocks were placed early on the
+// first SMs to free up, unevenly.)
+__device__ __forceinline__ void dependent_launch_enter() { cudaGridDependencySynchronize(); }
+
 // ---------------------------------------------------------------------------
 // Double-float arithmetic: a value as the unevaluated sum hi + lo of two
 // floats, kept exact by error-free transformations (Knuth's two-sum, Dekker's

@@ -9,6 +9,7 @@ namespace mlpcg {
 // ---------------------------------------------------------------------------
 template <typename T>
 __global__ void k_avg_pool2(const T *__restrict__ x, T *__restrict__ y, int n1, int n2, int n3) {
+  dependent_launch_enter();
   const int c1 = n1 / 2, c2 = n2 / 2, c3 = n3 / 2;
   const int64_t nc = cells(c1, c2, c3);
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -32,6 +33,7 @@ __global__ void k_avg_pool2(const T *__restrict__ x, T *__restrict__ y, int n1, 
 
 template <typename T>
 __global__ void k_avg_pool2_adjoint(const T *__restrict__ y, T *__restrict__ x, int n1, int n2, int n3) {
+  dependent_launch_enter();
   const int64_t n = cells(n1, n2, n3);
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
@@ -69,6 +71,7 @@ __device__ __forceinline__ Lin1 lin1(int f, int n) {
 
 template <typename T>
 __global__ void k_upsample2(const T *__restrict__ x, T *__restrict__ y, int n1, int n2, int n3) {
+  dependent_launch_enter();
   const int f1 = 2 * n1, f2 = 2 * n2, f3 = 2 * n3;
   const int64_t nf = cells(f1, f2, f3);
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -94,6 +97,7 @@ __global__ void k_upsample2(const T *__restrict__ x, T *__restrict__ y, int n1, 
 // (clamped at the ends); gathering keeps the kernel deterministic.
 template <typename T>
 __global__ void k_upsample2_adjoint(const T *__restrict__ y, T *__restrict__ x, int n1, int n2, int n3) {
+  dependent_launch_enter();
   const int f1 = 2 * n1, f2 = 2 * n2, f3 = 2 * n3;
   const int64_t nc = cells(n1, n2, n3);
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -138,6 +142,7 @@ template <typename T>
 __global__ void k_axpby(const float *__restrict__ c0, const T *__restrict__ x,
                         const float *__restrict__ c1, const T *__restrict__ y, T *__restrict__ out,
                         int64_t n) {
+  dependent_launch_enter();
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
   const float a = __fmul_rn(c0[0], ldf(x + q));
@@ -168,6 +173,7 @@ __device__ __forceinline__ int axis_class(int c, int n) { return c == 0 ? 0 : (c
 // Deterministic: the row assignment and every reduction order are fixed.
 __global__ void __launch_bounds__(kLinThreads)
 k_class_sums(const float *__restrict__ img, int n1, int n2, int n3, float2 *__restrict__ partial) {
+  dependent_launch_enter();
   __shared__ float2 ws[kLinWarps][81];  // per warp: (class * 3 + channel)
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int e = lane; e < 81; e += 32) ws[w][e] = make_float2(0.f, 0.f);
@@ -233,6 +239,7 @@ k_class_sums(const float *__restrict__ img, int n1, int n2, int n3, float2 *__re
 // double-float, in a fixed order (thread t takes blocks t, t + 256, ..., then a fixed tree).
 __global__ void __launch_bounds__(256) k_linear_reduce(const float2 *__restrict__ partial, int nblk,
                                                        double *__restrict__ cs) {
+  dependent_launch_enter();
   __shared__ float2 ws[8];
   const int c = blockIdx.x, t = threadIdx.x;
   float2 v[(kLinBlocks + 255) / 256];
@@ -259,6 +266,7 @@ __global__ void k_linear_finalize(const double *__restrict__ cs_g, int n1, int n
                                   const float *__restrict__ W, int64_t wstride, const float *__restrict__ bias,
                                   int64_t bstride, int nlin, float *__restrict__ z, int64_t zstride,
                                   float *__restrict__ yout) {
+  dependent_launch_enter();
   __shared__ double cs[27 * 3];
   __shared__ double ym[81];
   const int t = threadIdx.x;
@@ -300,6 +308,7 @@ __global__ void k_linear_finalize(const double *__restrict__ cs_g, int n1, int n
 
 __global__ void k_linear_backward(const float *__restrict__ g, const float *__restrict__ y,
                                   float *__restrict__ gw, float *__restrict__ gb) {
+  dependent_launch_enter();
   const int t = threadIdx.x;
   if (t < 81) gw[t] = y[t] * g[0];
   if (t == 0) gb[0] = g[0];
@@ -308,6 +317,7 @@ __global__ void k_linear_backward(const float *__restrict__ g, const float *__re
 // d z / d img(s, c) = g/N * sum over shifts d with c - d in grid of w[s][d]
 __global__ void k_linear_image_grad(const float *__restrict__ g, const float *__restrict__ W, int n1,
                                     int n2, int n3, float *__restrict__ gimg) {
+  dependent_launch_enter();
   const int64_t n = cells(n1, n2, n3);
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
@@ -336,6 +346,7 @@ __global__ void k_linear_image_grad(const float *__restrict__ g, const float *__
 template <typename T>
 __global__ void k_laplacian(const uint8_t *__restrict__ flags, const T *__restrict__ x,
                             T *__restrict__ y, int n1, int n2, int n3) {
+  dependent_launch_enter();
   const int64_t n = cells(n1, n2, n3);
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
@@ -364,6 +375,7 @@ __global__ void k_laplacian(const uint8_t *__restrict__ flags, const T *__restri
 
 // [air, fluid, non-solid] channels from flag codes
 __global__ void k_flags_to_image(const uint8_t *__restrict__ flags, float *__restrict__ img, int64_t n) {
+  dependent_launch_enter();
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
   const uint8_t f = flags[q];
@@ -414,6 +426,7 @@ __device__ __forceinline__ unsigned fluid_bits(const uint8_t *__restrict__ flags
 
 __global__ void __launch_bounds__(kFluidThreads)
 k_fluid_counts(const uint8_t *__restrict__ flags, int64_t n, uint32_t *__restrict__ cnt) {
+  dependent_launch_enter();
   const int64_t q0 = (int64_t)blockIdx.x * kFluidBlock + kFluidPer * threadIdx.x;
   int tot;
   block256_excl_scan(__popc(fluid_bits(flags, n, q0)), tot);
@@ -425,6 +438,7 @@ k_fluid_counts(const uint8_t *__restrict__ flags, int64_t n, uint32_t *__restric
 __global__ void __launch_bounds__(kFluidThreads)
 k_scatter_fluid(const double *__restrict__ vals, int64_t m, const uint8_t *__restrict__ flags,
                 const uint32_t *__restrict__ base, int64_t n, double *__restrict__ grid) {
+  dependent_launch_enter();
   const int64_t q0 = (int64_t)blockIdx.x * kFluidBlock + kFluidPer * threadIdx.x;
   const unsigned fm = fluid_bits(flags, n, q0);
   int tot;
@@ -442,6 +456,7 @@ k_scatter_fluid(const double *__restrict__ vals, int64_t m, const uint8_t *__res
 __global__ void __launch_bounds__(kFluidThreads)
 k_gather_fluid(const double *__restrict__ grid, const uint8_t *__restrict__ flags,
                const uint32_t *__restrict__ base, int64_t n, double *__restrict__ vals, int64_t m) {
+  dependent_launch_enter();
   const int64_t q0 = (int64_t)blockIdx.x * kFluidBlock + kFluidPer * threadIdx.x;
   const unsigned fm = fluid_bits(flags, n, q0);
   int tot;

@@ -309,6 +309,7 @@ __global__ void __launch_bounds__(PT)
 k_classify(const float *__restrict__ img, const uint8_t *__restrict__ src_cls, int n1, int n2, int n3,
            uint8_t *__restrict__ cls, uint32_t *__restrict__ rw, uint32_t *__restrict__ rcount,
            uint32_t *__restrict__ gcount) {
+  dependent_launch_enter();
   __shared__ __align__(16) uint8_t M[HX][HY][HZP];
   const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY, x0 = blockIdx.z * TX;
   const int64_t n = cells(n1, n2, n3);
@@ -433,6 +434,7 @@ k_classify(const float *__restrict__ img, const uint8_t *__restrict__ src_cls, i
 // exclusive prefix sum of the tile counts (one CTA of 1024 threads)
 __global__ void __launch_bounds__(1024)
 k_scan_tiles(const uint32_t *__restrict__ cnt, uint32_t *__restrict__ base, int ntiles) {
+  dependent_launch_enter();
   __shared__ uint32_t ws[32];
   __shared__ uint32_t carry;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -486,6 +488,7 @@ __device__ __forceinline__ float round_as(const __nv_bfloat16 *, float v) {
 template <typename KT>
 __global__ void __launch_bounds__(3 * KREC)
 k_kgen_uniform_all(const float *__restrict__ params, float *__restrict__ kuni, int n, int kind) {
+  dependent_launch_enter();
   const int b = blockIdx.x, c = threadIdx.x / KREC, p = threadIdx.x % KREC;
   const float *W = params + (size_t)b * 2214, *bias = W + 2187;
   float acc = 0.f;
@@ -510,6 +513,7 @@ __global__ void __launch_bounds__(PT)
 k_list_general(const uint8_t *__restrict__ cls, int n1, int n2, int n3, const uint32_t *__restrict__ gbase,
                uint32_t *__restrict__ list, const uint32_t *__restrict__ rw, const uint32_t *__restrict__ rbase,
                uint32_t *__restrict__ rlist) {
+  dependent_launch_enter();
   const int k0 = blockIdx.x * TZ + run_tz(threadIdx.x) * 8, j = blockIdx.y * TY + run_ty(threadIdx.x);
   uint2 cw[TX];
   uint32_t gm[TX];
@@ -572,6 +576,7 @@ k_fill_runs(const uint8_t *__restrict__ cls, const uint32_t *__restrict__ rlist,
             const uint32_t *__restrict__ rw, const uint32_t *__restrict__ rbase, const uint32_t *__restrict__ rcount,
             int n2, int n3, const float *__restrict__ kuni0, const float *__restrict__ kuni1, KT *__restrict__ rec0,
             KT *__restrict__ rec1) {
+  dependent_launch_enter();
   const uint64_t nrun = (uint64_t)__ldg(rlast_base) + __ldg(rlast_count);
   for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < 27 * nrun;
        t += (uint64_t)gridDim.x * blockDim.x) {
@@ -608,6 +613,7 @@ k_kgen_list(const float *__restrict__ img, int n1, int n2, int n3, const float *
             const uint32_t *__restrict__ glast_count, const uint32_t *__restrict__ rw,
             const uint32_t *__restrict__ rbase, const uint32_t *__restrict__ rcount, KT *__restrict__ rec0,
             KT *__restrict__ rec1) {
+  dependent_launch_enter();
   __shared__ float4 sW[NB * kSW];
   __shared__ float4 sWm[NB * kSW];
   __shared__ float sb[NB * 28];
@@ -651,6 +657,7 @@ k_kgen_t_list(int n1, int n2, int n3, const uint32_t *__restrict__ list, const u
               const uint32_t *__restrict__ rw, const uint32_t *__restrict__ rbase, const uint32_t *__restrict__ rcount,
               const KT *__restrict__ rec, const float *__restrict__ kuni, const uint32_t *__restrict__ rwT,
               const uint32_t *__restrict__ rbaseT, const uint32_t *__restrict__ rcountT, KT *__restrict__ recT) {
+  dependent_launch_enter();
   const uint32_t G = __ldg(glast_base) + __ldg(glast_count);
   for (uint32_t e = blockIdx.x * PT + threadIdx.x; e < G; e += gridDim.x * PT) {
     const uint32_t q = __ldg(list + e);
@@ -681,6 +688,7 @@ k_kgen_t_list(int n1, int n2, int n3, const uint32_t *__restrict__ list, const u
 template <typename KT>
 __global__ void __launch_bounds__(256)
 k_planes_transpose(const KT *__restrict__ K, KT *__restrict__ Kt, int64_t ps, int n1, int n2, int n3) {
+  dependent_launch_enter();
   const int64_t n = cells(n1, n2, n3);
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
@@ -699,6 +707,7 @@ k_planes_transpose(const KT *__restrict__ K, KT *__restrict__ Kt, int64_t ps, in
 
 // c[e] = c[e]^2 (the SPD kind's c0^2, c1^2; sm_model_3d.py:421)
 __global__ void k_square(float *__restrict__ c, int n) {
+  dependent_launch_enter();
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e < n) c[e] = c[e] * c[e];
 }
@@ -719,6 +728,7 @@ struct CoefArgs {
 // cell c at mrec[((b * 3 + m) * 27 + p) * 8 + c] = kuni[b][m][p].
 template <typename KT>
 __global__ void __launch_bounds__(256) k_material_records(const float *__restrict__ kuni, KT *__restrict__ mrec) {
+  dependent_launch_enter();
   const int b = blockIdx.x;
   for (int e = threadIdx.x; e < 3 * RREC; e += blockDim.x) {
     const int m = e / RREC, p = (e % RREC) / 8;
@@ -1111,6 +1121,7 @@ __global__ void __launch_bounds__(PT)
 k_pre_fused(const CoefArgs<KT> C, const XT *__restrict__ x,
             const float *__restrict__ xscale, YT *__restrict__ y, YT *__restrict__ ypool,
             const uint8_t *__restrict__ mask, int n1, int n2, int n3, const int *__restrict__ gate) {
+  dependent_launch_enter();
   if (gate && *gate != 0) return;  // batched solves: this system has stopped
   pre_fused_body<KT, XT, YT, POOL, CLS, false>(C, x, xscale, y, ypool, mask, n1, n2, n3, nullptr, nullptr,
                                               grid_tile());
@@ -1122,6 +1133,7 @@ template <typename KT, typename XT, typename YT, bool POOL, bool CLS>
 __global__ void __launch_bounds__(PT, 1)
 k_pre_fused_small(const CoefArgs<KT> C, const XT *__restrict__ x, YT *__restrict__ y, YT *__restrict__ ypool,
                   int n1, int n2, int n3, const int *__restrict__ gate) {
+  dependent_launch_enter();
   if (gate && *gate != 0) return;
   pre_fused_body<KT, XT, YT, POOL, CLS, false, false, true>(C, x, nullptr, y, ypool, nullptr, n1, n2, n3, nullptr,
                                                             nullptr, grid_tile());
@@ -1134,6 +1146,7 @@ __global__ void __launch_bounds__(PT)
 k_pre_fused_tma(const CoefArgs<KT> C, const __grid_constant__ CUtensorMap tmap, const float *__restrict__ xscale,
                 YT *__restrict__ y, YT *__restrict__ ypool, const uint8_t *__restrict__ mask, int n1, int n2, int n3,
                 const int *__restrict__ gate, int *__restrict__ err) {
+  dependent_launch_enter();
   if (gate && *gate != 0) return;
   pre_fused_body<KT, float, YT, true, CLS, true>(C, nullptr, xscale, y, ypool, mask, n1, n2, n3, &tmap, err,
                                                 grid_tile());
@@ -1221,6 +1234,7 @@ template <typename CT, typename YT, typename UT, bool SWAP, bool NEAREST = false
 __global__ void __launch_bounds__(PT)
 k_up_fine(const CT *__restrict__ xc, const YT *__restrict__ yl, const float *__restrict__ c0p,
           const float *__restrict__ c1p, UT *__restrict__ u, int n1, int n2, int n3, const int *__restrict__ gate) {
+  dependent_launch_enter();
   if (gate && *gate != 0) return;
   __shared__ __align__(16) float Cs[CX][CY][CZP];
   const int m1 = n1 / 2, m2 = n2 / 2, m3 = n3 / 2;
@@ -1308,18 +1322,48 @@ k_up_fine(const CT *__restrict__ xc, const YT *__restrict__ yl, const float *__r
   }
 }
 
+// The tile's share of the npsd products (ZDots): each thread's FP32 sums of its cells, added in
+// FP64 across the CTA in a fixed order; thread 0 stores the tile's two values.
+__device__ __forceinline__ void zdots_tile_store(float s0, float s1, const ZDots &zd, unsigned tile) {
+  __shared__ double red[2][PT / 32];
+  double v0 = s0, v1 = s1;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    v0 += __shfl_xor_sync(0xffffffffu, v0, o);
+    v1 += __shfl_xor_sync(0xffffffffu, v1, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = v0;
+    red[1][threadIdx.x >> 5] = v1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+#pragma unroll
+    for (int w = 0; w < PT / 32; ++w) {
+      a += red[0][w];
+      b += red[1][w];
+    }
+    zd.partial[2 * (size_t)tile] = a;
+    zd.partial[2 * (size_t)tile + 1] = b;
+  }
+}
+
 // UPIN: xc is the level's prolongated input u of k_up_fine (already combined
 // with y_l under swap), staged like a pre-block input.
 // TMA (UPIN, CT = float): the FP32 input u arrives by the tensor-memory accelerator as in the
 // level-0 pre-block (tma_tile_issue / tma_tile_wait).
+// ZD (OT = float): the npsd products of the output with the solver's directions (ZDots) as an
+// epilogue, while the output is still in registers.
 template <typename KT, typename CT, typename YT, typename OT, bool SWAP, bool CLS, bool UPIN, bool TMA,
-          bool COH = false, bool PREF = false>
+          bool COH = false, bool PREF = false, bool ZD = false>
 __device__ __forceinline__ void post_fused_body(const CoefArgs<KT> &C, const CT *__restrict__ xc,
                                                 const YT *__restrict__ yl, const float *__restrict__ c0p,
                                                 const float *__restrict__ c1p, OT *__restrict__ out,
                                                 const uint8_t *__restrict__ bmask,
                                                 const uint8_t *__restrict__ omask, int n1, int n2, int n3,
-                                                const CUtensorMap *tmap, int *err, const Tile &t) {
+                                                const CUtensorMap *tmap, int *err, const Tile &t,
+                                                const ZDots *zd = nullptr) {
   static_assert(!TMA || UPIN, "TMA staging needs the prolongated input");
   float(*S)[HY][HZP] = fine_tile_smem();
   TileWait &tw = tile_wait_smem();
@@ -1397,11 +1441,21 @@ __device__ __forceinline__ void post_fused_body(const CoefArgs<KT> &C, const CT 
   else tile_apply<KT, CLS, TMA ? 3 : 0>(S, smc, C, rwd, tb, t, n1, n2, n3, accs);
   const int tz = run_tz(threadIdx.x), ty = run_ty(threadIdx.x);
   const int k0 = z0 + tz * 8, j = y0 + ty;
-  if (k0 >= n3 || j >= n2) return;
+  const bool active = k0 < n3 && j < n2;
+  // ZD: products wanted (0, 1 or 2, the same for the whole CTA) and their vectors
+  int nd = 0;
+  const float *a1 = nullptr, *a0 = nullptr;
+  if constexpr (ZD) {
+    const int it = __ldg(zd->it), h = __ldg(zd->head);
+    nd = it < 2 ? it : 2;
+    a1 = zd->ring + (size_t)h * zd->n;
+    a0 = zd->ring + (size_t)((h + 2) % 3) * zd->n;
+  }
+  float s1 = 0.f, s0 = 0.f;
 #pragma unroll
   for (int tx = 0; tx < TX; ++tx) {
     const int i = x0 + tx;
-    if (i >= n1) continue;
+    if (!active || i >= n1) continue;
     const int64_t q = ((int64_t)i * n2 + j) * n3 + k0;
     float *acc = accs[tx];
     apply_run_mask(bw[tx], acc);
@@ -1413,6 +1467,23 @@ __device__ __forceinline__ void post_fused_body(const CoefArgs<KT> &C, const CT 
     }
     apply_run_mask(ow[tx], acc);
     st8(out + q, acc);
+    if constexpr (ZD) {
+      if (nd >= 1) {
+        float a[8];
+        ld8(a1 + q, a);
+#pragma unroll
+        for (int c = 0; c < 8; ++c) s1 = fmaf(acc[c], a[c], s1);
+      }
+      if (nd == 2) {
+        float a[8];
+        ld8(a0 + q, a);
+#pragma unroll
+        for (int c = 0; c < 8; ++c) s0 = fmaf(acc[c], a[c], s0);
+      }
+    }
+  }
+  if constexpr (ZD) {
+    if (nd > 0) zdots_tile_store(s1, s0, *zd, t.id);
   }
 }
 
@@ -1422,6 +1493,7 @@ k_post_fused(const CoefArgs<KT> C, const CT *__restrict__ xc, const YT *__restri
              const float *__restrict__ c0p, const float *__restrict__ c1p, OT *__restrict__ out,
              const uint8_t *__restrict__ bmask, const uint8_t *__restrict__ omask, int n1, int n2, int n3,
              const int *__restrict__ gate) {
+  dependent_launch_enter();
   if (gate && *gate != 0) return;
   post_fused_body<KT, CT, YT, OT, SWAP, CLS, UPIN, false>(C, xc, yl, c0p, c1p, out, bmask, omask, n1, n2, n3,
                                                           nullptr, nullptr, grid_tile());
@@ -1433,21 +1505,24 @@ __global__ void __launch_bounds__(PT, 1)
 k_post_fused_small(const CoefArgs<KT> C, const AT *__restrict__ xc, const AT *__restrict__ yl,
                    const float *__restrict__ c0p, const float *__restrict__ c1p, AT *__restrict__ out, int n1,
                    int n2, int n3, const int *__restrict__ gate) {
+  dependent_launch_enter();
   if (gate && *gate != 0) return;
   post_fused_body<KT, AT, AT, AT, SWAP, CLS, false, false, false, true>(C, xc, yl, c0p, c1p, out, nullptr, nullptr,
                                                                         n1, n2, n3, nullptr, nullptr, grid_tile());
 }
 
-// the post-block on an FP32 prolongated input u loaded by TMA through tmap
-template <typename KT, typename YT, typename OT, bool SWAP, bool CLS>
+// the post-block on an FP32 prolongated input u loaded by TMA through tmap; ZD: with the npsd
+// products of the output (zd)
+template <typename KT, typename YT, typename OT, bool SWAP, bool CLS, bool ZD = false>
 __global__ void __launch_bounds__(PT)
 k_post_fused_tma(const CoefArgs<KT> C, const __grid_constant__ CUtensorMap tmap, const YT *__restrict__ yl,
                  const float *__restrict__ c0p, const float *__restrict__ c1p, OT *__restrict__ out,
                  const uint8_t *__restrict__ bmask, const uint8_t *__restrict__ omask, int n1, int n2, int n3,
-                 const int *__restrict__ gate, int *__restrict__ err) {
+                 const int *__restrict__ gate, int *__restrict__ err, const ZDots zd) {
+  dependent_launch_enter();
   if (gate && *gate != 0) return;
-  post_fused_body<KT, float, YT, OT, SWAP, CLS, true, true>(C, nullptr, yl, c0p, c1p, out, bmask, omask, n1, n2,
-                                                            n3, &tmap, err, grid_tile());
+  post_fused_body<KT, float, YT, OT, SWAP, CLS, true, true, false, false, ZD>(
+      C, nullptr, yl, c0p, c1p, out, bmask, omask, n1, n2, n3, &tmap, err, grid_tile(), &zd);
 }
 
 // ---------------------------------------------------------------------------
@@ -1502,6 +1577,7 @@ __device__ __forceinline__ void prefetch_tile_records(const CoefArgs<KT> &C, uns
 template <typename KT, typename AT, bool CLS, bool SWAP>
 __global__ void __launch_bounds__(PT)
 k_coarse_cluster(const __grid_constant__ CoarseArgs<KT, AT> A, const int *__restrict__ gate) {
+  dependent_launch_enter();
   if (gate && *gate != 0) return;  // read alike by every CTA: the whole cluster leaves
   const unsigned r = blockIdx.x, nc = gridDim.x;
   if constexpr (CLS) {
@@ -1540,6 +1616,7 @@ k_coarse_cluster(const __grid_constant__ CoarseArgs<KT, AT> A, const int *__rest
 // ---------------------------------------------------------------------------
 template <typename T>
 __global__ void k_scale_copy(const float *__restrict__ x, const float *__restrict__ s, T *__restrict__ y, int64_t n) {
+  dependent_launch_enter();
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
   stf(y + q, x[q] * (s ? s[0] : 1.f));
@@ -1547,6 +1624,7 @@ __global__ void k_scale_copy(const float *__restrict__ x, const float *__restric
 
 template <typename T>
 __global__ void k_apply_mask(T *__restrict__ y, const uint8_t *__restrict__ m, int64_t n) {
+  dependent_launch_enter();
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
   if (!m[q]) stf(y + q, 0.f);
@@ -1554,12 +1632,14 @@ __global__ void k_apply_mask(T *__restrict__ y, const uint8_t *__restrict__ m, i
 
 template <typename TI, typename TO>
 __global__ void k_convert(const TI *__restrict__ x, TO *__restrict__ y, int64_t n) {
+  dependent_launch_enter();
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
   stf(y + q, ldf(x + q));
 }
 
 __global__ void k_fluid_mask(const float *__restrict__ img, uint8_t *__restrict__ m, int64_t n) {
+  dependent_launch_enter();
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
   m[q] = img[n + q] != 0.f;  // channel 1 = fluid (the reference masks with image[1] == 0)
@@ -1892,17 +1972,24 @@ static int launch_pre0(const PrecondPlan &P, const CoefArgs<KT> &C, const float 
 
 // The finest level's post-block on its prolongated input u (FP32, in P.ufine): TMA-staged when
 // the tensor map encodes, else the thread-staged kernel.
+// zd (non-NULL only when precond_zdots_tiles allows it): the npsd products as the TMA kernel's
+// epilogue.
 template <typename KT, typename AT, typename OT, bool SWAP>
 static int launch_post0(const PrecondPlan &P, const CoefArgs<KT> &C, const AT *yl, const float *c0, const float *c1,
-                        OT *out, const uint8_t *bm, const uint8_t *om, cudaStream_t st, const int *gate) {
+                        OT *out, const uint8_t *bm, const uint8_t *om, cudaStream_t st, const int *gate,
+                        const ZDots *zd = nullptr) {
   const auto &v = P.lv[0];
   const dim3 g = grid_of(v);
   const float *u = (const float *)P.ufine;
   CUtensorMap tm;
   if (encode_input_map(&tm, u, v)) {
-    if (v.cls) k_post_fused_tma<KT, AT, OT, SWAP, true><<<g, PT, 0, st>>>(C, tm, yl, c0, c1, out, bm, om, v.n1, v.n2, v.n3, gate, P.err);
-    else k_post_fused_tma<KT, AT, OT, SWAP, false><<<g, PT, 0, st>>>(C, tm, yl, c0, c1, out, bm, om, v.n1, v.n2, v.n3, gate, P.err);
+    const ZDots z = zd ? *zd : ZDots{};
+    if (zd && v.cls) k_post_fused_tma<KT, AT, OT, SWAP, true, true><<<g, PT, 0, st>>>(C, tm, yl, c0, c1, out, bm, om, v.n1, v.n2, v.n3, gate, P.err, z);
+    else if (zd) k_post_fused_tma<KT, AT, OT, SWAP, false, true><<<g, PT, 0, st>>>(C, tm, yl, c0, c1, out, bm, om, v.n1, v.n2, v.n3, gate, P.err, z);
+    else if (v.cls) k_post_fused_tma<KT, AT, OT, SWAP, true><<<g, PT, 0, st>>>(C, tm, yl, c0, c1, out, bm, om, v.n1, v.n2, v.n3, gate, P.err, z);
+    else k_post_fused_tma<KT, AT, OT, SWAP, false><<<g, PT, 0, st>>>(C, tm, yl, c0, c1, out, bm, om, v.n1, v.n2, v.n3, gate, P.err, z);
   } else {
+    MLPCG_REQUIRE(!zd, MLPCG_ERR_ARG, "precond apply: product epilogue without a TMA level-0 post-block");
     if (v.cls) k_post_fused<KT, float, AT, OT, SWAP, true, true><<<g, PT, 0, st>>>(C, u, yl, c0, c1, out, bm, om, v.n1, v.n2, v.n3, gate);
     else k_post_fused<KT, float, AT, OT, SWAP, false, true><<<g, PT, 0, st>>>(C, u, yl, c0, c1, out, bm, om, v.n1, v.n2, v.n3, gate);
   }
@@ -2205,7 +2292,8 @@ static void launch_post_level(const PrecondPlan &P, const PrecondPlan::Level &v,
 
 template <typename KT, typename AT>
 static int run_apply(const PrecondPlan &P, const float *r, const float *rscale, float *z, void *tmp0,
-                     cudaStream_t st, int s0 = 0, int s1 = 1 << 20, const int *gate = nullptr) {
+                     cudaStream_t st, int s0 = 0, int s1 = 1 << 20, const int *gate = nullptr,
+                     const ZDots *zd = nullptr) {
   if (P.kind == MLPCG_PRECOND_SPD) return run_apply_spd<KT, AT>(P, r, rscale, z, tmp0, st, s0, s1, gate);
   const int L = P.L;
   const uint8_t *m0 = P.mask ? P.fmask : nullptr;
@@ -2324,11 +2412,11 @@ static int run_apply(const PrecondPlan &P, const float *r, const float *rscale, 
         if (P.swap) {
           k_up_fine<AT, AT, float, true><<<g, PT, 0, st>>>(xc, yl, c0, c1, u, v.n1, v.n2, v.n3, gate);
           MLPCG_LAUNCH_CHECK();
-          RET_IF((launch_post0<KT, AT, float, true>(P, C, yl, c0, c1, z, bm, om, st, gate)));
+          RET_IF((launch_post0<KT, AT, float, true>(P, C, yl, c0, c1, z, bm, om, st, gate, zd)));
         } else {
           k_up_fine<AT, AT, float, false><<<g, PT, 0, st>>>(xc, yl, c0, c1, u, v.n1, v.n2, v.n3, gate);
           MLPCG_LAUNCH_CHECK();
-          RET_IF((launch_post0<KT, AT, float, false>(P, C, yl, c0, c1, z, bm, om, st, gate)));
+          RET_IF((launch_post0<KT, AT, float, false>(P, C, yl, c0, c1, z, bm, om, st, gate, zd)));
         }
       } else {
         AT *o = (AT *)P.xout[l];
@@ -2383,20 +2471,39 @@ namespace mlpcg {
 // the plan's copy-failed word (device memory; valid once the plan is set up)
 const int *precond_copy_flag(const mlpcg_precond *h) { return h->p.ready ? h->p.err : nullptr; }
 
+int64_t precond_level0_tiles(const mlpcg_precond *h);
+
+// Tiles of the finest level when the plan can compute the npsd products (ZDots) in its level-0
+// post-block -- the plain SM kind whose finest post-block is the TMA kernel -- else 0.
+int64_t precond_zdots_tiles(const mlpcg_precond *h) {
+  const PrecondPlan &P = h->p;
+  if (!P.ready || P.kind != MLPCG_PRECOND_SM || !P.lv[0].fast) return 0;
+  CUtensorMap tm;
+  if (!encode_input_map(&tm, (const float *)P.ufine, P.lv[0])) return 0;
+  return precond_level0_tiles(h);
+}
+
+// tiles of the finest level's grid (known from creation on)
+int64_t precond_level0_tiles(const mlpcg_precond *h) {
+  const dim3 g = grid_of(h->p.lv[0]);
+  return (int64_t)g.x * g.y * g.z;
+}
+
 // mlpcg_precond_apply whose fused kernels return at once while *gate != 0
-// (the batched solver passes each system's status word)
+// (the batched solver passes each system's status word); zd (only where precond_zdots_tiles > 0):
+// the npsd products computed by the level-0 post-block
 int precond_apply_gated(const mlpcg_precond *h, const float *r, const float *r_scale, float *z, const int *gate,
-                        void *stream) {
+                        void *stream, const ZDots *zd) {
   const PrecondPlan &P = h->p;
   cudaStream_t st = as_stream(stream);
   void *tmp0 = (char *)P.scratch + al256(96 * sizeof(float));
   if (P.kdt == MLPCG_BF16 && P.adt == MLPCG_BF16)
-    return run_apply<__nv_bfloat16, __nv_bfloat16>(P, r, r_scale, z, tmp0, st, 0, 1 << 20, gate);
+    return run_apply<__nv_bfloat16, __nv_bfloat16>(P, r, r_scale, z, tmp0, st, 0, 1 << 20, gate, zd);
   if (P.kdt == MLPCG_BF16 && P.adt == MLPCG_F32)
-    return run_apply<__nv_bfloat16, float>(P, r, r_scale, z, tmp0, st, 0, 1 << 20, gate);
+    return run_apply<__nv_bfloat16, float>(P, r, r_scale, z, tmp0, st, 0, 1 << 20, gate, zd);
   if (P.kdt == MLPCG_F32 && P.adt == MLPCG_BF16)
-    return run_apply<float, __nv_bfloat16>(P, r, r_scale, z, tmp0, st, 0, 1 << 20, gate);
-  return run_apply<float, float>(P, r, r_scale, z, tmp0, st, 0, 1 << 20, gate);
+    return run_apply<float, __nv_bfloat16>(P, r, r_scale, z, tmp0, st, 0, 1 << 20, gate, zd);
+  return run_apply<float, float>(P, r, r_scale, z, tmp0, st, 0, 1 << 20, gate, zd);
 }
 }  // namespace mlpcg
 

@@ -31,7 +31,10 @@
 
 struct mlpcg_precond;
 namespace mlpcg {
-int precond_apply_gated(const mlpcg_precond *, const float *, const float *, float *, const int *, void *);
+int precond_apply_gated(const mlpcg_precond *, const float *, const float *, float *, const int *, void *,
+                        const ZDots *);
+int64_t precond_zdots_tiles(const mlpcg_precond *);
+int64_t precond_level0_tiles(const mlpcg_precond *);
 const int *precond_copy_flag(const mlpcg_precond *);
 bool encode_grid_map(CUtensorMap *m, const float *base, int n1, int n2, int n3, int box_z, int box_y, int box_x);
 }
@@ -81,6 +84,8 @@ struct Vecs {
   float *p;        // 3 slots (NPSD ring) or 2 (NPCG ping-pong), n each
   float *Ap;       // 3 slots (NPSD) or 1 (NPCG)
   double *part;    // NRED * RB_MAX partial sums
+  double *zpart;   // NPSD: 2 per finest-level tile, the products z . Ap from the preconditioner's epilogue
+  int64_t ztiles;  // tiles summed by k_sd_dots_tiles
   double *hist;    // max_it + 1 relative residuals
   State *st;
   const int *perr; // the preconditioner plan's copy-failed word (its level-0 TMA tiles)
@@ -315,6 +320,7 @@ __device__ __forceinline__ void group_coords(const Vecs &V, uint32_t g, uint32_t
 // setup: state reset, then r = b - A x (FP64), bb = b.b, rr = r.r
 // ---------------------------------------------------------------------------
 __global__ void k_reset(State *st, int max_it, int true_every, int method, double tol, int stall_copies) {
+  dependent_launch_enter();
   if (threadIdx.x != 0) return;
   State S{};
   S.max_it = max_it;
@@ -331,6 +337,7 @@ __global__ void k_reset(State *st, int max_it, int true_every, int method, doubl
 // conversions use integer operations (df_from_double_bits); cells whose value
 // is exactly zero skip them.
 __global__ void __launch_bounds__(RT) k_prepare(Vecs V) {
+  dependent_launch_enter();
   for (uint32_t g = gtid(); g < V.ngroups; g += gstride()) {
     uint32_t q; int i, j, k0;
     group_coords(V, g, q, i, j, k0);
@@ -433,6 +440,7 @@ __device__ __forceinline__ void residual_pass(const Vecs &V, CSum &bb, CSum &rr)
 
 // The caller's x from the pairs, on the fluid cells (the others keep their values)
 __global__ void __launch_bounds__(RT) k_finalize(Vecs V) {
+  dependent_launch_enter();
   const XEff X = x_eff(V);  // with a still pending update of the iterate
   for (uint32_t g = gtid(); g < V.ngroups; g += gstride()) {
     const uint32_t q = 4u * g;
@@ -460,6 +468,7 @@ __global__ void __launch_bounds__(RT) k_finalize(Vecs V) {
 }
 
 __global__ void __launch_bounds__(RT) k_init(Vecs V) {
+  dependent_launch_enter();
   CSum bb, rr;
   residual_pass<true>(V, bb, rr);
   double v[2] = {bb.get(), rr.get()};
@@ -496,6 +505,7 @@ __global__ void __launch_bounds__(RT) k_init(Vecs V) {
 // q = z - c1 p_recent - c0 p_previous  (the two sequential projections of
 // cg_tests.py:226-233, with q.A p_previous expanded as d0 - c1 e_last).
 __global__ void __launch_bounds__(RT) k_sd_dots(Vecs V) {
+  dependent_launch_enter();
   const State &S = *V.st;
   if (S.status != ST_RUNNING) return;
   const int it = S.it;
@@ -541,8 +551,53 @@ __global__ void __launch_bounds__(RT) k_sd_dots(Vecs V) {
   }
 }
 
+// The same two products from the preconditioner's level-0 epilogue (ZDots): the per-tile FP64
+// partials summed by one block in a fixed order (each thread a strided share, then a fixed tree),
+// then c1, c0 as above.
+constexpr int ZT_THREADS = 1024;
+__global__ void __launch_bounds__(ZT_THREADS) k_sd_dots_tiles(Vecs V) {
+  dependent_launch_enter();
+  const State &S = *V.st;
+  if (S.status != ST_RUNNING) return;
+  const int it = S.it;
+  if (it == 0) {
+    if (threadIdx.x == 0) { V.st->c0 = 0.0; V.st->c1 = 0.0; }
+    return;
+  }
+  __shared__ double red[2][ZT_THREADS / 32];
+  double a1 = 0.0, a0 = 0.0;
+  for (int64_t t = threadIdx.x; t < V.ztiles; t += ZT_THREADS) {
+    a1 += V.zpart[2 * t];
+    a0 += V.zpart[2 * t + 1];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+    a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = a1;
+    red[1][threadIdx.x >> 5] = a0;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double o1 = 0.0, o0 = 0.0;
+    for (int w = 0; w < ZT_THREADS / 32; ++w) {
+      o1 += red[0][w];
+      o0 += red[1][w];
+    }
+    State &W = *V.st;
+    const int h = W.head, hp = (h + 2) % 3;
+    const double c1 = o1 / W.alpha[h];
+    const double c0 = it >= 2 ? (o0 - c1 * W.e_last) / W.alpha[hp] : 0.0;
+    W.c1 = c1;
+    W.c0 = c0;
+  }
+}
+
 // q = z - c1 p_recent - c0 p_previous into the next ring slot
 __global__ void __launch_bounds__(RT) k_sd_qform(Vecs V) {
+  dependent_launch_enter();
   const State &S = *V.st;
   if (S.status != ST_RUNNING) return;
   const int h = S.head, hp = (h + 2) % 3, hn = (h + 1) % 3;
@@ -576,6 +631,7 @@ __global__ void __launch_bounds__(RT) k_sd_qform(Vecs V) {
 
 // Aq, alpha = q.Aq, q.r, e = Aq.p_recent; then beta = q.r / alpha
 __global__ void __launch_bounds__(RT) k_sd_spmv(Vecs V) {
+  dependent_launch_enter();
   const State &S = *V.st;
   if (S.status != ST_RUNNING) return;
   const int h = S.head, hn = (h + 1) % 3;
@@ -630,6 +686,7 @@ __device__ __forceinline__ int sp_ty(int t) { return ((t >> 2) & 1) | ((t >> 3) 
 __global__ void __launch_bounds__(RT, 3) k_sd_spmv_tma(Vecs V, const __grid_constant__ CUtensorMap tq0,
                                                    const __grid_constant__ CUtensorMap tq1,
                                                    const __grid_constant__ CUtensorMap tq2) {
+  dependent_launch_enter();
   const State &S = *V.st;
   if (S.status != ST_RUNNING) return;
   __shared__ __align__(128) float T[SBX][SBY][SBZ];
@@ -777,6 +834,7 @@ __global__ void __launch_bounds__(RT, 3) k_sd_spmv_tma(Vecs V, const __grid_cons
 // NPCG
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(RT) k_cg_rz(Vecs V) {
+  dependent_launch_enter();
   const State &S = *V.st;
   if (S.status != ST_RUNNING) return;
   CSum t;
@@ -801,6 +859,7 @@ __global__ void __launch_bounds__(RT) k_cg_rz(Vecs V) {
 
 // p_new = z + beta p_old (ping-pong buffers), w = A p_new, pw = p_new . w, alpha = rz / pw
 __global__ void __launch_bounds__(RT) k_cg_pspmv(Vecs V) {
+  dependent_launch_enter();
   const State &S = *V.st;
   if (S.status != ST_RUNNING) return;
   const int cur = S.pp, nxt = cur ^ 1;
@@ -836,6 +895,7 @@ __global__ void __launch_bounds__(RT) k_cg_pspmv(Vecs V) {
 // shared: x += beta d (double-float); r -= beta A d; rr = r.r; decide whether a true residual is due
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(RT) k_update(Vecs V) {
+  dependent_launch_enter();
   const State &S = *V.st;
   if (S.status != ST_RUNNING) return;
   const float *D, *AD;
@@ -908,6 +968,7 @@ __global__ void __launch_bounds__(RT) k_update(Vecs V) {
 
 // r = b - A x (double-float) when due
 __global__ void __launch_bounds__(RT) k_true_residual(Vecs V) {
+  dependent_launch_enter();
   const State &S = *V.st;
   if (S.status != ST_RUNNING || !S.need_true) return;
   CSum bb, rr;
@@ -919,6 +980,7 @@ __global__ void __launch_bounds__(RT) k_true_residual(Vecs V) {
 
 // one thread: iteration bookkeeping, convergence, loop condition
 __global__ void k_control(Vecs V, cudaGraphConditionalHandle handle, int use_handle) {
+  dependent_launch_enter();
   State &S = *V.st;
   if (S.status == ST_RUNNING) {
     const int itn = S.it + 1;
@@ -951,6 +1013,7 @@ struct BatchStates {
   int count;
 };
 __global__ void k_batch_control(BatchStates B, cudaGraphConditionalHandle handle) {
+  dependent_launch_enter();
   const int t = threadIdx.x;
   const int running = (t < B.count && B.st[t]->status == ST_RUNNING) ? 1 : 0;
   const int any = __syncthreads_or(running);
@@ -975,10 +1038,15 @@ struct mlpcg_solver {
   int stall_copies = 0;                    // copy-stall test knob (mlpcg_solver_set_copy_stall)
   CUtensorMap qmap[3];                     // the three search-direction buffers, for the TMA SpMV
   bool qmap_ok = false;
+  bool dependent_launch = true;            // programmatic edges in the captured loop body
+  bool fused_dots = true;                  // NPSD: z . Ap in the preconditioner's level-0 epilogue
+  int64_t zcap = 0;                        // tiles of V.zpart
+  int dependent_edges = 0;                 // edges converted in the current graph
 };
 
 struct mlpcg_batch {
   std::vector<mlpcg_solver *> solvers;
+  int dependent_edges = 0;
   std::vector<cudaStream_t> streams;   // one per system: the graph's parallel branches
   std::vector<cudaEvent_t> joins;
   cudaEvent_t fork = nullptr;
@@ -1025,6 +1093,7 @@ static size_t solver_layout(mlpcg_solver &s, char *base) {
   s.V.p = (float *)take(nslots * n * 4);
   s.V.Ap = (float *)take(naps * n * 4);
   s.V.part = (double *)take(NRED * RB_MAX * 8);
+  s.V.zpart = s.zcap > 0 ? (double *)take(2 * s.zcap * 8) : nullptr;
   s.V.hist = (double *)take((s.max_it + 1) * 8);
   s.V.st = (State *)take(sizeof(State));
   return off;
@@ -1035,6 +1104,44 @@ static void destroy_graph(mlpcg_solver *s) {
   if (s->graph) cudaGraphDestroy(s->graph);
   s->exec = nullptr;
   s->graph = nullptr;
+}
+
+// Turns the captured loop body's kernel-to-kernel edges into programmatic ones:
+// the downstream kernel's blocks may be scheduled as the upstream kernel's
+// blocks exit, and they wait in dependent_launch_enter() for the upstream
+// grid's completion and writes -- the launch of each kernel of an iteration
+// overlaps its predecessor's tail, the order of every memory access is
+// unchanged.  Only edges into a
+// kernel with a single incoming edge are converted (the batch's join keeps its
+// ordinary edges).  Returns the number of converted edges, or -1 when the graph
+// API refused (the edges already converted stay, the refused one is restored).
+static int make_dependent_edges(cudaGraph_t body) {
+  size_t ne = 0;
+  if (cudaGraphGetEdges(body, nullptr, nullptr, nullptr, &ne) != cudaSuccess) return -1;
+  std::vector<cudaGraphNode_t> from(ne), to(ne);
+  std::vector<cudaGraphEdgeData> data(ne);
+  if (ne && cudaGraphGetEdges(body, from.data(), to.data(), data.data(), &ne) != cudaSuccess) return -1;
+  int converted = 0;
+  for (size_t e = 0; e < ne; ++e) {
+    size_t indeg = 0;
+    for (size_t f = 0; f < ne; ++f) indeg += to[f] == to[e];
+    cudaGraphNodeType a, b;
+    if (cudaGraphNodeGetType(from[e], &a) != cudaSuccess || cudaGraphNodeGetType(to[e], &b) != cudaSuccess)
+      return -1;
+    if (a != cudaGraphNodeTypeKernel || b != cudaGraphNodeTypeKernel || indeg != 1 ||
+        data[e].type != cudaGraphDependencyTypeDefault || data[e].from_port != cudaGraphKernelNodePortDefault)
+      continue;
+    cudaGraphEdgeData pe{};
+    pe.from_port = cudaGraphKernelNodePortProgrammatic;
+    pe.type = cudaGraphDependencyTypeProgrammatic;
+    if (cudaGraphRemoveDependencies(body, &from[e], &to[e], &data[e], 1) != cudaSuccess) return -1;
+    if (cudaGraphAddDependencies(body, &from[e], &to[e], &pe, 1) != cudaSuccess) {
+      cudaGraphAddDependencies(body, &from[e], &to[e], &data[e], 1);
+      return -1;
+    }
+    ++converted;
+  }
+  return converted;
 }
 
 // state reset, operator codes, b and x0 as pairs, the initial residual
@@ -1048,16 +1155,25 @@ static int start_solve(mlpcg_solver *s, cudaStream_t st) {
   return MLPCG_OK;
 }
 
+// NPSD with a plan whose level-0 post-block computes the products z . Ap (precond_zdots_tiles)
+static bool uses_fused_dots(const mlpcg_solver *s) {
+  return s->fused_dots && s->method == M_NPSD && s->V.zpart && s->zcap > 0 &&
+         precond_zdots_tiles(s->plan) == s->zcap;
+}
+
 static int enqueue_body(mlpcg_solver *s, cudaStream_t st, cudaGraphConditionalHandle h, int use_handle) {
   Vecs &V = s->V;
   const unsigned nb = (unsigned)V.nblk;
   State *S = V.st;
   // z = M (r / ||r||): the scale is read from the device state; the kernels
   // return at once once this system has stopped (its status word is nonzero)
-  int rc = precond_apply_gated(s->plan, V.r, &S->rscale, V.z, &S->status, st);
+  const bool zdots = uses_fused_dots(s);
+  const ZDots zd{V.Ap, &S->head, &S->it, V.zpart, V.n};
+  int rc = precond_apply_gated(s->plan, V.r, &S->rscale, V.z, &S->status, st, zdots ? &zd : nullptr);
   if (rc) return rc;
   if (s->method == M_NPSD) {
-    k_sd_dots<<<nb, RT, 0, st>>>(V);
+    if (zdots) k_sd_dots_tiles<<<1, ZT_THREADS, 0, st>>>(V);
+    else k_sd_dots<<<nb, RT, 0, st>>>(V);
     k_sd_qform<<<nb, RT, 0, st>>>(V);
     if (s->qmap_ok) k_sd_spmv_tma<<<nb, RT, 0, st>>>(V, s->qmap[0], s->qmap[1], s->qmap[2]);
     else k_sd_spmv<<<nb, RT, 0, st>>>(V);
@@ -1084,10 +1200,15 @@ int mlpcg_solver_create(int N1, int N2, int N3, const mlpcg_precond *plan, int m
   MLPCG_REQUIRE(N1 >= 1 && N2 >= 1 && N3 >= 1, MLPCG_ERR_SHAPE, "solver_create: bad grid");
   MLPCG_REQUIRE(N3 % 4 == 0, MLPCG_ERR_SHAPE, "solver_create: N3 (%d) must be a multiple of 4", N3);
   MLPCG_REQUIRE(cells(N1, N2, N3) < ((int64_t)1 << 31), MLPCG_ERR_SHAPE, "solver_create: grid must have < 2^31 cells");
+  int p1 = 0, p2 = 0, p3 = 0, pf = 0;
+  if (int rc = mlpcg_precond_level_info(plan, 0, &p1, &p2, &p3, &pf)) return rc;
+  MLPCG_REQUIRE(p1 == N1 && p2 == N2 && p3 == N3, MLPCG_ERR_SHAPE,
+                "solver_create: the plan's grid %dx%dx%d is not the solver's %dx%dx%d", p1, p2, p3, N1, N2, N3);
   auto *s = new mlpcg_solver();
   s->n1 = N1; s->n2 = N2; s->n3 = N3;
   s->method = method; s->max_it = max_it; s->tol = tol; s->true_every = true_every;
   s->plan = plan;
+  s->zcap = method == M_NPSD ? precond_level0_tiles(plan) : 0;
   s->bytes = solver_layout(*s, nullptr);
   *out = s;
   return MLPCG_OK;
@@ -1119,6 +1240,7 @@ int mlpcg_solver_bind(mlpcg_solver *s, void *workspace, size_t workspace_bytes, 
   V.n1 = s->n1; V.n2 = s->n2; V.n3 = s->n3;
   V.n = cells(s->n1, s->n2, s->n3);
   V.ngroups = (uint32_t)(V.n / 4);
+  V.ztiles = s->zcap;
   V.fd3 = make_fastdiv((uint32_t)s->n3);
   V.fd2 = make_fastdiv((uint32_t)s->n2);
   int64_t nb = ((int64_t)V.ngroups + RT * UNR - 1) / (RT * UNR);
@@ -1153,7 +1275,9 @@ static int solve_impl(mlpcg_solver *s, int use_graph, int zero_guess, cudaStream
     MLPCG_LAUNCH_CHECK();
     return MLPCG_OK;
   }
-  if (!s->exec) {
+  // capture with programmatic edges when enabled; a graph the runtime will not
+  // instantiate with them is captured again with ordinary edges
+  for (int dep = s->dependent_launch ? 1 : 0; !s->exec && dep >= 0; --dep) {
     if (!s->capture_stream)
       MLPCG_CUDA_CHECK(cudaStreamCreateWithFlags(&s->capture_stream, cudaStreamNonBlocking));
     MLPCG_CUDA_CHECK(cudaGraphCreate(&s->graph, 0));
@@ -1174,7 +1298,16 @@ static int solve_impl(mlpcg_solver *s, int use_graph, int zero_guess, cudaStream
     cudaError_t e = cudaStreamEndCapture(cs, &captured);
     if (rc) { destroy_graph(s); return rc; }
     if (e != cudaSuccess) { destroy_graph(s); MLPCG_CUDA_CHECK(e); }
-    MLPCG_CUDA_CHECK(cudaGraphInstantiate(&s->exec, s->graph, 0));
+    s->dependent_edges = dep ? make_dependent_edges(body) : 0;
+    const cudaError_t ei = s->dependent_edges < 0 ? cudaErrorNotSupported
+                                                  : cudaGraphInstantiate(&s->exec, s->graph, 0);
+    if (ei != cudaSuccess) {
+      s->exec = nullptr;
+      destroy_graph(s);
+      s->dependent_edges = 0;
+      cudaGetLastError();
+      if (!dep) MLPCG_CUDA_CHECK(ei);
+    }
   }
   // the loop only starts when the initial residual is not already converged:
   // the body's first kernels see status != RUNNING and the control kernel
@@ -1236,6 +1369,36 @@ int mlpcg_solver_set_copy_stall(mlpcg_solver *s, int on) {
   return MLPCG_OK;
 }
 
+int mlpcg_solver_set_dependent_launch(mlpcg_solver *s, int on) {
+  clear_error();
+  MLPCG_REQUIRE(s, MLPCG_ERR_ARG, "solver_set_dependent_launch: NULL solver");
+  if (s->dependent_launch != (on != 0)) destroy_graph(s);  // recaptured on the next solve
+  s->dependent_launch = on != 0;
+  return MLPCG_OK;
+}
+
+int mlpcg_solver_set_fused_dots(mlpcg_solver *s, int on) {
+  clear_error();
+  MLPCG_REQUIRE(s, MLPCG_ERR_ARG, "solver_set_fused_dots: NULL solver");
+  if (s->fused_dots != (on != 0)) destroy_graph(s);  // recaptured on the next solve
+  s->fused_dots = on != 0;
+  return MLPCG_OK;
+}
+
+int mlpcg_solver_fused_dots(const mlpcg_solver *s, int *active) {
+  clear_error();
+  MLPCG_REQUIRE(s && active, MLPCG_ERR_ARG, "solver_fused_dots: NULL argument");
+  *active = s->bound && uses_fused_dots(s) ? 1 : 0;
+  return MLPCG_OK;
+}
+
+int mlpcg_solver_dependent_edges(const mlpcg_solver *s, int *edges) {
+  clear_error();
+  MLPCG_REQUIRE(s && edges, MLPCG_ERR_ARG, "solver_dependent_edges: NULL argument");
+  *edges = s->exec ? s->dependent_edges : 0;
+  return MLPCG_OK;
+}
+
 int mlpcg_solver_get_schedule(const mlpcg_solver *s, int *blocks_in_use) {
   clear_error();
   MLPCG_REQUIRE(s && blocks_in_use, MLPCG_ERR_ARG, "solver_get_schedule: NULL argument");
@@ -1287,7 +1450,8 @@ int mlpcg_batch_solve(mlpcg_batch *b, void *stream) {
     s->V.zero_guess = 0;  // batches start from each solver's x
     if (int rc = start_solve(s, st)) return rc;
   }
-  if (!b->exec) {
+  // programmatic edges inside each system's chain as for one solver, when its first solver has them
+  for (int dep = b->solvers[0]->dependent_launch ? 1 : 0; !b->exec && dep >= 0; --dep) {
     if (!b->capture_stream) {
       MLPCG_CUDA_CHECK(cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking));
       MLPCG_CUDA_CHECK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
@@ -1332,7 +1496,16 @@ int mlpcg_batch_solve(mlpcg_batch *b, void *stream) {
     if (rc) { destroy_batch_graph(b); return rc; }
     if (e != cudaSuccess) { destroy_batch_graph(b); MLPCG_CUDA_CHECK(e); }
     if (e2 != cudaSuccess) { destroy_batch_graph(b); MLPCG_CUDA_CHECK(e2); }
-    MLPCG_CUDA_CHECK(cudaGraphInstantiate(&b->exec, b->graph, 0));
+    b->dependent_edges = dep ? make_dependent_edges(body) : 0;
+    const cudaError_t ei = b->dependent_edges < 0 ? cudaErrorNotSupported
+                                                  : cudaGraphInstantiate(&b->exec, b->graph, 0);
+    if (ei != cudaSuccess) {
+      b->exec = nullptr;
+      destroy_batch_graph(b);
+      b->dependent_edges = 0;
+      cudaGetLastError();
+      if (!dep) MLPCG_CUDA_CHECK(ei);
+    }
   }
   MLPCG_CUDA_CHECK(cudaGraphLaunch(b->exec, st));
   for (auto *s : b->solvers) {

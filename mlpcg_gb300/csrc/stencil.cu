@@ -24,6 +24,7 @@ template <typename KT>
 __global__ void __launch_bounds__(kGenThreads)
 k_stencil_gen(const float *__restrict__ img, FieldGeom g, const float *__restrict__ W,
               const float *__restrict__ bias, KT *__restrict__ K, int64_t ps) {
+  dependent_launch_enter();
   __shared__ float4 sW[kSW];
   __shared__ float4 sWm[kSW];
   __shared__ float sb[28];
@@ -54,6 +55,7 @@ template <typename KT, typename XT, typename YT, bool TRANS>
 __global__ void __launch_bounds__(256)
 k_stencil_apply(const KT *__restrict__ K, int64_t ps, const XT *__restrict__ x, FieldGeom gx,
                 YT *__restrict__ y) {
+  dependent_launch_enter();
   const int64_t n = cells(gx.n1, gx.n2, gx.n3);
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
@@ -88,6 +90,7 @@ template <bool TRANS>
 __global__ void __launch_bounds__(256)
 k_coeff_grad(const float *__restrict__ g, const float *__restrict__ x, FieldGeom gx, int B,
              float *__restrict__ dK, int64_t ps) {
+  dependent_launch_enter();
   const int64_t n = cells(gx.n1, gx.n2, gx.n3);
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
@@ -139,6 +142,7 @@ constexpr int kWgOut = 27 * kWgCols;
 __global__ void __launch_bounds__(256)
 k_wgrad_partial(const float *__restrict__ dK, int64_t ps, const float *__restrict__ img,
                 FieldGeom g, double *__restrict__ partial) {
+  dependent_launch_enter();
   __shared__ float sdK[27][kWgTile];
   __shared__ float sP[kWgCols][kWgTile];
   const int64_t n = cells(g.n1, g.n2, g.n3);
@@ -204,6 +208,7 @@ k_wgrad_partial(const float *__restrict__ dK, int64_t ps, const float *__restric
 
 __global__ void k_wgrad_finalize(const double *__restrict__ partial, int nblk,
                                  float *__restrict__ gw, float *__restrict__ gb) {
+  dependent_launch_enter();
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= 27 * 82) return;
   const int p = e / 82, col = e % 82;
@@ -219,6 +224,7 @@ __global__ void k_wgrad_finalize(const double *__restrict__ partial, int nblk,
 __global__ void __launch_bounds__(128)
 k_image_grad(const float *__restrict__ dK, int64_t ps, const float *__restrict__ W, int n1,
              int n2, int n3, float *__restrict__ gimg) {
+  dependent_launch_enter();
   __shared__ float sW[27 * 81];
   for (int t = threadIdx.x; t < 27 * 81; t += blockDim.x) sW[t] = W[t];
   __syncthreads();

@@ -148,6 +148,28 @@ class FusedSolver:
         npsd SpMV's first tile wait runs out on an ordinary copy and the solve ends 'copy_failed'."""
         call("mlpcg_solver_set_copy_stall", self._h, int(bool(on)))
 
+    def set_dependent_launch(self, on: bool):
+        """Programmatic edges between consecutive kernels of the captured iteration (on by default;
+        mlpcg_solver_set_dependent_launch): identical results, the launch gaps hidden."""
+        call("mlpcg_solver_set_dependent_launch", self._h, int(bool(on)))
+
+    def set_fused_dots(self, on: bool):
+        """npsd: the products z . Ap summed in the preconditioner's level-0 post-block (on by default,
+        where the plan allows it; mlpcg_solver_set_fused_dots) or in a separate pass."""
+        call("mlpcg_solver_set_fused_dots", self._h, int(bool(on)))
+
+    def fused_dots(self) -> bool:
+        """Whether the solve sums the npsd products in the preconditioner's epilogue."""
+        v = C.c_int()
+        call("mlpcg_solver_fused_dots", self._h, C.byref(v))
+        return bool(v.value)
+
+    def dependent_edges(self) -> int:
+        """Programmatic edges in the current graph (0 before the first graph solve or when off)."""
+        n = C.c_int()
+        call("mlpcg_solver_dependent_edges", self._h, C.byref(n))
+        return n.value
+
     def result(self, with_history=True) -> SolveResult:
         it, st, rel = C.c_int(), C.c_int(), C.c_double()
         hist = np.zeros(self.max_it + 1, dtype=np.float64)

@@ -294,12 +294,14 @@ def test_solve_host_fluid_vectors(cuda):
 
 
 def test_batch_of_uneven_systems_matches_single_solves(cuda):
-    """Systems of different sizes, methods and limits in one batched launch: every system's
-    iterations, status and solution equal its own solve; a system that starts converged stays at
-    zero iterations while the others run; the batch graph is reusable."""
+    """Systems of different sizes (16^3 to 96^3), methods and limits in one batched launch: every
+    system's iterations, status and solution equal its own solve; a system that starts converged
+    stays at zero iterations while the others run; the batch graph is reusable."""
     from mlpcg_gb300.solver import BatchSolver, FusedSolver
+    # the 96^3 system's levels 3 (12^3) and its coarsest run the general (untiled) kernels
     specs = [((16, 16, 16), 3, "npsd", 60, 1e-6, 1), ((24, 16, 32), 3, "npcg", 80, 1e-5, 2),
-             ((32, 32, 32), 3, "npsd", 100, 1e-6, 3), ((16, 24, 16), 2, "npsd", 50, 1e-6, 4)]
+             ((32, 32, 32), 3, "npsd", 100, 1e-6, 3), ((16, 24, 16), 2, "npsd", 50, 1e-6, 4),
+             ((96, 96, 96), 4, "npsd", 30, 1e-6, 5)]
     solvers, rhs, singles = [], [], []
     for shape, n, method, max_it, tol, seed in specs:
         s, flags, img = _scene(shape, seed, cuda)
@@ -334,6 +336,60 @@ def test_fused_graph_reuse_is_deterministic(cuda):
     assert r2.iterations == r1.iterations and torch.equal(x1, r2.x)  # deterministic reductions
     r3 = solver.solve(torch.as_tensor(s.rhs, device=cuda), use_graph=False)
     assert torch.equal(x1, r3.x) and r3.iterations == r1.iterations
+
+
+@pytest.mark.parametrize("method", ["npsd", "npcg"])
+def test_dependent_launch_gives_identical_solves(cuda, method):
+    """Programmatic edges in the captured iteration (the default): the graph has them, and x, the
+    iteration count and the residual history equal those of the graph with ordinary edges and of
+    the uncaptured loop, bit for bit (64^3, BF16 plan with TMA level-0 tiles and small levels)."""
+    from mlpcg_gb300.solver import FusedSolver
+    s, flags, img = _scene((64, 64, 64), 7, cuda)
+    m = _near_identity_model(4, cuda)
+    solver = FusedSolver(m, flags, method=method, max_it=30, tol=1e-9, storage=torch.bfloat16)
+    b = torch.as_tensor(s.rhs, device=cuda)
+    runs = {}
+    for key, dep, graph in (("dependent", True, True), ("ordinary", False, True), ("loop", True, False)):
+        solver.set_dependent_launch(dep)
+        r = solver.solve(b, use_graph=graph)
+        runs[key] = (r.iterations, r.status, r.x.clone(), np.array(r.history))
+        if key == "dependent":
+            assert solver.dependent_edges() > 10
+        if key == "ordinary":
+            assert solver.dependent_edges() == 0
+    it0, st0, x0, h0 = runs["dependent"]
+    assert it0 > 5
+    for key in ("ordinary", "loop"):
+        it, st, x, h = runs[key]
+        assert it == it0 and st == st0 and torch.equal(x, x0) and np.array_equal(h, h0), key
+
+
+def test_npsd_products_in_the_preconditioner_epilogue(cuda):
+    """npsd with z . Ap summed by the level-0 post-block (the default for this plan) against the
+    separate pass: the same products added in another order.  The rounding differences grow
+    slowly over 40 iterations of this slowly converging system (measured 4.4e-5 relative at most),
+    so the histories agree to 2e-4 and the solutions to 1e-3, with the same iteration count and
+    status; the epilogue is off for npcg and when switched off, and graph and loop solves with it
+    agree bit for bit."""
+    from mlpcg_gb300.solver import FusedSolver
+    s, flags, img = _scene((64, 64, 64), 7, cuda)
+    m = _near_identity_model(4, cuda)
+    b = torch.as_tensor(s.rhs, device=cuda)
+    solver = FusedSolver(m, flags, method="npsd", max_it=40, tol=1e-7, storage=torch.bfloat16)
+    assert solver.fused_dots()
+    r_fused = solver.solve(b)
+    x_fused, h_fused = r_fused.x.clone(), np.array(r_fused.history)
+    r_loop = solver.solve(b, use_graph=False)
+    assert torch.equal(r_loop.x, x_fused) and np.array_equal(np.array(r_loop.history), h_fused)
+    solver.set_fused_dots(False)
+    assert not solver.fused_dots()
+    r_sep = solver.solve(b)
+    assert r_sep.iterations == r_fused.iterations and r_sep.status == r_fused.status
+    h_sep = np.array(r_sep.history)[: r_sep.iterations + 1]
+    np.testing.assert_allclose(h_fused[: r_fused.iterations + 1], h_sep, rtol=2e-4)
+    assert float((r_sep.x - x_fused).norm() / r_sep.x.norm()) < 1e-3
+    npcg = FusedSolver(m, flags, method="npcg", max_it=5, tol=1e-7, plan=solver.plan)
+    assert not npcg.fused_dots()
 
 
 def test_fused_status_words(cuda):
