@@ -390,7 +390,7 @@ def run_ours(args, rank, world):
     mixed_t = [plan.class_counts_transposed(l)[1] for l in range(plan.levels + 1)] if plan.spd else None
     if plan.spd:
         roofline["mixed_runs_transposed"] = mixed_t
-    per_iter_bytes = iteration_bytes(plan, n, mixed, mixed_t, args.method)
+    per_iter_bytes = iteration_bytes(plan, n, mixed, mixed_t, args.method, solver.fused_dots())
     it_mean = statistics.mean(its)
 
     # ---- e2e: public API from pinned host buffers ----
@@ -437,14 +437,16 @@ def coeff_bytes(plan, level, n_level, mixed):
     return n_level / 8 * 4 + mixed * 27 * 8 * 2 + tiles * 4   # run words, mixed-run records, tile offsets
 
 
-def iteration_bytes(plan, n0, mixed, mixed_t=None, method="npsd"):
+def iteration_bytes(plan, n0, mixed, mixed_t=None, method="npsd", fused_dots=False):
     """Compulsory HBM bytes of one fused iteration (bf16 coefficients and activations; at level 0
     the input r, the prolongated input u, the output z and, for SPDSMModelDn3D, V's output v0 are
-    FP32, and the fluid mask is read once per application; mirrors run_apply / run_apply_spd)."""
+    FP32, and the fluid mask is read once per application; mirrors run_apply / run_apply_spd).
+    fused_dots: the npsd products read only Ap1, Ap0 (z is in the post-block's registers)."""
     total = 0.0
     # solver vectors: npsd dots + qform + spmv/dots, or npcg r.z + p/spmv; then the update (r every
     # iteration, 12 B; the double-float iterate with two directions every other one, 24 B)
-    vec = n0 * (12 + 16 + 18 + 24) if method == "npsd" else n0 * (8 + 17 + 24)
+    dots = 8 if fused_dots else 12
+    vec = n0 * (dots + 16 + 18 + 24) if method == "npsd" else n0 * (8 + 17 + 24)
     L = plan.levels
     if plan.kind == 2:   # V (prolongation pass on every level), then V^T
         for l in range(L):

@@ -491,6 +491,14 @@ int mlpcg_scatter_fluid(const double *fluid_values, int64_t m, const uint8_t *fl
                         int64_t n, double *grid, void *stream);
 int mlpcg_gather_fluid(const double *grid, const uint8_t *flags, const uint32_t *order, int64_t n,
                        double *fluid_values, int64_t m, void *stream);
+/* *mapped = 1 when ptr lies in page-locked host memory allocated or registered
+ * through CUDA (cudaHostAlloc / cudaMallocHost / cudaHostRegister) that kernels
+ * reach at the same address, else 0.  Such a buffer may be passed as the
+ * fluid-DOF vector of mlpcg_scatter_fluid / mlpcg_gather_fluid: the kernel then
+ * reads or writes it over the host link itself, with no staging copy (the
+ * caller keeps the host buffer alive and untouched until the stream reaches
+ * the call).  No counterpart in the reference. */
+int mlpcg_host_mapped(const void *ptr, int *mapped);
 
 /* =========================================================================
  * Reductions

@@ -81,6 +81,7 @@ _PROTOS = {
     "mlpcg_fluid_order": (_i, [_u8p, _i64, _vp, _vp]),
     "mlpcg_scatter_fluid": (_i, [_fp, _i64, _u8p, _vp, _i64, _fp, _vp]),
     "mlpcg_gather_fluid": (_i, [_fp, _u8p, _vp, _i64, _fp, _i64, _vp]),
+    "mlpcg_host_mapped": (_i, [_vp, _vp]),
     "mlpcg_dot_workspace": (_sz, [_i64]),
     "mlpcg_dot": (_i, [_vp, _vp, _i, _i64, _vp, _vp, _sz, _vp]),
     "mlpcg_dot_noalloc": (_i, [_vp, _vp, _i, _i64, _vp, _vp]),

@@ -328,6 +328,16 @@ int mlpcg_gather_fluid(const double *grid, const uint8_t *flags, const uint32_t 
   return launch_gather_fluid(grid, flags, order, n, fluid_values, m, as_stream(stream));
 }
 
+int mlpcg_host_mapped(const void *ptr, int *mapped) {
+  clear_error();
+  CHECK_PTR(ptr); CHECK_PTR(mapped);
+  cudaPointerAttributes a{};
+  const cudaError_t e = cudaPointerGetAttributes(&a, ptr);
+  if (e != cudaSuccess) cudaGetLastError();  // an address CUDA does not know: not mapped
+  *mapped = e == cudaSuccess && a.type == cudaMemoryTypeHost && a.devicePointer == ptr ? 1 : 0;
+  return MLPCG_OK;
+}
+
 size_t mlpcg_dot_workspace(int64_t n) { return dot_workspace(n < 1 ? 1 : n); }
 
 int mlpcg_dot(const void *x, const void *y, int dtype, int64_t n, double *out, void *workspace,

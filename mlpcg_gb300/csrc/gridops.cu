@@ -434,39 +434,50 @@ k_fluid_counts(const uint8_t *__restrict__ flags, int64_t n, uint32_t *__restric
 }
 
 // grid = the fluid values scattered to their cells, 0 elsewhere (and for
-// positions beyond the m values given)
+// positions beyond the m values given).  The block's values are one contiguous
+// range of vals: the block reads it with consecutive lanes on consecutive
+// values into shared memory (few, full transactions also when vals is host
+// memory read over the host link), then places them.
 __global__ void __launch_bounds__(kFluidThreads)
 k_scatter_fluid(const double *__restrict__ vals, int64_t m, const uint8_t *__restrict__ flags,
                 const uint32_t *__restrict__ base, int64_t n, double *__restrict__ grid) {
   dependent_launch_enter();
+  __shared__ double sv[kFluidBlock];
   const int64_t q0 = (int64_t)blockIdx.x * kFluidBlock + kFluidPer * threadIdx.x;
   const unsigned fm = fluid_bits(flags, n, q0);
   int tot;
-  int64_t pos = (int64_t)__ldg(base + blockIdx.x) + block256_excl_scan(__popc(fm), tot);
+  const int64_t b0 = (int64_t)__ldg(base + blockIdx.x);
+  int pos = block256_excl_scan(__popc(fm), tot);
+  for (int i = threadIdx.x; i < tot; i += kFluidThreads) sv[i] = b0 + i < m ? vals[b0 + i] : 0.0;
+  __syncthreads();
 #pragma unroll
   for (int u = 0; u < kFluidPer; ++u)
     if (q0 + u < n) {
       const bool f = (fm >> u) & 1u;
-      grid[q0 + u] = (f && pos < m) ? vals[pos] : 0.0;
+      grid[q0 + u] = f ? sv[pos] : 0.0;
       pos += f;
     }
 }
 
-// vals = the grid's values on the fluid cells (the first m of them)
+// vals = the grid's values on the fluid cells (the first m of them), placed in
+// shared memory first so that the block writes its contiguous range of vals
+// with consecutive lanes on consecutive values (full transactions also when
+// vals is host memory written over the host link)
 __global__ void __launch_bounds__(kFluidThreads)
 k_gather_fluid(const double *__restrict__ grid, const uint8_t *__restrict__ flags,
                const uint32_t *__restrict__ base, int64_t n, double *__restrict__ vals, int64_t m) {
   dependent_launch_enter();
+  __shared__ double sv[kFluidBlock];
   const int64_t q0 = (int64_t)blockIdx.x * kFluidBlock + kFluidPer * threadIdx.x;
   const unsigned fm = fluid_bits(flags, n, q0);
   int tot;
-  int64_t pos = (int64_t)__ldg(base + blockIdx.x) + block256_excl_scan(__popc(fm), tot);
+  const int64_t b0 = (int64_t)__ldg(base + blockIdx.x);
+  int pos = block256_excl_scan(__popc(fm), tot);
 #pragma unroll
   for (int u = 0; u < kFluidPer; ++u)
-    if ((fm >> u) & 1u) {
-      if (pos < m) vals[pos] = grid[q0 + u];
-      ++pos;
-    }
+    if ((fm >> u) & 1u) sv[pos++] = grid[q0 + u];
+  __syncthreads();
+  for (int i = threadIdx.x; i < tot && b0 + i < m; i += kFluidThreads) vals[b0 + i] = sv[i];
 }
 
 // ---------------------------------------------------------------------------

@@ -44,6 +44,15 @@ def flags_to_image(flags: torch.Tensor) -> torch.Tensor:
     return img
 
 
+def _host_mapped(t: torch.Tensor) -> bool:
+    """A contiguous FP64 tensor in pinned host memory that kernels reach at its own address."""
+    if t.is_cuda or t.dtype != torch.float64 or not t.is_contiguous() or not t.is_pinned():
+        return False
+    v = C.c_int(0)
+    call("mlpcg_host_mapped", C.c_void_p(t.data_ptr()), C.byref(v))
+    return bool(v.value)
+
+
 class FusedSolver:
     def __init__(self, model, flags: torch.Tensor, method="npsd", max_it=100, tol=1e-6, true_every=25,
                  storage=torch.bfloat16, act_storage=None, image=None, plan: PrecondPlan | None = None,
@@ -104,9 +113,12 @@ class FusedSolver:
         ``x_out_h``.  ``b_h`` and ``x_out_h`` are either full grids (N1*N2*N3 values) or fluid-DOF
         vectors -- one value per fluid cell of ``flags_h`` in flat cell order, the compressed vectors
         the reference's solvers take -- told apart by their size; fluid-DOF vectors move only the
-        fluid values over the host link.  The rhs is copied on a side stream while the image pyramid
-        and the coefficients are built from the flags, so its transfer hides behind the set-up.  With
-        pinned host buffers every copy is asynchronous; call ``result()`` to wait."""
+        fluid values over the host link.  The rhs is moved on a side stream while the image pyramid
+        and the coefficients are built from the flags, so its transfer hides behind the set-up.
+        Fluid-DOF vectors in pinned host memory that kernels reach (mlpcg_host_mapped) are read and
+        written by the scatter and gather kernels themselves, with no staging copy; other buffers go
+        through device copies.  With pinned host buffers every transfer is asynchronous; call
+        ``result()`` to wait."""
         dev = self.flags.device
         n = self.b.numel()
         fluid = b_h.numel() != n
@@ -118,26 +130,36 @@ class FusedSolver:
             self._order = torch.empty(int(self._lib.mlpcg_fluid_order_entries(n)), dtype=torch.int32, device=dev)
         side = self._side
         m = b_h.numel()
-        if fluid and (self._bf is None or self._bf.numel() < m):
+        direct_b = fluid and _host_mapped(b_h)
+        direct_x = fluid and x_out_h is not None and _host_mapped(x_out_h)
+        if fluid and not (direct_b and direct_x) and (self._bf is None or self._bf.numel() < m):
             self._bf = torch.empty(max(m, 1), dtype=torch.float64, device=dev)
             self._xf = torch.empty(max(m, 1), dtype=torch.float64, device=dev)
         side.wait_stream(main)  # the previous solve has finished with these buffers
-        with torch.cuda.stream(side):
-            if fluid:
-                self._bf[:m].copy_(b_h.reshape(-1), non_blocking=True)
-            else:
-                self.b.copy_(b_h.reshape(self.shape), non_blocking=True)
+        if not direct_b:
+            with torch.cuda.stream(side):
+                if fluid:
+                    self._bf[:m].copy_(b_h.reshape(-1), non_blocking=True)
+                else:
+                    self.b.copy_(b_h.reshape(self.shape), non_blocking=True)
         self.flags.copy_(flags_h.reshape(self.shape), non_blocking=True)
         st = _stream(dev)
         if fluid:
             call("mlpcg_fluid_order", _p(self.flags), n, _p(self._order), st)
+        if direct_b:  # the scatter reads the host vector beside the set-up, once the order is known
+            side.wait_stream(main)
+            call("mlpcg_scatter_fluid", C.c_void_p(b_h.data_ptr()), m, _p(self.flags), _p(self._order), n,
+                 _p(self.b), C.c_void_p(side.cuda_stream))
         self.set_image(model, flags_to_image(self.flags))
         main.wait_stream(side)
-        if fluid:
+        if fluid and not direct_b:
             call("mlpcg_scatter_fluid", _p(self._bf), m, _p(self.flags), _p(self._order), n, _p(self.b), st)
         self.launch(None, use_graph=use_graph)
         if x_out_h is not None:
-            if fluid:
+            if direct_x:
+                call("mlpcg_gather_fluid", _p(self.x), _p(self.flags), _p(self._order), n,
+                     C.c_void_p(x_out_h.data_ptr()), m, st)
+            elif fluid:
                 call("mlpcg_gather_fluid", _p(self.x), _p(self.flags), _p(self._order), n, _p(self._xf), m, st)
                 x_out_h.view(-1).copy_(self._xf[:m], non_blocking=True)
             else:

@@ -303,6 +303,7 @@ def main(argv=None):
             break
     log["train_s"] = time.time() - t_train
     log["steps_done"] = step
+    log["peak_device_gb"] = round(torch.cuda.max_memory_allocated(dev) / 1e9, 3)
     log["best"] = {"iterations": best[0], "rel_res": best[1]}
     save(model, out, args, log, best=False)
 

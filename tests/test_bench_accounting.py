@@ -27,6 +27,8 @@ def test_smallsm_iteration_bytes_dense():
     assert masked - got == pytest.approx(2 * N0)       # the block mask, read by both level-0 blocks
     swapped = bench.iteration_bytes(_plan(0, swap=True), N0, [None, None], method="npsd")
     assert swapped == pytest.approx(got)                # y read by the pass instead of the block
+    fused = bench.iteration_bytes(_plan(0), N0, [None, None], method="npsd", fused_dots=True)
+    assert got - fused == pytest.approx(4 * N0)         # z . Ap in the post-block: z not read again
 
 
 def test_spd_iteration_bytes_dense():

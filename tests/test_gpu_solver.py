@@ -277,8 +277,9 @@ def test_fluid_vectors_scatter_gather(cuda, shape):
 
 def test_solve_host_fluid_vectors(cuda):
     """solve_host with fluid-DOF vectors (the reference's compressed rhs / solution) equals the
-    grid solve on the fluid cells."""
-    from mlpcg_gb300.solver import FusedSolver
+    grid solve on the fluid cells, whether the kernels read and write the pinned host vectors
+    themselves or pageable vectors go through device copies."""
+    from mlpcg_gb300.solver import FusedSolver, _host_mapped
     s, flags, img = _scene((32, 32, 32), 6, cuda)
     m = _near_identity_model(3, cuda)
     solver = FusedSolver(m, flags.clone(), method="npsd", max_it=60, tol=1e-6)
@@ -287,10 +288,16 @@ def test_solve_host_fluid_vectors(cuda):
     x_ref = ref.x.cpu().reshape(-1)[torch.from_numpy(fl)]
     b_h = torch.from_numpy(np.ascontiguousarray(s.rhs.reshape(-1)[fl])).pin_memory()
     x_h = torch.empty(b_h.numel(), dtype=torch.float64).pin_memory()
+    assert _host_mapped(b_h) and _host_mapped(x_h) and not _host_mapped(b_h.clone())
     solver.solve_host(torch.from_numpy(s.flags).pin_memory(), b_h, x_h)
     r = solver.result()
     torch.cuda.synchronize()
     assert r.iterations == ref.iterations and torch.equal(x_h, x_ref)
+    b_p, x_p = b_h.clone(), torch.zeros_like(x_ref)       # pageable: staged copies
+    solver.solve_host(torch.from_numpy(s.flags), b_p, x_p)
+    r = solver.result()
+    torch.cuda.synchronize()
+    assert r.iterations == ref.iterations and torch.equal(x_p, x_ref)
 
 
 def test_batch_of_uneven_systems_matches_single_solves(cuda):
