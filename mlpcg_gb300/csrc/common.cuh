@@ -260,14 +260,12 @@ __device__ __forceinline__ float material_weight(const float *__restrict__ W, in
   return __fadd_rn(W[p * 81 + (mat == 1 ? 0 : 27) + pos], W[p * 81 + 54 + pos]);
 }
 
-template <int NB, typename Patch>
-__device__ __forceinline__ void coeffs_of_patch_n(const float4 *sW, const float4 *sWm, const float *sb, Patch v,
-                                                  float (*acc)[28]) {
-#pragma unroll
-  for (int b = 0; b < NB; ++b)
-#pragma unroll
-    for (int p = 0; p < 28; ++p) acc[b][p] = sb[b * 28 + p];
-  uint64_t mats = 0;
+// The material code of each patch position, 2 bits per position (position
+// m * 9 + nn * 3 + o at bits 2 pos); false when a position is none of the
+// three one-hot materials.
+template <typename Patch>
+__device__ __forceinline__ bool patch_materials(Patch v, uint64_t &mats) {
+  mats = 0;
   bool material = true;
 #pragma unroll
   for (int pos = 0; pos < 27; ++pos) {
@@ -276,25 +274,48 @@ __device__ __forceinline__ void coeffs_of_patch_n(const float4 *sW, const float4
     material = material && mt != 3;
     mats |= (uint64_t)(mt & 3) << (2 * pos);
   }
-  if (material) {
+  return material;
+}
+
+// The material form: the bias plus, position by position, the material's
+// table row (27 additions per coefficient).
+template <int NB>
+__device__ __forceinline__ void coeffs_of_materials_n(const float4 *sWm, const float *sb, uint64_t mats,
+                                                      float (*acc)[28]) {
 #pragma unroll
-    for (int pos = 0; pos < 27; ++pos) {
-      const int mt = (int)((mats >> (2 * pos)) & 3u);
+  for (int b = 0; b < NB; ++b)
 #pragma unroll
-      for (int b = 0; b < NB; ++b) {
-        const float4 *w = sWm + b * kSW + (mt * 27 + pos) * 7;
+    for (int p = 0; p < 28; ++p) acc[b][p] = sb[b * 28 + p];
 #pragma unroll
-        for (int pp = 0; pp < 7; ++pp) {
-          const float4 wv = w[pp];
-          acc[b][4 * pp + 0] = __fadd_rn(acc[b][4 * pp + 0], wv.x);
-          acc[b][4 * pp + 1] = __fadd_rn(acc[b][4 * pp + 1], wv.y);
-          acc[b][4 * pp + 2] = __fadd_rn(acc[b][4 * pp + 2], wv.z);
-          acc[b][4 * pp + 3] = __fadd_rn(acc[b][4 * pp + 3], wv.w);
-        }
+  for (int pos = 0; pos < 27; ++pos) {
+    const int mt = (int)((mats >> (2 * pos)) & 3u);
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      const float4 *w = sWm + b * kSW + (mt * 27 + pos) * 7;
+#pragma unroll
+      for (int pp = 0; pp < 7; ++pp) {
+        const float4 wv = w[pp];
+        acc[b][4 * pp + 0] = __fadd_rn(acc[b][4 * pp + 0], wv.x);
+        acc[b][4 * pp + 1] = __fadd_rn(acc[b][4 * pp + 1], wv.y);
+        acc[b][4 * pp + 2] = __fadd_rn(acc[b][4 * pp + 2], wv.z);
+        acc[b][4 * pp + 3] = __fadd_rn(acc[b][4 * pp + 3], wv.w);
       }
     }
+  }
+}
+
+template <int NB, typename Patch>
+__device__ __forceinline__ void coeffs_of_patch_n(const float4 *sW, const float4 *sWm, const float *sb, Patch v,
+                                                  float (*acc)[28]) {
+  uint64_t mats;
+  if (patch_materials(v, mats)) {
+    coeffs_of_materials_n<NB>(sWm, sb, mats, acc);
     return;
   }
+#pragma unroll
+  for (int b = 0; b < NB; ++b)
+#pragma unroll
+    for (int p = 0; p < 28; ++p) acc[b][p] = sb[b * 28 + p];
   for (int s = 0; s < 3; ++s) {
 #pragma unroll
     for (int m = 0; m < 3; ++m)

@@ -562,6 +562,104 @@ __device__ __forceinline__ RecPos rec_pos(const uint32_t *__restrict__ rw, const
   return rp;
 }
 
+// ---------------------------------------------------------------------------
+// Coefficient generation by neighbourhood pattern (level 0 of a one-hot image).
+// There every general cell's coefficients depend only on the 27 material codes
+// around it (the material form), and few distinct neighbourhoods occur: walls
+// and sphere surfaces repeat them.  k_pattern_keys puts each general cell's
+// 54-bit pattern into an open-addressed hash table (bounded linear probing)
+// and records its slot; k_pattern_coeffs evaluates every distinct pattern once
+// (coeffs_of_materials_n, the arithmetic of the per-cell path) into a table;
+// k_kgen_list then copies each cell's values from it.  A cell whose patch is not
+// one-hot, whose probe runs out, or whose pattern finds no table room
+// (kPatMax) evaluates its own patch.  The table order depends on the insertion
+// race, the values do not.
+// ---------------------------------------------------------------------------
+constexpr int kPatBits = 19;
+constexpr uint32_t kPatSlots = 1u << kPatBits;  // hash slots
+constexpr uint32_t kPatMax = 1u << 17;          // distinct patterns with table values
+constexpr int kPatProbe = 64;                   // slots tried per insertion
+constexpr unsigned long long kPatEmpty = ~0ull; // no 54-bit key has all bits set
+constexpr uint32_t kNoPattern = 0xffffffffu;
+
+// The pattern table as the record writers see it: cell_slot[q] is general cell q's hash slot
+// (kNoPattern: none), pidx[slot] its table entry (kNoPattern: none), pcoef the entries'
+// coefficients (NB blocks x 28 floats each).  cell_slot == NULL: no table.
+struct PatternArgs {
+  const uint32_t *cell_slot, *pidx;
+  const float *pcoef;
+};
+
+// cell_slot is indexed by cell (written for the general cells)
+__global__ void __launch_bounds__(256)
+k_pattern_keys(const float *__restrict__ img, int n1, int n2, int n3, const uint32_t *__restrict__ list,
+               const uint32_t *__restrict__ glast_base, const uint32_t *__restrict__ glast_count,
+               unsigned long long *__restrict__ keys, uint32_t *__restrict__ cell_slot) {
+  dependent_launch_enter();
+  const uint32_t G = __ldg(glast_base) + __ldg(glast_count);
+  const FieldGeom g = FieldGeom::make(n1, n2, n3, 0);
+  for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < G; e += gridDim.x * blockDim.x) {
+    const uint32_t q = __ldg(list + e);
+    const int k = (int)(q % (uint32_t)n3);
+    const uint32_t t = q / (uint32_t)n3;
+    const int j = (int)(t % (uint32_t)n2), i = (int)(t / (uint32_t)n2);
+    uint64_t mats;
+    uint32_t slot = kNoPattern;
+    if (patch_materials([&](int s, int m, int nn, int o) {
+          return g.at(img + s * g.bstride, i + m - 1, j + nn - 1, k + o - 1);
+        }, mats)) {
+      const unsigned long long key = mats;
+      const uint32_t h = (uint32_t)((key * 0x9E3779B97F4A7C15ull) >> (64 - kPatBits));
+      for (int p = 0; p < kPatProbe; ++p) {
+        const uint32_t sl = (h + (uint32_t)p) & (kPatSlots - 1);
+        unsigned long long cur = *reinterpret_cast<volatile unsigned long long *>(keys + sl);
+        if (cur == kPatEmpty) cur = atomicCAS(keys + sl, kPatEmpty, key);
+        if (cur == kPatEmpty || cur == key) {
+          slot = sl;
+          break;
+        }
+      }
+    }
+    cell_slot[q] = slot;
+  }
+}
+
+// One thread per hash slot: an occupied slot takes the next table entry (while
+// there is room) and its pattern's coefficients for the NB blocks.
+template <int NB>
+__global__ void __launch_bounds__(256)
+k_pattern_coeffs(const float *__restrict__ params, int b0, int b1, const unsigned long long *__restrict__ keys,
+                 uint32_t *__restrict__ pidx, uint32_t *__restrict__ pcount, float *__restrict__ pcoef) {
+  dependent_launch_enter();
+  __shared__ float4 sW[NB * kSW];
+  __shared__ float4 sWm[NB * kSW];
+  __shared__ float sb[NB * 28];
+#pragma unroll
+  for (int b = 0; b < NB; ++b) {
+    const float *W = params + (size_t)(b ? b1 : b0) * 2214;
+    load_weights_smem(W, W + 2187, sW + b * kSW, sWm + b * kSW, sb + b * 28);
+  }
+  __syncthreads();
+  for (uint32_t sl = blockIdx.x * blockDim.x + threadIdx.x; sl < kPatSlots; sl += gridDim.x * blockDim.x) {
+    const unsigned long long key = __ldg(keys + sl);
+    if (key == kPatEmpty) continue;
+    const uint32_t idx = atomicAdd(pcount, 1u);
+    if (idx >= kPatMax) {
+      pidx[sl] = kNoPattern;
+      continue;
+    }
+    float acc[NB][28];
+    coeffs_of_materials_n<NB>(sWm, sb, key, acc);
+    float4 *c = reinterpret_cast<float4 *>(pcoef + (size_t)idx * NB * 28);
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
+#pragma unroll
+      for (int v = 0; v < 7; ++v)
+        c[b * 7 + v] = make_float4(acc[b][4 * v], acc[b][4 * v + 1], acc[b][4 * v + 2], acc[b][4 * v + 3]);
+    pidx[sl] = idx;
+  }
+}
+
 // The uniform cells of every mixed run, for NB blocks (uniform vectors at
 // kuni0 / kuni1): thread (p, e) writes tap p of the record of mixed run e --
 // the run's 8 cells, contiguous in the record -- as one vector store, its
@@ -602,17 +700,74 @@ k_fill_runs(const uint8_t *__restrict__ cls, const uint32_t *__restrict__ rlist,
   }
 }
 
+// k_fill_runs with the pattern table (level 0): thread e writes the whole record of mixed run e,
+// looking up its general cells' table entries once; for each tap, consecutive threads store
+// consecutive runs' 16 bytes.  General cells without table values are written 0 (k_kgen_list
+// evaluates them afterwards).
+template <typename KT, int NB>
+__global__ void __launch_bounds__(256)
+k_fill_runs_pattern(const uint8_t *__restrict__ cls, const uint32_t *__restrict__ rlist,
+                    const uint32_t *__restrict__ rlast_base, const uint32_t *__restrict__ rlast_count,
+                    const uint32_t *__restrict__ rw, const uint32_t *__restrict__ rbase,
+                    const uint32_t *__restrict__ rcount, int n2, int n3, const float *__restrict__ kuni0,
+                    const float *__restrict__ kuni1, KT *__restrict__ rec0, KT *__restrict__ rec1,
+                    const PatternArgs pat) {
+  dependent_launch_enter();
+  const uint32_t nrun = __ldg(rlast_base) + __ldg(rlast_count);
+  for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < nrun; e += gridDim.x * blockDim.x) {
+    const uint32_t q = 8u * __ldg(rlist + e);
+    const int k = (int)(q % (uint32_t)n3);
+    const uint32_t r = q / (uint32_t)n3;
+    const int j = (int)(r % (uint32_t)n2), i = (int)(r / (uint32_t)n2);
+    const RecPos rp = rec_pos(rw, rbase, rcount, q, i, j, k, n2, n3);
+    const uint2 cw = __ldg(reinterpret_cast<const uint2 *>(cls + q));
+    // per cell: a material (0..2), or a table row (row + 3), or none (-1: written 0)
+    int64_t src[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      const int cl = class_of(cw, c);
+      src[c] = cl;
+      if (cl == CLS_GENERAL) {
+        src[c] = -1;
+        const uint32_t slot = __ldg(pat.cell_slot + q + c);
+        if (slot != kNoPattern) {
+          const uint32_t idx = __ldg(pat.pidx + slot);
+          if (idx != kNoPattern) src[c] = 3 + (int64_t)idx * NB * 28;
+        }
+      }
+    }
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      const float *ku = b ? kuni1 : kuni0;
+      KT *rec = (b ? rec1 : rec0) + rp.offset;
+      for (int p = 0; p < 27; ++p) {
+        float v[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c)
+          v[c] = src[c] < 0 ? 0.f
+                            : (src[c] < 3 ? __ldg(ku + src[c] * KREC + p) : __ldg(pat.pcoef + (src[c] - 3) + b * 28 + p));
+        st8(rec + (size_t)p * rp.stride, v);
+      }
+    }
+  }
+}
+
 // The coefficients of every general cell for NB blocks of one level at once
 // (the pre- and post-block share the level's image and run words), written
 // into the records of their runs.  Thread e of the grid-stride loop evaluates
 // list[e]; the count of general cells is read on the device.
+//
+// With the pattern table (PatternArgs), k_fill_runs has already written the
+// general cells whose pattern has table values; this kernel evaluates the
+// others' patches.
+
 template <typename KT, int NB>
 __global__ void __launch_bounds__(PT)
 k_kgen_list(const float *__restrict__ img, int n1, int n2, int n3, const float *__restrict__ params, int b0, int b1,
             const uint32_t *__restrict__ list, const uint32_t *__restrict__ glast_base,
             const uint32_t *__restrict__ glast_count, const uint32_t *__restrict__ rw,
             const uint32_t *__restrict__ rbase, const uint32_t *__restrict__ rcount, KT *__restrict__ rec0,
-            KT *__restrict__ rec1) {
+            KT *__restrict__ rec1, const PatternArgs pat) {
   dependent_launch_enter();
   __shared__ float4 sW[NB * kSW];
   __shared__ float4 sWm[NB * kSW];
@@ -630,6 +785,10 @@ k_kgen_list(const float *__restrict__ img, int n1, int n2, int n3, const float *
     const int k = (int)(q % (uint32_t)n3);
     const uint32_t t = q / (uint32_t)n3;
     const int j = (int)(t % (uint32_t)n2), i = (int)(t / (uint32_t)n2);
+    if (pat.cell_slot) {  // written by k_fill_runs when its pattern has table values
+      const uint32_t slot = __ldg(pat.cell_slot + q);
+      if (slot != kNoPattern && __ldg(pat.pidx + slot) != kNoPattern) continue;
+    }
     float acc[NB][28];
     coeffs_of_patch_n<NB>(sW, sWm, sb, [&](int s, int m, int nn, int o) {
       return g.at(img + s * g.bstride, i + m - 1, j + nn - 1, k + o - 1);
@@ -1384,6 +1543,26 @@ __device__ __forceinline__ void post_fused_body(const CoefArgs<KT> &C, const CT 
   const uint2 tb = load_tile_runs<KT, CLS>(C, t, n1, n2, n3, rwd);
   load_run_mask(bmask, t, n1, n2, n3, bw);
   load_run_mask(omask, t, n1, n2, n3, ow);
+  // ZD: products wanted (0, 1 or 2, the same for the whole CTA) and their vectors, whose segments
+  // of the thread's runs are asked into L2 now so that the epilogue's loads find them there
+  int nd = 0;
+  const float *a1 = nullptr, *a0 = nullptr;
+  if constexpr (ZD) {
+    const int it = __ldg(zd->it), h = __ldg(zd->head);
+    nd = it < 2 ? it : 2;
+    a1 = zd->ring + (size_t)h * zd->n;
+    a0 = zd->ring + (size_t)((h + 2) % 3) * zd->n;
+    const int pk = z0 + run_tz(threadIdx.x) * 8, pj = y0 + run_ty(threadIdx.x);
+    if (nd > 0 && pk < n3 && pj < n2) {
+#pragma unroll
+      for (int tx = 0; tx < TX; ++tx) {
+        if (x0 + tx >= n1) continue;
+        const int64_t q = ((int64_t)(x0 + tx) * n2 + pj) * n3 + pk;
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(a1 + q));
+        if (nd == 2) asm volatile("prefetch.global.L2 [%0];" ::"l"(a0 + q));
+      }
+    }
+  }
   if (UPIN) {
     if constexpr (!TMA) {
       FineStage fs;
@@ -1442,15 +1621,6 @@ __device__ __forceinline__ void post_fused_body(const CoefArgs<KT> &C, const CT 
   const int tz = run_tz(threadIdx.x), ty = run_ty(threadIdx.x);
   const int k0 = z0 + tz * 8, j = y0 + ty;
   const bool active = k0 < n3 && j < n2;
-  // ZD: products wanted (0, 1 or 2, the same for the whole CTA) and their vectors
-  int nd = 0;
-  const float *a1 = nullptr, *a0 = nullptr;
-  if constexpr (ZD) {
-    const int it = __ldg(zd->it), h = __ldg(zd->head);
-    nd = it < 2 ? it : 2;
-    a1 = zd->ring + (size_t)h * zd->n;
-    a0 = zd->ring + (size_t)((h + 2) % 3) * zd->n;
-  }
   float s1 = 0.f, s0 = 0.f;
 #pragma unroll
   for (int tx = 0; tx < TX; ++tx) {
@@ -1679,6 +1849,11 @@ struct PrecondPlan {
   uint32_t *glist = nullptr;  // general-cell list (setup scratch)
   uint32_t *rlist = nullptr;  // mixed-run list (setup scratch)
   uint32_t *glist2 = nullptr, *rlist2 = nullptr;  // the same for levels >= 1 (SM kind, side stream)
+  // level-0 pattern table (classed level 0): hash keys, table index per slot, entries used,
+  // coefficients per entry (2 blocks), pattern slot per general cell
+  unsigned long long *pkeys = nullptr;
+  uint32_t *pidx = nullptr, *pcount = nullptr, *cell_slot = nullptr;  // cell_slot: per level-0 cell
+  float *pcoef = nullptr;
   // setup: level 0's coefficient chain runs on the caller's stream, levels >= 1 and the linear
   // blocks on this stream beside it (forked and joined with the two events)
   cudaStream_t side = nullptr;
@@ -1733,7 +1908,7 @@ static int resident_ctas(F f) {
 template <typename KT>
 static KT *kgen_rec_type(void (*)(const float *, int, int, int, const float *, int, int, const uint32_t *,
                                   const uint32_t *, const uint32_t *, const uint32_t *, const uint32_t *,
-                                  const uint32_t *, KT *, KT *));
+                                  const uint32_t *, KT *, KT *, const PatternArgs));
 
 // blocks with uniform vectors / material records: 2L + 1 forward, plus l_t (SMALL_SPD kind) or
 // the 2L + 1 transposes (SPD kind)
@@ -1839,6 +2014,13 @@ static size_t plan_layout(PrecondPlan &P, char *base) {
   const bool par = P.kind == MLPCG_PRECOND_SM && nlist2 > 0;
   P.glist2 = par ? (uint32_t *)take((size_t)nlist2 * sizeof(uint32_t)) : nullptr;
   P.rlist2 = par ? (uint32_t *)take((size_t)(nlist2 / 8 + 1) * sizeof(uint32_t)) : nullptr;
+  if (P.lv[0].cls && nlist) {
+    P.pkeys = (unsigned long long *)take((size_t)kPatSlots * sizeof(unsigned long long));
+    P.pidx = (uint32_t *)take((size_t)kPatSlots * sizeof(uint32_t));
+    P.pcount = (uint32_t *)take(sizeof(uint32_t));
+    P.pcoef = (float *)take((size_t)kPatMax * 2 * 28 * sizeof(float));
+    P.cell_slot = (uint32_t *)take((size_t)P.lv[0].n * sizeof(uint32_t));
+  }
   for (int l = 0; l < P.L; ++l) P.y[l] = take(P.lv[l].ps * sa);
   for (int l = 1; l <= P.L; ++l) {
     P.xin[l] = take(P.lv[l].ps * sa);
@@ -2659,13 +2841,35 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
     const int fgrid = (int)std::min<int64_t>((int64_t)sm_count() * 8, (27 * (v.n / 8) + 255) / 256);
     const uint32_t *rlb = P.rbase[l] + v.ntiles - 1, *rlc = P.rcount[l] + v.ntiles - 1;
     // the mixed runs' uniform cells first (whole taps per vector store), then the general cells
+    // level 0 (one-hot image): the distinct neighbourhood patterns' coefficients first
+    PatternArgs pat{nullptr, nullptr, nullptr};
+    if (l == 0 && P.pkeys && gl == P.glist) {
+      MLPCG_CUDA_CHECK(cudaMemsetAsync(P.pkeys, 0xff, (size_t)kPatSlots * sizeof(unsigned long long), gs));
+      MLPCG_CUDA_CHECK(cudaMemsetAsync(P.pcount, 0, sizeof(uint32_t), gs));
+      k_pattern_keys<<<sm_count() * 8, 256, 0, gs>>>(im, v.n1, v.n2, v.n3, gl, lb, lc, P.pkeys, P.cell_slot);
+      MLPCG_LAUNCH_CHECK();
+      if (b1 >= 0) k_pattern_coeffs<2><<<sm_count() * 2, 256, 0, gs>>>(params, b0, b1, P.pkeys, P.pidx, P.pcount, P.pcoef);
+      else k_pattern_coeffs<1><<<sm_count() * 2, 256, 0, gs>>>(params, b0, b0, P.pkeys, P.pidx, P.pcount, P.pcoef);
+      MLPCG_LAUNCH_CHECK();
+      pat = PatternArgs{P.cell_slot, P.pidx, P.pcoef};
+    }
     auto launch = [&](auto kern, auto fill, const void *r0, const void *r1) {
       using KT = typename std::remove_pointer<decltype(kgen_rec_type(kern))>::type;
-      fill<<<fgrid, 256, 0, gs>>>(P.cls[l], rl, rlb, rlc, P.rw[l], P.rbase[l], P.rcount[l], v.n2, v.n3, u0, u1,
-                                  (KT *)r0, (KT *)r1);
+      if (pat.cell_slot) {
+        const int rgrid = (int)std::min<int64_t>((int64_t)sm_count() * 8, (v.n / 8 + 255) / 256);
+        if (b1 >= 0)
+          k_fill_runs_pattern<KT, 2><<<rgrid, 256, 0, gs>>>(P.cls[l], rl, rlb, rlc, P.rw[l], P.rbase[l], P.rcount[l],
+                                                            v.n2, v.n3, u0, u1, (KT *)r0, (KT *)r1, pat);
+        else
+          k_fill_runs_pattern<KT, 1><<<rgrid, 256, 0, gs>>>(P.cls[l], rl, rlb, rlc, P.rw[l], P.rbase[l], P.rcount[l],
+                                                            v.n2, v.n3, u0, u1, (KT *)r0, (KT *)r1, pat);
+      } else {
+        fill<<<fgrid, 256, 0, gs>>>(P.cls[l], rl, rlb, rlc, P.rw[l], P.rbase[l], P.rcount[l], v.n2, v.n3, u0, u1,
+                                    (KT *)r0, (KT *)r1);
+      }
       const int grid = (int)std::min<int64_t>((int64_t)sm_count() * resident_ctas(kern), (v.n + PT - 1) / PT);
       kern<<<grid, PT, 0, gs>>>(im, v.n1, v.n2, v.n3, params, b0, b1 >= 0 ? b1 : b0, gl, lb, lc, P.rw[l],
-                                P.rbase[l], P.rcount[l], (KT *)r0, (KT *)r1);
+                                P.rbase[l], P.rcount[l], (KT *)r0, (KT *)r1, pat);
     };
     if (P.kdt == MLPCG_BF16) {
       if (b1 >= 0) launch(k_kgen_list<__nv_bfloat16, 2>, k_fill_runs<__nv_bfloat16, 2>, K0, K1);

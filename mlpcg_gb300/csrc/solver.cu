@@ -566,9 +566,20 @@ __global__ void __launch_bounds__(ZT_THREADS) k_sd_dots_tiles(Vecs V) {
   }
   __shared__ double red[2][ZT_THREADS / 32];
   double a1 = 0.0, a0 = 0.0;
-  for (int64_t t = threadIdx.x; t < V.ztiles; t += ZT_THREADS) {
-    a1 += V.zpart[2 * t];
-    a0 += V.zpart[2 * t + 1];
+  // tiles t, t + 1024, ... in ascending order, eight loads in flight at a time
+  const double2 *zp = reinterpret_cast<const double2 *>(V.zpart);
+  for (int64_t t0 = threadIdx.x; t0 < V.ztiles; t0 += 8 * ZT_THREADS) {
+    double2 v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int64_t t = t0 + (int64_t)u * ZT_THREADS;
+      v[u] = t < V.ztiles ? zp[t] : make_double2(0.0, 0.0);
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      a1 += v[u].x;
+      a0 += v[u].y;
+    }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
