@@ -1814,6 +1814,21 @@ __global__ void k_fluid_mask(const float *__restrict__ img, uint8_t *__restrict_
   if (q >= n) return;
   m[q] = img[n + q] != 0.f;  // channel 1 = fluid (the reference masks with image[1] == 0)
 }
+// the same, 16 cells per thread (n a multiple of 16: 16-byte loads of channel 1, one 16-byte store)
+__global__ void k_fluid_mask16(const float *__restrict__ img, uint8_t *__restrict__ m, int64_t n) {
+  dependent_launch_enter();
+  const int64_t q = 16 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+  if (q >= n) return;
+  const float4 *f = reinterpret_cast<const float4 *>(img + n + q);
+  uint32_t w[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const float4 v = __ldg(f + u);
+    w[u] = (v.x != 0.f ? 1u : 0u) | (v.y != 0.f ? 1u << 8 : 0u) | (v.z != 0.f ? 1u << 16 : 0u) |
+           (v.w != 0.f ? 1u << 24 : 0u);
+  }
+  *reinterpret_cast<uint4 *>(m + q) = make_uint4(w[0], w[1], w[2], w[3]);
+}
 
 // ---------------------------------------------------------------------------
 // the plan object (host side; all device memory is the caller's workspace)
@@ -2775,14 +2790,31 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
   auto blk_w = [&](int b) { return params + (size_t)b * 2214; };
   auto blk_b = [&](int b) { return params + (size_t)b * 2214 + 2187; };
   const float *linp = params + (size_t)nblk * 2214;
-  // image pyramid
-  for (int l = 1; l <= L; ++l) {
-    const auto &v = P.lv[l - 1];
-    const float *src = (l == 1) ? image : P.img[l - 1];
-    RET_IF(launch_avg_pool2(src, P.img[l], MLPCG_F32, 3, v.n1, v.n2, v.n3, st));
+  // image pyramid (the SM kind's side stream builds it beside level 0's chain, below)
+  const bool side_chain = P.kind == MLPCG_PRECOND_SM && P.glist2;
+  auto pyramid = [&](cudaStream_t ps) -> int {
+    for (int l = 1; l <= L; ++l) {
+      const auto &v = P.lv[l - 1];
+      const float *src = (l == 1) ? image : P.img[l - 1];
+      RET_IF(launch_avg_pool2(src, P.img[l], MLPCG_F32, 3, v.n1, v.n2, v.n3, ps));
+    }
+    return MLPCG_OK;
+  };
+  auto fluid_mask = [&]() -> int {
+    const int64_t n0 = P.lv[0].n;
+    // 16-byte loads of channel 1 and stores of the mask when n0 is a multiple of 16 and the image
+    // 16-byte aligned (the mask is 256-byte aligned)
+    if (n0 % 16 == 0 && ((uintptr_t)image & 15) == 0)
+      k_fluid_mask16<<<blocks_for(n0 / 16, 256), 256, 0, st>>>(image, P.fmask, n0);
+    else
+      k_fluid_mask<<<blocks_for(n0, 256), 256, 0, st>>>(image, P.fmask, n0);
+    MLPCG_LAUNCH_CHECK();
+    return MLPCG_OK;
+  };
+  if (!side_chain) {
+    RET_IF(pyramid(st));
+    RET_IF(fluid_mask());
   }
-  k_fluid_mask<<<blocks_for(P.lv[0].n, 256), 256, 0, st>>>(image, P.fmask, P.lv[0].n);
-  MLPCG_LAUNCH_CHECK();
   // coefficients: dense planes, or class map + uniform vectors + general-cell records
   bool any_cls = false;
   for (int l = 0; l <= L; ++l) any_cls = any_cls || P.lv[l].cls;
@@ -2944,7 +2976,7 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
     RET_IF(gen_level(L, P.img[L], L, P.Kl, -1, nullptr, 2 * L));
     RET_IF(classify_t(L));
     RET_IF(gather_t(L, P.Kl, 2 * L, P.Klt, 2 * L + 1));
-  } else if (P.kind == MLPCG_PRECOND_SM && P.glist2) {
+  } else if (side_chain) {
     // levels >= 1 and then every level's c0 / c1 on the side stream, level 0 on the caller's
     if (!P.side) {
       // the side chain's kernels are small and latency-bound: the highest priority lets their CTAs
@@ -2960,6 +2992,7 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
     gs = P.side;
     gl = P.glist2;
     rl = P.rlist2;
+    RET_IF(pyramid(P.side));
     for (int l = 1; l < L; ++l) RET_IF(gen_level(l, P.img[l], l, P.Kpre[l], L + l, P.Kpost[l]));
     RET_IF(gen_level(L, P.img[L], 2 * L, P.Kl, -1, nullptr));
     RET_IF(setup_linear(P.side));
@@ -2967,6 +3000,7 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
     gs = st;
     gl = P.glist;
     rl = P.rlist;
+    RET_IF(fluid_mask());
     RET_IF(gen_level(0, image, 0, P.Kpre[0], L, P.Kpost[0]));
     MLPCG_CUDA_CHECK(cudaStreamWaitEvent(st, P.join_ev, 0));
     linear_done = true;
