@@ -245,6 +245,39 @@ constexpr uint32_t kMixed = 3;  // run word: bits 0-1 material or kMixed, bits 2
 
 // the class codes of the materials are patch_material's
 static_assert(CLS_SOLID == 0 && CLS_AIR == 1 && CLS_FLUID == 2 && CLS_GENERAL == 3, "material codes");
+
+// ---------------------------------------------------------------------------
+// Neighbourhood pattern table (level 0 of a one-hot image; see k_pattern_coeffs).
+// ---------------------------------------------------------------------------
+constexpr int kPatBits = 19;
+constexpr uint32_t kPatSlots = 1u << kPatBits;  // hash slots
+constexpr uint32_t kPatMax = 1u << 17;          // distinct patterns with table values
+constexpr int kPatProbe = 64;                   // slots tried per insertion
+constexpr unsigned long long kPatEmpty = ~0ull; // no 54-bit key has all bits set
+constexpr uint32_t kNoPattern = 0xffffffffu;
+
+// The pattern table as the record writers see it: cell_slot[q] is general cell q's hash slot
+// (kNoPattern: none), pidx[slot] its table entry (kNoPattern: none), pcoef the entries'
+// coefficients (NB blocks x 28 floats each), *fail nonzero when some general cell has no table
+// values.  cell_slot == NULL: no table.
+struct PatternArgs {
+  const uint32_t *cell_slot, *pidx;
+  const float *pcoef;
+  const uint32_t *fail;
+};
+
+// key's slot in the open-addressed table (linear probing from its hash, at most kPatProbe slots;
+// an empty slot is claimed with one compare-and-swap), or kNoPattern when the probe runs out
+__device__ __forceinline__ uint32_t pattern_insert(unsigned long long *keys, unsigned long long key) {
+  const uint32_t h = (uint32_t)((key * 0x9E3779B97F4A7C15ull) >> (64 - kPatBits));
+  for (int p = 0; p < kPatProbe; ++p) {
+    const uint32_t sl = (h + (uint32_t)p) & (kPatSlots - 1);
+    unsigned long long cur = *reinterpret_cast<volatile unsigned long long *>(keys + sl);
+    if (cur == kPatEmpty) cur = atomicCAS(keys + sl, kPatEmpty, key);
+    if (cur == kPatEmpty || cur == key) return sl;
+  }
+  return kNoPattern;
+}
 __device__ __forceinline__ int material_of(float a, float f, float s) { return patch_material(a, f, s); }
 __device__ __forceinline__ int class_of(uint2 cw, int c) {
   return (int)(((c < 4 ? cw.x : cw.y) >> (8 * (c & 3))) & 0xffu);
@@ -308,7 +341,8 @@ template <bool FROM_CLS>
 __global__ void __launch_bounds__(PT)
 k_classify(const float *__restrict__ img, const uint8_t *__restrict__ src_cls, int n1, int n2, int n3,
            uint8_t *__restrict__ cls, uint32_t *__restrict__ rw, uint32_t *__restrict__ rcount,
-           uint32_t *__restrict__ gcount) {
+           uint32_t *__restrict__ gcount, unsigned long long *__restrict__ pkeys, uint32_t *__restrict__ cell_slot,
+           uint32_t *__restrict__ pfail) {
   dependent_launch_enter();
   __shared__ __align__(16) uint8_t M[HX][HY][HZP];
   const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY, x0 = blockIdx.z * TX;
@@ -408,6 +442,28 @@ k_classify(const float *__restrict__ img, const uint8_t *__restrict__ src_cls, i
         all |= 1u << cl;
       }
       *reinterpret_cast<uint2 *>(cls + ((int64_t)i * n2 + j) * n3 + k0) = make_uint2(w[0], w[1]);
+      if (!FROM_CLS && pkeys) {
+        // each general cell's neighbourhood pattern -- 27 material codes, 2 bits each -- into the table
+#pragma unroll 1
+        for (int c = 0; c < 8; ++c) {
+          if (((w[c >> 2] >> (8 * (c & 3))) & 0xffu) != CLS_GENERAL) continue;
+          unsigned long long key = 0;
+          bool one_hot = true;
+#pragma unroll
+          for (int dx = 0; dx < 3; ++dx)
+#pragma unroll
+            for (int dy = 0; dy < 3; ++dy)
+#pragma unroll
+              for (int dz = 0; dz < 3; ++dz) {
+                const uint32_t code = M[tx + dx][ty + dy][tz * 8 + c + dz];
+                one_hot = one_hot && code != 3u;
+                key |= (unsigned long long)(code & 3u) << (2 * (dx * 9 + dy * 3 + dz));
+              }
+          const uint32_t slot = one_hot ? pattern_insert(pkeys, key) : kNoPattern;
+          if (slot == kNoPattern) atomicOr(pfail, 1u);
+          cell_slot[((int64_t)i * n2 + j) * n3 + k0 + c] = slot;
+        }
+      }
       mixed[tx] = __popc(all) != 1 || (all & (1u << CLS_GENERAL));
       word[tx] = mixed[tx] ? kMixed : (uint32_t)(__ffs(all) - 1);
       nmixed += mixed[tx];
@@ -566,70 +622,24 @@ __device__ __forceinline__ RecPos rec_pos(const uint32_t *__restrict__ rw, const
 // Coefficient generation by neighbourhood pattern (level 0 of a one-hot image).
 // There every general cell's coefficients depend only on the 27 material codes
 // around it (the material form), and few distinct neighbourhoods occur: walls
-// and sphere surfaces repeat them.  k_pattern_keys puts each general cell's
-// 54-bit pattern into an open-addressed hash table (bounded linear probing)
-// and records its slot; k_pattern_coeffs evaluates every distinct pattern once
-// (coeffs_of_materials_n, the arithmetic of the per-cell path) into a table;
-// k_kgen_list then copies each cell's values from it.  A cell whose patch is not
-// one-hot, whose probe runs out, or whose pattern finds no table room
-// (kPatMax) evaluates its own patch.  The table order depends on the insertion
-// race, the values do not.
+// and sphere surfaces repeat them.  k_classify puts each general cell's 54-bit
+// pattern into an open-addressed hash table (pattern_insert) and records its
+// slot; k_pattern_coeffs evaluates every distinct pattern once with the
+// arithmetic of the per-cell path into a table; k_fill_runs_pattern writes the
+// records from it.  A cell whose patch is not one-hot, whose probe runs out, or
+// whose pattern finds no table room (kPatMax) raises the failure flag and is
+// evaluated by k_kgen_list as before.  The table order depends on the
+// insertion race, the values do not.
 // ---------------------------------------------------------------------------
-constexpr int kPatBits = 19;
-constexpr uint32_t kPatSlots = 1u << kPatBits;  // hash slots
-constexpr uint32_t kPatMax = 1u << 17;          // distinct patterns with table values
-constexpr int kPatProbe = 64;                   // slots tried per insertion
-constexpr unsigned long long kPatEmpty = ~0ull; // no 54-bit key has all bits set
-constexpr uint32_t kNoPattern = 0xffffffffu;
 
-// The pattern table as the record writers see it: cell_slot[q] is general cell q's hash slot
-// (kNoPattern: none), pidx[slot] its table entry (kNoPattern: none), pcoef the entries'
-// coefficients (NB blocks x 28 floats each).  cell_slot == NULL: no table.
-struct PatternArgs {
-  const uint32_t *cell_slot, *pidx;
-  const float *pcoef;
-};
-
-// cell_slot is indexed by cell (written for the general cells)
-__global__ void __launch_bounds__(256)
-k_pattern_keys(const float *__restrict__ img, int n1, int n2, int n3, const uint32_t *__restrict__ list,
-               const uint32_t *__restrict__ glast_base, const uint32_t *__restrict__ glast_count,
-               unsigned long long *__restrict__ keys, uint32_t *__restrict__ cell_slot) {
-  dependent_launch_enter();
-  const uint32_t G = __ldg(glast_base) + __ldg(glast_count);
-  const FieldGeom g = FieldGeom::make(n1, n2, n3, 0);
-  for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < G; e += gridDim.x * blockDim.x) {
-    const uint32_t q = __ldg(list + e);
-    const int k = (int)(q % (uint32_t)n3);
-    const uint32_t t = q / (uint32_t)n3;
-    const int j = (int)(t % (uint32_t)n2), i = (int)(t / (uint32_t)n2);
-    uint64_t mats;
-    uint32_t slot = kNoPattern;
-    if (patch_materials([&](int s, int m, int nn, int o) {
-          return g.at(img + s * g.bstride, i + m - 1, j + nn - 1, k + o - 1);
-        }, mats)) {
-      const unsigned long long key = mats;
-      const uint32_t h = (uint32_t)((key * 0x9E3779B97F4A7C15ull) >> (64 - kPatBits));
-      for (int p = 0; p < kPatProbe; ++p) {
-        const uint32_t sl = (h + (uint32_t)p) & (kPatSlots - 1);
-        unsigned long long cur = *reinterpret_cast<volatile unsigned long long *>(keys + sl);
-        if (cur == kPatEmpty) cur = atomicCAS(keys + sl, kPatEmpty, key);
-        if (cur == kPatEmpty || cur == key) {
-          slot = sl;
-          break;
-        }
-      }
-    }
-    cell_slot[q] = slot;
-  }
-}
-
-// One thread per hash slot: an occupied slot takes the next table entry (while
-// there is room) and its pattern's coefficients for the NB blocks.
+// One warp per occupied hash slot: lane 0 takes the next table entry (while there is room), lane p
+// (< 28) sums coefficient p of each block -- the bias, then the material table row of each position
+// in order, as coeffs_of_materials_n does -- and stores it.
 template <int NB>
 __global__ void __launch_bounds__(256)
 k_pattern_coeffs(const float *__restrict__ params, int b0, int b1, const unsigned long long *__restrict__ keys,
-                 uint32_t *__restrict__ pidx, uint32_t *__restrict__ pcount, float *__restrict__ pcoef) {
+                 uint32_t *__restrict__ pidx, uint32_t *__restrict__ pcount, float *__restrict__ pcoef,
+                 uint32_t *__restrict__ pfail) {
   dependent_launch_enter();
   __shared__ float4 sW[NB * kSW];
   __shared__ float4 sWm[NB * kSW];
@@ -640,23 +650,40 @@ k_pattern_coeffs(const float *__restrict__ params, int b0, int b1, const unsigne
     load_weights_smem(W, W + 2187, sW + b * kSW, sWm + b * kSW, sb + b * 28);
   }
   __syncthreads();
-  for (uint32_t sl = blockIdx.x * blockDim.x + threadIdx.x; sl < kPatSlots; sl += gridDim.x * blockDim.x) {
-    const unsigned long long key = __ldg(keys + sl);
-    if (key == kPatEmpty) continue;
-    const uint32_t idx = atomicAdd(pcount, 1u);
-    if (idx >= kPatMax) {
-      pidx[sl] = kNoPattern;
-      continue;
+  const float *wm = reinterpret_cast<const float *>(sWm);
+  const int lane = threadIdx.x & 31;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t base = warp * 32; base < kPatSlots; base += nwarps * 32) {
+    const unsigned long long kl = __ldg(keys + base + lane);
+    uint32_t occ = __ballot_sync(0xffffffffu, kl != kPatEmpty);
+    while (occ) {
+      const int src = __ffs(occ) - 1;
+      occ &= occ - 1;
+      const unsigned long long key = __shfl_sync(0xffffffffu, kl, src);
+      uint32_t idx = 0;
+      if (lane == 0) idx = atomicAdd(pcount, 1u);
+      idx = __shfl_sync(0xffffffffu, idx, 0);
+      if (idx >= kPatMax) {
+        if (lane == 0) {
+          pidx[base + src] = kNoPattern;
+          atomicOr(pfail, 1u);
+        }
+        continue;
+      }
+      if (lane < 28) {
+#pragma unroll
+        for (int b = 0; b < NB; ++b) {
+          float acc = sb[b * 28 + lane];
+#pragma unroll
+          for (int pos = 0; pos < 27; ++pos) {
+            const int mt = (int)((key >> (2 * pos)) & 3u);
+            acc = __fadd_rn(acc, wm[b * kSW * 4 + (mt * 27 + pos) * 28 + lane]);
+          }
+          pcoef[(size_t)idx * NB * 28 + b * 28 + lane] = acc;
+        }
+      }
+      if (lane == 0) pidx[base + src] = idx;
     }
-    float acc[NB][28];
-    coeffs_of_materials_n<NB>(sWm, sb, key, acc);
-    float4 *c = reinterpret_cast<float4 *>(pcoef + (size_t)idx * NB * 28);
-#pragma unroll
-    for (int b = 0; b < NB; ++b)
-#pragma unroll
-      for (int v = 0; v < 7; ++v)
-        c[b * 7 + v] = make_float4(acc[b][4 * v], acc[b][4 * v + 1], acc[b][4 * v + 2], acc[b][4 * v + 3]);
-    pidx[sl] = idx;
   }
 }
 
@@ -769,6 +796,7 @@ k_kgen_list(const float *__restrict__ img, int n1, int n2, int n3, const float *
             const uint32_t *__restrict__ rbase, const uint32_t *__restrict__ rcount, KT *__restrict__ rec0,
             KT *__restrict__ rec1, const PatternArgs pat) {
   dependent_launch_enter();
+  if (pat.cell_slot && __ldg(pat.fail) == 0) return;  // k_fill_runs_pattern wrote every general cell
   __shared__ float4 sW[NB * kSW];
   __shared__ float4 sWm[NB * kSW];
   __shared__ float sb[NB * 28];
@@ -2032,7 +2060,7 @@ static size_t plan_layout(PrecondPlan &P, char *base) {
   if (P.lv[0].cls && nlist) {
     P.pkeys = (unsigned long long *)take((size_t)kPatSlots * sizeof(unsigned long long));
     P.pidx = (uint32_t *)take((size_t)kPatSlots * sizeof(uint32_t));
-    P.pcount = (uint32_t *)take(sizeof(uint32_t));
+    P.pcount = (uint32_t *)take(2 * sizeof(uint32_t));  // [0] entries used, [1] failure flag
     P.pcoef = (float *)take((size_t)kPatMax * 2 * 28 * sizeof(float));
     P.cell_slot = (uint32_t *)take((size_t)P.lv[0].n * sizeof(uint32_t));
   }
@@ -2855,8 +2883,16 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
       if (b1 >= 0) RET_IF(launch_stencil_gen(im, 0, v.n1, v.n2, v.n3, blk_w(b1), blk_b(b1), K1, P.kdt, v.ps, gs));
       return MLPCG_OK;
     }
+    // level 0 (one-hot image): classify also enters each general cell's neighbourhood pattern into
+    // the pattern table, whose distinct patterns' coefficients are then evaluated once
+    const bool use_pat = l == 0 && P.pkeys && gl == P.glist;
+    if (use_pat) {
+      MLPCG_CUDA_CHECK(cudaMemsetAsync(P.pkeys, 0xff, (size_t)kPatSlots * sizeof(unsigned long long), gs));
+      MLPCG_CUDA_CHECK(cudaMemsetAsync(P.pcount, 0, 2 * sizeof(uint32_t), gs));  // entries used, failure flag
+    }
     k_classify<false><<<grid_of(v), PT, 0, gs>>>(im, nullptr, v.n1, v.n2, v.n3, P.cls[l], P.rw[l], P.rcount[l],
-                                                 P.gcount[l]);
+                                                 P.gcount[l], use_pat ? P.pkeys : nullptr,
+                                                 use_pat ? P.cell_slot : nullptr, use_pat ? P.pcount + 1 : nullptr);
     MLPCG_LAUNCH_CHECK();
     k_scan_tiles<<<1, 1024, 0, gs>>>(P.rcount[l], P.rbase[l], (int)v.ntiles);
     MLPCG_LAUNCH_CHECK();
@@ -2873,17 +2909,15 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
     const int fgrid = (int)std::min<int64_t>((int64_t)sm_count() * 8, (27 * (v.n / 8) + 255) / 256);
     const uint32_t *rlb = P.rbase[l] + v.ntiles - 1, *rlc = P.rcount[l] + v.ntiles - 1;
     // the mixed runs' uniform cells first (whole taps per vector store), then the general cells
-    // level 0 (one-hot image): the distinct neighbourhood patterns' coefficients first
-    PatternArgs pat{nullptr, nullptr, nullptr};
-    if (l == 0 && P.pkeys && gl == P.glist) {
-      MLPCG_CUDA_CHECK(cudaMemsetAsync(P.pkeys, 0xff, (size_t)kPatSlots * sizeof(unsigned long long), gs));
-      MLPCG_CUDA_CHECK(cudaMemsetAsync(P.pcount, 0, sizeof(uint32_t), gs));
-      k_pattern_keys<<<sm_count() * 8, 256, 0, gs>>>(im, v.n1, v.n2, v.n3, gl, lb, lc, P.pkeys, P.cell_slot);
+    PatternArgs pat{nullptr, nullptr, nullptr, nullptr};
+    if (use_pat) {
+      const int pgrid = sm_count() * 4;
+      if (b1 >= 0)
+        k_pattern_coeffs<2><<<pgrid, 256, 0, gs>>>(params, b0, b1, P.pkeys, P.pidx, P.pcount, P.pcoef, P.pcount + 1);
+      else
+        k_pattern_coeffs<1><<<pgrid, 256, 0, gs>>>(params, b0, b0, P.pkeys, P.pidx, P.pcount, P.pcoef, P.pcount + 1);
       MLPCG_LAUNCH_CHECK();
-      if (b1 >= 0) k_pattern_coeffs<2><<<sm_count() * 2, 256, 0, gs>>>(params, b0, b1, P.pkeys, P.pidx, P.pcount, P.pcoef);
-      else k_pattern_coeffs<1><<<sm_count() * 2, 256, 0, gs>>>(params, b0, b0, P.pkeys, P.pidx, P.pcount, P.pcoef);
-      MLPCG_LAUNCH_CHECK();
-      pat = PatternArgs{P.cell_slot, P.pidx, P.pcoef};
+      pat = PatternArgs{P.cell_slot, P.pidx, P.pcoef, P.pcount + 1};
     }
     auto launch = [&](auto kern, auto fill, const void *r0, const void *r1) {
       using KT = typename std::remove_pointer<decltype(kgen_rec_type(kern))>::type;
@@ -2923,7 +2957,7 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
     const auto &v = P.lv[l];
     if (!v.cls) return MLPCG_OK;
     k_classify<true><<<grid_of(v), PT, 0, st>>>(nullptr, P.cls[l], v.n1, v.n2, v.n3, P.clsT[l], P.rwT[l],
-                                                P.rcountT[l], P.gcountT[l]);
+                                                P.rcountT[l], P.gcountT[l], nullptr, nullptr, nullptr);
     MLPCG_LAUNCH_CHECK();
     k_scan_tiles<<<1, 1024, 0, st>>>(P.rcountT[l], P.rbaseT[l], (int)v.ntiles);
     MLPCG_LAUNCH_CHECK();
