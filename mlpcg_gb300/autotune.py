@@ -8,7 +8,7 @@ in a JSON file so that a later process applies the choice without timing:
   per SM; keyed by device name, grid shape and method.
 * ``tune_plan``: the preconditioner's block schedule -- from how many tiles per
   SM down a level runs the block kernels that load each run's coefficients up
-  front (0, 1, 2 or 4), and whether the coarse levels run as one thread-block
+  front (0, 1, 2, 4 or 8), and whether the coarse levels run as one thread-block
   cluster launch; keyed by device name, grid shape, levels, coefficient dtype
   and method.  Every choice gives the same outputs.
 
@@ -119,7 +119,7 @@ def plan_key(device_name: str, shape, levels: int, dtype: str, method: str) -> s
 
 def plan_candidates(cluster_available: bool):
     """(small-level tiles per SM, coarse cluster) pairs to try."""
-    out = [(k, 0) for k in (0, 1, 2, 4)]
+    out = [(k, 0) for k in (0, 1, 2, 4, 8)]
     if cluster_available:
         out += [(k, 1) for k in (0, 2)]
     return out

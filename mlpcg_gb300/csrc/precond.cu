@@ -767,13 +767,23 @@ k_fill_runs_pattern(const uint8_t *__restrict__ cls, const uint32_t *__restrict_
     for (int b = 0; b < NB; ++b) {
       const float *ku = b ? kuni1 : kuni0;
       KT *rec = (b ? rec1 : rec0) + rp.offset;
-      for (int p = 0; p < 27; ++p) {
-        float v[8];
+      // taps in groups of four: one 16-byte load per cell (uniform vectors: 32 floats per material;
+      // table rows: 28 per block, both 16-byte aligned), then the four taps' stores
+      for (int p0 = 0; p0 < 27; p0 += 4) {
+        float4 g[8];
 #pragma unroll
-        for (int c = 0; c < 8; ++c)
-          v[c] = src[c] < 0 ? 0.f
-                            : (src[c] < 3 ? __ldg(ku + src[c] * KREC + p) : __ldg(pat.pcoef + (src[c] - 3) + b * 28 + p));
-        st8(rec + (size_t)p * rp.stride, v);
+        for (int c = 0; c < 8; ++c) {
+          const float *srcp = src[c] < 3 ? ku + src[c] * KREC + p0 : pat.pcoef + (src[c] - 3) + b * 28 + p0;
+          g[c] = src[c] < 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : __ldg(reinterpret_cast<const float4 *>(srcp));
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          if (p0 + u >= 27) break;
+          float v[8];
+#pragma unroll
+          for (int c = 0; c < 8; ++c) v[c] = u == 0 ? g[c].x : (u == 1 ? g[c].y : (u == 2 ? g[c].z : g[c].w));
+          st8(rec + (size_t)(p0 + u) * rp.stride, v);
+        }
       }
     }
   }

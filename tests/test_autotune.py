@@ -60,7 +60,7 @@ def test_tune_solver_applies_and_caches(cuda, tmp_path):
 
 
 def test_plan_candidates_and_key():
-    assert autotune.plan_candidates(False) == [(0, 0), (1, 0), (2, 0), (4, 0)]
+    assert autotune.plan_candidates(False) == [(0, 0), (1, 0), (2, 0), (4, 0), (8, 0)]
     assert autotune.plan_candidates(True)[-2:] == [(0, 1), (2, 1)]
     assert autotune.plan_key("NVIDIA GB300", (256, 256, 256), 5, "bfloat16", "npsd") == \
         "plan|NVIDIA GB300|256x256x256|L5|bfloat16|npsd"
