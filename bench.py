@@ -244,7 +244,8 @@ def setup_launches(plan):
             continue
         nb = 2 if l < n else 1
         cnt += 6 if cls[l] else nb                 # classify, 2 tile scans, list, records, fill | dense planes
-    return cnt + 2 * n + (1 if plan.kind == 1 else 0)   # c0/c1: class sums + finalize per level (+ squares)
+    cnt += 1 if cls[0] else 0                      # level 0: the pattern table's coefficients
+    return cnt + 3 * n + (1 if plan.kind == 1 else 0)   # c0/c1: class sums, reduce, finalize per level (+ squares)
 
 
 # ----------------------------------------------------------------------------
@@ -423,7 +424,7 @@ def run_ours(args, rank, world):
            "setup_ms": setup_ms, "solve_ms": solve_ms,
            "roofline": roofline, "clocks": clocks, "e2e": e2e, "meta": meta, "history": last.history.tolist(),
            "per_iter_bytes": per_iter_bytes, "launches": setup_launches(plan) + 2 +
-           it_mean * (precond_launches(plan) + (6 if args.method == "npsd" else 5)), "x": x_fused, "scene": scene,
+           it_mean * (precond_launches(plan) + (5 if args.method == "npsd" else 4)), "x": x_fused, "scene": scene,
            "model": model,
            "flags": flags, "b": b, "wall": t_wall, "tuned": tuned}
     return out

@@ -552,55 +552,41 @@ __global__ void __launch_bounds__(RT) k_sd_dots(Vecs V) {
 }
 
 // The same two products from the preconditioner's level-0 epilogue (ZDots): the per-tile FP64
-// partials summed by one block in a fixed order (each thread a strided share, then a fixed tree),
-// then c1, c0 as above.
-constexpr int ZT_THREADS = 1024;
-__global__ void __launch_bounds__(ZT_THREADS) k_sd_dots_tiles(Vecs V) {
+// partials summed by ZT_BLOCKS blocks (each thread a fixed strided share, then the blocks' fixed
+// reduction and the last block's sum in block order), then c1, c0 as above.
+constexpr int ZT_BLOCKS = 64;
+__global__ void __launch_bounds__(RT) k_sd_dots_tiles(Vecs V) {
   dependent_launch_enter();
   const State &S = *V.st;
   if (S.status != ST_RUNNING) return;
   const int it = S.it;
   if (it == 0) {
-    if (threadIdx.x == 0) { V.st->c0 = 0.0; V.st->c1 = 0.0; }
+    if (blockIdx.x == 0 && threadIdx.x == 0) { V.st->c0 = 0.0; V.st->c1 = 0.0; }
     return;
   }
-  __shared__ double red[2][ZT_THREADS / 32];
-  double a1 = 0.0, a0 = 0.0;
-  // tiles t, t + 1024, ... in ascending order, eight loads in flight at a time
   const double2 *zp = reinterpret_cast<const double2 *>(V.zpart);
-  for (int64_t t0 = threadIdx.x; t0 < V.ztiles; t0 += 8 * ZT_THREADS) {
-    double2 v[8];
+  const int64_t stride = (int64_t)gridDim.x * RT;
+  double a1 = 0.0, a0 = 0.0;
+  for (int64_t t0 = (int64_t)blockIdx.x * RT + threadIdx.x; t0 < V.ztiles; t0 += 4 * stride) {
+    double2 v[4];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) {
-      const int64_t t = t0 + (int64_t)u * ZT_THREADS;
+    for (int u = 0; u < 4; ++u) {
+      const int64_t t = t0 + u * stride;
       v[u] = t < V.ztiles ? zp[t] : make_double2(0.0, 0.0);
     }
 #pragma unroll
-    for (int u = 0; u < 8; ++u) {
+    for (int u = 0; u < 4; ++u) {
       a1 += v[u].x;
       a0 += v[u].y;
     }
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    a1 += __shfl_xor_sync(0xffffffffu, a1, o);
-    a0 += __shfl_xor_sync(0xffffffffu, a0, o);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    red[0][threadIdx.x >> 5] = a1;
-    red[1][threadIdx.x >> 5] = a0;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double o1 = 0.0, o0 = 0.0;
-    for (int w = 0; w < ZT_THREADS / 32; ++w) {
-      o1 += red[0][w];
-      o0 += red[1][w];
-    }
+  double v[2] = {a1, a0};
+  double o[2];
+  if (reduce_last<2>(v, V, 1, o) && threadIdx.x == 0) {
     State &W = *V.st;
     const int h = W.head, hp = (h + 2) % 3;
-    const double c1 = o1 / W.alpha[h];
-    const double c0 = it >= 2 ? (o0 - c1 * W.e_last) / W.alpha[hp] : 0.0;
+    const double c1 = o[0] / W.alpha[h];
+    const double c0 = it >= 2 ? (o[1] - c1 * W.e_last) / W.alpha[hp] : 0.0;
     W.c1 = c1;
     W.c0 = c0;
   }
@@ -977,21 +963,8 @@ __global__ void __launch_bounds__(RT) k_update(Vecs V) {
   }
 }
 
-// r = b - A x (double-float) when due
-__global__ void __launch_bounds__(RT) k_true_residual(Vecs V) {
-  dependent_launch_enter();
-  const State &S = *V.st;
-  if (S.status != ST_RUNNING || !S.need_true) return;
-  CSum bb, rr;
-  residual_pass<false>(V, bb, rr);
-  double v[2] = {0.0, rr.get()};
-  double o[2];
-  if (reduce_last<2>(v, V, 0, o) && threadIdx.x == 0) V.st->rr_true = o[1];
-}
-
 // one thread: iteration bookkeeping, convergence, loop condition
-__global__ void k_control(Vecs V, cudaGraphConditionalHandle handle, int use_handle) {
-  dependent_launch_enter();
+__device__ __forceinline__ void control_step(const Vecs &V, cudaGraphConditionalHandle handle, int use_handle) {
   State &S = *V.st;
   if (S.status == ST_RUNNING) {
     const int itn = S.it + 1;
@@ -1016,7 +989,28 @@ __global__ void k_control(Vecs V, cudaGraphConditionalHandle handle, int use_han
   if (use_handle) cudaGraphSetConditional(handle, S.status == ST_RUNNING ? 1u : 0u);
 }
 
-// Batched solves: one loop for many systems.  Each system's control kernel
+// The end of an iteration: r = b - A x (double-float) when due, then the control step -- by the
+// last block of that reduction, or by block 0 when no true residual is due (the other blocks then
+// return at once, whatever order they read the state in).
+__global__ void __launch_bounds__(RT) k_true_residual_control(Vecs V, cudaGraphConditionalHandle handle,
+                                                              int use_handle) {
+  dependent_launch_enter();
+  const State &S = *V.st;
+  if (S.status != ST_RUNNING || !S.need_true) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) control_step(V, handle, use_handle);
+    return;
+  }
+  CSum bb, rr;
+  residual_pass<false>(V, bb, rr);
+  double v[2] = {0.0, rr.get()};
+  double o[2];
+  if (reduce_last<2>(v, V, 0, o) && threadIdx.x == 0) {
+    V.st->rr_true = o[1];
+    control_step(V, handle, use_handle);
+  }
+}
+
+// Batched solves: one loop for many systems.  Each system's control step
 // updates its own state; this one keeps the loop running while any runs.
 constexpr int kMaxBatch = 64;
 struct BatchStates {
@@ -1183,7 +1177,7 @@ static int enqueue_body(mlpcg_solver *s, cudaStream_t st, cudaGraphConditionalHa
   int rc = precond_apply_gated(s->plan, V.r, &S->rscale, V.z, &S->status, st, zdots ? &zd : nullptr);
   if (rc) return rc;
   if (s->method == M_NPSD) {
-    if (zdots) k_sd_dots_tiles<<<1, ZT_THREADS, 0, st>>>(V);
+    if (zdots) k_sd_dots_tiles<<<ZT_BLOCKS, RT, 0, st>>>(V);
     else k_sd_dots<<<nb, RT, 0, st>>>(V);
     k_sd_qform<<<nb, RT, 0, st>>>(V);
     if (s->qmap_ok) k_sd_spmv_tma<<<nb, RT, 0, st>>>(V, s->qmap[0], s->qmap[1], s->qmap[2]);
@@ -1193,8 +1187,7 @@ static int enqueue_body(mlpcg_solver *s, cudaStream_t st, cudaGraphConditionalHa
     k_cg_pspmv<<<nb, RT, 0, st>>>(V);
   }
   k_update<<<nb, RT, 0, st>>>(V);
-  k_true_residual<<<full_grid(V), RT, 0, st>>>(V);
-  k_control<<<1, 1, 0, st>>>(V, h, use_handle);
+  k_true_residual_control<<<full_grid(V), RT, 0, st>>>(V, h, use_handle);
   MLPCG_LAUNCH_CHECK();
   return MLPCG_OK;
 }
@@ -1321,7 +1314,7 @@ static int solve_impl(mlpcg_solver *s, int use_graph, int zero_guess, cudaStream
     }
   }
   // the loop only starts when the initial residual is not already converged:
-  // the body's first kernels see status != RUNNING and the control kernel
+  // the body's first kernels see status != RUNNING and the control step
   // ends the loop after one pass.
   MLPCG_CUDA_CHECK(cudaGraphLaunch(s->exec, st));
   k_finalize<<<full_grid(V), RT, 0, st>>>(V);

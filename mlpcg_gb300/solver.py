@@ -3,7 +3,7 @@
 One CUDA graph per solver: a conditional WHILE node wraps one iteration
 (the fused preconditioner kernels, the orthogonalisation / SpMV / update
 kernels with FP64 cross-thread reductions, a double-float true residual every
-``true_every`` iterations, a one-thread control kernel).  ``solve`` is a
+``true_every`` iterations, the iteration's control step).  ``solve`` is a
 single graph launch; the host synchronises only to read the result.
 ``solve_host`` is the host-to-host form for a new frame, with the rhs
 transfer overlapped with the preconditioner set-up.
