@@ -794,9 +794,9 @@ k_fill_runs_pattern(const uint8_t *__restrict__ cls, const uint32_t *__restrict_
 // into the records of their runs.  Thread e of the grid-stride loop evaluates
 // list[e]; the count of general cells is read on the device.
 //
-// With the pattern table (PatternArgs), k_fill_runs has already written the
-// general cells whose pattern has table values; this kernel evaluates the
-// others' patches.
+// With the pattern table (PatternArgs), k_fill_runs_pattern has already
+// written the general cells whose pattern has table values; this kernel
+// evaluates the others' patches (and returns at once when there are none).
 
 template <typename KT, int NB>
 __global__ void __launch_bounds__(PT)
