@@ -1331,6 +1331,7 @@ __global__ void __launch_bounds__(PT, 1)
 k_pre_fused_small(const CoefArgs<KT> C, const XT *__restrict__ x, YT *__restrict__ y, YT *__restrict__ ypool,
                   int n1, int n2, int n3, const int *__restrict__ gate) {
   dependent_launch_enter();
+  dependent_launch_trigger();
   if (gate && *gate != 0) return;
   pre_fused_body<KT, XT, YT, POOL, CLS, false, false, true>(C, x, nullptr, y, ypool, nullptr, n1, n2, n3, nullptr,
                                                             nullptr, grid_tile());
@@ -1714,6 +1715,7 @@ k_post_fused_small(const CoefArgs<KT> C, const AT *__restrict__ xc, const AT *__
                    const float *__restrict__ c0p, const float *__restrict__ c1p, AT *__restrict__ out, int n1,
                    int n2, int n3, const int *__restrict__ gate) {
   dependent_launch_enter();
+  dependent_launch_trigger();
   if (gate && *gate != 0) return;
   post_fused_body<KT, AT, AT, AT, SWAP, CLS, false, false, false, true>(C, xc, yl, c0p, c1p, out, nullptr, nullptr,
                                                                         n1, n2, n3, nullptr, nullptr, grid_tile());

@@ -557,6 +557,7 @@ __global__ void __launch_bounds__(RT) k_sd_dots(Vecs V) {
 constexpr int ZT_BLOCKS = 64;
 __global__ void __launch_bounds__(RT) k_sd_dots_tiles(Vecs V) {
   dependent_launch_enter();
+  dependent_launch_trigger();
   const State &S = *V.st;
   if (S.status != ST_RUNNING) return;
   const int it = S.it;
@@ -595,6 +596,7 @@ __global__ void __launch_bounds__(RT) k_sd_dots_tiles(Vecs V) {
 // q = z - c1 p_recent - c0 p_previous into the next ring slot
 __global__ void __launch_bounds__(RT) k_sd_qform(Vecs V) {
   dependent_launch_enter();
+  dependent_launch_trigger();
   const State &S = *V.st;
   if (S.status != ST_RUNNING) return;
   const int h = S.head, hp = (h + 2) % 3, hn = (h + 1) % 3;
@@ -684,6 +686,7 @@ __global__ void __launch_bounds__(RT, 3) k_sd_spmv_tma(Vecs V, const __grid_cons
                                                    const __grid_constant__ CUtensorMap tq1,
                                                    const __grid_constant__ CUtensorMap tq2) {
   dependent_launch_enter();
+  dependent_launch_trigger();
   const State &S = *V.st;
   if (S.status != ST_RUNNING) return;
   __shared__ __align__(128) float T[SBX][SBY][SBZ];
@@ -893,6 +896,7 @@ __global__ void __launch_bounds__(RT) k_cg_pspmv(Vecs V) {
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(RT) k_update(Vecs V) {
   dependent_launch_enter();
+  dependent_launch_trigger();
   const State &S = *V.st;
   if (S.status != ST_RUNNING) return;
   const float *D, *AD;
