@@ -432,8 +432,9 @@ int mlpcg_solver_get_schedule(const mlpcg_solver *solver, int *blocks_in_use);
  * predecessor's last blocks run and wait on the device for its completion
  * (measured 0.5 % faster at 256^3, 1 % at 128^3).  Results
  * are identical either way.  Takes effect on the next solve (the graph is
- * rebuilt); batches built from the solver follow its first solver's setting.
- * If the runtime refuses such a graph, the solve captures ordinary edges.
+ * rebuilt).  Batches capture ordinary edges (measured faster with the systems'
+ * chains running side by side).  If the runtime refuses such a graph, the
+ * solve captures ordinary edges.
  * mlpcg_solver_dependent_edges reports the edges converted in the current
  * graph (0 before the first graph solve or with the feature off). */
 int mlpcg_solver_set_dependent_launch(mlpcg_solver *solver, int on);
