@@ -440,12 +440,13 @@ int mlpcg_solver_get_schedule(const mlpcg_solver *solver, int *blocks_in_use);
 int mlpcg_solver_set_dependent_launch(mlpcg_solver *solver, int on);
 int mlpcg_solver_dependent_edges(const mlpcg_solver *solver, int *edges);
 
-/* npsd products in the preconditioner (no counterpart in the reference; on by
- * default): z.Ap_recent and z.Ap_previous (cg_tests.py:226-233) are summed by
- * the plan's level-0 post-block while z is in registers, one FP64 partial per
- * tile, and reduced by one block in a fixed order -- z is not read again.
- * Applies to npsd solvers whose plan is the SmallSMModelDn3D kind with a
- * TMA-staged finest level; the others sum them in a separate pass.  The two
+/* Solver products in the preconditioner (no counterpart in the reference; on
+ * by default): npsd's z.Ap_recent and z.Ap_previous (cg_tests.py:226-233) or
+ * npcg's r.z (cg_tests.py:54,77) are summed by the plan's level-0 post-block
+ * while z is in registers, one FP64 partial per tile, and reduced in a fixed
+ * order -- z is not read again.  Applies to plans of the SmallSMModelDn3D and
+ * SmallSPDSMModelDn3D kinds with a TMA-staged finest level; the others sum
+ * them in a separate pass.  The two
  * forms add the same products in different orders (FP64 partials either
  * way).  Takes effect on the next solve; mlpcg_solver_fused_dots reports
  * whether a bound solver uses the epilogue. */

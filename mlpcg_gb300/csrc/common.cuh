@@ -48,17 +48,20 @@ inline size_t dtype_size(int dt) { return dt == MLPCG_F64 ? 8 : (dt == MLPCG_BF1
 __host__ __device__ inline int64_t cells(int n1, int n2, int n3) { return (int64_t)n1 * n2 * n3; }
 inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 
-// Optional epilogue of the finest post-block for the npsd solver: the products of
+// Optional epilogue of the finest post-block for the solvers: the products of
 // the new preconditioned residual z with the A-images of the two most recent
-// search directions, z . ring[head] and z . ring[(head + 2) % 3] (ring: three
-// slots of n floats; none at iteration 0, the first alone at iteration 1),
-// summed per tile of the finest level in FP64 into partial[2 * tile + k].
-// head and it are words of the solver's device state, read by the kernel.
+// search directions, z . ring[head] and z . ring[(head + 2) % 3] (npsd; ring:
+// three slots of n floats; none at iteration 0, the first alone at iteration
+// 1), or with one fixed vector, z . ring (single != 0: npcg's r . z, every
+// iteration), summed per tile of the finest level in FP64 into
+// partial[2 * tile + k].  head and it are words of the solver's device state,
+// read by the kernel.
 struct ZDots {
   const float *ring;
   const int *head, *it;
   double *partial;
   int64_t n;
+  int single;
 };
 
 // First statement of every kernel of this library.  A kernel reached through a

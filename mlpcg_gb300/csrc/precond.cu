@@ -1587,8 +1587,8 @@ __device__ __forceinline__ void post_fused_body(const CoefArgs<KT> &C, const CT 
   int nd = 0;
   const float *a1 = nullptr, *a0 = nullptr;
   if constexpr (ZD) {
-    const int it = __ldg(zd->it), h = __ldg(zd->head);
-    nd = it < 2 ? it : 2;
+    const int it = __ldg(zd->it), h = zd->single ? 0 : __ldg(zd->head);
+    nd = zd->single ? 1 : (it < 2 ? it : 2);
     a1 = zd->ring + (size_t)h * zd->n;
     a0 = zd->ring + (size_t)((h + 2) % 3) * zd->n;
     const int pk = z0 + run_tz(threadIdx.x) * 8, pj = y0 + run_ty(threadIdx.x);
@@ -2614,7 +2614,7 @@ static int run_apply(const PrecondPlan &P, const float *r, const float *rscale, 
           k_up_fine<AT, AT, float, true, true><<<g, PT, 0, st>>>((const AT *)P.xout[1], (const AT *)P.y[0], c0, c1,
                                                                   (float *)P.ufine, v.n1, v.n2, v.n3, gate);
           MLPCG_LAUNCH_CHECK();
-          RET_IF((launch_post0<KT, AT, float, true>(P, C, (const AT *)P.y[0], c0, c1, z, nullptr, om, st, gate)));
+          RET_IF((launch_post0<KT, AT, float, true>(P, C, (const AT *)P.y[0], c0, c1, z, nullptr, om, st, gate, zd)));
         } else {
           AT *u = (AT *)P.ufine;
           k_up_fine<AT, AT, AT, true, true><<<g, PT, 0, st>>>((const AT *)P.xout[l + 1], (const AT *)P.y[l], c0, c1, u,
@@ -2710,11 +2710,12 @@ const int *precond_copy_flag(const mlpcg_precond *h) { return h->p.ready ? h->p.
 
 int64_t precond_level0_tiles(const mlpcg_precond *h);
 
-// Tiles of the finest level when the plan can compute the npsd products (ZDots) in its level-0
-// post-block -- the plain SM kind whose finest post-block is the TMA kernel -- else 0.
+// Tiles of the finest level when the plan can compute the solver's products (ZDots) in its level-0
+// post-block -- the SmallSMModelDn3D and SmallSPDSMModelDn3D kinds, whose finest post-block is
+// the TMA kernel -- else 0.
 int64_t precond_zdots_tiles(const mlpcg_precond *h) {
   const PrecondPlan &P = h->p;
-  if (!P.ready || P.kind != MLPCG_PRECOND_SM || !P.lv[0].fast) return 0;
+  if (!P.ready || (P.kind != MLPCG_PRECOND_SM && P.kind != MLPCG_PRECOND_SMALL_SPD) || !P.lv[0].fast) return 0;
   CUtensorMap tm;
   if (!encode_input_map(&tm, (const float *)P.ufine, P.lv[0])) return 0;
   return precond_level0_tiles(h);

@@ -881,6 +881,36 @@ __global__ void __launch_bounds__(RT) k_cg_rz(Vecs V) {
   }
 }
 
+// r . z from the preconditioner's level-0 epilogue (ZDots, single product): the per-tile FP64
+// partials summed like k_sd_dots_tiles, then the same state update as k_cg_rz
+__global__ void __launch_bounds__(RT) k_cg_rz_tiles(Vecs V) {
+  dependent_launch_enter();
+  dependent_launch_trigger();
+  const State &S = *V.st;
+  if (S.status != ST_RUNNING) return;
+  const double2 *zp = reinterpret_cast<const double2 *>(V.zpart);
+  const int64_t stride = (int64_t)gridDim.x * RT;
+  double a = 0.0;
+  for (int64_t t0 = (int64_t)blockIdx.x * RT + threadIdx.x; t0 < V.ztiles; t0 += 4 * stride) {
+    double2 v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int64_t t = t0 + u * stride;
+      v[u] = t < V.ztiles ? zp[t] : make_double2(0.0, 0.0);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) a += v[u].x;
+  }
+  double v[1] = {a};
+  double o[1];
+  if (reduce_last<1>(v, V, 1, o) && threadIdx.x == 0) {
+    State &W = *V.st;
+    W.rz = o[0];
+    W.c1 = (W.it == 0) ? 0.0 : o[0] / W.rz_old;  // beta of the p update
+    W.rz_old = o[0];
+  }
+}
+
 // p_new = z + beta p_old (ping-pong buffers), w = A p_new, pw = p_new . w, alpha = rz / pw
 __global__ void __launch_bounds__(RT) k_cg_pspmv(Vecs V) {
   dependent_launch_enter();
@@ -1187,10 +1217,10 @@ static int start_solve(mlpcg_solver *s, cudaStream_t st) {
   return MLPCG_OK;
 }
 
-// NPSD with a plan whose level-0 post-block computes the products z . Ap (precond_zdots_tiles)
+// a plan whose level-0 post-block computes the solver's products (npsd z . Ap, npcg r . z;
+// precond_zdots_tiles)
 static bool uses_fused_dots(const mlpcg_solver *s) {
-  return s->fused_dots && s->method == M_NPSD && s->V.zpart && s->zcap > 0 &&
-         precond_zdots_tiles(s->plan) == s->zcap;
+  return s->fused_dots && s->V.zpart && s->zcap > 0 && precond_zdots_tiles(s->plan) == s->zcap;
 }
 
 static int enqueue_body(mlpcg_solver *s, cudaStream_t st, cudaGraphConditionalHandle h, int use_handle) {
@@ -1200,7 +1230,8 @@ static int enqueue_body(mlpcg_solver *s, cudaStream_t st, cudaGraphConditionalHa
   // z = M (r / ||r||): the scale is read from the device state; the kernels
   // return at once once this system has stopped (its status word is nonzero)
   const bool zdots = uses_fused_dots(s);
-  const ZDots zd{V.Ap, &S->head, &S->it, V.zpart, V.n};
+  const ZDots zd = s->method == M_NPSD ? ZDots{V.Ap, &S->head, &S->it, V.zpart, V.n, 0}
+                                        : ZDots{V.r, &S->head, &S->it, V.zpart, V.n, 1};
   int rc = precond_apply_gated(s->plan, V.r, &S->rscale, V.z, &S->status, st, zdots ? &zd : nullptr);
   if (rc) return rc;
   if (s->method == M_NPSD) {
@@ -1210,7 +1241,8 @@ static int enqueue_body(mlpcg_solver *s, cudaStream_t st, cudaGraphConditionalHa
     if (s->qmap_ok) k_sd_spmv_tma<<<nb, RT, 0, st>>>(V, s->qmap[0], s->qmap[1], s->qmap[2]);
     else k_sd_spmv<<<nb, RT, 0, st>>>(V);
   } else {
-    k_cg_rz<<<nb, RT, 0, st>>>(V);
+    if (zdots) k_cg_rz_tiles<<<ZT_BLOCKS, RT, 0, st>>>(V);
+    else k_cg_rz<<<nb, RT, 0, st>>>(V);
     k_cg_pspmv<<<nb, RT, 0, st>>>(V);
   }
   k_update<<<nb, RT, 0, st>>>(V);
@@ -1239,7 +1271,7 @@ int mlpcg_solver_create(int N1, int N2, int N3, const mlpcg_precond *plan, int m
   s->n1 = N1; s->n2 = N2; s->n3 = N3;
   s->method = method; s->max_it = max_it; s->tol = tol; s->true_every = true_every;
   s->plan = plan;
-  s->zcap = method == M_NPSD ? precond_level0_tiles(plan) : 0;
+  s->zcap = precond_level0_tiles(plan);
   s->bytes = solver_layout(*s, nullptr);
   *out = s;
   return MLPCG_OK;

@@ -176,12 +176,13 @@ class FusedSolver:
         call("mlpcg_solver_set_dependent_launch", self._h, int(bool(on)))
 
     def set_fused_dots(self, on: bool):
-        """npsd: the products z . Ap summed in the preconditioner's level-0 post-block (on by default,
-        where the plan allows it; mlpcg_solver_set_fused_dots) or in a separate pass."""
+        """The solver's products (npsd z . Ap, npcg r . z) summed in the preconditioner's level-0
+        post-block (on by default, where the plan allows it; mlpcg_solver_set_fused_dots) or in a
+        separate pass."""
         call("mlpcg_solver_set_fused_dots", self._h, int(bool(on)))
 
     def fused_dots(self) -> bool:
-        """Whether the solve sums the npsd products in the preconditioner's epilogue."""
+        """Whether the solve sums its products in the preconditioner's epilogue."""
         v = C.c_int()
         call("mlpcg_solver_fused_dots", self._h, C.byref(v))
         return bool(v.value)

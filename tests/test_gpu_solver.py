@@ -371,18 +371,19 @@ def test_dependent_launch_gives_identical_solves(cuda, method):
         assert it == it0 and st == st0 and torch.equal(x, x0) and np.array_equal(h, h0), key
 
 
-def test_npsd_products_in_the_preconditioner_epilogue(cuda):
-    """npsd with z . Ap summed by the level-0 post-block (the default for this plan) against the
-    separate pass: the same products added in another order.  The rounding differences grow
-    slowly over 40 iterations of this slowly converging system (measured 4.4e-5 relative at most),
-    so the histories agree to 2e-4 and the solutions to 1e-3, with the same iteration count and
-    status; the epilogue is off for npcg and when switched off, and graph and loop solves with it
-    agree bit for bit."""
+@pytest.mark.parametrize("method", ["npsd", "npcg"])
+def test_solver_products_in_the_preconditioner_epilogue(cuda, method):
+    """The solver's products summed by the level-0 post-block (npsd z . Ap, npcg r . z; the
+    default for this plan) against the separate pass: the same products added in another order.
+    The rounding differences grow slowly over 40 iterations of this slowly converging system
+    (measured 4.4e-5 relative at most), so the histories agree to 2e-4 and the solutions to 1e-3,
+    with the same iteration count and status; the epilogue is off when switched off, and graph
+    and loop solves with it agree bit for bit."""
     from mlpcg_gb300.solver import FusedSolver
     s, flags, img = _scene((64, 64, 64), 7, cuda)
     m = _near_identity_model(4, cuda)
     b = torch.as_tensor(s.rhs, device=cuda)
-    solver = FusedSolver(m, flags, method="npsd", max_it=40, tol=1e-7, storage=torch.bfloat16)
+    solver = FusedSolver(m, flags, method=method, max_it=40, tol=1e-7, storage=torch.bfloat16)
     assert solver.fused_dots()
     r_fused = solver.solve(b)
     x_fused, h_fused = r_fused.x.clone(), np.array(r_fused.history)
@@ -395,8 +396,6 @@ def test_npsd_products_in_the_preconditioner_epilogue(cuda):
     h_sep = np.array(r_sep.history)[: r_sep.iterations + 1]
     np.testing.assert_allclose(h_fused[: r_fused.iterations + 1], h_sep, rtol=2e-4)
     assert float((r_sep.x - x_fused).norm() / r_sep.x.norm()) < 1e-3
-    npcg = FusedSolver(m, flags, method="npcg", max_it=5, tol=1e-7, plan=solver.plan)
-    assert not npcg.fused_dots()
 
 
 def test_fused_status_words(cuda):
