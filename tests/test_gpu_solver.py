@@ -113,6 +113,26 @@ def test_plan_classed_is_bit_identical_to_dense(cuda, shape, n, seed, storage, s
     torch.cuda.synchronize()
 
 
+@pytest.mark.parametrize("storage", [torch.float32, torch.bfloat16])
+def test_plan_classed_equals_dense_with_non_one_hot_finest_image(cuda, storage):
+    """A finest image with fractional values in places: the general cells around them are not
+    one-hot patterns, so they take no pattern-table row and are evaluated one by one
+    (k_kgen_list's path behind the table's failure flag) -- the output still equals the dense
+    planes' bit for bit."""
+    from mlpcg_gb300.precond import PrecondPlan
+    s, flags, img = _scene((64, 64, 64), 4, cuda)
+    img = img.clone()
+    g = torch.Generator(device=cuda).manual_seed(3)
+    pick = torch.rand(img.shape[1:], device=cuda, generator=g) < 0.002
+    img[:, pick] = 0.5
+    m = _model(4, cuda, seed=3)
+    dense = PrecondPlan(m, img, storage=storage, layout="dense")
+    cls = PrecondPlan(m, img, storage=storage, layout="classed")
+    b = torch.randn(64 ** 3, device=cuda, generator=g)
+    assert cls.general_cells(0) > 0
+    assert torch.equal(dense.apply(b), cls.apply(b))
+
+
 def test_plan_classed_uniform_grid(cuda):
     """An all-fluid interior (only the wall layer differs) is almost entirely uniform."""
     from mlpcg_gb300.precond import PrecondPlan
