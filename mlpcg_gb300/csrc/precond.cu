@@ -1903,16 +1903,22 @@ struct PrecondPlan {
   void *ufine = nullptr;      // level-0 prolongated post-block input
   uint32_t *glist = nullptr;  // general-cell list (setup scratch)
   uint32_t *rlist = nullptr;  // mixed-run list (setup scratch)
-  uint32_t *glist2 = nullptr, *rlist2 = nullptr;  // the same for levels >= 1 (SM kind, side stream)
+  // SmallSMModelDn3D kind: each classed level >= 1 builds its coefficients on a stream of its own,
+  // with its own general-cell and mixed-run lists; each level's c0 / c1 pass its own workspace
+  std::vector<uint32_t *> glists, rlists;
+  std::vector<void *> lin_wss;
   // level-0 pattern table (classed level 0): hash keys, table index per slot, entries used,
   // coefficients per entry (2 blocks), pattern slot per general cell
   unsigned long long *pkeys = nullptr;
   uint32_t *pidx = nullptr, *pcount = nullptr, *cell_slot = nullptr;  // cell_slot: per level-0 cell
   float *pcoef = nullptr;
-  // setup: level 0's coefficient chain runs on the caller's stream, levels >= 1 and the linear
-  // blocks on this stream beside it (forked and joined with the two events)
-  cudaStream_t side = nullptr;
-  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+  // setup streams (SmallSMModelDn3D kind): level 0's coefficient chain runs on the caller's
+  // stream; sides[0] builds the image pyramid (recording img_ev[l] as level l's image is ready)
+  // and the coarse levels' c0 / c1; sides[l] (1 <= l <= L) level l's coefficients, then (l < L)
+  // its c0 / c1; sides[L + 1] level 0's c0 / c1.  Forked with fork_ev, joined with join_evs.
+  std::vector<cudaStream_t> sides;
+  cudaEvent_t fork_ev = nullptr;
+  std::vector<cudaEvent_t> img_ev, join_evs;
   std::vector<void *> Kpre, Kpost;   // dense planes, or mixed-run records on classed levels
   void *Kl = nullptr;
   std::vector<float *> Upre, Upost;  // classed levels: 3 x KREC uniform vectors per block
@@ -2033,7 +2039,7 @@ static size_t plan_layout(PrecondPlan &P, char *base) {
   }
   P.Uall = U;
   P.Mrec = take((size_t)nU * 3 * RREC * sk);
-  int64_t nlist = 0, nlist2 = 0;
+  int64_t nlist = 0;
   for (int l = 0; l <= P.L; ++l) {
     const auto &v = P.lv[l];
     if (!v.cls) continue;
@@ -2044,7 +2050,6 @@ static size_t plan_layout(PrecondPlan &P, char *base) {
     P.gcount[l] = (uint32_t *)take(v.ntiles * sizeof(uint32_t));
     P.gbase[l] = (uint32_t *)take(v.ntiles * sizeof(uint32_t));
     nlist = std::max<int64_t>(nlist, v.n);
-    if (l >= 1) nlist2 = std::max<int64_t>(nlist2, v.n);
   }
   P.clsT.assign(P.L + 1, nullptr);
   P.rwT.assign(P.L + 1, nullptr);
@@ -2065,10 +2070,14 @@ static size_t plan_layout(PrecondPlan &P, char *base) {
   // general-cell and mixed-run lists of one level at a time (setup only)
   P.glist = nlist ? (uint32_t *)take((size_t)nlist * sizeof(uint32_t)) : nullptr;
   P.rlist = nlist ? (uint32_t *)take((size_t)(nlist / 8 + 1) * sizeof(uint32_t)) : nullptr;
-  // the lists of levels >= 1 (SmallSMModelDn3D kind), built on the side stream beside level 0's
-  const bool par = P.kind == MLPCG_PRECOND_SM && nlist2 > 0;
-  P.glist2 = par ? (uint32_t *)take((size_t)nlist2 * sizeof(uint32_t)) : nullptr;
-  P.rlist2 = par ? (uint32_t *)take((size_t)(nlist2 / 8 + 1) * sizeof(uint32_t)) : nullptr;
+  // the lists of each classed level >= 1 (SmallSMModelDn3D kind), built on that level's stream
+  P.glists.assign(P.L + 1, nullptr);
+  P.rlists.assign(P.L + 1, nullptr);
+  for (int l = 1; P.kind == MLPCG_PRECOND_SM && l <= P.L; ++l) {
+    if (!P.lv[l].cls) continue;
+    P.glists[l] = (uint32_t *)take((size_t)P.lv[l].n * sizeof(uint32_t));
+    P.rlists[l] = (uint32_t *)take((size_t)(P.lv[l].n / 8 + 1) * sizeof(uint32_t));
+  }
   if (P.lv[0].cls && nlist) {
     P.pkeys = (unsigned long long *)take((size_t)kPatSlots * sizeof(unsigned long long));
     P.pidx = (uint32_t *)take((size_t)kPatSlots * sizeof(uint32_t));
@@ -2089,6 +2098,8 @@ static size_t plan_layout(PrecondPlan &P, char *base) {
   P.coef = (float *)take(2 * P.L * sizeof(float));
   P.fmask = (uint8_t *)take(P.lv[0].ps + 64);
   P.lin_ws = take(linear_workspace());
+  P.lin_wss.assign(P.L, nullptr);
+  for (int l = 0; P.kind == MLPCG_PRECOND_SM && l < P.L; ++l) P.lin_wss[l] = take(linear_workspace());
   P.err = (int *)take(2 * sizeof(int));  // [0]: a tile copy did not complete, [1]: copy-stall test knob
   // scratch last: the general path's temporaries (sized in the plan's byte count) follow it
   P.scratch = (float *)take(96 * sizeof(float));
@@ -2104,9 +2115,10 @@ typedef struct mlpcg_precond mlpcg_precond;
 struct mlpcg_precond {
   PrecondPlan p;
   ~mlpcg_precond() {
-    if (p.side) cudaStreamDestroy(p.side);
+    for (cudaStream_t s : p.sides) cudaStreamDestroy(s);
     if (p.fork_ev) cudaEventDestroy(p.fork_ev);
-    if (p.join_ev) cudaEventDestroy(p.join_ev);
+    for (cudaEvent_t e : p.img_ev) cudaEventDestroy(e);
+    for (cudaEvent_t e : p.join_evs) cudaEventDestroy(e);
   }
 };
 
@@ -2832,7 +2844,7 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
   auto blk_b = [&](int b) { return params + (size_t)b * 2214 + 2187; };
   const float *linp = params + (size_t)nblk * 2214;
   // image pyramid (the SM kind's side stream builds it beside level 0's chain, below)
-  const bool side_chain = P.kind == MLPCG_PRECOND_SM && P.glist2;
+  const bool side_chain = P.kind == MLPCG_PRECOND_SM && L >= 1;
   auto pyramid = [&](cudaStream_t ps) -> int {
     for (int l = 1; l <= L; ++l) {
       const auto &v = P.lv[l - 1];
@@ -2872,15 +2884,17 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
   // one level's blocks b0 (and b1 >= 0): dense planes, or class map + general-cell records;
   // their uniform vectors in slots u0s (and u1s), by default the block indices
   // c0 / c1 of every level (the linear blocks of sm_model_3d.py:236-239), on stream ls
+  // c0[l] and c1[l] in one pass over the level image (their weights are L*82 floats apart), on
+  // stream ls with workspace ws
+  auto linear_level = [&](int l, cudaStream_t ls, void *ws) -> int {
+    const auto &v = P.lv[l];
+    const float *im = (l == 0) ? image : P.img[l];
+    const float *w0 = linp + (size_t)l * 82;
+    return launch_linear_forward_strided(im, v.n1, v.n2, v.n3, w0, (int64_t)L * 82, w0 + 81, (int64_t)L * 82, 2,
+                                         P.coef + l, L, nullptr, ws, linear_workspace(), ls);
+  };
   auto setup_linear = [&](cudaStream_t ls) -> int {
-    for (int l = 0; l < L; ++l) {
-      const auto &v = P.lv[l];
-      const float *im = (l == 0) ? image : P.img[l];
-      // c0[l] and c1[l] in one pass over the level image: their weights are L*82 floats apart
-      const float *w0 = linp + (size_t)l * 82;
-      RET_IF(launch_linear_forward_strided(im, v.n1, v.n2, v.n3, w0, (int64_t)L * 82, w0 + 81, (int64_t)L * 82, 2,
-                                           P.coef + l, L, nullptr, P.lin_ws, linear_workspace(), ls));
-    }
+    for (int l = 0; l < L; ++l) RET_IF(linear_level(l, ls, P.lin_ws));
     return MLPCG_OK;
   };
   bool linear_done = false;
@@ -3024,32 +3038,50 @@ int mlpcg_precond_setup(mlpcg_precond *h, void *workspace, size_t workspace_byte
     RET_IF(classify_t(L));
     RET_IF(gather_t(L, P.Kl, 2 * L, P.Klt, 2 * L + 1));
   } else if (side_chain) {
-    // levels >= 1 and then every level's c0 / c1 on the side stream, level 0 on the caller's
-    if (!P.side) {
-      // the side chain's kernels are small and latency-bound: the highest priority lets their CTAs
-      // start as soon as level 0's free a slot
+    // the chains of the coarse levels are short and latency-bound: each on a stream of its own
+    // (the highest priority, so that their CTAs start as soon as level 0's free a slot)
+    const int ns = L + 2;
+    if ((int)P.sides.size() != ns) {
       int lo = 0, hi = 0;
       MLPCG_CUDA_CHECK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
-      MLPCG_CUDA_CHECK(cudaStreamCreateWithPriority(&P.side, cudaStreamNonBlocking, hi));
+      P.sides.assign(ns, nullptr);
+      P.img_ev.assign(L + 1, nullptr);
+      P.join_evs.assign(ns, nullptr);
+      for (int i = 0; i < ns; ++i) {
+        MLPCG_CUDA_CHECK(cudaStreamCreateWithPriority(&P.sides[i], cudaStreamNonBlocking, hi));
+        MLPCG_CUDA_CHECK(cudaEventCreateWithFlags(&P.join_evs[i], cudaEventDisableTiming));
+      }
+      for (int l = 0; l <= L; ++l) MLPCG_CUDA_CHECK(cudaEventCreateWithFlags(&P.img_ev[l], cudaEventDisableTiming));
       MLPCG_CUDA_CHECK(cudaEventCreateWithFlags(&P.fork_ev, cudaEventDisableTiming));
-      MLPCG_CUDA_CHECK(cudaEventCreateWithFlags(&P.join_ev, cudaEventDisableTiming));
     }
     MLPCG_CUDA_CHECK(cudaEventRecord(P.fork_ev, st));
-    MLPCG_CUDA_CHECK(cudaStreamWaitEvent(P.side, P.fork_ev, 0));
-    gs = P.side;
-    gl = P.glist2;
-    rl = P.rlist2;
-    RET_IF(pyramid(P.side));
-    for (int l = 1; l < L; ++l) RET_IF(gen_level(l, P.img[l], l, P.Kpre[l], L + l, P.Kpost[l]));
-    RET_IF(gen_level(L, P.img[L], 2 * L, P.Kl, -1, nullptr));
-    RET_IF(setup_linear(P.side));
-    MLPCG_CUDA_CHECK(cudaEventRecord(P.join_ev, P.side));
+    for (int i = 0; i < ns; ++i) MLPCG_CUDA_CHECK(cudaStreamWaitEvent(P.sides[i], P.fork_ev, 0));
+    // the pyramid on sides[0], level by level, each level's image announced
+    for (int l = 1; l <= L; ++l) {
+      const auto &v = P.lv[l - 1];
+      const float *src = (l == 1) ? image : P.img[l - 1];
+      RET_IF(launch_avg_pool2(src, P.img[l], MLPCG_F32, 3, v.n1, v.n2, v.n3, P.sides[0]));
+      MLPCG_CUDA_CHECK(cudaEventRecord(P.img_ev[l], P.sides[0]));
+    }
+    // level l's coefficients (and, for l < L, its c0 / c1) on sides[l]
+    for (int l = 1; l <= L; ++l) {
+      MLPCG_CUDA_CHECK(cudaStreamWaitEvent(P.sides[l], P.img_ev[l], 0));
+      gs = P.sides[l];
+      gl = P.glists[l];
+      rl = P.rlists[l];
+      if (l < L) RET_IF(gen_level(l, P.img[l], l, P.Kpre[l], L + l, P.Kpost[l]));
+      else RET_IF(gen_level(L, P.img[L], 2 * L, P.Kl, -1, nullptr));
+      if (l < L) RET_IF(linear_level(l, P.sides[l], P.lin_wss[l]));
+    }
+    // level 0's c0 / c1 needs only the caller's image
+    RET_IF(linear_level(0, P.sides[L + 1], P.lin_wss[0]));
+    for (int i = 0; i < ns; ++i) MLPCG_CUDA_CHECK(cudaEventRecord(P.join_evs[i], P.sides[i]));
     gs = st;
     gl = P.glist;
     rl = P.rlist;
     RET_IF(fluid_mask());
     RET_IF(gen_level(0, image, 0, P.Kpre[0], L, P.Kpost[0]));
-    MLPCG_CUDA_CHECK(cudaStreamWaitEvent(st, P.join_ev, 0));
+    for (int i = 0; i < ns; ++i) MLPCG_CUDA_CHECK(cudaStreamWaitEvent(st, P.join_evs[i], 0));
     linear_done = true;
   } else {
     for (int l = 0; l < L; ++l) RET_IF(gen_level(l, (l == 0) ? image : P.img[l], l, P.Kpre[l], L + l, P.Kpost[l]));
