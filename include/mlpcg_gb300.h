@@ -499,7 +499,9 @@ int mlpcg_gather_fluid(const double *grid, const uint8_t *flags, const uint32_t 
  * fluid-DOF vector of mlpcg_scatter_fluid / mlpcg_gather_fluid: the kernel then
  * reads or writes it over the host link itself, with no staging copy (the
  * caller keeps the host buffer alive and untouched until the stream reaches
- * the call).  No counterpart in the reference. */
+ * the call).  A scatter from such memory runs on two CTAs per SM, so that it
+ * leaves room for kernels of other streams while it waits on the link.  No
+ * counterpart in the reference. */
 int mlpcg_host_mapped(const void *ptr, int *mapped);
 
 /* =========================================================================

@@ -2,6 +2,8 @@
 // coefficients (sm_linear_3d) and the matrix-free mixed-boundary Laplacian.
 #include "common.cuh"
 
+#include <algorithm>
+
 namespace mlpcg {
 
 // ---------------------------------------------------------------------------
@@ -392,6 +394,8 @@ __global__ void k_flags_to_image(const uint8_t *__restrict__ flags, float *__res
 // cells (recomputed by a block scan in each pass).
 // ---------------------------------------------------------------------------
 constexpr int kFluidThreads = 256, kFluidPer = 4, kFluidBlock = kFluidThreads * kFluidPer;
+// CTAs per SM of a scatter whose values are read from host memory
+constexpr int kHostScatterCtasPerSm = 2;
 
 // exclusive scan of one int per thread over a 256-thread block
 __device__ __forceinline__ int block256_excl_scan(int v, int &total) {
@@ -434,29 +438,36 @@ k_fluid_counts(const uint8_t *__restrict__ flags, int64_t n, uint32_t *__restric
 }
 
 // grid = the fluid values scattered to their cells, 0 elsewhere (and for
-// positions beyond the m values given).  The block's values are one contiguous
+// positions beyond the m values given).  A block's values are one contiguous
 // range of vals: the block reads it with consecutive lanes on consecutive
 // values into shared memory (few, full transactions also when vals is host
-// memory read over the host link), then places them.
+// memory read over the host link), then places them.  Blocks step through the
+// cell blocks by the grid size, so that a scatter from host memory can run on
+// a few CTAs per SM beside other work: its speed is the host link's, and a
+// full grid would hold every SM while its loads wait on the link.
 __global__ void __launch_bounds__(kFluidThreads)
 k_scatter_fluid(const double *__restrict__ vals, int64_t m, const uint8_t *__restrict__ flags,
                 const uint32_t *__restrict__ base, int64_t n, double *__restrict__ grid) {
   dependent_launch_enter();
   __shared__ double sv[kFluidBlock];
-  const int64_t q0 = (int64_t)blockIdx.x * kFluidBlock + kFluidPer * threadIdx.x;
-  const unsigned fm = fluid_bits(flags, n, q0);
-  int tot;
-  const int64_t b0 = (int64_t)__ldg(base + blockIdx.x);
-  int pos = block256_excl_scan(__popc(fm), tot);
-  for (int i = threadIdx.x; i < tot; i += kFluidThreads) sv[i] = b0 + i < m ? vals[b0 + i] : 0.0;
-  __syncthreads();
+  const int64_t nb = (n + kFluidBlock - 1) / kFluidBlock;
+  for (int64_t blk = blockIdx.x; blk < nb; blk += gridDim.x) {
+    const int64_t q0 = blk * kFluidBlock + kFluidPer * threadIdx.x;
+    const unsigned fm = fluid_bits(flags, n, q0);
+    int tot;
+    const int64_t b0 = (int64_t)__ldg(base + blk);
+    // the scan's barrier also orders this block's sv writes after the previous pass's reads
+    int pos = block256_excl_scan(__popc(fm), tot);
+    for (int i = threadIdx.x; i < tot; i += kFluidThreads) sv[i] = b0 + i < m ? vals[b0 + i] : 0.0;
+    __syncthreads();
 #pragma unroll
-  for (int u = 0; u < kFluidPer; ++u)
-    if (q0 + u < n) {
-      const bool f = (fm >> u) & 1u;
-      grid[q0 + u] = f ? sv[pos] : 0.0;
-      pos += f;
-    }
+    for (int u = 0; u < kFluidPer; ++u)
+      if (q0 + u < n) {
+        const bool f = (fm >> u) & 1u;
+        grid[q0 + u] = f ? sv[pos] : 0.0;
+        pos += f;
+      }
+  }
 }
 
 // vals = the grid's values on the fluid cells (the first m of them), placed in
@@ -511,7 +522,18 @@ int launch_fluid_order(const uint8_t *flags, int64_t n, uint32_t *base, cudaStre
 
 int launch_scatter_fluid(const double *vals, int64_t m, const uint8_t *flags, const uint32_t *base, int64_t n,
                          double *grid, cudaStream_t st) {
-  k_scatter_fluid<<<(unsigned)fluid_blocks(n), kFluidThreads, 0, st>>>(vals, m, flags, base, n, grid);
+  int64_t blocks = fluid_blocks(n);
+  cudaPointerAttributes a{};
+  const cudaError_t e = cudaPointerGetAttributes(&a, vals);
+  if (e != cudaSuccess) cudaGetLastError();
+  if (e == cudaSuccess && a.type == cudaMemoryTypeHost) {  // read over the host link: a few CTAs per SM
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        sms <= 0)
+      sms = 152;
+    blocks = std::min<int64_t>(blocks, (int64_t)kHostScatterCtasPerSm * sms);
+  }
+  k_scatter_fluid<<<(unsigned)blocks, kFluidThreads, 0, st>>>(vals, m, flags, base, n, grid);
   MLPCG_LAUNCH_CHECK();
   return MLPCG_OK;
 }

@@ -1,4 +1,6 @@
 """Preconditioner plan and fused graph-captured solver vs the drop-in path and the FP64 oracle (GPU)."""
+import ctypes as C
+
 import numpy as np
 import pytest
 import torch
@@ -293,6 +295,32 @@ def test_fluid_vectors_scatter_gather(cuda, shape):
     out.fill_(9.0)
     call("mlpcg_gather_fluid", _p(src), _p(flags), _p(order), n, _p(out), k, st)
     assert torch.equal(out[:k], src[fluid[:k]]) and torch.all(out[k:] == 9.0)
+
+
+@pytest.mark.parametrize("shape", [(7, 13, 29), (128, 128, 96)])
+def test_fluid_scatter_from_pinned_host_memory(cuda, shape):
+    """The scatter reading pinned host memory runs on a capped grid whose CTAs step through the
+    cell blocks (1,536 blocks at 128 x 128 x 96, several per CTA): the same grid as torch indexing,
+    for the full and for a short vector."""
+    from mlpcg_gb300._lib import call, load
+    from mlpcg_gb300.ops import _p, _stream
+    g = torch.Generator(device=cuda).manual_seed(12)
+    flags = torch.randint(0, 4, shape, generator=g, device=cuda, dtype=torch.uint8)
+    n = flags.numel()
+    fluid = torch.nonzero(flags.view(-1) == 2).view(-1)
+    m = fluid.numel()
+    order = torch.empty(int(load().mlpcg_fluid_order_entries(n)), dtype=torch.int32, device=cuda)
+    st = _stream(flags.device)
+    call("mlpcg_fluid_order", _p(flags), n, _p(order), st)
+    vals = torch.randn(m, dtype=torch.float64, device=cuda, generator=g)
+    vals_h = vals.cpu().pin_memory()
+    for k in (m, m // 3):
+        grid = torch.full((n,), 5.0, dtype=torch.float64, device=cuda)
+        call("mlpcg_scatter_fluid", C.c_void_p(vals_h.data_ptr()), k, _p(flags), _p(order), n, _p(grid), st)
+        torch.cuda.synchronize()
+        ref = torch.zeros(n, dtype=torch.float64, device=cuda)
+        ref[fluid[:k]] = vals[:k]
+        assert torch.equal(grid, ref)
 
 
 def test_solve_host_fluid_vectors(cuda):
