@@ -298,10 +298,10 @@ def test_fluid_vectors_scatter_gather(cuda, shape):
 
 
 @pytest.mark.parametrize("shape", [(7, 13, 29), (128, 128, 96)])
-def test_fluid_scatter_from_pinned_host_memory(cuda, shape):
+def test_fluid_scatter_gather_with_pinned_host_memory(cuda, shape):
     """The scatter reading pinned host memory runs on a capped grid whose CTAs step through the
     cell blocks (1,536 blocks at 128 x 128 x 96, several per CTA): the same grid as torch indexing,
-    for the full and for a short vector."""
+    for the full and for a short vector; the gather writes pinned host memory directly."""
     from mlpcg_gb300._lib import call, load
     from mlpcg_gb300.ops import _p, _stream
     g = torch.Generator(device=cuda).manual_seed(12)
@@ -321,6 +321,12 @@ def test_fluid_scatter_from_pinned_host_memory(cuda, shape):
         ref = torch.zeros(n, dtype=torch.float64, device=cuda)
         ref[fluid[:k]] = vals[:k]
         assert torch.equal(grid, ref)
+    src = torch.randn(n, dtype=torch.float64, device=cuda, generator=g)
+    for k in (m, m // 3):  # the gather into pinned host memory
+        out_h = torch.full((m + 3,), 9.0, dtype=torch.float64).pin_memory()
+        call("mlpcg_gather_fluid", _p(src), _p(flags), _p(order), n, C.c_void_p(out_h.data_ptr()), k, st)
+        torch.cuda.synchronize()
+        assert torch.equal(out_h[:k], src[fluid[:k]].cpu()) and torch.all(out_h[k:] == 9.0)
 
 
 def test_solve_host_fluid_vectors(cuda):
