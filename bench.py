@@ -21,7 +21,11 @@ picked by mlpcg_gb300.autotune (config.solver_schedule).  Also reported:
                   buffers (flags, rhs in; solution out);
   * cpu_baseline -- the reference's CPU path (torch-CPU Conv3d blocks, FP64
                   CSR npsd) on this host, a bounded sample of iterations,
-                  extrapolated to the iteration count of the solve.
+                  extrapolated to the iteration count of the solve;
+  * amg_cpu_baseline -- the reference's other host comparator, AMG-
+                  preconditioned FP64 CG (smoothed aggregation, SPAI-0), run
+                  to the same tolerance on the same scene in a child process
+                  (oracle/amg.cpp; setup + solve time, iterations, residual).
 
 ``--model small_spd`` / ``--model spd`` run the same harness on the symmetric
 networks SmallSPDSMModelDn3D / SPDSMModelDn3D (default solver npcg, textbook
@@ -76,6 +80,9 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-reference-solution", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--no-amg", action="store_true",
+                    help="skip the host AMG-preconditioned CG comparator run beside the CPU baseline")
+    ap.add_argument("--amg-timeout", type=float, default=240.0)
     ap.add_argument("--no-graph", action="store_true",
                     help="plain launches of the same kernels with a host check per iteration (for profilers)")
     ap.add_argument("--batch", action="store_true",
@@ -564,6 +571,26 @@ def cpu_baseline(args, model_sd, scene, iterations, budget_s):
             "host_cpus": os.cpu_count(), "per_iteration_s": round(per_it, 3)}
 
 
+def amg_baseline(args, seed):
+    """The reference's other host comparator -- AMG-preconditioned CG (cg_tests.py:343-346 with
+    cxx_src/lib/AMGCLSolver.h:58-128) -- as restated by oracle/amg.cpp, run to the same tolerance on
+    the same scene in a child process on the host cores (its memory and threads stay out of this
+    process).  Setup + solve time, measured; the matrix assembly is not timed."""
+    cmd = [sys.executable, "-m", "oracle.amg", "--size", str(args.size), "--seed", str(seed),
+           "--spheres", str(args.spheres), "--tol", str(args.tol)]
+    try:
+        p = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=args.amg_timeout)
+    except subprocess.TimeoutExpired:
+        return {"unavailable": f"no result within {args.amg_timeout:.0f} s"}
+    if p.returncode != 0:
+        tail = (p.stderr.strip().splitlines() or ["no output"])[-1]
+        return {"unavailable": f"exit {p.returncode}: {tail[:200]}"}
+    try:
+        return json.loads(p.stdout.strip().splitlines()[-1])
+    except (IndexError, ValueError):
+        return {"unavailable": "no JSON line"}
+
+
 BATCH_SIZES = [64] * 4 + [96] * 4 + [128] * 4 + [192] * 4
 BATCH_SEEDS = list(range(100, 116))
 
@@ -737,6 +764,8 @@ def main():
     if not args.no_cpu:
         cpu = cpu_baseline(args, r["model"].state_dict(), r["scene"], int(statistics.mean(r["its"])),
                            args.cpu_seconds)
+        if not args.no_amg:
+            extra["amg_cpu_baseline"] = amg_baseline(args, replica_seed(args.seed, 0))
     it_mean = statistics.mean(r["its"])
     line = {"metric": METRIC, "value": round(r["ms"], 3), "unit": "ms", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(r["ms"], 3), "higher_is_better": False,

@@ -11,6 +11,12 @@ algorithm of the neural-preconditioned CG Poisson solve of kai-lan/MLPCG:
 * ``cg``        -- the reference's npcg / npcg_flex / npsd iterations;
 * ``cpu_path``  -- the reference's CPU path (torch-CPU Conv3d + unfold blocks,
                    torch-CPU CG), timed as the CPU baseline.
+* ``amg``       -- the reference's host AMG comparator (smoothed-aggregation
+                   AMG with SPAI-0 relaxation inside FP64 CG, as its AMGCL
+                   shim configures it), restated in C++ (``amg.cpp``, built
+                   with g++ / OpenMP) from the published methods: AMGCL is
+                   an un-vendored submodule, so this comparator's iteration
+                   counts are not pinned to AMGCL's.
 
 Parity is pinned: ``tests/golden/make_golden.py`` imports the reference's own
 Python modules (sm_model_3d_py.py, model.py, lib/discrete_laplacian.py,

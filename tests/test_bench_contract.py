@@ -31,3 +31,18 @@ def test_reference_arm_prints_one_contract_line():
     e2e = d["e2e"]
     assert e2e["value"] == d["value"] and e2e["unit"] == "ms"
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+
+
+def test_amg_comparator_leg_reports_a_measured_solve():
+    """The host AMG comparator beside the CPU baseline: a measured solve of the same scene to the
+    bench's tolerance, or an 'unavailable' reason when it does not finish in time."""
+    import argparse
+    sys.path.insert(0, str(ROOT))
+    import bench
+    a = argparse.Namespace(size=24, spheres=3, tol=1e-6, amg_timeout=240.0)
+    d = bench.amg_baseline(a, bench.replica_seed(7, 0))
+    assert d["kind"] == "port" and d["unit"] == "ms" and d["value"] > 0 and d["cores"] >= 1
+    assert d["rel_res"] < 1e-6 and 0 < d["iterations"] < 50
+    assert d["value"] == pytest.approx(d["setup_ms"] + d["solve_ms"], abs=0.2)
+    a.amg_timeout = 1e-3
+    assert "unavailable" in bench.amg_baseline(a, 7)
