@@ -26,7 +26,8 @@
 //    inverse m_i = a_ii / sum_j a_ij^2, one sweep before and one after the
 //    coarse correction, so the V-cycle is a symmetric operator and plain CG
 //    applies;
-//  * CG: FP64, OpenMP-parallel products and reductions.
+//  * CG: FP64, OpenMP-parallel products; reductions in a fixed order, so a
+//    solve repeats bit for bit with the same thread count.
 //
 // C entry points (ctypes, oracle/amg.py): amg_cg_solve and amg_apply.
 #include <omp.h>
@@ -77,29 +78,71 @@ void spmv_add(const Csr &A, const double *x, double *y) {
   }
 }
 
+// x . y from per-thread partial sums over fixed ranges, added in thread order:
+// the same bits on every run with the same thread count
 double dot(const double *x, const double *y, int64_t n) {
+  std::vector<double> part(omp_get_max_threads(), 0.0);
+  int used = 1;
+#pragma omp parallel num_threads((int)part.size())
+  {
+    const int t = omp_get_thread_num(), nt = omp_get_num_threads();
+    const int64_t lo = n * t / nt, hi = n * (t + 1) / nt;
+    double s = 0.0;
+    for (int64_t i = lo; i < hi; ++i) s += x[i] * y[i];
+    part[t] = s;
+    if (t == 0) used = nt;
+  }
   double s = 0.0;
-#pragma omp parallel for schedule(static) reduction(+ : s)
-  for (int64_t i = 0; i < n; ++i) s += x[i] * y[i];
+  for (int t = 0; t < used; ++t) s += part[t];
   return s;
 }
 
+std::vector<int64_t> row_bounds(int64_t rows, int parts) {
+  std::vector<int64_t> b(parts + 1);
+  for (int t = 0; t <= parts; ++t) b[t] = rows * t / parts;
+  return b;
+}
+
+// A^T, in parallel over row blocks: each block counts its entries per column,
+// and a column's entries are placed block after block, rows in order -- the
+// same arrays as a sequential transpose
 Csr transpose(const Csr &A) {
+  const int parts = omp_get_max_threads();
+  const std::vector<int64_t> bounds = row_bounds(A.rows, parts);
   Csr T;
   T.rows = A.cols;
   T.cols = A.rows;
   T.ptr.assign(T.rows + 1, 0);
-  for (int64_t k = 0; k < A.nnz(); ++k) ++T.ptr[A.col[k] + 1];
-  for (int64_t i = 0; i < T.rows; ++i) T.ptr[i + 1] += T.ptr[i];
   T.col.resize(A.nnz());
   T.val.resize(A.nnz());
-  std::vector<int64_t> pos(T.ptr.begin(), T.ptr.end() - 1);
-  for (int64_t i = 0; i < A.rows; ++i)
-    for (int64_t k = A.ptr[i]; k < A.ptr[i + 1]; ++k) {
-      const int64_t p = pos[A.col[k]]++;
-      T.col[p] = (int32_t)i;
-      T.val[p] = A.val[k];
+  std::vector<int64_t> pos((size_t)parts * A.cols, 0);
+#pragma omp parallel num_threads(parts)
+  {
+    const int t = omp_get_thread_num();
+    int64_t *cnt = pos.data() + (size_t)t * A.cols;
+    for (int64_t i = bounds[t]; i < bounds[t + 1]; ++i)
+      for (int64_t k = A.ptr[i]; k < A.ptr[i + 1]; ++k) ++cnt[A.col[k]];
+#pragma omp barrier
+#pragma omp single
+    {
+      int64_t run = 0;
+      for (int64_t c = 0; c < A.cols; ++c) {
+        T.ptr[c] = run;
+        for (int u = 0; u < parts; ++u) {
+          const int64_t v = pos[(size_t)u * A.cols + c];
+          pos[(size_t)u * A.cols + c] = run;
+          run += v;
+        }
+      }
+      T.ptr[A.cols] = run;
     }
+    for (int64_t i = bounds[t]; i < bounds[t + 1]; ++i)
+      for (int64_t k = A.ptr[i]; k < A.ptr[i + 1]; ++k) {
+        const int64_t p = cnt[A.col[k]]++;
+        T.col[p] = (int32_t)i;
+        T.val[p] = A.val[k];
+      }
+  }
   return T;
 }
 
@@ -132,12 +175,6 @@ Csr gather_blocks(std::vector<RowBlock> &blk, const std::vector<int64_t> &bounds
   return C;
 }
 
-std::vector<int64_t> row_bounds(int64_t rows, int parts) {
-  std::vector<int64_t> b(parts + 1);
-  for (int t = 0; t <= parts; ++t) b[t] = rows * t / parts;
-  return b;
-}
-
 // Galerkin product R A P, one coarse row at a time: sum over the fine rows i of
 // R's row I, over A's row i, over P's row j
 Csr galerkin(const Csr &R, const Csr &A, const Csr &P) {
@@ -148,6 +185,9 @@ Csr galerkin(const Csr &R, const Csr &A, const Csr &P) {
   {
     const int t = omp_get_thread_num();
     RowBlock &out = blk[t];
+    out.len.reserve(bounds[t + 1] - bounds[t]);
+    out.col.reserve((bounds[t + 1] - bounds[t]) * 27);
+    out.val.reserve((bounds[t + 1] - bounds[t]) * 27);
     std::vector<int64_t> marker(P.cols, -1);
     for (int64_t I = bounds[t]; I < bounds[t + 1]; ++I) {
       const int64_t start = (int64_t)out.col.size();
@@ -302,6 +342,11 @@ struct Hierarchy {
     {
       const int t = omp_get_thread_num();
       RowBlock &out = blk[t];
+      // at most one entry per coupling of the row, plus its own aggregate
+      const int64_t cap = A.ptr[bounds[t + 1]] - A.ptr[bounds[t]] + (bounds[t + 1] - bounds[t]);
+      out.len.reserve(bounds[t + 1] - bounds[t]);
+      out.col.reserve(cap);
+      out.val.reserve(cap);
       for (int64_t i = bounds[t]; i < bounds[t + 1]; ++i) {
         const size_t start = out.col.size();
         auto add = [&](int32_t K, double v) {

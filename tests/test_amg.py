@@ -2,6 +2,8 @@
 method of the reference's AMGCL comparator, cxx_src/lib/AMGCLSolver.h:58-128) on CPU: its matrix
 equals the oracle's, it solves to the tolerance asked, its V-cycle is symmetric positive definite
 (so plain CG applies), and its iteration count stays flat as the grid grows."""
+import os
+
 import numpy as np
 import pytest
 import scipy.sparse.linalg as spla
@@ -84,3 +86,16 @@ def test_stopping_rule_and_edge_cases():
     assert it0 == 0 and r0 == 0.0 and not x0.any()
     with pytest.raises(ValueError):
         amg.solve(A, b[:-1])
+
+
+def test_repeats_bit_for_bit_with_the_same_thread_count():
+    """Fixed-order reductions and a deterministic parallel transpose: the same solution bits on
+    every run with a given thread count; one thread and four threads agree to the tolerance."""
+    sc = _scene((32, 28, 36), 8)
+    A, fluid = amg.assemble_csr(sc.flags)
+    b = sc.rhs.ravel()[fluid]
+    x4 = [amg.solve(A, b, tol=1e-9, atol=1e-30, threads=4)[0] for _ in range(3)]
+    assert all(np.array_equal(x4[0], x) for x in x4[1:])
+    x1 = amg.solve(A, b, tol=1e-9, atol=1e-30, threads=1)[0]
+    amg.solve(A, b, threads=os.cpu_count() or 1)  # leave the process at its default thread count
+    assert np.linalg.norm(x1 - x4[0]) / np.linalg.norm(x1) < 1e-7
